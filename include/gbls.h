@@ -1,0 +1,209 @@
+/*
+ * gbls.h -- C ABI of the GB300 narrow-band level-set advection library.
+ *
+ * This is the drop-in boundary for OpenVDB's level-set advection hot path:
+ *   openvdb/openvdb/tools/LevelSetAdvect.h   class LevelSetAdvection   (:71-213)
+ *   openvdb/openvdb/tools/LevelSetTracker.h  class LevelSetTracker     (:56-256)
+ * Those are header-only C++ templates; a C++ caller keeps their call surface
+ * through include/openvdb_gb300/LevelSetAdvect.h, which packs an OpenVDB
+ * FloatGrid into a gbls_grid_desc and calls the functions below.  Every entry
+ * point takes plain pointers and sizes, returns a gbls_status (0 = success)
+ * and never throws; gbls_last_error() describes the last failure on the
+ * calling thread.
+ *
+ * Numeric codes of schemes and trim modes equal the reference enums
+ * (math/FiniteDifference.h:164-171 BiasedGradientScheme, :233-238
+ * TemporalIntegrationScheme, tools/LevelSetTracker.h:45-50 TrimMode), so a
+ * binding can pass the reference enum values straight through.
+ */
+#ifndef GBLS_H
+#define GBLS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBLS_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+typedef enum gbls_status {
+    GBLS_OK = 0,
+    GBLS_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size                         */
+    GBLS_ERR_VALUE = 2,            /* reference throws ValueError (bad scheme/map)  */
+    GBLS_ERR_RUNTIME = 3,          /* reference throws RuntimeError (not a level set,
+                                      non-uniform voxels)                           */
+    GBLS_ERR_CUDA = 4,             /* a CUDA call failed                             */
+    GBLS_ERR_OUT_OF_MEMORY = 5,
+    GBLS_ERR_INTERRUPTED = 6,      /* the interrupter asked to stop                  */
+    GBLS_ERR_DOMAIN = 7,           /* coordinates outside the supported index range */
+    GBLS_ERR_UNSUPPORTED = 8,      /* input the device tree cannot represent         */
+    GBLS_ERR_DEVICE_CHECK = 9      /* a device-side bounds check fired               */
+} gbls_status;
+
+/* ---- schemes (values equal the OpenVDB enums) ------------------------ */
+enum {
+    GBLS_FIRST_BIAS = 0,
+    GBLS_SECOND_BIAS = 1,
+    GBLS_THIRD_BIAS = 2,
+    GBLS_WENO5_BIAS = 3,
+    GBLS_HJWENO5_BIAS = 4
+};
+enum { GBLS_TVD_RK1 = 0, GBLS_TVD_RK2 = 1, GBLS_TVD_RK3 = 2 };
+enum { GBLS_TRIM_NONE = 0, GBLS_TRIM_INTERIOR = 1, GBLS_TRIM_EXTERIOR = 2, GBLS_TRIM_ALL = 3 };
+
+/* Arithmetic mode of the stencil kernels.
+ * PARITY evaluates the WENO5 weights in FP64 exactly as
+ *   math/FiniteDifference.h:301-321 does and every FP32 operation in the
+ *   reference's order without contraction: results are bit-identical to the
+ *   reference CPU path.
+ * FAST evaluates everything in FP32 (contracted, shared sub-expressions). */
+enum { GBLS_MODE_PARITY = 0, GBLS_MODE_FAST = 1 };
+
+/* Transform kinds accepted (tools/LevelSetAdvect.h:257-276 accepts these four;
+ * the device path supports the uniform-scale ones). */
+enum {
+    GBLS_MAP_UNIFORM_SCALE = 0,
+    GBLS_MAP_UNIFORM_SCALE_TRANSLATE = 1,
+    GBLS_MAP_TRANSLATION = 2
+};
+
+/* ---- host description of a FloatGrid level set -------------------------
+ * The tree is OpenVDB's Tree4<float,5,4,3>: root -> 4096^3 upper internal
+ * nodes (32^3 slots) -> 128^3 lower internal nodes (16^3 slots) -> 8^3 leaves.
+ * Canonical order of every list is the reference's tree order (root map
+ * order = lexicographic origin, then child offset), and tile tables hold 0.0f
+ * at slots occupied by a child.  Tiles are inactive (level sets carry no
+ * active tiles).  Leaf voxel n = (x<<6)|(y<<3)|z (tree/LeafNode.h:1069-1075);
+ * mask word w holds voxels 64w..64w+63, bit b = voxel 64w+b.
+ * Upper slot n = (x<<10)|(y<<5)|z with x=(i>>7)&31; lower slot n =
+ * (x<<8)|(y<<4)|z with x=(i>>3)&15.                                          */
+typedef struct gbls_grid_desc {
+    double voxel_size;            /* uniform voxel size dx                      */
+    double translation[3];        /* world offset of voxel (0,0,0)              */
+    int32_t map_type;             /* GBLS_MAP_*                                 */
+    float background;             /* outside value gamma > 0                    */
+    int64_t leaf_count;
+    int32_t* leaf_origins;        /* [leaf_count][3]                            */
+    uint64_t* leaf_masks;         /* [leaf_count][8]                            */
+    float* leaf_values;           /* [leaf_count][512]                          */
+    int64_t lower_count;
+    int32_t* lower_origins;       /* [lower_count][3]                           */
+    float* lower_tiles;           /* [lower_count][4096]                        */
+    int64_t upper_count;
+    int32_t* upper_origins;       /* [upper_count][3]                           */
+    float* upper_tiles;           /* [upper_count][32768]                       */
+    int64_t root_tile_count;
+    int32_t* root_tile_origins;   /* [root_tile_count][3]                       */
+    float* root_tile_values;      /* [root_tile_count]                          */
+} gbls_grid_desc;
+
+/* Sizes of a grid (to allocate a gbls_grid_desc for gbls_download). */
+typedef struct gbls_grid_counts {
+    int64_t leaf_count;
+    int64_t lower_count;
+    int64_t upper_count;
+    int64_t root_tile_count;
+    int64_t active_voxel_count;
+} gbls_grid_counts;
+
+/* ---- velocity fields ----------------------------------------------------
+ * The reference takes any functor with operator()(Coord ijk, float t)
+ * (tools/LevelSetAdvect.h:32-52).  These kinds cover the callers of the path:
+ *  CONSTANT     v(ijk,t) = constant  (DiscreteField of an empty Vec3fGrid whose
+ *               background is `constant`, tools/VelocityFields.h:42-94)
+ *  DENSE        aligned DiscreteField<Vec3fGrid>: the value stored at ijk inside
+ *               [dense_origin, dense_origin+dense_dims), dense_background outside
+ *  DEFORMATION  LeVeque's divergence-free deformation, see gbls_fields.h
+ *  ROTATION     constant + omega x (ijk - center)                            */
+enum {
+    GBLS_FIELD_CONSTANT = 0,
+    GBLS_FIELD_DENSE = 1,
+    GBLS_FIELD_DEFORMATION = 2,
+    GBLS_FIELD_ROTATION = 3
+};
+
+typedef struct gbls_field_desc {
+    int32_t kind;
+    float constant[3];
+    int32_t dense_origin[3];
+    int32_t dense_dims[3];
+    const float* dense_values;    /* [dims.x][dims.y][dims.z][3] in host memory  */
+    float dense_background[3];
+    float domain;                 /* DEFORMATION: voxels per unit length          */
+    float period;                 /* DEFORMATION: T, in time units                */
+    float scale;                  /* DEFORMATION: voxels per time unit per unit    */
+    float omega[3];               /* ROTATION: angular velocity (rad / time unit)  */
+    float center[3];              /* ROTATION: rotation centre (index space)       */
+} gbls_field_desc;
+
+typedef struct gbls_handle gbls_handle;   /* a device-resident level set      */
+typedef struct gbls_field gbls_field;     /* a device-resident velocity field */
+
+/* Interrupter hooks (util/NullInterrupter.h:29-49).  Any may be NULL.
+ * was_interrupted returns non-zero to stop; the call then returns
+ * GBLS_ERR_INTERRUPTED with the grid left at a substep boundary.            */
+typedef struct gbls_interrupter {
+    void (*start)(void* user, const char* name);
+    void (*end)(void* user);
+    int (*was_interrupted)(void* user, int percent);
+    void* user;
+} gbls_interrupter;
+
+/* ---- library ----------------------------------------------------------- */
+int gbls_abi_version(void);
+const char* gbls_last_error(void);
+/* Select the CUDA device used by handles created afterwards on this thread. */
+int gbls_set_device(int device);
+
+/* ---- grid lifetime (replaces the grid reference held by
+ *      LevelSetTracker(GridT&) tools/LevelSetTracker.h:258-277) ---------- */
+/* Upload a level set.  Returns GBLS_ERR_RUNTIME for a non-positive
+ * background or voxel size (the reference requires GRID_LEVEL_SET class and
+ * uniform voxels), GBLS_ERR_UNSUPPORTED for tiles other than +-background. */
+int gbls_create(const gbls_grid_desc* desc, gbls_handle** out);
+int gbls_destroy(gbls_handle* h);
+int gbls_get_counts(gbls_handle* h, gbls_grid_counts* out);
+/* Copy the grid back in canonical order into caller-allocated arrays sized
+ * by gbls_get_counts (replaces reading the mutated FloatGrid in place). */
+int gbls_download(gbls_handle* h, gbls_grid_desc* out);
+/* CUDA stream (cudaStream_t) for all work on this handle; NULL = default. */
+int gbls_set_stream(gbls_handle* h, void* stream);
+
+/* ---- tracker state (LevelSetTracker::State, tools/LevelSetTracker.h:74-83,
+ *      setters :137-173) ------------------------------------------------- */
+int gbls_set_tracker_state(gbls_handle* h, int spatial_scheme, int temporal_scheme,
+                           int norm_count, int grain_size);
+int gbls_get_tracker_state(gbls_handle* h, int* spatial_scheme, int* temporal_scheme,
+                           int* norm_count, int* grain_size);
+int gbls_set_trimming(gbls_handle* h, int trim_mode);       /* :171 */
+int gbls_set_precision(gbls_handle* h, int mode);           /* GBLS_MODE_* */
+int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr);
+
+/* ---- LevelSetTracker operations ---------------------------------------- */
+int gbls_track(gbls_handle* h);                              /* :302-315 */
+int gbls_normalize(gbls_handle* h);                          /* :394-446 */
+int gbls_prune(gbls_handle* h);                              /* :279-300 */
+int gbls_dilate(gbls_handle* h, int iterations);             /* :317-337 */
+int gbls_erode(gbls_handle* h, int iterations);              /* :339-349 */
+int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed); /* :351-364 */
+
+/* ---- velocity fields ---------------------------------------------------- */
+int gbls_field_create(const gbls_field_desc* desc, gbls_field** out);
+int gbls_field_destroy(gbls_field* f);
+
+/* ---- LevelSetAdvection::advect (tools/LevelSetAdvect.h:216-418) ---------
+ * Advects from t0 to t1 (t0 > t1 advects backward) with CFL-limited
+ * substeps; each substep runs the temporal scheme's RK stages with the
+ * biased spatial scheme, then the tracker pass.  cfl <= 0 selects the
+ * reference constant {0.3,0.9,1.0}/sqrt(3) for RK1/2/3 (:459-461).
+ * *substeps receives the CFL count the reference returns.                  */
+int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
+                int temporal_scheme, float t0, float t1, float cfl, uint64_t* substeps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBLS_H */

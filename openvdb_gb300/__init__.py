@@ -1,0 +1,5 @@
+"""GB300-native narrow-band level-set advection (OpenVDB LevelSetAdvection /
+LevelSetTracker hot path) behind a C ABI; see include/gbls.h."""
+from . import _abi
+from .fields import Field
+from .grid import HostGrid, bitwise_equal, compare, topology_equal

@@ -1,0 +1,92 @@
+"""ctypes mirror of include/gbls.h (structures and constants).
+
+Field order and types must match the C declarations exactly; the layout is
+checked against the compiled library in tests/test_abi.py.
+"""
+import ctypes as C
+
+GBLS_ABI_VERSION = 1
+
+# status codes
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_VALUE = 2
+ERR_RUNTIME = 3
+ERR_CUDA = 4
+ERR_OUT_OF_MEMORY = 5
+ERR_INTERRUPTED = 6
+ERR_DOMAIN = 7
+ERR_UNSUPPORTED = 8
+ERR_DEVICE_CHECK = 9
+
+# math::BiasedGradientScheme (math/FiniteDifference.h:164-171)
+FIRST_BIAS, SECOND_BIAS, THIRD_BIAS, WENO5_BIAS, HJWENO5_BIAS = 0, 1, 2, 3, 4
+# math::TemporalIntegrationScheme (math/FiniteDifference.h:233-238)
+TVD_RK1, TVD_RK2, TVD_RK3 = 0, 1, 2
+# lstrack::TrimMode (tools/LevelSetTracker.h:45-50)
+TRIM_NONE, TRIM_INTERIOR, TRIM_EXTERIOR, TRIM_ALL = 0, 1, 2, 3
+MODE_PARITY, MODE_FAST = 0, 1
+MAP_UNIFORM_SCALE, MAP_UNIFORM_SCALE_TRANSLATE, MAP_TRANSLATION = 0, 1, 2
+FIELD_CONSTANT, FIELD_DENSE, FIELD_DEFORMATION, FIELD_ROTATION = 0, 1, 2, 3
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("voxel_size", C.c_double),
+        ("translation", C.c_double * 3),
+        ("map_type", C.c_int32),
+        ("background", C.c_float),
+        ("leaf_count", C.c_int64),
+        ("leaf_origins", C.POINTER(C.c_int32)),
+        ("leaf_masks", C.POINTER(C.c_uint64)),
+        ("leaf_values", C.POINTER(C.c_float)),
+        ("lower_count", C.c_int64),
+        ("lower_origins", C.POINTER(C.c_int32)),
+        ("lower_tiles", C.POINTER(C.c_float)),
+        ("upper_count", C.c_int64),
+        ("upper_origins", C.POINTER(C.c_int32)),
+        ("upper_tiles", C.POINTER(C.c_float)),
+        ("root_tile_count", C.c_int64),
+        ("root_tile_origins", C.POINTER(C.c_int32)),
+        ("root_tile_values", C.POINTER(C.c_float)),
+    ]
+
+
+class GridCounts(C.Structure):
+    _fields_ = [
+        ("leaf_count", C.c_int64),
+        ("lower_count", C.c_int64),
+        ("upper_count", C.c_int64),
+        ("root_tile_count", C.c_int64),
+        ("active_voxel_count", C.c_int64),
+    ]
+
+
+class FieldDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("constant", C.c_float * 3),
+        ("dense_origin", C.c_int32 * 3),
+        ("dense_dims", C.c_int32 * 3),
+        ("dense_values", C.POINTER(C.c_float)),
+        ("dense_background", C.c_float * 3),
+        ("domain", C.c_float),
+        ("period", C.c_float),
+        ("scale", C.c_float),
+        ("omega", C.c_float * 3),
+        ("center", C.c_float * 3),
+    ]
+
+
+INTERRUPT_START = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p)
+INTERRUPT_END = C.CFUNCTYPE(None, C.c_void_p)
+INTERRUPT_CHECK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int)
+
+
+class Interrupter(C.Structure):
+    _fields_ = [
+        ("start", INTERRUPT_START),
+        ("end", INTERRUPT_END),
+        ("was_interrupted", INTERRUPT_CHECK),
+        ("user", C.c_void_p),
+    ]

@@ -1,0 +1,368 @@
+// Test-oracle harness around the UNMODIFIED reference implementation.
+//
+// This file is compiled (by oracle/ref/build_ref.py) together with the
+// reference's own headers and a handful of its .cc files, read in place from
+// the reference checkout, into oracle/_ref/libvdbref.so.  It exposes a small
+// C interface so the Python tests can (a) build reference level sets
+// (tools::createLevelSetSphere, tools::csgUnion), (b) convert between an
+// openvdb::FloatGrid and the gbls_grid_desc exchange format, and (c) run the
+// reference tools::LevelSetAdvection / tools::LevelSetTracker on them.
+// It is test infrastructure only: the product never links it.
+#include <openvdb/openvdb.h>
+#include <openvdb/tools/Composite.h>
+#include <openvdb/tools/LevelSetAdvect.h>
+#include <openvdb/tools/LevelSetSphere.h>
+#include <openvdb/tools/LevelSetTracker.h>
+#include <openvdb/tools/VelocityFields.h>
+
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "gbls.h"
+#include "gbls_fields.h"
+
+using namespace openvdb;
+using FloatTree = openvdb::FloatTree;
+using RootT = FloatTree::RootNodeType;
+using UpperT = RootT::ChildNodeType;
+using LowerT = UpperT::ChildNodeType;
+using LeafT = LowerT::ChildNodeType;
+
+namespace {
+
+thread_local std::string gLastError;
+
+int fail(int code, const std::string& msg) {
+    gLastError = msg;
+    return code;
+}
+
+struct RefGrid {
+    FloatGrid::Ptr grid;
+};
+
+// Velocity functor with the interface tools::LevelSetAdvection expects
+// (tools/LevelSetAdvect.h:32-52) evaluating the analytic fields of
+// gbls_fields.h at integer coordinates.
+struct AnalyticField {
+    using ValueType = float;
+    using VectorType = math::Vec3<float>;
+    gbls_field_desc desc;
+    math::Transform::Ptr xform;
+    const math::Transform& transform() const { return *xform; }
+    VectorType operator()(const Coord& ijk, float t) const {
+        float o[3];
+        if (desc.kind == GBLS_FIELD_DEFORMATION) {
+            gbls_deformation(ijk[0], ijk[1], ijk[2], t, desc.domain, desc.period, desc.scale, o);
+        } else {
+            gbls_rotation(ijk[0], ijk[1], ijk[2], desc.constant, desc.omega, desc.center, o);
+        }
+        return VectorType(o[0], o[1], o[2]);
+    }
+    VectorType operator()(const Vec3d& xyz, float t) const {
+        return (*this)(xform->worldToIndexNodeCentered(xyz), t);
+    }
+};
+
+Vec3fGrid::Ptr makeVelocityGrid(const gbls_field_desc& f, const math::Transform& xform) {
+    Vec3fGrid::Ptr vel;
+    if (f.kind == GBLS_FIELD_CONSTANT) {
+        vel = Vec3fGrid::create(Vec3f(f.constant[0], f.constant[1], f.constant[2]));
+    } else {
+        vel = Vec3fGrid::create(
+            Vec3f(f.dense_background[0], f.dense_background[1], f.dense_background[2]));
+        auto acc = vel->getAccessor();
+        const int nx = f.dense_dims[0], ny = f.dense_dims[1], nz = f.dense_dims[2];
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny; ++j)
+                for (int k = 0; k < nz; ++k) {
+                    const float* v = f.dense_values + 3 * ((size_t(i) * ny + j) * nz + k);
+                    acc.setValue(Coord(f.dense_origin[0] + i, f.dense_origin[1] + j,
+                                       f.dense_origin[2] + k),
+                                 Vec3f(v[0], v[1], v[2]));
+                }
+    }
+    vel->setTransform(xform.copy());
+    return vel;
+}
+
+template<typename FieldT>
+size_t runAdvect(FloatGrid& grid, const FieldT& field, int s, int t, int ts, int tt, int nc,
+                 float t0, float t1) {
+    tools::LevelSetAdvection<FloatGrid, FieldT> adv(grid, field);
+    adv.setSpatialScheme(math::BiasedGradientScheme(s));
+    adv.setTemporalScheme(math::TemporalIntegrationScheme(t));
+    adv.setTrackerSpatialScheme(math::BiasedGradientScheme(ts));
+    adv.setTrackerTemporalScheme(math::TemporalIntegrationScheme(tt));
+    adv.setNormCount(nc);
+    return adv.advect(t0, t1);
+}
+
+void configureTracker(tools::LevelSetTracker<FloatGrid>& tr, int ts, int tt, int nc, int trim) {
+    tr.setSpatialScheme(math::BiasedGradientScheme(ts));
+    tr.setTemporalScheme(math::TemporalIntegrationScheme(tt));
+    tr.setNormCount(nc);
+    tr.setTrimming(tools::lstrack::TrimMode(trim));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* vdbref_last_error() { return gLastError.c_str(); }
+
+int vdbref_init() { return 0; }
+
+int vdbref_set_threads(int n) {
+    tbb::shim::Pool::instance().resize(n);
+    return 0;
+}
+
+int vdbref_threads() { return tbb::shim::Pool::instance().threads(); }
+
+void vdbref_free(void* g) { delete static_cast<RefGrid*>(g); }
+
+// tools/LevelSetSphere.h:219-230
+int vdbref_sphere(float radius, float cx, float cy, float cz, float dx, float hw, void** out) {
+    try {
+        auto* rg = new RefGrid;
+        rg->grid = tools::createLevelSetSphere<FloatGrid>(radius, Vec3f(cx, cy, cz), dx, hw);
+        *out = rg;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
+// Sequential csgUnion of spheres (tools/Composite.h:886).
+int vdbref_union_spheres(int n, const float* centers, const float* radii, float dx, float hw,
+                         void** out) {
+    try {
+        FloatGrid::Ptr acc;
+        for (int i = 0; i < n; ++i) {
+            FloatGrid::Ptr s = tools::createLevelSetSphere<FloatGrid>(
+                radii[i], Vec3f(centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]), dx, hw);
+            if (!acc) acc = s;
+            else tools::csgUnion(*acc, *s);
+        }
+        auto* rg = new RefGrid;
+        rg->grid = acc;
+        *out = rg;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
+int vdbref_counts(void* g, gbls_grid_counts* c) {
+    const FloatTree& tree = static_cast<RefGrid*>(g)->grid->tree();
+    const RootT& root = tree.root();
+    int64_t nu = 0, nl = 0, nleaf = 0, nt = 0;
+    for (auto it = root.cbeginChildOn(); it; ++it) {
+        ++nu;
+        for (auto lit = it->cbeginChildOn(); lit; ++lit) {
+            ++nl;
+            for (auto fit = lit->cbeginChildOn(); fit; ++fit) ++nleaf;
+        }
+    }
+    for (auto it = root.cbeginValueAll(); it; ++it) ++nt;
+    c->leaf_count = nleaf;
+    c->lower_count = nl;
+    c->upper_count = nu;
+    c->root_tile_count = nt;
+    c->active_voxel_count = int64_t(tree.activeVoxelCount());
+    return 0;
+}
+
+// Canonical export: tree order everywhere, 0.0f at child slots of tile tables.
+int vdbref_export(void* g, gbls_grid_desc* d) {
+    const FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+    const FloatTree& tree = grid.tree();
+    const RootT& root = tree.root();
+    const math::Transform& xf = grid.transform();
+    d->voxel_size = grid.voxelSize()[0];
+    const Vec3d t = xf.indexToWorld(Vec3d(0, 0, 0));
+    d->translation[0] = t[0];
+    d->translation[1] = t[1];
+    d->translation[2] = t[2];
+    d->map_type = xf.mapType() == math::UniformScaleMap::mapType()   ? GBLS_MAP_UNIFORM_SCALE
+                  : xf.mapType() == math::TranslationMap::mapType() ? GBLS_MAP_TRANSLATION
+                                                                      : GBLS_MAP_UNIFORM_SCALE_TRANSLATE;
+    d->background = tree.background();
+    int64_t iu = 0, il = 0, ileaf = 0, it_ = 0;
+    for (auto uit = root.cbeginChildOn(); uit; ++uit) {
+        const UpperT& up = *uit;
+        const Coord o = up.origin();
+        std::memcpy(d->upper_origins + 3 * iu, o.data(), 12);
+        float* ut = d->upper_tiles + size_t(iu) * UpperT::NUM_VALUES;
+        for (Index n = 0; n < UpperT::NUM_VALUES; ++n) {
+            if (up.getChildMask().isOn(n)) { ut[n] = 0.0f; continue; }
+            if (up.getValueMask().isOn(n)) return fail(GBLS_ERR_UNSUPPORTED, "active tile");
+            ut[n] = up.getTable()[n].getValue();
+        }
+        ++iu;
+        for (auto lit = up.cbeginChildOn(); lit; ++lit) {
+            const LowerT& lo = *lit;
+            const Coord lo_o = lo.origin();
+            std::memcpy(d->lower_origins + 3 * il, lo_o.data(), 12);
+            float* lt = d->lower_tiles + size_t(il) * LowerT::NUM_VALUES;
+            for (Index n = 0; n < LowerT::NUM_VALUES; ++n) {
+                if (lo.getChildMask().isOn(n)) { lt[n] = 0.0f; continue; }
+                if (lo.getValueMask().isOn(n)) return fail(GBLS_ERR_UNSUPPORTED, "active tile");
+                lt[n] = lo.getTable()[n].getValue();
+            }
+            ++il;
+            for (auto fit = lo.cbeginChildOn(); fit; ++fit) {
+                const LeafT& leaf = *fit;
+                const Coord lf_o = leaf.origin();
+                std::memcpy(d->leaf_origins + 3 * ileaf, lf_o.data(), 12);
+                for (int w = 0; w < 8; ++w)
+                    d->leaf_masks[8 * ileaf + w] = leaf.getValueMask().template getWord<uint64_t>(w);
+                std::memcpy(d->leaf_values + 512 * size_t(ileaf), leaf.buffer().data(), 2048);
+                ++ileaf;
+            }
+        }
+    }
+    for (auto vit = root.cbeginValueAll(); vit; ++vit) {
+        if (vit.isValueOn()) return fail(GBLS_ERR_UNSUPPORTED, "active root tile");
+        const Coord c = vit.getCoord();
+        std::memcpy(d->root_tile_origins + 3 * it_, c.data(), 12);
+        d->root_tile_values[it_] = *vit;
+        ++it_;
+    }
+    return 0;
+}
+
+int vdbref_from_desc(const gbls_grid_desc* d, void** out) {
+    try {
+        FloatGrid::Ptr grid = FloatGrid::create(d->background);
+        math::Transform::Ptr xf = math::Transform::createLinearTransform(d->voxel_size);
+        if (d->translation[0] != 0.0 || d->translation[1] != 0.0 || d->translation[2] != 0.0)
+            xf->postTranslate(Vec3d(d->translation[0], d->translation[1], d->translation[2]));
+        grid->setTransform(xf);
+        grid->setGridClass(GRID_LEVEL_SET);
+        FloatTree& tree = grid->tree();
+        for (int64_t i = 0; i < d->root_tile_count; ++i) {
+            const int32_t* o = d->root_tile_origins + 3 * i;
+            tree.addTile(3, Coord(o[0], o[1], o[2]), d->root_tile_values[i], false);
+        }
+        // child slots of every internal node, from the node lists below it
+        std::vector<std::vector<char>> upperChild(d->upper_count,
+                                                  std::vector<char>(UpperT::NUM_VALUES, 0));
+        std::vector<std::vector<char>> lowerChild(d->lower_count,
+                                                  std::vector<char>(LowerT::NUM_VALUES, 0));
+        auto findUpper = [&](const int32_t* o) -> int64_t {
+            for (int64_t u = 0; u < d->upper_count; ++u) {
+                const int32_t* uo = d->upper_origins + 3 * u;
+                if ((o[0] & ~4095) == uo[0] && (o[1] & ~4095) == uo[1] && (o[2] & ~4095) == uo[2])
+                    return u;
+            }
+            return -1;
+        };
+        std::vector<int64_t> lowerIndexOfLeaf(d->leaf_count, -1);
+        for (int64_t l = 0; l < d->lower_count; ++l) {
+            const int32_t* lo = d->lower_origins + 3 * l;
+            const int64_t u = findUpper(lo);
+            if (u < 0) return fail(GBLS_ERR_INVALID_ARGUMENT, "lower node without upper node");
+            const int n = (((lo[0] >> 7) & 31) << 10) | (((lo[1] >> 7) & 31) << 5) | ((lo[2] >> 7) & 31);
+            upperChild[u][n] = 1;
+        }
+        for (int64_t f = 0; f < d->leaf_count; ++f) {
+            const int32_t* fo = d->leaf_origins + 3 * f;
+            for (int64_t l = 0; l < d->lower_count; ++l) {
+                const int32_t* lo = d->lower_origins + 3 * l;
+                if ((fo[0] & ~127) == lo[0] && (fo[1] & ~127) == lo[1] && (fo[2] & ~127) == lo[2]) {
+                    const int n = (((fo[0] >> 3) & 15) << 8) | (((fo[1] >> 3) & 15) << 4) | ((fo[2] >> 3) & 15);
+                    lowerChild[l][n] = 1;
+                    lowerIndexOfLeaf[f] = l;
+                    break;
+                }
+            }
+            if (lowerIndexOfLeaf[f] < 0) return fail(GBLS_ERR_INVALID_ARGUMENT, "leaf without lower node");
+        }
+        for (int64_t u = 0; u < d->upper_count; ++u) {
+            const int32_t* uo = d->upper_origins + 3 * u;
+            const float* ut = d->upper_tiles + size_t(u) * UpperT::NUM_VALUES;
+            for (int n = 0; n < int(UpperT::NUM_VALUES); ++n) {
+                if (upperChild[u][n]) continue;
+                const Coord c(uo[0] + ((n >> 10) & 31) * 128, uo[1] + ((n >> 5) & 31) * 128,
+                              uo[2] + (n & 31) * 128);
+                tree.addTile(2, c, ut[n], false);
+            }
+        }
+        for (int64_t l = 0; l < d->lower_count; ++l) {
+            const int32_t* lo = d->lower_origins + 3 * l;
+            const float* lt = d->lower_tiles + size_t(l) * LowerT::NUM_VALUES;
+            for (int n = 0; n < int(LowerT::NUM_VALUES); ++n) {
+                if (lowerChild[l][n]) continue;
+                const Coord c(lo[0] + ((n >> 8) & 15) * 8, lo[1] + ((n >> 4) & 15) * 8,
+                              lo[2] + (n & 15) * 8);
+                tree.addTile(1, c, lt[n], false);
+            }
+        }
+        for (int64_t f = 0; f < d->leaf_count; ++f) {
+            const int32_t* fo = d->leaf_origins + 3 * f;
+            LeafT* leaf = tree.touchLeaf(Coord(fo[0], fo[1], fo[2]));
+            std::memcpy(leaf->buffer().data(), d->leaf_values + 512 * size_t(f), 2048);
+            for (int w = 0; w < 8; ++w)
+                leaf->getValueMask().template getWord<uint64_t>(w) = d->leaf_masks[8 * f + w];
+        }
+        auto* rg = new RefGrid;
+        rg->grid = grid;
+        *out = rg;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
+// tools::LevelSetAdvection<FloatGrid, FieldT>::advect with the given schemes.
+int vdbref_advect(void* g, const gbls_field_desc* f, int spatial, int temporal, int tspatial,
+                  int ttemporal, int normCount, float t0, float t1, uint64_t* count) {
+    try {
+        FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+        size_t n = 0;
+        if (f->kind == GBLS_FIELD_CONSTANT || f->kind == GBLS_FIELD_DENSE) {
+            Vec3fGrid::Ptr vel = makeVelocityGrid(*f, grid.transform());
+            tools::DiscreteField<Vec3fGrid> field(*vel);
+            n = runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
+        } else {
+            AnalyticField field;
+            field.desc = *f;
+            field.xform = grid.transform().copy();
+            n = runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
+        }
+        if (count) *count = n;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
+// op: 0 track, 1 normalize, 2 prune, 3 dilate(arg), 4 erode(arg), 5 resize(arg)
+int vdbref_tracker_op(void* g, int op, int arg, int tspatial, int ttemporal, int normCount,
+                      int trim, int* result) {
+    try {
+        FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+        tools::LevelSetTracker<FloatGrid> tr(grid);
+        configureTracker(tr, tspatial, ttemporal, normCount, trim);
+        int r = 0;
+        switch (op) {
+        case 0: tr.track(); break;
+        case 1: tr.normalize(); break;
+        case 2: tr.prune(); break;
+        case 3: tr.dilate(arg); break;
+        case 4: tr.erode(arg); break;
+        case 5: r = tr.resize(Index(arg)) ? 1 : 0; break;
+        default: return fail(GBLS_ERR_INVALID_ARGUMENT, "bad tracker op");
+        }
+        if (result) *result = r;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_RUNTIME, e.what());
+    }
+}
+
+}  // extern "C"

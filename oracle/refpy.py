@@ -1,0 +1,140 @@
+"""ctypes wrapper of oracle/_ref/libvdbref.so: the UNMODIFIED reference
+(OpenVDB tools::LevelSetAdvection / LevelSetTracker, compiled from source by
+oracle/ref/build_ref.py).  Test infrastructure only.
+
+The library exists only where the reference checkout was present at build
+time (the development container); `available()` reports whether it loaded.
+"""
+import ctypes as C
+import os
+
+from openvdb_gb300 import _abi
+from openvdb_gb300.grid import HostGrid
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libvdbref.so")
+_lib = None
+
+
+def available():
+    try:
+        lib()
+        return True
+    except OSError:
+        return False
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(LIB_PATH)
+        L.vdbref_last_error.restype = C.c_char_p
+        L.vdbref_sphere.argtypes = [C.c_float] * 6 + [C.POINTER(C.c_void_p)]
+        L.vdbref_union_spheres.argtypes = [C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                           C.c_float, C.c_float, C.POINTER(C.c_void_p)]
+        L.vdbref_counts.argtypes = [C.c_void_p, C.POINTER(_abi.GridCounts)]
+        L.vdbref_export.argtypes = [C.c_void_p, C.POINTER(_abi.GridDesc)]
+        L.vdbref_from_desc.argtypes = [C.POINTER(_abi.GridDesc), C.POINTER(C.c_void_p)]
+        L.vdbref_free.argtypes = [C.c_void_p]
+        L.vdbref_free.restype = None
+        L.vdbref_advect.argtypes = [C.c_void_p, C.POINTER(_abi.FieldDesc)] + [C.c_int] * 5 + \
+            [C.c_float, C.c_float, C.POINTER(C.c_uint64)]
+        L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
+        L.vdbref_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("reference oracle error %d: %s" % (rc, lib().vdbref_last_error().decode()))
+
+
+def set_threads(n):
+    lib().vdbref_set_threads(int(n))
+
+
+def threads():
+    return lib().vdbref_threads()
+
+
+class RefGrid:
+    """A reference openvdb::FloatGrid held by the harness."""
+
+    def __init__(self, handle):
+        self.h = C.c_void_p(handle)
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value and _lib is not None:
+            _lib.vdbref_free(self.h)
+            self.h = None
+
+    @classmethod
+    def sphere(cls, radius, center=(0.0, 0.0, 0.0), voxel_size=1.0, half_width=3.0):
+        h = C.c_void_p()
+        _check(lib().vdbref_sphere(radius, center[0], center[1], center[2], voxel_size,
+                                   half_width, C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def union_of_spheres(cls, centers, radii, voxel_size=1.0, half_width=3.0):
+        import numpy as np
+        c = np.ascontiguousarray(centers, np.float32).reshape(-1)
+        r = np.ascontiguousarray(radii, np.float32).reshape(-1)
+        h = C.c_void_p()
+        _check(lib().vdbref_union_spheres(len(r), c.ctypes.data_as(C.POINTER(C.c_float)),
+                                          r.ctypes.data_as(C.POINTER(C.c_float)), voxel_size,
+                                          half_width, C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_host(cls, grid):
+        d = grid.desc()
+        h = C.c_void_p()
+        _check(lib().vdbref_from_desc(C.byref(d), C.byref(h)))
+        return cls(h.value)
+
+    def counts(self):
+        c = _abi.GridCounts()
+        _check(lib().vdbref_counts(self.h, C.byref(c)))
+        return c
+
+    def to_host(self):
+        g = HostGrid.allocate(self.counts())
+        d = g.desc()
+        _check(lib().vdbref_export(self.h, C.byref(d)))
+        g.copy_scalars_from(d)
+        return g
+
+    def advect(self, field, t0, t1, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK2,
+               tracker_spatial=_abi.HJWENO5_BIAS, tracker_temporal=_abi.TVD_RK1, norm_count=3):
+        n = C.c_uint64()
+        fd = field.desc() if hasattr(field, "desc") else field
+        _check(lib().vdbref_advect(self.h, C.byref(fd), spatial, temporal, tracker_spatial,
+                                   tracker_temporal, norm_count, t0, t1, C.byref(n)))
+        return n.value
+
+    def tracker_op(self, op, arg=0, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1,
+                   norm_count=3, trim=_abi.TRIM_ALL):
+        r = C.c_int()
+        _check(lib().vdbref_tracker_op(self.h, op, arg, spatial, temporal, norm_count, trim,
+                                       C.byref(r)))
+        return r.value
+
+    def track(self, **kw):
+        self.tracker_op(0, **kw)
+
+    def normalize(self, **kw):
+        self.tracker_op(1, **kw)
+
+    def prune(self, **kw):
+        self.tracker_op(2, **kw)
+
+    def dilate(self, n=1, **kw):
+        self.tracker_op(3, n, **kw)
+
+    def erode(self, n=1, **kw):
+        self.tracker_op(4, n, **kw)
+
+    def resize(self, half_width=3, **kw):
+        return bool(self.tracker_op(5, half_width, **kw))
