@@ -203,6 +203,24 @@ int gbls_field_destroy(gbls_field* f);
 int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
                 int temporal_scheme, float t0, float t1, float cfl, uint64_t* substeps);
 
+
+/* ---- host construction of level sets ------------------------------------
+ * gbls_host_sphere replaces tools::createLevelSetSphere
+ * (tools/LevelSetSphere.h:219-230): same rasterisation, background and
+ * signed flood fill, so the result equals the reference grid voxel for voxel.
+ * gbls_host_union_of_spheres rasterises the union of spheres directly (the
+ * minimum of the sphere distances, then the same signed flood fill).
+ * gbls_host_grid_view returns a descriptor pointing into the host grid's
+ * arrays (valid until gbls_host_grid_free).                                 */
+typedef struct gbls_host_grid gbls_host_grid;
+int gbls_host_sphere(float radius, const float center[3], float voxel_size, float half_width,
+                     gbls_host_grid** out);
+int gbls_host_union_of_spheres(int64_t n, const float* centers, const float* radii,
+                               float voxel_size, float half_width, gbls_host_grid** out);
+int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* view);
+int gbls_host_grid_free(gbls_host_grid* g);
+const char* gbls_host_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,4 +2,6 @@
 LevelSetTracker hot path) behind a C ABI; see include/gbls.h."""
 from . import _abi
 from .fields import Field
-from .grid import HostGrid, bitwise_equal, compare, topology_equal
+from .grid import HostGrid, bitwise_equal, compare, digest, summary, topology_equal
+from .levelset import (FAST, PARITY, DeviceField, DeviceLevelSet, LevelSetAdvection,
+                       LevelSetTracker)

@@ -1,0 +1,1510 @@
+// C ABI of the GB300 narrow-band level-set library (include/gbls.h).
+//
+// Host orchestration of LevelSetAdvection::advect (tools/LevelSetAdvect.h:
+// 338-418) and LevelSetTracker::track (tools/LevelSetTracker.h:302-315) over
+// the device tree described in gbls_internal.cuh.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gbls.h"
+#include "gbls_internal.cuh"
+#include "stencil.h"
+#include "stencil_ops.cuh"
+#include "topology.cuh"
+
+using namespace gbls;
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local int g_device = 0;
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+void cuda_check(cudaError_t e, const char* what, int line) {
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation)
+            fail(GBLS_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+        fail(GBLS_ERR_CUDA, std::string(what) + " (line " + std::to_string(line) + "): " +
+                                cudaGetErrorString(e));
+    }
+}
+#define CU(x) cuda_check((x), #x, __LINE__)
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return GBLS_OK;
+    } catch (const Error& e) {
+        g_last_error = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return GBLS_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return GBLS_ERR_RUNTIME;
+    }
+}
+
+// Growable device array.
+template <class T>
+struct DevArray {
+    T* p = nullptr;
+    size_t cap = 0;
+    DevArray() = default;
+    DevArray(const DevArray&) = delete;
+    DevArray& operator=(const DevArray&) = delete;
+    ~DevArray() {
+        if (p) cudaFree(p);
+    }
+    // Ensure room for n elements, keeping the first `keep` elements.
+    void reserve(size_t n, cudaStream_t s, size_t keep = 0, double growth = 1.5) {
+        if (n <= cap) return;
+        size_t nc = std::max(n, size_t(double(cap) * growth));
+        if (nc < 16) nc = 16;
+        T* q = nullptr;
+        CU(cudaMalloc(&q, nc * sizeof(T)));
+        if (p && keep) CU(cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, s));
+        if (p) {
+            CU(cudaStreamSynchronize(s));
+            CU(cudaFree(p));
+        }
+        p = q;
+        cap = nc;
+    }
+    void upload(const T* h, size_t n, cudaStream_t s) {
+        reserve(n, s);
+        if (n) CU(cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void download(T* h, size_t n, cudaStream_t s) const {
+        if (n) CU(cudaMemcpyAsync(h, p, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+};
+
+inline unsigned blocks_for(int64_t n, int threads) { return unsigned((n + threads - 1) / threads); }
+
+// ---------------------------------------------------------------------------
+// topology kernels
+// ---------------------------------------------------------------------------
+
+// Candidate leaves created by NN_FACE dilation: a missing face neighbour
+// that would receive active bits.  Emits (key << 1) | tile sign.
+__global__ void k_emit_candidates(int64_t n, const uint64_t* keys, const int32_t* slot,
+                                  const int32_t* nbr, const uint64_t* am, uint64_t* cand,
+                                  unsigned long long* count) {
+    const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (l >= n) return;
+    const int32_t* nb = nbr + 6 * l;
+    bool any_missing = false;
+    for (int f = 0; f < 6; ++f) any_missing |= nb[f] < 0;
+    if (!any_missing) return;
+    uint64_t m[8];
+    const int s = slot[l];
+    for (int w = 0; w < 8; ++w) m[w] = am[size_t(s) * 8 + w];
+    for (int f = 0; f < 6; ++f) {
+        if (nb[f] >= 0) continue;
+        if (!face_layer_nonzero(m, f)) continue;
+        const uint64_t nk = neighbour_key(keys[l], f);
+        if (!origin_in_range(nk)) continue;
+        const unsigned long long at = atomicAdd(count, 1ull);
+        cand[at] = (nk << 1) | uint64_t(nb[f] == NBR_TILE_NEG ? 1 : 0);
+    }
+}
+
+// Give the sorted unique new leaves their slots; their masks start empty and
+// every voxel takes the tile value (tree/InternalNode.h:2874-2876).
+__global__ void k_new_leaves(int64_t n, const uint64_t* cand, const int32_t* free_slots,
+                             int64_t nfree, uint64_t* new_keys, int32_t* new_slots, uint64_t* am,
+                             uint64_t* sm) {
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    const uint64_t c = cand[j];
+    const int32_t s = free_slots[nfree - 1 - j];
+    new_keys[j] = c >> 1;
+    new_slots[j] = s;
+    const uint64_t fill = (c & 1) ? ~uint64_t(0) : uint64_t(0);
+    for (int w = 0; w < 8; ++w) {
+        am[size_t(s) * 8 + w] = 0;
+        sm[size_t(s) * 8 + w] = fill;
+    }
+}
+
+// Merge two sorted, disjoint key lists (with their slots) into tree order.
+__global__ void k_merge(int64_t na, const uint64_t* ka, const int32_t* sa, int64_t nb,
+                        const uint64_t* kb, const int32_t* sb, uint64_t* ko, int32_t* so) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < na) {
+        const int64_t pos = i + lower_bound_u64(kb, nb, ka[i]);
+        ko[pos] = ka[i];
+        so[pos] = sa[i];
+    } else if (i < na + nb) {
+        const int64_t j = i - na;
+        const int64_t pos = j + lower_bound_u64(ka, na, kb[j]);
+        ko[pos] = kb[j];
+        so[pos] = sb[j];
+    }
+}
+
+// Face-neighbour table: slot of the neighbour leaf, else the sign of the
+// tile covering it.
+__global__ void k_build_nbr(int64_t n, const uint64_t* keys, const int32_t* slot, NodeTables nt,
+                            int32_t* nbr) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n * 6) return;
+    const int64_t l = i / 6;
+    const int f = int(i - l * 6);
+    const uint64_t nk = neighbour_key(keys[l], f);
+    int32_t r;
+    if (!origin_in_range(nk)) {
+        r = NBR_TILE_POS;
+    } else {
+        const int64_t j = find_u64(keys, n, nk);
+        r = (j >= 0) ? slot[j] : (tile_sign(nt, nk) ? NBR_TILE_NEG : NBR_TILE_POS);
+    }
+    nbr[i] = r;
+}
+
+// NN_FACE dilation of every leaf mask into dmask (8 threads per leaf).
+__global__ void k_dilate(int64_t n, const int32_t* slot, const int32_t* nbr, const uint64_t* am,
+                         uint64_t* dmask) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n * 8) return;
+    const int64_t l = i >> 3;
+    const int x = int(i & 7);
+    const int s = slot[l];
+    const int32_t* nb = nbr + 6 * l;
+    const uint64_t* own = am + size_t(s) * 8;
+    auto P = [&](int f) -> const uint64_t* { return nb[f] >= 0 ? am + size_t(nb[f]) * 8 : nullptr; };
+    dmask[size_t(s) * 8 + x] = dilate_word(own, x, P(0), P(1), P(2), P(3), P(4), P(5));
+}
+
+// Lower nodes missing for new leaves (rare): append lower keys.
+__global__ void k_missing_lower(int64_t n, const uint64_t* new_keys, const uint64_t* lower_keys,
+                                int64_t nlower, uint64_t* out, unsigned long long* count) {
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j >= n) return;
+    const uint64_t lk = new_keys[j] >> 12;
+    if (find_u64(lower_keys, nlower, lk) >= 0) return;
+    out[atomicAdd(count, 1ull)] = lk;
+}
+
+__global__ void k_keep_flags(int64_t n, const int32_t* cnt, int32_t* keep) {
+    const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (l >= n) return;
+    keep[l] = cnt[l] > 0 ? 1 : 0;
+}
+
+// Leaf-level prune (tools/Prune.h:305-312 with getTileValue :326-329): an
+// inactive leaf becomes a lower-node tile of the sign of its first voxel;
+// its slot returns to the free stack.
+__global__ void k_prune_scatter(int64_t n, const uint64_t* keys, const int32_t* slot,
+                                const int32_t* keep, const int32_t* idx, const uint64_t* sm,
+                                uint64_t* ko, int32_t* so, int32_t* free_slots, int64_t nfree,
+                                const uint64_t* lower_keys, int64_t nlower, uint64_t* lower_sign,
+                                unsigned long long* nkept, unsigned long long* err) {
+    const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (l >= n) return;
+    const int64_t k = idx[l];
+    if (l == n - 1) *nkept = (unsigned long long)(k + keep[l]);
+    if (keep[l]) {
+        ko[k] = keys[l];
+        so[k] = slot[l];
+        return;
+    }
+    const int s = slot[l];
+    free_slots[nfree + (l - k)] = s;
+    const uint64_t key = keys[l];
+    const int64_t li = find_u64(lower_keys, nlower, key >> 12);
+    if (li < 0) {
+        atomicAdd(err, 1ull);
+        return;
+    }
+    const uint32_t nbit = uint32_t(key & 4095);
+    unsigned long long* word = reinterpret_cast<unsigned long long*>(lower_sign + li * 64 + (nbit >> 6));
+    const unsigned long long bit = 1ull << (nbit & 63);
+    if (sm[size_t(s) * 8] & 1) atomicOr(word, bit);
+    else atomicAnd(word, ~bit);
+}
+
+// Lower nodes without leaves (pruned into upper-node tiles by the host).
+// flag: 0 = keep, 1 = empty with a positive first value, 2 = empty negative.
+__global__ void k_lower_status(int64_t nlower, const uint64_t* lower_keys, const uint64_t* lower_sign,
+                               const uint64_t* keys, const unsigned long long* nleaf, uint8_t* flags,
+                               unsigned long long* nempty) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nlower) return;
+    const int64_t n = int64_t(*nleaf);
+    const uint64_t lk = lower_keys[i];
+    const int64_t j = lower_bound_u64(keys, n, lk << 12);
+    const bool has = j < n && (keys[j] >> 12) == lk;
+    if (has) {
+        flags[i] = 0;
+    } else {
+        flags[i] = (lower_sign[i * 64] & 1) ? 2 : 1;
+        atomicAdd(nempty, 1ull);
+    }
+}
+
+// Rebuild lower sign rows after node insertion/removal: row r copies old row
+// src[r] >= 0, or is filled with the sign (-1 - src[r]).
+__global__ void k_remap_rows(int64_t nrows, const int32_t* src, const uint64_t* old_sign, uint64_t* new_sign) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= nrows * 64) return;
+    const int64_t r = i >> 6;
+    const int w = int(i & 63);
+    const int32_t s = src[r];
+    new_sign[i] = (s >= 0) ? old_sign[int64_t(s) * 64 + w] : ((-1 - s) ? ~uint64_t(0) : uint64_t(0));
+}
+
+__global__ void k_count_active(int64_t n, const int32_t* slot, const uint64_t* am, unsigned long long* out) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    unsigned long long c = 0;
+    if (i < n * 8) c = __popcll(am[size_t(slot[i >> 3]) * 8 + (i & 7)]);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// Pack leaf values into the slot layout (upload) / unpack (download).
+__global__ void k_unpack(int64_t n, const int32_t* slot, const uint64_t* am, const uint64_t* sm,
+                         const float* vals, float gamma, float* dense) {
+    const int64_t l = blockIdx.x;
+    if (l >= n) return;
+    const int s = slot[l];
+    __shared__ int pre[9];
+    __shared__ uint64_t m[8];
+    if (threadIdx.x < 8) m[threadIdx.x] = am[size_t(s) * 8 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int w = 0; w < 8; ++w) { pre[w] = acc; acc += __popcll(m[w]); }
+        pre[8] = acc;
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < LEAF_VOX; v += blockDim.x) {
+        const int w = v >> 6, b = v & 63;
+        float val;
+        if ((m[w] >> b) & 1) {
+            val = vals[size_t(s) * LEAF_VOX + pre[w] + __popcll(m[w] & ((1ull << b) - 1))];
+        } else {
+            val = ((sm[size_t(s) * 8 + w] >> b) & 1) ? -gamma : gamma;
+        }
+        dense[l * LEAF_VOX + v] = val;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------
+
+struct gbls_field {
+    gbls_field_desc desc{};
+    int device = 0;
+    DevArray<float> dense;
+};
+
+struct gbls_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    double voxel_size = 1.0;
+    double translation[3] = {0, 0, 0};
+    int map_type = GBLS_MAP_UNIFORM_SCALE;
+    float gamma = 3.0f;
+    // LevelSetTracker::State defaults (tools/LevelSetTracker.h:74-83)
+    int tr_spatial = GBLS_HJWENO5_BIAS, tr_temporal = GBLS_TVD_RK1, norm_count = 3, grain = 1;
+    int trim = GBLS_TRIM_ALL;
+    int mode = GBLS_MODE_PARITY;
+    gbls_interrupter intr{};
+    bool has_intr = false;
+
+    // leaves in tree order (double-buffered for merge / compaction)
+    int64_t nleaf = 0;
+    DevArray<uint64_t> keys[2];
+    DevArray<int32_t> slot[2];
+    int kc = 0;
+    DevArray<int32_t> nbr;
+    // slot storage: 3 mask sets, 3 value buffers, dilation mask
+    int64_t slot_cap = 0;
+    DevArray<uint64_t> am[3], sm[3];
+    DevArray<float> vals[3];
+    DevArray<uint64_t> dmask;
+    DevArray<int32_t> free_slots;
+    int64_t nfree = 0;
+    int mc = 0, vc = 0;  // current mask set / value buffer
+    // node tables: device arrays + host mirrors of keys, upper signs, root tiles
+    std::vector<uint64_t> lower_keys_h, upper_keys_h, upper_sign_h, root_keys_h;
+    std::vector<uint8_t> root_sign_h;
+    DevArray<uint64_t> lower_keys, lower_sign, upper_keys, upper_sign, root_keys;
+    DevArray<uint8_t> root_sign;
+    bool nodes_checked = false;  // empty nodes of the input removed by a prune
+    // scratch
+    DevArray<uint64_t> cand, cand_sorted, new_keys;
+    DevArray<int32_t> new_slots, cnt, keep, idx, remap;
+    DevArray<uint8_t> cub_tmp, flags;
+    DevStatus* st_d = nullptr;
+    DevStatus* st_h = nullptr;
+    DevArray<unsigned long long> u64s;
+
+    ~gbls_handle() {
+        if (st_d) cudaFree(st_d);
+        if (st_h) cudaFreeHost(st_h);
+    }
+
+    NodeTables nodes() const {
+        NodeTables t;
+        t.lower_keys = lower_keys.p;
+        t.lower_sign = lower_sign.p;
+        t.upper_keys = upper_keys.p;
+        t.upper_sign = upper_sign.p;
+        t.root_keys = root_keys.p;
+        t.root_sign = root_sign.p;
+        t.nlower = int64_t(lower_keys_h.size());
+        t.nupper = int64_t(upper_keys_h.size());
+        t.nroot = int64_t(root_keys_h.size());
+        return t;
+    }
+    uint64_t* K() { return keys[kc].p; }
+    int32_t* S() { return slot[kc].p; }
+    Layout layout(int m, int v) const { return Layout{am[m].p, sm[m].p, vals[v].p}; }
+
+    void sync() { CU(cudaStreamSynchronize(stream)); }
+    void read_status() {
+        CU(cudaMemcpyAsync(st_h, st_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+        sync();
+        if (st_h->error) fail(GBLS_ERR_DEVICE_CHECK, "device-side tree consistency check failed");
+    }
+    void clear_status() { CU(cudaMemsetAsync(st_d, 0, sizeof(DevStatus), stream)); }
+
+    void ensure_leaf_cap(int64_t n) {
+        const size_t keep_n = size_t(nleaf);
+        for (int b = 0; b < 2; ++b) {
+            keys[b].reserve(n, stream, b == kc ? keep_n : 0);
+            slot[b].reserve(n, stream, b == kc ? keep_n : 0);
+        }
+        nbr.reserve(size_t(n) * 6, stream);
+        cnt.reserve(n, stream);
+        keep.reserve(n, stream);
+        idx.reserve(n, stream);
+    }
+
+    // Make at least `need` free slots available.
+    void ensure_free_slots(int64_t need) {
+        if (nfree >= need) return;
+        const int64_t old = slot_cap;
+        int64_t nc = std::max(old + (need - nfree), int64_t(double(old) * 1.5) + 1024);
+        for (int b = 0; b < 3; ++b) {
+            am[b].reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
+            sm[b].reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
+            vals[b].reserve(size_t(nc) * LEAF_VOX, stream, size_t(old) * LEAF_VOX, 1.0);
+        }
+        dmask.reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
+        free_slots.reserve(size_t(nc), stream, size_t(nfree), 1.0);
+        // push the new slots below the existing free ones so that they are
+        // used last: [new slots..., old free slots...]
+        std::vector<int32_t> fresh;
+        for (int64_t s = nc - 1; s >= old; --s) fresh.push_back(int32_t(s));
+        const int64_t nnew = nc - old;
+        DevArray<int32_t> tmp;
+        tmp.reserve(size_t(nnew + nfree), stream);
+        CU(cudaMemcpyAsync(tmp.p, fresh.data(), nnew * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+        if (nfree)
+            CU(cudaMemcpyAsync(tmp.p + nnew, free_slots.p, nfree * sizeof(int32_t),
+                               cudaMemcpyDeviceToDevice, stream));
+        CU(cudaMemcpyAsync(free_slots.p, tmp.p, (nnew + nfree) * sizeof(int32_t),
+                           cudaMemcpyDeviceToDevice, stream));
+        sync();
+        nfree += nnew;
+        slot_cap = nc;
+    }
+
+    void upload_upper_root() {
+        upper_keys.upload(upper_keys_h.data(), upper_keys_h.size(), stream);
+        upper_sign.upload(upper_sign_h.data(), upper_sign_h.size(), stream);
+        root_keys.upload(root_keys_h.data(), root_keys_h.size(), stream);
+        root_sign.upload(root_sign_h.data(), root_sign_h.size(), stream);
+        sync();  // host vectors may change right after
+    }
+
+    void rebuild_nbr() {
+        if (nleaf == 0) return;
+        k_build_nbr<<<blocks_for(nleaf * 6, 256), 256, 0, stream>>>(nleaf, K(), S(), nodes(), nbr.p);
+        CU(cudaGetLastError());
+    }
+};
+
+namespace {
+
+int other_of(int a, int b) {
+    for (int i = 0; i < 3; ++i)
+        if (i != a && i != b) return i;
+    return -1;
+}
+
+// Remap lower-node rows: src[r] = old row or -1-sign for a new row.
+void remap_lower(gbls_handle& h, const std::vector<uint64_t>& new_keys, const std::vector<int32_t>& src) {
+    const int64_t n = int64_t(new_keys.size());
+    DevArray<uint64_t> ns;
+    ns.reserve(size_t(std::max<int64_t>(n, 1)) * 64, h.stream);
+    h.remap.upload(src.data(), src.size(), h.stream);
+    if (n) k_remap_rows<<<blocks_for(n * 64, 256), 256, 0, h.stream>>>(n, h.remap.p, h.lower_sign.p, ns.p);
+    CU(cudaGetLastError());
+    std::swap(h.lower_sign.p, ns.p);
+    std::swap(h.lower_sign.cap, ns.cap);
+    h.lower_keys_h = new_keys;
+    h.lower_keys.upload(new_keys.data(), new_keys.size(), h.stream);
+    h.sync();
+}
+
+int upper_bit(const gbls_handle& h, size_t ui, uint32_t slotn) {
+    return int((h.upper_sign_h[ui * 512 + (slotn >> 6)] >> (slotn & 63)) & 1);
+}
+
+// Create the lower (and upper) nodes that new leaves need
+// (tree/InternalNode.h:2868-2878, tree/RootNode.h:3255-3266): a new node's
+// tiles take the value of the tile it replaces.
+void insert_nodes(gbls_handle& h, std::vector<uint64_t> miss) {
+    std::sort(miss.begin(), miss.end());
+    miss.erase(std::unique(miss.begin(), miss.end()), miss.end());
+    // upper nodes first
+    std::vector<uint64_t> new_up;
+    for (uint64_t lk : miss) {
+        const uint64_t uk = lk >> 15;
+        if (!std::binary_search(h.upper_keys_h.begin(), h.upper_keys_h.end(), uk)) new_up.push_back(uk);
+    }
+    std::sort(new_up.begin(), new_up.end());
+    new_up.erase(std::unique(new_up.begin(), new_up.end()), new_up.end());
+    if (!new_up.empty()) {
+        std::vector<uint64_t> keys;
+        std::vector<uint64_t> signs;
+        size_t a = 0, b = 0;
+        while (a < h.upper_keys_h.size() || b < new_up.size()) {
+            if (b >= new_up.size() || (a < h.upper_keys_h.size() && h.upper_keys_h[a] < new_up[b])) {
+                keys.push_back(h.upper_keys_h[a]);
+                signs.insert(signs.end(), h.upper_sign_h.begin() + a * 512, h.upper_sign_h.begin() + (a + 1) * 512);
+                ++a;
+            } else {
+                const uint64_t uk = new_up[b++];
+                int sgn = 0;
+                auto it = std::lower_bound(h.root_keys_h.begin(), h.root_keys_h.end(), uk);
+                if (it != h.root_keys_h.end() && *it == uk) {
+                    const size_t ri = size_t(it - h.root_keys_h.begin());
+                    sgn = h.root_sign_h[ri];
+                    h.root_keys_h.erase(h.root_keys_h.begin() + ri);
+                    h.root_sign_h.erase(h.root_sign_h.begin() + ri);
+                }
+                keys.push_back(uk);
+                signs.insert(signs.end(), 512, sgn ? ~uint64_t(0) : uint64_t(0));
+            }
+        }
+        h.upper_keys_h.swap(keys);
+        h.upper_sign_h.swap(signs);
+        h.upload_upper_root();
+    }
+    // lower nodes
+    std::vector<uint64_t> keys;
+    std::vector<int32_t> src;
+    size_t a = 0, b = 0;
+    while (a < h.lower_keys_h.size() || b < miss.size()) {
+        if (b >= miss.size() || (a < h.lower_keys_h.size() && h.lower_keys_h[a] < miss[b])) {
+            keys.push_back(h.lower_keys_h[a]);
+            src.push_back(int32_t(a));
+            ++a;
+        } else {
+            const uint64_t lk = miss[b++];
+            const uint64_t uk = lk >> 15;
+            const size_t ui = size_t(std::lower_bound(h.upper_keys_h.begin(), h.upper_keys_h.end(), uk) -
+                                     h.upper_keys_h.begin());
+            keys.push_back(lk);
+            src.push_back(-1 - upper_bit(h, ui, uint32_t(lk & 32767)));
+        }
+    }
+    remap_lower(h, keys, src);
+}
+
+// Node-level part of pruneLevelSet (tools/Prune.h:305-322): lower nodes
+// without leaves become upper tiles of the sign of their first value, upper
+// nodes without lower nodes become root tiles; +background root tiles are
+// erased (RootNode::eraseBackgroundTiles).
+void prune_nodes(gbls_handle& h, bool lower_changed) {
+    const int64_t nl = int64_t(h.lower_keys_h.size());
+    if (lower_changed && nl) {
+        std::vector<uint8_t> fl(static_cast<size_t>(nl));
+        h.flags.download(fl.data(), size_t(nl), h.stream);
+        h.sync();
+        std::vector<uint64_t> keys;
+        std::vector<int32_t> src;
+        for (int64_t i = 0; i < nl; ++i) {
+            const uint64_t lk = h.lower_keys_h[size_t(i)];
+            if (fl[size_t(i)] == 0) {
+                keys.push_back(lk);
+                src.push_back(int32_t(i));
+                continue;
+            }
+            const uint64_t uk = lk >> 15;
+            auto it = std::lower_bound(h.upper_keys_h.begin(), h.upper_keys_h.end(), uk);
+            if (it == h.upper_keys_h.end() || *it != uk) fail(GBLS_ERR_DEVICE_CHECK, "lower node without upper node");
+            const size_t ui = size_t(it - h.upper_keys_h.begin());
+            const uint32_t n = uint32_t(lk & 32767);
+            uint64_t& w = h.upper_sign_h[ui * 512 + (n >> 6)];
+            if (fl[size_t(i)] == 2) w |= (uint64_t(1) << (n & 63));
+            else w &= ~(uint64_t(1) << (n & 63));
+        }
+        remap_lower(h, keys, src);
+    }
+    // upper nodes without lower nodes
+    std::vector<uint64_t> ukeys, usign;
+    bool changed = lower_changed;
+    for (size_t u = 0; u < h.upper_keys_h.size(); ++u) {
+        const uint64_t uk = h.upper_keys_h[u];
+        auto it = std::lower_bound(h.lower_keys_h.begin(), h.lower_keys_h.end(), uk << 15);
+        const bool has = it != h.lower_keys_h.end() && ((*it) >> 15) == uk;
+        if (has) {
+            ukeys.push_back(uk);
+            usign.insert(usign.end(), h.upper_sign_h.begin() + u * 512, h.upper_sign_h.begin() + (u + 1) * 512);
+        } else {
+            changed = true;
+            if (h.upper_sign_h[u * 512] & 1) {
+                auto rt = std::lower_bound(h.root_keys_h.begin(), h.root_keys_h.end(), uk);
+                const size_t ri = size_t(rt - h.root_keys_h.begin());
+                h.root_keys_h.insert(rt, uk);
+                h.root_sign_h.insert(h.root_sign_h.begin() + ri, 1);
+            }
+        }
+    }
+    h.upper_keys_h.swap(ukeys);
+    h.upper_sign_h.swap(usign);
+    // eraseBackgroundTiles
+    for (size_t r = 0; r < h.root_sign_h.size();) {
+        if (h.root_sign_h[r] == 0) {
+            h.root_keys_h.erase(h.root_keys_h.begin() + r);
+            h.root_sign_h.erase(h.root_sign_h.begin() + r);
+            changed = true;
+        } else {
+            ++r;
+        }
+    }
+    if (changed) h.upload_upper_root();
+}
+
+// ---- dilation: new leaves, node creation, neighbour table, dmask ----------
+void dilate_topology(gbls_handle& h) {
+    if (h.nleaf == 0) return;
+    const int64_t L = h.nleaf;
+    h.cand.reserve(size_t(L) * 6, h.stream);
+    h.clear_status();
+    k_emit_candidates<<<blocks_for(L, 128), 128, 0, h.stream>>>(L, h.K(), h.S(), h.nbr.p, h.am[h.mc].p,
+                                                                 h.cand.p, &h.st_d->n_cand);
+    CU(cudaGetLastError());
+    h.read_status();
+    const int64_t nc = int64_t(h.st_h->n_cand);
+    int64_t nnew = 0;
+    if (nc > 0) {
+        h.cand_sorted.reserve(size_t(nc), h.stream);
+        h.u64s.reserve(1, h.stream);
+        size_t b1 = 0, b2 = 0;
+        CU(cub::DeviceRadixSort::SortKeys(nullptr, b1, h.cand.p, h.cand_sorted.p, int(nc), 0, 64, h.stream));
+        CU(cub::DeviceSelect::Unique(nullptr, b2, h.cand_sorted.p, h.cand.p, h.u64s.p, int(nc), h.stream));
+        h.cub_tmp.reserve(std::max(b1, b2), h.stream);
+        b1 = b2 = h.cub_tmp.cap;
+        CU(cub::DeviceRadixSort::SortKeys(h.cub_tmp.p, b1, h.cand.p, h.cand_sorted.p, int(nc), 0, 64, h.stream));
+        CU(cub::DeviceSelect::Unique(h.cub_tmp.p, b2, h.cand_sorted.p, h.cand.p, h.u64s.p, int(nc), h.stream));
+        unsigned long long n_u = 0;
+        CU(cudaMemcpyAsync(&n_u, h.u64s.p, sizeof(n_u), cudaMemcpyDeviceToHost, h.stream));
+        h.sync();
+        nnew = int64_t(n_u);
+    }
+    if (nnew > 0) {
+        h.ensure_free_slots(nnew);
+        h.ensure_leaf_cap(L + nnew);
+        h.new_keys.reserve(size_t(nnew), h.stream);
+        h.new_slots.reserve(size_t(nnew), h.stream);
+        k_new_leaves<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(nnew, h.cand.p, h.free_slots.p, h.nfree,
+                                                                   h.new_keys.p, h.new_slots.p,
+                                                                   h.am[h.mc].p, h.sm[h.mc].p);
+        CU(cudaGetLastError());
+        h.nfree -= nnew;
+        const int ko = 1 - h.kc;
+        k_merge<<<blocks_for(L + nnew, 256), 256, 0, h.stream>>>(L, h.K(), h.S(), nnew, h.new_keys.p,
+                                                                 h.new_slots.p, h.keys[ko].p, h.slot[ko].p);
+        CU(cudaGetLastError());
+        h.kc = ko;
+        h.nleaf = L + nnew;
+        // lower / upper nodes for the new leaves
+        h.cand_sorted.reserve(size_t(nnew), h.stream);
+        h.clear_status();
+        k_missing_lower<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(
+            nnew, h.new_keys.p, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.cand_sorted.p,
+            &h.st_d->n_lower_miss);
+        CU(cudaGetLastError());
+        h.read_status();
+        const int64_t nm = int64_t(h.st_h->n_lower_miss);
+        if (nm > 0) {
+            std::vector<uint64_t> miss(static_cast<size_t>(nm));
+            h.cand_sorted.download(miss.data(), size_t(nm), h.stream);
+            h.sync();
+            insert_nodes(h, miss);
+        }
+    }
+    h.rebuild_nbr();
+    k_dilate<<<blocks_for(h.nleaf * 8, 256), 256, 0, h.stream>>>(h.nleaf, h.S(), h.nbr.p, h.am[h.mc].p,
+                                                                  h.dmask.p);
+    CU(cudaGetLastError());
+}
+
+// ---- normalize / trim passes ----------------------------------------------
+void launch_norm(gbls_handle& h, const NormArgs& a) {
+    if (h.mode == GBLS_MODE_PARITY) launch_norm_parity(a, h.stream);
+    else launch_norm_fast(a, h.stream);
+    CU(cudaGetLastError());
+}
+
+void start_intr(gbls_handle& h, const char* msg) {
+    if (h.has_intr && h.intr.start) h.intr.start(h.intr.user, msg);
+}
+void end_intr(gbls_handle& h) {
+    if (h.has_intr && h.intr.end) h.intr.end(h.intr.user);
+}
+bool check_intr(gbls_handle& h) {
+    if (h.has_intr && h.intr.was_interrupted) return h.intr.was_interrupted(h.intr.user, -1) == 0;
+    return true;
+}
+
+// Normalizer::normalize (tools/LevelSetTracker.h:528-598) over the voxels of
+// pmask, starting from the current layout; when `trim` is set the final
+// stage also applies Trim.  With norm_count == 0 and trim set, a trim-only
+// pass runs.  Leaves the result as the current layout and per-leaf counts
+// in h.cnt.
+void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim) {
+    if (h.nleaf == 0) return;
+    const float dx = float(h.voxel_size);
+    const float mdt = dx * (h.tr_temporal == GBLS_TVD_RK1 ? 0.3f : h.tr_temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f);
+    const float invdx = 1.0f / dx;
+    NormArgs base{};
+    base.nleaf = h.nleaf;
+    base.slot = h.S();
+    base.nbr = h.nbr.p;
+    base.pmask = pmask;
+    base.gamma = h.gamma;
+    base.mdt = mdt;
+    base.invdx = invdx;
+    base.out_count = h.cnt.p;
+    const int iters = h.norm_count;
+    if (iters <= 0) {
+        if (!trim) return;
+        NormArgs a = base;
+        const int mo = other_of(h.mc, h.mc), vo = other_of(h.vc, h.vc);
+        a.src = h.layout(h.mc, h.vc);
+        a.copy_only = 1;
+        a.trim = trim;
+        a.out_vals = h.vals[vo].p;
+        a.out_amask = h.am[mo].p;
+        a.out_smask = h.sm[mo].p;
+        start_intr(h, "Pruning Level Set");
+        launch_norm(h, a);
+        end_intr(h);
+        h.mc = mo;
+        h.vc = vo;
+        return;
+    }
+    const int stages = h.tr_temporal == GBLS_TVD_RK1 ? 1 : h.tr_temporal == GBLS_TVD_RK2 ? 2 : 3;
+    for (int it = 0; it < iters; ++it) {
+        const int m0 = h.mc, v0 = h.vc;  // phi_n
+        int ms = m0, vs = v0;           // current stencil source
+        for (int st = 0; st < stages; ++st) {
+            const bool last = (st == stages - 1);
+            NormArgs a = base;
+            a.src = h.layout(ms, vs);
+            a.phi = h.layout(m0, v0);
+            a.trim = (last && it == iters - 1) ? trim : 0;
+            int mo, vo;
+            if (st == 0) {
+                mo = other_of(m0, m0);
+                vo = other_of(v0, v0);
+                a.has_phi = 0;
+                a.alpha = 0.0f;
+                a.beta = 1.0f;
+            } else {
+                // euler12 (1/2), euler34 (3/4), euler13 (1/3): Alpha = N/D, Beta = 1 - Alpha
+                const float alpha = (stages == 2) ? 1.0f / 2.0f : (st == 1 ? 3.0f / 4.0f : 1.0f / 3.0f);
+                a.has_phi = 1;
+                a.alpha = alpha;
+                a.beta = 1.0f - alpha;
+                if (last) {  // may overwrite phi_n (read only at the own voxel)
+                    mo = m0;
+                    vo = v0;
+                    if (mo == ms) mo = other_of(ms, m0);
+                    if (vo == vs) vo = other_of(vs, v0);
+                } else {
+                    mo = other_of(ms, m0);
+                    vo = other_of(vs, v0);
+                }
+            }
+            a.out_vals = h.vals[vo].p;
+            a.out_amask = h.am[mo].p;
+            a.out_smask = h.sm[mo].p;
+            start_intr(h, "Normalizing level set");
+            launch_norm(h, a);
+            end_intr(h);
+            ms = mo;
+            vs = vo;
+        }
+        h.mc = ms;
+        h.vc = vs;
+        pmask = h.am[h.mc].p;  // later iterations update the (now current) active set
+        base.pmask = pmask;
+    }
+}
+
+// Leaf + node prune after a trim pass (LevelSetTracker::prune,
+// tools/LevelSetTracker.h:279-300).  Uses per-leaf counts in h.cnt.
+void prune_compact(gbls_handle& h) {
+    const int64_t L = h.nleaf;
+    bool lower_changed = false;
+    if (L > 0) {
+        k_keep_flags<<<blocks_for(L, 256), 256, 0, h.stream>>>(L, h.cnt.p, h.keep.p);
+        CU(cudaGetLastError());
+        size_t bytes = 0;
+        CU(cub::DeviceScan::ExclusiveSum(nullptr, bytes, h.keep.p, h.idx.p, int(L), h.stream));
+        h.cub_tmp.reserve(bytes, h.stream);
+        bytes = h.cub_tmp.cap;
+        CU(cub::DeviceScan::ExclusiveSum(h.cub_tmp.p, bytes, h.keep.p, h.idx.p, int(L), h.stream));
+        h.clear_status();
+        const int ko = 1 - h.kc;
+        k_prune_scatter<<<blocks_for(L, 256), 256, 0, h.stream>>>(
+            L, h.K(), h.S(), h.keep.p, h.idx.p, h.sm[h.mc].p, h.keys[ko].p, h.slot[ko].p, h.free_slots.p,
+            h.nfree, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.lower_sign.p, &h.st_d->n_cand,
+            &h.st_d->error);
+        CU(cudaGetLastError());
+        h.kc = ko;
+        const int64_t nl = int64_t(h.lower_keys_h.size());
+        h.flags.reserve(size_t(std::max<int64_t>(nl, 1)), h.stream);
+        if (nl)
+            k_lower_status<<<blocks_for(nl, 128), 128, 0, h.stream>>>(nl, h.lower_keys.p, h.lower_sign.p,
+                                                                       h.K(), &h.st_d->n_cand, h.flags.p,
+                                                                       &h.st_d->n_lower_empty);
+        CU(cudaGetLastError());
+        h.read_status();
+        const int64_t kept = int64_t(h.st_h->n_cand);
+        h.nfree += L - kept;
+        h.nleaf = kept;
+        lower_changed = h.st_h->n_lower_empty > 0;
+    } else if (!h.lower_keys_h.empty()) {
+        // no leaves: every lower node is empty
+        const int64_t nl = int64_t(h.lower_keys_h.size());
+        h.flags.reserve(size_t(nl), h.stream);
+        h.clear_status();
+        k_lower_status<<<blocks_for(nl, 128), 128, 0, h.stream>>>(nl, h.lower_keys.p, h.lower_sign.p, h.K(),
+                                                                   &h.st_d->n_cand, h.flags.p,
+                                                                   &h.st_d->n_lower_empty);
+        CU(cudaGetLastError());
+        h.read_status();
+        lower_changed = true;
+    }
+    if (lower_changed || !h.nodes_checked || !h.root_keys_h.empty()) prune_nodes(h, lower_changed);
+    h.nodes_checked = true;
+    h.rebuild_nbr();
+}
+
+void track(gbls_handle& h) {
+    dilate_topology(h);
+    normalize_pass(h, h.dmask.p, h.trim);
+    if (h.nleaf > 0 && h.norm_count <= 0 && !h.trim) {
+        // no normalisation and no trimming: the dilated mask becomes active as is
+        NormArgs a{};
+        a.nleaf = h.nleaf;
+        a.slot = h.S();
+        a.nbr = h.nbr.p;
+        a.src = h.layout(h.mc, h.vc);
+        a.pmask = h.dmask.p;
+        a.copy_only = 1;
+        a.gamma = h.gamma;
+        a.out_count = h.cnt.p;
+        const int mo = other_of(h.mc, h.mc), vo = other_of(h.vc, h.vc);
+        a.out_vals = h.vals[vo].p;
+        a.out_amask = h.am[mo].p;
+        a.out_smask = h.sm[mo].p;
+        launch_norm(h, a);
+        h.mc = mo;
+        h.vc = vo;
+    }
+    start_intr(h, "Pruning Level Set");
+    prune_compact(h);
+    end_intr(h);
+}
+
+void check_scheme(int spatial, int temporal) {
+    if (spatial < GBLS_FIRST_BIAS || spatial > GBLS_HJWENO5_BIAS)
+        fail(GBLS_ERR_VALUE, "Spatial difference scheme not supported!");
+    if (temporal < GBLS_TVD_RK1 || temporal > GBLS_TVD_RK3)
+        fail(GBLS_ERR_VALUE, "Temporal integration scheme not supported!");
+    if (spatial != GBLS_HJWENO5_BIAS)
+        fail(GBLS_ERR_UNSUPPORTED, "the device path implements the HJWENO5_BIAS spatial scheme");
+}
+
+FieldParams field_params(const gbls_field* f) {
+    FieldParams p{};
+    const gbls_field_desc& d = f->desc;
+    p.kind = d.kind;
+    for (int i = 0; i < 3; ++i) {
+        p.constant[i] = d.constant[i];
+        p.dense_origin[i] = d.dense_origin[i];
+        p.dense_dims[i] = d.dense_dims[i];
+        p.dense_background[i] = d.dense_background[i];
+        p.omega[i] = d.omega[i];
+        p.center[i] = d.center[i];
+    }
+    p.dense = f->dense.p;
+    p.domain = d.domain;
+    p.period = d.period;
+    p.scale = d.scale;
+    return p;
+}
+
+// max |v|^2 over the active voxels at time t (sampleField, :447-455).
+float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
+    if (f->desc.kind == GBLS_FIELD_CONSTANT) {
+        const float* c = f->desc.constant;
+        return c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    }
+    h.clear_status();
+    CflArgs a{};
+    a.nleaf = h.nleaf;
+    a.keys = h.K();
+    a.slot = h.S();
+    a.amask = h.am[h.mc].p;
+    a.t0 = t;
+    a.field = field_params(f);
+    a.max_bits = &h.st_d->max_v2_bits;
+    launch_cfl(a, h.stream);
+    CU(cudaGetLastError());
+    h.read_status();
+    float m;
+    std::memcpy(&m, &h.st_h->max_v2_bits, 4);
+    return m;
+}
+
+void rk_stage(gbls_handle& h, const RkArgs& a) {
+    if (h.mode == GBLS_MODE_PARITY) launch_rk_parity(a, h.stream);
+    else launch_rk_fast(a, h.stream);
+    CU(cudaGetLastError());
+}
+
+// The TVD-RK stages of one substep (tools/LevelSetAdvect.h:360-405).
+void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, float dt, bool backward) {
+    RkArgs base{};
+    base.nleaf = h.nleaf;
+    base.keys = h.K();
+    base.slot = h.S();
+    base.nbr = h.nbr.p;
+    base.dt = dt;
+    base.gamma = h.gamma;
+    base.t0 = t0;
+    base.backward = backward ? 1 : 0;
+    base.invdx = 1.0 / h.voxel_size;
+    base.field = field_params(f);
+    const int a0 = h.vc, b0 = (h.vc + 1) % 3, c0 = (h.vc + 2) % 3;
+    auto stage = [&](int src, int phin, int out, float alpha, int has_phi, const char* msg) {
+        RkArgs a = base;
+        a.src = h.layout(h.mc, src);
+        a.phin = h.vals[phin].p;
+        a.out = h.vals[out].p;
+        a.alpha = alpha;
+        a.beta = 1.0f - alpha;
+        a.has_phi = has_phi;
+        start_intr(h, msg);
+        rk_stage(h, a);
+        end_intr(h);
+    };
+    if (temporal == GBLS_TVD_RK1) {
+        stage(a0, a0, b0, 0.0f, 0, "Advecting level set using TVD_RK1");
+        h.vc = b0;
+    } else if (temporal == GBLS_TVD_RK2) {
+        stage(a0, a0, b0, 0.0f, 0, "Advecting level set using TVD_RK1 (step 1 of 2)");
+        stage(b0, a0, a0, 1.0f / 2.0f, 1, "Advecting level set using TVD_RK1 (step 2 of 2)");
+        h.vc = a0;
+    } else {
+        stage(a0, a0, b0, 0.0f, 0, "Advecting level set using TVD_RK3 (step 1 of 3)");
+        stage(b0, a0, c0, 3.0f / 4.0f, 1, "Advecting level set using TVD_RK3 (step 2 of 3)");
+        stage(c0, a0, a0, 1.0f / 3.0f, 1, "Advecting level set using TVD_RK3 (step 3 of 3)");
+        h.vc = a0;
+    }
+}
+
+// ---- upload / download ------------------------------------------------------
+bool is_pm_gamma(float v, float g) { return v == g || v == -g; }
+
+void upload(gbls_handle& h, const gbls_grid_desc* d) {
+    if (!(d->voxel_size > 0.0)) fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
+    if (!(d->background > 0.0f)) fail(GBLS_ERR_RUNTIME, "LevelSetTracker expected a level set (positive background)");
+    if (d->map_type < GBLS_MAP_UNIFORM_SCALE || d->map_type > GBLS_MAP_TRANSLATION)
+        fail(GBLS_ERR_VALUE, "MapType not supported!");
+    h.voxel_size = d->voxel_size;
+    for (int i = 0; i < 3; ++i) h.translation[i] = d->translation[i];
+    h.map_type = d->map_type;
+    h.gamma = d->background;
+    const float g = d->background;
+    const int64_t L = d->leaf_count;
+    if (L < 0 || d->lower_count < 0 || d->upper_count < 0 || d->root_tile_count < 0)
+        fail(GBLS_ERR_INVALID_ARGUMENT, "negative count");
+    if (L > 0 && (!d->leaf_origins || !d->leaf_masks || !d->leaf_values))
+        fail(GBLS_ERR_INVALID_ARGUMENT, "null leaf arrays");
+    auto check_origin = [&](const int32_t* o, int align) {
+        for (int a = 0; a < 3; ++a) {
+            if (o[a] % align != 0) fail(GBLS_ERR_INVALID_ARGUMENT, "node origin not aligned");
+            if (o[a] < -COORD_SAFE || o[a] >= COORD_SAFE) fail(GBLS_ERR_DOMAIN, "coordinate outside the supported range");
+        }
+    };
+    // leaves, sorted into tree order
+    std::vector<std::pair<uint64_t, int64_t>> order(static_cast<size_t>(L));
+    for (int64_t i = 0; i < L; ++i) {
+        const int32_t* o = d->leaf_origins + 3 * i;
+        check_origin(o, 8);
+        order[size_t(i)] = {leaf_key(o[0], o[1], o[2]), i};
+    }
+    std::sort(order.begin(), order.end());
+    for (size_t i = 1; i < order.size(); ++i)
+        if (order[i].first == order[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate leaf");
+    std::vector<uint64_t> keys(static_cast<size_t>(L)), am(static_cast<size_t>(L) * 8), sm(static_cast<size_t>(L) * 8, 0);
+    std::vector<int32_t> slots(static_cast<size_t>(L));
+    std::vector<float> vals(static_cast<size_t>(L) * LEAF_VOX, 0.0f);
+    for (int64_t i = 0; i < L; ++i) {
+        const int64_t src = order[size_t(i)].second;
+        keys[size_t(i)] = order[size_t(i)].first;
+        slots[size_t(i)] = int32_t(i);
+        const float* v = d->leaf_values + src * LEAF_VOX;
+        int rank = 0;
+        for (int w = 0; w < 8; ++w) {
+            const uint64_t m = d->leaf_masks[src * 8 + w];
+            am[size_t(i) * 8 + w] = m;
+            uint64_t s = 0;
+            for (int b = 0; b < 64; ++b) {
+                const float x = v[w * 64 + b];
+                if (x < 0.0f) s |= uint64_t(1) << b;
+                if ((m >> b) & 1) {
+                    vals[size_t(i) * LEAF_VOX + rank++] = x;
+                } else if (!is_pm_gamma(x, g)) {
+                    fail(GBLS_ERR_UNSUPPORTED, "inactive leaf value other than +-background");
+                }
+            }
+            sm[size_t(i) * 8 + w] = s;
+        }
+    }
+    // lower nodes
+    std::vector<std::pair<uint64_t, int64_t>> lo(size_t(d->lower_count));
+    for (int64_t i = 0; i < d->lower_count; ++i) {
+        const int32_t* o = d->lower_origins + 3 * i;
+        check_origin(o, 128);
+        lo[size_t(i)] = {leaf_key(o[0], o[1], o[2]) >> 12, i};
+    }
+    std::sort(lo.begin(), lo.end());
+    std::vector<uint64_t> lkeys(lo.size()), lsign(lo.size() * 64, 0);
+    for (size_t i = 0; i < lo.size(); ++i) {
+        if (i && lo[i].first == lo[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate lower node");
+        lkeys[i] = lo[i].first;
+        const float* t = d->lower_tiles + lo[i].second * LOWER_SLOTS;
+        for (int n = 0; n < LOWER_SLOTS; ++n) {
+            const uint64_t k = (lkeys[i] << 12) | uint64_t(n);
+            if (std::binary_search(keys.begin(), keys.end(), k)) continue;  // child slot
+            if (!is_pm_gamma(t[n], g)) fail(GBLS_ERR_UNSUPPORTED, "lower-node tile other than +-background");
+            if (t[n] < 0.0f) lsign[i * 64 + (n >> 6)] |= uint64_t(1) << (n & 63);
+        }
+    }
+    for (uint64_t k : keys)
+        if (!std::binary_search(lkeys.begin(), lkeys.end(), k >> 12))
+            fail(GBLS_ERR_INVALID_ARGUMENT, "leaf without lower node");
+    // upper nodes
+    std::vector<std::pair<uint64_t, int64_t>> up(size_t(d->upper_count));
+    for (int64_t i = 0; i < d->upper_count; ++i) {
+        const int32_t* o = d->upper_origins + 3 * i;
+        check_origin(o, 4096);
+        up[size_t(i)] = {leaf_key(o[0], o[1], o[2]) >> 27, i};
+    }
+    std::sort(up.begin(), up.end());
+    std::vector<uint64_t> ukeys(up.size()), usign(up.size() * 512, 0);
+    for (size_t i = 0; i < up.size(); ++i) {
+        if (i && up[i].first == up[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate upper node");
+        ukeys[i] = up[i].first;
+        const float* t = d->upper_tiles + up[i].second * UPPER_SLOTS;
+        for (int n = 0; n < UPPER_SLOTS; ++n) {
+            const uint64_t k = (ukeys[i] << 15) | uint64_t(n);
+            if (std::binary_search(lkeys.begin(), lkeys.end(), k)) continue;
+            if (!is_pm_gamma(t[n], g)) fail(GBLS_ERR_UNSUPPORTED, "upper-node tile other than +-background");
+            if (t[n] < 0.0f) usign[i * 512 + (n >> 6)] |= uint64_t(1) << (n & 63);
+        }
+    }
+    for (uint64_t k : lkeys)
+        if (!std::binary_search(ukeys.begin(), ukeys.end(), k >> 15))
+            fail(GBLS_ERR_INVALID_ARGUMENT, "lower node without upper node");
+    // root tiles
+    std::vector<std::pair<uint64_t, uint8_t>> rt(size_t(d->root_tile_count));
+    for (int64_t i = 0; i < d->root_tile_count; ++i) {
+        const int32_t* o = d->root_tile_origins + 3 * i;
+        check_origin(o, 4096);
+        const float v = d->root_tile_values[i];
+        if (!is_pm_gamma(v, g)) fail(GBLS_ERR_UNSUPPORTED, "root tile other than +-background");
+        rt[size_t(i)] = {leaf_key(o[0], o[1], o[2]) >> 27, uint8_t(v < 0.0f ? 1 : 0)};
+    }
+    std::sort(rt.begin(), rt.end());
+    h.root_keys_h.clear();
+    h.root_sign_h.clear();
+    for (auto& r : rt) {
+        if (std::binary_search(ukeys.begin(), ukeys.end(), r.first))
+            fail(GBLS_ERR_INVALID_ARGUMENT, "root tile overlaps an upper node");
+        h.root_keys_h.push_back(r.first);
+        h.root_sign_h.push_back(r.second);
+    }
+    // device state
+    h.nleaf = L;
+    h.kc = 0;
+    h.mc = 0;
+    h.vc = 0;
+    h.slot_cap = 0;
+    h.nfree = 0;
+    h.ensure_leaf_cap(std::max<int64_t>(L, 16) + L / 2);
+    const int64_t scap = L + L / 2 + 1024;
+    for (int b = 0; b < 3; ++b) {
+        h.am[b].reserve(size_t(scap) * 8, h.stream);
+        h.sm[b].reserve(size_t(scap) * 8, h.stream);
+        h.vals[b].reserve(size_t(scap) * LEAF_VOX, h.stream);
+    }
+    h.dmask.reserve(size_t(scap) * 8, h.stream);
+    h.free_slots.reserve(size_t(scap), h.stream);
+    h.slot_cap = scap;
+    std::vector<int32_t> fs;
+    for (int64_t s = scap - 1; s >= L; --s) fs.push_back(int32_t(s));
+    h.nfree = int64_t(fs.size());
+    h.free_slots.upload(fs.data(), fs.size(), h.stream);
+    h.keys[0].upload(keys.data(), keys.size(), h.stream);
+    h.slot[0].upload(slots.data(), slots.size(), h.stream);
+    h.am[0].upload(am.data(), am.size(), h.stream);
+    h.sm[0].upload(sm.data(), sm.size(), h.stream);
+    h.vals[0].upload(vals.data(), vals.size(), h.stream);
+    h.lower_keys_h = lkeys;
+    h.lower_keys.upload(lkeys.data(), lkeys.size(), h.stream);
+    h.lower_sign.upload(lsign.data(), lsign.size(), h.stream);
+    h.upper_keys_h = ukeys;
+    h.upper_sign_h = usign;
+    h.nodes_checked = false;
+    h.upload_upper_root();
+    h.rebuild_nbr();
+    h.sync();
+}
+
+void download(gbls_handle& h, gbls_grid_desc* d) {
+    const int64_t L = h.nleaf;
+    if (d->leaf_count != L || d->lower_count != int64_t(h.lower_keys_h.size()) ||
+        d->upper_count != int64_t(h.upper_keys_h.size()) || d->root_tile_count != int64_t(h.root_keys_h.size()))
+        fail(GBLS_ERR_INVALID_ARGUMENT, "descriptor counts do not match gbls_get_counts");
+    d->voxel_size = h.voxel_size;
+    for (int i = 0; i < 3; ++i) d->translation[i] = h.translation[i];
+    d->map_type = h.map_type;
+    d->background = h.gamma;
+    const float g = h.gamma;
+    std::vector<uint64_t> keys(static_cast<size_t>(L));
+    std::vector<int32_t> slots(static_cast<size_t>(L));
+    h.keys[h.kc].download(keys.data(), size_t(L), h.stream);
+    h.slot[h.kc].download(slots.data(), size_t(L), h.stream);
+    h.sync();
+    if (L > 0) {
+        DevArray<float> dense;
+        dense.reserve(size_t(L) * LEAF_VOX, h.stream);
+        k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S(), h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, g,
+                                                     dense.p);
+        CU(cudaGetLastError());
+        dense.download(d->leaf_values, size_t(L) * LEAF_VOX, h.stream);
+        std::vector<uint64_t> am(size_t(h.slot_cap) * 8);
+        h.am[h.mc].download(am.data(), am.size(), h.stream);
+        h.sync();
+        for (int64_t i = 0; i < L; ++i) {
+            int32_t x, y, z;
+            key_origin(keys[size_t(i)], x, y, z);
+            d->leaf_origins[3 * i] = x;
+            d->leaf_origins[3 * i + 1] = y;
+            d->leaf_origins[3 * i + 2] = z;
+            for (int w = 0; w < 8; ++w) d->leaf_masks[8 * i + w] = am[size_t(slots[size_t(i)]) * 8 + w];
+        }
+    }
+    const size_t nl = h.lower_keys_h.size();
+    std::vector<uint64_t> lsign(nl * 64);
+    h.lower_sign.download(lsign.data(), lsign.size(), h.stream);
+    h.sync();
+    for (size_t i = 0; i < nl; ++i) {
+        int32_t x, y, z;
+        key_origin(h.lower_keys_h[i] << 12, x, y, z);
+        d->lower_origins[3 * i] = x;
+        d->lower_origins[3 * i + 1] = y;
+        d->lower_origins[3 * i + 2] = z;
+        float* t = d->lower_tiles + i * LOWER_SLOTS;
+        for (int n = 0; n < LOWER_SLOTS; ++n) {
+            const uint64_t k = (h.lower_keys_h[i] << 12) | uint64_t(n);
+            if (std::binary_search(keys.begin(), keys.end(), k)) { t[n] = 0.0f; continue; }
+            t[n] = ((lsign[i * 64 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
+        }
+    }
+    for (size_t i = 0; i < h.upper_keys_h.size(); ++i) {
+        int32_t x, y, z;
+        key_origin(h.upper_keys_h[i] << 27, x, y, z);
+        d->upper_origins[3 * i] = x;
+        d->upper_origins[3 * i + 1] = y;
+        d->upper_origins[3 * i + 2] = z;
+        float* t = d->upper_tiles + i * UPPER_SLOTS;
+        for (int n = 0; n < UPPER_SLOTS; ++n) {
+            const uint64_t k = (h.upper_keys_h[i] << 15) | uint64_t(n);
+            if (std::binary_search(h.lower_keys_h.begin(), h.lower_keys_h.end(), k)) { t[n] = 0.0f; continue; }
+            t[n] = ((h.upper_sign_h[i * 512 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
+        }
+    }
+    for (size_t i = 0; i < h.root_keys_h.size(); ++i) {
+        int32_t x, y, z;
+        key_origin(h.root_keys_h[i] << 27, x, y, z);
+        d->root_tile_origins[3 * i] = x;
+        d->root_tile_origins[3 * i + 1] = y;
+        d->root_tile_origins[3 * i + 2] = z;
+        d->root_tile_values[i] = h.root_sign_h[i] ? -g : g;
+    }
+}
+
+int64_t active_count(gbls_handle& h) {
+    if (h.nleaf == 0) return 0;
+    h.u64s.reserve(1, h.stream);
+    CU(cudaMemsetAsync(h.u64s.p, 0, sizeof(unsigned long long), h.stream));
+    k_count_active<<<blocks_for(h.nleaf * 8, 256), 256, 0, h.stream>>>(h.nleaf, h.S(), h.am[h.mc].p, h.u64s.p);
+    CU(cudaGetLastError());
+    unsigned long long n = 0;
+    CU(cudaMemcpyAsync(&n, h.u64s.p, sizeof(n), cudaMemcpyDeviceToHost, h.stream));
+    h.sync();
+    return int64_t(n);
+}
+
+struct DeviceGuard {
+    int prev = 0;
+    explicit DeviceGuard(int dev) {
+        CU(cudaGetDevice(&prev));
+        if (prev != dev) CU(cudaSetDevice(dev));
+    }
+    ~DeviceGuard() { cudaSetDevice(prev); }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int gbls_abi_version(void) { return GBLS_ABI_VERSION; }
+
+const char* gbls_last_error(void) { return g_last_error.c_str(); }
+
+int gbls_set_device(int device) {
+    return guarded([&] {
+        int n = 0;
+        CU(cudaGetDeviceCount(&n));
+        if (device < 0 || device >= n) fail(GBLS_ERR_INVALID_ARGUMENT, "no such CUDA device");
+        g_device = device;
+    });
+}
+
+int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
+    if (!desc || !out) {
+        g_last_error = "null argument";
+        return GBLS_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    gbls_handle* h = nullptr;
+    const int rc = guarded([&] {
+        DeviceGuard g(g_device);
+        h = new gbls_handle;
+        h->device = g_device;
+        CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
+        CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
+        upload(*h, desc);
+    });
+    if (rc != GBLS_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBLS_OK;
+}
+
+int gbls_destroy(gbls_handle* h) {
+    if (!h) return GBLS_OK;
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        cudaStreamSynchronize(h->stream);
+        delete h;
+    });
+}
+
+int gbls_get_counts(gbls_handle* h, gbls_grid_counts* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        out->leaf_count = h->nleaf;
+        out->lower_count = int64_t(h->lower_keys_h.size());
+        out->upper_count = int64_t(h->upper_keys_h.size());
+        out->root_tile_count = int64_t(h->root_keys_h.size());
+        out->active_voxel_count = active_count(*h);
+    });
+}
+
+int gbls_download(gbls_handle* h, gbls_grid_desc* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        download(*h, out);
+    });
+}
+
+int gbls_set_stream(gbls_handle* h, void* stream) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        CU(cudaStreamSynchronize(h->stream));
+        h->stream = static_cast<cudaStream_t>(stream);
+    });
+}
+
+int gbls_set_tracker_state(gbls_handle* h, int spatial, int temporal, int norm_count, int grain_size) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        if (spatial < GBLS_FIRST_BIAS || spatial > GBLS_HJWENO5_BIAS) fail(GBLS_ERR_VALUE, "Spatial difference scheme not supported!");
+        if (temporal < GBLS_TVD_RK1 || temporal > GBLS_TVD_RK3) fail(GBLS_ERR_VALUE, "Temporal integration scheme not supported!");
+        h->tr_spatial = spatial;
+        h->tr_temporal = temporal;
+        h->norm_count = norm_count;
+        h->grain = grain_size;
+    });
+}
+
+int gbls_get_tracker_state(gbls_handle* h, int* spatial, int* temporal, int* norm_count, int* grain_size) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (spatial) *spatial = h->tr_spatial;
+    if (temporal) *temporal = h->tr_temporal;
+    if (norm_count) *norm_count = h->norm_count;
+    if (grain_size) *grain_size = h->grain;
+    return GBLS_OK;
+}
+
+int gbls_set_trimming(gbls_handle* h, int trim_mode) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (trim_mode < GBLS_TRIM_NONE || trim_mode > GBLS_TRIM_ALL) {
+        g_last_error = "bad trim mode";
+        return GBLS_ERR_VALUE;
+    }
+    h->trim = trim_mode;
+    return GBLS_OK;
+}
+
+int gbls_set_precision(gbls_handle* h, int mode) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (mode != GBLS_MODE_PARITY && mode != GBLS_MODE_FAST) {
+        g_last_error = "bad precision mode";
+        return GBLS_ERR_VALUE;
+    }
+    h->mode = mode;
+    return GBLS_OK;
+}
+
+int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (intr) {
+        h->intr = *intr;
+        h->has_intr = true;
+    } else {
+        h->intr = gbls_interrupter{};
+        h->has_intr = false;
+    }
+    return GBLS_OK;
+}
+
+int gbls_track(gbls_handle* h) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        track(*h);
+        h->sync();
+    });
+}
+
+int gbls_normalize(gbls_handle* h) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        normalize_pass(*h, h->am[h->mc].p, 0);
+        h->sync();
+    });
+}
+
+int gbls_prune(gbls_handle* h) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        start_intr(*h, "Pruning Level Set");
+        if (h->nleaf > 0) {
+            // Trim (or a plain copy that records per-leaf counts)
+            NormArgs a{};
+            a.nleaf = h->nleaf;
+            a.slot = h->S();
+            a.nbr = h->nbr.p;
+            a.src = h->layout(h->mc, h->vc);
+            a.pmask = h->am[h->mc].p;
+            a.copy_only = 1;
+            a.trim = h->trim;
+            a.gamma = h->gamma;
+            a.out_count = h->cnt.p;
+            const int mo = other_of(h->mc, h->mc), vo = other_of(h->vc, h->vc);
+            a.out_vals = h->vals[vo].p;
+            a.out_amask = h->am[mo].p;
+            a.out_smask = h->sm[mo].p;
+            launch_norm(*h, a);
+            h->mc = mo;
+            h->vc = vo;
+        }
+        prune_compact(*h);
+        end_intr(*h);
+        h->sync();
+    });
+}
+
+int gbls_dilate(gbls_handle* h, int iterations) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        for (int i = 0; i < iterations; ++i) {
+            dilate_topology(*h);
+            if (h->nleaf == 0) break;
+            NormArgs a{};
+            a.nleaf = h->nleaf;
+            a.slot = h->S();
+            a.nbr = h->nbr.p;
+            a.src = h->layout(h->mc, h->vc);
+            a.pmask = h->dmask.p;
+            a.copy_only = 1;
+            a.gamma = h->gamma;
+            a.out_count = h->cnt.p;
+            const int mo = other_of(h->mc, h->mc), vo = other_of(h->vc, h->vc);
+            a.out_vals = h->vals[vo].p;
+            a.out_amask = h->am[mo].p;
+            a.out_smask = h->sm[mo].p;
+            launch_norm(*h, a);
+            h->mc = mo;
+            h->vc = vo;
+        }
+        h->sync();
+    });
+}
+
+int gbls_erode(gbls_handle* h, int iterations) {
+    (void)iterations;
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    g_last_error = "erode is not implemented on the device path";
+    return GBLS_ERR_UNSUPPORTED;
+}
+
+int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
+    (void)half_width;
+    if (changed) *changed = 0;
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    g_last_error = "resize is not implemented on the device path";
+    return GBLS_ERR_UNSUPPORTED;
+}
+
+int gbls_field_create(const gbls_field_desc* desc, gbls_field** out) {
+    if (!desc || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    *out = nullptr;
+    gbls_field* f = nullptr;
+    const int rc = guarded([&] {
+        if (desc->kind < GBLS_FIELD_CONSTANT || desc->kind > GBLS_FIELD_ROTATION)
+            fail(GBLS_ERR_VALUE, "unknown field kind");
+        DeviceGuard g(g_device);
+        f = new gbls_field;
+        f->desc = *desc;
+        f->device = g_device;
+        if (desc->kind == GBLS_FIELD_DENSE) {
+            const int64_t n = int64_t(desc->dense_dims[0]) * desc->dense_dims[1] * desc->dense_dims[2];
+            if (n <= 0 || !desc->dense_values) fail(GBLS_ERR_INVALID_ARGUMENT, "empty dense field");
+            f->dense.upload(desc->dense_values, size_t(n) * 3, nullptr);
+            CU(cudaStreamSynchronize(nullptr));
+        }
+        f->desc.dense_values = nullptr;
+        if (desc->kind == GBLS_FIELD_DEFORMATION && !(desc->domain > 0.0f && desc->period != 0.0f))
+            fail(GBLS_ERR_VALUE, "deformation field needs domain > 0 and period != 0");
+    });
+    if (rc != GBLS_OK) {
+        delete f;
+        return rc;
+    }
+    *out = f;
+    return GBLS_OK;
+}
+
+int gbls_field_destroy(gbls_field* f) {
+    if (!f) return GBLS_OK;
+    return guarded([&] {
+        DeviceGuard g(f->device);
+        delete f;
+    });
+}
+
+int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int temporal, float t0, float t1,
+                float cfl, uint64_t* substeps) {
+    if (substeps) *substeps = 0;
+    if (!h || !field) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    uint64_t count = 0;
+    bool interrupted = false;
+    const int rc = guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(spatial, temporal);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        if (t0 - t1 == 0.0f) return;  // math::isZero(time0 - time1)
+        const bool forward = t0 < t1;
+        const float dx = float(h->voxel_size);
+        const float cfl_ref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) /
+                              std::sqrt(3.0f);
+        const float C = cfl > 0.0f ? cfl : cfl_ref;
+        while (forward ? t0 < t1 : t0 > t1) {
+            if (!check_intr(*h)) { interrupted = true; break; }
+            if (h->nleaf == 0) break;  // sampleField returns 0 for an empty grid
+            start_intr(*h, "Sampling advection field");
+            const float maxv2 = max_speed_sqr(*h, field, t0);
+            end_intr(*h);
+            if (!(maxv2 > 1e-5f) && !(maxv2 < -1e-5f)) break;  // isApproxZero(maxAbsV, Delta)
+            const float span = std::fabs(t1 - t0);
+            const float lim = C * dx / std::sqrt(maxv2);
+            const float dt = (lim < span) ? lim : span;  // math::Min
+            if (dt == 0.0f) break;
+            advect_stages(*h, field, temporal, t0, dt, !forward);
+            t0 += forward ? dt : -dt;
+            ++count;
+            track(*h);
+        }
+        h->sync();
+    });
+    if (substeps) *substeps = count;
+    if (rc == GBLS_OK && interrupted) {
+        g_last_error = "interrupted";
+        return GBLS_ERR_INTERRUPTED;
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,18 @@
+// Host launchers of the stencil kernels (one set per arithmetic policy).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace gbls {
+struct RkArgs;
+struct NormArgs;
+struct CflArgs;
+
+// Bit-faithful to the reference arithmetic (FP64 WENO weights).
+void launch_rk_parity(const RkArgs& a, cudaStream_t s);
+void launch_norm_parity(const NormArgs& a, cudaStream_t s);
+// FP32 arithmetic.
+void launch_rk_fast(const RkArgs& a, cudaStream_t s);
+void launch_norm_fast(const NormArgs& a, cudaStream_t s);
+// Max |v|^2 over active voxels (exact in both modes).
+void launch_cfl(const CflArgs& a, cudaStream_t s);
+}  // namespace gbls

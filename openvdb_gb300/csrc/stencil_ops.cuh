@@ -1,0 +1,376 @@
+// Stencil arithmetic and the per-leaf kernels of the advection hot path.
+//
+// Included by two translation units with different arithmetic policies:
+//   stencil_parity.cu  ParityArith: every operation of the reference,
+//                      in its order and its types (FP64 WENO weights), with
+//                      explicit round-to-nearest intrinsics so no operation
+//                      can be contracted or reassociated.  Bit-identical to
+//                      the reference CPU path compiled without contraction.
+//   stencil_fast.cu    FastArith: FP32 throughout, contracted, one division
+//                      per WENO5.
+#pragma once
+
+#include "gbls_internal.cuh"
+#include "../../include/gbls_fields.h"
+
+namespace gbls {
+
+// ---- arithmetic policies ---------------------------------------------------
+
+struct ParityArith {
+    static constexpr bool kParity = true;
+    __device__ __forceinline__ static float add(float a, float b) { return __fadd_rn(a, b); }
+    __device__ __forceinline__ static float sub(float a, float b) { return __fsub_rn(a, b); }
+    __device__ __forceinline__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+    __device__ __forceinline__ static float div(float a, float b) { return __fdiv_rn(a, b); }
+    __device__ __forceinline__ static float sqrt(float a) { return __fsqrt_rn(a); }
+
+    // math::WENO5<float> (math/FiniteDifference.h:301-321), scale2 = 0.01f.
+    // Types follow the C++ expression: `2*v2`, `4*v2`, Pow2 of a float are
+    // float; anything multiplied by a double literal or by C is double.
+    __device__ static float weno5(float v1, float v2, float v3, float v4, float v5) {
+        const double C = 13.0 / 12.0;
+        const double eps = 1.0e-6 * static_cast<double>(0.01f);
+        // A1 = 0.1/Pow2(C*Pow2(v1-2*v2+v3) + 0.25*Pow2(v1-4*v2+3.0*v3) + eps)
+        const float t1 = __fadd_rn(__fsub_rn(v1, __fmul_rn(2.0f, v2)), v3);
+        const double s1a = __dmul_rn(C, double(__fmul_rn(t1, t1)));
+        const double u1 = __dadd_rn(double(__fsub_rn(v1, __fmul_rn(4.0f, v2))), __dmul_rn(3.0, double(v3)));
+        const double s1b = __dmul_rn(0.25, __dmul_rn(u1, u1));
+        const double d1 = __dadd_rn(__dadd_rn(s1a, s1b), eps);
+        const double A1 = __ddiv_rn(0.1, __dmul_rn(d1, d1));
+        // A2 = 0.6/Pow2(C*Pow2(v2-2*v3+v4) + 0.25*Pow2(v2-v4) + eps)
+        const float t2 = __fadd_rn(__fsub_rn(v2, __fmul_rn(2.0f, v3)), v4);
+        const double s2a = __dmul_rn(C, double(__fmul_rn(t2, t2)));
+        const float u2 = __fsub_rn(v2, v4);
+        const double s2b = __dmul_rn(0.25, double(__fmul_rn(u2, u2)));
+        const double d2 = __dadd_rn(__dadd_rn(s2a, s2b), eps);
+        const double A2 = __ddiv_rn(0.6, __dmul_rn(d2, d2));
+        // A3 = 0.3/Pow2(C*Pow2(v3-2*v4+v5) + 0.25*Pow2(3.0*v3-4*v4+v5) + eps)
+        const float t3 = __fadd_rn(__fsub_rn(v3, __fmul_rn(2.0f, v4)), v5);
+        const double s3a = __dmul_rn(C, double(__fmul_rn(t3, t3)));
+        const double u3 = __dadd_rn(__dsub_rn(__dmul_rn(3.0, double(v3)), double(__fmul_rn(4.0f, v4))),
+                                    double(v5));
+        const double s3b = __dmul_rn(0.25, __dmul_rn(u3, u3));
+        const double d3 = __dadd_rn(__dadd_rn(s3a, s3b), eps);
+        const double A3 = __ddiv_rn(0.3, __dmul_rn(d3, d3));
+        // A1*(2v1-7v2+11v3) + A2*(5v3-v2+2v4) + A3*(2v3+5v4-v5)
+        const double p1 = __dadd_rn(__dsub_rn(__dmul_rn(2.0, double(v1)), __dmul_rn(7.0, double(v2))),
+                                    __dmul_rn(11.0, double(v3)));
+        const double p2 = __dadd_rn(__dsub_rn(__dmul_rn(5.0, double(v3)), double(v2)),
+                                    __dmul_rn(2.0, double(v4)));
+        const double p3 = __dsub_rn(__dadd_rn(__dmul_rn(2.0, double(v3)), __dmul_rn(5.0, double(v4))),
+                                    double(v5));
+        const double num = __dadd_rn(__dadd_rn(__dmul_rn(A1, p1), __dmul_rn(A2, p2)), __dmul_rn(A3, p3));
+        const double den = __dmul_rn(6.0, __dadd_rn(__dadd_rn(A1, A2), A3));
+        return __double2float_rn(__ddiv_rn(double(__double2float_rn(num)), den));
+    }
+
+    // Vec3d(iGradient) -> map.applyIJT (x 1/dx in double) -> Vec3f
+    // (math/Operators.h:838-845, math/Maps.h:767-771).
+    __device__ __forceinline__ static float ijt(float g, double invdx) {
+        return __double2float_rn(__dmul_rn(double(g), invdx));
+    }
+};
+
+struct FastArith {
+    static constexpr bool kParity = false;
+    __device__ __forceinline__ static float add(float a, float b) { return a + b; }
+    __device__ __forceinline__ static float sub(float a, float b) { return a - b; }
+    __device__ __forceinline__ static float mul(float a, float b) { return a * b; }
+    __device__ __forceinline__ static float div(float a, float b) { return __fdividef(a, b); }
+    __device__ __forceinline__ static float sqrt(float a) { return sqrtf(a); }
+
+    // Shu's WENO5 in FP32.  The three weights share one reciprocal:
+    // w_k = c_k / d_k^2 are scaled by d1^2 d2^2 d3^2 (d_k >= eps = 1e-8, so
+    // the products stay above 1e-32, far from FP32 underflow).
+    __device__ __forceinline__ static float weno5(float v1, float v2, float v3, float v4, float v5) {
+        const float C = 13.0f / 12.0f;
+        const float eps = 1.0e-8f;
+        const float t1 = v1 - 2.0f * v2 + v3, u1 = v1 - 4.0f * v2 + 3.0f * v3;
+        const float t2 = v2 - 2.0f * v3 + v4, u2 = v2 - v4;
+        const float t3 = v3 - 2.0f * v4 + v5, u3 = 3.0f * v3 - 4.0f * v4 + v5;
+        const float d1 = C * t1 * t1 + 0.25f * u1 * u1 + eps;
+        const float d2 = C * t2 * t2 + 0.25f * u2 * u2 + eps;
+        const float d3 = C * t3 * t3 + 0.25f * u3 * u3 + eps;
+        const float q1 = d1 * d1, q2 = d2 * d2, q3 = d3 * d3;
+        const float A1 = 0.1f * (q2 * q3), A2 = 0.6f * (q1 * q3), A3 = 0.3f * (q1 * q2);
+        const float p1 = 2.0f * v1 - 7.0f * v2 + 11.0f * v3;
+        const float p2 = 5.0f * v3 - v2 + 2.0f * v4;
+        const float p3 = 2.0f * v3 + 5.0f * v4 - v5;
+        const float num = A1 * p1 + A2 * p2 + A3 * p3;
+        const float den = 6.0f * (A1 + A2 + A3);
+        return __fdividef(num, den);
+    }
+
+    __device__ __forceinline__ static float ijt(float g, double invdx) { return g * float(invdx); }
+};
+
+// ---- HJ-WENO5 one-sided derivatives on the staged tile --------------------
+// D1<FD_HJWENO5> (math/FiniteDifference.h:1177-1274):
+//   WENO5(S3-S2, S2-S1, S1-S0, S0-Sm1, Sm1-Sm2)
+// D1<BD_HJWENO5> (:1381-1389 and its stencil form):
+//   -WENO5(Sm3-Sm2, Sm2-Sm1, Sm1-S0, S0-S1, S1-S2)
+template <class A>
+__device__ __forceinline__ float hj_fd(float m2, float m1, float c, float p1, float p2, float p3) {
+    return A::weno5(A::sub(p3, p2), A::sub(p2, p1), A::sub(p1, c), A::sub(c, m1), A::sub(m1, m2));
+}
+template <class A>
+__device__ __forceinline__ float hj_bd(float m3, float m2, float m1, float c, float p1, float p2) {
+    return -A::weno5(A::sub(m3, m2), A::sub(m2, m1), A::sub(m1, c), A::sub(c, p1), A::sub(p1, p2));
+}
+
+// The seven values along one axis around the centre, S(-3..3).
+struct Line7 {
+    float v[7];
+};
+
+__device__ __forceinline__ Line7 tile_line(const float* tile, int x, int y, int z, int axis) {
+    Line7 L;
+    const int stride = axis == 0 ? TILE_DIM * TILE_DIM : axis == 1 ? TILE_DIM : 1;
+    const int c = tile_index(x, y, z);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) L.v[k] = tile[c + (k - 3) * stride];
+    return L;
+}
+
+template <class A>
+__device__ __forceinline__ float line_fd(const Line7& L) {
+    return hj_fd<A>(L.v[1], L.v[2], L.v[3], L.v[4], L.v[5], L.v[6]);
+}
+template <class A>
+__device__ __forceinline__ float line_bd(const Line7& L) {
+    return hj_bd<A>(L.v[0], L.v[1], L.v[2], L.v[3], L.v[4], L.v[5]);
+}
+
+// std::max / std::min as used by math::Max / math::Min.
+__device__ __forceinline__ float ref_max(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float ref_min(float a, float b) { return (b < a) ? b : a; }
+
+// math::GodunovsNormSqrd (math/FiniteDifference.h:324-357) with
+// gradient_m = BD ("down"), gradient_p = FD ("up").
+template <class A>
+__device__ __forceinline__ float godunov(bool outside, const float* dm, const float* dp) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float term;
+        if (outside) {
+            const float a = ref_max(dm[k], 0.0f), b = ref_min(dp[k], 0.0f);
+            term = ref_max(A::mul(a, a), A::mul(b, b));
+        } else {
+            const float a = ref_min(dm[k], 0.0f), b = ref_max(dp[k], 0.0f);
+            term = ref_max(A::mul(a, a), A::mul(b, b));
+        }
+        acc = (k == 0) ? term : A::add(acc, term);
+    }
+    return acc;
+}
+
+// ---- velocity --------------------------------------------------------------
+__device__ __forceinline__ void eval_field(const FieldParams& f, int i, int j, int k, float t,
+                                           float out[3]) {
+    switch (f.kind) {
+    case 0:  // GBLS_FIELD_CONSTANT
+        out[0] = f.constant[0]; out[1] = f.constant[1]; out[2] = f.constant[2];
+        break;
+    case 1: {  // GBLS_FIELD_DENSE: aligned DiscreteField lookup
+        const int a = i - f.dense_origin[0], b = j - f.dense_origin[1], c = k - f.dense_origin[2];
+        if (a >= 0 && b >= 0 && c >= 0 && a < f.dense_dims[0] && b < f.dense_dims[1] && c < f.dense_dims[2]) {
+            const float* p = f.dense + 3 * ((size_t(a) * f.dense_dims[1] + b) * f.dense_dims[2] + c);
+            out[0] = __ldg(p); out[1] = __ldg(p + 1); out[2] = __ldg(p + 2);
+        } else {
+            out[0] = f.dense_background[0]; out[1] = f.dense_background[1]; out[2] = f.dense_background[2];
+        }
+        break;
+    }
+    case 2:  // GBLS_FIELD_DEFORMATION
+        gbls_deformation(i, j, k, t, f.domain, f.period, f.scale, out);
+        break;
+    default:  // GBLS_FIELD_ROTATION
+        gbls_rotation(i, j, k, f.constant, f.omega, f.center, out);
+        break;
+    }
+}
+
+// ---- kernel arguments -------------------------------------------------------
+struct RkArgs {
+    int64_t nleaf;
+    const uint64_t* keys;
+    const int32_t* slot;
+    const int32_t* nbr;
+    Layout src;            // stencil buffer (masks of the current active set)
+    const float* phin;     // buffer of the convex combination (same layout)
+    float* out;            // result buffer (same layout)
+    float dt, alpha, beta, gamma, t0;
+    int has_phi;           // Nominator != 0
+    int backward;          // velocity negated (t0 > t1)
+    double invdx;
+    FieldParams field;
+};
+
+struct NormArgs {
+    int64_t nleaf;
+    const int32_t* slot;
+    const int32_t* nbr;
+    Layout src;             // stencil buffer and its layout
+    Layout phi;             // convex-combination buffer and its layout
+    const uint64_t* pmask;  // [slots*8] voxels to update
+    float* out_vals;
+    uint64_t* out_amask;
+    uint64_t* out_smask;
+    int32_t* out_count;     // [nleaf] active voxels after the pass
+    float alpha, beta, gamma, mdt, invdx;
+    int has_phi;
+    int trim;               // TrimMode bits: 1 interior, 2 exterior
+    int copy_only;          // 1: value = staged value (relayout / trim only)
+};
+
+struct CflArgs {
+    int64_t nleaf;
+    const uint64_t* keys;
+    const int32_t* slot;
+    const uint64_t* amask;
+    float t0;
+    FieldParams field;
+    unsigned int* max_bits;  // float bits of max |v|^2 (values >= 0)
+};
+
+// ---- kernels ----------------------------------------------------------------
+constexpr int STENCIL_THREADS = 128;
+
+// One TVD-RK stage of LevelSetAdvection::Advect::euler<N,D>
+// (tools/LevelSetAdvect.h:543-572): for every active voxel
+//   a = phi_c - dt * (v . GradientBiased<HJWENO5>(phi))
+//   out = N ? alpha*phin + beta*a : a
+template <class A>
+__global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs a) {
+    __shared__ float tile[TILE_VOX];
+    __shared__ LeafStage st;
+    const int64_t l = blockIdx.x;
+    if (l >= a.nleaf) return;
+    const int s = a.slot[l];
+    stage_masks(st, a.src, s, a.nbr + 6 * l);
+    load_tile(tile, st, a.src.vals, a.gamma);
+    __syncthreads();
+    int ox, oy, oz;
+    key_origin(a.keys[l], ox, oy, oz);
+    const int n = st.pre[0][8];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int v = select_voxel(st.am[0], st.pre[0], i);
+        const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+        float vel[3];
+        eval_field(a.field, ox + x, oy + y, oz + z, a.t0, vel);
+        if (a.backward) { vel[0] = -vel[0]; vel[1] = -vel[1]; vel[2] = -vel[2]; }
+        float g[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const Line7 L = tile_line(tile, x, y, z, ax);
+            g[ax] = A::ijt(vel[ax] < 0.0f ? line_fd<A>(L) : line_bd<A>(L), a.invdx);
+        }
+        const float dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
+        const float c = tile[tile_index(x, y, z)];
+        const float r = A::sub(c, A::mul(a.dt, dot));
+        float o = r;
+        if (a.has_phi) {
+            const float p = a.phin[size_t(s) * LEAF_VOX + i];
+            o = A::add(A::mul(a.alpha, p), A::mul(a.beta, r));
+        }
+        a.out[size_t(s) * LEAF_VOX + i] = o;
+    }
+}
+
+// One stage of LevelSetTracker::Normalizer::euler<N,D>
+// (tools/LevelSetTracker.h:623-676) over the voxels of pmask, optionally
+// followed by Trim (tools/LevelSetTracker.h:473-506), writing the result in
+// the layout of the surviving active set.
+template <class A>
+__global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormArgs a) {
+    __shared__ float tile[TILE_VOX];
+    __shared__ LeafStage st;
+    __shared__ float res[LEAF_VOX];
+    __shared__ uint64_t pm[8], fin[8], fsg[8], phm[8];
+    __shared__ int ppre[9], fpre[9], phpre[9];
+    const int64_t l = blockIdx.x;
+    if (l >= a.nleaf) return;
+    const int s = a.slot[l];
+    const int t = threadIdx.x;
+    stage_masks(st, a.src, s, a.nbr + 6 * l);
+    load_tile(tile, st, a.src.vals, a.gamma);
+    if (t < 8) {
+        pm[t] = a.pmask[size_t(s) * 8 + t];
+        fin[t] = 0;
+        fsg[t] = st.sm[0][t] & ~pm[t];
+        if (a.has_phi) phm[t] = a.phi.amask[size_t(s) * 8 + t];
+    }
+    __syncthreads();
+    if (t == 0) {
+        int acc = 0, acc2 = 0;
+        for (int w = 0; w < 8; ++w) {
+            ppre[w] = acc; acc += popc64(pm[w]);
+            phpre[w] = acc2; if (a.has_phi) acc2 += popc64(phm[w]);
+        }
+        ppre[8] = acc; phpre[8] = acc2;
+    }
+    __syncthreads();
+    const int n = ppre[8];
+    const float g = a.gamma;
+    for (int i = t; i < n; i += blockDim.x) {
+        const int v = select_voxel(pm, ppre, i);
+        const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+        const float phi0 = tile[tile_index(x, y, z)];
+        float val = phi0;
+        if (!a.copy_only) {
+            float up[3], down[3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const Line7 L = tile_line(tile, x, y, z, ax);
+                up[ax] = line_fd<A>(L);
+                down[ax] = line_bd<A>(L);
+            }
+            const float nsq = godunov<A>(phi0 > 0.0f, down, up);
+            float vv = A::div(phi0, A::add(A::sqrt(A::add(A::mul(phi0, phi0), nsq)), 1e-8f));
+            vv = A::sub(phi0, A::mul(A::mul(a.mdt, vv), A::sub(A::mul(A::sqrt(nsq), a.invdx), 1.0f)));
+            if (a.has_phi) {
+                const int w = v >> 6, b = v & 63;
+                float p;
+                if ((phm[w] >> b) & 1) {
+                    p = a.phi.vals[size_t(s) * LEAF_VOX + phpre[w] + popc64(phm[w] & ((uint64_t(1) << b) - 1))];
+                } else {
+                    p = ((a.phi.smask[size_t(s) * 8 + w] >> b) & 1) ? -g : g;
+                }
+                vv = A::add(A::mul(a.alpha, p), A::mul(a.beta, vv));
+            }
+            val = vv;
+        }
+        bool act = true, neg = val < 0.0f;
+        if ((a.trim & 1) && val <= -g) { act = false; neg = true; val = -g; }
+        else if ((a.trim & 2) && val >= g) { act = false; neg = false; val = g; }
+        res[v] = val;
+        const uint64_t bit = uint64_t(1) << (v & 63);
+        if (act) atomicOr(reinterpret_cast<unsigned long long*>(&fin[v >> 6]), (unsigned long long)bit);
+        if (neg) atomicOr(reinterpret_cast<unsigned long long*>(&fsg[v >> 6]), (unsigned long long)bit);
+    }
+    __syncthreads();
+    if (t == 0) {
+        int acc = 0;
+        for (int w = 0; w < 8; ++w) { fpre[w] = acc; acc += popc64(fin[w]); }
+        fpre[8] = acc;
+    }
+    __syncthreads();
+    const int nf = fpre[8];
+    for (int i = t; i < nf; i += blockDim.x) {
+        const int v = select_voxel(fin, fpre, i);
+        a.out_vals[size_t(s) * LEAF_VOX + i] = res[v];
+    }
+    if (t < 8) {
+        a.out_amask[size_t(s) * 8 + t] = fin[t];
+        a.out_smask[size_t(s) * 8 + t] = fsg[t];
+    }
+    if (t == 0 && a.out_count) a.out_count[l] = nf;
+}
+
+// Max of |v|^2 over the active voxels (LevelSetAdvection::Advect::sampleField,
+// tools/LevelSetAdvect.h:447-455): Vec3f::lengthSqr in float, no contraction.
+__global__ void cfl_max_kernel(const CflArgs a);
+
+}  // namespace gbls

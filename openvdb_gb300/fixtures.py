@@ -1,0 +1,70 @@
+"""Level-set fixtures built by the native host code (gbls_host_*).
+
+sphere() equals tools::createLevelSetSphere (tools/LevelSetSphere.h:219-230)
+voxel for voxel; union_of_spheres() rasterises a union of spheres directly.
+The workload generators below produce the seeded inputs of the benchmark
+configurations.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._lib import check, lib
+from .grid import HostGrid
+
+
+def _from_native(handle):
+    d = _abi.GridDesc()
+    L = lib()
+    try:
+        check(L.gbls_host_grid_view(handle, C.byref(d)), host=True)
+
+        def arr(ptr, n, shape, dtype):
+            if n == 0:
+                return np.zeros((0,) + shape, dtype)
+            ct = np.ctypeslib.as_array(ptr, shape=(n * int(np.prod(shape)),))
+            return np.array(ct, dtype=dtype).reshape((n,) + shape)
+
+        g = HostGrid(
+            voxel_size=d.voxel_size, background=d.background, map_type=d.map_type,
+            leaf_origins=arr(d.leaf_origins, d.leaf_count, (3,), np.int32),
+            leaf_masks=arr(d.leaf_masks, d.leaf_count, (8,), np.uint64),
+            leaf_values=arr(d.leaf_values, d.leaf_count, (512,), np.float32),
+            lower_origins=arr(d.lower_origins, d.lower_count, (3,), np.int32),
+            lower_tiles=arr(d.lower_tiles, d.lower_count, (4096,), np.float32),
+            upper_origins=arr(d.upper_origins, d.upper_count, (3,), np.int32),
+            upper_tiles=arr(d.upper_tiles, d.upper_count, (32768,), np.float32),
+            root_tile_origins=arr(d.root_tile_origins, d.root_tile_count, (3,), np.int32),
+            root_tile_values=arr(d.root_tile_values, d.root_tile_count, (), np.float32),
+        )
+    finally:
+        L.gbls_host_grid_free(handle)
+    return g
+
+
+def sphere(radius, center=(0.0, 0.0, 0.0), voxel_size=1.0, half_width=3.0):
+    """createLevelSetSphere<FloatGrid>(radius, center, voxel_size, half_width)."""
+    h = C.c_void_p()
+    c = (C.c_float * 3)(*center)
+    check(lib().gbls_host_sphere(radius, c, voxel_size, half_width, C.byref(h)), host=True)
+    return _from_native(h)
+
+
+def union_of_spheres(centers, radii, voxel_size=1.0, half_width=3.0):
+    c = np.ascontiguousarray(centers, np.float32).reshape(-1)
+    r = np.ascontiguousarray(radii, np.float32).reshape(-1)
+    h = C.c_void_p()
+    check(lib().gbls_host_union_of_spheres(len(r), c.ctypes.data_as(C.POINTER(C.c_float)),
+                                           r.ctypes.data_as(C.POINTER(C.c_float)), voxel_size,
+                                           half_width, C.byref(h)), host=True)
+    return _from_native(h)
+
+
+def sixty_four_spheres(seed=2024, n=64, domain=1024.0, rmin=20.0, rmax=80.0):
+    """Seeded centres U[0,domain]^3 and radii U[rmin,rmax] (cx, cy, cz, r per sphere)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vals = rng.random((n, 4))
+    centers = (vals[:, :3] * domain).astype(np.float32)
+    radii = (rmin + vals[:, 3] * (rmax - rmin)).astype(np.float32)
+    return centers, radii

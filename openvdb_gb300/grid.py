@@ -157,3 +157,33 @@ def bitwise_equal(a, b):
     return (topology_equal(a, b)
             and np.array_equal(a.leaf_values.view(np.uint32), b.leaf_values.view(np.uint32))
             and a.background == b.background and a.voxel_size == b.voxel_size)
+
+
+def digest(g):
+    """SHA-256 over the canonical arrays of a grid (bit-exact fingerprint)."""
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.float32(g.background).tobytes())
+    h.update(np.float64(g.voxel_size).tobytes())
+    for k in ("leaf_origins", "leaf_masks", "leaf_values", "lower_origins", "lower_tiles",
+              "upper_origins", "upper_tiles", "root_tile_origins", "root_tile_values"):
+        a = np.ascontiguousarray(getattr(g, k))
+        h.update(k.encode())
+        h.update(np.int64(a.size).tobytes())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def summary(g):
+    """Small order-independent statistics of a grid (for messages and fixtures)."""
+    act = g.active_values().astype(np.float64)
+    return {
+        "leaves": int(g.leaf_count),
+        "active": int(act.size),
+        "lower": int(len(g.lower_origins)),
+        "upper": int(len(g.upper_origins)),
+        "root_tiles": int(len(g.root_tile_origins)),
+        "sum": float(act.sum()),
+        "sum_abs": float(np.abs(act).sum()),
+        "negative": int((act < 0).sum()),
+    }

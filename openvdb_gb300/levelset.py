@@ -1,0 +1,274 @@
+"""Python mirror of OpenVDB's LevelSetTracker / LevelSetAdvection call surface
+over the C ABI (include/gbls.h).
+
+Reference interfaces:
+  tools/LevelSetTracker.h:56-256  LevelSetTracker (ctor :258-277, setters
+                                  :137-173, track :302-315, normalize :394-446,
+                                  prune :279-300, dilate :317-337)
+  tools/LevelSetAdvect.h:71-213   LevelSetAdvection (ctor defaults :86-89,
+                                  advect :216-289)
+
+The level set lives on the GPU in a DeviceLevelSet; the reference mutates its
+FloatGrid in place, here the DeviceLevelSet is mutated in place and
+to_host() returns the grid in the reference's canonical layout.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._lib import GblsError, check, lib
+from .grid import HostGrid
+
+HJWENO5_BIAS = _abi.HJWENO5_BIAS
+TVD_RK1, TVD_RK2, TVD_RK3 = _abi.TVD_RK1, _abi.TVD_RK2, _abi.TVD_RK3
+PARITY, FAST = _abi.MODE_PARITY, _abi.MODE_FAST
+
+
+class ValueError_(ValueError):
+    """openvdb::ValueError (unsupported scheme or map)."""
+
+
+class RuntimeError_(RuntimeError):
+    """openvdb::RuntimeError (not a level set / non-uniform voxels)."""
+
+
+def _raise(e):
+    if e.code == _abi.ERR_VALUE:
+        raise ValueError_(str(e)) from None
+    if e.code == _abi.ERR_RUNTIME:
+        raise RuntimeError_(str(e)) from None
+    raise e
+
+
+def _call(rc):
+    try:
+        return check(rc)
+    except GblsError as e:
+        _raise(e)
+
+
+class DeviceLevelSet:
+    """A narrow-band FP32 level set resident on the GPU (one gbls_handle)."""
+
+    def __init__(self, grid, device=0):
+        L = lib()
+        _call(L.gbls_set_device(int(device)))
+        self._h = C.c_void_p()
+        self._keep = grid  # the descriptor points into grid's arrays during create
+        d = grid.desc()
+        _call(L.gbls_create(C.byref(d), C.byref(self._h)))
+        self._keep = None
+        self.voxel_size = grid.voxel_size
+        self.background = grid.background
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().gbls_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def counts(self):
+        c = _abi.GridCounts()
+        _call(lib().gbls_get_counts(self._h, C.byref(c)))
+        return c
+
+    def active_voxel_count(self):
+        return self.counts().active_voxel_count
+
+    def leaf_count(self):
+        return self.counts().leaf_count
+
+    def to_host(self):
+        g = HostGrid.allocate(self.counts())
+        d = g.desc()
+        _call(lib().gbls_download(self._h, C.byref(d)))
+        g.copy_scalars_from(d)
+        return g
+
+    def set_precision(self, mode):
+        _call(lib().gbls_set_precision(self._h, int(mode)))
+
+    def set_stream(self, stream_ptr):
+        _call(lib().gbls_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+
+class DeviceField:
+    """A velocity field uploaded to the GPU (gbls_field)."""
+
+    def __init__(self, field):
+        self._h = C.c_void_p()
+        self._field = field
+        d = field.desc()
+        _call(lib().gbls_field_create(C.byref(d), C.byref(self._h)))
+
+    def __del__(self):
+        try:
+            if self._h.value:
+                lib().gbls_field_destroy(self._h)
+        except Exception:
+            pass
+
+
+class LevelSetTracker:
+    """tools::LevelSetTracker<FloatGrid> over a DeviceLevelSet."""
+
+    def __init__(self, grid, interrupter=None):
+        self._grid = grid
+        self._intr_keep = None
+        if interrupter is not None:
+            self.setInterrupter(interrupter)
+
+    # ---- state (tools/LevelSetTracker.h:74-83, :137-173) ----
+    def _state(self):
+        s, t, n, g = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _call(lib().gbls_get_tracker_state(self._grid.handle, C.byref(s), C.byref(t), C.byref(n),
+                                           C.byref(g)))
+        return [s.value, t.value, n.value, g.value]
+
+    def _set(self, i, v):
+        st = self._state()
+        st[i] = int(v)
+        _call(lib().gbls_set_tracker_state(self._grid.handle, *st))
+
+    def getSpatialScheme(self):
+        return self._state()[0]
+
+    def setSpatialScheme(self, s):
+        self._set(0, s)
+
+    def getTemporalScheme(self):
+        return self._state()[1]
+
+    def setTemporalScheme(self, t):
+        self._set(1, t)
+
+    def getNormCount(self):
+        return self._state()[2]
+
+    def setNormCount(self, n):
+        self._set(2, n)
+
+    def getGrainSize(self):
+        return self._state()[3]
+
+    def setGrainSize(self, g):
+        self._set(3, g)
+
+    def setTrimming(self, mode):
+        _call(lib().gbls_set_trimming(self._grid.handle, int(mode)))
+
+    def voxelSize(self):
+        return np.float32(self._grid.voxel_size)
+
+    def getHalfWidth(self):
+        return float(np.float32(self._grid.background) / np.float32(self._grid.voxel_size))
+
+    def grid(self):
+        return self._grid
+
+    def setInterrupter(self, obj):
+        """obj has start(name), end(), wasInterrupted(percent) (util/NullInterrupter.h:29-49)."""
+        start = _abi.INTERRUPT_START(lambda u, name: obj.start(name.decode() if name else ""))
+        end = _abi.INTERRUPT_END(lambda u: obj.end())
+        chk = _abi.INTERRUPT_CHECK(lambda u, p: 1 if obj.wasInterrupted(p) else 0)
+        it = _abi.Interrupter(start, end, chk, None)
+        self._intr_keep = (start, end, chk, it)
+        _call(lib().gbls_set_interrupter(self._grid.handle, C.byref(it)))
+
+    # ---- operations ----
+    def track(self):
+        _call(lib().gbls_track(self._grid.handle))
+
+    def normalize(self):
+        _call(lib().gbls_normalize(self._grid.handle))
+
+    def prune(self):
+        _call(lib().gbls_prune(self._grid.handle))
+
+    def dilate(self, iterations=1):
+        _call(lib().gbls_dilate(self._grid.handle, int(iterations)))
+
+    def erode(self, iterations=1):
+        _call(lib().gbls_erode(self._grid.handle, int(iterations)))
+
+    def resize(self, half_width=3):
+        ch = C.c_int()
+        _call(lib().gbls_resize(self._grid.handle, int(half_width), C.byref(ch)))
+        return bool(ch.value)
+
+
+class LevelSetAdvection:
+    """tools::LevelSetAdvection<FloatGrid, FieldT> over a DeviceLevelSet.
+
+    Defaults follow the reference constructor (tools/LevelSetAdvect.h:86-89):
+    HJWENO5 + TVD_RK2 for advection, and the tracker's HJWENO5 + TVD_RK1 with
+    normCount 3.  `cfl` <= 0 keeps the reference CFL number; `precision`
+    selects PARITY (bit-identical to the reference) or FAST (FP32) kernels.
+    """
+
+    def __init__(self, grid, field, interrupter=None):
+        self._grid = grid
+        self._field = field if isinstance(field, DeviceField) else DeviceField(field)
+        self.tracker = LevelSetTracker(grid, interrupter)
+        self._spatial = HJWENO5_BIAS
+        self._temporal = TVD_RK2
+        self.cfl = 0.0
+
+    def getSpatialScheme(self):
+        return self._spatial
+
+    def setSpatialScheme(self, s):
+        self._spatial = int(s)
+
+    def getTemporalScheme(self):
+        return self._temporal
+
+    def setTemporalScheme(self, t):
+        self._temporal = int(t)
+
+    def getTrackerSpatialScheme(self):
+        return self.tracker.getSpatialScheme()
+
+    def setTrackerSpatialScheme(self, s):
+        self.tracker.setSpatialScheme(s)
+
+    def getTrackerTemporalScheme(self):
+        return self.tracker.getTemporalScheme()
+
+    def setTrackerTemporalScheme(self, t):
+        self.tracker.setTemporalScheme(t)
+
+    def getNormCount(self):
+        return self.tracker.getNormCount()
+
+    def setNormCount(self, n):
+        self.tracker.setNormCount(n)
+
+    def getGrainSize(self):
+        return self.tracker.getGrainSize()
+
+    def setGrainSize(self, g):
+        self.tracker.setGrainSize(g)
+
+    def setPrecision(self, mode):
+        self._grid.set_precision(mode)
+
+    def advect(self, t0, t1):
+        """Advect from t0 to t1; returns the number of CFL substeps."""
+        n = C.c_uint64()
+        rc = lib().gbls_advect(self._grid.handle, self._field._h, self._spatial, self._temporal,
+                               np.float32(t0), np.float32(t1), np.float32(self.cfl), C.byref(n))
+        if rc == _abi.ERR_INTERRUPTED:
+            return n.value
+        _call(rc)
+        return n.value

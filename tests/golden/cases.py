@@ -1,0 +1,133 @@
+"""Parity cases shared by the golden-vector generator and the GPU tests.
+
+Each case builds an input level set, then applies a list of operations:
+  ("advect", t0, t1)            LevelSetAdvection::advect with the case schemes
+  ("track",) ("normalize",) ("prune",) ("dilate", n)
+                                LevelSetTracker operations
+  ("state", {...})              change tracker state (norm_count, tr_temporal, trim)
+The golden file records, after every operation, the SHA-256 digest of the
+grid's canonical arrays (openvdb_gb300.grid.digest) and the substep count.
+"""
+import numpy as np
+
+from openvdb_gb300 import _abi
+from openvdb_gb300.fields import Field
+
+HJ = _abi.HJWENO5_BIAS
+RK1, RK2, RK3 = _abi.TVD_RK1, _abi.TVD_RK2, _abi.TVD_RK3
+
+
+def smoothed_noise(n, sigma, amplitude, seed):
+    """Seeded Gaussian-smoothed noise velocity on an n^3 grid, shape (n,n,n,3)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    v = rng.standard_normal((n, n, n, 3))
+    r = int(3 * sigma)
+    x = np.arange(-r, r + 1)
+    k = np.exp(-0.5 * (x / sigma) ** 2)
+    k /= k.sum()
+    for ax in range(3):
+        v = np.apply_along_axis(lambda a: np.convolve(np.pad(a, r, mode="wrap"), k, "valid"), ax, v)
+    v *= amplitude / np.abs(v).max()
+    return v.astype(np.float32)
+
+
+def union8():
+    rng = np.random.Generator(np.random.PCG64(7))
+    c = (16 + rng.random((8, 3)) * 96).astype(np.float32)
+    r = (8 + rng.random(8) * 12).astype(np.float32)
+    return c, r
+
+
+CASES = {
+    # configuration 1 at the reference CFL: sphere r=64, constant velocity,
+    # HJWENO5 + TVD_RK3, tracker HJWENO5 + TVD_RK1 with one renormalisation
+    "cfg1_sphere64": dict(
+        fixture=("sphere", 64.0, (0.0, 0.0, 0.0), 1.0, 3.0),
+        field=("constant", (1.0, 0.5, 0.25)),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", float(t), float(t + 1)) for t in range(10)],
+    ),
+    "sphere20_deformation": dict(
+        fixture=("sphere", 20.0, (32.0, 30.0, 34.0), 1.0, 3.0),
+        field=("deformation", 64.0, 8.0, 1.0),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", float(t), float(t + 1)) for t in range(4)],
+    ),
+    "sphere16_rotation_backward": dict(
+        fixture=("sphere", 16.0, (5.5, -3.25, 2.0), 1.0, 3.0),
+        field=("rotation", (0.3, -0.2, 0.1), (0.02, -0.03, 0.05), (5.0, -3.0, 2.0)),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", 3.0, 2.0), ("advect", 2.0, 1.0)],
+    ),
+    "sphere12_rk1_default_tracker": dict(
+        fixture=("sphere", 12.0, (0.0, 1.0, 2.0), 1.0, 3.0),
+        field=("constant", (-0.7, 0.4, 1.1)),
+        schemes=(HJ, RK1, HJ, RK1, 3),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.5)],
+    ),
+    "sphere12_rk2": dict(
+        fixture=("sphere", 12.0, (0.0, 1.0, 2.0), 1.0, 3.0),
+        field=("constant", (-0.7, 0.4, 1.1)),
+        schemes=(HJ, RK2, HJ, RK1, 3),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.5)],
+    ),
+    "sphere24_tracker_rk3_rk2": dict(
+        fixture=("sphere", 24.0, (-10.0, 4.0, 9.0), 1.0, 3.0),
+        field=("constant", (0.6, -0.9, 0.2)),
+        schemes=(HJ, RK3, HJ, RK3, 2),
+        ops=[("advect", 0.0, 1.0), ("state", {"tr_temporal": RK2}), ("advect", 1.0, 2.0)],
+    ),
+    "tracker_ops": dict(
+        fixture=("sphere", 20.0, (1.0, 2.0, 3.0), 1.0, 3.0),
+        field=("constant", (0.0, 0.0, 0.0)),
+        schemes=(HJ, RK1, HJ, RK1, 3),
+        ops=[("normalize",), ("dilate", 2), ("normalize",), ("prune",), ("track",),
+             ("state", {"trim": _abi.TRIM_INTERIOR}), ("dilate", 1), ("track",),
+             ("state", {"trim": _abi.TRIM_EXTERIOR}), ("track",),
+             ("state", {"trim": _abi.TRIM_NONE}), ("track",),
+             ("state", {"trim": _abi.TRIM_ALL, "norm_count": 0}), ("track",)],
+    ),
+    "union8_deformation": dict(
+        fixture=("union8",),
+        field=("deformation", 128.0, 10.0, 1.0),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", float(t), float(t + 1)) for t in range(3)],
+    ),
+    "sphere12_dense_noise": dict(
+        fixture=("sphere", 12.0, (16.0, 16.0, 16.0), 1.0, 3.0),
+        field=("dense", 32, 4.0, 1.0, 11),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", float(t), float(t + 1)) for t in range(3)],
+    ),
+    "sphere_half_voxel": dict(
+        fixture=("sphere", 6.0, (0.25, -0.5, 1.0), 0.5, 3.0),
+        field=("constant", (0.5, 0.25, -0.3)),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+    ),
+}
+
+
+def make_field(spec):
+    kind = spec[0]
+    if kind == "constant":
+        return Field.constant_field(spec[1])
+    if kind == "deformation":
+        return Field.deformation(domain=spec[1], period=spec[2], scale=spec[3])
+    if kind == "rotation":
+        return Field.rotation(spec[1], spec[2], spec[3])
+    if kind == "dense":
+        n, sigma, amp, seed = spec[1:]
+        return Field.dense(smoothed_noise(n, sigma, amp, seed), origin=(0, 0, 0),
+                           background=(0.0, 0.0, 0.0))
+    raise ValueError(kind)
+
+
+def make_fixture(spec):
+    from openvdb_gb300 import fixtures
+    if spec[0] == "sphere":
+        return fixtures.sphere(spec[1], spec[2], spec[3], spec[4])
+    if spec[0] == "union8":
+        c, r = union8()
+        return fixtures.union_of_spheres(c, r)
+    raise ValueError(spec[0])

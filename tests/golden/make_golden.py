@@ -1,0 +1,86 @@
+"""Generate tests/golden/parity_cases.json from the reference implementation.
+
+Runs every case of tests/golden/cases.py through the UNMODIFIED reference
+(tools::LevelSetAdvection / tools::LevelSetTracker compiled from the
+reference checkout into oracle/_ref/libvdbref.so by oracle/ref/build_ref.py)
+and records the digest of the grid after each operation.  The input level
+sets come from openvdb_gb300.fixtures; for spheres the generator first
+checks that they equal the reference's own createLevelSetSphere bit for bit.
+Each case also runs with one and with all oracle threads, which must agree.
+
+Usage: python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, HERE)
+
+from cases import CASES, make_field, make_fixture  # noqa: E402
+from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
+from oracle import refpy  # noqa: E402
+
+
+def run_reference(name, case, threads):
+    refpy.set_threads(threads)
+    fx = case["fixture"]
+    host = make_fixture(fx)
+    if fx[0] == "sphere":
+        ref_sphere = refpy.RefGrid.sphere(fx[1], fx[2], fx[3], fx[4]).to_host()
+        assert bitwise_equal(host, ref_sphere), "fixture differs from createLevelSetSphere: " + name
+    g = refpy.RefGrid.from_host(host)
+    assert bitwise_equal(g.to_host(), host), "round trip through the reference grid: " + name
+    field = make_field(case["field"])
+    sp, tp, tsp, ttp, nc = case["schemes"]
+    trim = 3
+    out = [{"op": "input", "digest": digest(host), "summary": summary(host)}]
+    for op in case["ops"]:
+        rec = {"op": list(op) if op[0] != "state" else ["state", op[1]]}
+        if op[0] == "state":
+            s = op[1]
+            nc = s.get("norm_count", nc)
+            ttp = s.get("tr_temporal", ttp)
+            trim = s.get("trim", trim)
+            out.append(rec)
+            continue
+        kw = dict(spatial=tsp, temporal=ttp, norm_count=nc, trim=trim)
+        if op[0] == "advect":
+            rec["count"] = g.advect(field, op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp,
+                                    tracker_temporal=ttp, norm_count=nc)
+        elif op[0] == "track":
+            g.track(**kw)
+        elif op[0] == "normalize":
+            g.normalize(**kw)
+        elif op[0] == "prune":
+            g.prune(**kw)
+        elif op[0] == "dilate":
+            g.dilate(op[1], **kw)
+        else:
+            raise ValueError(op)
+        h = g.to_host()
+        rec["digest"] = digest(h)
+        rec["summary"] = summary(h)
+        out.append(rec)
+    return out
+
+
+def main():
+    nthreads = os.cpu_count() or 1
+    result = {}
+    for name, case in CASES.items():
+        a = run_reference(name, case, 1)
+        b = run_reference(name, case, nthreads)
+        assert a == b, "reference result depends on the thread count: " + name
+        result[name] = a
+        last = a[-1]
+        print("%-32s ops=%d final leaves=%s active=%s" % (name, len(a) - 1, last.get("summary", {}).get("leaves"),
+                                                          last.get("summary", {}).get("active")))
+    with open(os.path.join(HERE, "parity_cases.json"), "w") as f:
+        json.dump(result, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

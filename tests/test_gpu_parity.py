@@ -1,0 +1,85 @@
+"""Bit-exact parity of the device path (PARITY mode) with the reference.
+
+The reference digests in tests/golden/parity_cases.json were produced by
+tests/golden/make_golden.py from the reference's own LevelSetAdvection /
+LevelSetTracker compiled from source.  Every operation of every case must
+reproduce the reference grid exactly: leaf set, masks, values, node tiles.
+On a mismatch the device grid is written to $GBLS_DUMP_DIR for diagnosis.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from cases import CASES, make_field, make_fixture
+from openvdb_gb300 import PARITY, DeviceLevelSet, LevelSetAdvection, LevelSetTracker, digest, summary
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = json.load(open(os.path.join(HERE, "golden", "parity_cases.json")))
+
+
+def _dump(name, step, g):
+    d = os.environ.get("GBLS_DUMP_DIR")
+    if not d:
+        return
+    os.makedirs(d, exist_ok=True)
+    np.savez_compressed(os.path.join(d, "%s_%02d.npz" % (name, step)),
+                        **{k: getattr(g, k) for k in ("leaf_origins", "leaf_masks", "leaf_values",
+                                                       "lower_origins", "lower_tiles", "upper_origins",
+                                                       "upper_tiles", "root_tile_origins",
+                                                       "root_tile_values")})
+
+
+def run_case(name, mode=PARITY, check=True):
+    case, gold = CASES[name], GOLD[name]
+    host = make_fixture(case["fixture"])
+    assert digest(host) == gold[0]["digest"], "input fixture differs from the reference input"
+    dev = DeviceLevelSet(host)
+    dev.set_precision(mode)
+    sp, tp, tsp, ttp, nc = case["schemes"]
+    adv = LevelSetAdvection(dev, make_field(case["field"]))
+    adv.setSpatialScheme(sp)
+    adv.setTemporalScheme(tp)
+    adv.setTrackerSpatialScheme(tsp)
+    adv.setTrackerTemporalScheme(ttp)
+    adv.setNormCount(nc)
+    tr = adv.tracker
+    results = []
+    for step, (op, rec) in enumerate(zip(case["ops"], gold[1:]), start=1):
+        if op[0] == "state":
+            s = op[1]
+            if "norm_count" in s:
+                tr.setNormCount(s["norm_count"])
+            if "tr_temporal" in s:
+                tr.setTemporalScheme(s["tr_temporal"])
+            if "trim" in s:
+                tr.setTrimming(s["trim"])
+            continue
+        count = None
+        if op[0] == "advect":
+            count = adv.advect(op[1], op[2])
+        elif op[0] == "track":
+            tr.track()
+        elif op[0] == "normalize":
+            tr.normalize()
+        elif op[0] == "prune":
+            tr.prune()
+        elif op[0] == "dilate":
+            tr.dilate(op[1])
+        g = dev.to_host()
+        results.append((op, count, g))
+        if check:
+            if count is not None:
+                assert count == rec["count"], (name, step, op, count, rec["count"])
+            if digest(g) != rec["digest"]:
+                _dump(name, step, g)
+                pytest.fail("%s op %d %s: device %s != reference %s" % (name, step, op, summary(g),
+                                                                        rec["summary"]))
+    return results
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(CASES))
+def test_parity_bit_exact(name):
+    run_case(name)
