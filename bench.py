@@ -1,0 +1,288 @@
+"""Benchmark: narrow-band level-set advection (RK3-HJWENO5 + track) on one GB300.
+
+Workload (the 64-sphere configuration): the union of 64 spheres with seeded
+centres U[0,1024]^3 and radii U[20,80] voxels (half-width 3, voxel size 1),
+advected by LeVeque's divergence-free deformation field on the unit cube
+mapped to 1024^3, scaled by cos(pi t / 100) (1 voxel per time unit per unit
+of field), HJWENO5 + TVD-RK3 with CFL 0.5, tracker HJWENO5 + TVD-RK1 with one
+renormalisation per substep.  One bench step = advect(t, t+1) (all CFL
+substeps of one time unit, each followed by the tracker pass).
+
+Metric: voxel-updates/s = sum over substeps of the active voxels at the
+substep start / device time (CUDA events on the library stream, L2 flushed
+between steps).  `e2e` runs the same steps through the host-facing API: the
+level set is uploaded from host arrays, advected and downloaded every step.
+
+  python bench.py [--steps K] [--warmup W] [--mode fast|parity] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "narrow-band voxel-updates/s per RK3-HJWENO5 step (FP32)"
+UNIT = "voxel-updates/s"
+WORKLOAD = {"workload": "64-sphere union, LeVeque deformation x cos(pi t/100), 1024^3 domain",
+            "spheres": 64, "seed": 2024, "domain": 1024, "radii": [20, 80], "half_width": 3,
+            "spatial": "HJWENO5", "temporal": "TVD_RK3", "cfl": 0.5, "tracker": "HJWENO5/TVD_RK1",
+            "norm_count": 1, "l2": "flushed between steps (256 MiB write)"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_workload():
+    from openvdb_gb300 import Field, fixtures
+    centers, radii = fixtures.sixty_four_spheres(seed=2024)
+    host = fixtures.union_of_spheres(centers, radii, 1.0, 3.0)
+    field = Field.deformation(domain=1024.0, period=100.0, scale=1.0)
+    return host, field
+
+
+def make_advection(dev, field, cfl=0.5):
+    from openvdb_gb300 import LevelSetAdvection
+    from openvdb_gb300.levelset import HJWENO5_BIAS, TVD_RK1, TVD_RK3
+    adv = LevelSetAdvection(dev, field)
+    adv.setSpatialScheme(HJWENO5_BIAS)
+    adv.setTemporalScheme(TVD_RK3)
+    adv.setTrackerSpatialScheme(HJWENO5_BIAS)
+    adv.setTrackerTemporalScheme(TVD_RK1)
+    adv.setNormCount(1)
+    adv.cfl = cfl
+    return adv
+
+
+def host_bytes(g):
+    return int(sum(getattr(g, k).nbytes for k in ("leaf_origins", "leaf_masks", "leaf_values",
+                                                   "lower_origins", "lower_tiles", "upper_origins",
+                                                   "upper_tiles", "root_tile_origins", "root_tile_values")))
+
+
+def run_gb300(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from openvdb_gb300 import FAST, PARITY, DeviceLevelSet
+    from openvdb_gb300.levelset import DeviceField
+
+    torch.cuda.init()
+    dev_index = 0
+    torch.cuda.set_device(dev_index)
+    t_build = time.perf_counter()
+    host, field = build_workload()
+    t_build = time.perf_counter() - t_build
+    dev = DeviceLevelSet(host, device=dev_index)
+    mode = FAST if args.mode == "fast" else PARITY
+    dev.set_precision(mode)
+    stream = torch.cuda.Stream()
+    dev.set_stream(stream.cuda_stream)
+    dfield = DeviceField(field)
+    adv = make_advection(dev, dfield, cfl=args.cfl)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    t = 0.0
+    for _ in range(args.warmup):
+        adv.advect(t, t + 1.0)
+        t += 1.0
+    torch.cuda.synchronize()
+
+    dev.reset_stats()
+    dev.set_profiling(True)
+    clocks = ClockSampler()
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        adv.advect(t, t + 1.0)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        t += 1.0
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dev.set_profiling(False)
+    st = dev.stats()
+    total = sum(times)
+    value = st["voxel_updates"] / total
+
+    peak, peak_kind = measured_peaks()
+    rk_gbs = st["rk_bytes"] / (st["rk_ms"] / 1e3) / 1e9 if st["rk_ms"] > 0 else 0.0
+    norm_gbs = st["norm_bytes"] / (st["norm_ms"] / 1e3) / 1e9 if st["norm_ms"] > 0 else 0.0
+    dominant = "rk_stage" if st["rk_ms"] >= st["norm_ms"] else "normalize"
+    achieved = rk_gbs if dominant == "rk_stage" else norm_gbs
+    launches = st["rk_launches"] if dominant == "rk_stage" else st["norm_launches"]
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(dominant + "_" + args.mode)
+
+    # end to end through the host-facing API: upload, advect one time unit, download
+    e2e = None
+    if args.e2e_steps > 0:
+        g = dev.to_host()
+        te = t
+        e2e_updates = 0
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            h2d += host_bytes(g)
+            d = DeviceLevelSet(g, device=dev_index)
+            d.set_precision(mode)
+            a = make_advection(d, dfield, cfl=args.cfl)
+            a.advect(te, te + 1.0)
+            e2e_updates += d.stats()["voxel_updates"]
+            g = d.to_host()
+            d2h += host_bytes(g)
+            d.close()
+            te += 1.0
+        el = time.perf_counter() - t0
+        e2e = {"value": e2e_updates / el, "unit": UNIT, "h2d_bytes_per_step": h2d // args.e2e_steps,
+               "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
+
+    cfg = dict(WORKLOAD)
+    cfg.update({"mode": args.mode, "active_voxels_initial": int(host.active_voxel_count()),
+                "leaves_initial": int(host.leaf_count), "fixture_build_s": round(t_build, 2),
+                "substeps": int(st["substeps"]), "t_start": float(t - args.steps),
+                "active_voxels_end": int(st["active_voxels"]),
+                "rho_dilated": (st["dilated_voxels"] / st["voxel_updates"]) if st["voxel_updates"] else None})
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "replicas", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
+        "config": cfg,
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "launches": int(launches),
+                     "rk_stage_gbs": rk_gbs, "normalize_gbs": norm_gbs,
+                     "rk_stage_ms": st["rk_ms"], "normalize_ms": st["norm_ms"],
+                     "step_ms_total": 1e3 * total},
+        "e2e": e2e,
+        "gpu_launches": int(st["kernel_launches"]),
+        "clocks": clk,
+        "cpu_baseline": cpu_baseline(args) if args.cpu_baseline else None,
+    }
+    print(json.dumps(out))
+
+
+def cpu_baseline(args):
+    """The oracle's CPU restatement of the path on a bounded sample."""
+    try:
+        from oracle import port
+    except ImportError:
+        return None
+    if not port.available():
+        return None
+    return port.bench_sample(seconds=args.cpu_seconds)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    try:
+        from oracle import port
+        ok = port.available()
+    except ImportError:
+        ok = False
+    if not ok:
+        print(json.dumps({"impl": "reference", "unavailable": "CPU oracle port not built on this host"}))
+        return
+    res = port.bench_reference(steps=args.steps, warmup=args.warmup, seconds=args.cpu_seconds)
+    res.update({"impl": "reference", "metric": METRIC, "unit": UNIT, "higher_is_better": True,
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "config": WORKLOAD})
+    res["e2e"] = {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    print(json.dumps(res))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="fast", choices=["fast", "parity"])
+    ap.add_argument("--cfl", type=float, default=0.5)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -204,6 +204,29 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
                 int temporal_scheme, float t0, float t1, float cfl, uint64_t* substeps);
 
 
+
+/* ---- measurement ----------------------------------------------------------
+ * Counters since the last gbls_reset_stats.  voxel_updates is the sum over
+ * CFL substeps of the active voxel count at the start of the substep.  With
+ * profiling enabled the stencil kernels are bracketed by CUDA events on the
+ * handle's stream and their device time and algorithmic bytes (FP32 values
+ * read and written for active voxels only) are accumulated.               */
+typedef struct gbls_stats {
+    uint64_t substeps;
+    uint64_t voxel_updates;
+    uint64_t kernel_launches;      /* every kernel this library launched    */
+    uint64_t rk_launches;          /* advection RK stage kernel             */
+    uint64_t norm_launches;        /* renormalise / trim kernel             */
+    double rk_ms, norm_ms;         /* device time (profiling only)          */
+    double rk_bytes, norm_bytes;   /* algorithmic bytes of those launches   */
+    uint64_t dilated_voxels;       /* voxels renormalised by track passes   */
+    int64_t active_voxels;         /* current                               */
+    int64_t leaves;                /* current                               */
+} gbls_stats;
+int gbls_get_stats(gbls_handle* h, gbls_stats* out);
+int gbls_reset_stats(gbls_handle* h);
+int gbls_set_profiling(gbls_handle* h, int enable);
+
 /* ---- host construction of level sets ------------------------------------
  * gbls_host_sphere replaces tools::createLevelSetSphere
  * (tools/LevelSetSphere.h:219-230): same rasterisation, background and

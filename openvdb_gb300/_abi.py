@@ -90,3 +90,20 @@ class Interrupter(C.Structure):
         ("was_interrupted", INTERRUPT_CHECK),
         ("user", C.c_void_p),
     ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("substeps", C.c_uint64),
+        ("voxel_updates", C.c_uint64),
+        ("kernel_launches", C.c_uint64),
+        ("rk_launches", C.c_uint64),
+        ("norm_launches", C.c_uint64),
+        ("rk_ms", C.c_double),
+        ("norm_ms", C.c_double),
+        ("rk_bytes", C.c_double),
+        ("norm_bytes", C.c_double),
+        ("dilated_voxels", C.c_uint64),
+        ("active_voxels", C.c_int64),
+        ("leaves", C.c_int64),
+    ]

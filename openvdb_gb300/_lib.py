@@ -55,6 +55,9 @@ def lib():
         "gbls_field_destroy": ([vp], C.c_int),
         "gbls_advect": ([vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                          P(C.c_uint64)], C.c_int),
+        "gbls_get_stats": ([vp, P(_abi.Stats)], C.c_int),
+        "gbls_reset_stats": ([vp], C.c_int),
+        "gbls_set_profiling": ([vp, C.c_int], C.c_int),
         "gbls_host_sphere": ([C.c_float, P(C.c_float), C.c_float, C.c_float, P(vp)], C.c_int),
         "gbls_host_union_of_spheres": ([C.c_int64, P(C.c_float), P(C.c_float), C.c_float,
                                         C.c_float, P(vp)], C.c_int),

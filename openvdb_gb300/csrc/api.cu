@@ -192,6 +192,38 @@ __global__ void k_dilate(int64_t n, const int32_t* slot, const int32_t* nbr, con
     dmask[size_t(s) * 8 + x] = dilate_word(own, x, P(0), P(1), P(2), P(3), P(4), P(5));
 }
 
+// NN_FACE erosion of every leaf mask (tools/Morphology.h NodeMaskOp::erode6
+// over 8-bit z rows; missing neighbours count as inactive, empty leaves stay
+// empty).  8 threads per leaf.
+__global__ void k_erode(int64_t n, const int32_t* slot, const int32_t* nbr, const uint64_t* in,
+                        uint64_t* out) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n * 8) return;
+    const int64_t l = i >> 3;
+    const int x = int(i & 7);
+    const int s = slot[l];
+    const int32_t* nb = nbr + 6 * l;
+    const uint64_t* own = in + size_t(s) * 8;
+    auto W = [&](int f, int word) -> uint64_t { return nb[f] >= 0 ? in[size_t(nb[f]) * 8 + word] : 0; };
+    const uint64_t w = own[x];
+    uint64_t e = w;
+    e &= ((w << 1) & 0xFEFEFEFEFEFEFEFEull) | ((W(4, x) >> 7) & 0x0101010101010101ull);
+    e &= ((w >> 1) & 0x7F7F7F7F7F7F7F7Full) | ((W(5, x) << 7) & 0x8080808080808080ull);
+    e &= (w << 8) | (W(2, x) >> 56);
+    e &= (w >> 8) | (W(3, x) << 56);
+    e &= (x > 0) ? own[x - 1] : W(0, 7);
+    e &= (x < 7) ? own[x + 1] : W(1, 0);
+    out[size_t(s) * 8 + x] = e;
+}
+
+// m[s] &= ~a[s] over the leaves (voxels activated by a dilation).
+__global__ void k_andnot(int64_t n, const int32_t* slot, uint64_t* m, const uint64_t* a) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n * 8) return;
+    const size_t k = size_t(slot[i >> 3]) * 8 + (i & 7);
+    m[k] &= ~a[k];
+}
+
 // Lower nodes missing for new leaves (rare): append lower keys.
 __global__ void k_missing_lower(int64_t n, const uint64_t* new_keys, const uint64_t* lower_keys,
                                 int64_t nlower, uint64_t* out, unsigned long long* count) {
@@ -215,6 +247,7 @@ __global__ void k_prune_scatter(int64_t n, const uint64_t* keys, const int32_t* 
                                 const int32_t* keep, const int32_t* idx, const uint64_t* sm,
                                 uint64_t* ko, int32_t* so, int32_t* free_slots, int64_t nfree,
                                 const uint64_t* lower_keys, int64_t nlower, uint64_t* lower_sign,
+                                const int32_t* cnt, unsigned long long* nactive,
                                 unsigned long long* nkept, unsigned long long* err) {
     const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (l >= n) return;
@@ -223,6 +256,7 @@ __global__ void k_prune_scatter(int64_t n, const uint64_t* keys, const int32_t* 
     if (keep[l]) {
         ko[k] = keys[l];
         so[k] = slot[l];
+        atomicAdd(nactive, (unsigned long long)cnt[l]);
         return;
     }
     const int s = slot[l];
@@ -342,7 +376,7 @@ struct gbls_handle {
     int64_t slot_cap = 0;
     DevArray<uint64_t> am[3], sm[3];
     DevArray<float> vals[3];
-    DevArray<uint64_t> dmask;
+    DevArray<uint64_t> dmask, emask;
     DevArray<int32_t> free_slots;
     int64_t nfree = 0;
     int mc = 0, vc = 0;  // current mask set / value buffer
@@ -359,10 +393,48 @@ struct gbls_handle {
     DevStatus* st_d = nullptr;
     DevStatus* st_h = nullptr;
     DevArray<unsigned long long> u64s;
+    unsigned long long* acc_d = nullptr;  // [2] normalize voxels processed / written
+    // measurement
+    gbls_stats stats{};
+    int64_t nactive = -1;  // active voxels, -1 = unknown
+    bool profiling = false;
+    struct Pending {
+        cudaEvent_t a, b;
+        int kind;  // 0 rk, 1 norm
+        double bytes;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
 
     ~gbls_handle() {
         if (st_d) cudaFree(st_d);
         if (st_h) cudaFreeHost(st_h);
+        if (acc_d) cudaFree(acc_d);
+        for (auto& p : pending) { event_pool.push_back(p.a); event_pool.push_back(p.b); }
+        for (auto e : event_pool) cudaEventDestroy(e);
+    }
+
+    cudaEvent_t event() {
+        if (event_pool.empty()) {
+            cudaEvent_t e;
+            CU(cudaEventCreate(&e));
+            return e;
+        }
+        cudaEvent_t e = event_pool.back();
+        event_pool.pop_back();
+        return e;
+    }
+    // Accumulate the device time of completed profiled launches.
+    void resolve_pending() {
+        for (auto& p : pending) {
+            float ms = 0.0f;
+            CU(cudaEventElapsedTime(&ms, p.a, p.b));
+            if (p.kind == 0) stats.rk_ms += ms;
+            else stats.norm_ms += ms;
+            event_pool.push_back(p.a);
+            event_pool.push_back(p.b);
+        }
+        pending.clear();
     }
 
     NodeTables nodes() const {
@@ -382,7 +454,10 @@ struct gbls_handle {
     int32_t* S() { return slot[kc].p; }
     Layout layout(int m, int v) const { return Layout{am[m].p, sm[m].p, vals[v].p}; }
 
-    void sync() { CU(cudaStreamSynchronize(stream)); }
+    void sync() {
+        CU(cudaStreamSynchronize(stream));
+        if (!pending.empty()) resolve_pending();
+    }
     void read_status() {
         CU(cudaMemcpyAsync(st_h, st_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
         sync();
@@ -413,6 +488,7 @@ struct gbls_handle {
             vals[b].reserve(size_t(nc) * LEAF_VOX, stream, size_t(old) * LEAF_VOX, 1.0);
         }
         dmask.reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
+        emask.reserve(size_t(nc) * 8, stream, 0, 1.0);
         free_slots.reserve(size_t(nc), stream, size_t(nfree), 1.0);
         // push the new slots below the existing free ones so that they are
         // used last: [new slots..., old free slots...]
@@ -443,6 +519,7 @@ struct gbls_handle {
     void rebuild_nbr() {
         if (nleaf == 0) return;
         k_build_nbr<<<blocks_for(nleaf * 6, 256), 256, 0, stream>>>(nleaf, K(), S(), nodes(), nbr.p);
+        ++stats.kernel_launches;
         CU(cudaGetLastError());
     }
 };
@@ -461,7 +538,10 @@ void remap_lower(gbls_handle& h, const std::vector<uint64_t>& new_keys, const st
     DevArray<uint64_t> ns;
     ns.reserve(size_t(std::max<int64_t>(n, 1)) * 64, h.stream);
     h.remap.upload(src.data(), src.size(), h.stream);
-    if (n) k_remap_rows<<<blocks_for(n * 64, 256), 256, 0, h.stream>>>(n, h.remap.p, h.lower_sign.p, ns.p);
+    if (n) {
+        k_remap_rows<<<blocks_for(n * 64, 256), 256, 0, h.stream>>>(n, h.remap.p, h.lower_sign.p, ns.p);
+        ++h.stats.kernel_launches;
+    }
     CU(cudaGetLastError());
     std::swap(h.lower_sign.p, ns.p);
     std::swap(h.lower_sign.cap, ns.cap);
@@ -609,6 +689,7 @@ void dilate_topology(gbls_handle& h) {
     h.clear_status();
     k_emit_candidates<<<blocks_for(L, 128), 128, 0, h.stream>>>(L, h.K(), h.S(), h.nbr.p, h.am[h.mc].p,
                                                                  h.cand.p, &h.st_d->n_cand);
+    ++h.stats.kernel_launches;
     CU(cudaGetLastError());
     h.read_status();
     const int64_t nc = int64_t(h.st_h->n_cand);
@@ -636,11 +717,13 @@ void dilate_topology(gbls_handle& h) {
         k_new_leaves<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(nnew, h.cand.p, h.free_slots.p, h.nfree,
                                                                    h.new_keys.p, h.new_slots.p,
                                                                    h.am[h.mc].p, h.sm[h.mc].p);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.nfree -= nnew;
         const int ko = 1 - h.kc;
         k_merge<<<blocks_for(L + nnew, 256), 256, 0, h.stream>>>(L, h.K(), h.S(), nnew, h.new_keys.p,
                                                                  h.new_slots.p, h.keys[ko].p, h.slot[ko].p);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.kc = ko;
         h.nleaf = L + nnew;
@@ -650,6 +733,7 @@ void dilate_topology(gbls_handle& h) {
         k_missing_lower<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(
             nnew, h.new_keys.p, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.cand_sorted.p,
             &h.st_d->n_lower_miss);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.read_status();
         const int64_t nm = int64_t(h.st_h->n_lower_miss);
@@ -663,14 +747,29 @@ void dilate_topology(gbls_handle& h) {
     h.rebuild_nbr();
     k_dilate<<<blocks_for(h.nleaf * 8, 256), 256, 0, h.stream>>>(h.nleaf, h.S(), h.nbr.p, h.am[h.mc].p,
                                                                   h.dmask.p);
+    ++h.stats.kernel_launches;
     CU(cudaGetLastError());
 }
 
 // ---- normalize / trim passes ----------------------------------------------
-void launch_norm(gbls_handle& h, const NormArgs& a) {
+void launch_norm(gbls_handle& h, const NormArgs& a0) {
+    NormArgs a = a0;
+    a.acc = h.acc_d;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h.profiling) {
+        e0 = h.event();
+        e1 = h.event();
+        CU(cudaEventRecord(e0, h.stream));
+    }
     if (h.mode == GBLS_MODE_PARITY) launch_norm_parity(a, h.stream);
     else launch_norm_fast(a, h.stream);
     CU(cudaGetLastError());
+    if (h.profiling) {
+        CU(cudaEventRecord(e1, h.stream));
+        h.pending.push_back({e0, e1, 1, 0.0});
+    }
+    ++h.stats.norm_launches;
+    ++h.stats.kernel_launches;
 }
 
 void start_intr(gbls_handle& h, const char* msg) {
@@ -689,7 +788,7 @@ bool check_intr(gbls_handle& h) {
 // stage also applies Trim.  With norm_count == 0 and trim set, a trim-only
 // pass runs.  Leaves the result as the current layout and per-leaf counts
 // in h.cnt.
-void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim) {
+void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim, int carry = 0) {
     if (h.nleaf == 0) return;
     const float dx = float(h.voxel_size);
     const float mdt = dx * (h.tr_temporal == GBLS_TVD_RK1 ? 0.3f : h.tr_temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f);
@@ -703,6 +802,7 @@ void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim) {
     base.mdt = mdt;
     base.invdx = invdx;
     base.out_count = h.cnt.p;
+    base.carry = carry;
     const int iters = h.norm_count;
     if (iters <= 0) {
         if (!trim) return;
@@ -765,9 +865,35 @@ void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim) {
         }
         h.mc = ms;
         h.vc = vs;
-        pmask = h.am[h.mc].p;  // later iterations update the (now current) active set
-        base.pmask = pmask;
+        if (!carry) {
+            pmask = h.am[h.mc].p;  // later iterations update the (now current) active set
+            base.pmask = pmask;
+        }
     }
+}
+
+// Copy the current values into the layout of pmask (| the active set when
+// `carry`), optionally trimming; records per-leaf counts in h.cnt.
+void relayout(gbls_handle& h, const uint64_t* pmask, int carry, int trim) {
+    if (h.nleaf == 0) return;
+    NormArgs a{};
+    a.nleaf = h.nleaf;
+    a.slot = h.S();
+    a.nbr = h.nbr.p;
+    a.src = h.layout(h.mc, h.vc);
+    a.pmask = pmask;
+    a.copy_only = 1;
+    a.carry = carry;
+    a.trim = trim;
+    a.gamma = h.gamma;
+    a.out_count = h.cnt.p;
+    const int mo = other_of(h.mc, h.mc), vo = other_of(h.vc, h.vc);
+    a.out_vals = h.vals[vo].p;
+    a.out_amask = h.am[mo].p;
+    a.out_smask = h.sm[mo].p;
+    launch_norm(h, a);
+    h.mc = mo;
+    h.vc = vo;
 }
 
 // Leaf + node prune after a trim pass (LevelSetTracker::prune,
@@ -777,6 +903,7 @@ void prune_compact(gbls_handle& h) {
     bool lower_changed = false;
     if (L > 0) {
         k_keep_flags<<<blocks_for(L, 256), 256, 0, h.stream>>>(L, h.cnt.p, h.keep.p);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         size_t bytes = 0;
         CU(cub::DeviceScan::ExclusiveSum(nullptr, bytes, h.keep.p, h.idx.p, int(L), h.stream));
@@ -787,21 +914,25 @@ void prune_compact(gbls_handle& h) {
         const int ko = 1 - h.kc;
         k_prune_scatter<<<blocks_for(L, 256), 256, 0, h.stream>>>(
             L, h.K(), h.S(), h.keep.p, h.idx.p, h.sm[h.mc].p, h.keys[ko].p, h.slot[ko].p, h.free_slots.p,
-            h.nfree, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.lower_sign.p, &h.st_d->n_cand,
-            &h.st_d->error);
+            h.nfree, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.lower_sign.p, h.cnt.p,
+            &h.st_d->n_active, &h.st_d->n_cand, &h.st_d->error);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.kc = ko;
         const int64_t nl = int64_t(h.lower_keys_h.size());
         h.flags.reserve(size_t(std::max<int64_t>(nl, 1)), h.stream);
-        if (nl)
+        if (nl) {
             k_lower_status<<<blocks_for(nl, 128), 128, 0, h.stream>>>(nl, h.lower_keys.p, h.lower_sign.p,
                                                                        h.K(), &h.st_d->n_cand, h.flags.p,
                                                                        &h.st_d->n_lower_empty);
+            ++h.stats.kernel_launches;
+        }
         CU(cudaGetLastError());
         h.read_status();
         const int64_t kept = int64_t(h.st_h->n_cand);
         h.nfree += L - kept;
         h.nleaf = kept;
+        h.nactive = int64_t(h.st_h->n_active);
         lower_changed = h.st_h->n_lower_empty > 0;
     } else if (!h.lower_keys_h.empty()) {
         // no leaves: every lower node is empty
@@ -811,9 +942,11 @@ void prune_compact(gbls_handle& h) {
         k_lower_status<<<blocks_for(nl, 128), 128, 0, h.stream>>>(nl, h.lower_keys.p, h.lower_sign.p, h.K(),
                                                                    &h.st_d->n_cand, h.flags.p,
                                                                    &h.st_d->n_lower_empty);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.read_status();
         lower_changed = true;
+        h.nactive = 0;
     }
     if (lower_changed || !h.nodes_checked || !h.root_keys_h.empty()) prune_nodes(h, lower_changed);
     h.nodes_checked = true;
@@ -891,6 +1024,7 @@ float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
     a.field = field_params(f);
     a.max_bits = &h.st_d->max_v2_bits;
     launch_cfl(a, h.stream);
+    ++h.stats.kernel_launches;
     CU(cudaGetLastError());
     h.read_status();
     float m;
@@ -899,9 +1033,24 @@ float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
 }
 
 void rk_stage(gbls_handle& h, const RkArgs& a) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (h.profiling) {
+        e0 = h.event();
+        e1 = h.event();
+        CU(cudaEventRecord(e0, h.stream));
+    }
     if (h.mode == GBLS_MODE_PARITY) launch_rk_parity(a, h.stream);
     else launch_rk_fast(a, h.stream);
     CU(cudaGetLastError());
+    // FP32 values of the active voxels: stencil read + result write (+ phi_n read)
+    const double bytes = double(h.nactive) * (a.has_phi ? 12.0 : 8.0);
+    if (h.profiling) {
+        CU(cudaEventRecord(e1, h.stream));
+        h.pending.push_back({e0, e1, 0, bytes});
+    }
+    h.stats.rk_bytes += bytes;
+    ++h.stats.rk_launches;
+    ++h.stats.kernel_launches;
 }
 
 // The TVD-RK stages of one substep (tools/LevelSetAdvect.h:360-405).
@@ -1083,6 +1232,7 @@ void upload(gbls_handle& h, const gbls_grid_desc* d) {
         h.vals[b].reserve(size_t(scap) * LEAF_VOX, h.stream);
     }
     h.dmask.reserve(size_t(scap) * 8, h.stream);
+    h.emask.reserve(size_t(scap) * 8, h.stream);
     h.free_slots.reserve(size_t(scap), h.stream);
     h.slot_cap = scap;
     std::vector<int32_t> fs;
@@ -1103,6 +1253,7 @@ void upload(gbls_handle& h, const gbls_grid_desc* d) {
     h.upload_upper_root();
     h.rebuild_nbr();
     h.sync();
+    h.nactive = -1;
 }
 
 void download(gbls_handle& h, gbls_grid_desc* d) {
@@ -1125,6 +1276,7 @@ void download(gbls_handle& h, gbls_grid_desc* d) {
         dense.reserve(size_t(L) * LEAF_VOX, h.stream);
         k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S(), h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, g,
                                                      dense.p);
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         dense.download(d->leaf_values, size_t(L) * LEAF_VOX, h.stream);
         std::vector<uint64_t> am(size_t(h.slot_cap) * 8);
@@ -1184,6 +1336,7 @@ int64_t active_count(gbls_handle& h) {
     h.u64s.reserve(1, h.stream);
     CU(cudaMemsetAsync(h.u64s.p, 0, sizeof(unsigned long long), h.stream));
     k_count_active<<<blocks_for(h.nleaf * 8, 256), 256, 0, h.stream>>>(h.nleaf, h.S(), h.am[h.mc].p, h.u64s.p);
+    ++h.stats.kernel_launches;
     CU(cudaGetLastError());
     unsigned long long n = 0;
     CU(cudaMemcpyAsync(&n, h.u64s.p, sizeof(n), cudaMemcpyDeviceToHost, h.stream));
@@ -1233,6 +1386,8 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
         h->device = g_device;
         CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
         CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
+        CU(cudaMalloc(&h->acc_d, 2 * sizeof(unsigned long long)));
+        CU(cudaMemset(h->acc_d, 0, 2 * sizeof(unsigned long long)));
         upload(*h, desc);
     });
     if (rc != GBLS_OK) {
@@ -1359,73 +1514,113 @@ int gbls_prune(gbls_handle* h) {
     return guarded([&] {
         DeviceGuard g(h->device);
         start_intr(*h, "Pruning Level Set");
-        if (h->nleaf > 0) {
-            // Trim (or a plain copy that records per-leaf counts)
-            NormArgs a{};
-            a.nleaf = h->nleaf;
-            a.slot = h->S();
-            a.nbr = h->nbr.p;
-            a.src = h->layout(h->mc, h->vc);
-            a.pmask = h->am[h->mc].p;
-            a.copy_only = 1;
-            a.trim = h->trim;
-            a.gamma = h->gamma;
-            a.out_count = h->cnt.p;
-            const int mo = other_of(h->mc, h->mc), vo = other_of(h->vc, h->vc);
-            a.out_vals = h->vals[vo].p;
-            a.out_amask = h->am[mo].p;
-            a.out_smask = h->sm[mo].p;
-            launch_norm(*h, a);
-            h->mc = mo;
-            h->vc = vo;
-        }
+        relayout(*h, h->am[h->mc].p, 0, h->trim);  // Trim (records per-leaf counts)
         prune_compact(*h);
         end_intr(*h);
         h->sync();
     });
 }
 
+// LevelSetTracker::dilate (tools/LevelSetTracker.h:317-337): per iteration a
+// NN_FACE dilation, the background grows by dx, and (normCount > 0) the
+// newly activated voxels are renormalised with the others held fixed.
 int gbls_dilate(gbls_handle* h, int iterations) {
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
+        if (h->norm_count > 0) check_scheme(h->tr_spatial, h->tr_temporal);
+        const float dx = float(h->voxel_size);
         for (int i = 0; i < iterations; ++i) {
             dilate_topology(*h);
-            if (h->nleaf == 0) break;
-            NormArgs a{};
-            a.nleaf = h->nleaf;
-            a.slot = h->S();
-            a.nbr = h->nbr.p;
-            a.src = h->layout(h->mc, h->vc);
-            a.pmask = h->dmask.p;
-            a.copy_only = 1;
-            a.gamma = h->gamma;
-            a.out_count = h->cnt.p;
-            const int mo = other_of(h->mc, h->mc), vo = other_of(h->vc, h->vc);
-            a.out_vals = h->vals[vo].p;
-            a.out_amask = h->am[mo].p;
-            a.out_smask = h->sm[mo].p;
-            launch_norm(*h, a);
-            h->mc = mo;
-            h->vc = vo;
+            const int m_old = h->mc;
+            relayout(*h, h->dmask.p, 0, 0);  // new voxels active with their old values
+            h->gamma = dx + h->gamma;         // changeLevelSetBackground(mDx + background)
+            h->nactive = -1;
+            if (h->norm_count > 0 && h->nleaf > 0) {
+                k_andnot<<<blocks_for(h->nleaf * 8, 256), 256, 0, h->stream>>>(h->nleaf, h->S(), h->dmask.p,
+                                                                                h->am[m_old].p);
+                ++h->stats.kernel_launches;
+                CU(cudaGetLastError());
+                normalize_pass(*h, h->dmask.p, 0, 1);
+            }
         }
         h->sync();
     });
 }
 
+// LevelSetTracker::erode (tools/LevelSetTracker.h:339-349): NN_FACE erosion,
+// pruneLevelSet, then the background shrinks by iterations * dx.
 int gbls_erode(gbls_handle* h, int iterations) {
-    (void)iterations;
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
-    g_last_error = "erode is not implemented on the device path";
-    return GBLS_ERR_UNSUPPORTED;
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (iterations > 0 && h->nleaf > 0) {
+            const uint64_t* in = h->am[h->mc].p;
+            uint64_t* bufs[2] = {h->dmask.p, h->emask.p};
+            for (int i = 0; i < iterations; ++i) {
+                uint64_t* out = bufs[i & 1];
+                k_erode<<<blocks_for(h->nleaf * 8, 256), 256, 0, h->stream>>>(h->nleaf, h->S(), h->nbr.p, in, out);
+                ++h->stats.kernel_launches;
+                CU(cudaGetLastError());
+                in = out;
+            }
+            relayout(*h, in, 0, 0);
+        } else if (h->nleaf > 0) {
+            relayout(*h, h->am[h->mc].p, 1, 0);
+        }
+        prune_compact(*h);
+        h->gamma = h->gamma - float(iterations) * float(h->voxel_size);
+        h->sync();
+    });
 }
 
+// LevelSetTracker::resize (tools/LevelSetTracker.h:351-364).
 int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
-    (void)half_width;
     if (changed) *changed = 0;
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
-    g_last_error = "resize is not implemented on the device path";
-    return GBLS_ERR_UNSUPPORTED;
+    const int w_old = int(std::floor(h->gamma / float(h->voxel_size)));
+    const int w_new = int(half_width);
+    int rc = GBLS_OK;
+    if (w_old < w_new) rc = gbls_dilate(h, w_new - w_old);
+    else if (w_old > w_new) rc = gbls_erode(h, w_old - w_new);
+    if (changed) *changed = (w_old != w_new) ? 1 : 0;
+    return rc;
+}
+
+int gbls_get_stats(gbls_handle* h, gbls_stats* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        h->sync();
+        unsigned long long acc[2] = {0, 0};
+        CU(cudaMemcpy(acc, h->acc_d, sizeof(acc), cudaMemcpyDeviceToHost));
+        *out = h->stats;
+        out->dilated_voxels = acc[0];
+        out->norm_bytes = 4.0 * double(acc[0] + acc[1]);
+        if (h->nactive < 0) h->nactive = active_count(*h);
+        out->active_voxels = h->nactive;
+        out->leaves = h->nleaf;
+    });
+}
+
+int gbls_reset_stats(gbls_handle* h) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        h->sync();
+        h->stats = gbls_stats{};
+        CU(cudaMemsetAsync(h->acc_d, 0, 2 * sizeof(unsigned long long), h->stream));
+        h->sync();
+    });
+}
+
+int gbls_set_profiling(gbls_handle* h, int enable) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        h->sync();
+        h->profiling = enable != 0;
+    });
 }
 
 int gbls_field_create(const gbls_field_desc* desc, gbls_field** out) {
@@ -1492,6 +1687,9 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             const float lim = C * dx / std::sqrt(maxv2);
             const float dt = (lim < span) ? lim : span;  // math::Min
             if (dt == 0.0f) break;
+            if (h->nactive < 0) h->nactive = active_count(*h);
+            h->stats.voxel_updates += uint64_t(h->nactive);
+            ++h->stats.substeps;
             advect_stages(*h, field, temporal, t0, dt, !forward);
             t0 += forward ? dt : -dt;
             ++count;

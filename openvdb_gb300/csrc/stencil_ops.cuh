@@ -223,6 +223,9 @@ struct NormArgs {
     int has_phi;
     int trim;               // TrimMode bits: 1 interior, 2 exterior
     int copy_only;          // 1: value = staged value (relayout / trim only)
+    int carry;              // 1: active voxels outside pmask stay active unchanged
+                            // 0: they become inactive (erosion relayout)
+    unsigned long long* acc;  // [2] += voxels processed, voxels written (may be null)
 };
 
 struct CflArgs {
@@ -280,15 +283,16 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
 }
 
 // One stage of LevelSetTracker::Normalizer::euler<N,D>
-// (tools/LevelSetTracker.h:623-676) over the voxels of pmask, optionally
+// (tools/LevelSetTracker.h:623-676) over the voxels of pmask (the masked
+// form :661-670 when `carry` keeps the other active voxels), optionally
 // followed by Trim (tools/LevelSetTracker.h:473-506), writing the result in
-// the layout of the surviving active set.
+// the layout of the surviving active set.  Voxels visited: pmask | active.
 template <class A>
 __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ float res[LEAF_VOX];
-    __shared__ uint64_t pm[8], fin[8], fsg[8], phm[8];
+    __shared__ uint64_t pm[8], um[8], fin[8], fsg[8], phm[8];
     __shared__ int ppre[9], fpre[9], phpre[9];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
@@ -298,15 +302,16 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
     load_tile(tile, st, a.src.vals, a.gamma);
     if (t < 8) {
         pm[t] = a.pmask[size_t(s) * 8 + t];
+        um[t] = pm[t] | st.am[0][t];
         fin[t] = 0;
-        fsg[t] = st.sm[0][t] & ~pm[t];
+        fsg[t] = st.sm[0][t] & ~um[t];
         if (a.has_phi) phm[t] = a.phi.amask[size_t(s) * 8 + t];
     }
     __syncthreads();
     if (t == 0) {
         int acc = 0, acc2 = 0;
         for (int w = 0; w < 8; ++w) {
-            ppre[w] = acc; acc += popc64(pm[w]);
+            ppre[w] = acc; acc += popc64(um[w]);
             phpre[w] = acc2; if (a.has_phi) acc2 += popc64(phm[w]);
         }
         ppre[8] = acc; phpre[8] = acc2;
@@ -315,10 +320,18 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
     const int n = ppre[8];
     const float g = a.gamma;
     for (int i = t; i < n; i += blockDim.x) {
-        const int v = select_voxel(pm, ppre, i);
+        const int v = select_voxel(um, ppre, i);
         const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
         const float phi0 = tile[tile_index(x, y, z)];
         float val = phi0;
+        if (!((pm[v >> 6] >> (v & 63)) & 1)) {
+            // active voxel outside the processed set
+            res[v] = val;
+            const uint64_t bit = uint64_t(1) << (v & 63);
+            if (a.carry) atomicOr(reinterpret_cast<unsigned long long*>(&fin[v >> 6]), (unsigned long long)bit);
+            if (val < 0.0f) atomicOr(reinterpret_cast<unsigned long long*>(&fsg[v >> 6]), (unsigned long long)bit);
+            continue;
+        }
         if (!a.copy_only) {
             float up[3], down[3];
 #pragma unroll
@@ -366,7 +379,15 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         a.out_amask[size_t(s) * 8 + t] = fin[t];
         a.out_smask[size_t(s) * 8 + t] = fsg[t];
     }
-    if (t == 0 && a.out_count) a.out_count[l] = nf;
+    if (t == 0) {
+        if (a.out_count) a.out_count[l] = nf;
+        if (a.acc) {
+            int np = 0;
+            for (int w = 0; w < 8; ++w) np += popc64(pm[w]);
+            atomicAdd(a.acc, (unsigned long long)np);
+            atomicAdd(a.acc + 1, (unsigned long long)nf);
+        }
+    }
 }
 
 // Max of |v|^2 over the active voxels (LevelSetAdvection::Advect::sampleField,

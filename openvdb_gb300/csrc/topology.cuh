@@ -15,6 +15,7 @@ struct DevStatus {
     unsigned long long error;          // device-side consistency check failures
     unsigned int max_v2_bits;          // CFL reduction
     unsigned int pad;
+    unsigned long long n_active;       // active voxels of the kept leaves
 };
 
 // Face layer of a leaf mask that a missing neighbour on face f would receive.

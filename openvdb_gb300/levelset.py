@@ -101,6 +101,17 @@ class DeviceLevelSet:
     def set_stream(self, stream_ptr):
         _call(lib().gbls_set_stream(self._h, C.c_void_p(stream_ptr)))
 
+    def stats(self):
+        st = _abi.Stats()
+        _call(lib().gbls_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _abi.Stats._fields_}
+
+    def reset_stats(self):
+        _call(lib().gbls_reset_stats(self._h))
+
+    def set_profiling(self, enable=True):
+        _call(lib().gbls_set_profiling(self._h, 1 if enable else 0))
+
 
 class DeviceField:
     """A velocity field uploaded to the GPU (gbls_field)."""
