@@ -227,6 +227,17 @@ int gbls_get_stats(gbls_handle* h, gbls_stats* out);
 int gbls_reset_stats(gbls_handle* h);
 int gbls_set_profiling(gbls_handle* h, int enable);
 
+/* ---- allocation-free active-voxel count ----------------------------------
+ * No counterpart in the reference (its trees live in host memory).
+ * Returns in *out the same count as gbls_get_counts' active_voxel_count, but
+ * allocates no device memory: for host applications that give the library a
+ * fixed device-memory budget and forbid allocations afterwards.  Scratch is a
+ * 512 KiB static device array (at most 2,097,152 leaves; larger grids are
+ * rejected with GBLS_ERR_INVALID_ARGUMENT).  The first call on each device
+ * looks up that array's device address and should precede any stream
+ * capture.  Calls that overlap on the GPU share the array and race.        */
+int gbls_count_active_noalloc(gbls_handle* h, int64_t* out);
+
 /* ---- host construction of level sets ------------------------------------
  * gbls_host_sphere replaces tools::createLevelSetSphere
  * (tools/LevelSetSphere.h:219-230): same rasterisation, background and

@@ -1623,6 +1623,29 @@ int gbls_set_profiling(gbls_handle* h, int enable) {
     });
 }
 
+}  // extern "C"
+
+namespace gbls {
+int noalloc_count_active(int device, int64_t nleaf, const int32_t* slot, const uint64_t* am,
+                         cudaStream_t stream, int64_t* out, std::string* err);
+}
+
+extern "C" {
+
+// Active-voxel count that allocates nothing (see noalloc.cu for the scratch
+// array, its size limit and its set-up).  Same result as the
+// active_voxel_count of gbls_get_counts.
+int gbls_count_active_noalloc(gbls_handle* h, int64_t* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        std::string err;
+        const int rc = gbls::noalloc_count_active(h->device, h->nleaf, h->S(), h->am[h->mc].p, h->stream, out, &err);
+        if (rc == 1) fail(GBLS_ERR_INVALID_ARGUMENT, err);
+        if (rc != 0) fail(GBLS_ERR_CUDA, err);
+    });
+}
+
 int gbls_field_create(const gbls_field_desc* desc, gbls_field** out) {
     if (!desc || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     *out = nullptr;
