@@ -350,6 +350,8 @@ struct gbls_field {
     gbls_field_desc desc{};
     int device = 0;
     DevArray<float> dense;
+    DevArray<float> tab;  // DEFORMATION: sin(pi i/domain), sin(2 pi i/domain) per coordinate
+    int tab_lo = 0, tab_n = 0;
 };
 
 struct gbls_handle {
@@ -989,8 +991,15 @@ void check_scheme(int spatial, int temporal) {
         fail(GBLS_ERR_UNSUPPORTED, "the device path implements the HJWENO5_BIAS spatial scheme");
 }
 
-FieldParams field_params(const gbls_field* f) {
+FieldParams field_params(const gbls_field* f, float t) {
     FieldParams p{};
+    if (f->desc.kind == GBLS_FIELD_DEFORMATION && f->tab_n > 0) {
+        p.tab = f->tab.p;
+        p.tab_lo = f->tab_lo;
+        p.tab_n = f->tab_n;
+        // the amplitude factor of gbls_deformation, same float operations
+        p.amp = gbls_cospi(f->desc.domain == 0.0f ? 0.0f : t / f->desc.period) * f->desc.scale;
+    }
     const gbls_field_desc& d = f->desc;
     p.kind = d.kind;
     for (int i = 0; i < 3; ++i) {
@@ -1021,7 +1030,7 @@ float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
     a.slot = h.S();
     a.amask = h.am[h.mc].p;
     a.t0 = t;
-    a.field = field_params(f);
+    a.field = field_params(f, t);
     a.max_bits = &h.st_d->max_v2_bits;
     launch_cfl(a, h.stream);
     ++h.stats.kernel_launches;
@@ -1065,7 +1074,7 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
     base.t0 = t0;
     base.backward = backward ? 1 : 0;
     base.invdx = 1.0 / h.voxel_size;
-    base.field = field_params(f);
+    base.field = field_params(f, t0);
     const int a0 = h.vc, b0 = (h.vc + 1) % 3, c0 = (h.vc + 2) % 3;
     auto stage = [&](int src, int phin, int out, float alpha, int has_phi, const char* msg) {
         RkArgs a = base;
@@ -1664,8 +1673,24 @@ int gbls_field_create(const gbls_field_desc* desc, gbls_field** out) {
             CU(cudaStreamSynchronize(nullptr));
         }
         f->desc.dense_values = nullptr;
-        if (desc->kind == GBLS_FIELD_DEFORMATION && !(desc->domain > 0.0f && desc->period != 0.0f))
-            fail(GBLS_ERR_VALUE, "deformation field needs domain > 0 and period != 0");
+        if (desc->kind == GBLS_FIELD_DEFORMATION) {
+            if (!(desc->domain > 0.0f && desc->period != 0.0f))
+                fail(GBLS_ERR_VALUE, "deformation field needs domain > 0 and period != 0");
+            // per-coordinate sine tables over [-8192, domain + 8192): entries are
+            // computed with the same functions as the direct evaluation
+            const int lo = -8192;
+            const int n = int(std::min(1.0e6f, std::ceil(desc->domain))) + 2 * 8192;
+            std::vector<float> tab(size_t(n) * 2);
+            for (int q = 0; q < n; ++q) {
+                const float x = float(lo + q) / desc->domain;
+                tab[size_t(q) * 2] = gbls_sinpi(x);
+                tab[size_t(q) * 2 + 1] = gbls_sinpi(x * 2.0f);
+            }
+            f->tab.upload(tab.data(), tab.size(), nullptr);
+            CU(cudaStreamSynchronize(nullptr));
+            f->tab_lo = lo;
+            f->tab_n = n;
+        }
     });
     if (rc != GBLS_OK) {
         delete f;

@@ -179,77 +179,103 @@ struct LeafStage {
     int slot[7];
 };
 
-// Stage masks for a leaf (slot s, neighbours nb[6]) from layout L.
-// Must be called by all threads of the CTA; ends with a barrier.
-__device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const int32_t* nb) {
+// Stencil kernels run one leaf per CTA of STAGE_THREADS threads: thread t
+// owns bit t of every 64-bit mask word, so the staging below is straight-line
+// code with every load independent.
+constexpr int STAGE_THREADS = 64;
+
+// Stage the masks of a leaf (slot s) and of its face neighbours nb[6] from
+// layout L, with per-word prefix counts.  Threads 56..63 load pm[8] (the
+// processed-voxel mask of the centre) when pmask is given.  Ends with a
+// barrier.
+__device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const int32_t* nb,
+                                   const uint64_t* pmask, uint64_t* pm) {
     const int t = threadIdx.x;
-    if (t < 7) st.slot[t] = (t == 0) ? s : nb[t - 1];
-    __syncthreads();
+    uint64_t c = 0;
     if (t < 56) {
         const int r = t >> 3, w = t & 7;
-        const int sl = st.slot[r];
+        const int sl = (r == 0) ? s : nb[r - 1];
+        uint64_t a, g;
         if (sl >= 0) {
-            st.am[r][w] = L.amask[size_t(sl) * 8 + w];
-            st.sm[r][w] = L.smask[size_t(sl) * 8 + w];
+            a = L.amask[size_t(sl) * 8 + w];
+            g = L.smask[size_t(sl) * 8 + w];
         } else {
-            st.am[r][w] = 0;
-            st.sm[r][w] = (sl == NBR_TILE_NEG) ? ~uint64_t(0) : uint64_t(0);
+            a = 0;
+            g = (sl == NBR_TILE_NEG) ? ~uint64_t(0) : uint64_t(0);
         }
+        st.am[r][w] = a;
+        st.sm[r][w] = g;
+        if (w == 0) st.slot[r] = sl;
+        c = uint64_t(__popcll(a));
+    } else if (pmask) {
+        pm[t - 56] = pmask[size_t(s) * 8 + (t - 56)];
     }
-    __syncthreads();
-    if (t < 7) {
-        int acc = 0;
-        for (int w = 0; w < 8; ++w) {
-            st.pre[t][w] = acc;
-            acc += popc64(st.am[t][w]);
-        }
-        st.pre[t][8] = acc;
+    // inclusive scan of the popcounts within each group of 8 lanes
+    uint32_t v = uint32_t(c);
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, d, 8);
+        if ((t & 7) >= d) v += u;
+    }
+    if (t < 56) {
+        const int r = t >> 3, w = t & 7;
+        st.pre[r][w + 1] = int(v);
+        if (w == 0) st.pre[r][0] = 0;
     }
     __syncthreads();
 }
 
-// Value of voxel v of staged leaf r (0 = centre, 1..6 = faces).
-__device__ __forceinline__ float staged_value(const LeafStage& st, const float* vals, int r, int v,
-                                              float gamma) {
-    const int w = v >> 6, b = v & 63;
+__device__ __forceinline__ float staged_load(const LeafStage& st, const float* vals, int r, int w,
+                                             int b, float gamma) {
     const uint64_t m = st.am[r][w];
     if ((m >> b) & 1) {
-        const int rank = st.pre[r][w] + popc64(m & ((uint64_t(1) << b) - 1));
+        const int rank = st.pre[r][w] + __popcll(m & ((uint64_t(1) << b) - 1));
         return __ldg(vals + size_t(st.slot[r]) * LEAF_VOX + rank);
     }
     return ((st.sm[r][w] >> b) & 1) ? -gamma : gamma;
 }
 
-// Fill the 14^3 tile (centre + face slabs) from staged masks.
+// Fill the 14^3 tile (centre block + three-voxel face slabs).  Thread t
+// handles bit t of each centre word and the (t>>3, t&7) column of every slab
+// layer; all 26 loads of a thread are independent.  Requires
+// blockDim.x == STAGE_THREADS.  No barrier at the end.
 __device__ inline void load_tile(float* tile, const LeafStage& st, const float* vals, float gamma) {
-    for (int p = threadIdx.x; p < TILE_POINTS; p += blockDim.x) {
-        int r, x, y, z, nx, ny, nz;
-        if (p < 512) {
-            r = 0;
-            x = p >> 6; y = (p >> 3) & 7; z = p & 7;
-            nx = x; ny = y; nz = z;
-        } else {
-            const int q = p - 512;
-            const int f = q / 192, e = q - f * 192;
-            r = f + 1;
-            // e enumerates a 3 x 8 x 8 slab: depth d (0..2), then the two in-plane axes.
-            const int d = e >> 6, a = (e >> 3) & 7, c = e & 7;
-            switch (f) {
-            case 0: x = -3 + d; y = a; z = c; nx = x + 8; ny = y; nz = z; break;
-            case 1: x = 8 + d;  y = a; z = c; nx = x - 8; ny = y; nz = z; break;
-            case 2: x = a; y = -3 + d; z = c; nx = x; ny = y + 8; nz = z; break;
-            case 3: x = a; y = 8 + d;  z = c; nx = x; ny = y - 8; nz = z; break;
-            case 4: x = a; y = c; z = -3 + d; nx = x; ny = y; nz = z + 8; break;
-            default: x = a; y = c; z = 8 + d; nx = x; ny = y; nz = z - 8; break;
-            }
-        }
-        tile[tile_index(x, y, z)] = staged_value(st, vals, r, (nx << 6) | (ny << 3) | nz, gamma);
+    const int t = threadIdx.x;
+    const int a = t >> 3, c = t & 7;
+    float cv[8], fv[18];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) cv[k] = staged_load(st, vals, 0, k, t, gamma);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        fv[0 * 3 + d] = staged_load(st, vals, 1, 5 + d, t, gamma);                 // -x: (5+d, a, c)
+        fv[1 * 3 + d] = staged_load(st, vals, 2, d, t, gamma);                     // +x: (d, a, c)
+        fv[2 * 3 + d] = staged_load(st, vals, 3, a, ((5 + d) << 3) | c, gamma);    // -y: (a, 5+d, c)
+        fv[3 * 3 + d] = staged_load(st, vals, 4, a, (d << 3) | c, gamma);          // +y: (a, d, c)
+        fv[4 * 3 + d] = staged_load(st, vals, 5, a, (c << 3) | (5 + d), gamma);    // -z: (a, c, 5+d)
+        fv[5 * 3 + d] = staged_load(st, vals, 6, a, (c << 3) | d, gamma);          // +z: (a, c, d)
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) tile[tile_index(k, a, c)] = cv[k];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        tile[tile_index(-3 + d, a, c)] = fv[0 * 3 + d];
+        tile[tile_index(8 + d, a, c)] = fv[1 * 3 + d];
+        tile[tile_index(a, -3 + d, c)] = fv[2 * 3 + d];
+        tile[tile_index(a, 8 + d, c)] = fv[3 * 3 + d];
+        tile[tile_index(a, c, -3 + d)] = fv[4 * 3 + d];
+        tile[tile_index(a, c, 8 + d)] = fv[5 * 3 + d];
     }
 }
 
 // ---- velocity fields (device form of gbls_field_desc) -------------------
 struct FieldParams {
     int kind;
+    // DEFORMATION: per-coordinate tables tab[2*(i-tab_lo)] = sin(pi i/domain),
+    // tab[2*(i-tab_lo)+1] = sin(2 pi i/domain) (same function as the direct
+    // evaluation, so identical bits) and the per-substep amplitude.
+    const float* tab;
+    int tab_lo, tab_n;
+    float amp;
     float constant[3];
     int dense_origin[3];
     int dense_dims[3];

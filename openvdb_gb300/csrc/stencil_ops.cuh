@@ -183,9 +183,24 @@ __device__ __forceinline__ void eval_field(const FieldParams& f, int i, int j, i
         }
         break;
     }
-    case 2:  // GBLS_FIELD_DEFORMATION
-        gbls_deformation(i, j, k, t, f.domain, f.period, f.scale, out);
+    case 2: {  // GBLS_FIELD_DEFORMATION
+        const unsigned ia = unsigned(i - f.tab_lo), ja = unsigned(j - f.tab_lo), ka = unsigned(k - f.tab_lo);
+        if (f.tab && ia < unsigned(f.tab_n) && ja < unsigned(f.tab_n) && ka < unsigned(f.tab_n)) {
+            // gbls_deformation with its sines read from the per-coordinate tables
+            const float sx = f.tab[2 * ia], s2x = f.tab[2 * ia + 1];
+            const float sy = f.tab[2 * ja], s2y = f.tab[2 * ja + 1];
+            const float sz = f.tab[2 * ka], s2z = f.tab[2 * ka + 1];
+            const float u = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, sx), sx), s2y), s2z);
+            const float v = __fmul_rn(__fmul_rn(__fmul_rn(s2x, sy), sy), s2z);
+            const float w = __fmul_rn(__fmul_rn(__fmul_rn(s2x, s2y), sz), sz);
+            out[0] = __fmul_rn(u, f.amp);
+            out[1] = -__fmul_rn(v, f.amp);
+            out[2] = -__fmul_rn(w, f.amp);
+        } else {
+            gbls_deformation(i, j, k, t, f.domain, f.period, f.scale, out);
+        }
         break;
+    }
     default:  // GBLS_FIELD_ROTATION
         gbls_rotation(i, j, k, f.constant, f.omega, f.center, out);
         break;
@@ -239,7 +254,22 @@ struct CflArgs {
 };
 
 // ---- kernels ----------------------------------------------------------------
-constexpr int STENCIL_THREADS = 128;
+constexpr int STENCIL_THREADS = STAGE_THREADS;
+
+// list[rank] = voxel for every set bit of m[8] (thread t handles bit t of
+// each word); returns the number of set bits.
+__device__ __forceinline__ int build_list(uint16_t* list, const uint64_t* m) {
+    const int t = threadIdx.x;
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    int base = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t w = m[k];
+        if ((w >> t) & 1) list[base + __popcll(w & low)] = uint16_t((k << 6) | t);
+        base += __popcll(w);
+    }
+    return base;
+}
 
 // One TVD-RK stage of LevelSetAdvection::Advect::euler<N,D>
 // (tools/LevelSetAdvect.h:543-572): for every active voxel
@@ -249,17 +279,18 @@ template <class A>
 __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
+    __shared__ uint16_t list[LEAF_VOX];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
-    stage_masks(st, a.src, s, a.nbr + 6 * l);
+    stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
     load_tile(tile, st, a.src.vals, a.gamma);
+    const int n = build_list(list, st.am[0]);
     __syncthreads();
     int ox, oy, oz;
     key_origin(a.keys[l], ox, oy, oz);
-    const int n = st.pre[0][8];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int v = select_voxel(st.am[0], st.pre[0], i);
+    for (int i = threadIdx.x; i < n; i += STENCIL_THREADS) {
+        const int v = list[i];
         const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
         float vel[3];
         eval_field(a.field, ox + x, oy + y, oz + z, a.t0, vel);
@@ -292,42 +323,33 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ float res[LEAF_VOX];
+    __shared__ uint16_t list[LEAF_VOX];
     __shared__ uint64_t pm[8], um[8], fin[8], fsg[8], phm[8];
-    __shared__ int ppre[9], fpre[9], phpre[9];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
     const int t = threadIdx.x;
-    stage_masks(st, a.src, s, a.nbr + 6 * l);
-    load_tile(tile, st, a.src.vals, a.gamma);
+    stage_masks(st, a.src, s, a.nbr + 6 * l, a.pmask, pm);
     if (t < 8) {
-        pm[t] = a.pmask[size_t(s) * 8 + t];
         um[t] = pm[t] | st.am[0][t];
         fin[t] = 0;
         fsg[t] = st.sm[0][t] & ~um[t];
         if (a.has_phi) phm[t] = a.phi.amask[size_t(s) * 8 + t];
     }
+    load_tile(tile, st, a.src.vals, a.gamma);
     __syncthreads();
-    if (t == 0) {
-        int acc = 0, acc2 = 0;
-        for (int w = 0; w < 8; ++w) {
-            ppre[w] = acc; acc += popc64(um[w]);
-            phpre[w] = acc2; if (a.has_phi) acc2 += popc64(phm[w]);
-        }
-        ppre[8] = acc; phpre[8] = acc2;
-    }
+    const int n = build_list(list, um);
     __syncthreads();
-    const int n = ppre[8];
     const float g = a.gamma;
-    for (int i = t; i < n; i += blockDim.x) {
-        const int v = select_voxel(um, ppre, i);
+    for (int i = t; i < n; i += STENCIL_THREADS) {
+        const int v = list[i];
         const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
         const float phi0 = tile[tile_index(x, y, z)];
         float val = phi0;
-        if (!((pm[v >> 6] >> (v & 63)) & 1)) {
+        const uint64_t bit = uint64_t(1) << (v & 63);
+        if (!(pm[v >> 6] & bit)) {
             // active voxel outside the processed set
             res[v] = val;
-            const uint64_t bit = uint64_t(1) << (v & 63);
             if (a.carry) atomicOr(reinterpret_cast<unsigned long long*>(&fin[v >> 6]), (unsigned long long)bit);
             if (val < 0.0f) atomicOr(reinterpret_cast<unsigned long long*>(&fsg[v >> 6]), (unsigned long long)bit);
             continue;
@@ -347,7 +369,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
                 const int w = v >> 6, b = v & 63;
                 float p;
                 if ((phm[w] >> b) & 1) {
-                    p = a.phi.vals[size_t(s) * LEAF_VOX + phpre[w] + popc64(phm[w] & ((uint64_t(1) << b) - 1))];
+                    int rank = __popcll(phm[w] & (bit - 1));
+                    for (int k = 0; k < w; ++k) rank += __popcll(phm[k]);
+                    p = a.phi.vals[size_t(s) * LEAF_VOX + rank];
                 } else {
                     p = ((a.phi.smask[size_t(s) * 8 + w] >> b) & 1) ? -g : g;
                 }
@@ -356,36 +380,33 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
             val = vv;
         }
         bool act = true, neg = val < 0.0f;
-        if ((a.trim & 1) && val <= -g) { act = false; neg = true; val = -g; }
-        else if ((a.trim & 2) && val >= g) { act = false; neg = false; val = g; }
+        if ((a.trim & 1) && val <= -g) { act = false; neg = true; }
+        else if ((a.trim & 2) && val >= g) { act = false; neg = false; }
         res[v] = val;
-        const uint64_t bit = uint64_t(1) << (v & 63);
         if (act) atomicOr(reinterpret_cast<unsigned long long*>(&fin[v >> 6]), (unsigned long long)bit);
         if (neg) atomicOr(reinterpret_cast<unsigned long long*>(&fsg[v >> 6]), (unsigned long long)bit);
     }
     __syncthreads();
-    if (t == 0) {
-        int acc = 0;
-        for (int w = 0; w < 8; ++w) { fpre[w] = acc; acc += popc64(fin[w]); }
-        fpre[8] = acc;
-    }
-    __syncthreads();
-    const int nf = fpre[8];
-    for (int i = t; i < nf; i += blockDim.x) {
-        const int v = select_voxel(fin, fpre, i);
-        a.out_vals[size_t(s) * LEAF_VOX + i] = res[v];
+    // packed output in the layout of fin: thread t writes bit t of each word
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    int base = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t w = fin[k];
+        if ((w >> t) & 1) a.out_vals[size_t(s) * LEAF_VOX + base + __popcll(w & low)] = res[(k << 6) | t];
+        base += __popcll(w);
     }
     if (t < 8) {
         a.out_amask[size_t(s) * 8 + t] = fin[t];
         a.out_smask[size_t(s) * 8 + t] = fsg[t];
     }
     if (t == 0) {
-        if (a.out_count) a.out_count[l] = nf;
+        if (a.out_count) a.out_count[l] = base;
         if (a.acc) {
             int np = 0;
-            for (int w = 0; w < 8; ++w) np += popc64(pm[w]);
+            for (int w = 0; w < 8; ++w) np += __popcll(pm[w]);
             atomicAdd(a.acc, (unsigned long long)np);
-            atomicAdd(a.acc + 1, (unsigned long long)nf);
+            atomicAdd(a.acc + 1, (unsigned long long)base);
         }
     }
 }
