@@ -250,13 +250,17 @@ __global__ void k_prune_scatter(int64_t n, const uint64_t* keys, const int32_t* 
                                 const int32_t* cnt, unsigned long long* nactive,
                                 unsigned long long* nkept, unsigned long long* err) {
     const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    // active voxels of the kept leaves: warp sum, one atomic per warp
+    // (blockDim is a multiple of 32, every lane takes part)
+    unsigned long long c = (l < n && keep[l]) ? (unsigned long long)cnt[l] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(nactive, c);
     if (l >= n) return;
     const int64_t k = idx[l];
     if (l == n - 1) *nkept = (unsigned long long)(k + keep[l]);
     if (keep[l]) {
         ko[k] = keys[l];
         so[k] = slot[l];
-        atomicAdd(nactive, (unsigned long long)cnt[l]);
         return;
     }
     const int s = slot[l];

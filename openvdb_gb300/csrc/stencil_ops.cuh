@@ -133,6 +133,20 @@ __device__ __forceinline__ Line7 tile_line(const float* tile, int x, int y, int 
     return L;
 }
 
+// The upwind derivative V<0 ? FD : BD with a single WENO5 evaluation: FD
+// reads the line mirrored (a_k = S[3-k], k=-3..2 -> v[6-k]) with the same
+// difference pattern as BD (a_k = v[k]), and BD negates the result.  Same
+// operations on the same operands as hj_fd / hj_bd.
+template <class A>
+__device__ __forceinline__ float line_upwind(const Line7& L, bool fd) {
+    float a[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = fd ? L.v[6 - k] : L.v[k];
+    const float w = A::weno5(A::sub(a[0], a[1]), A::sub(a[1], a[2]), A::sub(a[2], a[3]),
+                             A::sub(a[3], a[4]), A::sub(a[4], a[5]));
+    return fd ? w : -w;
+}
+
 template <class A>
 __device__ __forceinline__ float line_fd(const Line7& L) {
     return hj_fd<A>(L.v[1], L.v[2], L.v[3], L.v[4], L.v[5], L.v[6]);
@@ -299,7 +313,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             const Line7 L = tile_line(tile, x, y, z, ax);
-            g[ax] = A::ijt(vel[ax] < 0.0f ? line_fd<A>(L) : line_bd<A>(L), a.invdx);
+            g[ax] = A::ijt(line_upwind<A>(L, vel[ax] < 0.0f), a.invdx);
         }
         const float dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
         const float c = tile[tile_index(x, y, z)];
@@ -324,7 +338,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
     __shared__ LeafStage st;
     __shared__ float res[LEAF_VOX];
     __shared__ uint16_t list[LEAF_VOX];
+    __shared__ uint8_t flag[LEAF_VOX];  // bit 0: active after the pass, bit 1: negative
     __shared__ uint64_t pm[8], um[8], fin[8], fsg[8], phm[8];
+    __shared__ uint32_t half[2][2][8];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
@@ -350,8 +366,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         if (!(pm[v >> 6] & bit)) {
             // active voxel outside the processed set
             res[v] = val;
-            if (a.carry) atomicOr(reinterpret_cast<unsigned long long*>(&fin[v >> 6]), (unsigned long long)bit);
-            if (val < 0.0f) atomicOr(reinterpret_cast<unsigned long long*>(&fsg[v >> 6]), (unsigned long long)bit);
+            flag[v] = uint8_t((a.carry ? 1 : 0) | (val < 0.0f ? 2 : 0));
             continue;
         }
         if (!a.copy_only) {
@@ -383,8 +398,29 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         if ((a.trim & 1) && val <= -g) { act = false; neg = true; }
         else if ((a.trim & 2) && val >= g) { act = false; neg = false; }
         res[v] = val;
-        if (act) atomicOr(reinterpret_cast<unsigned long long*>(&fin[v >> 6]), (unsigned long long)bit);
-        if (neg) atomicOr(reinterpret_cast<unsigned long long*>(&fsg[v >> 6]), (unsigned long long)bit);
+        flag[v] = uint8_t((act ? 1 : 0) | (neg ? 2 : 0));
+    }
+    __syncthreads();
+    // gather the flags of the visited voxels into the output masks with ballots
+    {
+        const int w = t >> 5, lane = t & 31;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int v = (k << 6) | t;
+            const bool vis = (um[k] >> t) & 1;
+            const uint8_t f = vis ? flag[v] : uint8_t(0);
+            const uint32_t ba = __ballot_sync(0xffffffffu, f & 1);
+            const uint32_t bn = __ballot_sync(0xffffffffu, (f >> 1) & 1);
+            if (lane == 0) {
+                half[0][w][k] = ba;
+                half[1][w][k] = bn;
+            }
+        }
+    }
+    __syncthreads();
+    if (t < 8) {
+        fin[t] = uint64_t(half[0][0][t]) | (uint64_t(half[0][1][t]) << 32);
+        fsg[t] |= uint64_t(half[1][0][t]) | (uint64_t(half[1][1][t]) << 32);
     }
     __syncthreads();
     // packed output in the layout of fin: thread t writes bit t of each word
