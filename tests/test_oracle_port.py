@@ -1,0 +1,55 @@
+"""The oracle's C++ restatement against the reference's golden digests (CPU)."""
+import json
+import os
+
+import pytest
+
+from cases import CASES, make_field, make_fixture
+from openvdb_gb300.grid import digest, summary
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = json.load(open(os.path.join(HERE, "golden", "parity_cases.json")))
+
+port = pytest.importorskip("oracle.port")
+if not port.available():
+    pytest.skip("oracle port not built", allow_module_level=True)
+
+
+def run_port(name, threads=0):
+    case, gold = CASES[name], GOLD[name]
+    host = make_fixture(case["fixture"])
+    g = port.PortGrid(host, threads)
+    field = make_field(case["field"])
+    sp, tp, tsp, ttp, nc = case["schemes"]
+    trim = 3
+    for step, (op, rec) in enumerate(zip(case["ops"], gold[1:]), start=1):
+        if op[0] == "state":
+            s = op[1]
+            nc = s.get("norm_count", nc)
+            ttp = s.get("tr_temporal", ttp)
+            trim = s.get("trim", trim)
+            continue
+        kw = dict(spatial=tsp, temporal=ttp, norm_count=nc, trim=trim)
+        if op[0] == "advect":
+            n = g.advect(field, op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp,
+                         tracker_temporal=ttp, norm_count=nc)
+            assert n == rec["count"], (name, step, n, rec["count"])
+        elif op[0] == "track":
+            g.track(**kw)
+        elif op[0] == "normalize":
+            g.normalize(**kw)
+        elif op[0] == "prune":
+            g.prune(**kw)
+        elif op[0] == "dilate":
+            g.dilate(op[1], **kw)
+        h = g.to_host()
+        assert digest(h) == rec["digest"], (name, step, op, summary(h), rec["summary"])
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_port_matches_reference(name):
+    run_port(name)
+
+
+def test_port_thread_independent():
+    run_port("sphere20_deformation", threads=1)
