@@ -1078,6 +1078,7 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
     base.t0 = t0;
     base.backward = backward ? 1 : 0;
     base.invdx = 1.0 / h.voxel_size;
+    base.invdx_f = float(1.0 / h.voxel_size);
     base.field = field_params(f, t0);
     const int a0 = h.vc, b0 = (h.vc + 1) % 3, c0 = (h.vc + 2) % 3;
     auto stage = [&](int src, int phin, int out, float alpha, int has_phi, const char* msg) {

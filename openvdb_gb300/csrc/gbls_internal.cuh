@@ -176,6 +176,8 @@ struct LeafStage {
     uint64_t am[7][8];
     uint64_t sm[7][8];
     int pre[7][9];
+    int preh[7][16];       // rank of the first voxel of each 32-bit half word
+    const float* vp[7];    // packed values of each staged leaf (null for a tile)
     int slot[7];
 };
 
@@ -185,13 +187,13 @@ struct LeafStage {
 constexpr int STAGE_THREADS = 64;
 
 // Stage the masks of a leaf (slot s) and of its face neighbours nb[6] from
-// layout L, with per-word prefix counts.  Threads 56..63 load pm[8] (the
-// processed-voxel mask of the centre) when pmask is given.  Ends with a
-// barrier.
+// layout L, with per-word and per-half-word prefix counts.  Threads 56..63
+// load pm[8] (the processed-voxel mask of the centre) when pmask is given.
+// Ends with a barrier.
 __device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const int32_t* nb,
                                    const uint64_t* pmask, uint64_t* pm) {
     const int t = threadIdx.x;
-    uint64_t c = 0;
+    uint32_t clo = 0, c = 0;
     if (t < 56) {
         const int r = t >> 3, w = t & 7;
         const int sl = (r == 0) ? s : nb[r - 1];
@@ -205,13 +207,17 @@ __device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const 
         }
         st.am[r][w] = a;
         st.sm[r][w] = g;
-        if (w == 0) st.slot[r] = sl;
-        c = uint64_t(__popcll(a));
+        if (w == 0) {
+            st.slot[r] = sl;
+            st.vp[r] = sl >= 0 ? L.vals + size_t(sl) * LEAF_VOX : nullptr;
+        }
+        clo = uint32_t(__popc(uint32_t(a)));
+        c = clo + uint32_t(__popc(uint32_t(a >> 32)));
     } else if (pmask) {
         pm[t - 56] = pmask[size_t(s) * 8 + (t - 56)];
     }
     // inclusive scan of the popcounts within each group of 8 lanes
-    uint32_t v = uint32_t(c);
+    uint32_t v = c;
 #pragma unroll
     for (int d = 1; d < 8; d <<= 1) {
         const uint32_t u = __shfl_up_sync(0xffffffffu, v, d, 8);
@@ -221,38 +227,39 @@ __device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const 
         const int r = t >> 3, w = t & 7;
         st.pre[r][w + 1] = int(v);
         if (w == 0) st.pre[r][0] = 0;
+        st.preh[r][2 * w] = int(v - c);
+        st.preh[r][2 * w + 1] = int(v - c + clo);
     }
     __syncthreads();
 }
 
-__device__ __forceinline__ float staged_load(const LeafStage& st, const float* vals, int r, int w,
-                                             int b, float gamma) {
-    const uint64_t m = st.am[r][w];
-    if ((m >> b) & 1) {
-        const int rank = st.pre[r][w] + __popcll(m & ((uint64_t(1) << b) - 1));
-        return __ldg(vals + size_t(st.slot[r]) * LEAF_VOX + rank);
-    }
-    return ((st.sm[r][w] >> b) & 1) ? -gamma : gamma;
+// Value of bit b of word w of staged leaf r (packed value, else +-gamma).
+__device__ __forceinline__ float staged_load(const LeafStage& st, int r, int w, int b, float gamma) {
+    const int h = b >> 5, bb = b & 31;
+    const uint32_t m = reinterpret_cast<const uint32_t*>(&st.am[r][w])[h];
+    if ((m >> bb) & 1) return __ldg(st.vp[r] + st.preh[r][2 * w + h] + __popc(m & ((1u << bb) - 1u)));
+    const uint32_t g = reinterpret_cast<const uint32_t*>(&st.sm[r][w])[h];
+    return ((g >> bb) & 1) ? -gamma : gamma;
 }
 
 // Fill the 14^3 tile (centre block + three-voxel face slabs).  Thread t
 // handles bit t of each centre word and the (t>>3, t&7) column of every slab
 // layer; all 26 loads of a thread are independent.  Requires
 // blockDim.x == STAGE_THREADS.  No barrier at the end.
-__device__ inline void load_tile(float* tile, const LeafStage& st, const float* vals, float gamma) {
+__device__ inline void load_tile(float* tile, const LeafStage& st, float gamma) {
     const int t = threadIdx.x;
     const int a = t >> 3, c = t & 7;
     float cv[8], fv[18];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) cv[k] = staged_load(st, vals, 0, k, t, gamma);
+    for (int k = 0; k < 8; ++k) cv[k] = staged_load(st, 0, k, t, gamma);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        fv[0 * 3 + d] = staged_load(st, vals, 1, 5 + d, t, gamma);                 // -x: (5+d, a, c)
-        fv[1 * 3 + d] = staged_load(st, vals, 2, d, t, gamma);                     // +x: (d, a, c)
-        fv[2 * 3 + d] = staged_load(st, vals, 3, a, ((5 + d) << 3) | c, gamma);    // -y: (a, 5+d, c)
-        fv[3 * 3 + d] = staged_load(st, vals, 4, a, (d << 3) | c, gamma);          // +y: (a, d, c)
-        fv[4 * 3 + d] = staged_load(st, vals, 5, a, (c << 3) | (5 + d), gamma);    // -z: (a, c, 5+d)
-        fv[5 * 3 + d] = staged_load(st, vals, 6, a, (c << 3) | d, gamma);          // +z: (a, c, d)
+        fv[0 * 3 + d] = staged_load(st, 1, 5 + d, t, gamma);                 // -x: (5+d, a, c)
+        fv[1 * 3 + d] = staged_load(st, 2, d, t, gamma);                     // +x: (d, a, c)
+        fv[2 * 3 + d] = staged_load(st, 3, a, ((5 + d) << 3) | c, gamma);    // -y: (a, 5+d, c)
+        fv[3 * 3 + d] = staged_load(st, 4, a, (d << 3) | c, gamma);          // +y: (a, d, c)
+        fv[4 * 3 + d] = staged_load(st, 5, a, (c << 3) | (5 + d), gamma);    // -z: (a, c, 5+d)
+        fv[5 * 3 + d] = staged_load(st, 6, a, (c << 3) | d, gamma);          // +z: (a, c, d)
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) tile[tile_index(k, a, c)] = cv[k];

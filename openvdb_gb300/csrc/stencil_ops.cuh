@@ -67,7 +67,7 @@ struct ParityArith {
 
     // Vec3d(iGradient) -> map.applyIJT (x 1/dx in double) -> Vec3f
     // (math/Operators.h:838-845, math/Maps.h:767-771).
-    __device__ __forceinline__ static float ijt(float g, double invdx) {
+    __device__ __forceinline__ static float ijt(float g, double invdx, float) {
         return __double2float_rn(__dmul_rn(double(g), invdx));
     }
 };
@@ -102,7 +102,7 @@ struct FastArith {
         return __fdividef(num, den);
     }
 
-    __device__ __forceinline__ static float ijt(float g, double invdx) { return g * float(invdx); }
+    __device__ __forceinline__ static float ijt(float g, double, float invdx) { return g * invdx; }
 };
 
 // ---- HJ-WENO5 one-sided derivatives on the staged tile --------------------
@@ -133,18 +133,38 @@ __device__ __forceinline__ Line7 tile_line(const float* tile, int x, int y, int 
     return L;
 }
 
-// The upwind derivative V<0 ? FD : BD with a single WENO5 evaluation: FD
-// reads the line mirrored (a_k = S[3-k], k=-3..2 -> v[6-k]) with the same
-// difference pattern as BD (a_k = v[k]), and BD negates the result.  Same
-// operations on the same operands as hj_fd / hj_bd.
+// One-sided HJ-WENO5 derivatives from the six differences D_k = S(k-2) - S(k-3)
+// of a line (k = 0..5): FD = WENO5(D5, D4, D3, D2, D1) is the reference's FD
+// operand list; BD = -WENO5(-D0, ..., -D4) = WENO5(D0, ..., D4) because WENO5
+// is odd in its arguments — exactly, operation by operation, in any IEEE
+// rounding-to-nearest arithmetic (squares, products and sums change sign
+// exactly).  Same operands and operations as hj_fd / hj_bd.
+struct Diff6 {
+    float d[6];
+};
+template <class A>
+__device__ __forceinline__ Diff6 line_diffs(const Line7& L) {
+    Diff6 D;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) D.d[k] = A::sub(L.v[k + 1], L.v[k]);
+    return D;
+}
+template <class A>
+__device__ __forceinline__ float diff_fd(const Diff6& D) {
+    return A::weno5(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);
+}
+template <class A>
+__device__ __forceinline__ float diff_bd(const Diff6& D) {
+    return A::weno5(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);
+}
+// V<0 ? FD : BD with one WENO5 evaluation on selected operands.
 template <class A>
 __device__ __forceinline__ float line_upwind(const Line7& L, bool fd) {
-    float a[6];
+    const Diff6 D = line_diffs<A>(L);
+    float in[5];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) a[k] = fd ? L.v[6 - k] : L.v[k];
-    const float w = A::weno5(A::sub(a[0], a[1]), A::sub(a[1], a[2]), A::sub(a[2], a[3]),
-                             A::sub(a[3], a[4]), A::sub(a[4], a[5]));
-    return fd ? w : -w;
+    for (int k = 0; k < 5; ++k) in[k] = fd ? D.d[5 - k] : D.d[k];
+    return A::weno5(in[0], in[1], in[2], in[3], in[4]);
 }
 
 template <class A>
@@ -233,7 +253,8 @@ struct RkArgs {
     float dt, alpha, beta, gamma, t0;
     int has_phi;           // Nominator != 0
     int backward;          // velocity negated (t0 > t1)
-    double invdx;
+    double invdx;          // 1/dx (parity: applied in double like applyIJT)
+    float invdx_f;         // 1/dx in float (fast)
     FieldParams field;
 };
 
@@ -294,26 +315,52 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ uint16_t list[LEAF_VOX];
+    __shared__ float vtab[6][8];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
     stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
-    load_tile(tile, st, a.src.vals, a.gamma);
+    load_tile(tile, st, a.gamma);
     const int n = build_list(list, st.am[0]);
     __syncthreads();
     int ox, oy, oz;
     key_origin(a.keys[l], ox, oy, oz);
+    // deformation field: the leaf's 8 sines per axis and function, staged once
+    const bool tabbed = a.field.kind == 2 && a.field.tab && ox - a.field.tab_lo >= 0 &&
+                        oy - a.field.tab_lo >= 0 && oz - a.field.tab_lo >= 0 &&
+                        ox + 8 - a.field.tab_lo <= a.field.tab_n && oy + 8 - a.field.tab_lo <= a.field.tab_n &&
+                        oz + 8 - a.field.tab_lo <= a.field.tab_n;
+    if (tabbed) {
+        if (threadIdx.x < 48) {
+            const int ax = threadIdx.x >> 4, fn = (threadIdx.x >> 3) & 1, q = threadIdx.x & 7;
+            const int o = ax == 0 ? ox : ax == 1 ? oy : oz;
+            vtab[ax * 2 + fn][q] = a.field.tab[2 * (o + q - a.field.tab_lo) + fn];
+        }
+        __syncthreads();
+    }
     for (int i = threadIdx.x; i < n; i += STENCIL_THREADS) {
         const int v = list[i];
         const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
         float vel[3];
-        eval_field(a.field, ox + x, oy + y, oz + z, a.t0, vel);
+        if (tabbed) {
+            // gbls_deformation with the staged sines (same operations)
+            const float sx = vtab[0][x], s2x = vtab[1][x], sy = vtab[2][y], s2y = vtab[3][y];
+            const float sz = vtab[4][z], s2z = vtab[5][z];
+            const float u = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, sx), sx), s2y), s2z);
+            const float w = __fmul_rn(__fmul_rn(__fmul_rn(s2x, sy), sy), s2z);
+            const float q = __fmul_rn(__fmul_rn(__fmul_rn(s2x, s2y), sz), sz);
+            vel[0] = __fmul_rn(u, a.field.amp);
+            vel[1] = -__fmul_rn(w, a.field.amp);
+            vel[2] = -__fmul_rn(q, a.field.amp);
+        } else {
+            eval_field(a.field, ox + x, oy + y, oz + z, a.t0, vel);
+        }
         if (a.backward) { vel[0] = -vel[0]; vel[1] = -vel[1]; vel[2] = -vel[2]; }
         float g[3];
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             const Line7 L = tile_line(tile, x, y, z, ax);
-            g[ax] = A::ijt(line_upwind<A>(L, vel[ax] < 0.0f), a.invdx);
+            g[ax] = A::ijt(line_upwind<A>(L, vel[ax] < 0.0f), a.invdx, a.invdx_f);
         }
         const float dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
         const float c = tile[tile_index(x, y, z)];
@@ -352,7 +399,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         fsg[t] = st.sm[0][t] & ~um[t];
         if (a.has_phi) phm[t] = a.phi.amask[size_t(s) * 8 + t];
     }
-    load_tile(tile, st, a.src.vals, a.gamma);
+    load_tile(tile, st, a.gamma);
     __syncthreads();
     const int n = build_list(list, um);
     __syncthreads();
@@ -373,9 +420,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
             float up[3], down[3];
 #pragma unroll
             for (int ax = 0; ax < 3; ++ax) {
-                const Line7 L = tile_line(tile, x, y, z, ax);
-                up[ax] = line_fd<A>(L);
-                down[ax] = line_bd<A>(L);
+                const Diff6 D = line_diffs<A>(tile_line(tile, x, y, z, ax));
+                up[ax] = diff_fd<A>(D);
+                down[ax] = diff_bd<A>(D);
             }
             const float nsq = godunov<A>(phi0 > 0.0f, down, up);
             float vv = A::div(phi0, A::add(A::sqrt(A::add(A::mul(phi0, phi0), nsq)), 1e-8f));
