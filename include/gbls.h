@@ -205,6 +205,23 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
 
 
 
+/* ---- batches of independent level sets --------------------------------------
+ * A batch handle holds n level sets (instances) that share the voxel size and
+ * background; gbls_batch_advect advances every instance i from t0 to t1 with
+ * its own CFL substep sequence exactly as n separate
+ * LevelSetAdvection::advect calls would (tools/LevelSetAdvect.h:338-418),
+ * in one set of kernel launches per substep.  fields[i] is instance i's
+ * velocity (CONSTANT, DEFORMATION or ROTATION); substeps[i] receives its CFL
+ * count.  At most 512 instances.  The tracker state and the precision mode
+ * of the handle apply to every instance.                                      */
+#define GBLS_MAX_INSTANCES 512
+int gbls_batch_create(int32_t n, const gbls_grid_desc* descs, gbls_handle** out);
+int gbls_batch_instances(gbls_handle* h, int32_t* n);
+int gbls_batch_get_counts(gbls_handle* h, int32_t instance, gbls_grid_counts* out);
+int gbls_batch_download(gbls_handle* h, int32_t instance, gbls_grid_desc* out);
+int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial, int temporal,
+                      float t0, float t1, float cfl, uint64_t* substeps);
+
 /* ---- measurement ----------------------------------------------------------
  * Counters since the last gbls_reset_stats.  voxel_updates is the sum over
  * CFL substeps of the active voxel count at the start of the substep.  With
@@ -251,6 +268,9 @@ int gbls_host_sphere(float radius, const float center[3], float voxel_size, floa
                      gbls_host_grid** out);
 int gbls_host_union_of_spheres(int64_t n, const float* centers, const float* radii,
                                float voxel_size, float half_width, gbls_host_grid** out);
+/* A torus around the y axis (no counterpart in OpenVDB; batch fixtures). */
+int gbls_host_torus(float major_radius, float minor_radius, const float center[3],
+                    float voxel_size, float half_width, gbls_host_grid** out);
 int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* view);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);

@@ -61,6 +61,15 @@ def lib():
         "gbls_host_sphere": ([C.c_float, P(C.c_float), C.c_float, C.c_float, P(vp)], C.c_int),
         "gbls_host_union_of_spheres": ([C.c_int64, P(C.c_float), P(C.c_float), C.c_float,
                                         C.c_float, P(vp)], C.c_int),
+        "gbls_host_torus": ([C.c_float, C.c_float, P(C.c_float), C.c_float, C.c_float, P(vp)],
+                            C.c_int),
+        "gbls_batch_create": ([C.c_int32, P(_abi.GridDesc), P(vp)], C.c_int),
+        "gbls_batch_instances": ([vp, P(C.c_int32)], C.c_int),
+        "gbls_batch_get_counts": ([vp, C.c_int32, P(_abi.GridCounts)], C.c_int),
+        "gbls_batch_download": ([vp, C.c_int32, P(_abi.GridDesc)], C.c_int),
+        "gbls_batch_advect": ([vp, P(_abi.FieldDesc), C.c_int, C.c_int, C.c_float, C.c_float,
+                               C.c_float, P(C.c_uint64)], C.c_int),
+        "gbls_count_active_noalloc": ([vp, P(C.c_int64)], C.c_int),
         "gbls_host_grid_view": ([vp, P(_abi.GridDesc)], C.c_int),
         "gbls_host_grid_free": ([vp], C.c_int),
         "gbls_host_last_error": ([], C.c_char_p),

@@ -105,9 +105,10 @@ inline unsigned blocks_for(int64_t n, int threads) { return unsigned((n + thread
 // that would receive active bits.  Emits (key << 1) | tile sign.
 __global__ void k_emit_candidates(int64_t n, const uint64_t* keys, const int32_t* slot,
                                   const int32_t* nbr, const uint64_t* am, uint64_t* cand,
-                                  unsigned long long* count) {
+                                  unsigned long long* count, const uint8_t* inst_run) {
     const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (l >= n) return;
+    if (inst_run && !inst_run[key_instance(keys[l])]) return;
     const int32_t* nb = nbr + 6 * l;
     bool any_missing = false;
     for (int f = 0; f < 6; ++f) any_missing |= nb[f] < 0;
@@ -180,7 +181,7 @@ __global__ void k_build_nbr(int64_t n, const uint64_t* keys, const int32_t* slot
 
 // NN_FACE dilation of every leaf mask into dmask (8 threads per leaf).
 __global__ void k_dilate(int64_t n, const int32_t* slot, const int32_t* nbr, const uint64_t* am,
-                         uint64_t* dmask) {
+                         uint64_t* dmask, const uint64_t* keys, const uint8_t* inst_run) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (i >= n * 8) return;
     const int64_t l = i >> 3;
@@ -188,6 +189,10 @@ __global__ void k_dilate(int64_t n, const int32_t* slot, const int32_t* nbr, con
     const int s = slot[l];
     const int32_t* nb = nbr + 6 * l;
     const uint64_t* own = am + size_t(s) * 8;
+    if (inst_run && !inst_run[key_instance(keys[l])]) {  // finished instance: unchanged
+        dmask[size_t(s) * 8 + x] = own[x];
+        return;
+    }
     auto P = [&](int f) -> const uint64_t* { return nb[f] >= 0 ? am + size_t(nb[f]) * 8 : nullptr; };
     dmask[size_t(s) * 8 + x] = dilate_word(own, x, P(0), P(1), P(2), P(3), P(4), P(5));
 }
@@ -248,7 +253,8 @@ __global__ void k_prune_scatter(int64_t n, const uint64_t* keys, const int32_t* 
                                 uint64_t* ko, int32_t* so, int32_t* free_slots, int64_t nfree,
                                 const uint64_t* lower_keys, int64_t nlower, uint64_t* lower_sign,
                                 const int32_t* cnt, unsigned long long* nactive,
-                                unsigned long long* nkept, unsigned long long* err) {
+                                unsigned long long* nkept, unsigned long long* err,
+                                unsigned long long* inst_active) {
     const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     // active voxels of the kept leaves: warp sum, one atomic per warp
     // (blockDim is a multiple of 32, every lane takes part)
@@ -261,6 +267,7 @@ __global__ void k_prune_scatter(int64_t n, const uint64_t* keys, const int32_t* 
     if (keep[l]) {
         ko[k] = keys[l];
         so[k] = slot[l];
+        if (inst_active) atomicAdd(inst_active + key_instance(keys[l]), (unsigned long long)cnt[l]);
         return;
     }
     const int s = slot[l];
@@ -314,6 +321,16 @@ __global__ void k_count_active(int64_t n, const int32_t* slot, const uint64_t* a
     if (i < n * 8) c = __popcll(am[size_t(slot[i >> 3]) * 8 + (i & 7)]);
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// Active voxels per instance (one atomic per leaf).
+__global__ void k_count_active_inst(int64_t n, const uint64_t* keys, const int32_t* slot, const uint64_t* am,
+                                    unsigned long long* out) {
+    const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (l >= n) return;
+    unsigned long long c = 0;
+    for (int w = 0; w < 8; ++w) c += __popcll(am[size_t(slot[l]) * 8 + w]);
+    if (c) atomicAdd(out + key_instance(keys[l]), c);
 }
 
 // Pack leaf values into the slot layout (upload) / unpack (download).
@@ -400,6 +417,15 @@ struct gbls_handle {
     DevStatus* st_h = nullptr;
     DevArray<unsigned long long> u64s;
     unsigned long long* acc_d = nullptr;  // [2] normalize voxels processed / written
+    // batches: instance id in key bits 54..62
+    int ninst = 1;
+    bool batch_run = false;  // kernels see the per-instance arrays below
+    DevArray<uint8_t> inst_run;
+    DevArray<float> inst_dt, inst_t0;
+    DevArray<FieldParams> inst_field;
+    DevArray<unsigned int> inst_max;
+    DevArray<unsigned long long> inst_active;
+    const uint8_t* run_ptr() const { return batch_run ? inst_run.p : nullptr; }
     // measurement
     gbls_stats stats{};
     int64_t nactive = -1;  // active voxels, -1 = unknown
@@ -694,7 +720,7 @@ void dilate_topology(gbls_handle& h) {
     h.cand.reserve(size_t(L) * 6, h.stream);
     h.clear_status();
     k_emit_candidates<<<blocks_for(L, 128), 128, 0, h.stream>>>(L, h.K(), h.S(), h.nbr.p, h.am[h.mc].p,
-                                                                 h.cand.p, &h.st_d->n_cand);
+                                                                 h.cand.p, &h.st_d->n_cand, h.run_ptr());
     ++h.stats.kernel_launches;
     CU(cudaGetLastError());
     h.read_status();
@@ -752,7 +778,7 @@ void dilate_topology(gbls_handle& h) {
     }
     h.rebuild_nbr();
     k_dilate<<<blocks_for(h.nleaf * 8, 256), 256, 0, h.stream>>>(h.nleaf, h.S(), h.nbr.p, h.am[h.mc].p,
-                                                                  h.dmask.p);
+                                                                  h.dmask.p, h.K(), h.run_ptr());
     ++h.stats.kernel_launches;
     CU(cudaGetLastError());
 }
@@ -809,6 +835,8 @@ void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim, int carry =
     base.invdx = invdx;
     base.out_count = h.cnt.p;
     base.carry = carry;
+    base.keys = h.K();
+    base.inst_run = h.run_ptr();
     const int iters = h.norm_count;
     if (iters <= 0) {
         if (!trim) return;
@@ -917,11 +945,12 @@ void prune_compact(gbls_handle& h) {
         bytes = h.cub_tmp.cap;
         CU(cub::DeviceScan::ExclusiveSum(h.cub_tmp.p, bytes, h.keep.p, h.idx.p, int(L), h.stream));
         h.clear_status();
+        if (h.batch_run) CU(cudaMemsetAsync(h.inst_active.p, 0, size_t(h.ninst) * sizeof(unsigned long long), h.stream));
         const int ko = 1 - h.kc;
         k_prune_scatter<<<blocks_for(L, 256), 256, 0, h.stream>>>(
             L, h.K(), h.S(), h.keep.p, h.idx.p, h.sm[h.mc].p, h.keys[ko].p, h.slot[ko].p, h.free_slots.p,
             h.nfree, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.lower_sign.p, h.cnt.p,
-            &h.st_d->n_active, &h.st_d->n_cand, &h.st_d->error);
+            &h.st_d->n_active, &h.st_d->n_cand, &h.st_d->error, h.batch_run ? h.inst_active.p : nullptr);
         ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.kc = ko;
@@ -940,7 +969,10 @@ void prune_compact(gbls_handle& h) {
         h.nleaf = kept;
         h.nactive = int64_t(h.st_h->n_active);
         lower_changed = h.st_h->n_lower_empty > 0;
-    } else if (!h.lower_keys_h.empty()) {
+    } else if (h.batch_run) {
+        CU(cudaMemsetAsync(h.inst_active.p, 0, size_t(h.ninst) * sizeof(unsigned long long), h.stream));
+    }
+    if (L == 0 && !h.lower_keys_h.empty()) {
         // no leaves: every lower node is empty
         const int64_t nl = int64_t(h.lower_keys_h.size());
         h.flags.reserve(size_t(nl), h.stream);
@@ -1079,7 +1111,13 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
     base.backward = backward ? 1 : 0;
     base.invdx = 1.0 / h.voxel_size;
     base.invdx_f = float(1.0 / h.voxel_size);
-    base.field = field_params(f, t0);
+    if (f) base.field = field_params(f, t0);
+    if (h.batch_run) {
+        base.inst_run = h.inst_run.p;
+        base.inst_dt = h.inst_dt.p;
+        base.inst_t0 = h.inst_t0.p;
+        base.inst_field = h.inst_field.p;
+    }
     const int a0 = h.vc, b0 = (h.vc + 1) % 3, c0 = (h.vc + 2) % 3;
     auto stage = [&](int src, int phin, int out, float alpha, int has_phi, const char* msg) {
         RkArgs a = base;
@@ -1094,6 +1132,7 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
         end_intr(h);
     };
     if (temporal == GBLS_TVD_RK1) {
+        base.copy_done = 1;  // the only stage writes the result buffer
         stage(a0, a0, b0, 0.0f, 0, "Advecting level set using TVD_RK1");
         h.vc = b0;
     } else if (temporal == GBLS_TVD_RK2) {
@@ -1111,125 +1150,122 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
 // ---- upload / download ------------------------------------------------------
 bool is_pm_gamma(float v, float g) { return v == g || v == -g; }
 
-void upload(gbls_handle& h, const gbls_grid_desc* d) {
-    if (!(d->voxel_size > 0.0)) fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
-    if (!(d->background > 0.0f)) fail(GBLS_ERR_RUNTIME, "LevelSetTracker expected a level set (positive background)");
-    if (d->map_type < GBLS_MAP_UNIFORM_SCALE || d->map_type > GBLS_MAP_TRANSLATION)
+// Upload n level sets (instance i from descs[i]; n == 1 for a plain handle).
+void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
+    if (n < 1 || n > GBLS_MAX_INSTANCES) fail(GBLS_ERR_INVALID_ARGUMENT, "instance count out of range");
+    const gbls_grid_desc* d0 = descs;
+    if (!(d0->voxel_size > 0.0)) fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
+    if (!(d0->background > 0.0f)) fail(GBLS_ERR_RUNTIME, "LevelSetTracker expected a level set (positive background)");
+    if (d0->map_type < GBLS_MAP_UNIFORM_SCALE || d0->map_type > GBLS_MAP_TRANSLATION)
         fail(GBLS_ERR_VALUE, "MapType not supported!");
-    h.voxel_size = d->voxel_size;
-    for (int i = 0; i < 3; ++i) h.translation[i] = d->translation[i];
-    h.map_type = d->map_type;
-    h.gamma = d->background;
-    const float g = d->background;
-    const int64_t L = d->leaf_count;
-    if (L < 0 || d->lower_count < 0 || d->upper_count < 0 || d->root_tile_count < 0)
-        fail(GBLS_ERR_INVALID_ARGUMENT, "negative count");
-    if (L > 0 && (!d->leaf_origins || !d->leaf_masks || !d->leaf_values))
-        fail(GBLS_ERR_INVALID_ARGUMENT, "null leaf arrays");
+    h.voxel_size = d0->voxel_size;
+    for (int i = 0; i < 3; ++i) h.translation[i] = d0->translation[i];
+    h.map_type = d0->map_type;
+    h.gamma = d0->background;
+    h.ninst = n;
+    const float g = d0->background;
     auto check_origin = [&](const int32_t* o, int align) {
         for (int a = 0; a < 3; ++a) {
             if (o[a] % align != 0) fail(GBLS_ERR_INVALID_ARGUMENT, "node origin not aligned");
             if (o[a] < -COORD_SAFE || o[a] >= COORD_SAFE) fail(GBLS_ERR_DOMAIN, "coordinate outside the supported range");
         }
     };
-    // leaves, sorted into tree order
-    std::vector<std::pair<uint64_t, int64_t>> order(static_cast<size_t>(L));
-    for (int64_t i = 0; i < L; ++i) {
-        const int32_t* o = d->leaf_origins + 3 * i;
-        check_origin(o, 8);
-        order[size_t(i)] = {leaf_key(o[0], o[1], o[2]), i};
+    struct Src { uint64_t key; int inst; int64_t idx; bool operator<(const Src& o) const { return key < o.key; } };
+    std::vector<Src> lv, lo, up, rt;
+    for (int q = 0; q < n; ++q) {
+        const gbls_grid_desc* d = descs + q;
+        if (d->voxel_size != d0->voxel_size || d->background != d0->background)
+            fail(GBLS_ERR_INVALID_ARGUMENT, "batch instances must share voxel size and background");
+        if (d->leaf_count < 0 || d->lower_count < 0 || d->upper_count < 0 || d->root_tile_count < 0)
+            fail(GBLS_ERR_INVALID_ARGUMENT, "negative count");
+        if (d->leaf_count > 0 && (!d->leaf_origins || !d->leaf_masks || !d->leaf_values))
+            fail(GBLS_ERR_INVALID_ARGUMENT, "null leaf arrays");
+        const uint64_t ib = uint64_t(q) << KEY_INST_SHIFT;
+        for (int64_t i = 0; i < d->leaf_count; ++i) {
+            const int32_t* o = d->leaf_origins + 3 * i;
+            check_origin(o, 8);
+            lv.push_back({leaf_key(o[0], o[1], o[2]) | ib, q, i});
+        }
+        for (int64_t i = 0; i < d->lower_count; ++i) {
+            const int32_t* o = d->lower_origins + 3 * i;
+            check_origin(o, 128);
+            lo.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 12, q, i});
+        }
+        for (int64_t i = 0; i < d->upper_count; ++i) {
+            const int32_t* o = d->upper_origins + 3 * i;
+            check_origin(o, 4096);
+            up.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 27, q, i});
+        }
+        for (int64_t i = 0; i < d->root_tile_count; ++i) {
+            const int32_t* o = d->root_tile_origins + 3 * i;
+            check_origin(o, 4096);
+            rt.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 27, q, i});
+        }
     }
-    std::sort(order.begin(), order.end());
-    for (size_t i = 1; i < order.size(); ++i)
-        if (order[i].first == order[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate leaf");
+    std::sort(lv.begin(), lv.end());
+    std::sort(lo.begin(), lo.end());
+    std::sort(up.begin(), up.end());
+    std::sort(rt.begin(), rt.end());
+    const int64_t L = int64_t(lv.size());
     std::vector<uint64_t> keys(static_cast<size_t>(L)), am(static_cast<size_t>(L) * 8), sm(static_cast<size_t>(L) * 8, 0);
     std::vector<int32_t> slots(static_cast<size_t>(L));
     std::vector<float> vals(static_cast<size_t>(L) * LEAF_VOX, 0.0f);
     for (int64_t i = 0; i < L; ++i) {
-        const int64_t src = order[size_t(i)].second;
-        keys[size_t(i)] = order[size_t(i)].first;
+        if (i && lv[size_t(i)].key == lv[size_t(i - 1)].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate leaf");
+        const gbls_grid_desc* d = descs + lv[size_t(i)].inst;
+        const int64_t src = lv[size_t(i)].idx;
+        keys[size_t(i)] = lv[size_t(i)].key;
         slots[size_t(i)] = int32_t(i);
         const float* v = d->leaf_values + src * LEAF_VOX;
         int rank = 0;
         for (int w = 0; w < 8; ++w) {
             const uint64_t m = d->leaf_masks[src * 8 + w];
             am[size_t(i) * 8 + w] = m;
-            uint64_t s = 0;
+            uint64_t sg = 0;
             for (int b = 0; b < 64; ++b) {
                 const float x = v[w * 64 + b];
-                if (x < 0.0f) s |= uint64_t(1) << b;
-                if ((m >> b) & 1) {
-                    vals[size_t(i) * LEAF_VOX + rank++] = x;
-                } else if (!is_pm_gamma(x, g)) {
-                    fail(GBLS_ERR_UNSUPPORTED, "inactive leaf value other than +-background");
-                }
+                if (x < 0.0f) sg |= uint64_t(1) << b;
+                if ((m >> b) & 1) vals[size_t(i) * LEAF_VOX + rank++] = x;
+                else if (!is_pm_gamma(x, g)) fail(GBLS_ERR_UNSUPPORTED, "inactive leaf value other than +-background");
             }
-            sm[size_t(i) * 8 + w] = s;
+            sm[size_t(i) * 8 + w] = sg;
         }
     }
-    // lower nodes
-    std::vector<std::pair<uint64_t, int64_t>> lo(size_t(d->lower_count));
-    for (int64_t i = 0; i < d->lower_count; ++i) {
-        const int32_t* o = d->lower_origins + 3 * i;
-        check_origin(o, 128);
-        lo[size_t(i)] = {leaf_key(o[0], o[1], o[2]) >> 12, i};
-    }
-    std::sort(lo.begin(), lo.end());
     std::vector<uint64_t> lkeys(lo.size()), lsign(lo.size() * 64, 0);
     for (size_t i = 0; i < lo.size(); ++i) {
-        if (i && lo[i].first == lo[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate lower node");
-        lkeys[i] = lo[i].first;
-        const float* t = d->lower_tiles + lo[i].second * LOWER_SLOTS;
-        for (int n = 0; n < LOWER_SLOTS; ++n) {
-            const uint64_t k = (lkeys[i] << 12) | uint64_t(n);
-            if (std::binary_search(keys.begin(), keys.end(), k)) continue;  // child slot
-            if (!is_pm_gamma(t[n], g)) fail(GBLS_ERR_UNSUPPORTED, "lower-node tile other than +-background");
-            if (t[n] < 0.0f) lsign[i * 64 + (n >> 6)] |= uint64_t(1) << (n & 63);
+        if (i && lo[i].key == lo[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate lower node");
+        lkeys[i] = lo[i].key;
+        const float* t = descs[lo[i].inst].lower_tiles + lo[i].idx * LOWER_SLOTS;
+        for (int q = 0; q < LOWER_SLOTS; ++q) {
+            if (std::binary_search(keys.begin(), keys.end(), (lkeys[i] << 12) | uint64_t(q))) continue;
+            if (!is_pm_gamma(t[q], g)) fail(GBLS_ERR_UNSUPPORTED, "lower-node tile other than +-background");
+            if (t[q] < 0.0f) lsign[i * 64 + (q >> 6)] |= uint64_t(1) << (q & 63);
         }
     }
     for (uint64_t k : keys)
-        if (!std::binary_search(lkeys.begin(), lkeys.end(), k >> 12))
-            fail(GBLS_ERR_INVALID_ARGUMENT, "leaf without lower node");
-    // upper nodes
-    std::vector<std::pair<uint64_t, int64_t>> up(size_t(d->upper_count));
-    for (int64_t i = 0; i < d->upper_count; ++i) {
-        const int32_t* o = d->upper_origins + 3 * i;
-        check_origin(o, 4096);
-        up[size_t(i)] = {leaf_key(o[0], o[1], o[2]) >> 27, i};
-    }
-    std::sort(up.begin(), up.end());
+        if (!std::binary_search(lkeys.begin(), lkeys.end(), k >> 12)) fail(GBLS_ERR_INVALID_ARGUMENT, "leaf without lower node");
     std::vector<uint64_t> ukeys(up.size()), usign(up.size() * 512, 0);
     for (size_t i = 0; i < up.size(); ++i) {
-        if (i && up[i].first == up[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate upper node");
-        ukeys[i] = up[i].first;
-        const float* t = d->upper_tiles + up[i].second * UPPER_SLOTS;
-        for (int n = 0; n < UPPER_SLOTS; ++n) {
-            const uint64_t k = (ukeys[i] << 15) | uint64_t(n);
-            if (std::binary_search(lkeys.begin(), lkeys.end(), k)) continue;
-            if (!is_pm_gamma(t[n], g)) fail(GBLS_ERR_UNSUPPORTED, "upper-node tile other than +-background");
-            if (t[n] < 0.0f) usign[i * 512 + (n >> 6)] |= uint64_t(1) << (n & 63);
+        if (i && up[i].key == up[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate upper node");
+        ukeys[i] = up[i].key;
+        const float* t = descs[up[i].inst].upper_tiles + up[i].idx * UPPER_SLOTS;
+        for (int q = 0; q < UPPER_SLOTS; ++q) {
+            if (std::binary_search(lkeys.begin(), lkeys.end(), (ukeys[i] << 15) | uint64_t(q))) continue;
+            if (!is_pm_gamma(t[q], g)) fail(GBLS_ERR_UNSUPPORTED, "upper-node tile other than +-background");
+            if (t[q] < 0.0f) usign[i * 512 + (q >> 6)] |= uint64_t(1) << (q & 63);
         }
     }
     for (uint64_t k : lkeys)
-        if (!std::binary_search(ukeys.begin(), ukeys.end(), k >> 15))
-            fail(GBLS_ERR_INVALID_ARGUMENT, "lower node without upper node");
-    // root tiles
-    std::vector<std::pair<uint64_t, uint8_t>> rt(size_t(d->root_tile_count));
-    for (int64_t i = 0; i < d->root_tile_count; ++i) {
-        const int32_t* o = d->root_tile_origins + 3 * i;
-        check_origin(o, 4096);
-        const float v = d->root_tile_values[i];
-        if (!is_pm_gamma(v, g)) fail(GBLS_ERR_UNSUPPORTED, "root tile other than +-background");
-        rt[size_t(i)] = {leaf_key(o[0], o[1], o[2]) >> 27, uint8_t(v < 0.0f ? 1 : 0)};
-    }
-    std::sort(rt.begin(), rt.end());
+        if (!std::binary_search(ukeys.begin(), ukeys.end(), k >> 15)) fail(GBLS_ERR_INVALID_ARGUMENT, "lower node without upper node");
     h.root_keys_h.clear();
     h.root_sign_h.clear();
-    for (auto& r : rt) {
-        if (std::binary_search(ukeys.begin(), ukeys.end(), r.first))
-            fail(GBLS_ERR_INVALID_ARGUMENT, "root tile overlaps an upper node");
-        h.root_keys_h.push_back(r.first);
-        h.root_sign_h.push_back(r.second);
+    for (size_t i = 0; i < rt.size(); ++i) {
+        const float v = descs[rt[i].inst].root_tile_values[rt[i].idx];
+        if (!is_pm_gamma(v, g)) fail(GBLS_ERR_UNSUPPORTED, "root tile other than +-background");
+        if (std::binary_search(ukeys.begin(), ukeys.end(), rt[i].key)) fail(GBLS_ERR_INVALID_ARGUMENT, "root tile overlaps an upper node");
+        if (i && rt[i].key == rt[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate root tile");
+        h.root_keys_h.push_back(rt[i].key);
+        h.root_sign_h.push_back(uint8_t(v < 0.0f ? 1 : 0));
     }
     // device state
     h.nleaf = L;
@@ -1250,7 +1286,7 @@ void upload(gbls_handle& h, const gbls_grid_desc* d) {
     h.free_slots.reserve(size_t(scap), h.stream);
     h.slot_cap = scap;
     std::vector<int32_t> fs;
-    for (int64_t s = scap - 1; s >= L; --s) fs.push_back(int32_t(s));
+    for (int64_t q = scap - 1; q >= L; --q) fs.push_back(int32_t(q));
     h.nfree = int64_t(fs.size());
     h.free_slots.upload(fs.data(), fs.size(), h.stream);
     h.keys[0].upload(keys.data(), keys.size(), h.stream);
@@ -1266,29 +1302,65 @@ void upload(gbls_handle& h, const gbls_grid_desc* d) {
     h.nodes_checked = false;
     h.upload_upper_root();
     h.rebuild_nbr();
+    h.inst_run.reserve(size_t(n), h.stream);
+    h.inst_dt.reserve(size_t(n), h.stream);
+    h.inst_t0.reserve(size_t(n), h.stream);
+    h.inst_field.reserve(size_t(n), h.stream);
+    h.inst_max.reserve(size_t(n), h.stream);
+    h.inst_active.reserve(size_t(n), h.stream);
     h.sync();
     h.nactive = -1;
 }
 
-void download(gbls_handle& h, gbls_grid_desc* d) {
-    const int64_t L = h.nleaf;
-    if (d->leaf_count != L || d->lower_count != int64_t(h.lower_keys_h.size()) ||
-        d->upper_count != int64_t(h.upper_keys_h.size()) || d->root_tile_count != int64_t(h.root_keys_h.size()))
+// Index ranges [lo, hi) of instance `inst` in the leaf / lower / upper / root
+// lists (all of them for inst < 0): instance bits are the top key bits, so
+// every list is sorted by instance first.
+struct InstRange {
+    int64_t l0, l1, lo0, lo1, u0, u1, r0, r1;
+};
+
+InstRange inst_range(gbls_handle& h, const std::vector<uint64_t>& keys, int inst) {
+    InstRange r{0, int64_t(keys.size()), 0, int64_t(h.lower_keys_h.size()), 0,
+                int64_t(h.upper_keys_h.size()), 0, int64_t(h.root_keys_h.size())};
+    if (inst < 0) return r;
+    auto rng = [](const std::vector<uint64_t>& v, uint64_t a, uint64_t b, int64_t& x, int64_t& y) {
+        x = int64_t(std::lower_bound(v.begin(), v.end(), a) - v.begin());
+        y = int64_t(std::lower_bound(v.begin(), v.end(), b) - v.begin());
+    };
+    const uint64_t q = uint64_t(inst), q1 = uint64_t(inst + 1);
+    rng(keys, q << KEY_INST_SHIFT, q1 << KEY_INST_SHIFT, r.l0, r.l1);
+    rng(h.lower_keys_h, q << (KEY_INST_SHIFT - 12), q1 << (KEY_INST_SHIFT - 12), r.lo0, r.lo1);
+    rng(h.upper_keys_h, q << (KEY_INST_SHIFT - 27), q1 << (KEY_INST_SHIFT - 27), r.u0, r.u1);
+    rng(h.root_keys_h, q << (KEY_INST_SHIFT - 27), q1 << (KEY_INST_SHIFT - 27), r.r0, r.r1);
+    return r;
+}
+
+std::vector<uint64_t> host_keys(gbls_handle& h) {
+    std::vector<uint64_t> keys(static_cast<size_t>(h.nleaf));
+    h.keys[h.kc].download(keys.data(), size_t(h.nleaf), h.stream);
+    h.sync();
+    return keys;
+}
+
+void download(gbls_handle& h, gbls_grid_desc* d, int inst) {
+    const std::vector<uint64_t> keys = host_keys(h);
+    const InstRange R = inst_range(h, keys, inst);
+    const int64_t L = R.l1 - R.l0;
+    if (d->leaf_count != L || d->lower_count != R.lo1 - R.lo0 || d->upper_count != R.u1 - R.u0 ||
+        d->root_tile_count != R.r1 - R.r0)
         fail(GBLS_ERR_INVALID_ARGUMENT, "descriptor counts do not match gbls_get_counts");
     d->voxel_size = h.voxel_size;
     for (int i = 0; i < 3; ++i) d->translation[i] = h.translation[i];
     d->map_type = h.map_type;
     d->background = h.gamma;
     const float g = h.gamma;
-    std::vector<uint64_t> keys(static_cast<size_t>(L));
-    std::vector<int32_t> slots(static_cast<size_t>(L));
-    h.keys[h.kc].download(keys.data(), size_t(L), h.stream);
-    h.slot[h.kc].download(slots.data(), size_t(L), h.stream);
+    std::vector<int32_t> slots(static_cast<size_t>(h.nleaf));
+    h.slot[h.kc].download(slots.data(), size_t(h.nleaf), h.stream);
     h.sync();
     if (L > 0) {
         DevArray<float> dense;
         dense.reserve(size_t(L) * LEAF_VOX, h.stream);
-        k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S(), h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, g,
+        k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S() + R.l0, h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, g,
                                                      dense.p);
         ++h.stats.kernel_launches;
         CU(cudaGetLastError());
@@ -1298,50 +1370,53 @@ void download(gbls_handle& h, gbls_grid_desc* d) {
         h.sync();
         for (int64_t i = 0; i < L; ++i) {
             int32_t x, y, z;
-            key_origin(keys[size_t(i)], x, y, z);
+            key_origin(keys[size_t(R.l0 + i)], x, y, z);
             d->leaf_origins[3 * i] = x;
             d->leaf_origins[3 * i + 1] = y;
             d->leaf_origins[3 * i + 2] = z;
-            for (int w = 0; w < 8; ++w) d->leaf_masks[8 * i + w] = am[size_t(slots[size_t(i)]) * 8 + w];
+            for (int w = 0; w < 8; ++w) d->leaf_masks[8 * i + w] = am[size_t(slots[size_t(R.l0 + i)]) * 8 + w];
         }
     }
     const size_t nl = h.lower_keys_h.size();
     std::vector<uint64_t> lsign(nl * 64);
     h.lower_sign.download(lsign.data(), lsign.size(), h.stream);
     h.sync();
-    for (size_t i = 0; i < nl; ++i) {
+    for (int64_t i = R.lo0; i < R.lo1; ++i) {
+        const int64_t o = i - R.lo0;
         int32_t x, y, z;
-        key_origin(h.lower_keys_h[i] << 12, x, y, z);
-        d->lower_origins[3 * i] = x;
-        d->lower_origins[3 * i + 1] = y;
-        d->lower_origins[3 * i + 2] = z;
-        float* t = d->lower_tiles + i * LOWER_SLOTS;
+        key_origin(h.lower_keys_h[size_t(i)] << 12, x, y, z);
+        d->lower_origins[3 * o] = x;
+        d->lower_origins[3 * o + 1] = y;
+        d->lower_origins[3 * o + 2] = z;
+        float* t = d->lower_tiles + o * LOWER_SLOTS;
         for (int n = 0; n < LOWER_SLOTS; ++n) {
-            const uint64_t k = (h.lower_keys_h[i] << 12) | uint64_t(n);
+            const uint64_t k = (h.lower_keys_h[size_t(i)] << 12) | uint64_t(n);
             if (std::binary_search(keys.begin(), keys.end(), k)) { t[n] = 0.0f; continue; }
-            t[n] = ((lsign[i * 64 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
+            t[n] = ((lsign[size_t(i) * 64 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
         }
     }
-    for (size_t i = 0; i < h.upper_keys_h.size(); ++i) {
+    for (int64_t i = R.u0; i < R.u1; ++i) {
+        const int64_t o = i - R.u0;
         int32_t x, y, z;
-        key_origin(h.upper_keys_h[i] << 27, x, y, z);
-        d->upper_origins[3 * i] = x;
-        d->upper_origins[3 * i + 1] = y;
-        d->upper_origins[3 * i + 2] = z;
-        float* t = d->upper_tiles + i * UPPER_SLOTS;
+        key_origin(h.upper_keys_h[size_t(i)] << 27, x, y, z);
+        d->upper_origins[3 * o] = x;
+        d->upper_origins[3 * o + 1] = y;
+        d->upper_origins[3 * o + 2] = z;
+        float* t = d->upper_tiles + o * UPPER_SLOTS;
         for (int n = 0; n < UPPER_SLOTS; ++n) {
-            const uint64_t k = (h.upper_keys_h[i] << 15) | uint64_t(n);
+            const uint64_t k = (h.upper_keys_h[size_t(i)] << 15) | uint64_t(n);
             if (std::binary_search(h.lower_keys_h.begin(), h.lower_keys_h.end(), k)) { t[n] = 0.0f; continue; }
-            t[n] = ((h.upper_sign_h[i * 512 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
+            t[n] = ((h.upper_sign_h[size_t(i) * 512 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
         }
     }
-    for (size_t i = 0; i < h.root_keys_h.size(); ++i) {
+    for (int64_t i = R.r0; i < R.r1; ++i) {
+        const int64_t o = i - R.r0;
         int32_t x, y, z;
-        key_origin(h.root_keys_h[i] << 27, x, y, z);
-        d->root_tile_origins[3 * i] = x;
-        d->root_tile_origins[3 * i + 1] = y;
-        d->root_tile_origins[3 * i + 2] = z;
-        d->root_tile_values[i] = h.root_sign_h[i] ? -g : g;
+        key_origin(h.root_keys_h[size_t(i)] << 27, x, y, z);
+        d->root_tile_origins[3 * o] = x;
+        d->root_tile_origins[3 * o + 1] = y;
+        d->root_tile_origins[3 * o + 2] = z;
+        d->root_tile_values[o] = h.root_sign_h[size_t(i)] ? -g : g;
     }
 }
 
@@ -1402,7 +1477,7 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
         CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
         CU(cudaMalloc(&h->acc_d, 2 * sizeof(unsigned long long)));
         CU(cudaMemset(h->acc_d, 0, 2 * sizeof(unsigned long long)));
-        upload(*h, desc);
+        upload(*h, desc, 1);
     });
     if (rc != GBLS_OK) {
         delete h;
@@ -1437,7 +1512,7 @@ int gbls_download(gbls_handle* h, gbls_grid_desc* out) {
     if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
-        download(*h, out);
+        download(*h, out, -1);
     });
 }
 
@@ -1598,6 +1673,205 @@ int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
     if (w_old < w_new) rc = gbls_dilate(h, w_new - w_old);
     else if (w_old > w_new) rc = gbls_erode(h, w_old - w_new);
     if (changed) *changed = (w_old != w_new) ? 1 : 0;
+    return rc;
+}
+
+int gbls_batch_create(int32_t n, const gbls_grid_desc* descs, gbls_handle** out) {
+    if (!descs || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    *out = nullptr;
+    gbls_handle* h = nullptr;
+    const int rc = guarded([&] {
+        DeviceGuard g(g_device);
+        h = new gbls_handle;
+        h->device = g_device;
+        CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
+        CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
+        CU(cudaMalloc(&h->acc_d, 2 * sizeof(unsigned long long)));
+        CU(cudaMemset(h->acc_d, 0, 2 * sizeof(unsigned long long)));
+        upload(*h, descs, int(n));
+    });
+    if (rc != GBLS_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBLS_OK;
+}
+
+int gbls_batch_instances(gbls_handle* h, int32_t* n) {
+    if (!h || !n) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    *n = h->ninst;
+    return GBLS_OK;
+}
+
+int gbls_batch_get_counts(gbls_handle* h, int32_t instance, gbls_grid_counts* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        if (instance < 0 || instance >= h->ninst) fail(GBLS_ERR_INVALID_ARGUMENT, "no such instance");
+        DeviceGuard g(h->device);
+        const std::vector<uint64_t> keys = host_keys(*h);
+        const InstRange R = inst_range(*h, keys, instance);
+        out->leaf_count = R.l1 - R.l0;
+        out->lower_count = R.lo1 - R.lo0;
+        out->upper_count = R.u1 - R.u0;
+        out->root_tile_count = R.r1 - R.r0;
+        out->active_voxel_count = 0;
+        if (R.l1 > R.l0) {
+            h->u64s.reserve(1, h->stream);
+            CU(cudaMemsetAsync(h->u64s.p, 0, sizeof(unsigned long long), h->stream));
+            k_count_active<<<blocks_for((R.l1 - R.l0) * 8, 256), 256, 0, h->stream>>>(R.l1 - R.l0, h->S() + R.l0,
+                                                                                      h->am[h->mc].p, h->u64s.p);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+            unsigned long long c = 0;
+            CU(cudaMemcpyAsync(&c, h->u64s.p, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+            h->sync();
+            out->active_voxel_count = int64_t(c);
+        }
+    });
+}
+
+int gbls_batch_download(gbls_handle* h, int32_t instance, gbls_grid_desc* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        if (instance < 0 || instance >= h->ninst) fail(GBLS_ERR_INVALID_ARGUMENT, "no such instance");
+        DeviceGuard g(h->device);
+        download(*h, out, instance);
+    });
+}
+
+// n independent LevelSetAdvection::advect loops (tools/LevelSetAdvect.h:338-418),
+// one substep of every still-running instance per pass.
+int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial, int temporal, float t0,
+                      float t1, float cfl, uint64_t* substeps) {
+    if (!h || !fields) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    const int n = h->ninst;
+    std::vector<uint64_t> count(static_cast<size_t>(n), 0);
+    bool interrupted = false;
+    const int rc = guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(spatial, temporal);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        std::vector<FieldParams> fp(static_cast<size_t>(n));
+        bool all_constant = true;
+        for (int i = 0; i < n; ++i) {
+            const gbls_field_desc& d = fields[i];
+            if (d.kind != GBLS_FIELD_CONSTANT && d.kind != GBLS_FIELD_ROTATION && d.kind != GBLS_FIELD_DEFORMATION)
+                fail(GBLS_ERR_UNSUPPORTED, "batch fields must be CONSTANT, ROTATION or DEFORMATION");
+            if (d.kind == GBLS_FIELD_DEFORMATION && !(d.domain > 0.0f && d.period != 0.0f))
+                fail(GBLS_ERR_VALUE, "deformation field needs domain > 0 and period != 0");
+            gbls_field tmp;
+            tmp.desc = d;
+            fp[size_t(i)] = field_params(&tmp, t0);  // no tables: direct evaluation
+            all_constant &= d.kind == GBLS_FIELD_CONSTANT;
+        }
+        h->inst_field.upload(fp.data(), fp.size(), h->stream);
+        if (t0 - t1 == 0.0f) { h->sync(); return; }
+        const bool forward = t0 < t1;
+        const float dx = float(h->voxel_size);
+        const float cfl_ref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) /
+                              std::sqrt(3.0f);
+        const float C = cfl > 0.0f ? cfl : cfl_ref;
+        std::vector<float> t(static_cast<size_t>(n), t0), dt(static_cast<size_t>(n), 0.0f);
+        std::vector<uint8_t> done(static_cast<size_t>(n), 0), run(static_cast<size_t>(n), 0);
+        std::vector<unsigned long long> act(static_cast<size_t>(n), 0);
+        std::vector<unsigned int> mx(static_cast<size_t>(n), 0);
+        // active voxels per instance
+        CU(cudaMemsetAsync(h->inst_active.p, 0, size_t(n) * sizeof(unsigned long long), h->stream));
+        if (h->nleaf > 0) {
+            k_count_active_inst<<<blocks_for(h->nleaf, 256), 256, 0, h->stream>>>(h->nleaf, h->K(), h->S(),
+                                                                                   h->am[h->mc].p, h->inst_active.p);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+        }
+        h->inst_active.download(act.data(), size_t(n), h->stream);
+        h->sync();
+        h->batch_run = true;
+        for (;;) {
+            int nrun = 0;
+            for (int i = 0; i < n; ++i) {
+                run[size_t(i)] = !done[size_t(i)] && (forward ? t[size_t(i)] < t1 : t[size_t(i)] > t1);
+                nrun += run[size_t(i)];
+            }
+            if (!nrun) break;
+            if (!check_intr(*h)) { interrupted = true; break; }
+            // sampleField per instance (:426-464)
+            for (int i = 0; i < n; ++i) {
+                if (!run[size_t(i)]) continue;
+                if (act[size_t(i)] == 0) { run[size_t(i)] = 0; done[size_t(i)] = 1; }
+            }
+            h->inst_run.upload(run.data(), size_t(n), h->stream);
+            h->inst_t0.upload(t.data(), size_t(n), h->stream);
+            if (!all_constant) {
+                CU(cudaMemsetAsync(h->inst_max.p, 0, size_t(n) * sizeof(unsigned int), h->stream));
+                CflArgs a{};
+                a.nleaf = h->nleaf;
+                a.keys = h->K();
+                a.slot = h->S();
+                a.amask = h->am[h->mc].p;
+                a.max_bits = h->inst_max.p;
+                a.inst_run = h->inst_run.p;
+                a.inst_t0 = h->inst_t0.p;
+                a.inst_field = h->inst_field.p;
+                launch_cfl(a, h->stream);
+                ++h->stats.kernel_launches;
+                CU(cudaGetLastError());
+                h->inst_max.download(mx.data(), size_t(n), h->stream);
+                h->sync();
+            }
+            uint64_t upd = 0;
+            nrun = 0;
+            for (int i = 0; i < n; ++i) {
+                if (!run[size_t(i)]) continue;
+                float maxv2;
+                if (fields[i].kind == GBLS_FIELD_CONSTANT) {
+                    const float* c = fields[i].constant;
+                    maxv2 = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+                } else {
+                    std::memcpy(&maxv2, &mx[size_t(i)], 4);
+                }
+                float d = 0.0f;
+                if (maxv2 > 1e-5f || maxv2 < -1e-5f) {
+                    const float span = std::fabs(t1 - t[size_t(i)]);
+                    const float lim = C * dx / std::sqrt(maxv2);
+                    d = (lim < span) ? lim : span;
+                }
+                if (d == 0.0f) {
+                    run[size_t(i)] = 0;
+                    done[size_t(i)] = 1;
+                    continue;
+                }
+                dt[size_t(i)] = d;
+                upd += act[size_t(i)];
+                ++nrun;
+            }
+            if (!nrun) break;
+            h->inst_run.upload(run.data(), size_t(n), h->stream);
+            h->inst_dt.upload(dt.data(), size_t(n), h->stream);
+            h->stats.voxel_updates += upd;
+            h->stats.substeps += uint64_t(nrun);
+            h->nactive = -1;
+            advect_stages(*h, nullptr, temporal, t0, 0.0f, !forward);
+            for (int i = 0; i < n; ++i) {
+                if (!run[size_t(i)]) continue;
+                t[size_t(i)] += forward ? dt[size_t(i)] : -dt[size_t(i)];
+                ++count[size_t(i)];
+            }
+            track(*h);
+            h->inst_active.download(act.data(), size_t(n), h->stream);
+            h->sync();
+        }
+        h->batch_run = false;
+        h->nactive = -1;
+        h->sync();
+    });
+    h->batch_run = false;
+    if (substeps)
+        for (int i = 0; i < n; ++i) substeps[i] = count[size_t(i)];
+    if (rc == GBLS_OK && interrupted) {
+        g_last_error = "interrupted";
+        return GBLS_ERR_INTERRUPTED;
+    }
     return rc;
 }
 

@@ -393,6 +393,59 @@ int gbls_host_union_of_spheres(int64_t n, const float* centers, const float* rad
     }
 }
 
+// Torus around the y axis through `center`: major radius R, tube radius r
+// (voxel units after dividing by dx), rasterised over its bounding box with
+// the leapfrogging of tools/LevelSetSphere.h:154-173 (the distance is exact,
+// so skipping floor(d - w) voxels never misses the band), then signed flood
+// filled.
+int gbls_host_torus(float major_radius, float minor_radius, const float center[3], float voxel_size,
+                    float half_width, gbls_host_grid** out) {
+    if (!out || !center) { g_fix_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    *out = nullptr;
+    if (!(major_radius > 0) || !(minor_radius > 0) || !(minor_radius < major_radius)) {
+        g_fix_error = "torus radii must satisfy 0 < minor < major";
+        return GBLS_ERR_VALUE;
+    }
+    if (!(voxel_size > 0.0f)) { g_fix_error = "voxel size must be positive"; return GBLS_ERR_VALUE; }
+    if (!(half_width > 1)) { g_fix_error = "half-width must be larger than one"; return GBLS_ERR_VALUE; }
+    try {
+        Tree t;
+        t.bg = static_cast<float>(double(voxel_size) * double(half_width));
+        const float dx = voxel_size, w = half_width;
+        const float R = major_radius / dx, r = minor_radius / dx;
+        const float cx = center[0] / dx, cy = center[1] / dx, cz = center[2] / dx;
+        const float ext = R + r + w, exty = r + w;
+        const int imin = int(std::floor(cx - ext)), imax = int(std::ceil(cx + ext));
+        const int jmin = int(std::floor(cy - exty)), jmax = int(std::ceil(cy + exty));
+        const int kmin = int(std::floor(cz - ext)), kmax = int(std::ceil(cz + ext));
+        const float bg = t.bg;
+        raster_parallel(imin, imax + 1, [&](int32_t a, int32_t b, LeafMap& m) {
+            for (int32_t i = a; i < b; ++i) {
+                const float x = float(i) - cx;
+                for (int32_t j = jmin; j <= jmax; ++j) {
+                    const float y2 = pow2(float(j) - cy);
+                    int step = 1;
+                    for (int32_t k = kmin; k <= kmax; k += step) {
+                        step = 1;
+                        const float q = std::sqrt(x * x + pow2(float(k) - cz)) - R;
+                        const float v = std::sqrt(q * q + y2) - r;
+                        const float d = std::fabs(v);
+                        if (d < w) set_voxel(m, i, j, k, dx * v, bg);
+                        else step += int(std::floor(d - w));
+                    }
+                }
+            }
+        }, t.leaves);
+        build_nodes(t);
+        signed_flood_fill(t);
+        *out = export_tree(t, voxel_size);
+        return GBLS_OK;
+    } catch (const std::bad_alloc&) {
+        g_fix_error = "out of host memory";
+        return GBLS_ERR_OUT_OF_MEMORY;
+    }
+}
+
 int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* d) {
     if (!g || !d) { g_fix_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     std::memset(d, 0, sizeof(*d));

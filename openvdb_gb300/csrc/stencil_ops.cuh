@@ -256,6 +256,13 @@ struct RkArgs {
     double invdx;          // 1/dx (parity: applied in double like applyIJT)
     float invdx_f;         // 1/dx in float (fast)
     FieldParams field;
+    // batches (null for a single level set): per-instance running flag, dt,
+    // substep start time and velocity field; instance = key >> 54
+    const uint8_t* inst_run;
+    const float* inst_dt;
+    const float* inst_t0;
+    const FieldParams* inst_field;
+    int copy_done;         // the stage's output becomes the result: copy finished instances
 };
 
 struct NormArgs {
@@ -276,6 +283,8 @@ struct NormArgs {
     int carry;              // 1: active voxels outside pmask stay active unchanged
                             // 0: they become inactive (erosion relayout)
     unsigned long long* acc;  // [2] += voxels processed, voxels written (may be null)
+    const uint64_t* keys;     // batches: leaf keys (instance = key >> 54)
+    const uint8_t* inst_run;  // batches: finished instances are copied through
 };
 
 struct CflArgs {
@@ -285,7 +294,10 @@ struct CflArgs {
     const uint64_t* amask;
     float t0;
     FieldParams field;
-    unsigned int* max_bits;  // float bits of max |v|^2 (values >= 0)
+    unsigned int* max_bits;  // float bits of max |v|^2 (values >= 0); [instances] for batches
+    const uint8_t* inst_run;
+    const float* inst_t0;
+    const FieldParams* inst_field;
 };
 
 // ---- kernels ----------------------------------------------------------------
@@ -316,25 +328,44 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
     __shared__ LeafStage st;
     __shared__ uint16_t list[LEAF_VOX];
     __shared__ float vtab[6][8];
+    __shared__ FieldParams sf;
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
+    const uint64_t key = a.keys[l];
+    float dt = a.dt, t0 = a.t0;
+    if (a.inst_run) {
+        const uint32_t inst = key_instance(key);
+        if (!a.inst_run[inst]) {
+            if (a.copy_done) {  // keep a finished instance's values in the result buffer
+                int n = 0;
+                for (int w = 0; w < 8; ++w) n += __popcll(a.src.amask[size_t(s) * 8 + w]);
+                for (int i = threadIdx.x; i < n; i += STENCIL_THREADS)
+                    a.out[size_t(s) * LEAF_VOX + i] = a.src.vals[size_t(s) * LEAF_VOX + i];
+            }
+            return;
+        }
+        dt = a.inst_dt[inst];
+        t0 = a.inst_t0[inst];
+        if (threadIdx.x == 0) sf = a.inst_field[inst];
+    } else if (threadIdx.x == 0) {
+        sf = a.field;
+    }
     stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
     load_tile(tile, st, a.gamma);
     const int n = build_list(list, st.am[0]);
     __syncthreads();
     int ox, oy, oz;
-    key_origin(a.keys[l], ox, oy, oz);
+    key_origin(key, ox, oy, oz);
     // deformation field: the leaf's 8 sines per axis and function, staged once
-    const bool tabbed = a.field.kind == 2 && a.field.tab && ox - a.field.tab_lo >= 0 &&
-                        oy - a.field.tab_lo >= 0 && oz - a.field.tab_lo >= 0 &&
-                        ox + 8 - a.field.tab_lo <= a.field.tab_n && oy + 8 - a.field.tab_lo <= a.field.tab_n &&
-                        oz + 8 - a.field.tab_lo <= a.field.tab_n;
+    const bool tabbed = sf.kind == 2 && sf.tab && ox - sf.tab_lo >= 0 && oy - sf.tab_lo >= 0 &&
+                        oz - sf.tab_lo >= 0 && ox + 8 - sf.tab_lo <= sf.tab_n &&
+                        oy + 8 - sf.tab_lo <= sf.tab_n && oz + 8 - sf.tab_lo <= sf.tab_n;
     if (tabbed) {
         if (threadIdx.x < 48) {
             const int ax = threadIdx.x >> 4, fn = (threadIdx.x >> 3) & 1, q = threadIdx.x & 7;
             const int o = ax == 0 ? ox : ax == 1 ? oy : oz;
-            vtab[ax * 2 + fn][q] = a.field.tab[2 * (o + q - a.field.tab_lo) + fn];
+            vtab[ax * 2 + fn][q] = sf.tab[2 * (o + q - sf.tab_lo) + fn];
         }
         __syncthreads();
     }
@@ -349,11 +380,11 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
             const float u = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, sx), sx), s2y), s2z);
             const float w = __fmul_rn(__fmul_rn(__fmul_rn(s2x, sy), sy), s2z);
             const float q = __fmul_rn(__fmul_rn(__fmul_rn(s2x, s2y), sz), sz);
-            vel[0] = __fmul_rn(u, a.field.amp);
-            vel[1] = -__fmul_rn(w, a.field.amp);
-            vel[2] = -__fmul_rn(q, a.field.amp);
+            vel[0] = __fmul_rn(u, sf.amp);
+            vel[1] = -__fmul_rn(w, sf.amp);
+            vel[2] = -__fmul_rn(q, sf.amp);
         } else {
-            eval_field(a.field, ox + x, oy + y, oz + z, a.t0, vel);
+            eval_field(sf, ox + x, oy + y, oz + z, t0, vel);
         }
         if (a.backward) { vel[0] = -vel[0]; vel[1] = -vel[1]; vel[2] = -vel[2]; }
         float g[3];
@@ -364,7 +395,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
         }
         const float dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
         const float c = tile[tile_index(x, y, z)];
-        const float r = A::sub(c, A::mul(a.dt, dot));
+        const float r = A::sub(c, A::mul(dt, dot));
         float o = r;
         if (a.has_phi) {
             const float p = a.phin[size_t(s) * LEAF_VOX + i];
@@ -392,8 +423,12 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
     const int t = threadIdx.x;
+    const bool run = !a.inst_run || a.inst_run[key_instance(a.keys[l])];
+    const int carry = run ? a.carry : 1;
+    const int trim = run ? a.trim : 0;
     stage_masks(st, a.src, s, a.nbr + 6 * l, a.pmask, pm);
     if (t < 8) {
+        if (!run) pm[t] = 0;
         um[t] = pm[t] | st.am[0][t];
         fin[t] = 0;
         fsg[t] = st.sm[0][t] & ~um[t];
@@ -413,7 +448,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         if (!(pm[v >> 6] & bit)) {
             // active voxel outside the processed set
             res[v] = val;
-            flag[v] = uint8_t((a.carry ? 1 : 0) | (val < 0.0f ? 2 : 0));
+            flag[v] = uint8_t((carry ? 1 : 0) | (val < 0.0f ? 2 : 0));
             continue;
         }
         if (!a.copy_only) {
@@ -442,8 +477,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
             val = vv;
         }
         bool act = true, neg = val < 0.0f;
-        if ((a.trim & 1) && val <= -g) { act = false; neg = true; }
-        else if ((a.trim & 2) && val >= g) { act = false; neg = false; }
+        if ((trim & 1) && val <= -g) { act = false; neg = true; }
+        else if ((trim & 2) && val >= g) { act = false; neg = false; }
         res[v] = val;
         flag[v] = uint8_t((act ? 1 : 0) | (neg ? 2 : 0));
     }
@@ -496,6 +531,6 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
 
 // Max of |v|^2 over the active voxels (LevelSetAdvection::Advect::sampleField,
 // tools/LevelSetAdvect.h:447-455): Vec3f::lengthSqr in float, no contraction.
-__global__ void cfl_max_kernel(const CflArgs a);
+__global__ void cfl_max_kernel(const __grid_constant__ CflArgs a);
 
 }  // namespace gbls

@@ -51,6 +51,15 @@ def sphere(radius, center=(0.0, 0.0, 0.0), voxel_size=1.0, half_width=3.0):
     return _from_native(h)
 
 
+def torus(major_radius, minor_radius, center=(0.0, 0.0, 0.0), voxel_size=1.0, half_width=3.0):
+    """Narrow-band torus around the y axis (batch fixtures)."""
+    h = C.c_void_p()
+    c = (C.c_float * 3)(*center)
+    check(lib().gbls_host_torus(major_radius, minor_radius, c, voxel_size, half_width, C.byref(h)),
+          host=True)
+    return _from_native(h)
+
+
 def union_of_spheres(centers, radii, voxel_size=1.0, half_width=3.0):
     c = np.ascontiguousarray(centers, np.float32).reshape(-1)
     r = np.ascontiguousarray(radii, np.float32).reshape(-1)
@@ -68,3 +77,30 @@ def sixty_four_spheres(seed=2024, n=64, domain=1024.0, rmin=20.0, rmax=80.0):
     centers = (vals[:, :3] * domain).astype(np.float32)
     radii = (rmin + vals[:, 3] * (rmax - rmin)).astype(np.float32)
     return centers, radii
+
+
+def batch_instances(n=512, seed=7, rmin=8.0, rmax=128.0):
+    """Seeded batch: 50/50 spheres and tori, radius log-uniform in [rmin, rmax],
+    torus tube ratio U[0.2, 0.4]; each with a constant-plus-rotation velocity
+    (constant U[-1,1]^3, angular velocity U[-0.01,0.01]^3 rad per time unit
+    about the shape's centre).  Returns (list of shape specs, list of Fields)."""
+    from .fields import Field
+    rng = np.random.Generator(np.random.PCG64(seed))
+    specs, fields = [], []
+    for i in range(n):
+        kind = "sphere" if rng.random() < 0.5 else "torus"
+        R = float(np.float32(np.exp(np.log(rmin) + rng.random() * (np.log(rmax) - np.log(rmin)))))
+        ratio = float(np.float32(0.2 + 0.2 * rng.random()))
+        center = tuple(float(np.float32(x)) for x in rng.random(3) * 16.0)
+        c = tuple(float(np.float32(x)) for x in rng.uniform(-1.0, 1.0, 3))
+        om = tuple(float(np.float32(x)) for x in rng.uniform(-0.01, 0.01, 3))
+        specs.append((kind, R, ratio, center))
+        fields.append(Field.rotation(c, om, center))
+    return specs, fields
+
+
+def build_instance(spec):
+    kind, R, ratio, center = spec
+    if kind == "sphere":
+        return sphere(R, center)
+    return torus(R, max(1.6, R * ratio), center)

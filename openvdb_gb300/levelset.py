@@ -283,3 +283,69 @@ class LevelSetAdvection:
             return n.value
         _call(rc)
         return n.value
+
+
+class DeviceBatch:
+    """Many independent level sets on the GPU (gbls_batch_*): each instance is
+    advanced exactly as its own LevelSetAdvection::advect call would."""
+
+    def __init__(self, grids, device=0):
+        L = lib()
+        _call(L.gbls_set_device(int(device)))
+        self._keep = list(grids)
+        descs = (_abi.GridDesc * len(self._keep))(*[g.desc() for g in self._keep])
+        self._h = C.c_void_p()
+        _call(L.gbls_batch_create(len(self._keep), descs, C.byref(self._h)))
+        self._keep = None
+        self.n = len(descs)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        try:
+            if self._h.value:
+                lib().gbls_destroy(self._h)
+        except Exception:
+            pass
+
+    def set_precision(self, mode):
+        _call(lib().gbls_set_precision(self._h, int(mode)))
+
+    def set_tracker(self, spatial=HJWENO5_BIAS, temporal=TVD_RK1, norm_count=1, grain=1):
+        _call(lib().gbls_set_tracker_state(self._h, int(spatial), int(temporal), int(norm_count),
+                                           int(grain)))
+
+    def counts(self, i):
+        c = _abi.GridCounts()
+        _call(lib().gbls_batch_get_counts(self._h, int(i), C.byref(c)))
+        return c
+
+    def to_host(self, i):
+        g = HostGrid.allocate(self.counts(i))
+        d = g.desc()
+        _call(lib().gbls_batch_download(self._h, int(i), C.byref(d)))
+        g.copy_scalars_from(d)
+        return g
+
+    def advect(self, fields, t0, t1, spatial=HJWENO5_BIAS, temporal=TVD_RK3, cfl=0.0):
+        fd = (_abi.FieldDesc * self.n)(*[f.desc() for f in fields])
+        counts = (C.c_uint64 * self.n)()
+        _call(lib().gbls_batch_advect(self._h, fd, int(spatial), int(temporal), np.float32(t0),
+                                      np.float32(t1), np.float32(cfl), counts))
+        return list(counts)
+
+    def stats(self):
+        st = _abi.Stats()
+        _call(lib().gbls_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _abi.Stats._fields_}
+
+    def reset_stats(self):
+        _call(lib().gbls_reset_stats(self._h))
+
+    def set_profiling(self, enable=True):
+        _call(lib().gbls_set_profiling(self._h, 1 if enable else 0))
+
+    def set_stream(self, stream_ptr):
+        _call(lib().gbls_set_stream(self._h, C.c_void_p(stream_ptr)))

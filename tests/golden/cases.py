@@ -131,3 +131,14 @@ def make_fixture(spec):
         c, r = union8()
         return fixtures.union_of_spheres(c, r)
     raise ValueError(spec[0])
+
+
+# Batched advection: each instance must equal its own reference advect call.
+BATCH = dict(n=6, seed=11, rmin=6.0, rmax=20.0, schemes=(HJ, RK3, HJ, RK1, 1),
+             ops=[(0.0, 1.0), (1.0, 2.0)])
+
+
+def make_batch():
+    from openvdb_gb300 import fixtures
+    specs, fields = fixtures.batch_instances(BATCH["n"], BATCH["seed"], BATCH["rmin"], BATCH["rmax"])
+    return [fixtures.build_instance(s) for s in specs], fields

@@ -19,7 +19,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from cases import CASES, make_field, make_fixture  # noqa: E402
+from cases import BATCH, CASES, make_batch, make_field, make_fixture  # noqa: E402
 from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
 from oracle import refpy  # noqa: E402
 
@@ -78,8 +78,27 @@ def main():
         last = a[-1]
         print("%-32s ops=%d final leaves=%s active=%s" % (name, len(a) - 1, last.get("summary", {}).get("leaves"),
                                                           last.get("summary", {}).get("active")))
+    result["__batch__"] = run_batch()
     with open(os.path.join(HERE, "parity_cases.json"), "w") as f:
         json.dump(result, f, indent=1, sort_keys=True)
+
+
+def run_batch():
+    """Each instance of the batch case advected alone by the reference."""
+    grids, fields = make_batch()
+    sp, tp, tsp, ttp, nc = BATCH["schemes"]
+    out = []
+    for g, f in zip(grids, fields):
+        r = refpy.RefGrid.from_host(g)
+        rec = [{"op": "input", "digest": digest(g), "summary": summary(g)}]
+        for t0, t1 in BATCH["ops"]:
+            n = r.advect(f, t0, t1, spatial=sp, temporal=tp, tracker_spatial=tsp, tracker_temporal=ttp,
+                         norm_count=nc)
+            h = r.to_host()
+            rec.append({"op": ["advect", t0, t1], "count": n, "digest": digest(h), "summary": summary(h)})
+        out.append(rec)
+    print("batch: %d instances" % len(out))
+    return out
 
 
 if __name__ == "__main__":

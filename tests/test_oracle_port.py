@@ -53,3 +53,16 @@ def test_port_matches_reference(name):
 
 def test_port_thread_independent():
     run_port("sphere20_deformation", threads=1)
+
+
+def test_port_batch_instances_match_reference():
+    from cases import BATCH, make_batch
+    grids, fields = make_batch()
+    sp, tp, tsp, ttp, nc = BATCH["schemes"]
+    for g, f, rec in zip(grids, fields, GOLD["__batch__"]):
+        p = port.PortGrid(g)
+        for step, (t0, t1) in enumerate(BATCH["ops"], start=1):
+            n = p.advect(f, t0, t1, spatial=sp, temporal=tp, tracker_spatial=tsp, tracker_temporal=ttp,
+                         norm_count=nc)
+            assert n == rec[step]["count"]
+            assert digest(p.to_host()) == rec[step]["digest"]
