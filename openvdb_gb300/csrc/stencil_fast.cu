@@ -1,17 +1,21 @@
 // FP32 stencil kernels and the CFL reduction.
 #include "stencil.h"
 #include "stencil_ops.cuh"
+#include "stencil_fast2.cuh"
 
 namespace gbls {
 
 void launch_rk_fast(const RkArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    rk_stage_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    rk_stage_kernel_x2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 void launch_norm_fast(const NormArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    normalize_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    if (!a.copy_only && !a.has_phi)
+        normalize_kernel_x2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    else
+        normalize_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 // One CTA per leaf, thread t visits bit t of each active-mask word;
