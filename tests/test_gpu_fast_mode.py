@@ -55,5 +55,5 @@ def test_fast_mode_close_to_parity(name):
         worst = max(worst, dmax / band)
         print("%s step %d: max|dphi| = %.3g (%.3g of band width), active-state flips %d of %d"
               % (name, k + 1, dmax, dmax / band, flips, n))
-        assert flips <= max(8, n // 20000), (name, k, flips)
-    assert worst <= 1e-4, worst
+        assert flips == 0, (name, k, flips)
+    assert worst <= 1e-5, worst
