@@ -205,6 +205,27 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
 
 
 
+/* ---- adjoint ---------------------------------------------------------------
+ * No counterpart in the reference (it has no derivatives).  While recording
+ * is enabled, every CFL substep of gbls_advect (TVD_RK3 advection, TVD_RK1
+ * tracker with normCount 1 and full trimming) is written to a tape on the
+ * device.  gbls_adjoint_backward then runs the transposed substeps in reverse
+ * with the recorded topology, upwind directions, Godunov branches, trimming
+ * and dt held fixed:
+ *   dl_final[n_final]     dL/dphi on the active voxels after the last
+ *                         recorded substep, in canonical order (tree-ordered
+ *                         leaves, voxels in leaf order)
+ *   dl_initial[n_initial] receives dL/dphi on the active voxels before the
+ *                         first recorded substep, same order
+ *   dl_velocity           receives dL/dv on a DENSE field's grid
+ *                         [nx][ny][nz][3] (may be NULL; zero for other kinds)
+ * `field` must be the field the recorded substeps used.  Recording again
+ * (or disabling it) discards the tape.                                     */
+int gbls_adjoint_record(gbls_handle* h, int enable);
+int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int64_t* substeps);
+int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final,
+                          float* dl_initial, float* dl_velocity);
+
 /* ---- batches of independent level sets --------------------------------------
  * A batch handle holds n level sets (instances) that share the voxel size and
  * background; gbls_batch_advect advances every instance i from t0 to t1 with

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -14,6 +15,7 @@
 #include <vector>
 
 #include "../../include/gbls.h"
+#include "adjoint.h"
 #include "gbls_internal.cuh"
 #include "stencil.h"
 #include "stencil_ops.cuh"
@@ -367,6 +369,23 @@ __global__ void k_unpack(int64_t n, const int32_t* slot, const uint64_t* am, con
 // handle
 // ---------------------------------------------------------------------------
 
+// One recorded CFL substep of the adjoint tape (leaf-index numbering).
+struct TapeStep {
+    // RK part on the substep's leaf list
+    int64_t n = 0;
+    DevArray<uint64_t> keys, am, sm;
+    DevArray<int32_t> nbr;
+    DevArray<float> phin, phi1, phi2;
+    float dt = 0.0f, t0 = 0.0f;
+    bool backward = false;
+    // tracker part on the dilated (merged) list
+    int64_t nm = 0;
+    DevArray<uint64_t> keys_m, am3, sm3, pmask, fin;
+    DevArray<int32_t> nbr_m, keep, idx;
+    DevArray<float> phi3;
+    float gamma = 0.0f;
+};
+
 struct gbls_field {
     gbls_field_desc desc{};
     int device = 0;
@@ -426,6 +445,11 @@ struct gbls_handle {
     DevArray<unsigned int> inst_max;
     DevArray<unsigned long long> inst_active;
     const uint8_t* run_ptr() const { return batch_run ? inst_run.p : nullptr; }
+    // adjoint tape
+    bool tape_on = false;
+    std::vector<std::unique_ptr<TapeStep>> tape;
+    TapeStep* tape_cur = nullptr;
+    DevArray<int32_t> tape_inv;
     // measurement
     gbls_stats stats{};
     int64_t nactive = -1;  // active voxels, -1 = unknown
@@ -804,6 +828,40 @@ void launch_norm(gbls_handle& h, const NormArgs& a0) {
     ++h.stats.kernel_launches;
 }
 
+// ---- adjoint tape recording ----------------------------------------------
+void tape_list(gbls_handle& h, int64_t n, DevArray<uint64_t>& keys, DevArray<int32_t>& nbr) {
+    keys.reserve(size_t(std::max<int64_t>(n, 1)), h.stream);
+    nbr.reserve(size_t(std::max<int64_t>(n, 1)) * 6, h.stream);
+    if (n == 0) return;
+    CU(cudaMemcpyAsync(keys.p, h.K(), size_t(n) * 8, cudaMemcpyDeviceToDevice, h.stream));
+    h.tape_inv.reserve(size_t(h.slot_cap), h.stream);
+    launch_nbr_to_index(n, h.S(), h.nbr.p, h.tape_inv.p, h.slot_cap, nbr.p, h.stream);
+    CU(cudaGetLastError());
+}
+
+void tape_values(gbls_handle& h, int64_t n, int m, int v, DevArray<uint64_t>* am, DevArray<uint64_t>* sm,
+                 DevArray<float>* vals) {
+    if (am) am->reserve(size_t(std::max<int64_t>(n, 1)) * 8, h.stream);
+    if (sm) sm->reserve(size_t(std::max<int64_t>(n, 1)) * 8, h.stream);
+    if (vals) vals->reserve(size_t(std::max<int64_t>(n, 1)) * LEAF_VOX, h.stream);
+    launch_tape_gather(n, h.S(), h.am[m].p, h.sm[m].p, v >= 0 ? h.vals[v].p : nullptr, am ? am->p : nullptr,
+                       sm ? sm->p : nullptr, vals ? vals->p : nullptr, h.stream);
+    CU(cudaGetLastError());
+}
+
+void tape_begin_substep(gbls_handle& h, float t0, float dt, bool backward) {
+    h.tape.emplace_back(new TapeStep);
+    TapeStep& st = *h.tape.back();
+    h.tape_cur = &st;
+    st.n = h.nleaf;
+    st.dt = dt;
+    st.t0 = t0;
+    st.backward = backward;
+    st.gamma = h.gamma;
+    tape_list(h, st.n, st.keys, st.nbr);
+    tape_values(h, st.n, h.mc, h.vc, &st.am, &st.sm, &st.phin);
+}
+
 void start_intr(gbls_handle& h, const char* msg) {
     if (h.has_intr && h.intr.start) h.intr.start(h.intr.user, msg);
 }
@@ -993,7 +1051,17 @@ void prune_compact(gbls_handle& h) {
 
 void track(gbls_handle& h) {
     dilate_topology(h);
+    TapeStep* tp = h.tape_cur;
+    if (tp) {
+        tp->nm = h.nleaf;
+        tape_list(h, tp->nm, tp->keys_m, tp->nbr_m);
+        tape_values(h, tp->nm, h.mc, h.vc, &tp->am3, &tp->sm3, &tp->phi3);
+        tp->pmask.reserve(size_t(std::max<int64_t>(tp->nm, 1)) * 8, h.stream);
+        launch_mask_gather(tp->nm, h.S(), h.dmask.p, tp->pmask.p, h.stream);
+        CU(cudaGetLastError());
+    }
     normalize_pass(h, h.dmask.p, h.trim);
+    if (tp) tape_values(h, tp->nm, h.mc, -1, &tp->fin, nullptr, nullptr);
     if (h.nleaf > 0 && h.norm_count <= 0 && !h.trim) {
         // no normalisation and no trimming: the dilated mask becomes active as is
         NormArgs a{};
@@ -1013,9 +1081,18 @@ void track(gbls_handle& h) {
         h.mc = mo;
         h.vc = vo;
     }
+    if (tp) {  // prune_compact overwrites keep / idx only when the list is non-empty
+        tp->keep.reserve(size_t(std::max<int64_t>(tp->nm, 1)), h.stream);
+        tp->idx.reserve(size_t(std::max<int64_t>(tp->nm, 1)), h.stream);
+    }
     start_intr(h, "Pruning Level Set");
     prune_compact(h);
     end_intr(h);
+    if (tp && tp->nm > 0) {
+        CU(cudaMemcpyAsync(tp->keep.p, h.keep.p, size_t(tp->nm) * 4, cudaMemcpyDeviceToDevice, h.stream));
+        CU(cudaMemcpyAsync(tp->idx.p, h.idx.p, size_t(tp->nm) * 4, cudaMemcpyDeviceToDevice, h.stream));
+    }
+    h.tape_cur = nullptr;
 }
 
 void check_scheme(int spatial, int temporal) {
@@ -1141,7 +1218,9 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
         h.vc = a0;
     } else {
         stage(a0, a0, b0, 0.0f, 0, "Advecting level set using TVD_RK3 (step 1 of 3)");
+        if (h.tape_cur) tape_values(h, h.nleaf, h.mc, b0, nullptr, nullptr, &h.tape_cur->phi1);
         stage(b0, a0, c0, 3.0f / 4.0f, 1, "Advecting level set using TVD_RK3 (step 2 of 3)");
+        if (h.tape_cur) tape_values(h, h.nleaf, h.mc, c0, nullptr, nullptr, &h.tape_cur->phi2);
         stage(c0, a0, a0, 1.0f / 3.0f, 1, "Advecting level set using TVD_RK3 (step 3 of 3)");
         h.vc = a0;
     }
@@ -1676,6 +1755,165 @@ int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
     return rc;
 }
 
+// ---- adjoint -----------------------------------------------------------------
+int gbls_adjoint_record(gbls_handle* h, int enable) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        h->sync();
+        h->tape.clear();
+        h->tape_cur = nullptr;
+        h->tape_on = enable != 0;
+    });
+}
+
+namespace {
+// Active counts of the leaves of a recorded mask array (host).
+std::vector<int> mask_counts(gbls_handle& h, const DevArray<uint64_t>& m, int64_t n) {
+    std::vector<uint64_t> w(static_cast<size_t>(n) * 8);
+    m.download(w.data(), w.size(), h.stream);
+    h.sync();
+    std::vector<int> c(static_cast<size_t>(n));
+    for (int64_t l = 0; l < n; ++l) {
+        int k = 0;
+        for (int q = 0; q < 8; ++q) k += __builtin_popcountll(w[size_t(l) * 8 + q]);
+        c[size_t(l)] = k;
+    }
+    return c;
+}
+}  // namespace
+
+int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int64_t* substeps) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (substeps) *substeps = int64_t(h->tape.size());
+        if (n_final) *n_final = active_count(*h);
+        if (n_initial) {
+            if (h->tape.empty()) *n_initial = active_count(*h);
+            else {
+                const auto c = mask_counts(*h, h->tape[0]->am, h->tape[0]->n);
+                int64_t t = 0;
+                for (int x : c) t += x;
+                *n_initial = t;
+            }
+        }
+    });
+}
+
+// Reverse sweep over the tape: dL/dphi on the final active voxels (canonical
+// order) -> dL/dphi on the initial active voxels and, for a DENSE field,
+// dL/dvelocity on its grid.
+int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final, float* dl_initial,
+                          float* dl_velocity) {
+    if (!h || !field || !dl_final || !dl_initial) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (h->tape.empty()) fail(GBLS_ERR_INVALID_ARGUMENT, "no recorded substeps");
+        const int S = int(h->tape.size());
+        cudaStream_t st = h->stream;
+        // final list = kept leaves of the last merged list, with masks fin
+        TapeStep& last = *h->tape[size_t(S - 1)];
+        std::vector<int32_t> keep(static_cast<size_t>(last.nm));
+        if (last.nm) last.keep.download(keep.data(), keep.size(), st);
+        const auto finc = mask_counts(*h, last.fin, last.nm);
+        std::vector<float> lam_h;
+        int64_t nf = 0, off = 0;
+        for (int64_t i = 0; i < last.nm; ++i) if (keep[size_t(i)]) ++nf;
+        lam_h.assign(size_t(std::max<int64_t>(nf, 1)) * LEAF_VOX, 0.0f);
+        int64_t j = 0;
+        for (int64_t i = 0; i < last.nm; ++i) {
+            if (!keep[size_t(i)]) continue;
+            for (int r = 0; r < finc[size_t(i)]; ++r) lam_h[size_t(j) * LEAF_VOX + r] = dl_final[off + r];
+            off += finc[size_t(i)];
+            ++j;
+        }
+        DevArray<float> lam_next, lam4, lam3, lamA, lp2, lp1, lpn, dvel;
+        lam_next.upload(lam_h.data(), lam_h.size(), st);
+        const bool want_vel = dl_velocity && field->desc.kind == GBLS_FIELD_DENSE;
+        size_t nvel = 0;
+        if (want_vel) {
+            nvel = size_t(field->desc.dense_dims[0]) * field->desc.dense_dims[1] * field->desc.dense_dims[2] * 3;
+            dvel.reserve(nvel, st);
+            CU(cudaMemsetAsync(dvel.p, 0, nvel * 4, st));
+        }
+        const float dx = float(h->voxel_size);
+        const float mdt = dx * 0.3f, invdx = 1.0f / dx;
+        for (int s = S - 1; s >= 0; --s) {
+            TapeStep& tp = *h->tape[size_t(s)];
+            const size_t nm = size_t(std::max<int64_t>(tp.nm, 1)) * LEAF_VOX, n = size_t(std::max<int64_t>(tp.n, 1)) * LEAF_VOX;
+            lam4.reserve(nm, st);
+            lam3.reserve(nm, st);
+            CU(cudaMemsetAsync(lam3.p, 0, nm * 4, st));
+            AdjExpandArgs ea{tp.nm, tp.pmask.p, tp.fin.p, tp.keep.p, tp.idx.p, lam_next.p, lam4.p};
+            launch_adj_expand(ea, st);
+            AdjNormArgs na{};
+            na.nleaf = tp.nm;
+            na.nbr = tp.nbr_m.p;
+            na.src = Layout{tp.am3.p, tp.sm3.p, tp.phi3.p};
+            na.pmask = tp.pmask.p;
+            na.lam4 = lam4.p;
+            na.lam3 = lam3.p;
+            na.gamma = tp.gamma;
+            na.mdt = mdt;
+            na.invdx = invdx;
+            launch_adj_norm(na, st);
+            lamA.reserve(n, st);
+            AdjMapArgs ma{tp.n, tp.keys.p, tp.am.p, tp.keys_m.p, tp.nm, lam3.p, lamA.p};
+            launch_adj_map(ma, st);
+            lp2.reserve(n, st);
+            lp1.reserve(n, st);
+            lpn.reserve(n, st);
+            CU(cudaMemsetAsync(lp2.p, 0, n * 4, st));
+            CU(cudaMemsetAsync(lp1.p, 0, n * 4, st));
+            CU(cudaMemsetAsync(lpn.p, 0, n * 4, st));
+            AdjRkArgs ra{};
+            ra.nleaf = tp.n;
+            ra.keys = tp.keys.p;
+            ra.nbr = tp.nbr.p;
+            ra.dt = tp.dt;
+            ra.gamma = tp.gamma;
+            ra.invdx = invdx;
+            ra.t0 = tp.t0;
+            ra.backward = tp.backward ? 1 : 0;
+            ra.field = field_params(field, tp.t0);
+            ra.field.tab = nullptr;  // direct evaluation in the adjoint
+            ra.dvel = want_vel ? dvel.p : nullptr;
+            // stage 3: phi3 = 1/3 phin + 2/3 (phi2 - dt v.grad phi2)
+            ra.src = Layout{tp.am.p, tp.sm.p, tp.phi2.p};
+            ra.lam_out = lamA.p; ra.lam_in = lp2.p; ra.lam_phin = lpn.p;
+            ra.alpha = 1.0f / 3.0f; ra.beta = 1.0f - 1.0f / 3.0f;
+            launch_adj_rk(ra, st);
+            // stage 2: phi2 = 3/4 phin + 1/4 (phi1 - dt v.grad phi1)
+            ra.src = Layout{tp.am.p, tp.sm.p, tp.phi1.p};
+            ra.lam_out = lp2.p; ra.lam_in = lp1.p; ra.lam_phin = lpn.p;
+            ra.alpha = 3.0f / 4.0f; ra.beta = 1.0f - 3.0f / 4.0f;
+            launch_adj_rk(ra, st);
+            // stage 1: phi1 = phin - dt v.grad phin
+            ra.src = Layout{tp.am.p, tp.sm.p, tp.phin.p};
+            ra.lam_out = lp1.p; ra.lam_in = lpn.p; ra.lam_phin = lpn.p;
+            ra.alpha = 0.0f; ra.beta = 1.0f;
+            launch_adj_rk(ra, st);
+            CU(cudaGetLastError());
+            h->stats.kernel_launches += 6;
+            std::swap(lam_next.p, lpn.p);
+            std::swap(lam_next.cap, lpn.cap);
+        }
+        // initial list: the first step's list and masks
+        TapeStep& first = *h->tape[0];
+        const auto c0 = mask_counts(*h, first.am, first.n);
+        std::vector<float> out(size_t(std::max<int64_t>(first.n, 1)) * LEAF_VOX);
+        lam_next.download(out.data(), size_t(first.n) * LEAF_VOX, st);
+        if (want_vel) dvel.download(dl_velocity, nvel, st);
+        h->sync();
+        off = 0;
+        for (int64_t l = 0; l < first.n; ++l) {
+            for (int r = 0; r < c0[size_t(l)]; ++r) dl_initial[off + r] = out[size_t(l) * LEAF_VOX + r];
+            off += c0[size_t(l)];
+        }
+    });
+}
+
 int gbls_batch_create(int32_t n, const gbls_grid_desc* descs, gbls_handle** out) {
     if (!descs || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     *out = nullptr;
@@ -2017,6 +2255,13 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             if (h->nactive < 0) h->nactive = active_count(*h);
             h->stats.voxel_updates += uint64_t(h->nactive);
             ++h->stats.substeps;
+            if (h->tape_on) {
+                if (temporal != GBLS_TVD_RK3 || h->tr_temporal != GBLS_TVD_RK1 || h->norm_count != 1 ||
+                    h->trim != GBLS_TRIM_ALL)
+                    fail(GBLS_ERR_UNSUPPORTED, "the adjoint records TVD_RK3 advection with a TVD_RK1 tracker, "
+                                               "normCount 1 and full trimming");
+                tape_begin_substep(*h, t0, dt, !forward);
+            }
             advect_stages(*h, field, temporal, t0, dt, !forward);
             t0 += forward ? dt : -dt;
             ++count;
