@@ -27,6 +27,10 @@ def lib():
         L.oport_last_error.restype = C.c_char_p
         L.oport_create.argtypes = [C.POINTER(_abi.GridDesc), C.c_int]
         L.oport_create.restype = vp
+        L.oport_create_prec.argtypes = [C.POINTER(_abi.GridDesc), C.c_int, C.c_int]
+        L.oport_create_prec.restype = vp
+        L.oport_active_values.argtypes = [vp, C.POINTER(C.c_double)]
+        L.oport_set_active_values.argtypes = [vp, C.POINTER(C.c_double)]
         L.oport_free.argtypes = [vp]
         L.oport_free.restype = None
         L.oport_set_threads.argtypes = [vp, C.c_int]
@@ -56,10 +60,22 @@ def _check(rc):
 class PortGrid:
     """A level set held by the C++ restatement."""
 
-    def __init__(self, host, threads=0):
+    def __init__(self, host, threads=0, precision=32):
+        """precision 32: bit-identical to the reference; 64: the same scheme
+        (same constants, same operations) evaluated in FP64."""
         d = host.desc()
-        self.h = C.c_void_p(lib().oport_create(C.byref(d), int(threads)))
+        self.h = C.c_void_p(lib().oport_create_prec(C.byref(d), int(threads), int(precision)))
         self.updates = 0
+
+    def active_values(self):
+        out = np.zeros(self.counts().active_voxel_count, np.float64)
+        _check(lib().oport_active_values(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def set_active_values(self, values):
+        v = np.ascontiguousarray(values, np.float64)
+        assert v.size == self.counts().active_voxel_count
+        _check(lib().oport_set_active_values(self.h, v.ctypes.data_as(C.POINTER(C.c_double))))
 
     def __del__(self):
         if getattr(self, "h", None) and self.h.value and _lib is not None:

@@ -33,6 +33,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <type_traits>
 #include <unordered_set>
 #include <vector>
 
@@ -70,640 +71,39 @@ struct Pool {
     }
 };
 
-struct Leaf {
-    uint64_t key;
-    uint64_t mask[8];
-    float buf[3][512];  // buffer 0 = the tree's values; 1, 2 = RK auxiliaries
-};
+namespace p32 {
+using Real = float;
+#include "port_impl.h"
+Advector adv_of(Grid&);
+}  // namespace p32
+namespace p64 {
+using Real = double;
+#include "port_impl.h"
+Advector adv_of(Grid&);
+}  // namespace p64
 
-inline bool on(const uint64_t* m, int n) { return (m[n >> 6] >> (n & 63)) & 1; }
-inline void set_on(uint64_t* m, int n) { m[n >> 6] |= uint64_t(1) << (n & 63); }
-inline void set_off(uint64_t* m, int n) { m[n >> 6] &= ~(uint64_t(1) << (n & 63)); }
+}  // namespace
 
-// ---- arithmetic of the reference (math/FiniteDifference.h:301-321) -------
-inline float weno5(float v1, float v2, float v3, float v4, float v5) {
-    const double C = 13.0 / 12.0;
-    const double eps = 1.0e-6 * static_cast<double>(0.01f);
-    auto p2f = [](float x) { return x * x; };
-    auto p2d = [](double x) { return x * x; };
-    const double A1 = 0.1 / p2d(C * p2f(v1 - 2 * v2 + v3) + 0.25 * p2d(v1 - 4 * v2 + 3.0 * v3) + eps),
-                 A2 = 0.6 / p2d(C * p2f(v2 - 2 * v3 + v4) + 0.25 * p2f(v2 - v4) + eps),
-                 A3 = 0.3 / p2d(C * p2f(v3 - 2 * v4 + v5) + 0.25 * p2d(3.0 * v3 - 4 * v4 + v5) + eps);
-    return static_cast<float>(static_cast<float>(A1 * (2.0 * v1 - 7.0 * v2 + 11.0 * v3) +
-                                                 A2 * (5.0 * v3 - v2 + 2.0 * v4) +
-                                                 A3 * (2.0 * v3 + 5.0 * v4 - v5)) /
-                              (6.0 * (A1 + A2 + A3)));
-}
-// D1<FD_HJWENO5>::difference(xp3, xp2, xp1, xp0, xm1, xm2)
-inline float hj_fd(float xp3, float xp2, float xp1, float xp0, float xm1, float xm2) {
-    return weno5(xp3 - xp2, xp2 - xp1, xp1 - xp0, xp0 - xm1, xm1 - xm2);
-}
-// D1<BD_HJWENO5>::difference(xm3, xm2, xm1, xm0, xp1, xp2) = -FD(...)
-inline float hj_bd(float xm3, float xm2, float xm1, float xm0, float xp1, float xp2) {
-    return -hj_fd(xm3, xm2, xm1, xm0, xp1, xp2);
-}
-inline float fmaxr(float a, float b) { return (a < b) ? b : a; }  // std::max
-inline float fminr(float a, float b) { return (b < a) ? b : a; }  // std::min
+namespace {
 
-// ---- the level set ---------------------------------------------------------
-struct Grid {
-    float gamma = 3.0f;
-    double voxel_size = 1.0;
-    double translation[3] = {0, 0, 0};
-    int map_type = GBLS_MAP_UNIFORM_SCALE;
-    std::vector<Leaf*> leaves;                       // tree order
-    std::unordered_map<uint64_t, Leaf*> index;       // key -> leaf
-    std::map<uint64_t, std::vector<uint64_t>> lower; // lower key -> 64 sign words
-    std::map<uint64_t, std::vector<uint64_t>> upper; // upper key -> 512 sign words
-    std::map<uint64_t, uint8_t> root;                // upper key -> tile sign
-    Pool pool;
-
-    ~Grid() { for (Leaf* l : leaves) delete l; }
-
-    // sign of the tile covering leaf-sized region k (ValueAccessor::getValue)
-    int tile_sign(uint64_t k) const {
-        auto li = lower.find(k >> 12);
-        if (li != lower.end()) { const uint32_t n = uint32_t(k & 4095); return int((li->second[n >> 6] >> (n & 63)) & 1); }
-        auto ui = upper.find(k >> 27);
-        if (ui != upper.end()) { const uint32_t n = uint32_t((k >> 12) & 32767); return int((ui->second[n >> 6] >> (n & 63)) & 1); }
-        auto ri = root.find(k >> 27);
-        return ri != root.end() ? ri->second : 0;
-    }
-    Leaf* probe(uint64_t k) const {
-        auto it = index.find(k);
-        return it == index.end() ? nullptr : it->second;
-    }
-    void rebuild_order() {
-        std::sort(leaves.begin(), leaves.end(), [](const Leaf* a, const Leaf* b) { return a->key < b->key; });
-    }
-    size_t active_count() const {
-        size_t n = 0;
-        for (const Leaf* l : leaves) for (int w = 0; w < 8; ++w) n += size_t(__builtin_popcountll(l->mask[w]));
-        return n;
+// A grid of either precision behind the C interface.
+struct Handle {
+    int prec;  // 32 or 64
+    p32::Grid* g32 = nullptr;
+    p64::Grid* g64 = nullptr;
+    ~Handle() {
+        delete g32;
+        delete g64;
     }
 };
 
-inline uint64_t nkey(uint64_t k, int f) {
-    int32_t x, y, z;
-    origin_of(k, x, y, z);
-    if (f == 0) x -= 8; else if (f == 1) x += 8; else if (f == 2) y -= 8; else if (f == 3) y += 8; else if (f == 4) z -= 8; else z += 8;
-    return key_of(x, y, z);
+template <class F32, class F64>
+auto dispatch(void* hp, F32&& f32, F64&& f64) {
+    Handle* h = static_cast<Handle*>(hp);
+    return h->prec == 64 ? f64(*h->g64) : f32(*h->g32);
 }
 
-// 14^3 view of buffer `b` around a leaf: centre values and three-voxel face
-// slabs (NineteenPointStencil, math/Stencils.h:816-863, reads only these).
-struct Tile {
-    float v[14 * 14 * 14];
-    float& at(int x, int y, int z) { return v[(x + 3) * 196 + (y + 3) * 14 + (z + 3)]; }
-    float at(int x, int y, int z) const { return v[(x + 3) * 196 + (y + 3) * 14 + (z + 3)]; }
-};
-
-void gather(const Grid& g, const Leaf* L, int b, Tile& t) {
-    for (int n = 0; n < 512; ++n) t.at(n >> 6, (n >> 3) & 7, n & 7) = L->buf[b][n];
-    for (int f = 0; f < 6; ++f) {
-        const uint64_t k = nkey(L->key, f);
-        const Leaf* N = g.probe(k);
-        const float tv = N ? 0.0f : (g.tile_sign(k) ? -g.gamma : g.gamma);
-        for (int d = 0; d < 3; ++d)
-            for (int a = 0; a < 8; ++a)
-                for (int c = 0; c < 8; ++c) {
-                    int x, y, z, nx, ny, nz;
-                    switch (f) {
-                    case 0: x = -3 + d; y = a; z = c; nx = 5 + d; ny = a; nz = c; break;
-                    case 1: x = 8 + d; y = a; z = c; nx = d; ny = a; nz = c; break;
-                    case 2: x = a; y = -3 + d; z = c; nx = a; ny = 5 + d; nz = c; break;
-                    case 3: x = a; y = 8 + d; z = c; nx = a; ny = d; nz = c; break;
-                    case 4: x = a; y = c; z = -3 + d; nx = a; ny = c; nz = 5 + d; break;
-                    default: x = a; y = c; z = 8 + d; nx = a; ny = c; nz = d; break;
-                    }
-                    t.at(x, y, z) = N ? N->buf[b][(nx << 6) | (ny << 3) | nz] : tv;
-                }
-    }
-}
-
-struct Field {
-    gbls_field_desc d{};
-    std::vector<float> dense;
-    void eval(int i, int j, int k, float t, float out[3]) const {
-        switch (d.kind) {
-        case GBLS_FIELD_CONSTANT: out[0] = d.constant[0]; out[1] = d.constant[1]; out[2] = d.constant[2]; break;
-        case GBLS_FIELD_DENSE: {
-            const int a = i - d.dense_origin[0], b = j - d.dense_origin[1], c = k - d.dense_origin[2];
-            if (a >= 0 && b >= 0 && c >= 0 && a < d.dense_dims[0] && b < d.dense_dims[1] && c < d.dense_dims[2]) {
-                const float* p = dense.data() + 3 * ((size_t(a) * d.dense_dims[1] + b) * d.dense_dims[2] + c);
-                out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
-            } else {
-                out[0] = d.dense_background[0]; out[1] = d.dense_background[1]; out[2] = d.dense_background[2];
-            }
-            break;
-        }
-        case GBLS_FIELD_DEFORMATION: gbls_deformation(i, j, k, t, d.domain, d.period, d.scale, out); break;
-        default: gbls_rotation(i, j, k, d.constant, d.omega, d.center, out); break;
-        }
-    }
-};
-
-struct Tracker {
-    int spatial = GBLS_HJWENO5_BIAS, temporal = GBLS_TVD_RK1, norm_count = 3, trim = GBLS_TRIM_ALL;
-};
-
-// ---- Normalizer (tools/LevelSetTracker.h:511-676) --------------------------
-// One stage: result[n] = N ? alpha*phi[n] + beta*v : v over the voxels of the
-// process set (the active set, or `mask` when given).
-void norm_stage(Grid& g, const Tracker& tr, int phiBuf, int resBuf, float alpha, bool hasPhi,
-                const std::unordered_map<uint64_t, std::vector<uint64_t>>* mask) {
-    const float dx = float(g.voxel_size);
-    const float mDt = dx * (tr.temporal == GBLS_TVD_RK1 ? 0.3f : tr.temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f);
-    const float mInvDx = 1.0f / dx;
-    const float beta = 1.0f - alpha;
-    g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-        Tile t;
-        for (size_t li = a; li < b; ++li) {
-            Leaf* L = g.leaves[li];
-            const uint64_t* pm = L->mask;
-            if (mask) {
-                auto it = mask->find(L->key);
-                if (it == mask->end()) continue;
-                pm = it->second.data();
-            }
-            gather(g, L, 0, t);
-            for (int n = 0; n < 512; ++n) {
-                if (!on(pm, n)) continue;
-                const int x = n >> 6, y = (n >> 3) & 7, z = n & 7;
-                auto S = [&](int dx_, int dy_, int dz_) { return t.at(x + dx_, y + dy_, z + dz_); };
-                const float up[3] = {hj_fd(S(3, 0, 0), S(2, 0, 0), S(1, 0, 0), S(0, 0, 0), S(-1, 0, 0), S(-2, 0, 0)),
-                                     hj_fd(S(0, 3, 0), S(0, 2, 0), S(0, 1, 0), S(0, 0, 0), S(0, -1, 0), S(0, -2, 0)),
-                                     hj_fd(S(0, 0, 3), S(0, 0, 2), S(0, 0, 1), S(0, 0, 0), S(0, 0, -1), S(0, 0, -2))};
-                const float dn[3] = {hj_bd(S(-3, 0, 0), S(-2, 0, 0), S(-1, 0, 0), S(0, 0, 0), S(1, 0, 0), S(2, 0, 0)),
-                                     hj_bd(S(0, -3, 0), S(0, -2, 0), S(0, -1, 0), S(0, 0, 0), S(0, 1, 0), S(0, 2, 0)),
-                                     hj_bd(S(0, 0, -3), S(0, 0, -2), S(0, 0, -1), S(0, 0, 0), S(0, 0, 1), S(0, 0, 2))};
-                const float phi0 = S(0, 0, 0);
-                // GodunovsNormSqrd(phi0 > 0, down, up) (math/FiniteDifference.h:324-357)
-                float nsq;
-                if (phi0 > 0) {
-                    nsq = fmaxr(fmaxr(dn[0], 0) * fmaxr(dn[0], 0), fminr(up[0], 0) * fminr(up[0], 0));
-                    nsq += fmaxr(fmaxr(dn[1], 0) * fmaxr(dn[1], 0), fminr(up[1], 0) * fminr(up[1], 0));
-                    nsq += fmaxr(fmaxr(dn[2], 0) * fmaxr(dn[2], 0), fminr(up[2], 0) * fminr(up[2], 0));
-                } else {
-                    nsq = fmaxr(fminr(dn[0], 0) * fminr(dn[0], 0), fmaxr(up[0], 0) * fmaxr(up[0], 0));
-                    nsq += fmaxr(fminr(dn[1], 0) * fminr(dn[1], 0), fmaxr(up[1], 0) * fmaxr(up[1], 0));
-                    nsq += fmaxr(fminr(dn[2], 0) * fminr(dn[2], 0), fmaxr(up[2], 0) * fmaxr(up[2], 0));
-                }
-                // eval (tools/LevelSetTracker.h:623-643)
-                float v = phi0 / (std::sqrt(phi0 * phi0 + nsq) + 1e-8f);
-                v = phi0 - mDt * v * (std::sqrt(nsq) * mInvDx - 1.0f);
-                L->buf[resBuf][n] = hasPhi ? alpha * L->buf[phiBuf][n] + beta * v : v;
-            }
-        }
-    });
-}
-
-void copy_aux(Grid& g, int nAux) {
-    g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-        for (size_t i = a; i < b; ++i)
-            for (int k = 1; k <= nAux; ++k) std::memcpy(g.leaves[i]->buf[k], g.leaves[i]->buf[0], 2048);
-    });
-}
-void swap_buf(Grid& g, int k) {
-    for (Leaf* L : g.leaves) {
-        float tmp[512];
-        std::memcpy(tmp, L->buf[0], 2048);
-        std::memcpy(L->buf[0], L->buf[k], 2048);
-        std::memcpy(L->buf[k], tmp, 2048);
-    }
-}
-
-// Normalizer::normalize (:528-598)
-void normalize(Grid& g, const Tracker& tr, const std::unordered_map<uint64_t, std::vector<uint64_t>>* mask) {
-    copy_aux(g, tr.temporal == GBLS_TVD_RK3 ? 2 : 1);
-    for (int n = 0; n < tr.norm_count; ++n) {
-        if (tr.temporal == GBLS_TVD_RK1) {
-            norm_stage(g, tr, 0, 1, 0.0f, false, mask); swap_buf(g, 1);
-        } else if (tr.temporal == GBLS_TVD_RK2) {
-            norm_stage(g, tr, 0, 1, 0.0f, false, mask); swap_buf(g, 1);
-            norm_stage(g, tr, 1, 1, 1.0f / 2.0f, true, mask); swap_buf(g, 1);
-        } else {
-            norm_stage(g, tr, 0, 1, 0.0f, false, mask); swap_buf(g, 1);
-            norm_stage(g, tr, 1, 2, 3.0f / 4.0f, true, mask); swap_buf(g, 2);
-            norm_stage(g, tr, 1, 2, 1.0f / 3.0f, true, mask); swap_buf(g, 2);
-        }
-    }
-}
-
-// Create a leaf at key k filled with its tile value, creating the lower and
-// upper nodes it needs with the value of the tile they replace.
-Leaf* touch_leaf(Grid& g, uint64_t k) {
-    const float tv = g.tile_sign(k) ? -g.gamma : g.gamma;
-    const uint64_t lk = k >> 12, uk = k >> 27;
-    if (!g.upper.count(uk)) {
-        uint8_t s = 0;
-        auto r = g.root.find(uk);
-        if (r != g.root.end()) { s = r->second; g.root.erase(r); }
-        g.upper[uk] = std::vector<uint64_t>(512, s ? ~uint64_t(0) : 0);
-    }
-    if (!g.lower.count(lk)) {
-        const uint32_t n = uint32_t(lk & 32767);
-        const int s = int((g.upper[uk][n >> 6] >> (n & 63)) & 1);
-        g.lower[lk] = std::vector<uint64_t>(64, s ? ~uint64_t(0) : 0);
-    }
-    Leaf* L = new Leaf;
-    L->key = k;
-    std::memset(L->mask, 0, sizeof(L->mask));
-    for (int b = 0; b < 3; ++b) std::fill(L->buf[b], L->buf[b] + 512, tv);
-    g.leaves.push_back(L);
-    g.index[k] = L;
-    return L;
-}
-
-// dilateActiveValues(NN_FACE, IGNORE_TILES), one iteration (tools/Morphology.h:612-812)
-void dilate1(Grid& g) {
-    const size_t n0 = g.leaves.size();
-    // new leaves: missing face neighbours that receive active voxels
-    std::vector<uint64_t> cand;
-    for (size_t i = 0; i < n0; ++i) {
-        const Leaf* L = g.leaves[i];
-        const uint64_t* m = L->mask;
-        uint64_t any[6];
-        any[0] = m[0]; any[1] = m[7];
-        uint64_t ym = 0, yp = 0, zm = 0, zp = 0;
-        for (int w = 0; w < 8; ++w) {
-            ym |= m[w] & 0xFFull; yp |= m[w] & 0xFF00000000000000ull;
-            zm |= m[w] & 0x0101010101010101ull; zp |= m[w] & 0x8080808080808080ull;
-        }
-        any[2] = ym; any[3] = yp; any[4] = zm; any[5] = zp;
-        for (int f = 0; f < 6; ++f)
-            if (any[f] && !g.probe(nkey(L->key, f))) cand.push_back(nkey(L->key, f));
-    }
-    std::sort(cand.begin(), cand.end());
-    cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-    for (uint64_t k : cand) touch_leaf(g, k);
-    g.rebuild_order();
-    // new masks from the old ones
-    std::unordered_map<const Leaf*, std::array<uint64_t, 8>> old;
-    old.reserve(g.leaves.size());
-    for (const Leaf* L : g.leaves) {
-        std::array<uint64_t, 8> a;
-        std::memcpy(a.data(), L->mask, 64);
-        old[L] = a;
-    }
-    g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-        for (size_t i = a; i < b; ++i) {
-            Leaf* L = g.leaves[i];
-            const uint64_t* own = old.at(L).data();
-            const uint64_t* nb[6];
-            for (int f = 0; f < 6; ++f) {
-                const Leaf* N = g.probe(nkey(L->key, f));
-                nb[f] = N ? old.at(N).data() : nullptr;
-            }
-            for (int x = 0; x < 8; ++x) {
-                const uint64_t w = own[x];
-                uint64_t d = w | ((w << 1) & 0xFEFEFEFEFEFEFEFEull) | ((w >> 1) & 0x7F7F7F7F7F7F7F7Full) | (w << 8) | (w >> 8);
-                d |= x > 0 ? own[x - 1] : (nb[0] ? nb[0][7] : 0);
-                d |= x < 7 ? own[x + 1] : (nb[1] ? nb[1][0] : 0);
-                if (nb[2]) d |= nb[2][x] >> 56;
-                if (nb[3]) d |= nb[3][x] << 56;
-                if (nb[4]) d |= (nb[4][x] >> 7) & 0x0101010101010101ull;
-                if (nb[5]) d |= (nb[5][x] << 7) & 0x8080808080808080ull;
-                L->mask[x] = d;
-            }
-        }
-    });
-}
-
-// erodeActiveValues(NN_FACE, IGNORE_TILES), `iter` iterations
-void erode(Grid& g, int iter) {
-    for (int it = 0; it < iter; ++it) {
-        std::unordered_map<const Leaf*, std::array<uint64_t, 8>> old;
-        for (const Leaf* L : g.leaves) {
-            std::array<uint64_t, 8> a;
-            std::memcpy(a.data(), L->mask, 64);
-            old[L] = a;
-        }
-        for (Leaf* L : g.leaves) {
-            const uint64_t* own = old.at(L).data();
-            uint64_t W[6][8];
-            for (int f = 0; f < 6; ++f) {
-                const Leaf* N = g.probe(nkey(L->key, f));
-                for (int x = 0; x < 8; ++x) W[f][x] = N ? old.at(N)[x] : 0;
-            }
-            for (int x = 0; x < 8; ++x) {
-                const uint64_t w = own[x];
-                uint64_t e = w;
-                e &= ((w << 1) & 0xFEFEFEFEFEFEFEFEull) | ((W[4][x] >> 7) & 0x0101010101010101ull);
-                e &= ((w >> 1) & 0x7F7F7F7F7F7F7F7Full) | ((W[5][x] << 7) & 0x8080808080808080ull);
-                e &= (w << 8) | (W[2][x] >> 56);
-                e &= (w >> 8) | (W[3][x] << 56);
-                e &= x > 0 ? own[x - 1] : W[0][7];
-                e &= x < 7 ? own[x + 1] : W[1][0];
-                L->mask[x] = e;
-            }
-        }
-    }
-}
-
-// Trim (tools/LevelSetTracker.h:473-506)
-void trim(Grid& g, int mode) {
-    if (mode == GBLS_TRIM_NONE) return;
-    const float gamma = g.gamma;
-    g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-        for (size_t i = a; i < b; ++i) {
-            Leaf* L = g.leaves[i];
-            for (int n = 0; n < 512; ++n) {
-                if (!on(L->mask, n)) continue;
-                const float v = L->buf[0][n];
-                if ((mode & 1) && v <= -gamma) { set_off(L->mask, n); L->buf[0][n] = -gamma; }
-                else if ((mode & 2) && v >= gamma) { set_off(L->mask, n); L->buf[0][n] = gamma; }
-            }
-        }
-    });
-}
-
-// pruneLevelSet (tools/Prune.h:266-330, 391-397): bottom-up
-void prune_level_set(Grid& g) {
-    std::vector<Leaf*> keep;
-    for (Leaf* L : g.leaves) {
-        bool any = false;
-        for (int w = 0; w < 8; ++w) any |= L->mask[w] != 0;
-        if (any) { keep.push_back(L); continue; }
-        const uint64_t k = L->key;
-        auto& ls = g.lower.at(k >> 12);
-        const uint32_t n = uint32_t(k & 4095);
-        if (L->buf[0][0] < 0) ls[n >> 6] |= uint64_t(1) << (n & 63);
-        else ls[n >> 6] &= ~(uint64_t(1) << (n & 63));
-        g.index.erase(k);
-        delete L;
-    }
-    g.leaves.swap(keep);
-    std::unordered_set<uint64_t> lowerWithLeaves;
-    for (Leaf* L : g.leaves) lowerWithLeaves.insert(L->key >> 12);
-    for (auto it = g.lower.begin(); it != g.lower.end();) {
-        if (lowerWithLeaves.count(it->first)) { ++it; continue; }
-        const uint64_t lk = it->first;
-        auto& us = g.upper.at(lk >> 15);
-        const uint32_t n = uint32_t(lk & 32767);
-        if (it->second[0] & 1) us[n >> 6] |= uint64_t(1) << (n & 63);
-        else us[n >> 6] &= ~(uint64_t(1) << (n & 63));
-        it = g.lower.erase(it);
-    }
-    std::unordered_set<uint64_t> upperWithLower;
-    for (auto& kv : g.lower) upperWithLower.insert(kv.first >> 15);
-    for (auto it = g.upper.begin(); it != g.upper.end();) {
-        if (upperWithLower.count(it->first)) { ++it; continue; }
-        g.root[it->first] = uint8_t(it->second[0] & 1);
-        it = g.upper.erase(it);
-    }
-    for (auto it = g.root.begin(); it != g.root.end();) {  // eraseBackgroundTiles
-        if (it->second == 0) it = g.root.erase(it);
-        else ++it;
-    }
-}
-
-// changeLevelSetBackground: every inactive value becomes +-background by sign
-void change_background(Grid& g, float bg) {
-    g.gamma = bg;
-    g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-        for (size_t i = a; i < b; ++i) {
-            Leaf* L = g.leaves[i];
-            for (int n = 0; n < 512; ++n)
-                if (!on(L->mask, n)) L->buf[0][n] = L->buf[0][n] < 0 ? -bg : bg;
-        }
-    });
-}
-
-void prune(Grid& g, const Tracker& tr) {
-    trim(g, tr.trim);
-    prune_level_set(g);
-}
-
-void track(Grid& g, const Tracker& tr) {
-    dilate1(g);
-    normalize(g, tr, nullptr);
-    prune(g, tr);
-}
-
-void tracker_dilate(Grid& g, const Tracker& tr, int iterations) {
-    const float dx = float(g.voxel_size);
-    for (int i = 0; i < iterations; ++i) {
-        std::unordered_map<uint64_t, std::array<uint64_t, 8>> before;
-        for (const Leaf* L : g.leaves) { std::array<uint64_t, 8> a; std::memcpy(a.data(), L->mask, 64); before[L->key] = a; }
-        dilate1(g);
-        change_background(g, dx + g.gamma);
-        if (tr.norm_count > 0) {
-            std::unordered_map<uint64_t, std::vector<uint64_t>> mask;
-            for (const Leaf* L : g.leaves) {
-                std::vector<uint64_t> m(8);
-                auto it = before.find(L->key);
-                bool any = false;
-                for (int w = 0; w < 8; ++w) {
-                    m[w] = L->mask[w] & ~(it == before.end() ? 0 : it->second[w]);
-                    any |= m[w] != 0;
-                }
-                if (any) mask[L->key] = m;
-            }
-            normalize(g, tr, &mask);
-        }
-    }
-}
-
-void tracker_erode(Grid& g, int iterations) {
-    erode(g, iterations);
-    prune_level_set(g);
-    change_background(g, g.gamma - float(iterations) * float(g.voxel_size));
-}
-
-// ---- LevelSetAdvection (tools/LevelSetAdvect.h:338-572) ---------------------
-struct Advector {
-    Grid& g;
-    const Field& field;
-    Tracker tr;
-    int temporal = GBLS_TVD_RK3;
-    float cfl = 0.0f;
-    std::vector<size_t> offsets;
-    std::vector<float> vel;  // [active][3]
-
-    float sample_field(float t0, float t1) {
-        if (g.leaves.empty()) return 0.0f;
-        offsets.resize(g.leaves.size() + 1);
-        size_t acc = 0;
-        for (size_t i = 0; i < g.leaves.size(); ++i) {
-            offsets[i] = acc;
-            for (int w = 0; w < 8; ++w) acc += size_t(__builtin_popcountll(g.leaves[i]->mask[w]));
-        }
-        offsets[g.leaves.size()] = acc;
-        vel.assign(acc * 3, 0.0f);
-        const bool fwd = t0 < t1;
-        g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-            for (size_t i = a; i < b; ++i) {
-                const Leaf* L = g.leaves[i];
-                int32_t ox, oy, oz;
-                origin_of(L->key, ox, oy, oz);
-                float* v = vel.data() + 3 * offsets[i];
-                for (int n = 0; n < 512; ++n) {
-                    if (!on(L->mask, n)) continue;
-                    float o[3];
-                    field.eval(ox + (n >> 6), oy + ((n >> 3) & 7), oz + (n & 7), t0, o);
-                    v[0] = fwd ? o[0] : -o[0]; v[1] = fwd ? o[1] : -o[1]; v[2] = fwd ? o[2] : -o[2];
-                    v += 3;
-                }
-            }
-        });
-        float maxAbsV = 0;
-        for (size_t i = 0; i < acc; ++i) {
-            const float* v = vel.data() + 3 * i;
-            maxAbsV = fmaxr(maxAbsV, v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-        }
-        if (!(maxAbsV > 1e-5f) && !(maxAbsV < -1e-5f)) return 0.0f;
-        const float CFLref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) / std::sqrt(3.0f);
-        const float CFL = cfl > 0.0f ? cfl : CFLref;
-        const float dt = std::fabs(t1 - t0), dx = float(g.voxel_size);
-        return fminr(dt, CFL * dx / std::sqrt(maxAbsV));
-    }
-
-    // euler<N,D>(dt, phiBuffer, resultBuffer)
-    void euler(float dt, int phiBuf, int resBuf, float alpha, bool hasPhi) {
-        const double invdx = 1.0 / g.voxel_size;
-        const float beta = 1.0f - alpha;
-        g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
-            Tile t;
-            for (size_t i = a; i < b; ++i) {
-                Leaf* L = g.leaves[i];
-                gather(g, L, 0, t);
-                const float* v = vel.data() + 3 * offsets[i];
-                for (int n = 0; n < 512; ++n) {
-                    if (!on(L->mask, n)) continue;
-                    const int x = n >> 6, y = (n >> 3) & 7, z = n & 7;
-                    auto S = [&](int dx_, int dy_, int dz_) { return t.at(x + dx_, y + dy_, z + dz_); };
-                    const float gx = v[0] < 0 ? hj_fd(S(3, 0, 0), S(2, 0, 0), S(1, 0, 0), S(0, 0, 0), S(-1, 0, 0), S(-2, 0, 0))
-                                              : hj_bd(S(-3, 0, 0), S(-2, 0, 0), S(-1, 0, 0), S(0, 0, 0), S(1, 0, 0), S(2, 0, 0));
-                    const float gy = v[1] < 0 ? hj_fd(S(0, 3, 0), S(0, 2, 0), S(0, 1, 0), S(0, 0, 0), S(0, -1, 0), S(0, -2, 0))
-                                              : hj_bd(S(0, -3, 0), S(0, -2, 0), S(0, -1, 0), S(0, 0, 0), S(0, 1, 0), S(0, 2, 0));
-                    const float gz = v[2] < 0 ? hj_fd(S(0, 0, 3), S(0, 0, 2), S(0, 0, 1), S(0, 0, 0), S(0, 0, -1), S(0, 0, -2))
-                                              : hj_bd(S(0, 0, -3), S(0, 0, -2), S(0, 0, -1), S(0, 0, 0), S(0, 0, 1), S(0, 0, 2));
-                    // Vec3d -> applyIJT (x 1/dx in double) -> Vec3f
-                    const float g0 = float(double(gx) * invdx), g1 = float(double(gy) * invdx), g2 = float(double(gz) * invdx);
-                    const float av = S(0, 0, 0) - dt * (v[0] * g0 + v[1] * g1 + v[2] * g2);
-                    L->buf[resBuf][n] = hasPhi ? alpha * L->buf[phiBuf][n] + beta * av : av;
-                    v += 3;
-                }
-            }
-        });
-    }
-
-    uint64_t advect(float t0, float t1, const std::function<bool()>& interrupted, uint64_t* updates) {
-        uint64_t count = 0;
-        if (t0 - t1 == 0.0f) return 0;
-        const bool fwd = t0 < t1;
-        while (fwd ? t0 < t1 : t0 > t1) {
-            if (interrupted && interrupted()) break;
-            copy_aux(g, temporal == GBLS_TVD_RK3 ? 2 : 1);
-            const float dt = sample_field(t0, t1);
-            if (dt == 0.0f) break;
-            if (updates) *updates += offsets.back();
-            if (temporal == GBLS_TVD_RK1) {
-                euler(dt, 0, 1, 0.0f, false); swap_buf(g, 1);
-            } else if (temporal == GBLS_TVD_RK2) {
-                euler(dt, 0, 1, 0.0f, false); swap_buf(g, 1);
-                euler(dt, 1, 1, 1.0f / 2.0f, true); swap_buf(g, 1);
-            } else {
-                euler(dt, 0, 1, 0.0f, false); swap_buf(g, 1);
-                euler(dt, 1, 2, 3.0f / 4.0f, true); swap_buf(g, 2);
-                euler(dt, 1, 2, 1.0f / 3.0f, true); swap_buf(g, 2);
-            }
-            t0 += fwd ? dt : -dt;
-            ++count;
-            track(g, tr);
-        }
-        return count;
-    }
-};
-
-// ---- canonical import / export ----------------------------------------------
-Grid* import_desc(const gbls_grid_desc* d) {
-    Grid* g = new Grid;
-    g->gamma = d->background;
-    g->voxel_size = d->voxel_size;
-    g->map_type = d->map_type;
-    for (int i = 0; i < 3; ++i) g->translation[i] = d->translation[i];
-    for (int64_t i = 0; i < d->leaf_count; ++i) {
-        const int32_t* o = d->leaf_origins + 3 * i;
-        Leaf* L = new Leaf;
-        L->key = key_of(o[0], o[1], o[2]);
-        std::memcpy(L->mask, d->leaf_masks + 8 * i, 64);
-        std::memcpy(L->buf[0], d->leaf_values + 512 * i, 2048);
-        g->leaves.push_back(L);
-        g->index[L->key] = L;
-    }
-    g->rebuild_order();
-    for (int64_t i = 0; i < d->lower_count; ++i) {
-        const int32_t* o = d->lower_origins + 3 * i;
-        const uint64_t lk = key_of(o[0], o[1], o[2]) >> 12;
-        std::vector<uint64_t> s(64, 0);
-        for (int n = 0; n < 4096; ++n)
-            if (d->lower_tiles[i * 4096 + n] < 0) s[n >> 6] |= uint64_t(1) << (n & 63);
-        g->lower[lk] = s;
-    }
-    for (int64_t i = 0; i < d->upper_count; ++i) {
-        const int32_t* o = d->upper_origins + 3 * i;
-        const uint64_t uk = key_of(o[0], o[1], o[2]) >> 27;
-        std::vector<uint64_t> s(512, 0);
-        for (int n = 0; n < 32768; ++n)
-            if (d->upper_tiles[i * 32768 + n] < 0) s[n >> 6] |= uint64_t(1) << (n & 63);
-        g->upper[uk] = s;
-    }
-    for (int64_t i = 0; i < d->root_tile_count; ++i) {
-        const int32_t* o = d->root_tile_origins + 3 * i;
-        g->root[key_of(o[0], o[1], o[2]) >> 27] = d->root_tile_values[i] < 0 ? 1 : 0;
-    }
-    return g;
-}
-
-void export_desc(const Grid& g, gbls_grid_desc* d) {
-    d->voxel_size = g.voxel_size;
-    for (int i = 0; i < 3; ++i) d->translation[i] = g.translation[i];
-    d->map_type = g.map_type;
-    d->background = g.gamma;
-    std::unordered_set<uint64_t> leafKeys, lowerKeys;
-    for (size_t i = 0; i < g.leaves.size(); ++i) {
-        const Leaf* L = g.leaves[i];
-        int32_t x, y, z;
-        origin_of(L->key, x, y, z);
-        d->leaf_origins[3 * i] = x; d->leaf_origins[3 * i + 1] = y; d->leaf_origins[3 * i + 2] = z;
-        std::memcpy(d->leaf_masks + 8 * i, L->mask, 64);
-        std::memcpy(d->leaf_values + 512 * i, L->buf[0], 2048);
-        leafKeys.insert(L->key);
-    }
-    size_t i = 0;
-    for (auto& kv : g.lower) {
-        int32_t x, y, z;
-        origin_of(kv.first << 12, x, y, z);
-        d->lower_origins[3 * i] = x; d->lower_origins[3 * i + 1] = y; d->lower_origins[3 * i + 2] = z;
-        for (int n = 0; n < 4096; ++n) {
-            const uint64_t k = (kv.first << 12) | uint64_t(n);
-            d->lower_tiles[i * 4096 + n] = leafKeys.count(k) ? 0.0f : (((kv.second[n >> 6] >> (n & 63)) & 1) ? -g.gamma : g.gamma);
-        }
-        lowerKeys.insert(kv.first);
-        ++i;
-    }
-    i = 0;
-    for (auto& kv : g.upper) {
-        int32_t x, y, z;
-        origin_of(kv.first << 27, x, y, z);
-        d->upper_origins[3 * i] = x; d->upper_origins[3 * i + 1] = y; d->upper_origins[3 * i + 2] = z;
-        for (int n = 0; n < 32768; ++n) {
-            const uint64_t k = (kv.first << 15) | uint64_t(n);
-            d->upper_tiles[i * 32768 + n] = lowerKeys.count(k) ? 0.0f : (((kv.second[n >> 6] >> (n & 63)) & 1) ? -g.gamma : g.gamma);
-        }
-        ++i;
-    }
-    i = 0;
-    for (auto& kv : g.root) {
-        int32_t x, y, z;
-        origin_of(kv.first << 27, x, y, z);
-        d->root_tile_origins[3 * i] = x; d->root_tile_origins[3 * i + 1] = y; d->root_tile_origins[3 * i + 2] = z;
-        d->root_tile_values[i] = kv.second ? -g.gamma : g.gamma;
-        ++i;
-    }
-}
+int nthreads_of(int threads) { return threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency())); }
 
 }  // namespace
 
@@ -711,80 +111,126 @@ extern "C" {
 
 const char* oport_last_error() { return g_err.c_str(); }
 
-void* oport_create(const gbls_grid_desc* d, int threads) {
-    Grid* g = import_desc(d);
-    g->pool.nthreads = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));
-    return g;
+// precision 32: bit-identical to the reference; 64: the same scheme in FP64
+void* oport_create_prec(const gbls_grid_desc* d, int threads, int precision) {
+    Handle* h = new Handle;
+    h->prec = precision == 64 ? 64 : 32;
+    if (h->prec == 64) {
+        h->g64 = p64::import_desc(d);
+        h->g64->pool.nthreads = nthreads_of(threads);
+    } else {
+        h->g32 = p32::import_desc(d);
+        h->g32->pool.nthreads = nthreads_of(threads);
+    }
+    return h;
 }
-void oport_free(void* g) { delete static_cast<Grid*>(g); }
-void oport_set_threads(void* g, int threads) {
-    static_cast<Grid*>(g)->pool.nthreads = threads > 0 ? threads : int(std::max(1u, std::thread::hardware_concurrency()));
+void* oport_create(const gbls_grid_desc* d, int threads) { return oport_create_prec(d, threads, 32); }
+void oport_free(void* h) { delete static_cast<Handle*>(h); }
+void oport_set_threads(void* h, int threads) {
+    dispatch(h, [&](p32::Grid& g) { g.pool.nthreads = nthreads_of(threads); return 0; },
+             [&](p64::Grid& g) { g.pool.nthreads = nthreads_of(threads); return 0; });
 }
 
-int oport_counts(void* gp, gbls_grid_counts* c) {
-    const Grid& g = *static_cast<Grid*>(gp);
-    c->leaf_count = int64_t(g.leaves.size());
-    c->lower_count = int64_t(g.lower.size());
-    c->upper_count = int64_t(g.upper.size());
-    c->root_tile_count = int64_t(g.root.size());
-    c->active_voxel_count = int64_t(g.active_count());
-    return 0;
+int oport_counts(void* h, gbls_grid_counts* c) {
+    auto f = [&](auto& g) {
+        c->leaf_count = int64_t(g.leaves.size());
+        c->lower_count = int64_t(g.lower.size());
+        c->upper_count = int64_t(g.upper.size());
+        c->root_tile_count = int64_t(g.root.size());
+        c->active_voxel_count = int64_t(g.active_count());
+        return 0;
+    };
+    return dispatch(h, f, f);
 }
 
-int oport_export(void* g, gbls_grid_desc* d) {
-    export_desc(*static_cast<Grid*>(g), d);
-    return 0;
+int oport_export(void* h, gbls_grid_desc* d) {
+    return dispatch(h, [&](p32::Grid& g) { p32::export_desc(g, d); return 0; },
+                    [&](p64::Grid& g) { p64::export_desc(g, d); return 0; });
+}
+
+// Active values in canonical order, as double.
+int oport_active_values(void* h, double* out) {
+    auto f = [&](auto& g) {
+        size_t k = 0;
+        for (const auto* L : g.leaves)
+            for (int n = 0; n < 512; ++n)
+                if ((L->mask[n >> 6] >> (n & 63)) & 1) out[k++] = double(L->buf[0][n]);
+        return 0;
+    };
+    return dispatch(h, f, f);
+}
+
+// Replace the active values (canonical order) from doubles.
+int oport_set_active_values(void* h, const double* in) {
+    auto f = [&](auto& g) {
+        size_t k = 0;
+        for (auto* L : g.leaves)
+            for (int n = 0; n < 512; ++n)
+                if ((L->mask[n >> 6] >> (n & 63)) & 1) L->buf[0][n] = decltype(L->buf[0][0])(in[k++]);
+        return 0;
+    };
+    return dispatch(h, f, f);
 }
 
 // op: 0 track, 1 normalize, 2 prune, 3 dilate(arg), 4 erode(arg), 5 resize(arg)
-int oport_tracker_op(void* gp, int op, int arg, int spatial, int temporal, int norm_count, int trim_mode, int* result) {
-    Grid& g = *static_cast<Grid*>(gp);
+int oport_tracker_op(void* h, int op, int arg, int spatial, int temporal, int norm_count, int trim_mode, int* result) {
     if (spatial != GBLS_HJWENO5_BIAS) { g_err = "the oracle port implements HJWENO5_BIAS"; return GBLS_ERR_UNSUPPORTED; }
-    Tracker tr;
-    tr.temporal = temporal;
-    tr.norm_count = norm_count;
-    tr.trim = trim_mode;
-    int r = 0;
-    switch (op) {
-    case 0: track(g, tr); break;
-    case 1: normalize(g, tr, nullptr); break;
-    case 2: prune(g, tr); break;
-    case 3: tracker_dilate(g, tr, arg); break;
-    case 4: tracker_erode(g, arg); break;
-    case 5: {
-        const int wOld = int(std::floor(g.gamma / float(g.voxel_size)));
-        if (wOld < arg) tracker_dilate(g, tr, arg - wOld);
-        else if (wOld > arg) tracker_erode(g, wOld - arg);
-        r = wOld != arg;
-        break;
-    }
-    default: g_err = "bad op"; return GBLS_ERR_INVALID_ARGUMENT;
-    }
-    if (result) *result = r;
-    return 0;
+    auto f = [&](auto& g, auto tr) {
+        tr.temporal = temporal;
+        tr.norm_count = norm_count;
+        tr.trim = trim_mode;
+        int r = 0;
+        using G = std::remove_reference_t<decltype(g)>;
+        (void)sizeof(G);
+        switch (op) {
+        case 0: track(g, tr); break;
+        case 1: normalize(g, tr, nullptr); break;
+        case 2: prune(g, tr); break;
+        case 3: tracker_dilate(g, tr, arg); break;
+        case 4: tracker_erode(g, arg); break;
+        case 5: {
+            const int wOld = int(std::floor(float(g.gamma) / float(g.voxel_size)));
+            if (wOld < arg) tracker_dilate(g, tr, arg - wOld);
+            else if (wOld > arg) tracker_erode(g, wOld - arg);
+            r = wOld != arg;
+            break;
+        }
+        default: g_err = "bad op"; return int(GBLS_ERR_INVALID_ARGUMENT);
+        }
+        if (result) *result = r;
+        return 0;
+    };
+    return dispatch(h, [&](p32::Grid& g) { return f(g, p32::Tracker{}); },
+                    [&](p64::Grid& g) { return f(g, p64::Tracker{}); });
 }
 
-int oport_advect(void* gp, const gbls_field_desc* fd, int spatial, int temporal, int tspatial, int ttemporal,
+int oport_advect(void* h, const gbls_field_desc* fd, int spatial, int temporal, int tspatial, int ttemporal,
                  int norm_count, float t0, float t1, float cfl, uint64_t* count, uint64_t* updates) {
-    Grid& g = *static_cast<Grid*>(gp);
     if (spatial != GBLS_HJWENO5_BIAS || tspatial != GBLS_HJWENO5_BIAS) {
         g_err = "the oracle port implements HJWENO5_BIAS";
         return GBLS_ERR_UNSUPPORTED;
     }
-    Field f;
-    f.d = *fd;
-    if (fd->kind == GBLS_FIELD_DENSE)
-        f.dense.assign(fd->dense_values, fd->dense_values + size_t(3) * fd->dense_dims[0] * fd->dense_dims[1] * fd->dense_dims[2]);
-    Advector a{g, f};
-    a.tr.temporal = ttemporal;
-    a.tr.norm_count = norm_count;
-    a.temporal = temporal;
-    a.cfl = cfl;
-    uint64_t u = 0;
-    const uint64_t n = a.advect(t0, t1, nullptr, &u);
-    if (count) *count = n;
-    if (updates) *updates = u;
-    return 0;
+    auto f = [&](auto& g, auto field) {
+        field.d = *fd;
+        if (fd->kind == GBLS_FIELD_DENSE)
+            field.dense.assign(fd->dense_values,
+                               fd->dense_values + size_t(3) * fd->dense_dims[0] * fd->dense_dims[1] * fd->dense_dims[2]);
+        using G = std::remove_reference_t<decltype(g)>;
+        using A = decltype(adv_of(g));
+        A a{g, field};
+        a.tr.temporal = ttemporal;
+        a.tr.norm_count = norm_count;
+        a.temporal = temporal;
+        a.cfl = cfl;
+        uint64_t u = 0;
+        const uint64_t n = a.advect(t0, t1, nullptr, &u);
+        if (count) *count = n;
+        if (updates) *updates = u;
+        (void)sizeof(G);
+        return 0;
+    };
+    return dispatch(h, [&](p32::Grid& g) { return f(g, p32::Field{}); },
+                    [&](p64::Grid& g) { return f(g, p64::Field{}); });
 }
 
 }  // extern "C"

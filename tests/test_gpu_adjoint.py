@@ -1,12 +1,16 @@
-"""Adjoint of advection + tracking against central finite differences.
+"""Adjoint of advection + tracking against an FP64 reference gradient.
 
-Loss L = sum over the final band of (phi_T - phi_target)^2.  The adjoint holds
-the recorded topology, upwind directions, Godunov branches, trimming and CFL
-time steps fixed, so each probe direction perturbs a few seeded voxels of
-phi_0 (or a few cells of the velocity grid): a dense perturbation moves some
-voxel across the trim threshold and changes the topology, which the
-finite difference would see as a jump.  Probes whose perturbed runs change
-the topology are rejected.
+Loss L = sum over the final band of (phi_T - phi_target)^2.  The reference
+gradient comes from central differences of the FP64 run of the same scheme
+(the oracle's restatement compiled for double: same constants, same
+operations) with h = 1e-6 along seeded dense probe directions; in FP64 the
+difference is neither limited by rounding nor, at that step, by the strong
+nonlinearity of the WENO5 weights.  The adjoint under test is the GPU
+reverse sweep of the FP32 forward pass.  It holds the recorded topology,
+upwind directions, Godunov branches, trimming and CFL time steps fixed;
+probes whose perturbed FP64 runs change the topology are rejected, and
+velocity probes use intervals below the CFL limit so that dt does not depend
+on the velocity.
 """
 import time
 
@@ -16,84 +20,90 @@ import pytest
 from cases import smoothed_noise
 
 
-def _sdf_sphere(grid, radius, center):
-    c = grid.active_coords().astype(np.float64)
-    return np.sqrt(((c - np.asarray(center)) ** 2).sum(1)) - radius
+def _sdf_sphere(coords, radius, center):
+    return np.sqrt(((coords.astype(np.float64) - np.asarray(center)) ** 2).sum(1)) - radius
 
 
-def _loss(phi, target):
-    d = phi.astype(np.float64) - target
-    return float((d * d).sum()), 2.0 * d
+def _fp64_loss(template, phi0, field, times, target_fn):
+    from oracle import port
+    g = port.PortGrid(template, precision=64)
+    g.set_active_values(phi0)
+    counts = [g.advect(field, times[k], times[k + 1], temporal=2, tracker_temporal=0, norm_count=1)
+              for k in range(len(times) - 1)]
+    host = g.to_host()
+    d = g.active_values() - target_fn(host.active_coords())
+    return float((d * d).sum()), host, counts
 
 
 def _same_topology(a, b):
     return np.array_equal(a.leaf_origins, b.leaf_origins) and np.array_equal(a.leaf_masks, b.leaf_masks)
 
 
-def _probe(tape, phi0, vel, times, gT, target_fn, g_phi, g_vel, rng, kind, h, nsel=8):
-    dphi = np.zeros_like(phi0)
-    dv = np.zeros_like(vel)
-    if kind == "phi":
-        idx = rng.choice(phi0.size, nsel, replace=False)
-        dphi[idx] = rng.standard_normal(nsel).astype(np.float32)
-    else:
-        flat = dv.reshape(-1)
-        idx = rng.choice(flat.size, nsel, replace=False)
-        flat[idx] = rng.standard_normal(nsel).astype(np.float32)
-    vals = []
-    for sgn in (1.0, -1.0):
-        tape.set_velocity(vel + sgn * h * dv)
-        p, g = tape.forward(phi0 + sgn * h * dphi, times, record=False)
-        if not _same_topology(g, gT):
-            tape.set_velocity(vel)
-            return None
-        vals.append(_loss(p, target_fn(g))[0])
-    tape.set_velocity(vel)
-    fd = (vals[0] - vals[1]) / (2 * h)
-    ad = float(np.dot(g_phi.astype(np.float64), dphi) + np.dot(g_vel.reshape(-1).astype(np.float64), dv.reshape(-1)))
-    return fd, ad
-
-
-@pytest.mark.gpu
-def test_adjoint_matches_finite_differences():
-    from openvdb_gb300 import PARITY, fixtures
+def _check_case(template, vel, times, target_fn, nprobe, vel_probes, tol_median, tol_max, seed):
+    from openvdb_gb300 import PARITY, Field
     from openvdb_gb300.adjoint import AdvectionTape
+    port = pytest.importorskip("oracle.port")
+    assert port.available()
 
-    center, r0, rt = (16.0, 16.0, 16.0), 9.0, 10.0
-    template = fixtures.sphere(r0, center)
-    vel = smoothed_noise(32, 3.0, 0.8, seed=5)
-    times = [0.0, 0.3, 0.6, 0.9, 1.2]  # below the CFL limit: dt independent of v
     tape = AdvectionTape(template, vel, mode=PARITY)
     phi0 = template.active_values().copy()
     phiT, gT = tape.forward(phi0, times)
-    assert tape.substeps == [1, 1, 1, 1]
-    target = lambda g: _sdf_sphere(g, rt, center)
-    _, dL = _loss(phiT, target(gT))
-    g_phi, g_vel = tape.backward(dL.astype(np.float32))
+    d = phiT.astype(np.float64) - target_fn(gT.active_coords())
+    g_phi, g_vel = tape.backward((2.0 * d).astype(np.float32))
     assert np.isfinite(g_phi).all() and np.isfinite(g_vel).all()
-    rng = np.random.Generator(np.random.PCG64(1234))
-    checked = {"phi": 0, "vel": 0}
-    for trial in range(40):
-        kind = "phi" if trial % 2 == 0 else "vel"
-        r = _probe(tape, phi0, vel, times, gT, target, g_phi, g_vel, rng, kind, 1e-3)
-        if r is None:
+
+    base_field = Field.dense(vel)
+    _, host0, counts0 = _fp64_loss(template, phi0.astype(np.float64), base_field, times, target_fn)
+    assert _same_topology(host0, gT), "FP64 run and FP32 run differ in topology"
+    rng = np.random.Generator(np.random.PCG64(seed))
+    errs = []
+    for k in range(nprobe):
+        is_vel = vel_probes and k % 2 == 1
+        if is_vel:
+            h = 1e-4
+            dv = rng.standard_normal(vel.shape).astype(np.float32)
+            vp = (vel + h * dv).astype(np.float32)
+            vm = (vel - h * dv).astype(np.float32)
+            Lp, hp, cp = _fp64_loss(template, phi0.astype(np.float64), Field.dense(vp), times, target_fn)
+            Lm, hm, cm = _fp64_loss(template, phi0.astype(np.float64), Field.dense(vm), times, target_fn)
+            ad = float(np.dot(g_vel.reshape(-1).astype(np.float64),
+                              (vp.astype(np.float64) - vm.astype(np.float64)).reshape(-1))) / (2 * h)
+        else:
+            h = 1e-6
+            dphi = rng.standard_normal(phi0.size)
+            Lp, hp, cp = _fp64_loss(template, phi0 + h * dphi, base_field, times, target_fn)
+            Lm, hm, cm = _fp64_loss(template, phi0 - h * dphi, base_field, times, target_fn)
+            ad = float(np.dot(g_phi.astype(np.float64), dphi))
+        if not (_same_topology(hp, host0) and _same_topology(hm, host0) and cp == counts0 and cm == counts0):
             continue
-        fd, ad = r
-        scale = max(abs(fd), abs(ad), 1e-3)
-        tol = 1e-2 if kind == "phi" else 5e-2  # velocity probes cross upwind switches at v = 0
-        print("%s probe %d: fd %+.6e adjoint %+.6e rel %.2e" % (kind, trial, fd, ad, abs(fd - ad) / scale))
-        assert abs(fd - ad) <= tol * scale + 1e-3, (kind, trial, fd, ad)
-        checked[kind] += 1
-        if min(checked.values()) >= 8:
-            break
-    assert min(checked.values()) >= 6, checked
+        fd = (Lp - Lm) / (2 * h)
+        rel = abs(fd - ad) / max(abs(fd), 1e-12)
+        errs.append(rel)
+        print("%s probe %d: fp64 fd %+.9e adjoint %+.9e rel %.2e" % ("vel" if is_vel else "phi", k, fd, ad, rel))
+    assert len(errs) >= nprobe * 3 // 4, len(errs)
+    errs = np.array(errs)
+    print("relative error: median %.2e max %.2e over %d probes" % (np.median(errs), errs.max(), errs.size))
+    assert np.median(errs) < tol_median and errs.max() < tol_max
+    return tape
 
 
 @pytest.mark.gpu
-def test_adjoint_inverse_problem_scale_and_cost():
-    """The 128^3 adjoint configuration: phi_0 a radius-40 sphere, the target
-    a seeded 5%-perturbed radius-44 sphere, a seeded smoothed-noise velocity
-    grid (sigma 4 voxels, amplitude 1), 20 unit steps; probes of dL/dphi_0 and
+def test_adjoint_matches_fp64_reference_gradient():
+    from openvdb_gb300 import fixtures
+    center, r0, rt = (16.0, 16.0, 16.0), 9.0, 10.0
+    template = fixtures.sphere(r0, center)
+    vel = smoothed_noise(32, 3.0, 0.8, seed=5)
+    times = [0.0, 0.3, 0.6, 0.9, 1.2]  # below the CFL limit: dt = 0.3 independent of v
+    _check_case(template, vel, times, lambda c: _sdf_sphere(c, rt, center), nprobe=64, vel_probes=True,
+                tol_median=1e-3, tol_max=1e-2, seed=1234)
+
+
+@pytest.mark.gpu
+def test_adjoint_inverse_problem_128():
+    """The 128^3 adjoint configuration: phi_0 a radius-40 sphere, the target a
+    seeded 5%-perturbed radius-44 sphere, a seeded smoothed-noise velocity
+    grid (sigma 4 voxels, amplitude 1 voxel per time unit), 20 unit steps of
+    RK3-HJWENO5; dL/dphi_0 against the FP64 reference on seeded probes, and
     the cost of forward + adjoint against the plain forward pass."""
     import torch
     from openvdb_gb300 import FAST, fixtures
@@ -106,8 +116,8 @@ def test_adjoint_inverse_problem_scale_and_cost():
     amps = rng.uniform(-1.0, 1.0, 4)
     amps /= np.abs(amps).sum()
 
-    def target(g):
-        c = g.active_coords().astype(np.float64) - center
+    def target(coords):
+        c = coords.astype(np.float64) - center
         r = np.linalg.norm(c, axis=1)
         n = c / np.maximum(r, 1e-9)[:, None]
         return r - 44.0 * (1.0 + 0.05 * (n @ axes.T) @ amps)
@@ -117,7 +127,7 @@ def test_adjoint_inverse_problem_scale_and_cost():
     times = [float(t) for t in range(21)]
     tape = AdvectionTape(template, vel, mode=FAST)
     phi0 = template.active_values().copy()
-    # plain forward, then forward with the tape, then the adjoint
+    tape.forward(phi0, times, record=False)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     tape.forward(phi0, times, record=False)
@@ -125,26 +135,16 @@ def test_adjoint_inverse_problem_scale_and_cost():
     t0 = time.perf_counter()
     phiT, gT = tape.forward(phi0, times, record=True)
     t_rec = time.perf_counter() - t0
-    L, dL = _loss(phiT, target(gT))
+    d = phiT.astype(np.float64) - target(gT.active_coords())
     t0 = time.perf_counter()
-    g_phi, g_vel = tape.backward(dL.astype(np.float32))
+    g_phi, g_vel = tape.backward((2.0 * d).astype(np.float32))
     t_adj = time.perf_counter() - t0
     print("adjoint 128^3: %d substeps, %d -> %d active voxels, L = %.6g" % (sum(tape.substeps), phi0.size,
-                                                                            phiT.size, L))
+                                                                            phiT.size, float((d * d).sum())))
     print("wall time: forward %.3f s, recorded forward %.3f s, adjoint %.3f s, (fwd+adj)/fwd = %.2f"
           % (t_plain, t_rec, t_adj, (t_rec + t_adj) / t_plain))
-    assert np.isfinite(g_phi).all() and np.isfinite(g_vel).all()
-    assert np.abs(g_vel).max() > 0
-    checked = 0
-    for trial in range(12):
-        r = _probe(tape, phi0, vel, times, gT, target, g_phi, g_vel, rng, "phi", 1e-3)
-        if r is None:
-            continue
-        fd, ad = r
-        scale = max(abs(fd), abs(ad), 1e-3)
-        print("phi probe %d: fd %+.6e adjoint %+.6e rel %.2e" % (trial, fd, ad, abs(fd - ad) / scale))
-        assert abs(fd - ad) <= 2e-2 * scale + 1e-3, (trial, fd, ad)
-        checked += 1
-        if checked >= 4:
-            break
-    assert checked >= 3
+    assert (t_rec + t_adj) / t_plain < 3.5
+    assert np.isfinite(g_phi).all() and np.isfinite(g_vel).all() and np.abs(g_vel).max() > 0
+    # dL/dphi_0 against the FP64 reference (the PARITY forward matches the FP64 topology)
+    _check_case(template, vel, times, target, nprobe=8, vel_probes=False, tol_median=1e-2, tol_max=5e-2,
+                seed=77)
