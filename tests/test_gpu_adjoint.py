@@ -3,14 +3,17 @@
 Loss L = sum over the final band of (phi_T - phi_target)^2.  The reference
 gradient comes from central differences of the FP64 run of the same scheme
 (the oracle's restatement compiled for double: same constants, same
-operations) with h = 1e-6 along seeded dense probe directions; in FP64 the
+operations) with h = 1e-6 along seeded dense directions in phi_0 and h = 1e-4
+along seeded sparse directions in the velocity grid; in FP64 the
 difference is neither limited by rounding nor, at that step, by the strong
 nonlinearity of the WENO5 weights.  The adjoint under test is the GPU
 reverse sweep of the FP32 forward pass.  It holds the recorded topology,
 upwind directions, Godunov branches, trimming and CFL time steps fixed;
-probes whose perturbed FP64 runs change the topology are rejected, and
+probes whose perturbed FP64 runs change the topology after any interval are
+rejected, and
 velocity probes use intervals below the CFL limit so that dt does not depend
-on the velocity.
+on the velocity, and perturb only components away from zero, where the
+upwind side (fixed in the adjoint) cannot switch.
 """
 import time
 
@@ -28,11 +31,16 @@ def _fp64_loss(template, phi0, field, times, target_fn):
     from oracle import port
     g = port.PortGrid(template, precision=64)
     g.set_active_values(phi0)
-    counts = [g.advect(field, times[k], times[k + 1], temporal=2, tracker_temporal=0, norm_count=1)
-              for k in range(len(times) - 1)]
-    host = g.to_host()
+    # substep counts and the topology after every interval: a voxel trimmed
+    # in one interval and re-activated in a later one leaves the final
+    # topology unchanged but makes L jump
+    trail = []
+    for k in range(len(times) - 1):
+        n = g.advect(field, times[k], times[k + 1], temporal=2, tracker_temporal=0, norm_count=1)
+        host = g.to_host()
+        trail.append((n, host.leaf_origins.tobytes(), host.leaf_masks.tobytes()))
     d = g.active_values() - target_fn(host.active_coords())
-    return float((d * d).sum()), host, counts
+    return float((d * d).sum()), host, trail
 
 
 def _same_topology(a, b):
@@ -56,33 +64,53 @@ def _check_case(template, vel, times, target_fn, nprobe, vel_probes, tol_median,
     _, host0, counts0 = _fp64_loss(template, phi0.astype(np.float64), base_field, times, target_fn)
     assert _same_topology(host0, gT), "FP64 run and FP32 run differ in topology"
     rng = np.random.Generator(np.random.PCG64(seed))
-    errs = []
+    c = template.active_coords()
+    inside = ((c >= 0) & (c < np.array(vel.shape[:3]))).all(1)
+    vox = np.ravel_multi_index(c[inside].T, vel.shape[:3])
+    comp = (vox[:, None] * 3 + np.arange(3)).reshape(-1)
+    cand = comp[np.abs(vel.reshape(-1)[comp]) > 0.05]
+    errs, kinds = [], []
     for k in range(nprobe):
         is_vel = vel_probes and k % 2 == 1
         if is_vel:
             h = 1e-4
-            dv = rng.standard_normal(vel.shape).astype(np.float32)
+            # sparse: 32 components at voxels of the initial band, away from
+            # v = 0 (where the upwind side, fixed in the adjoint, switches); a
+            # dense direction moves every voxel and crosses Godunov/upwind
+            # kinks, which leaves its difference quotient uncertain at 1e-2
+            dv = np.zeros(vel.shape, np.float32)
+            pick = rng.choice(cand, 32, replace=False)
+            dv.reshape(-1)[pick] = rng.standard_normal(32)
             vp = (vel + h * dv).astype(np.float32)
             vm = (vel - h * dv).astype(np.float32)
             Lp, hp, cp = _fp64_loss(template, phi0.astype(np.float64), Field.dense(vp), times, target_fn)
             Lm, hm, cm = _fp64_loss(template, phi0.astype(np.float64), Field.dense(vm), times, target_fn)
             ad = float(np.dot(g_vel.reshape(-1).astype(np.float64),
                               (vp.astype(np.float64) - vm.astype(np.float64)).reshape(-1))) / (2 * h)
+            gnorm = float(np.linalg.norm(g_vel.reshape(-1)[pick].astype(np.float64)))
         else:
             h = 1e-6
             dphi = rng.standard_normal(phi0.size)
             Lp, hp, cp = _fp64_loss(template, phi0 + h * dphi, base_field, times, target_fn)
             Lm, hm, cm = _fp64_loss(template, phi0 - h * dphi, base_field, times, target_fn)
             ad = float(np.dot(g_phi.astype(np.float64), dphi))
-        if not (_same_topology(hp, host0) and _same_topology(hm, host0) and cp == counts0 and cm == counts0):
+            gnorm = float(np.linalg.norm(g_phi.astype(np.float64)))
+        if not (cp == counts0 and cm == counts0):
             continue
         fd = (Lp - Lm) / (2 * h)
-        rel = abs(fd - ad) / max(abs(fd), 1e-12)
+        # g.d of a standard normal direction d has the scale |g| on the
+        # direction's support; a direction nearly orthogonal to g is measured
+        # against a tenth of that scale, not against its own tiny |fd|
+        rel = abs(fd - ad) / max(abs(fd), 0.1 * gnorm, 1e-12)
         errs.append(rel)
+        kinds.append(is_vel)
         print("%s probe %d: fp64 fd %+.9e adjoint %+.9e rel %.2e" % ("vel" if is_vel else "phi", k, fd, ad, rel))
     assert len(errs) >= nprobe * 3 // 4, len(errs)
-    errs = np.array(errs)
-    print("relative error: median %.2e max %.2e over %d probes" % (np.median(errs), errs.max(), errs.size))
+    errs, kinds = np.array(errs), np.array(kinds)
+    for name, sel in (("phi", ~kinds), ("velocity", kinds)):
+        if sel.any():
+            print("%s probes: relative error median %.2e max %.2e over %d probes"
+                  % (name, np.median(errs[sel]), errs[sel].max(), sel.sum()))
     assert np.median(errs) < tol_median and errs.max() < tol_max
     return tape
 
