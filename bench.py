@@ -191,7 +191,16 @@ def run_gb300(args):
     # end to end through the host-facing API: upload, advect one time unit, download
     e2e = None
     if args.e2e_steps > 0:
-        g = dev.to_host()
+        # the level set lives in page-locked host memory; each step uploads
+        # it, advects one time unit and downloads the result into the same
+        # buffers (an in-place update of the host grid)
+        from openvdb_gb300 import HostArena
+        arena = HostArena(pinned=True)
+        g = dev.to_host(arena)
+        d = DeviceLevelSet(g, device=dev_index)  # untimed warm-up of the host path
+        g = d.to_host(arena)
+        d.close()
+        torch.cuda.synchronize()
         te = t
         e2e_updates = 0
         h2d = d2h = 0
@@ -203,7 +212,7 @@ def run_gb300(args):
             a = make_advection(d, dfield, cfl=args.cfl)
             a.advect(te, te + 1.0)
             e2e_updates += d.stats()["voxel_updates"]
-            g = d.to_host()
+            g = d.to_host(arena)
             d2h += host_bytes(g)
             d.close()
             te += 1.0
@@ -274,7 +283,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="fast", choices=["fast", "parity"])
     ap.add_argument("--cfl", type=float, default=0.5)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()

@@ -2,6 +2,6 @@
 LevelSetTracker hot path) behind a C ABI; see include/gbls.h."""
 from . import _abi
 from .fields import Field
-from .grid import HostGrid, bitwise_equal, compare, digest, summary, topology_equal
+from .grid import HostArena, HostGrid, bitwise_equal, compare, digest, summary, topology_equal
 from .levelset import (FAST, PARITY, DeviceBatch, DeviceField, DeviceLevelSet, LevelSetAdvection,
                        LevelSetTracker)

@@ -17,6 +17,7 @@
 #include "../../include/gbls.h"
 #include "adjoint.h"
 #include "gbls_internal.cuh"
+#include "io.h"
 #include "stencil.h"
 #include "stencil_ops.cuh"
 #include "topology.cuh"
@@ -432,6 +433,9 @@ struct gbls_handle {
     DevArray<uint64_t> cand, cand_sorted, new_keys;
     DevArray<int32_t> new_slots, cnt, keep, idx, remap;
     DevArray<uint8_t> cub_tmp, flags;
+    DevArray<int32_t> io_perm;   // upload: staged index of each leaf / lower / upper node
+    DevArray<float> io_tiles;    // staged node tiles (upload and download)
+    DevArray<int32_t> io_orig;   // download: leaf origins
     DevStatus* st_d = nullptr;
     DevStatus* st_h = nullptr;
     DevArray<unsigned long long> u64s;
@@ -1249,8 +1253,11 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
             if (o[a] < -COORD_SAFE || o[a] >= COORD_SAFE) fail(GBLS_ERR_DOMAIN, "coordinate outside the supported range");
         }
     };
-    struct Src { uint64_t key; int inst; int64_t idx; bool operator<(const Src& o) const { return key < o.key; } };
+    // Keys of every node with its index in the staged (concatenated) input
+    // arrays; inputs in tree order (the usual case) need no sort.
+    struct Src { uint64_t key; int64_t idx; bool operator<(const Src& o) const { return key < o.key; } };
     std::vector<Src> lv, lo, up, rt;
+    std::vector<int64_t> lv_base(size_t(n) + 1, 0), lo_base(size_t(n) + 1, 0), up_base(size_t(n) + 1, 0);
     for (int q = 0; q < n; ++q) {
         const gbls_grid_desc* d = descs + q;
         if (d->voxel_size != d0->voxel_size || d->background != d0->background)
@@ -1259,91 +1266,68 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
             fail(GBLS_ERR_INVALID_ARGUMENT, "negative count");
         if (d->leaf_count > 0 && (!d->leaf_origins || !d->leaf_masks || !d->leaf_values))
             fail(GBLS_ERR_INVALID_ARGUMENT, "null leaf arrays");
+        if ((d->lower_count > 0 && (!d->lower_origins || !d->lower_tiles)) ||
+            (d->upper_count > 0 && (!d->upper_origins || !d->upper_tiles)) ||
+            (d->root_tile_count > 0 && (!d->root_tile_origins || !d->root_tile_values)))
+            fail(GBLS_ERR_INVALID_ARGUMENT, "null node arrays");
         const uint64_t ib = uint64_t(q) << KEY_INST_SHIFT;
+        lv_base[size_t(q) + 1] = lv_base[size_t(q)] + d->leaf_count;
+        lo_base[size_t(q) + 1] = lo_base[size_t(q)] + d->lower_count;
+        up_base[size_t(q) + 1] = up_base[size_t(q)] + d->upper_count;
         for (int64_t i = 0; i < d->leaf_count; ++i) {
             const int32_t* o = d->leaf_origins + 3 * i;
             check_origin(o, 8);
-            lv.push_back({leaf_key(o[0], o[1], o[2]) | ib, q, i});
+            lv.push_back({leaf_key(o[0], o[1], o[2]) | ib, lv_base[size_t(q)] + i});
         }
         for (int64_t i = 0; i < d->lower_count; ++i) {
             const int32_t* o = d->lower_origins + 3 * i;
             check_origin(o, 128);
-            lo.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 12, q, i});
+            lo.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 12, lo_base[size_t(q)] + i});
         }
         for (int64_t i = 0; i < d->upper_count; ++i) {
             const int32_t* o = d->upper_origins + 3 * i;
             check_origin(o, 4096);
-            up.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 27, q, i});
+            up.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 27, up_base[size_t(q)] + i});
         }
         for (int64_t i = 0; i < d->root_tile_count; ++i) {
             const int32_t* o = d->root_tile_origins + 3 * i;
             check_origin(o, 4096);
-            rt.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 27, q, i});
+            rt.push_back({(leaf_key(o[0], o[1], o[2]) | ib) >> 27, int64_t(q) << 32 | i});
         }
     }
-    std::sort(lv.begin(), lv.end());
-    std::sort(lo.begin(), lo.end());
-    std::sort(up.begin(), up.end());
-    std::sort(rt.begin(), rt.end());
-    const int64_t L = int64_t(lv.size());
-    std::vector<uint64_t> keys(static_cast<size_t>(L)), am(static_cast<size_t>(L) * 8), sm(static_cast<size_t>(L) * 8, 0);
-    std::vector<int32_t> slots(static_cast<size_t>(L));
-    std::vector<float> vals(static_cast<size_t>(L) * LEAF_VOX, 0.0f);
-    for (int64_t i = 0; i < L; ++i) {
-        if (i && lv[size_t(i)].key == lv[size_t(i - 1)].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate leaf");
-        const gbls_grid_desc* d = descs + lv[size_t(i)].inst;
-        const int64_t src = lv[size_t(i)].idx;
-        keys[size_t(i)] = lv[size_t(i)].key;
-        slots[size_t(i)] = int32_t(i);
-        const float* v = d->leaf_values + src * LEAF_VOX;
-        int rank = 0;
-        for (int w = 0; w < 8; ++w) {
-            const uint64_t m = d->leaf_masks[src * 8 + w];
-            am[size_t(i) * 8 + w] = m;
-            uint64_t sg = 0;
-            for (int b = 0; b < 64; ++b) {
-                const float x = v[w * 64 + b];
-                if (x < 0.0f) sg |= uint64_t(1) << b;
-                if ((m >> b) & 1) vals[size_t(i) * LEAF_VOX + rank++] = x;
-                else if (!is_pm_gamma(x, g)) fail(GBLS_ERR_UNSUPPORTED, "inactive leaf value other than +-background");
-            }
-            sm[size_t(i) * 8 + w] = sg;
+    auto order = [](std::vector<Src>& v, const char* dup) {
+        if (!std::is_sorted(v.begin(), v.end())) std::sort(v.begin(), v.end());
+        for (size_t i = 1; i < v.size(); ++i)
+            if (v[i].key == v[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, dup);
+    };
+    order(lv, "duplicate leaf");
+    order(lo, "duplicate lower node");
+    order(up, "duplicate upper node");
+    order(rt, "duplicate root tile");
+    const int64_t L = int64_t(lv.size()), NLO = int64_t(lo.size()), NUP = int64_t(up.size());
+    std::vector<uint64_t> keys(static_cast<size_t>(L)), lkeys(static_cast<size_t>(NLO)), ukeys(static_cast<size_t>(NUP));
+    std::vector<int32_t> perm(static_cast<size_t>(L + NLO + NUP));
+    for (int64_t i = 0; i < L; ++i) { keys[size_t(i)] = lv[size_t(i)].key; perm[size_t(i)] = int32_t(lv[size_t(i)].idx); }
+    for (int64_t i = 0; i < NLO; ++i) { lkeys[size_t(i)] = lo[size_t(i)].key; perm[size_t(L + i)] = int32_t(lo[size_t(i)].idx); }
+    for (int64_t i = 0; i < NUP; ++i) { ukeys[size_t(i)] = up[size_t(i)].key; perm[size_t(L + NLO + i)] = int32_t(up[size_t(i)].idx); }
+    // every leaf under a lower node, every lower node under an upper node (sorted walks)
+    auto parents = [](const std::vector<uint64_t>& child, int shift, const std::vector<uint64_t>& par, const char* msg) {
+        size_t p = 0;
+        for (uint64_t k : child) {
+            const uint64_t pk = k >> shift;
+            while (p < par.size() && par[p] < pk) ++p;
+            if (p == par.size() || par[p] != pk) fail(GBLS_ERR_INVALID_ARGUMENT, msg);
         }
-    }
-    std::vector<uint64_t> lkeys(lo.size()), lsign(lo.size() * 64, 0);
-    for (size_t i = 0; i < lo.size(); ++i) {
-        if (i && lo[i].key == lo[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate lower node");
-        lkeys[i] = lo[i].key;
-        const float* t = descs[lo[i].inst].lower_tiles + lo[i].idx * LOWER_SLOTS;
-        for (int q = 0; q < LOWER_SLOTS; ++q) {
-            if (std::binary_search(keys.begin(), keys.end(), (lkeys[i] << 12) | uint64_t(q))) continue;
-            if (!is_pm_gamma(t[q], g)) fail(GBLS_ERR_UNSUPPORTED, "lower-node tile other than +-background");
-            if (t[q] < 0.0f) lsign[i * 64 + (q >> 6)] |= uint64_t(1) << (q & 63);
-        }
-    }
-    for (uint64_t k : keys)
-        if (!std::binary_search(lkeys.begin(), lkeys.end(), k >> 12)) fail(GBLS_ERR_INVALID_ARGUMENT, "leaf without lower node");
-    std::vector<uint64_t> ukeys(up.size()), usign(up.size() * 512, 0);
-    for (size_t i = 0; i < up.size(); ++i) {
-        if (i && up[i].key == up[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate upper node");
-        ukeys[i] = up[i].key;
-        const float* t = descs[up[i].inst].upper_tiles + up[i].idx * UPPER_SLOTS;
-        for (int q = 0; q < UPPER_SLOTS; ++q) {
-            if (std::binary_search(lkeys.begin(), lkeys.end(), (ukeys[i] << 15) | uint64_t(q))) continue;
-            if (!is_pm_gamma(t[q], g)) fail(GBLS_ERR_UNSUPPORTED, "upper-node tile other than +-background");
-            if (t[q] < 0.0f) usign[i * 512 + (q >> 6)] |= uint64_t(1) << (q & 63);
-        }
-    }
-    for (uint64_t k : lkeys)
-        if (!std::binary_search(ukeys.begin(), ukeys.end(), k >> 15)) fail(GBLS_ERR_INVALID_ARGUMENT, "lower node without upper node");
+    };
+    parents(keys, 12, lkeys, "leaf without lower node");
+    parents(lkeys, 15, ukeys, "lower node without upper node");
     h.root_keys_h.clear();
     h.root_sign_h.clear();
-    for (size_t i = 0; i < rt.size(); ++i) {
-        const float v = descs[rt[i].inst].root_tile_values[rt[i].idx];
+    for (const Src& r : rt) {
+        const float v = descs[r.idx >> 32].root_tile_values[r.idx & 0xffffffff];
         if (!is_pm_gamma(v, g)) fail(GBLS_ERR_UNSUPPORTED, "root tile other than +-background");
-        if (std::binary_search(ukeys.begin(), ukeys.end(), rt[i].key)) fail(GBLS_ERR_INVALID_ARGUMENT, "root tile overlaps an upper node");
-        if (i && rt[i].key == rt[i - 1].key) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate root tile");
-        h.root_keys_h.push_back(rt[i].key);
+        if (std::binary_search(ukeys.begin(), ukeys.end(), r.key)) fail(GBLS_ERR_INVALID_ARGUMENT, "root tile overlaps an upper node");
+        h.root_keys_h.push_back(r.key);
         h.root_sign_h.push_back(uint8_t(v < 0.0f ? 1 : 0));
     }
     // device state
@@ -1365,19 +1349,57 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     h.free_slots.reserve(size_t(scap), h.stream);
     h.slot_cap = scap;
     std::vector<int32_t> fs;
+    fs.reserve(size_t(scap - L));
     for (int64_t q = scap - 1; q >= L; --q) fs.push_back(int32_t(q));
     h.nfree = int64_t(fs.size());
+    std::vector<int32_t> slots(static_cast<size_t>(L));
+    for (int64_t i = 0; i < L; ++i) slots[size_t(i)] = int32_t(i);
     h.free_slots.upload(fs.data(), fs.size(), h.stream);
     h.keys[0].upload(keys.data(), keys.size(), h.stream);
     h.slot[0].upload(slots.data(), slots.size(), h.stream);
-    h.am[0].upload(am.data(), am.size(), h.stream);
-    h.sm[0].upload(sm.data(), sm.size(), h.stream);
-    h.vals[0].upload(vals.data(), vals.size(), h.stream);
+    h.io_perm.upload(perm.data(), perm.size(), h.stream);
     h.lower_keys_h = lkeys;
     h.lower_keys.upload(lkeys.data(), lkeys.size(), h.stream);
-    h.lower_sign.upload(lsign.data(), lsign.size(), h.stream);
+    h.upper_keys.upload(ukeys.data(), ukeys.size(), h.stream);
+    h.lower_sign.reserve(size_t(std::max<int64_t>(NLO, 1)) * 64, h.stream);
+    h.upper_sign.reserve(size_t(std::max<int64_t>(NUP, 1)) * 512, h.stream);
+    h.io_tiles.reserve(size_t(std::max<int64_t>(NLO * LOWER_SLOTS + NUP * UPPER_SLOTS, 1)), h.stream);
+    // stage the inputs (mask set 1 and value buffer 1 are free) and pack them
+    float* lo_stage = h.io_tiles.p;
+    float* up_stage = h.io_tiles.p + NLO * LOWER_SLOTS;
+    for (int q = 0; q < n; ++q) {
+        const gbls_grid_desc* d = descs + q;
+        const size_t a = size_t(lv_base[size_t(q)]), b = size_t(lo_base[size_t(q)]), c = size_t(up_base[size_t(q)]);
+        if (d->leaf_count) {
+            CU(cudaMemcpyAsync(h.am[1].p + a * 8, d->leaf_masks, size_t(d->leaf_count) * 64, cudaMemcpyHostToDevice, h.stream));
+            CU(cudaMemcpyAsync(h.vals[1].p + a * LEAF_VOX, d->leaf_values, size_t(d->leaf_count) * LEAF_VOX * 4,
+                               cudaMemcpyHostToDevice, h.stream));
+        }
+        if (d->lower_count)
+            CU(cudaMemcpyAsync(lo_stage + b * LOWER_SLOTS, d->lower_tiles, size_t(d->lower_count) * LOWER_SLOTS * 4,
+                               cudaMemcpyHostToDevice, h.stream));
+        if (d->upper_count)
+            CU(cudaMemcpyAsync(up_stage + c * UPPER_SLOTS, d->upper_tiles, size_t(d->upper_count) * UPPER_SLOTS * 4,
+                               cudaMemcpyHostToDevice, h.stream));
+    }
+    h.clear_status();
+    unsigned long long* err = &h.st_d->io_err;
+    launch_pack_leaves(L, h.io_perm.p, h.am[1].p, h.vals[1].p, g, h.am[0].p, h.sm[0].p, h.vals[0].p, err, h.stream);
+    launch_node_signs(NLO, 12, h.lower_keys.p, h.io_perm.p + L, lo_stage, h.keys[0].p, L, g, h.lower_sign.p, err,
+                      IO_ERR_LOWER_TILE, h.stream);
+    launch_node_signs(NUP, 15, h.upper_keys.p, h.io_perm.p + L + NLO, up_stage, h.lower_keys.p, NLO, g,
+                      h.upper_sign.p, err, IO_ERR_UPPER_TILE, h.stream);
+    h.stats.kernel_launches += (L > 0) + (NLO > 0) + (NUP > 0);
+    CU(cudaGetLastError());
+    std::vector<uint64_t> usign(static_cast<size_t>(NUP) * 512);
+    h.upper_sign.download(usign.data(), usign.size(), h.stream);
+    h.read_status();
+    const unsigned long long e = h.st_h->io_err;
+    if (e & IO_ERR_LEAF_VALUE) fail(GBLS_ERR_UNSUPPORTED, "inactive leaf value other than +-background");
+    if (e & IO_ERR_LOWER_TILE) fail(GBLS_ERR_UNSUPPORTED, "lower-node tile other than +-background");
+    if (e & IO_ERR_UPPER_TILE) fail(GBLS_ERR_UNSUPPORTED, "upper-node tile other than +-background");
     h.upper_keys_h = ukeys;
-    h.upper_sign_h = usign;
+    h.upper_sign_h.swap(usign);
     h.nodes_checked = false;
     h.upload_upper_root();
     h.rebuild_nbr();
@@ -1422,81 +1444,63 @@ std::vector<uint64_t> host_keys(gbls_handle& h) {
 }
 
 void download(gbls_handle& h, gbls_grid_desc* d, int inst) {
-    const std::vector<uint64_t> keys = host_keys(h);
-    const InstRange R = inst_range(h, keys, inst);
-    const int64_t L = R.l1 - R.l0;
-    if (d->leaf_count != L || d->lower_count != R.lo1 - R.lo0 || d->upper_count != R.u1 - R.u0 ||
-        d->root_tile_count != R.r1 - R.r0)
+    InstRange R{0, h.nleaf, 0, int64_t(h.lower_keys_h.size()), 0, int64_t(h.upper_keys_h.size()), 0,
+                int64_t(h.root_keys_h.size())};
+    if (inst >= 0) R = inst_range(h, host_keys(h), inst);
+    const int64_t L = R.l1 - R.l0, NLO = R.lo1 - R.lo0, NUP = R.u1 - R.u0;
+    if (d->leaf_count != L || d->lower_count != NLO || d->upper_count != NUP || d->root_tile_count != R.r1 - R.r0)
         fail(GBLS_ERR_INVALID_ARGUMENT, "descriptor counts do not match gbls_get_counts");
+    if ((L > 0 && (!d->leaf_origins || !d->leaf_masks || !d->leaf_values)) ||
+        (NLO > 0 && (!d->lower_origins || !d->lower_tiles)) || (NUP > 0 && (!d->upper_origins || !d->upper_tiles)) ||
+        (R.r1 > R.r0 && (!d->root_tile_origins || !d->root_tile_values)))
+        fail(GBLS_ERR_INVALID_ARGUMENT, "null arrays in the download descriptor");
     d->voxel_size = h.voxel_size;
     for (int i = 0; i < 3; ++i) d->translation[i] = h.translation[i];
     d->map_type = h.map_type;
     d->background = h.gamma;
     const float g = h.gamma;
-    std::vector<int32_t> slots(static_cast<size_t>(h.nleaf));
-    h.slot[h.kc].download(slots.data(), size_t(h.nleaf), h.stream);
-    h.sync();
+    // dense values, masks and origins are assembled in the free value
+    // buffer / mask set, node tiles in the tile staging buffer
     if (L > 0) {
-        DevArray<float> dense;
-        dense.reserve(size_t(L) * LEAF_VOX, h.stream);
+        float* dense = h.vals[other_of(h.vc, h.vc)].p;
+        uint64_t* masks = h.am[other_of(h.mc, h.mc)].p;
+        h.io_orig.reserve(size_t(L) * 3, h.stream);
         k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S() + R.l0, h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, g,
-                                                     dense.p);
-        ++h.stats.kernel_launches;
+                                                     dense);
+        launch_leaf_headers(L, h.K() + R.l0, h.S() + R.l0, h.am[h.mc].p, h.io_orig.p, masks, h.stream);
+        h.stats.kernel_launches += 2;
         CU(cudaGetLastError());
-        dense.download(d->leaf_values, size_t(L) * LEAF_VOX, h.stream);
-        std::vector<uint64_t> am(size_t(h.slot_cap) * 8);
-        h.am[h.mc].download(am.data(), am.size(), h.stream);
-        h.sync();
-        for (int64_t i = 0; i < L; ++i) {
+        CU(cudaMemcpyAsync(d->leaf_values, dense, size_t(L) * LEAF_VOX * 4, cudaMemcpyDeviceToHost, h.stream));
+        CU(cudaMemcpyAsync(d->leaf_masks, masks, size_t(L) * 64, cudaMemcpyDeviceToHost, h.stream));
+        CU(cudaMemcpyAsync(d->leaf_origins, h.io_orig.p, size_t(L) * 12, cudaMemcpyDeviceToHost, h.stream));
+    }
+    if (NLO + NUP > 0) {
+        h.io_tiles.reserve(size_t(NLO * LOWER_SLOTS + NUP * UPPER_SLOTS), h.stream);
+        float* lt = h.io_tiles.p;
+        float* ut = h.io_tiles.p + NLO * LOWER_SLOTS;
+        launch_node_tiles(NLO, 12, h.lower_keys.p + R.lo0, h.lower_sign.p + R.lo0 * 64, h.K(), h.nleaf, g, lt,
+                          h.stream);
+        launch_node_tiles(NUP, 15, h.upper_keys.p + R.u0, h.upper_sign.p + R.u0 * 512, h.lower_keys.p,
+                          int64_t(h.lower_keys_h.size()), g, ut, h.stream);
+        h.stats.kernel_launches += (NLO > 0) + (NUP > 0);
+        CU(cudaGetLastError());
+        if (NLO) CU(cudaMemcpyAsync(d->lower_tiles, lt, size_t(NLO) * LOWER_SLOTS * 4, cudaMemcpyDeviceToHost, h.stream));
+        if (NUP) CU(cudaMemcpyAsync(d->upper_tiles, ut, size_t(NUP) * UPPER_SLOTS * 4, cudaMemcpyDeviceToHost, h.stream));
+    }
+    auto origins = [](const std::vector<uint64_t>& k, int64_t a, int64_t b, int shift, int32_t* out) {
+        for (int64_t i = a; i < b; ++i) {
             int32_t x, y, z;
-            key_origin(keys[size_t(R.l0 + i)], x, y, z);
-            d->leaf_origins[3 * i] = x;
-            d->leaf_origins[3 * i + 1] = y;
-            d->leaf_origins[3 * i + 2] = z;
-            for (int w = 0; w < 8; ++w) d->leaf_masks[8 * i + w] = am[size_t(slots[size_t(R.l0 + i)]) * 8 + w];
+            key_origin(k[size_t(i)] << shift, x, y, z);
+            out[3 * (i - a)] = x;
+            out[3 * (i - a) + 1] = y;
+            out[3 * (i - a) + 2] = z;
         }
-    }
-    const size_t nl = h.lower_keys_h.size();
-    std::vector<uint64_t> lsign(nl * 64);
-    h.lower_sign.download(lsign.data(), lsign.size(), h.stream);
+    };
+    origins(h.lower_keys_h, R.lo0, R.lo1, 12, d->lower_origins);
+    origins(h.upper_keys_h, R.u0, R.u1, 27, d->upper_origins);
+    origins(h.root_keys_h, R.r0, R.r1, 27, d->root_tile_origins);
+    for (int64_t i = R.r0; i < R.r1; ++i) d->root_tile_values[i - R.r0] = h.root_sign_h[size_t(i)] ? -g : g;
     h.sync();
-    for (int64_t i = R.lo0; i < R.lo1; ++i) {
-        const int64_t o = i - R.lo0;
-        int32_t x, y, z;
-        key_origin(h.lower_keys_h[size_t(i)] << 12, x, y, z);
-        d->lower_origins[3 * o] = x;
-        d->lower_origins[3 * o + 1] = y;
-        d->lower_origins[3 * o + 2] = z;
-        float* t = d->lower_tiles + o * LOWER_SLOTS;
-        for (int n = 0; n < LOWER_SLOTS; ++n) {
-            const uint64_t k = (h.lower_keys_h[size_t(i)] << 12) | uint64_t(n);
-            if (std::binary_search(keys.begin(), keys.end(), k)) { t[n] = 0.0f; continue; }
-            t[n] = ((lsign[size_t(i) * 64 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
-        }
-    }
-    for (int64_t i = R.u0; i < R.u1; ++i) {
-        const int64_t o = i - R.u0;
-        int32_t x, y, z;
-        key_origin(h.upper_keys_h[size_t(i)] << 27, x, y, z);
-        d->upper_origins[3 * o] = x;
-        d->upper_origins[3 * o + 1] = y;
-        d->upper_origins[3 * o + 2] = z;
-        float* t = d->upper_tiles + o * UPPER_SLOTS;
-        for (int n = 0; n < UPPER_SLOTS; ++n) {
-            const uint64_t k = (h.upper_keys_h[size_t(i)] << 15) | uint64_t(n);
-            if (std::binary_search(h.lower_keys_h.begin(), h.lower_keys_h.end(), k)) { t[n] = 0.0f; continue; }
-            t[n] = ((h.upper_sign_h[size_t(i) * 512 + (n >> 6)] >> (n & 63)) & 1) ? -g : g;
-        }
-    }
-    for (int64_t i = R.r0; i < R.r1; ++i) {
-        const int64_t o = i - R.r0;
-        int32_t x, y, z;
-        key_origin(h.root_keys_h[size_t(i)] << 27, x, y, z);
-        d->root_tile_origins[3 * o] = x;
-        d->root_tile_origins[3 * o + 1] = y;
-        d->root_tile_origins[3 * o + 2] = z;
-        d->root_tile_values[o] = h.root_sign_h[size_t(i)] ? -g : g;
-    }
 }
 
 int64_t active_count(gbls_handle& h) {

@@ -16,6 +16,7 @@ struct DevStatus {
     unsigned int max_v2_bits;          // CFL reduction
     unsigned int pad;
     unsigned long long n_active;       // active voxels of the kept leaves
+    unsigned long long io_err;         // upload value checks (IO_ERR_* bits of io.h)
 };
 
 // Face layer of a leaf mask that a missing neighbour on face f would receive.

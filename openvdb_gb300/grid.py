@@ -18,6 +18,39 @@ def _ptr(a, ctype):
     return a.ctypes.data_as(C.POINTER(ctype))
 
 
+class HostArena:
+    """Reusable host storage for downloads, optionally page-locked.
+
+    HostGrid.allocate(counts, arena) hands out views into buffers that grow
+    on demand and are reused by the next allocation from the same arena, so
+    repeated downloads touch no fresh pages.  A grid allocated from an arena
+    is overwritten by the next allocation from it: uploading it first and
+    downloading the result into the same arena updates the grid in place.
+    """
+
+    def __init__(self, pinned=False, headroom=1.25):
+        self.pinned = bool(pinned)
+        self.headroom = float(headroom)  # capacity factor of every (re)allocation
+        self._bufs = {}
+
+    def _alloc(self, nbytes):
+        if self.pinned:
+            import torch
+            t = torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True)
+            return t, t.numpy()
+        a = np.empty(max(nbytes, 1), np.uint8)
+        return a, a
+
+    def array(self, name, shape, dtype):
+        nbytes = int(np.prod(shape, dtype=np.int64)) * np.dtype(dtype).itemsize
+        held = self._bufs.get(name)
+        if held is None or held[1].nbytes < nbytes:
+            cap = int(nbytes * self.headroom) + 64
+            held = self._alloc(cap)
+            self._bufs[name] = held
+        return held[1][:nbytes].view(dtype).reshape(shape)
+
+
 class HostGrid:
     """Numpy arrays describing one FloatGrid level set."""
 
@@ -47,7 +80,22 @@ class HostGrid:
 
     # ---- construction from counts (to receive a download) ---------------
     @classmethod
-    def allocate(cls, counts):
+    def allocate(cls, counts, arena=None):
+        """Arrays for a download of `counts` (every element is written by the
+        download); from `arena` when given, else freshly zeroed."""
+        if arena is not None:
+            g = cls()
+            for k, tail, dt, n in (("leaf_origins", (3,), np.int32, counts.leaf_count),
+                                   ("leaf_masks", (8,), np.uint64, counts.leaf_count),
+                                   ("leaf_values", (512,), np.float32, counts.leaf_count),
+                                   ("lower_origins", (3,), np.int32, counts.lower_count),
+                                   ("lower_tiles", (LOWER_SLOTS,), np.float32, counts.lower_count),
+                                   ("upper_origins", (3,), np.int32, counts.upper_count),
+                                   ("upper_tiles", (UPPER_SLOTS,), np.float32, counts.upper_count),
+                                   ("root_tile_origins", (3,), np.int32, counts.root_tile_count),
+                                   ("root_tile_values", (), np.float32, counts.root_tile_count)):
+                setattr(g, k, arena.array(k, (n,) + tail, dt))
+            return g
         return cls(
             leaf_origins=np.zeros((counts.leaf_count, 3), np.int32),
             leaf_masks=np.zeros((counts.leaf_count, 8), np.uint64),

@@ -88,8 +88,9 @@ class DeviceLevelSet:
     def leaf_count(self):
         return self.counts().leaf_count
 
-    def to_host(self):
-        g = HostGrid.allocate(self.counts())
+    def to_host(self, arena=None):
+        """Download into a new HostGrid (arrays from `arena` when given)."""
+        g = HostGrid.allocate(self.counts(), arena)
         d = g.desc()
         _call(lib().gbls_download(self._h, C.byref(d)))
         g.copy_scalars_from(d)
