@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <memory>
 #include <cstring>
 #include <new>
@@ -454,6 +455,10 @@ struct gbls_handle {
     std::vector<std::unique_ptr<TapeStep>> tape;
     TapeStep* tape_cur = nullptr;
     DevArray<int32_t> tape_inv;
+    // work enqueued by the advection loop right before the read-back that
+    // ends a tracker pass (the next substep's CFL reduction), so that one
+    // synchronisation serves both
+    std::function<void()> before_prune_sync;
     // measurement
     gbls_stats stats{};
     int64_t nactive = -1;  // active voxels, -1 = unknown
@@ -1025,6 +1030,7 @@ void prune_compact(gbls_handle& h) {
             ++h.stats.kernel_launches;
         }
         CU(cudaGetLastError());
+        if (h.before_prune_sync) h.before_prune_sync();
         h.read_status();
         const int64_t kept = int64_t(h.st_h->n_cand);
         h.nfree += L - kept;
@@ -1135,14 +1141,14 @@ FieldParams field_params(const gbls_field* f, float t) {
 }
 
 // max |v|^2 over the active voxels at time t (sampleField, :447-455).
-float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
-    if (f->desc.kind == GBLS_FIELD_CONSTANT) {
-        const float* c = f->desc.constant;
-        return c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-    }
-    h.clear_status();
+// Enqueue the CFL reduction (max |v|^2 over the active voxels at time t)
+// into the status block, which the caller has cleared; the leaf count is
+// read on the device when `nleaf_dev` is given (h.nleaf is then an upper
+// bound).
+void enqueue_max_speed(gbls_handle& h, const gbls_field* f, float t, const unsigned long long* nleaf_dev) {
     CflArgs a{};
     a.nleaf = h.nleaf;
+    a.nleaf_dev = nleaf_dev;
     a.keys = h.K();
     a.slot = h.S();
     a.amask = h.am[h.mc].p;
@@ -1152,10 +1158,23 @@ float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
     launch_cfl(a, h.stream);
     ++h.stats.kernel_launches;
     CU(cudaGetLastError());
-    h.read_status();
+}
+
+float status_max_speed(const gbls_handle& h) {
     float m;
     std::memcpy(&m, &h.st_h->max_v2_bits, 4);
     return m;
+}
+
+float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
+    if (f->desc.kind == GBLS_FIELD_CONSTANT) {
+        const float* c = f->desc.constant;
+        return c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    }
+    h.clear_status();
+    enqueue_max_speed(h, f, t, nullptr);
+    h.read_status();
+    return status_max_speed(h);
 }
 
 void rk_stage(gbls_handle& h, const RkArgs& a) {
@@ -2245,11 +2264,20 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
         const float cfl_ref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) /
                               std::sqrt(3.0f);
         const float C = cfl > 0.0f ? cfl : cfl_ref;
+        // the CFL reduction of substep k+1 rides on the read-back that ends
+        // the tracker pass of substep k
+        bool have_next = false;
+        float next_v2 = 0.0f;
+        struct Reset {
+            gbls_handle* h;
+            ~Reset() { h->before_prune_sync = nullptr; }
+        } reset{h};
         while (forward ? t0 < t1 : t0 > t1) {
             if (!check_intr(*h)) { interrupted = true; break; }
             if (h->nleaf == 0) break;  // sampleField returns 0 for an empty grid
             start_intr(*h, "Sampling advection field");
-            const float maxv2 = max_speed_sqr(*h, field, t0);
+            const float maxv2 = have_next ? next_v2 : max_speed_sqr(*h, field, t0);
+            have_next = false;
             end_intr(*h);
             if (!(maxv2 > 1e-5f) && !(maxv2 < -1e-5f)) break;  // isApproxZero(maxAbsV, Delta)
             const float span = std::fabs(t1 - t0);
@@ -2269,7 +2297,21 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             advect_stages(*h, field, temporal, t0, dt, !forward);
             t0 += forward ? dt : -dt;
             ++count;
+            const bool more = forward ? t0 < t1 : t0 > t1;
+            bool queued = false;
+            if (more && field->desc.kind != GBLS_FIELD_CONSTANT) {
+                const float tn = t0;
+                h->before_prune_sync = [h, field, tn, &queued] {
+                    enqueue_max_speed(*h, field, tn, &h->st_d->n_cand);
+                    queued = true;
+                };
+            }
             track(*h);
+            h->before_prune_sync = nullptr;
+            if (queued) {
+                next_v2 = status_max_speed(*h);
+                have_next = true;
+            }
         }
         h->sync();
     });

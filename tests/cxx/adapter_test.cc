@@ -1,0 +1,169 @@
+// Host-side checks of the C++ drop-in (include/openvdb_gb300/*.h) against
+// the reference's own OpenVDB types, compiled from the reference headers:
+//   1. pack(createLevelSetSphere grid) equals the library's sphere fixture
+//      descriptor element for element (tree order, tiles, masks, values);
+//   2. unpack -> pack round trips, in place, with a changed background;
+//   3. status codes map to the reference's exception types;
+//   4. the tracker constructor rejects what the reference rejects;
+//   5. an aligned DiscreteField becomes a dense box holding field(ijk);
+//      a non-aligned one is refused;
+//   6. advect() either runs on a GPU or fails with an OpenVDB exception.
+// Prints "ok <n>" per check; exits non-zero on the first failure.
+#include <openvdb/openvdb.h>
+#include <openvdb/tools/LevelSetSphere.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "openvdb_gb300/LevelSetAdvect.h"
+
+using namespace openvdb;
+
+static int g_n = 0;
+#define CHECK(c)                                                              \
+    do {                                                                      \
+        if (!(c)) {                                                           \
+            std::fprintf(stderr, "FAILED %s:%d: %s\n", __FILE__, __LINE__, #c); \
+            std::exit(1);                                                     \
+        }                                                                     \
+    } while (0)
+
+template <class T>
+static bool same(const T* a, const T* b, int64_t n) {
+    return n == 0 || std::memcmp(a, b, size_t(n) * sizeof(T)) == 0;
+}
+
+static bool sameDesc(const gbls_grid_desc& a, const gbls_grid_desc& b) {
+    return a.voxel_size == b.voxel_size && a.background == b.background && a.leaf_count == b.leaf_count &&
+           a.lower_count == b.lower_count && a.upper_count == b.upper_count &&
+           a.root_tile_count == b.root_tile_count && same(a.leaf_origins, b.leaf_origins, 3 * a.leaf_count) &&
+           same(a.leaf_masks, b.leaf_masks, 8 * a.leaf_count) &&
+           same(a.leaf_values, b.leaf_values, 512 * a.leaf_count) &&
+           same(a.lower_origins, b.lower_origins, 3 * a.lower_count) &&
+           same(a.lower_tiles, b.lower_tiles, 4096 * a.lower_count) &&
+           same(a.upper_origins, b.upper_origins, 3 * a.upper_count) &&
+           same(a.upper_tiles, b.upper_tiles, 32768 * a.upper_count) &&
+           same(a.root_tile_origins, b.root_tile_origins, 3 * a.root_tile_count) &&
+           same(a.root_tile_values, b.root_tile_values, a.root_tile_count);
+}
+
+template <class E>
+static bool throwsAs(int rc) {
+    try {
+        openvdb_gb300::detail::check(rc);
+    } catch (const E&) {
+        return true;
+    } catch (...) {
+        return false;
+    }
+    return false;
+}
+
+int main() {
+    namespace og = openvdb_gb300;
+    // 1. pack == fixture
+    const float center[3] = {3.5f, -7.25f, 1.0f};
+    FloatGrid::Ptr sphere = tools::createLevelSetSphere<FloatGrid>(30.0f, Vec3f(center[0], center[1], center[2]), 1.0f, 3.0f);
+    og::detail::HostGrid packed = og::detail::pack(*sphere);
+    gbls_grid_desc pd = packed.desc();
+    gbls_host_grid* fix = nullptr;
+    CHECK(gbls_host_sphere(30.0f, center, 1.0f, 3.0f, &fix) == GBLS_OK);
+    gbls_grid_desc fd{};
+    CHECK(gbls_host_grid_view(fix, &fd) == GBLS_OK);
+    CHECK(pd.leaf_count > 100 && pd.upper_count >= 2);
+    CHECK(sameDesc(pd, fd));
+    std::printf("ok %d pack equals fixture (%lld leaves)\n", ++g_n, (long long)pd.leaf_count);
+
+    // 2. unpack -> pack, into a new grid and in place with another background
+    FloatGrid::Ptr copy = FloatGrid::create(0.0f);
+    copy->setTransform(sphere->transform().copy());
+    og::detail::unpack(packed, *copy);
+    og::detail::HostGrid again = og::detail::pack(*copy);
+    gbls_grid_desc ad = again.desc();
+    CHECK(sameDesc(pd, ad));
+    CHECK(copy->activeVoxelCount() == sphere->activeVoxelCount());
+    og::detail::HostGrid shifted = packed;
+    shifted.background = 4.0f;
+    for (float& v : shifted.lower_tiles) v = v > 0.0f ? 4.0f : v < 0.0f ? -4.0f : 0.0f;
+    for (float& v : shifted.upper_tiles) v = v > 0.0f ? 4.0f : v < 0.0f ? -4.0f : 0.0f;
+    for (float& v : shifted.root_tile_values) v = v > 0.0f ? 4.0f : -4.0f;
+    FloatTree* before = &copy->tree();
+    og::detail::unpack(shifted, *copy);
+    CHECK(&copy->tree() == before && copy->background() == 4.0f);
+    og::detail::HostGrid s2 = og::detail::pack(*copy);
+    gbls_grid_desc sd = shifted.desc(), s2d = s2.desc();
+    CHECK(sameDesc(sd, s2d));
+    std::printf("ok %d unpack/pack round trip (in place, background %g)\n", ++g_n, copy->background());
+
+    // 3. status -> exception
+    CHECK(throwsAs<ValueError>(GBLS_ERR_VALUE));
+    CHECK(throwsAs<RuntimeError>(GBLS_ERR_RUNTIME));
+    CHECK(throwsAs<ValueError>(GBLS_ERR_INVALID_ARGUMENT));
+    CHECK(throwsAs<NotImplementedError>(GBLS_ERR_UNSUPPORTED));
+    CHECK(throwsAs<IndexError>(GBLS_ERR_DOMAIN));
+    CHECK(throwsAs<std::bad_alloc>(GBLS_ERR_OUT_OF_MEMORY));
+    CHECK(throwsAs<RuntimeError>(GBLS_ERR_CUDA));
+    og::detail::check(GBLS_OK);
+    og::detail::check(GBLS_ERR_INTERRUPTED);
+    std::printf("ok %d status codes map to OpenVDB exceptions\n", ++g_n);
+
+    // 4. tracker constructor checks
+    FloatGrid::Ptr fog = FloatGrid::create(0.0f);
+    fog->setGridClass(GRID_FOG_VOLUME);
+    bool threw = false;
+    try {
+        og::tools::LevelSetTracker<FloatGrid> t(*fog);
+    } catch (const RuntimeError&) {
+        threw = true;
+    }
+    CHECK(threw);
+    og::tools::LevelSetTracker<FloatGrid> tracker(*sphere);
+    CHECK(tracker.getNormCount() == 3 && tracker.getTemporalScheme() == math::TVD_RK1 &&
+          tracker.getHalfWidth() == 3.0f && tracker.leafs().leafCount() == size_t(pd.leaf_count));
+    std::printf("ok %d tracker constructor and defaults\n", ++g_n);
+
+    // 5. DiscreteField -> dense box
+    Vec3SGrid::Ptr vel = Vec3SGrid::create(Vec3s(0.25f, -0.5f, 1.0f));
+    vel->setTransform(sphere->transform().copy());
+    vel->tree().setValue(Coord(1, 2, 3), Vec3s(2.0f, 3.0f, 4.0f));
+    tools::DiscreteField<Vec3SGrid> field(*vel);
+    std::vector<float> store;
+    gbls_field_desc d = og::FieldTraits<tools::DiscreteField<Vec3SGrid>>::describe(field, *sphere, 0.0f, 1.0f, store);
+    CHECK(d.kind == GBLS_FIELD_DENSE && d.dense_values == store.data());
+    auto at = [&](int x, int y, int z, int c) {
+        const size_t i = ((size_t(x - d.dense_origin[0]) * d.dense_dims[1] + size_t(y - d.dense_origin[1])) *
+                              d.dense_dims[2] + size_t(z - d.dense_origin[2])) * 3 + c;
+        return store[i];
+    };
+    CHECK(at(1, 2, 3, 0) == 2.0f && at(1, 2, 3, 2) == 4.0f && at(0, 0, 0, 1) == -0.5f);
+    CoordBBox band;
+    CHECK(sphere->tree().evalActiveVoxelBoundingBox(band));
+    for (int a = 0; a < 3; ++a)
+        CHECK(d.dense_origin[a] <= band.min()[a] - 8 && d.dense_origin[a] + d.dense_dims[a] - 1 >= band.max()[a] + 8);
+    Vec3SGrid::Ptr vel2 = vel->deepCopy();
+    vel2->setTransform(math::Transform::createLinearTransform(0.5));
+    tools::DiscreteField<Vec3SGrid> field2(*vel2);
+    threw = false;
+    try {
+        og::FieldTraits<tools::DiscreteField<Vec3SGrid>>::describe(field2, *sphere, 0.0f, 1.0f, store);
+    } catch (const NotImplementedError&) {
+        threw = true;
+    }
+    CHECK(threw);
+    std::printf("ok %d DiscreteField dense box (%d x %d x %d)\n", ++g_n, d.dense_dims[0], d.dense_dims[1], d.dense_dims[2]);
+
+    // 6. advect: runs on a GPU, else an OpenVDB exception (no GPU here)
+    og::tools::LevelSetAdvection<FloatGrid, og::ConstantField> adv(*sphere, og::ConstantField{Vec3f(1.0f, 0.5f, 0.25f)});
+    adv.setTemporalScheme(math::TVD_RK3);
+    adv.setNormCount(1);
+    try {
+        const size_t n = adv.advect(0.0f, 1.0f);
+        std::printf("ok %d advect ran on a device: %zu substeps, %llu active voxels\n", ++g_n, n,
+                    (unsigned long long)sphere->activeVoxelCount());
+    } catch (const openvdb::Exception& e) {
+        std::printf("ok %d advect without a device: %s\n", ++g_n, e.what());
+    }
+    gbls_host_grid_free(fix);
+    return 0;
+}
