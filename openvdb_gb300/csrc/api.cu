@@ -437,6 +437,7 @@ struct gbls_handle {
     DevArray<int32_t> io_perm;   // upload: staged index of each leaf / lower / upper node
     DevArray<float> io_tiles;    // staged node tiles (upload and download)
     DevArray<int32_t> io_orig;   // download: leaf origins
+    DevArray<float> cfl_part;    // CFL reduction: per-leaf maxima
     DevStatus* st_d = nullptr;
     DevStatus* st_h = nullptr;
     DevArray<unsigned long long> u64s;
@@ -1155,8 +1156,10 @@ void enqueue_max_speed(gbls_handle& h, const gbls_field* f, float t, const unsig
     a.t0 = t;
     a.field = field_params(f, t);
     a.max_bits = &h.st_d->max_v2_bits;
+    h.cfl_part.reserve(size_t(std::max<int64_t>(h.nleaf, 1)), h.stream);
+    a.part = h.cfl_part.p;
     launch_cfl(a, h.stream);
-    ++h.stats.kernel_launches;
+    h.stats.kernel_launches += 2;
     CU(cudaGetLastError());
 }
 

@@ -296,6 +296,7 @@ struct CflArgs {
     FieldParams field;
     unsigned int* max_bits;  // float bits of max |v|^2 (values >= 0); [instances] for batches
     const unsigned long long* nleaf_dev;  // when set: the leaf count is min(nleaf, *nleaf_dev)
+    float* part;             // single level set: per-leaf maxima [nleaf] (scratch)
     const uint8_t* inst_run;
     const float* inst_t0;
     const FieldParams* inst_field;
