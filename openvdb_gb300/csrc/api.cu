@@ -2139,8 +2139,9 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
             h->inst_dt.upload(dt.data(), size_t(n), h->stream);
             h->stats.voxel_updates += upd;
             h->stats.substeps += uint64_t(nrun);
-            h->nactive = -1;
+            h->nactive = int64_t(upd);  // the RK stages' algorithmic bytes count the running instances
             advect_stages(*h, nullptr, temporal, t0, 0.0f, !forward);
+            h->nactive = -1;
             for (int i = 0; i < n; ++i) {
                 if (!run[size_t(i)]) continue;
                 t[size_t(i)] += forward ? dt[size_t(i)] : -dt[size_t(i)];
