@@ -323,6 +323,10 @@ def run_batch(args):
         "clocks": clk,
         "cpu_baseline": None,
     }
+    if args.cpu_baseline:
+        from oracle import build_oracle, port
+        build_oracle.build()
+        out["cpu_baseline"] = port.bench_batch_sample(args.cpu_seconds)
     print(json.dumps(out))
 
 

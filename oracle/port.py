@@ -188,3 +188,26 @@ def bench_reference(steps=10, warmup=3, seconds=15.0, threads=0):
             "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": nthreads,
                              "kind": "port",
                              "sample": "64-sphere workload, %d time steps in %.1f s" % (nsteps, tot)}}
+
+
+def bench_batch_sample(seconds=15.0, threads=0):
+    """CPU baseline of the batched configuration: the restatement advances the
+    seeded instances in order, one time unit each (RK3, tracker RK1, one
+    renormalisation, CFL 0.5), until `seconds` of CPU time are spent."""
+    from openvdb_gb300 import fixtures
+    specs, fields = fixtures.batch_instances(n=512, seed=7)
+    nthreads = threads if threads > 0 else (os.cpu_count() or 1)
+    updates, el, done = 0, 0.0, 0
+    for spec, field in zip(specs, fields):
+        g = PortGrid(fixtures.build_instance(spec), threads)
+        t0 = time.perf_counter()
+        g.advect(field, 0.0, 1.0, temporal=_abi.TVD_RK3, norm_count=1, cfl=0.5, tracker_temporal=_abi.TVD_RK1)
+        el += time.perf_counter() - t0
+        updates += g.updates
+        done += 1
+        if el >= seconds:
+            break
+    return {"value": updates / el, "unit": "voxel-updates/s", "cores": nthreads, "kind": "port",
+            "sample": "batched configuration: the first %d of 512 instances, one time unit each (%.1f s), "
+                      "all host threads" % (done, el)}
+
