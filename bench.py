@@ -330,6 +330,95 @@ def run_batch(args):
     print(json.dumps(out))
 
 
+ADJOINT_WORKLOAD = {"workload": "inverse problem: sphere r=160 -> torus R=160 r=48 (y axis) in 512^3, dense "
+                                "512^3 x 3 velocity (seeded separable sine modes, amplitude 0.05), 200 unit "
+                                "steps, checkpoint every 10, normalised gradient descent on the velocity",
+                    "domain": 512, "steps": 200, "checkpoint_every": 10, "spatial": "HJWENO5",
+                    "temporal": "TVD_RK3", "cfl": 0.5, "tracker": "HJWENO5/TVD_RK1", "norm_count": 1}
+
+
+def _initial_velocity(n, amp, seed):
+    """Seeded smooth velocity: per component a sum of three separable sine modes."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = np.arange(n, dtype=np.float64) * (2.0 * np.pi / n)
+    vel = np.zeros((n, n, n, 3), np.float32)
+    for c in range(3):
+        acc = np.zeros((n, n, n), np.float32)
+        for _ in range(3):
+            k = rng.integers(1, 4, 3)
+            ph = rng.uniform(0.0, 2.0 * np.pi, 3)
+            a = rng.uniform(-1.0, 1.0)
+            fx, fy, fz = (np.sin(k[i] * x + ph[i]).astype(np.float32) for i in range(3))
+            acc += np.float32(a) * fx[:, None, None] * fy[None, :, None] * fz[None, None, :]
+        vel[..., c] = amp * acc / 3.0
+    return vel
+
+
+def run_adjoint(args):
+    """Checkpointed adjoint at scale: `--steps` gradient-descent iterations, each a
+    200-step forward pass (checkpoints every 10 steps) and the reverse sweep."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from openvdb_gb300 import FAST, fixtures
+    from openvdb_gb300.adjoint import CheckpointedAdvection
+
+    torch.cuda.init()
+    torch.cuda.set_device(0)
+    n, c = 512, np.array([256.0, 256.0, 256.0])
+    template = fixtures.sphere(160.0, tuple(c))
+    vel = _initial_velocity(n, 0.05, 5)
+
+    def target(coords):
+        d = coords.astype(np.float64) - c
+        q = np.sqrt(d[:, 0] ** 2 + d[:, 2] ** 2) - 160.0
+        return np.sqrt(q * q + d[:, 1] ** 2) - 48.0
+
+    times = [float(t) for t in range(201)]
+    ck = CheckpointedAdvection(template, vel, every=10, mode=FAST, cfl=args.cfl)
+    v_dev = torch.from_numpy(vel).cuda()
+    phi0 = template.active_values().copy()
+    total = torch.cuda.mem_get_info()[1]
+    min_free = total
+    hist, t_fwd, t_adj, vu_fwd, vu_adj, subs = [], 0.0, 0.0, 0, 0, []
+    for it in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        phiT, gT = ck.forward(phi0, times)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        min_free = min(min_free, torch.cuda.mem_get_info()[0])
+        d = phiT.astype(np.float64) - target(gT.active_coords())
+        hist.append(float((d * d).sum()))
+        _, dvel, rec = ck.backward((2.0 * d).astype(np.float32))
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        min_free = min(min_free, torch.cuda.mem_get_info()[0])
+        t_fwd += t1 - t0
+        t_adj += t2 - t1
+        vu_fwd += ck.voxel_updates
+        vu_adj += ck.recorded_voxel_updates
+        subs.append(ck.substeps)
+        gmax = float(dvel.abs().max())
+        if gmax > 0:
+            v_dev -= (0.05 / gmax) * dvel
+        del dvel
+        ck.set_velocity(v_dev.cpu().numpy())
+        print("iteration %d: L %.6g, %d substeps, forward %.2f s, adjoint %.2f s"
+              % (it, hist[-1], ck.substeps, t1 - t0, t2 - t1), file=sys.stderr, flush=True)
+    cfg = dict(ADJOINT_WORKLOAD)
+    cfg.update({"iterations": args.steps, "active_voxels_initial": int(phi0.size)})
+    out = {"metric": "checkpointed adjoint: forward voxel-updates/s, (recorded forward + adjoint) / forward time",
+           "forward_value": vu_fwd / t_fwd, "unit": UNIT,
+           "adjoint_value": vu_adj / t_adj,
+           "cost_ratio": (t_fwd + t_adj) / t_fwd, "forward_s_per_iteration": t_fwd / args.steps,
+           "adjoint_s_per_iteration": t_adj / args.steps, "substeps_per_iteration": subs,
+           "loss_first": hist[0], "loss_last": hist[-1], "loss": hist,
+           "peak_device_gb": (total - min_free) / 1e9, "dtype": "f32", "data": "synthetic (seeded fixtures)",
+           "config": cfg}
+    print(json.dumps(out))
+
+
 def cpu_baseline(args):
     """The oracle's CPU restatement of the path on a bounded sample."""
     try:
@@ -371,13 +460,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="sphere64", choices=["sphere64", "batch512"],
-                    help="sphere64: the headline 64-sphere line; batch512: the batched configuration")
+    ap.add_argument("--workload", default="sphere64", choices=["sphere64", "batch512", "adjoint512"],
+                    help="sphere64: the headline 64-sphere line; batch512: the batched configuration; "
+                         "adjoint512: the checkpointed inverse problem (--steps = iterations)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     else:
-        run_batch(args) if args.workload == "batch512" else run_gb300(args)
+        {"batch512": run_batch, "adjoint512": run_adjoint}.get(args.workload, run_gb300)(args)
 
 
 if __name__ == "__main__":

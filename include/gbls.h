@@ -225,6 +225,12 @@ int gbls_adjoint_record(gbls_handle* h, int enable);
 int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int64_t* substeps);
 int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final,
                           float* dl_initial, float* dl_velocity);
+/* As gbls_adjoint_backward, but dL/dv (dense field layout) is ADDED into
+ * dl_velocity_device, device memory of the handle's device, and nothing of it
+ * is copied to the host: a checkpointed reverse sweep accumulates the
+ * velocity gradient of its segments in place.  No reference counterpart.    */
+int gbls_adjoint_backward_accumulate(gbls_handle* h, const gbls_field* field, const float* dl_final,
+                                     float* dl_initial, float* dl_velocity_device);
 
 /* ---- batches of independent level sets --------------------------------------
  * A batch handle holds n level sets (instances) that share the voxel size and

@@ -33,6 +33,8 @@ def _declare():
     P = C.POINTER(C.c_float)
     L.gbls_adjoint_backward.argtypes = [vp, vp, P, P, P]
     L.gbls_adjoint_backward.restype = C.c_int
+    L.gbls_adjoint_backward_accumulate.argtypes = [vp, vp, P, P, vp]
+    L.gbls_adjoint_backward_accumulate.restype = C.c_int
     _declared = True
 
 
@@ -50,14 +52,19 @@ class AdvectionTape:
     """Advect a level set with recording; then pull gradients back."""
 
     def __init__(self, template, velocity, origin=(0, 0, 0), background=(0.0, 0.0, 0.0),
-                 mode=PARITY, cfl=0.0):
+                 mode=PARITY, cfl=0.0, field=None):
+        """`field`: an existing DeviceField of `velocity` to share (not re-uploaded)."""
         _declare()
         self.template = template
         self.origin = tuple(origin)
         self.background = tuple(background)
         self.mode = mode
         self.cfl = cfl
-        self.set_velocity(velocity)
+        if field is not None:
+            self.velocity = velocity
+            self.field = field
+        else:
+            self.set_velocity(velocity)
         self.dev = None
 
     def set_velocity(self, velocity):
@@ -92,6 +99,81 @@ class AdvectionTape:
         _call(lib().gbls_adjoint_backward(self.dev.handle, self.field._h, dlf.ctypes.data_as(P),
                                           d0.ctypes.data_as(P), dv.ctypes.data_as(P)))
         return d0, dv
+
+    def backward_accumulate(self, dl_final, dvel):
+        """dL/dphi_final -> dL/dphi0 (host); dL/dvelocity is added into `dvel`, a
+        float32 CUDA tensor of the velocity grid's shape on the tape's device."""
+        n0, nf, ns = C.c_int64(), C.c_int64(), C.c_int64()
+        _call(lib().gbls_adjoint_sizes(self.dev.handle, C.byref(n0), C.byref(nf), C.byref(ns)))
+        dlf = np.ascontiguousarray(dl_final, np.float32).reshape(-1)
+        assert dlf.size == nf.value, (dlf.size, nf.value)
+        assert dvel.is_cuda and dvel.dtype.is_floating_point and dvel.is_contiguous()
+        d0 = np.zeros(n0.value, np.float32)
+        P = C.POINTER(C.c_float)
+        _call(lib().gbls_adjoint_backward_accumulate(self.dev.handle, self.field._h, dlf.ctypes.data_as(P),
+                                                     d0.ctypes.data_as(P), C.c_void_p(dvel.data_ptr())))
+        return d0
+
+
+class CheckpointedAdvection:
+    """Adjoint of a long advection with checkpoints: the forward pass keeps the
+    level set only at the start of every segment of `every` intervals (host
+    grids); the reverse sweep re-runs each segment with recording, from the
+    last to the first, and pulls dL/dphi back through it while dL/dv
+    accumulates on the device.  Memory: one segment's tape plus the
+    checkpoints, instead of the tape of the whole horizon."""
+
+    def __init__(self, template, velocity, every=10, origin=(0, 0, 0), background=(0.0, 0.0, 0.0),
+                 mode=PARITY, cfl=0.0):
+        _declare()
+        self.template = template
+        self.every = int(every)
+        self.origin = tuple(origin)
+        self.background = tuple(background)
+        self.mode = mode
+        self.cfl = cfl
+        self.set_velocity(velocity)
+
+    def set_velocity(self, velocity):
+        self.velocity = np.ascontiguousarray(velocity, np.float32)
+        self.field = DeviceField(Field.dense(self.velocity, self.origin, self.background))
+
+    def _tape(self, grid):
+        return AdvectionTape(grid, self.velocity, self.origin, self.background, self.mode, self.cfl, field=self.field)
+
+    def forward(self, phi0, times):
+        """Advect through times[0] -> times[-1]; returns (phi_final, final HostGrid)."""
+        self.times = list(times)
+        self.segments = []  # (start grid, its times)
+        self.substeps = 0
+        self.voxel_updates = 0
+        g = with_active_values(self.template, phi0)
+        for a in range(0, len(self.times) - 1, self.every):
+            seg = self.times[a:a + self.every + 1]
+            self.segments.append((g, seg))
+            tape = self._tape(g)
+            _, g = tape.forward(g.active_values(), seg, record=False)
+            self.substeps += sum(tape.substeps)
+            self.voxel_updates += tape.dev.stats()["voxel_updates"]
+            tape.dev.close()
+        return g.active_values().copy(), g
+
+    def backward(self, dl_final, dvel=None):
+        """dL/dphi_final -> (dL/dphi0, dL/dv as a CUDA tensor, recorded substeps)."""
+        import torch
+        if dvel is None:
+            dvel = torch.zeros(self.velocity.shape, dtype=torch.float32, device="cuda")
+        lam = np.asarray(dl_final, np.float32)
+        recorded = 0
+        self.recorded_voxel_updates = 0
+        for g, seg in reversed(self.segments):
+            tape = self._tape(g)
+            tape.forward(g.active_values(), seg, record=True)
+            recorded += sum(tape.substeps)
+            self.recorded_voxel_updates += tape.dev.stats()["voxel_updates"]
+            lam = tape.backward_accumulate(lam, dvel)
+            tape.dev.close()
+        return lam, dvel, recorded
 
 
 def make_autograd_function():

@@ -1855,8 +1855,10 @@ int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int
 // Reverse sweep over the tape: dL/dphi on the final active voxels (canonical
 // order) -> dL/dphi on the initial active voxels and, for a DENSE field,
 // dL/dvelocity on its grid.
-int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final, float* dl_initial,
-                          float* dl_velocity) {
+// Reverse sweep over the tape.  dL/dv goes to host memory (zeroed first) or,
+// with vel_on_device, is added into the caller's device array.
+static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final, float* dl_initial,
+                     float* dl_velocity, bool vel_on_device) {
     if (!h || !field || !dl_final || !dl_initial) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -1883,10 +1885,16 @@ int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* 
         lam_next.upload(lam_h.data(), lam_h.size(), st);
         const bool want_vel = dl_velocity && field->desc.kind == GBLS_FIELD_DENSE;
         size_t nvel = 0;
+        float* dv = nullptr;
         if (want_vel) {
             nvel = size_t(field->desc.dense_dims[0]) * field->desc.dense_dims[1] * field->desc.dense_dims[2] * 3;
-            dvel.reserve(nvel, st);
-            CU(cudaMemsetAsync(dvel.p, 0, nvel * 4, st));
+            if (vel_on_device) {
+                dv = dl_velocity;
+            } else {
+                dvel.reserve(nvel, st);
+                CU(cudaMemsetAsync(dvel.p, 0, nvel * 4, st));
+                dv = dvel.p;
+            }
         }
         const float dx = float(h->voxel_size);
         const float mdt = dx * 0.3f, invdx = 1.0f / dx;
@@ -1929,7 +1937,7 @@ int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* 
             ra.backward = tp.backward ? 1 : 0;
             ra.field = field_params(field, tp.t0);
             ra.field.tab = nullptr;  // direct evaluation in the adjoint
-            ra.dvel = want_vel ? dvel.p : nullptr;
+            ra.dvel = dv;
             // stage 3: phi3 = 1/3 phin + 2/3 (phi2 - dt v.grad phi2)
             ra.src = Layout{tp.am.p, tp.sm.p, tp.phi2.p};
             ra.lam_out = lamA.p; ra.lam_in = lp2.p; ra.lam_phin = lpn.p;
@@ -1955,7 +1963,7 @@ int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* 
         const auto c0 = mask_counts(*h, first.am, first.n);
         std::vector<float> out(size_t(std::max<int64_t>(first.n, 1)) * LEAF_VOX);
         lam_next.download(out.data(), size_t(first.n) * LEAF_VOX, st);
-        if (want_vel) dvel.download(dl_velocity, nvel, st);
+        if (want_vel && !vel_on_device) dvel.download(dl_velocity, nvel, st);
         h->sync();
         off = 0;
         for (int64_t l = 0; l < first.n; ++l) {
@@ -1963,6 +1971,25 @@ int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* 
             off += c0[size_t(l)];
         }
     });
+}
+
+int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final, float* dl_initial,
+                          float* dl_velocity) {
+    return adjoint_backward(h, field, dl_final, dl_initial, dl_velocity, false);
+}
+
+int gbls_adjoint_backward_accumulate(gbls_handle* h, const gbls_field* field, const float* dl_final,
+                                     float* dl_initial, float* dl_velocity_device) {
+    if (h && dl_velocity_device) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, dl_velocity_device) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+            at.device != h->device) {
+            cudaGetLastError();
+            g_last_error = "dl_velocity_device is not device memory of the handle's device";
+            return GBLS_ERR_INVALID_ARGUMENT;
+        }
+    }
+    return adjoint_backward(h, field, dl_final, dl_initial, dl_velocity_device, true);
 }
 
 int gbls_batch_create(int32_t n, const gbls_grid_desc* descs, gbls_handle** out) {

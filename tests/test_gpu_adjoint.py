@@ -176,3 +176,32 @@ def test_adjoint_inverse_problem_128():
     # dL/dphi_0 against the FP64 reference (the PARITY forward matches the FP64 topology)
     _check_case(template, vel, times, target, nprobe=8, vel_probes=False, tol_median=1e-2, tol_max=5e-2,
                 seed=77)
+
+
+@pytest.mark.gpu
+def test_checkpointed_matches_single_tape():
+    """Segments of 2 intervals with recompute give the gradients of one tape
+    over the whole horizon (dL/dv accumulated on the device; float atomics
+    make the sums order-dependent, hence a relative tolerance)."""
+    import torch
+    from openvdb_gb300 import FAST, fixtures
+    from openvdb_gb300.adjoint import AdvectionTape, CheckpointedAdvection
+    center = (16.0, 16.0, 16.0)
+    template = fixtures.sphere(9.0, center)
+    vel = smoothed_noise(32, 3.0, 0.8, seed=5)
+    times = [0.0, 0.5, 1.0, 1.5, 2.0, 2.5, 3.0]
+    phi0 = template.active_values().copy()
+    tape = AdvectionTape(template, vel, mode=FAST, cfl=0.5)
+    phiT, gT = tape.forward(phi0, times)
+    d = phiT.astype(np.float64) - _sdf_sphere(gT.active_coords(), 10.0, center)
+    g_phi, g_vel = tape.backward((2.0 * d).astype(np.float32))
+
+    ck = CheckpointedAdvection(template, vel, every=2, mode=FAST, cfl=0.5)
+    phiT2, gT2 = ck.forward(phi0, times)
+    assert np.array_equal(phiT2, phiT) and ck.substeps == sum(tape.substeps)
+    g_phi2, dvel, recorded = ck.backward((2.0 * d).astype(np.float32))
+    g_vel2 = dvel.cpu().numpy()
+    assert recorded == ck.substeps and len(ck.segments) == 3
+    assert np.abs(g_phi2 - g_phi).max() <= 1e-5 * np.abs(g_phi).max()
+    assert np.abs(g_vel2 - g_vel).max() <= 1e-5 * np.abs(g_vel).max()
+    torch.cuda.synchronize()
