@@ -256,15 +256,10 @@ __global__ void k_tape_gather(int64_t n, const int32_t* slot, const uint64_t* am
         if (am_o) am_o[size_t(l) * 8 + t] = am[size_t(s) * 8 + t];
         if (sm_o) sm_o[size_t(l) * 8 + t] = sm[size_t(s) * 8 + t];
     }
-    if (vals_o) {  // dense block -> active values packed by rank (64 threads: bit t of each word)
-        const uint64_t below = (uint64_t(1) << t) - 1;
-        int base = 0;
-        for (int w = 0; w < 8; ++w) {
-            const uint64_t m = am[size_t(s) * 8 + w];
-            if ((m >> t) & 1)
-                vals_o[size_t(l) * LEAF_VOX + base + __popcll(m & below)] = vals[size_t(s) * LEAF_VOX + (w << 6) + t];
-            base += __popcll(m);
-        }
+    if (vals_o) {
+        int cnt = 0;
+        for (int w = 0; w < 8; ++w) cnt += __popcll(am[size_t(s) * 8 + w]);
+        for (int i = t; i < cnt; i += blockDim.x) vals_o[size_t(l) * LEAF_VOX + i] = vals[size_t(s) * LEAF_VOX + i];
     }
 }
 

@@ -148,30 +148,6 @@ __global__ void k_new_leaves(int64_t n, const uint64_t* cand, const int32_t* fre
     }
 }
 
-// Value blocks of the new leaves: every voxel takes the tile value.
-__global__ void k_fill_new_leaves(int64_t n, const uint64_t* cand, const int32_t* new_slots, float* vals,
-                                  float gamma) {
-    const int64_t j = blockIdx.x;
-    if (j >= n) return;
-    const float v = (cand[j] & 1) ? -gamma : gamma;
-    float* out = vals + size_t(new_slots[j]) * LEAF_VOX;
-    for (int i = threadIdx.x; i < LEAF_VOX; i += blockDim.x) out[i] = v;
-}
-
-// Inactive entries of every value block take +-gamma by their sign bit
-// (after the background changes, tools/LevelSetTracker.h changeLevelSetBackground).
-__global__ void k_set_background(int64_t n, const int32_t* slot, const uint64_t* am, const uint64_t* sm,
-                                 float* vals, float gamma) {
-    const int64_t l = blockIdx.x;
-    if (l >= n) return;
-    const int s = slot[l];
-    const int t = threadIdx.x;  // 64 threads: bit t of every word
-    for (int k = 0; k < 8; ++k) {
-        const uint64_t a = am[size_t(s) * 8 + k], g = sm[size_t(s) * 8 + k];
-        if (!((a >> t) & 1)) vals[size_t(s) * LEAF_VOX + (k << 6) + t] = ((g >> t) & 1) ? -gamma : gamma;
-    }
-}
-
 // Merge two sorted, disjoint key lists (with their slots) into tree order.
 __global__ void k_merge(int64_t na, const uint64_t* ka, const int32_t* sa, int64_t nb,
                         const uint64_t* kb, const int32_t* sb, uint64_t* ko, int32_t* so) {
@@ -361,18 +337,30 @@ __global__ void k_count_active_inst(int64_t n, const uint64_t* keys, const int32
     if (c) atomicAdd(out + key_instance(keys[l]), c);
 }
 
-// Download: dense leaf values in tree order (inactive voxels from the sign
-// mask, which the stored blocks agree with).
+// Pack leaf values into the slot layout (upload) / unpack (download).
 __global__ void k_unpack(int64_t n, const int32_t* slot, const uint64_t* am, const uint64_t* sm,
                          const float* vals, float gamma, float* dense) {
     const int64_t l = blockIdx.x;
     if (l >= n) return;
     const int s = slot[l];
+    __shared__ int pre[9];
+    __shared__ uint64_t m[8];
+    if (threadIdx.x < 8) m[threadIdx.x] = am[size_t(s) * 8 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int w = 0; w < 8; ++w) { pre[w] = acc; acc += __popcll(m[w]); }
+        pre[8] = acc;
+    }
+    __syncthreads();
     for (int v = threadIdx.x; v < LEAF_VOX; v += blockDim.x) {
         const int w = v >> 6, b = v & 63;
         float val;
-        if ((am[size_t(s) * 8 + w] >> b) & 1) val = vals[size_t(s) * LEAF_VOX + v];
-        else val = ((sm[size_t(s) * 8 + w] >> b) & 1) ? -gamma : gamma;
+        if ((m[w] >> b) & 1) {
+            val = vals[size_t(s) * LEAF_VOX + pre[w] + __popcll(m[w] & ((1ull << b) - 1))];
+        } else {
+            val = ((sm[size_t(s) * 8 + w] >> b) & 1) ? -gamma : gamma;
+        }
         dense[l * LEAF_VOX + v] = val;
     }
 }
@@ -795,9 +783,7 @@ void dilate_topology(gbls_handle& h) {
         k_new_leaves<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(nnew, h.cand.p, h.free_slots.p, h.nfree,
                                                                    h.new_keys.p, h.new_slots.p,
                                                                    h.am[h.mc].p, h.sm[h.mc].p);
-        k_fill_new_leaves<<<unsigned(nnew), 128, 0, h.stream>>>(nnew, h.cand.p, h.new_slots.p, h.vals[h.vc].p,
-                                                                  h.gamma);
-        h.stats.kernel_launches += 2;
+        ++h.stats.kernel_launches;
         CU(cudaGetLastError());
         h.nfree -= nnew;
         const int ko = 1 - h.kc;
@@ -827,15 +813,6 @@ void dilate_topology(gbls_handle& h) {
     h.rebuild_nbr();
     k_dilate<<<blocks_for(h.nleaf * 8, 256), 256, 0, h.stream>>>(h.nleaf, h.S(), h.nbr.p, h.am[h.mc].p,
                                                                   h.dmask.p, h.K(), h.run_ptr());
-    ++h.stats.kernel_launches;
-    CU(cudaGetLastError());
-}
-
-// Rewrite the inactive entries of the current value blocks to +-h.gamma.
-void set_background(gbls_handle& h) {
-    if (h.nleaf == 0) return;
-    k_set_background<<<unsigned(h.nleaf), 64, 0, h.stream>>>(h.nleaf, h.S(), h.am[h.mc].p, h.sm[h.mc].p,
-                                                              h.vals[h.vc].p, h.gamma);
     ++h.stats.kernel_launches;
     CU(cudaGetLastError());
 }
@@ -1752,7 +1729,6 @@ int gbls_dilate(gbls_handle* h, int iterations) {
             const int m_old = h->mc;
             relayout(*h, h->dmask.p, 0, 0);  // new voxels active with their old values
             h->gamma = dx + h->gamma;         // changeLevelSetBackground(mDx + background)
-            set_background(*h);
             h->nactive = -1;
             if (h->norm_count > 0 && h->nleaf > 0) {
                 k_andnot<<<blocks_for(h->nleaf * 8, 256), 256, 0, h->stream>>>(h->nleaf, h->S(), h->dmask.p,
@@ -1788,7 +1764,6 @@ int gbls_erode(gbls_handle* h, int iterations) {
         }
         prune_compact(*h);
         h->gamma = h->gamma - float(iterations) * float(h->voxel_size);
-        set_background(*h);
         h->sync();
     });
 }

@@ -8,16 +8,13 @@
 //     origin, tree/RootNode.h:157 + math/Coord.h:157-162; then the upper-node
 //     child offset; then the lower-node child offset);
 //   * per leaf a storage slot: an active-voxel mask, a sign mask (bit set when
-//     the voxel value is negative) and a 512-float value block in voxel order
-//     (value of voxel v = vals[slot*512 + v]).  Every inactive voxel of a
-//     narrow band level set holds exactly +background or -background (signed
-//     flood fill, tools/SignedFloodFill.h:111-139; trimming,
-//     tools/LevelSetTracker.h:473-506; new leaves inherit a +-background
-//     tile, tree/InternalNode.h:2874-2876): the sign mask reproduces it, and
-//     every kernel that writes a value block writes all 512 entries so that
-//     the stored inactive values always equal +-background.  The adjoint tape
-//     stores the active values packed by rank instead (value of active voxel
-//     v = tape[l*512 + rank(v)], staged with staged_load / load_tile);
+//     the voxel value is negative) and the active values packed in voxel
+//     order at the start of a 512-float slot (OnIndex-style: value of active
+//     voxel v = vals[slot*512 + rank(v)]).  Every inactive voxel of a narrow
+//     band level set holds exactly +background or -background (signed flood
+//     fill, tools/SignedFloodFill.h:111-139; trimming,
+//     tools/LevelSetTracker.h:473-506; new leaves inherit a +-background tile,
+//     tree/InternalNode.h:2874-2876), so the sign mask reproduces it exactly;
 //   * node tables: sorted lower/upper node keys with one sign bit per child
 //     slot (the +-background tile value of every slot that holds no child) and
 //     a small sorted list of root tiles.  A key k has lower-node key k>>12 and
@@ -263,44 +260,6 @@ __device__ inline void load_tile(float* tile, const LeafStage& st, float gamma) 
         fv[3 * 3 + d] = staged_load(st, 4, a, (d << 3) | c, gamma);          // +y: (a, d, c)
         fv[4 * 3 + d] = staged_load(st, 5, a, (c << 3) | (5 + d), gamma);    // -z: (a, c, 5+d)
         fv[5 * 3 + d] = staged_load(st, 6, a, (c << 3) | d, gamma);          // +z: (a, c, d)
-    }
-#pragma unroll
-    for (int k = 0; k < 8; ++k) tile[tile_index(k, a, c)] = cv[k];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        tile[tile_index(-3 + d, a, c)] = fv[0 * 3 + d];
-        tile[tile_index(8 + d, a, c)] = fv[1 * 3 + d];
-        tile[tile_index(a, -3 + d, c)] = fv[2 * 3 + d];
-        tile[tile_index(a, 8 + d, c)] = fv[3 * 3 + d];
-        tile[tile_index(a, c, -3 + d)] = fv[4 * 3 + d];
-        tile[tile_index(a, c, 8 + d)] = fv[5 * 3 + d];
-    }
-}
-
-// Dense slots (the forward state): a slot holds all 512 values of its leaf,
-// inactive voxels at +-gamma by their sign, so a staged value is one load
-// at the voxel offset; a missing neighbour is a tile of one sign.
-__device__ __forceinline__ float staged_load_dense(const LeafStage& st, int r, int v, float gamma) {
-    const float* p = st.vp[r];
-    if (p) return __ldg(p + v);
-    return st.sm[r][0] ? -gamma : gamma;  // tile: sign words all ones or all zeros
-}
-
-// load_tile over dense slots (same tile, same thread mapping).
-__device__ inline void load_tile_dense(float* tile, const LeafStage& st, float gamma) {
-    const int t = threadIdx.x;
-    const int a = t >> 3, c = t & 7;
-    float cv[8], fv[18];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) cv[k] = staged_load_dense(st, 0, (k << 6) | t, gamma);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        fv[0 * 3 + d] = staged_load_dense(st, 1, ((5 + d) << 6) | t, gamma);          // -x: (5+d, a, c)
-        fv[1 * 3 + d] = staged_load_dense(st, 2, (d << 6) | t, gamma);                // +x: (d, a, c)
-        fv[2 * 3 + d] = staged_load_dense(st, 3, (a << 6) | ((5 + d) << 3) | c, gamma);  // -y: (a, 5+d, c)
-        fv[3 * 3 + d] = staged_load_dense(st, 4, (a << 6) | (d << 3) | c, gamma);        // +y: (a, d, c)
-        fv[4 * 3 + d] = staged_load_dense(st, 5, (a << 6) | (c << 3) | (5 + d), gamma);  // -z: (a, c, 5+d)
-        fv[5 * 3 + d] = staged_load_dense(st, 6, (a << 6) | (c << 3) | d, gamma);        // +z: (a, c, d)
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) tile[tile_index(k, a, c)] = cv[k];

@@ -20,18 +20,21 @@ k_pack_leaves(int64_t n, const int32_t* perm, const uint64_t* in_masks, const fl
     __shared__ uint32_t neg[8][2];
     if (t < 8) m[t] = in_masks[src * 8 + t];
     __syncthreads();
+    const uint64_t below = (uint64_t(1) << t) - 1;
     const float* v = in_vals + src * LEAF_VOX;
     float* out = vals + l * LEAF_VOX;
+    int base = 0;
     bool bad = false;
 #pragma unroll
     for (int w = 0; w < 8; ++w) {
         const uint64_t mw = m[w];
         const float x = v[w * 64 + t];
-        out[w * 64 + t] = x;  // dense block: every voxel at its offset
-        if (!((mw >> t) & 1)) bad |= !(x == gamma || x == -gamma);
+        if ((mw >> t) & 1) out[base + __popcll(mw & below)] = x;
+        else bad |= !(x == gamma || x == -gamma);
         // the sign mask records x < 0 for every voxel, active or not
         const uint32_t b = __ballot_sync(0xffffffffu, x < 0.0f);
         if ((t & 31) == 0) neg[w][t >> 5] = b;
+        base += __popcll(mw);
     }
     if (bad) atomicOr(err, IO_ERR_LEAF_VALUE);
     __syncthreads();

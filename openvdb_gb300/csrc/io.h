@@ -15,7 +15,7 @@ constexpr unsigned long long IO_ERR_LOWER_TILE = 2;   // lower-node tile other t
 constexpr unsigned long long IO_ERR_UPPER_TILE = 4;   // upper-node tile other than +-background
 
 // Leaf l (tree order) takes the dense values and mask of staged leaf
-// perm[l]: writes am/sm and the 512-value block of slot l.  Sets IO_ERR_LEAF_VALUE in *err.
+// perm[l]: writes am/sm/vals of slot l.  Sets IO_ERR_LEAF_VALUE in *err.
 void launch_pack_leaves(int64_t n, const int32_t* perm, const uint64_t* in_masks, const float* in_vals,
                         float gamma, uint64_t* am, uint64_t* sm, float* vals, unsigned long long* err,
                         cudaStream_t s);

@@ -71,7 +71,12 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkAr
     if (a.inst_run) {
         const uint32_t inst = key_instance(key);
         if (!a.inst_run[inst]) {
-            if (a.copy_done) copy_block(a.out, a.src.vals, s);
+            if (a.copy_done) {
+                int n = 0;
+                for (int w = 0; w < 8; ++w) n += __popcll(a.src.amask[size_t(s) * 8 + w]);
+                for (int i = threadIdx.x; i < n; i += STENCIL_THREADS)
+                    a.out[size_t(s) * LEAF_VOX + i] = a.src.vals[size_t(s) * LEAF_VOX + i];
+            }
             return;
         }
         dt = a.inst_dt[inst];
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkAr
         sf = a.field;
     }
     stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
-    load_tile_dense(tile, st, a.gamma);
+    load_tile(tile, st, a.gamma);
     const int n = build_list(list, st.am[0]);
     __syncthreads();
     int ox, oy, oz;
@@ -141,13 +146,12 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkAr
         const float2 c = make_float2(tile[c0], tile[c1]);
         float2 r = fma2(dot, make_float2(-dt2.x, -dt2.y), c);
         if (a.has_phi) {
-            const float2 ph = make_float2(a.phin[size_t(s) * LEAF_VOX + v0], a.phin[size_t(s) * LEAF_VOX + v1]);
+            const float2 ph = make_float2(a.phin[size_t(s) * LEAF_VOX + i0], a.phin[size_t(s) * LEAF_VOX + i1]);
             r = fma2(f2(a.alpha), ph, mul2(f2(a.beta), r));
         }
-        a.out[size_t(s) * LEAF_VOX + v0] = r.x;
-        if (i1 != i0) a.out[size_t(s) * LEAF_VOX + v1] = r.y;
+        a.out[size_t(s) * LEAF_VOX + i0] = r.x;
+        if (i1 != i0) a.out[size_t(s) * LEAF_VOX + i1] = r.y;
     }
-    write_inactive(a.out, s, st.am[0], tile);
 }
 
 // FAST renormalisation stage (RK1 form, no convex combination) on voxel
@@ -175,7 +179,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel_x2(const Nor
         fin[t] = 0;
         fsg[t] = st.sm[0][t] & ~um[t];
     }
-    load_tile_dense(tile, st, a.gamma);
+    load_tile(tile, st, a.gamma);
     __syncthreads();
     const int n = build_list(list, um);
     __syncthreads();
@@ -248,7 +252,14 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel_x2(const Nor
         fsg[t] |= uint64_t(half[1][0][t]) | (uint64_t(half[1][1][t]) << 32);
     }
     __syncthreads();
-    const int base = write_result_block(a.out_vals, s, fin, fsg, res, g);
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    int base = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t w = fin[k];
+        if ((w >> t) & 1) a.out_vals[size_t(s) * LEAF_VOX + base + __popcll(w & low)] = res[(k << 6) | t];
+        base += __popcll(w);
+    }
     if (t < 8) {
         a.out_amask[size_t(s) * 8 + t] = fin[t];
         a.out_smask[size_t(s) * 8 + t] = fsg[t];

@@ -320,36 +320,6 @@ __device__ __forceinline__ int build_list(uint16_t* list, const uint64_t* m) {
     return base;
 }
 
-// Copy a whole value block (a finished batch instance keeps its values).
-__device__ __forceinline__ void copy_block(float* out, const float* in, int s) {
-    for (int v = threadIdx.x; v < LEAF_VOX; v += blockDim.x)
-        out[size_t(s) * LEAF_VOX + v] = in[size_t(s) * LEAF_VOX + v];
-}
-
-// Inactive entries of a result block: the +-background of the staged centre
-// (thread t writes bit t of each word; STENCIL_THREADS == 64).
-__device__ __forceinline__ void write_inactive(float* out, int s, const uint64_t* am, const float* tile) {
-    const int t = threadIdx.x;
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (!((am[k] >> t) & 1)) out[size_t(s) * LEAF_VOX + (k << 6) + t] = tile[tile_index(k, t >> 3, t & 7)];
-}
-
-// A renormalised block: the result at the voxels of fin, +-g by fsg at the
-// others (thread t writes bit t of each word).  Returns popcount(fin).
-__device__ __forceinline__ int write_result_block(float* out, int s, const uint64_t* fin, const uint64_t* fsg,
-                                                  const float* res, float g) {
-    const int t = threadIdx.x;
-    int base = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int v = (k << 6) | t;
-        out[size_t(s) * LEAF_VOX + v] = ((fin[k] >> t) & 1) ? res[v] : (((fsg[k] >> t) & 1) ? -g : g);
-        base += __popcll(fin[k]);
-    }
-    return base;
-}
-
 // One TVD-RK stage of LevelSetAdvection::Advect::euler<N,D>
 // (tools/LevelSetAdvect.h:543-572): for every active voxel
 //   a = phi_c - dt * (v . GradientBiased<HJWENO5>(phi))
@@ -369,7 +339,12 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
     if (a.inst_run) {
         const uint32_t inst = key_instance(key);
         if (!a.inst_run[inst]) {
-            if (a.copy_done) copy_block(a.out, a.src.vals, s);  // keep a finished instance's values
+            if (a.copy_done) {  // keep a finished instance's values in the result buffer
+                int n = 0;
+                for (int w = 0; w < 8; ++w) n += __popcll(a.src.amask[size_t(s) * 8 + w]);
+                for (int i = threadIdx.x; i < n; i += STENCIL_THREADS)
+                    a.out[size_t(s) * LEAF_VOX + i] = a.src.vals[size_t(s) * LEAF_VOX + i];
+            }
             return;
         }
         dt = a.inst_dt[inst];
@@ -379,7 +354,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
         sf = a.field;
     }
     stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
-    load_tile_dense(tile, st, a.gamma);
+    load_tile(tile, st, a.gamma);
     const int n = build_list(list, st.am[0]);
     __syncthreads();
     int ox, oy, oz;
@@ -425,12 +400,11 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
         const float r = A::sub(c, A::mul(dt, dot));
         float o = r;
         if (a.has_phi) {
-            const float p = a.phin[size_t(s) * LEAF_VOX + v];
+            const float p = a.phin[size_t(s) * LEAF_VOX + i];
             o = A::add(A::mul(a.alpha, p), A::mul(a.beta, r));
         }
-        a.out[size_t(s) * LEAF_VOX + v] = o;
+        a.out[size_t(s) * LEAF_VOX + i] = o;
     }
-    write_inactive(a.out, s, st.am[0], tile);
 }
 
 // One stage of LevelSetTracker::Normalizer::euler<N,D>
@@ -462,7 +436,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         fsg[t] = st.sm[0][t] & ~um[t];
         if (a.has_phi) phm[t] = a.phi.amask[size_t(s) * 8 + t];
     }
-    load_tile_dense(tile, st, a.gamma);
+    load_tile(tile, st, a.gamma);
     __syncthreads();
     const int n = build_list(list, um);
     __syncthreads();
@@ -494,7 +468,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
                 const int w = v >> 6, b = v & 63;
                 float p;
                 if ((phm[w] >> b) & 1) {
-                    p = a.phi.vals[size_t(s) * LEAF_VOX + v];
+                    int rank = __popcll(phm[w] & (bit - 1));
+                    for (int k = 0; k < w; ++k) rank += __popcll(phm[k]);
+                    p = a.phi.vals[size_t(s) * LEAF_VOX + rank];
                 } else {
                     p = ((a.phi.smask[size_t(s) * 8 + w] >> b) & 1) ? -g : g;
                 }
@@ -531,7 +507,15 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
         fsg[t] |= uint64_t(half[1][0][t]) | (uint64_t(half[1][1][t]) << 32);
     }
     __syncthreads();
-    const int base = write_result_block(a.out_vals, s, fin, fsg, res, g);
+    // packed output in the layout of fin: thread t writes bit t of each word
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    int base = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t w = fin[k];
+        if ((w >> t) & 1) a.out_vals[size_t(s) * LEAF_VOX + base + __popcll(w & low)] = res[(k << 6) | t];
+        base += __popcll(w);
+    }
     if (t < 8) {
         a.out_amask[size_t(s) * 8 + t] = fin[t];
         a.out_smask[size_t(s) * 8 + t] = fsg[t];
