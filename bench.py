@@ -184,9 +184,14 @@ def run_gb300(args):
     achieved = rk_gbs if dominant == "rk_stage" else norm_gbs
     launches = st["rk_launches"] if dominant == "rk_stage" else st["norm_launches"]
     traffic = None
-    tp = os.path.join(HERE, "profiles", "traffic.json")
+    # DRAM bytes per launch of the dominant kernel from one ncu capture
+    # (profiles/traffic.txt: "<kernel>_<mode> <bytes>" per line)
+    tp = os.path.join(HERE, "profiles", "traffic.txt")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(dominant + "_" + args.mode)
+        for line in open(tp):
+            f = line.split()
+            if len(f) == 2 and f[0] == dominant + "_" + args.mode:
+                traffic = int(f[1])
 
     # end to end through the host-facing API: upload, advect one time unit, download
     e2e = None
