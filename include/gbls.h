@@ -205,6 +205,19 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
 
 
 
+/* ---- level-set morphing ------------------------------------------------------
+ * Replaces tools::LevelSetMorphing<FloatGrid>::advect (tools/LevelSetMorph.h:
+ * 243-262): h moves towards the level set `target` with speed
+ * phi - target (times the smooth-step of the alpha mask's value mapped from
+ * [mask_min, mask_max] to [0, 1], or one minus it when invert_mask), CFL
+ * substeps from t0 while t0 < t1, each followed by the tracker pass with h's
+ * tracker state.  `target` and `alpha_mask` (may be NULL) are level sets
+ * created with gbls_create on the same device with the same transform.
+ * GBLS_ERR_VALUE for mask_min >= mask_max with a mask (setMaskRange).       */
+int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial_scheme,
+               int temporal_scheme, float t0, float t1, float mask_min, float mask_max, int invert_mask,
+               uint64_t* substeps);
+
 /* ---- adjoint ---------------------------------------------------------------
  * No counterpart in the reference (it has no derivatives).  While recording
  * is enabled, every CFL substep of gbls_advect (TVD_RK3 advection, TVD_RK1

@@ -19,6 +19,7 @@
 #include "adjoint.h"
 #include "gbls_internal.cuh"
 #include "io.h"
+#include "morph_ops.cuh"
 #include "stencil.h"
 #include "stencil_ops.cuh"
 #include "topology.cuh"
@@ -438,6 +439,7 @@ struct gbls_handle {
     DevArray<float> io_tiles;    // staged node tiles (upload and download)
     DevArray<int32_t> io_orig;   // download: leaf origins
     DevArray<float> cfl_part;    // CFL reduction: per-leaf maxima
+    DevArray<float> morph_speed; // LevelSetMorphing: speed per active voxel, packed like the values
     DevStatus* st_d = nullptr;
     DevStatus* st_h = nullptr;
     DevArray<unsigned long long> u64s;
@@ -1250,6 +1252,92 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
         stage(c0, a0, a0, 1.0f / 3.0f, 1, "Advecting level set using TVD_RK3 (step 3 of 3)");
         h.vc = a0;
     }
+}
+
+// ---- LevelSetMorphing (tools/LevelSetMorph.h) -------------------------------
+LookupGrid lookup_grid(gbls_handle& g) {
+    LookupGrid L{};
+    L.keys = g.K();
+    L.slot = g.S();
+    L.nleaf = g.nleaf;
+    L.layout = g.layout(g.mc, g.vc);
+    L.nodes = g.nodes();
+    L.gamma = g.gamma;
+    return L;
+}
+
+// The RK stages of one morphing substep (Morph::advect, LevelSetMorph.h:
+// 479-510): euler01 / euler12 / euler34 / euler13 over the same buffers as
+// the advection stages.
+void morph_stages(gbls_handle& h, int temporal, float dt) {
+    MorphArgs base{};
+    base.nleaf = h.nleaf;
+    base.slot = h.S();
+    base.nbr = h.nbr.p;
+    base.dt = dt;
+    base.gamma = h.gamma;
+    const double inv = 1.0 / h.voxel_size;  // map.getInvScaleSqr()[0]
+    base.invdxdx = float(inv * inv);
+    base.speed = h.morph_speed.p;
+    const int a0 = h.vc, b0 = (h.vc + 1) % 3, c0 = (h.vc + 2) % 3;
+    auto stage = [&](int src, int phin, int out, float alpha, int has_phi) {
+        MorphArgs a = base;
+        a.src = h.layout(h.mc, src);
+        a.phin = h.vals[phin].p;
+        a.out = h.vals[out].p;
+        a.alpha = alpha;
+        a.beta = 1.0f - alpha;
+        a.has_phi = has_phi;
+        start_intr(h, "Morphing level set");
+        if (h.mode == GBLS_MODE_PARITY) launch_morph_stage_parity(a, h.stream);
+        else launch_morph_stage_fast(a, h.stream);
+        CU(cudaGetLastError());
+        ++h.stats.kernel_launches;
+        end_intr(h);
+    };
+    if (temporal == GBLS_TVD_RK1) {
+        stage(a0, a0, b0, 0.0f, 0);
+        h.vc = b0;
+    } else if (temporal == GBLS_TVD_RK2) {
+        stage(a0, a0, b0, 0.0f, 0);
+        stage(b0, a0, a0, 1.0f / 2.0f, 1);
+        h.vc = a0;
+    } else {
+        stage(a0, a0, b0, 0.0f, 0);
+        stage(b0, a0, c0, 3.0f / 4.0f, 1);
+        stage(c0, a0, a0, 1.0f / 3.0f, 1);
+        h.vc = a0;
+    }
+}
+
+// Morph::sampleSpeed (LevelSetMorph.h:521-546): speed per active voxel and
+// the maximum of 1e-6 and every |s|.
+float morph_sample_speed(gbls_handle& h, gbls_handle& target, gbls_handle* mask, float mask_min, float inv_norm,
+                         int invert) {
+    h.cfl_part.reserve(size_t(std::max<int64_t>(h.nleaf, 1)), h.stream);
+    h.morph_speed.reserve(size_t(h.slot_cap) * LEAF_VOX, h.stream);
+    MorphSpeedArgs a{};
+    a.nleaf = h.nleaf;
+    a.keys = h.K();
+    a.slot = h.S();
+    a.src = h.layout(h.mc, h.vc);
+    a.speed = h.morph_speed.p;
+    a.part = h.cfl_part.p;
+    a.target = lookup_grid(target);
+    a.has_mask = mask ? 1 : 0;
+    if (mask) a.mask = lookup_grid(*mask);
+    a.mask_min = mask_min;
+    a.mask_inv_norm = inv_norm;
+    a.invert = invert;
+    h.clear_status();
+    if (h.mode == GBLS_MODE_PARITY) launch_morph_speed_parity(a, &h.st_d->max_v2_bits, h.stream);
+    else launch_morph_speed_fast(a, &h.st_d->max_v2_bits, h.stream);
+    CU(cudaGetLastError());
+    h.stats.kernel_launches += 2;
+    h.read_status();
+    float m;
+    std::memcpy(&m, &h.st_h->max_v2_bits, 4);
+    return (1e-6f < m) ? m : 1e-6f;  // mMaxAbsS starts at mMinAbsS = 1e-6
 }
 
 // ---- upload / download ------------------------------------------------------
@@ -2343,6 +2431,64 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                 next_v2 = status_max_speed(*h);
                 have_next = true;
             }
+        }
+        h->sync();
+    });
+    if (substeps) *substeps = count;
+    if (rc == GBLS_OK && interrupted) {
+        g_last_error = "interrupted";
+        return GBLS_ERR_INTERRUPTED;
+    }
+    return rc;
+}
+
+// LevelSetMorphing::advect (tools/LevelSetMorph.h:243-262, Morph::advect
+// :479-510): CFL substeps from t0 towards t1 (forward time only), each with
+// the speed sampled once, the RK stages and a tracker pass.
+int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial, int temporal, float t0,
+               float t1, float mask_min, float mask_max, int invert_mask, uint64_t* substeps) {
+    if (substeps) *substeps = 0;
+    if (!h || !target) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    uint64_t count = 0;
+    bool interrupted = false;
+    const int rc = guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(spatial, temporal);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        if (h->ninst > 1 || target->ninst > 1 || (alpha_mask && alpha_mask->ninst > 1))
+            fail(GBLS_ERR_UNSUPPORTED, "morphing works on single level sets, not batches");
+        if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "the adjoint records advection only");
+        auto same_device_and_map = [&](const gbls_handle* o) {
+            return o->device == h->device && o->voxel_size == h->voxel_size && o->map_type == h->map_type &&
+                   o->translation[0] == h->translation[0] && o->translation[1] == h->translation[1] &&
+                   o->translation[2] == h->translation[2];
+        };
+        if (!same_device_and_map(target) || (alpha_mask && !same_device_and_map(alpha_mask)))
+            fail(GBLS_ERR_UNSUPPORTED, "target and alpha mask must share the level set's device and transform "
+                                       "(the trilinear sampling of non-aligned grids has no device form)");
+        if (alpha_mask && !(mask_min < mask_max)) fail(GBLS_ERR_VALUE, "Invalid mask range (expects min < max)");
+        const float delta = mask_max - mask_min;  // setMaskRange: mDeltaMask = max - min
+        const float inv_norm = 1.0f / delta;
+        const float C = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) / std::sqrt(3.0f);
+        const float dx = float(h->voxel_size);
+        target->sync();
+        if (alpha_mask) alpha_mask->sync();
+        while (t0 < t1) {
+            if (!check_intr(*h)) { interrupted = true; break; }
+            if (h->nleaf == 0) break;  // sampleSpeed returns 0 for an empty grid
+            const float max_s = morph_sample_speed(*h, *target, alpha_mask, mask_min, inv_norm, invert_mask ? 1 : 0);
+            if (!(std::fabs(1e-6f - max_s) > 1e-8f)) break;  // isApproxEqual(mMinAbsS, mMaxAbsS): dt = 0
+            const float span = std::fabs(t1 - t0);
+            const float lim = C * dx / max_s;
+            const float dt = (lim < span) ? lim : span;  // math::Min
+            if (dt == 0.0f) break;
+            if (h->nactive < 0) h->nactive = active_count(*h);
+            h->stats.voxel_updates += uint64_t(h->nactive);
+            ++h->stats.substeps;
+            morph_stages(*h, temporal, dt);
+            t0 += dt;
+            ++count;
+            track(*h);
         }
         h->sync();
     });

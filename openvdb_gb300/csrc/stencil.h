@@ -15,4 +15,11 @@ void launch_rk_fast(const RkArgs& a, cudaStream_t s);
 void launch_norm_fast(const NormArgs& a, cudaStream_t s);
 // Max |v|^2 over active voxels (exact in both modes).
 void launch_cfl(const CflArgs& a, cudaStream_t s);
+// LevelSetMorphing: speed sampling (+ max |s| into *max_bits) and RK stages.
+struct MorphSpeedArgs;
+struct MorphArgs;
+void launch_morph_speed_parity(const MorphSpeedArgs& a, unsigned int* max_bits, cudaStream_t s);
+void launch_morph_stage_parity(const MorphArgs& a, cudaStream_t s);
+void launch_morph_speed_fast(const MorphSpeedArgs& a, unsigned int* max_bits, cudaStream_t s);
+void launch_morph_stage_fast(const MorphArgs& a, cudaStream_t s);
 }  // namespace gbls

@@ -1,5 +1,6 @@
 // FP32 stencil kernels and the CFL reduction.
 #include "stencil.h"
+#include "morph_ops.cuh"
 #include "stencil_ops.cuh"
 #include "stencil_fast2.cuh"
 
@@ -109,6 +110,31 @@ __global__ void __launch_bounds__(1024) cfl_reduce_kernel(const float* part, int
         for (int i = 1; i < 32; ++i) x = ref_max(x, wm[i]);
         atomicMax(max_bits, __float_as_uint(x));
     }
+}
+
+__global__ void __launch_bounds__(1024) morph_reduce_kernel(const float* part, int64_t n, unsigned int* max_bits) {
+    float m = 0.0f;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = ref_max(m, part[i]);
+    for (int o = 16; o > 0; o >>= 1) m = ref_max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float wm[32];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float x = wm[0];
+        for (int i = 1; i < 32; ++i) x = ref_max(x, wm[i]);
+        atomicMax(max_bits, __float_as_uint(x));
+    }
+}
+
+void launch_morph_speed_fast(const MorphSpeedArgs& a, unsigned int* max_bits, cudaStream_t s) {
+    if (a.nleaf <= 0) return;
+    morph_speed_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    morph_reduce_kernel<<<1, 1024, 0, s>>>(a.part, a.nleaf, max_bits);
+}
+
+void launch_morph_stage_fast(const MorphArgs& a, cudaStream_t s) {
+    if (a.nleaf <= 0) return;
+    morph_stage_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 void launch_cfl(const CflArgs& a, cudaStream_t s) {

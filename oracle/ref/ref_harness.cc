@@ -11,6 +11,7 @@
 #include <openvdb/openvdb.h>
 #include <openvdb/tools/Composite.h>
 #include <openvdb/tools/LevelSetAdvect.h>
+#include <openvdb/tools/LevelSetMorph.h>
 #include <openvdb/tools/LevelSetSphere.h>
 #include <openvdb/tools/LevelSetTracker.h>
 #include <openvdb/tools/VelocityFields.h>
@@ -319,6 +320,32 @@ int vdbref_from_desc(const gbls_grid_desc* d, void** out) {
 }
 
 // tools::LevelSetAdvection<FloatGrid, FieldT>::advect with the given schemes.
+// tools::LevelSetMorphing<FloatGrid>::advect towards `target`, with an
+// optional alpha mask (mask may be null).
+int vdbref_morph(void* g, void* target, void* mask, int spatial, int temporal, int tspatial, int ttemporal,
+                 int normCount, float t0, float t1, float minMask, float maxMask, int invert, uint64_t* count) {
+    try {
+        FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+        const FloatGrid& tgt = *static_cast<RefGrid*>(target)->grid;
+        tools::LevelSetMorphing<FloatGrid> morph(grid, tgt);
+        if (mask) {
+            morph.setAlphaMask(*static_cast<RefGrid*>(mask)->grid);
+            morph.setMaskRange(minMask, maxMask);
+            morph.invertMask(invert != 0);
+        }
+        morph.setSpatialScheme(math::BiasedGradientScheme(spatial));
+        morph.setTemporalScheme(math::TemporalIntegrationScheme(temporal));
+        morph.setTrackerSpatialScheme(math::BiasedGradientScheme(tspatial));
+        morph.setTrackerTemporalScheme(math::TemporalIntegrationScheme(ttemporal));
+        morph.setNormCount(normCount);
+        const size_t n = morph.advect(t0, t1);
+        if (count) *count = n;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
 int vdbref_advect(void* g, const gbls_field_desc* f, int spatial, int temporal, int tspatial,
                   int ttemporal, int normCount, float t0, float t1, uint64_t* count) {
     try {

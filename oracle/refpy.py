@@ -41,6 +41,8 @@ def lib():
             [C.c_float, C.c_float, C.POINTER(C.c_uint64)]
         L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
         L.vdbref_set_threads.argtypes = [C.c_int]
+        L.vdbref_morph.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_float] * 4 + [C.c_int,
+                                                                                    C.POINTER(C.c_uint64)]
         _lib = L
     return _lib
 
@@ -112,6 +114,16 @@ class RefGrid:
         fd = field.desc() if hasattr(field, "desc") else field
         _check(lib().vdbref_advect(self.h, C.byref(fd), spatial, temporal, tracker_spatial,
                                    tracker_temporal, norm_count, t0, t1, C.byref(n)))
+        return n.value
+
+    def morph(self, target, t0, t1, mask=None, mask_range=(0.0, 1.0), invert=False,
+              spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK2, tracker_spatial=_abi.HJWENO5_BIAS,
+              tracker_temporal=_abi.TVD_RK1, norm_count=3):
+        """tools::LevelSetMorphing::advect(t0, t1) towards the RefGrid `target`."""
+        n = C.c_uint64()
+        _check(lib().vdbref_morph(self.h, target.h, mask.h if mask is not None else None, spatial, temporal,
+                                  tracker_spatial, tracker_temporal, norm_count, t0, t1, mask_range[0],
+                                  mask_range[1], 1 if invert else 0, C.byref(n)))
         return n.value
 
     def tracker_op(self, op, arg=0, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1,

@@ -130,7 +130,36 @@ def make_fixture(spec):
     if spec[0] == "union8":
         c, r = union8()
         return fixtures.union_of_spheres(c, r)
+    if spec[0] == "torus":
+        return fixtures.torus(spec[1], spec[2], spec[3])
     raise ValueError(spec[0])
+
+
+# LevelSetMorphing (tools/LevelSetMorph.h): source fixture morphed towards a
+# target fixture, optionally with an alpha mask (a level set), through the
+# listed advect(t0, t1) calls.  Fixture specs as for make_fixture, plus
+# ("torus", R, r, center).
+MORPH_CASES = {
+    "morph_sphere_to_sphere_rk2": dict(
+        source=("sphere", 12.0, (0.0, 0.0, 0.0), 1.0, 3.0),
+        target=("sphere", 15.0, (2.0, 1.0, -1.0), 1.0, 3.0),
+        schemes=(HJ, RK2, HJ, RK1, 3),
+        ops=[("morph", 0.0, 1.0), ("morph", 1.0, 2.0), ("morph", 2.0, 4.0)],
+    ),
+    "morph_sphere_to_torus_rk3": dict(
+        source=("sphere", 16.0, (0.0, 0.0, 0.0), 1.0, 3.0),
+        target=("torus", 14.0, 5.0, (0.5, -0.5, 0.0)),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("morph", 0.0, 1.0), ("morph", 1.0, 2.0), ("morph", 2.0, 3.0)],
+    ),
+    "morph_masked_rk1": dict(
+        source=("sphere", 14.0, (0.0, 0.0, 0.0), 1.0, 3.0),
+        target=("sphere", 10.0, (3.0, 0.0, 0.0), 1.0, 3.0),
+        mask=("sphere", 9.0, (8.0, 4.0, 0.0), 1.0, 3.0),
+        schemes=(HJ, RK1, HJ, RK1, 2),
+        ops=[("morph", 0.0, 1.0, (-2.0, 2.0), False), ("morph", 1.0, 2.0, (-1.0, 3.0), True)],
+    ),
+}
 
 
 # Batched advection: each instance must equal its own reference advect call.

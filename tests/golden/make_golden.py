@@ -1,7 +1,7 @@
 """Generate tests/golden/parity_cases.json from the reference implementation.
 
 Runs every case of tests/golden/cases.py through the UNMODIFIED reference
-(tools::LevelSetAdvection / tools::LevelSetTracker compiled from the
+(tools::LevelSetAdvection / tools::LevelSetTracker / tools::LevelSetMorphing compiled from the
 reference checkout into oracle/_ref/libvdbref.so by oracle/ref/build_ref.py)
 and records the digest of the grid after each operation.  The input level
 sets come from openvdb_gb300.fixtures; for spheres the generator first
@@ -19,7 +19,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from cases import BATCH, CASES, make_batch, make_field, make_fixture  # noqa: E402
+from cases import BATCH, CASES, MORPH_CASES, make_batch, make_field, make_fixture  # noqa: E402
 from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
 from oracle import refpy  # noqa: E402
 
@@ -79,8 +79,36 @@ def main():
         print("%-32s ops=%d final leaves=%s active=%s" % (name, len(a) - 1, last.get("summary", {}).get("leaves"),
                                                           last.get("summary", {}).get("active")))
     result["__batch__"] = run_batch()
+    morph = {}
+    for name, case in MORPH_CASES.items():
+        a = run_morph(name, case, 1)
+        b = run_morph(name, case, nthreads)
+        assert a == b, "reference result depends on the thread count: " + name
+        morph[name] = a
+        print("%-32s ops=%d final active=%s" % (name, len(a) - 1, a[-1]["summary"]["active"]))
+    result["__morph__"] = morph
     with open(os.path.join(HERE, "parity_cases.json"), "w") as f:
         json.dump(result, f, indent=1, sort_keys=True)
+
+
+def run_morph(name, case, threads):
+    """A LevelSetMorphing case: digests after every advect(t0, t1) call."""
+    refpy.set_threads(threads)
+    src, tgt = make_fixture(case["source"]), make_fixture(case["target"])
+    g = refpy.RefGrid.from_host(src)
+    target = refpy.RefGrid.from_host(tgt)
+    mask = refpy.RefGrid.from_host(make_fixture(case["mask"])) if "mask" in case else None
+    sp, tp, tsp, ttp, nc = case["schemes"]
+    out = [{"op": "input", "digest": digest(src), "target": digest(tgt), "summary": summary(src)}]
+    for op in case["ops"]:
+        kw = {}
+        if len(op) > 3:
+            kw = dict(mask=mask, mask_range=op[3], invert=op[4])
+        n = g.morph(target, op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp, tracker_temporal=ttp,
+                    norm_count=nc, **kw)
+        h = g.to_host()
+        out.append({"op": list(op), "count": n, "digest": digest(h), "summary": summary(h)})
+    return out
 
 
 def run_batch():
