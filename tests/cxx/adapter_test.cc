@@ -17,6 +17,7 @@
 #include <cstring>
 
 #include "openvdb_gb300/LevelSetAdvect.h"
+#include "openvdb_gb300/LevelSetMorph.h"
 
 using namespace openvdb;
 
@@ -163,6 +164,31 @@ int main() {
                     (unsigned long long)sphere->activeVoxelCount());
     } catch (const openvdb::Exception& e) {
         std::printf("ok %d advect without a device: %s\n", ++g_n, e.what());
+    }
+    // 7. morphing: same defaults and range checks as the reference; runs on a
+    //    GPU, else an OpenVDB exception
+    FloatGrid::Ptr src2 = tools::createLevelSetSphere<FloatGrid>(12.0f, Vec3f(0.0f), 1.0f, 3.0f);
+    FloatGrid::Ptr tgt2 = tools::createLevelSetSphere<FloatGrid>(15.0f, Vec3f(2.0f, 1.0f, -1.0f), 1.0f, 3.0f);
+    og::tools::LevelSetMorphing<FloatGrid> morph(*src2, *tgt2);
+    FloatGrid::Ptr src2ref = src2->deepCopy();
+    tools::LevelSetMorphing<FloatGrid> refMorph(*src2ref, *tgt2);
+    CHECK(morph.getTemporalScheme() == refMorph.getTemporalScheme() && morph.getNormCount() == refMorph.getNormCount() &&
+          morph.minMask() == refMorph.minMask() && morph.maxMask() == refMorph.maxMask());
+    threw = false;
+    try {
+        morph.setMaskRange(1.0f, 1.0f);
+    } catch (const ValueError&) {
+        threw = true;
+    }
+    CHECK(threw);
+    morph.setMaskRange(-2.0f, 2.0f);
+    refMorph.setMaskRange(-2.0f, 2.0f);
+    CHECK(morph.minMask() == refMorph.minMask() && morph.maxMask() == refMorph.maxMask());
+    try {
+        const size_t n = morph.advect(0.0f, 1.0f);
+        std::printf("ok %d morph ran on a device: %zu substeps\n", ++g_n, n);
+    } catch (const openvdb::Exception& e) {
+        std::printf("ok %d morph without a device: %s\n", ++g_n, e.what());
     }
     gbls_host_grid_free(fix);
     return 0;
