@@ -205,6 +205,24 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
 
 
 
+/* ---- level-set filters ----------------------------------------------------------
+ * Replaces tools::LevelSetFilter<FloatGrid> (tools/LevelSetFilter.h:93-157):
+ * the filter followed by the tracker pass with h's tracker state.
+ * LAPLACIAN: one Laplacian-flow step; MEAN / GAUSSIAN: box filter(s) of
+ * half width `width` (1..3 on the device); OFFSET: offset by `value` in
+ * CFL-limited increments, each tracked.  MEAN_CURVATURE, FILLET and MEDIAN
+ * return GBLS_ERR_UNSUPPORTED.                                               */
+enum {
+    GBLS_FILTER_LAPLACIAN = 0,
+    GBLS_FILTER_MEAN = 1,
+    GBLS_FILTER_GAUSSIAN = 2,
+    GBLS_FILTER_OFFSET = 3,
+    GBLS_FILTER_MEAN_CURVATURE = 4,
+    GBLS_FILTER_FILLET = 5,
+    GBLS_FILTER_MEDIAN = 6
+};
+int gbls_filter(gbls_handle* h, int filter, int width, float value);
+
 /* ---- level-set morphing ------------------------------------------------------
  * Replaces tools::LevelSetMorphing<FloatGrid>::advect (tools/LevelSetMorph.h:
  * 243-262): h moves towards the level set `target` with speed

@@ -18,6 +18,7 @@
 #include "../../include/gbls.h"
 #include "adjoint.h"
 #include "gbls_internal.cuh"
+#include "filter_ops.cuh"
 #include "io.h"
 #include "morph_ops.cuh"
 #include "stencil.h"
@@ -1340,6 +1341,43 @@ float morph_sample_speed(gbls_handle& h, gbls_handle& target, gbls_handle* mask,
     return (1e-6f < m) ? m : 1e-6f;  // mMaxAbsS starts at mMinAbsS = 1e-6
 }
 
+// ---- LevelSetFilter (tools/LevelSetFilter.h) -------------------------------
+// One Filter::cook pass: every active voxel from the current values into the
+// free value buffer, which becomes current (swapLeafBuffer).
+void filter_pass(gbls_handle& h, FilterArgs a, const char* msg) {
+    if (h.nleaf == 0) return;
+    const int vo = other_of(h.vc, h.vc);
+    a.nleaf = h.nleaf;
+    a.slot = h.S();
+    a.nbr = h.nbr.p;
+    a.src = h.layout(h.mc, h.vc);
+    a.out = h.vals[vo].p;
+    a.gamma = h.gamma;
+    start_intr(h, msg);
+    if (h.mode == GBLS_MODE_PARITY) launch_filter_parity(a, h.stream);
+    else launch_filter_fast(a, h.stream);
+    CU(cudaGetLastError());
+    ++h.stats.kernel_launches;
+    end_intr(h);
+    h.vc = vo;
+}
+
+// Filter::box (:277-289): axis-0, axis-2 and axis-1 averages (the
+// reference's boxX/boxY/boxZ bind Avg<0>, Avg<2>, Avg<1>), then track.
+void filter_box(gbls_handle& h, int width) {
+    width = std::max(1, width);
+    if (width > 3) fail(GBLS_ERR_UNSUPPORTED, "box widths above 3 voxels exceed the device stencil halo");
+    FilterArgs a{};
+    a.op = FILTER_BOX;
+    a.width = width;
+    a.frac = 1.0f / float(2 * width + 1);
+    for (int axis : {0, 2, 1}) {
+        a.axis = axis;
+        filter_pass(h, a, "Mean-value flow of level set");
+    }
+    track(h);
+}
+
 // ---- upload / download ------------------------------------------------------
 bool is_pm_gamma(float v, float g) { return v == g || v == -g; }
 
@@ -2435,6 +2473,67 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
         h->sync();
     });
     if (substeps) *substeps = count;
+    if (rc == GBLS_OK && interrupted) {
+        g_last_error = "interrupted";
+        return GBLS_ERR_INTERRUPTED;
+    }
+    return rc;
+}
+
+// LevelSetFilter (tools/LevelSetFilter.h:93-157): one filter, then the
+// tracker pass with h's tracker state (the filter is a LevelSetTracker).
+int gbls_filter(gbls_handle* h, int filter, int width, float value) {
+    if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    bool interrupted = false;
+    const int rc = guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        if (h->ninst > 1) fail(GBLS_ERR_UNSUPPORTED, "filters work on single level sets, not batches");
+        if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "the adjoint records advection only");
+        const float dx = float(h->voxel_size);  // LevelSetTracker::voxelSize()
+        switch (filter) {
+        case GBLS_FILTER_LAPLACIAN: {  // Filter::laplacian :305-315, laplacianImpl :452-477
+            FilterArgs a{};
+            a.op = FILTER_LAPLACIAN;
+            a.dt = (dx * dx) / 6.0f;
+            const float inv2dx = float(0.5 / double(dx));  // GradStencil(grid, dx)
+            a.invdx2 = float(4.0 * double(inv2dx) * double(inv2dx));
+            filter_pass(*h, a, "Laplacian flow of level set");
+            track(*h);
+            break;
+        }
+        case GBLS_FILTER_MEAN:  // Filter::mean :257-263
+            filter_box(*h, width);
+            break;
+        case GBLS_FILTER_GAUSSIAN:  // Filter::gaussian :265-271: four box filters
+            for (int n = 0; n < 4; ++n) filter_box(*h, width);
+            break;
+        case GBLS_FILTER_OFFSET: {  // Filter::offset :317-334
+            const float cfl = 0.5f * dx, offset = std::fabs(value);
+            float dist = 0.0f;
+            while (offset - dist > 0.001f * cfl) {
+                if (!check_intr(*h)) { interrupted = true; break; }
+                const float rest = offset - dist;
+                const float delta = (cfl < rest) ? cfl : rest;  // math::Min
+                dist += delta;
+                FilterArgs a{};
+                a.op = FILTER_OFFSET;
+                a.offset = std::copysign(delta, value);
+                filter_pass(*h, a, "Offsetting level set");
+                track(*h);
+            }
+            break;
+        }
+        case GBLS_FILTER_MEAN_CURVATURE:
+        case GBLS_FILTER_FILLET:
+        case GBLS_FILTER_MEDIAN:
+            fail(GBLS_ERR_UNSUPPORTED, "this filter has no device form yet");
+        default:
+            fail(GBLS_ERR_VALUE, "unknown filter");
+        }
+        h->nactive = -1;
+        h->sync();
+    });
     if (rc == GBLS_OK && interrupted) {
         g_last_error = "interrupted";
         return GBLS_ERR_INTERRUPTED;

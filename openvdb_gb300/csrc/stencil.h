@@ -22,4 +22,8 @@ void launch_morph_speed_parity(const MorphSpeedArgs& a, unsigned int* max_bits, 
 void launch_morph_stage_parity(const MorphArgs& a, cudaStream_t s);
 void launch_morph_speed_fast(const MorphSpeedArgs& a, unsigned int* max_bits, cudaStream_t s);
 void launch_morph_stage_fast(const MorphArgs& a, cudaStream_t s);
+// LevelSetFilter passes.
+struct FilterArgs;
+void launch_filter_parity(const FilterArgs& a, cudaStream_t s);
+void launch_filter_fast(const FilterArgs& a, cudaStream_t s);
 }  // namespace gbls

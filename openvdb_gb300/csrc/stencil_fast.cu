@@ -1,5 +1,6 @@
 // FP32 stencil kernels and the CFL reduction.
 #include "stencil.h"
+#include "filter_ops.cuh"
 #include "morph_ops.cuh"
 #include "stencil_ops.cuh"
 #include "stencil_fast2.cuh"
@@ -141,6 +142,11 @@ void launch_cfl(const CflArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
     cfl_max_kernel<<<unsigned(a.nleaf), CFL_THREADS, 0, s>>>(a);
     if (!a.inst_run) cfl_reduce_kernel<<<1, 1024, 0, s>>>(a.part, a.nleaf, a.max_bits);
+}
+
+void launch_filter_fast(const FilterArgs& a, cudaStream_t s) {
+    if (a.nleaf <= 0) return;
+    filter_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 }  // namespace gbls

@@ -2,6 +2,7 @@
 // explicit round-to-nearest intrinsics of ParityArith, so that every FP32
 // and FP64 operation is rounded exactly where the reference rounds it.
 #include "stencil.h"
+#include "filter_ops.cuh"
 #include "morph_ops.cuh"
 #include "stencil_ops.cuh"
 
@@ -26,6 +27,11 @@ void launch_morph_speed_parity(const MorphSpeedArgs& a, unsigned int* max_bits, 
 void launch_morph_stage_parity(const MorphArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
     morph_stage_kernel<ParityArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+}
+
+void launch_filter_parity(const FilterArgs& a, cudaStream_t s) {
+    if (a.nleaf <= 0) return;
+    filter_kernel<ParityArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 }  // namespace gbls

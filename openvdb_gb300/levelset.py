@@ -286,6 +286,42 @@ class LevelSetAdvection:
         return n.value
 
 
+class LevelSetFilter(LevelSetTracker):
+    """tools::LevelSetFilter<FloatGrid> (tools/LevelSetFilter.h:47-160): filters
+    on a DeviceLevelSet, each followed by track() with this tracker's state.
+    Masks (the optional alpha-mask argument) and the meanCurvature, fillet and
+    median filters have no device form (NotImplementedError / GBLS status)."""
+
+    def _filter(self, op, width=1, value=0.0, mask=None):
+        if mask is not None:
+            raise NotImplementedError("masked level-set filters have no device form")
+        rc = lib().gbls_filter(self._grid.handle, int(op), int(width), np.float32(value))
+        if rc == _abi.ERR_INTERRUPTED:
+            return
+        _call(rc)
+
+    def laplacian(self, mask=None):
+        self._filter(0, mask=mask)
+
+    def mean(self, width=1, mask=None):
+        self._filter(1, width, mask=mask)
+
+    def gaussian(self, width=1, mask=None):
+        self._filter(2, width, mask=mask)
+
+    def offset(self, value, mask=None):
+        self._filter(3, 1, value, mask=mask)
+
+    def meanCurvature(self, mask=None):
+        self._filter(4, mask=mask)
+
+    def fillet(self, mask=None):
+        self._filter(5, mask=mask)
+
+    def median(self, width=1, mask=None):
+        self._filter(6, width, mask=mask)
+
+
 class LevelSetMorphing:
     """tools::LevelSetMorphing<FloatGrid> over DeviceLevelSets
     (tools/LevelSetMorph.h:47-141): `source` moves towards `target`.

@@ -11,6 +11,7 @@
 #include <openvdb/openvdb.h>
 #include <openvdb/tools/Composite.h>
 #include <openvdb/tools/LevelSetAdvect.h>
+#include <openvdb/tools/LevelSetFilter.h>
 #include <openvdb/tools/LevelSetMorph.h>
 #include <openvdb/tools/LevelSetSphere.h>
 #include <openvdb/tools/LevelSetTracker.h>
@@ -320,6 +321,33 @@ int vdbref_from_desc(const gbls_grid_desc* d, void** out) {
 }
 
 // tools::LevelSetAdvection<FloatGrid, FieldT>::advect with the given schemes.
+// tools::LevelSetFilter<FloatGrid>: op 0 laplacian, 1 mean(width),
+// 2 gaussian(width), 3 offset(value), 4 meanCurvature, 5 fillet,
+// 6 median(width), with the given tracker state.
+int vdbref_filter(void* g, int op, int width, float value, int tspatial, int ttemporal, int normCount, int trim) {
+    try {
+        FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+        tools::LevelSetFilter<FloatGrid> f(grid);
+        f.setSpatialScheme(math::BiasedGradientScheme(tspatial));
+        f.setTemporalScheme(math::TemporalIntegrationScheme(ttemporal));
+        f.setNormCount(normCount);
+        f.setTrimming(tools::lstrack::TrimMode(trim));
+        switch (op) {
+        case 0: f.laplacian(); break;
+        case 1: f.mean(width); break;
+        case 2: f.gaussian(width); break;
+        case 3: f.offset(value); break;
+        case 4: f.meanCurvature(); break;
+        case 5: f.fillet(); break;
+        case 6: f.median(width); break;
+        default: return fail(GBLS_ERR_VALUE, "unknown filter");
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
 // tools::LevelSetMorphing<FloatGrid>::advect towards `target`, with an
 // optional alpha mask (mask may be null).
 int vdbref_morph(void* g, void* target, void* mask, int spatial, int temporal, int tspatial, int ttemporal,

@@ -41,6 +41,7 @@ def lib():
             [C.c_float, C.c_float, C.POINTER(C.c_uint64)]
         L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
         L.vdbref_set_threads.argtypes = [C.c_int]
+        L.vdbref_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4
         L.vdbref_morph.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_float] * 4 + [C.c_int,
                                                                                     C.POINTER(C.c_uint64)]
         _lib = L
@@ -125,6 +126,12 @@ class RefGrid:
                                   tracker_spatial, tracker_temporal, norm_count, t0, t1, mask_range[0],
                                   mask_range[1], 1 if invert else 0, C.byref(n)))
         return n.value
+
+    def filter(self, op, width=1, value=0.0, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1, norm_count=3,
+               trim=_abi.TRIM_ALL):
+        """tools::LevelSetFilter: op 0 laplacian, 1 mean, 2 gaussian, 3 offset, 4 meanCurvature,
+        5 fillet, 6 median."""
+        _check(lib().vdbref_filter(self.h, op, width, value, spatial, temporal, norm_count, trim))
 
     def tracker_op(self, op, arg=0, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1,
                    norm_count=3, trim=_abi.TRIM_ALL):

@@ -162,6 +162,23 @@ MORPH_CASES = {
 }
 
 
+# LevelSetFilter (tools/LevelSetFilter.h): filters applied in sequence to one
+# fixture; each op is (filter, width, value) with filter 0 laplacian, 1 mean,
+# 2 gaussian, 3 offset; tracker schemes as (spatial, temporal, normCount).
+FILTER_CASES = {
+    "filter_sphere_ops": dict(
+        fixture=("sphere", 14.0, (0.5, -1.0, 2.0), 1.0, 3.0),
+        tracker=(HJ, RK1, 3),
+        ops=[(0, 1, 0.0), (1, 1, 0.0), (3, 1, 1.3), (2, 2, 0.0), (3, 1, -0.7), (1, 3, 0.0)],
+    ),
+    "filter_torus_rk2_tracker": dict(
+        fixture=("torus", 14.0, 4.0, (0.0, 0.0, 0.0)),
+        tracker=(HJ, RK2, 1),
+        ops=[(0, 1, 0.0), (0, 1, 0.0), (2, 1, 0.0), (3, 1, 0.4)],
+    ),
+}
+
+
 # Batched advection: each instance must equal its own reference advect call.
 BATCH = dict(n=6, seed=11, rmin=6.0, rmax=20.0, schemes=(HJ, RK3, HJ, RK1, 1),
              ops=[(0.0, 1.0), (1.0, 2.0)])

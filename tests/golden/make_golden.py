@@ -19,7 +19,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from cases import BATCH, CASES, MORPH_CASES, make_batch, make_field, make_fixture  # noqa: E402
+from cases import BATCH, CASES, FILTER_CASES, MORPH_CASES, make_batch, make_field, make_fixture  # noqa: E402
 from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
 from oracle import refpy  # noqa: E402
 
@@ -87,6 +87,14 @@ def main():
         morph[name] = a
         print("%-32s ops=%d final active=%s" % (name, len(a) - 1, a[-1]["summary"]["active"]))
     result["__morph__"] = morph
+    filt = {}
+    for name, case in FILTER_CASES.items():
+        a = run_filter(case, 1)
+        b = run_filter(case, nthreads)
+        assert a == b, "reference result depends on the thread count: " + name
+        filt[name] = a
+        print("%-32s ops=%d final active=%s" % (name, len(a) - 1, a[-1]["summary"]["active"]))
+    result["__filter__"] = filt
     with open(os.path.join(HERE, "parity_cases.json"), "w") as f:
         json.dump(result, f, indent=1, sort_keys=True)
 
@@ -108,6 +116,20 @@ def run_morph(name, case, threads):
                     norm_count=nc, **kw)
         h = g.to_host()
         out.append({"op": list(op), "count": n, "digest": digest(h), "summary": summary(h)})
+    return out
+
+
+def run_filter(case, threads):
+    """A LevelSetFilter case: digests after every filter call."""
+    refpy.set_threads(threads)
+    src = make_fixture(case["fixture"])
+    g = refpy.RefGrid.from_host(src)
+    tsp, ttp, nc = case["tracker"]
+    out = [{"op": "input", "digest": digest(src), "summary": summary(src)}]
+    for op, width, value in case["ops"]:
+        g.filter(op, width, value, spatial=tsp, temporal=ttp, norm_count=nc)
+        h = g.to_host()
+        out.append({"op": [op, width, value], "digest": digest(h), "summary": summary(h)})
     return out
 
 
