@@ -133,7 +133,8 @@ public:
     GridType& mutableGrid() { return *mGrid; }
     void rebuildLeafs() { mLeafs->rebuildLeafArray(); }
 
-private:
+protected:
+    // Upload, apply `op` to the device level set, download into the grid.
     template <typename Op>
     void run(Op op) {
         detail::Handle h;
@@ -145,6 +146,7 @@ private:
         rebuildLeafs();
     }
 
+private:
     GridType* mGrid;
     std::unique_ptr<LeafManagerType> mLeafs;
     InterruptT* mInterrupter;

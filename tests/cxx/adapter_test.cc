@@ -17,6 +17,7 @@
 #include <cstring>
 
 #include "openvdb_gb300/LevelSetAdvect.h"
+#include "openvdb_gb300/LevelSetFilter.h"
 #include "openvdb_gb300/LevelSetMorph.h"
 
 using namespace openvdb;
@@ -189,6 +190,23 @@ int main() {
         std::printf("ok %d morph ran on a device: %zu substeps\n", ++g_n, n);
     } catch (const openvdb::Exception& e) {
         std::printf("ok %d morph without a device: %s\n", ++g_n, e.what());
+    }
+    // 8. filters: the tracker base, mask range checks, masks refused
+    og::tools::LevelSetFilter<FloatGrid> filt(*src2);
+    CHECK(filt.getNormCount() == 3 && filt.minMask() == 0.0f && filt.maxMask() == 1.0f);
+    FloatGrid maskGrid(0.0f);
+    threw = false;
+    try {
+        filt.gaussian(1, &maskGrid);
+    } catch (const NotImplementedError&) {
+        threw = true;
+    }
+    CHECK(threw);
+    try {
+        filt.laplacian();
+        std::printf("ok %d filter ran on a device\n", ++g_n);
+    } catch (const openvdb::Exception& e) {
+        std::printf("ok %d filter without a device: %s\n", ++g_n, e.what());
     }
     gbls_host_grid_free(fix);
     return 0;
