@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define GBLS_ABI_VERSION 1
+#define GBLS_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------- */
 typedef enum gbls_status {
@@ -137,6 +137,15 @@ typedef struct gbls_field_desc {
     float scale;                  /* DEFORMATION: voxels per time unit per unit    */
     float omega[3];               /* ROTATION: angular velocity (rad / time unit)  */
     float center[3];              /* ROTATION: rotation centre (index space)       */
+    /* DENSE: the velocity grid's own transform.  dense_map_type 0 = aligned
+     * with the level set (the index-space lookup field(ijk)); otherwise
+     * 1 + GBLS_MAP_*, with dense_voxel_size and dense_translation (world units):
+     * each voxel samples the grid trilinearly (BoxSampler) at its world
+     * position mapped into the grid's index space, as the reference's
+     * non-aligned sample<false> path does (tools/LevelSetAdvect.h:476-486).  */
+    int32_t dense_map_type;
+    double dense_voxel_size;
+    double dense_translation[3];
 } gbls_field_desc;
 
 typedef struct gbls_handle gbls_handle;   /* a device-resident level set      */

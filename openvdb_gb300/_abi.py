@@ -5,7 +5,7 @@ checked against the compiled library in tests/test_abi.py.
 """
 import ctypes as C
 
-GBLS_ABI_VERSION = 1
+GBLS_ABI_VERSION = 2
 
 # status codes
 OK = 0
@@ -75,6 +75,9 @@ class FieldDesc(C.Structure):
         ("scale", C.c_float),
         ("omega", C.c_float * 3),
         ("center", C.c_float * 3),
+        ("dense_map_type", C.c_int32),
+        ("dense_voxel_size", C.c_double),
+        ("dense_translation", C.c_double * 3),
     ]
 
 

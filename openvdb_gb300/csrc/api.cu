@@ -1118,7 +1118,10 @@ void check_scheme(int spatial, int temporal) {
         fail(GBLS_ERR_UNSUPPORTED, "the device path implements the HJWENO5_BIAS spatial scheme");
 }
 
-FieldParams field_params(const gbls_field* f, float t) {
+// Device form of a field for level set h at time t.  A dense field whose
+// transform differs from h's (the reference compares transforms,
+// tools/LevelSetAdvect.h:437) is sampled trilinearly.
+FieldParams field_params(const gbls_handle& h, const gbls_field* f, float t) {
     FieldParams p{};
     if (f->desc.kind == GBLS_FIELD_DEFORMATION && f->tab_n > 0) {
         p.tab = f->tab.p;
@@ -1138,6 +1141,23 @@ FieldParams field_params(const gbls_field* f, float t) {
         p.center[i] = d.center[i];
     }
     p.dense = f->dense.p;
+    if (d.kind == GBLS_FIELD_DENSE && d.dense_map_type != 0) {
+        const int vmap = d.dense_map_type - 1;  // GBLS_MAP_* of the velocity grid
+        const bool same = vmap == h.map_type && d.dense_voxel_size == h.voxel_size &&
+                          d.dense_translation[0] == h.translation[0] && d.dense_translation[1] == h.translation[1] &&
+                          d.dense_translation[2] == h.translation[2];
+        if (!same) {
+            p.xform = 1;
+            // map.applyMap = ijk * scale + translation for the three linear
+            // map kinds (scale 1 for a translation, translation 0 for a scale)
+            p.ls_scale = h.map_type == GBLS_MAP_TRANSLATION ? 1.0 : h.voxel_size;
+            p.vel_inv_scale = vmap == GBLS_MAP_TRANSLATION ? 1.0 : 1.0 / d.dense_voxel_size;
+            for (int i = 0; i < 3; ++i) {
+                p.ls_translation[i] = h.map_type == GBLS_MAP_UNIFORM_SCALE ? 0.0 : h.translation[i];
+                p.vel_translation[i] = vmap == GBLS_MAP_UNIFORM_SCALE ? 0.0 : d.dense_translation[i];
+            }
+        }
+    }
     p.domain = d.domain;
     p.period = d.period;
     p.scale = d.scale;
@@ -1157,7 +1177,7 @@ void enqueue_max_speed(gbls_handle& h, const gbls_field* f, float t, const unsig
     a.slot = h.S();
     a.amask = h.am[h.mc].p;
     a.t0 = t;
-    a.field = field_params(f, t);
+    a.field = field_params(h, f, t);
     a.max_bits = &h.st_d->max_v2_bits;
     h.cfl_part.reserve(size_t(std::max<int64_t>(h.nleaf, 1)), h.stream);
     a.part = h.cfl_part.p;
@@ -1217,7 +1237,7 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, 
     base.backward = backward ? 1 : 0;
     base.invdx = 1.0 / h.voxel_size;
     base.invdx_f = float(1.0 / h.voxel_size);
-    if (f) base.field = field_params(f, t0);
+    if (f) base.field = field_params(h, f, t0);
     if (h.batch_run) {
         base.inst_run = h.inst_run.p;
         base.inst_dt = h.inst_dt.p;
@@ -1984,6 +2004,8 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
         }
         DevArray<float> lam_next, lam4, lam3, lamA, lp2, lp1, lpn, dvel;
         lam_next.upload(lam_h.data(), lam_h.size(), st);
+        if (field_params(*h, field, 0.0f).xform)
+            fail(GBLS_ERR_UNSUPPORTED, "the adjoint differentiates velocity grids aligned with the level set only");
         const bool want_vel = dl_velocity && field->desc.kind == GBLS_FIELD_DENSE;
         size_t nvel = 0;
         float* dv = nullptr;
@@ -2036,7 +2058,7 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
             ra.invdx = invdx;
             ra.t0 = tp.t0;
             ra.backward = tp.backward ? 1 : 0;
-            ra.field = field_params(field, tp.t0);
+            ra.field = field_params(*h, field, tp.t0);
             ra.field.tab = nullptr;  // direct evaluation in the adjoint
             ra.dvel = dv;
             // stage 3: phi3 = 1/3 phin + 2/3 (phi2 - dt v.grad phi2)
@@ -2179,7 +2201,7 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
                 fail(GBLS_ERR_VALUE, "deformation field needs domain > 0 and period != 0");
             gbls_field tmp;
             tmp.desc = d;
-            fp[size_t(i)] = field_params(&tmp, t0);  // no tables: direct evaluation
+            fp[size_t(i)] = field_params(*h, &tmp, t0);  // no tables: direct evaluation
             all_constant &= d.kind == GBLS_FIELD_CONSTANT;
         }
         h->inst_field.upload(fp.data(), fp.size(), h->stream);
@@ -2366,6 +2388,9 @@ int gbls_field_create(const gbls_field_desc* desc, gbls_field** out) {
         if (desc->kind == GBLS_FIELD_DENSE) {
             const int64_t n = int64_t(desc->dense_dims[0]) * desc->dense_dims[1] * desc->dense_dims[2];
             if (n <= 0 || !desc->dense_values) fail(GBLS_ERR_INVALID_ARGUMENT, "empty dense field");
+            if (desc->dense_map_type < 0 || desc->dense_map_type > GBLS_MAP_TRANSLATION + 1 ||
+                (desc->dense_map_type != 0 && !(desc->dense_voxel_size > 0.0)))
+                fail(GBLS_ERR_VALUE, "dense field transform must be a uniform scale and/or translation");
             f->dense.upload(desc->dense_values, size_t(n) * 3, nullptr);
             CU(cudaStreamSynchronize(nullptr));
         }

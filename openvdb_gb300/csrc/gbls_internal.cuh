@@ -288,6 +288,11 @@ struct FieldParams {
     int dense_dims[3];
     const float* dense;  // device [nx][ny][nz][3]
     float dense_background[3];
+    // DENSE with its own transform: world = ijk * ls_scale + ls_translation
+    // (the level set's map), grid index = (world - vel_translation) *
+    // vel_inv_scale (the velocity grid's inverse map), then trilinear.
+    int xform;
+    double ls_scale, ls_translation[3], vel_inv_scale, vel_translation[3];
     float domain, period, scale;
     float omega[3];
     float center[3];

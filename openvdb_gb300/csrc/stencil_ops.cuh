@@ -201,19 +201,68 @@ __device__ __forceinline__ float godunov(bool outside, const float* dm, const fl
 }
 
 // ---- velocity --------------------------------------------------------------
+// Value of the dense velocity grid at its index (a, b, c) (background outside).
+__device__ __forceinline__ void dense_value(const FieldParams& f, int i, int j, int k, float out[3]) {
+    const int a = i - f.dense_origin[0], b = j - f.dense_origin[1], c = k - f.dense_origin[2];
+    if (a >= 0 && b >= 0 && c >= 0 && a < f.dense_dims[0] && b < f.dense_dims[1] && c < f.dense_dims[2]) {
+        const float* p = f.dense + 3 * ((size_t(a) * f.dense_dims[1] + b) * f.dense_dims[2] + c);
+        out[0] = __ldg(p); out[1] = __ldg(p + 1); out[2] = __ldg(p + 2);
+    } else {
+        out[0] = f.dense_background[0]; out[1] = f.dense_background[1]; out[2] = f.dense_background[2];
+    }
+}
+
+// BoxSampler's `a + ValueT((b - a) * weight)` per component
+// (tools/Interpolation.h:716-722): float difference, double product,
+// rounded back to float, float sum.
+__device__ __forceinline__ float box_lerp(float a, float b, double w) {
+    return __fadd_rn(a, __double2float_rn(__dmul_rn(double(__fsub_rn(b, a)), w)));
+}
+
+// DiscreteField::operator()(xyz, t) at the world position of voxel ijk
+// (map.applyMap, tools/LevelSetAdvect.h:482-483): worldToIndex into the
+// velocity grid, then BoxSampler::sample (tools/Interpolation.h:714-762).
+// Explicit round-to-nearest intrinsics keep it exact in every build unit.
+__device__ inline void dense_trilinear(const FieldParams& f, int i, int j, int k, float out[3]) {
+    const int ijk[3] = {i, j, k};
+    int i0[3];
+    double uvw[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double w = __dadd_rn(__dmul_rn(double(ijk[a]), f.ls_scale), f.ls_translation[a]);
+        const double q = __dmul_rn(__dsub_rn(w, f.vel_translation[a]), f.vel_inv_scale);
+        const double fl = floor(q);
+        i0[a] = int(fl);
+        uvw[a] = __dsub_rn(q, double(i0[a]));
+    }
+    float d[2][2][2][3];
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int z = 0; z < 2; ++z) dense_value(f, i0[0] + x, i0[1] + y, i0[2] + z, d[x][y][z]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float a0 = box_lerp(box_lerp(d[0][0][0][c], d[0][0][1][c], uvw[2]),
+                                  box_lerp(d[0][1][0][c], d[0][1][1][c], uvw[2]), uvw[1]);
+        const float a1 = box_lerp(box_lerp(d[1][0][0][c], d[1][0][1][c], uvw[2]),
+                                  box_lerp(d[1][1][0][c], d[1][1][1][c], uvw[2]), uvw[1]);
+        out[c] = box_lerp(a0, a1, uvw[0]);
+    }
+}
+
 __device__ __forceinline__ void eval_field(const FieldParams& f, int i, int j, int k, float t,
                                            float out[3]) {
     switch (f.kind) {
     case 0:  // GBLS_FIELD_CONSTANT
         out[0] = f.constant[0]; out[1] = f.constant[1]; out[2] = f.constant[2];
         break;
-    case 1: {  // GBLS_FIELD_DENSE: aligned DiscreteField lookup
-        const int a = i - f.dense_origin[0], b = j - f.dense_origin[1], c = k - f.dense_origin[2];
-        if (a >= 0 && b >= 0 && c >= 0 && a < f.dense_dims[0] && b < f.dense_dims[1] && c < f.dense_dims[2]) {
-            const float* p = f.dense + 3 * ((size_t(a) * f.dense_dims[1] + b) * f.dense_dims[2] + c);
-            out[0] = __ldg(p); out[1] = __ldg(p + 1); out[2] = __ldg(p + 2);
-        } else {
-            out[0] = f.dense_background[0]; out[1] = f.dense_background[1]; out[2] = f.dense_background[2];
+    case 1: {  // GBLS_FIELD_DENSE
+        if (f.xform) {
+            dense_trilinear(f, i, j, k, out);
+        } else {  // aligned DiscreteField lookup
+            dense_value(f, i, j, k, out);
         }
         break;
     }

@@ -2,7 +2,8 @@
 
 The reference advects in any functor with operator()(Coord, t)
 (tools/LevelSetAdvect.h:32-52).  The kinds here cover the reference's
-DiscreteField (tools/VelocityFields.h:42-94) in its aligned form, plus two
+DiscreteField (tools/VelocityFields.h:42-94), aligned or with its own
+transform (trilinear BoxSampler), plus two
 analytic fields whose arithmetic is defined in include/gbls_fields.h.
 """
 import ctypes as C
@@ -24,6 +25,9 @@ class Field:
         self.scale = float(kw.get("scale", 1.0))
         self.omega = tuple(kw.get("omega", (0.0, 0.0, 0.0)))
         self.center = tuple(kw.get("center", (0.0, 0.0, 0.0)))
+        self.dense_map_type = int(kw.get("dense_map_type", 0))
+        self.dense_voxel_size = float(kw.get("dense_voxel_size", 1.0))
+        self.dense_translation = tuple(float(x) for x in kw.get("dense_translation", (0.0, 0.0, 0.0)))
         if self.dense_values is not None:
             self.dense_values = np.ascontiguousarray(self.dense_values, np.float32)
             assert self.dense_values.ndim == 4 and self.dense_values.shape[3] == 3
@@ -38,6 +42,16 @@ class Field:
         """Aligned DiscreteField over a dense Vec3f block values[nx,ny,nz,3]."""
         return cls(_abi.FIELD_DENSE, dense_values=values, dense_origin=origin,
                    dense_background=background)
+
+    @classmethod
+    def dense_xform(cls, values, voxel_size, translation=(0.0, 0.0, 0.0), origin=(0, 0, 0),
+                    background=(0.0, 0.0, 0.0)):
+        """DiscreteField over a dense Vec3f block values[nx,ny,nz,3] in a grid
+        with its own transform (uniform scale `voxel_size`, world
+        `translation`): sampled trilinearly at each voxel's world position."""
+        mt = _abi.MAP_UNIFORM_SCALE_TRANSLATE if any(translation) else _abi.MAP_UNIFORM_SCALE
+        return cls(_abi.FIELD_DENSE, dense_values=values, dense_origin=origin, dense_background=background,
+                   dense_map_type=1 + mt, dense_voxel_size=voxel_size, dense_translation=translation)
 
     @classmethod
     def deformation(cls, domain=1024.0, period=100.0, scale=1.0):
@@ -61,4 +75,7 @@ class Field:
         d.scale = self.scale
         d.omega[:] = self.omega
         d.center[:] = self.center
+        d.dense_map_type = self.dense_map_type
+        d.dense_voxel_size = self.dense_voxel_size
+        d.dense_translation[:] = self.dense_translation
         return d

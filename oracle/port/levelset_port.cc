@@ -215,6 +215,7 @@ int oport_advect(void* h, const gbls_field_desc* fd, int spatial, int temporal, 
         if (fd->kind == GBLS_FIELD_DENSE)
             field.dense.assign(fd->dense_values,
                                fd->dense_values + size_t(3) * fd->dense_dims[0] * fd->dense_dims[1] * fd->dense_dims[2]);
+        field.set_level_set_map(g.map_type, g.voxel_size, g.translation);
         using G = std::remove_reference_t<decltype(g)>;
         using A = decltype(adv_of(g));
         A a{g, field};

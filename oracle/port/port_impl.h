@@ -117,19 +117,65 @@ void gather(const Grid& g, const Leaf* L, int b, Tile& t) {
 struct Field {
     gbls_field_desc d{};
     std::vector<float> dense;
+    // a dense grid with its own transform (tools/LevelSetAdvect.h:482-483):
+    // world = ijk * ls_scale + ls_t, grid index = (world - vel_t) * vel_inv
+    bool xform = false;
+    double ls_scale = 1, ls_t[3] = {0, 0, 0}, vel_inv = 1, vel_t[3] = {0, 0, 0};
+
+    // Sampling setup for a level set with map (map_type, voxel_size, translation).
+    void set_level_set_map(int map_type, double voxel_size, const double* translation) {
+        xform = false;
+        if (d.kind != GBLS_FIELD_DENSE || d.dense_map_type == 0) return;
+        const int vmap = d.dense_map_type - 1;
+        if (vmap == map_type && d.dense_voxel_size == voxel_size && d.dense_translation[0] == translation[0] &&
+            d.dense_translation[1] == translation[1] && d.dense_translation[2] == translation[2])
+            return;  // same transform: the aligned lookup
+        xform = true;
+        ls_scale = map_type == GBLS_MAP_TRANSLATION ? 1.0 : voxel_size;
+        vel_inv = vmap == GBLS_MAP_TRANSLATION ? 1.0 : 1.0 / d.dense_voxel_size;
+        for (int a = 0; a < 3; ++a) {
+            ls_t[a] = map_type == GBLS_MAP_UNIFORM_SCALE ? 0.0 : translation[a];
+            vel_t[a] = vmap == GBLS_MAP_UNIFORM_SCALE ? 0.0 : d.dense_translation[a];
+        }
+    }
+    void grid_value(int i, int j, int k, float out[3]) const {
+        const int a = i - d.dense_origin[0], b = j - d.dense_origin[1], c = k - d.dense_origin[2];
+        if (a >= 0 && b >= 0 && c >= 0 && a < d.dense_dims[0] && b < d.dense_dims[1] && c < d.dense_dims[2]) {
+            const float* p = dense.data() + 3 * ((size_t(a) * d.dense_dims[1] + b) * d.dense_dims[2] + c);
+            out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
+        } else {
+            out[0] = d.dense_background[0]; out[1] = d.dense_background[1]; out[2] = d.dense_background[2];
+        }
+    }
+    // BoxSampler (tools/Interpolation.h:714-762): a + float(double(b - a) * w)
+    static float lerp(float a, float b, double w) { return a + float(double(b - a) * w); }
+    void trilinear(int i, int j, int k, float out[3]) const {
+        const int ijk[3] = {i, j, k};
+        int i0[3];
+        double uvw[3];
+        for (int a = 0; a < 3; ++a) {
+            const double w = double(ijk[a]) * ls_scale + ls_t[a];
+            const double q = (w - vel_t[a]) * vel_inv;
+            i0[a] = int(std::floor(q));
+            uvw[a] = q - double(i0[a]);
+        }
+        float v[2][2][2][3];
+        for (int x = 0; x < 2; ++x)
+            for (int y = 0; y < 2; ++y)
+                for (int z = 0; z < 2; ++z) grid_value(i0[0] + x, i0[1] + y, i0[2] + z, v[x][y][z]);
+        for (int c = 0; c < 3; ++c) {
+            const float a0 = lerp(lerp(v[0][0][0][c], v[0][0][1][c], uvw[2]), lerp(v[0][1][0][c], v[0][1][1][c], uvw[2]), uvw[1]);
+            const float a1 = lerp(lerp(v[1][0][0][c], v[1][0][1][c], uvw[2]), lerp(v[1][1][0][c], v[1][1][1][c], uvw[2]), uvw[1]);
+            out[c] = lerp(a0, a1, uvw[0]);
+        }
+    }
     void eval(int i, int j, int k, float t, float out[3]) const {
         switch (d.kind) {
         case GBLS_FIELD_CONSTANT: out[0] = d.constant[0]; out[1] = d.constant[1]; out[2] = d.constant[2]; break;
-        case GBLS_FIELD_DENSE: {
-            const int a = i - d.dense_origin[0], b = j - d.dense_origin[1], c = k - d.dense_origin[2];
-            if (a >= 0 && b >= 0 && c >= 0 && a < d.dense_dims[0] && b < d.dense_dims[1] && c < d.dense_dims[2]) {
-                const float* p = dense.data() + 3 * ((size_t(a) * d.dense_dims[1] + b) * d.dense_dims[2] + c);
-                out[0] = p[0]; out[1] = p[1]; out[2] = p[2];
-            } else {
-                out[0] = d.dense_background[0]; out[1] = d.dense_background[1]; out[2] = d.dense_background[2];
-            }
+        case GBLS_FIELD_DENSE:
+            if (xform) trilinear(i, j, k, out);
+            else grid_value(i, j, k, out);
             break;
-        }
         case GBLS_FIELD_DEFORMATION: gbls_deformation(i, j, k, t, d.domain, d.period, d.scale, out); break;
         default: gbls_rotation(i, j, k, d.constant, d.omega, d.center, out); break;
         }

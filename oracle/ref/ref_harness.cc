@@ -86,7 +86,16 @@ Vec3fGrid::Ptr makeVelocityGrid(const gbls_field_desc& f, const math::Transform&
                                  Vec3f(v[0], v[1], v[2]));
                 }
     }
-    vel->setTransform(xform.copy());
+    if (f.kind == GBLS_FIELD_DENSE && f.dense_map_type != 0) {
+        // the velocity grid's own transform (1 + GBLS_MAP_*)
+        math::Transform::Ptr vx = math::Transform::createLinearTransform(
+            f.dense_map_type - 1 == GBLS_MAP_TRANSLATION ? 1.0 : f.dense_voxel_size);
+        if (f.dense_map_type - 1 != GBLS_MAP_UNIFORM_SCALE)
+            vx->postTranslate(Vec3d(f.dense_translation[0], f.dense_translation[1], f.dense_translation[2]));
+        vel->setTransform(vx);
+    } else {
+        vel->setTransform(xform.copy());
+    }
     return vel;
 }
 

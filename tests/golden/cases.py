@@ -99,6 +99,20 @@ CASES = {
         schemes=(HJ, RK3, HJ, RK1, 1),
         ops=[("advect", float(t), float(t + 1)) for t in range(3)],
     ),
+    # non-aligned DiscreteField: the velocity grid has its own voxel size and
+    # translation, sampled trilinearly at every voxel's world position
+    "sphere12_dense_xform": dict(
+        fixture=("sphere", 12.0, (16.0, 16.0, 16.0), 1.0, 3.0),
+        field=("dense_xform", 24, 3.0, 1.0, 13, 1.5, (0.3, -0.2, 0.1), (0, 0, 0)),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        ops=[("advect", float(t), float(t + 1)) for t in range(3)],
+    ),
+    "half_voxel_dense_xform": dict(
+        fixture=("sphere", 6.0, (0.25, -0.5, 1.0), 0.5, 3.0),
+        field=("dense_xform", 32, 4.0, 0.5, 17, 1.0, (0.0, 0.0, 0.0), (-10, -10, -10)),
+        schemes=(HJ, RK2, HJ, RK1, 3),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+    ),
     "sphere_half_voxel": dict(
         fixture=("sphere", 6.0, (0.25, -0.5, 1.0), 0.5, 3.0),
         field=("constant", (0.5, 0.25, -0.3)),
@@ -120,6 +134,10 @@ def make_field(spec):
         n, sigma, amp, seed = spec[1:]
         return Field.dense(smoothed_noise(n, sigma, amp, seed), origin=(0, 0, 0),
                            background=(0.0, 0.0, 0.0))
+    if kind == "dense_xform":
+        n, sigma, amp, seed, voxel, translation, origin = spec[1:]
+        return Field.dense_xform(smoothed_noise(n, sigma, amp, seed), voxel, translation, origin=origin,
+                                 background=(0.0, 0.0, 0.0))
     raise ValueError(kind)
 
 
