@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <new>
 #include <string>
@@ -324,23 +325,22 @@ struct FieldTraits<RotationField> {
 // Largest dense velocity box the DiscreteField form builds (voxels).
 constexpr int64_t kMaxDenseFieldVoxels = int64_t(1) << 28;
 
-// tools::DiscreteField aligned with the level set: the index-space lookup
-// of sample<Aligned> (tools/LevelSetAdvect.h:470-478) reads field(ijk, t),
-// which is time independent.  The device form is a dense box of those
-// values around the band: the level set's active bounding box widened by
-// the stencil reach plus the distance the band can travel in [t0, t1] at
-// the largest speed inside the box (widened again until that holds).
-// Voxels outside the box take the value sampled at the box's first corner
-// beyond the band reach, i.e. they are never read.  A non-aligned field
-// (trilinear BoxSampler) has no device form.
+// tools::DiscreteField over a Vec3 grid.  Aligned with the level set, the
+// index-space lookup of sample<Aligned> (tools/LevelSetAdvect.h:470-478)
+// reads field(ijk, t); otherwise every voxel samples the grid trilinearly at
+// its world position (sample<false>), which the device reproduces from the
+// grid's values and transform.  Either way the device form is a dense box of
+// the grid's own values, read exactly through field(Coord, t) in the grid's
+// index space, around the band: the level set's active bounding box mapped
+// into the grid's index space and widened by the stencil and interpolation
+// reach plus the distance the band can travel in [t0, t1] at the largest
+// speed inside the box (widened again until that holds).  The grid
+// transform must be a uniform scale and/or translation.
 template <typename VelGridT, typename SamplerT>
 struct FieldTraits<openvdb::tools::DiscreteField<VelGridT, SamplerT>> {
     using FieldT = openvdb::tools::DiscreteField<VelGridT, SamplerT>;
     template <typename GridT>
     static gbls_field_desc describe(const FieldT& f, const GridT& ls, float t0, float t1, std::vector<float>& store) {
-        if (!(f.transform() == ls.transform()))
-            OPENVDB_THROW(openvdb::NotImplementedError,
-                          "DiscreteField not aligned with the level set: trilinear sampling has no device form");
         gbls_field_desc d{};
         d.kind = GBLS_FIELD_DENSE;
         openvdb::CoordBBox band;
@@ -348,8 +348,34 @@ struct FieldTraits<openvdb::tools::DiscreteField<VelGridT, SamplerT>> {
             d.kind = GBLS_FIELD_CONSTANT;
             return d;
         }
-        const double span = std::fabs(double(t1) - double(t0)) / ls.voxelSize()[0];
-        int margin = 8;
+        const openvdb::math::Transform& vx = f.transform();
+        const bool aligned = vx == ls.transform();
+        double vox = ls.voxelSize()[0];
+        if (!aligned) {
+            detail::HostGrid tmp;
+            detail::exportTransform(vx, tmp);  // throws unless a uniform linear map
+            d.dense_map_type = 1 + tmp.map_type;
+            d.dense_voxel_size = tmp.voxel_size;
+            for (int i = 0; i < 3; ++i) d.dense_translation[i] = tmp.translation[i];
+            vox = tmp.voxel_size;
+            // the band's box in the velocity grid's index space
+            openvdb::Vec3d lo(std::numeric_limits<double>::max()), hi(-std::numeric_limits<double>::max());
+            for (int c = 0; c < 8; ++c) {
+                const openvdb::Coord k((c & 1) ? band.max()[0] : band.min()[0], (c & 2) ? band.max()[1] : band.min()[1],
+                                       (c & 4) ? band.max()[2] : band.min()[2]);
+                const openvdb::Vec3d q = vx.worldToIndex(ls.transform().indexToWorld(k));
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = std::min(lo[a], q[a]);
+                    hi[a] = std::max(hi[a], q[a]);
+                }
+            }
+            band = openvdb::CoordBBox(openvdb::Coord(int(std::floor(lo[0])), int(std::floor(lo[1])), int(std::floor(lo[2]))),
+                                      openvdb::Coord(int(std::ceil(hi[0])), int(std::ceil(hi[1])), int(std::ceil(hi[2]))));
+        }
+        // distance in grid voxels: the band may travel span * vmax world units
+        const double span = std::fabs(double(t1) - double(t0)) / vox;
+        const int reach = int(std::ceil(4.0 * ls.voxelSize()[0] / vox)) + 2;
+        int margin = reach + 4;
         for (;;) {
             openvdb::CoordBBox box = band;
             box.expand(margin);
@@ -370,7 +396,7 @@ struct FieldTraits<openvdb::tools::DiscreteField<VelGridT, SamplerT>> {
                             vmax = std::max(vmax, std::fabs(double(v[i])));
                         }
                     }
-            const int need = int(std::ceil(span * vmax * std::sqrt(3.0))) + 8;
+            const int need = int(std::ceil(span * vmax * std::sqrt(3.0))) + reach + 4;
             if (need <= margin) {
                 for (int i = 0; i < 3; ++i) {
                     d.dense_origin[i] = box.min()[i];
