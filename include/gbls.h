@@ -173,6 +173,13 @@ int gbls_set_device(int device);
  * background or voxel size (the reference requires GRID_LEVEL_SET class and
  * uniform voxels), GBLS_ERR_UNSUPPORTED for tiles other than +-background. */
 int gbls_create(const gbls_grid_desc* desc, gbls_handle** out);
+/* Replace the level set held by h with `desc` (the checks of gbls_create),
+ * keeping h's device allocations, stream, precision mode, tracker state,
+ * trimming and interrupter; the adjoint tape is discarded.  A long-lived
+ * LevelSetAdvection / LevelSetTracker object re-uploads its grid this way on
+ * every call.  After a refused upload h holds an empty level set.  Not for
+ * batch handles.  No reference counterpart (the reference holds the grid).  */
+int gbls_upload(gbls_handle* h, const gbls_grid_desc* desc);
 int gbls_destroy(gbls_handle* h);
 int gbls_get_counts(gbls_handle* h, gbls_grid_counts* out);
 /* Copy the grid back in canonical order into caller-allocated arrays sized

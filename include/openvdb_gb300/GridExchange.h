@@ -224,12 +224,13 @@ public:
         if (mH) gbls_destroy(mH);
         mH = nullptr;
     }
+    // Create on first use; later uploads keep the device allocations.
     template <typename GridT>
     void upload(const GridT& grid) {
-        reset();
         HostGrid h = pack(grid);
         gbls_grid_desc d = h.desc();
-        check(gbls_create(&d, &mH));
+        if (mH) check(gbls_upload(mH, &d));
+        else check(gbls_create(&d, &mH));
     }
     template <typename GridT>
     void download(GridT& grid) const {

@@ -6,8 +6,9 @@
 // runs the whole CFL substep loop (RK stages + track() per substep) on the
 // device and writes the result back into the same tree; it returns the
 // number of CFL substeps, like the reference.  FieldT reaches the device
-// through openvdb_gb300::FieldTraits (an aligned tools::DiscreteField, or the
-// analytic ConstantField / DeformationField / RotationField).
+// through openvdb_gb300::FieldTraits (a tools::DiscreteField, aligned or
+// with its own transform, or the analytic ConstantField / DeformationField /
+// RotationField).  The device level set is kept between advect() calls.
 //
 //   openvdb::tools::DiscreteField<openvdb::Vec3SGrid> field(*velocity);
 //   openvdb_gb300::tools::LevelSetAdvection<openvdb::FloatGrid,
@@ -79,7 +80,7 @@ public:
             gbls_field* f;
             ~FieldGuard() { gbls_field_destroy(f); }
         } guard{field};
-        detail::Handle h;
+        detail::Handle& h = mTracker.device();
         h.upload(mTracker.grid());
         mTracker.configure(h.get());
         uint64_t count = 0;

@@ -68,13 +68,13 @@ public:
 
     // tools/LevelSetMorph.h:243-262 + Morph::advect :479-510.
     size_t advect(ValueType time0, ValueType time1) {
-        detail::Handle h, target, mask;
+        detail::Handle& h = mTracker.device();
         h.upload(mTracker.grid());
-        target.upload(*mTarget);
-        if (mMask) mask.upload(*mMask);
+        mTargetDevice.upload(*mTarget);
+        if (mMask) mMaskDevice.upload(*mMask);
         mTracker.configure(h.get());
         uint64_t count = 0;
-        detail::check(gbls_morph(h.get(), target.get(), mMask ? mask.get() : nullptr, int(mSpatialScheme),
+        detail::check(gbls_morph(h.get(), mTargetDevice.get(), mMask ? mMaskDevice.get() : nullptr, int(mSpatialScheme),
                                  int(mTemporalScheme), float(time0), float(time1), float(mMinMask),
                                  float(mMaxMask), mInvertMask ? 1 : 0, &count));
         h.download(mTracker.mutableGrid());
@@ -90,6 +90,7 @@ private:
     // the range as given (gbls_morph forms max - min as setMaskRange does)
     ValueType mMinMask = 0, mMaxMask = 1, mDeltaMask = 1;
     bool mInvertMask = false;
+    detail::Handle mTargetDevice, mMaskDevice;
 };
 
 }  // namespace tools

@@ -137,16 +137,21 @@ protected:
     // Upload, apply `op` to the device level set, download into the grid.
     template <typename Op>
     void run(Op op) {
-        detail::Handle h;
-        h.upload(*mGrid);
-        configure(h.get());
-        const int rc = op(h.get());
+        mDevice.upload(*mGrid);
+        configure(mDevice.get());
+        const int rc = op(mDevice.get());
         detail::check(rc);
-        h.download(*mGrid);
+        mDevice.download(*mGrid);
         rebuildLeafs();
     }
 
+public:
+    // The device level set of this tracker, kept between calls so that
+    // repeated operations re-use its allocations (gbls_upload).
+    detail::Handle& device() { return mDevice; }
+
 private:
+    detail::Handle mDevice;
     GridType* mGrid;
     std::unique_ptr<LeafManagerType> mLeafs;
     InterruptT* mInterrupter;

@@ -36,6 +36,7 @@ def lib():
         "gbls_last_error": ([], C.c_char_p),
         "gbls_set_device": ([C.c_int], C.c_int),
         "gbls_create": ([P(_abi.GridDesc), P(vp)], C.c_int),
+        "gbls_upload": ([vp, P(_abi.GridDesc)], C.c_int),
         "gbls_destroy": ([vp], C.c_int),
         "gbls_get_counts": ([vp, P(_abi.GridCounts)], C.c_int),
         "gbls_download": ([vp, P(_abi.GridDesc)], C.c_int),

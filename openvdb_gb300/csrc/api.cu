@@ -1738,6 +1738,30 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
     return GBLS_OK;
 }
 
+int gbls_upload(gbls_handle* h, const gbls_grid_desc* desc) {
+    if (!h || !desc) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (h->ninst != 1) fail(GBLS_ERR_INVALID_ARGUMENT, "batch handles take their level sets at creation");
+        h->sync();
+        h->tape.clear();
+        h->tape_cur = nullptr;
+        try {
+            upload(*h, desc, 1);
+        } catch (...) {
+            // a refused upload leaves an empty level set, not a partial one
+            h->nleaf = 0;
+            h->nactive = 0;
+            h->lower_keys_h.clear();
+            h->upper_keys_h.clear();
+            h->upper_sign_h.clear();
+            h->root_keys_h.clear();
+            h->root_sign_h.clear();
+            throw;
+        }
+    });
+}
+
 int gbls_destroy(gbls_handle* h) {
     if (!h) return GBLS_OK;
     return guarded([&] {

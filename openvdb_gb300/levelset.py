@@ -66,6 +66,18 @@ class DeviceLevelSet:
     def handle(self):
         return self._h
 
+    def upload(self, grid):
+        """Replace the level set with `grid`, keeping this handle's device
+        allocations and settings (gbls_upload)."""
+        self._keep = grid
+        d = grid.desc()
+        try:
+            _call(lib().gbls_upload(self._h, C.byref(d)))
+        finally:
+            self._keep = None
+        self.voxel_size = grid.voxel_size
+        self.background = grid.background
+
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             lib().gbls_destroy(self._h)

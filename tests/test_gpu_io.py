@@ -100,3 +100,25 @@ def test_rejects_malformed_inputs():
 
     # the handle is still usable after refusals
     assert bitwise_equal(DeviceLevelSet(base).to_host(), base)
+
+
+@pytest.mark.gpu
+def test_reupload_into_existing_handle():
+    """gbls_upload replaces the level set and keeps the handle usable; a
+    refused upload leaves an empty level set."""
+    grids = _grids()
+    dev = DeviceLevelSet(grids[0])
+    for g in (grids[2], grids[1], grids[3], grids[0]):
+        dev.upload(g)
+        out = dev.to_host()
+        assert bitwise_equal(out, g), compare(out, g)
+    bad = grids[1].copy()
+    bad.leaf_values = bad.leaf_values.copy()
+    li, vi = np.argwhere(~bad.active_mask_bool())[0]
+    bad.leaf_values[li, vi] = 0.0
+    with pytest.raises(GblsError) as e:
+        dev.upload(bad)
+    assert e.value.code == _abi.ERR_UNSUPPORTED
+    assert dev.counts().leaf_count == 0 and dev.active_voxel_count() == 0
+    dev.upload(grids[2])
+    assert bitwise_equal(dev.to_host(), grids[2])
