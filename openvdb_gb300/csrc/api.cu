@@ -1498,14 +1498,15 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
         h.root_keys_h.push_back(r.key);
         h.root_sign_h.push_back(uint8_t(v < 0.0f ? 1 : 0));
     }
-    // device state
-    h.nleaf = L;
+    // device state (nothing of a previous level set is kept)
+    h.nleaf = 0;
     h.kc = 0;
     h.mc = 0;
     h.vc = 0;
     h.slot_cap = 0;
     h.nfree = 0;
     h.ensure_leaf_cap(std::max<int64_t>(L, 16) + L / 2);
+    h.nleaf = L;
     const int64_t scap = L + L / 2 + 1024;
     for (int b = 0; b < 3; ++b) {
         h.am[b].reserve(size_t(scap) * 8, h.stream);
