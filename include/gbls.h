@@ -224,10 +224,10 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
 /* ---- level-set filters ----------------------------------------------------------
  * Replaces tools::LevelSetFilter<FloatGrid> (tools/LevelSetFilter.h:93-157):
  * the filter followed by the tracker pass with h's tracker state.
- * LAPLACIAN: one Laplacian-flow step; MEAN / GAUSSIAN: box filter(s) of
- * half width `width` (1..3 on the device); OFFSET: offset by `value` in
- * CFL-limited increments, each tracked.  MEAN_CURVATURE, FILLET and MEDIAN
- * return GBLS_ERR_UNSUPPORTED.                                               */
+ * LAPLACIAN, MEAN_CURVATURE, FILLET: one flow step; MEAN / GAUSSIAN: box
+ * filter(s) and MEDIAN: median filter of half width `width` (1..3 on the
+ * device, GBLS_ERR_UNSUPPORTED above); OFFSET: offset by `value` in
+ * CFL-limited increments, each tracked.                                      */
 enum {
     GBLS_FILTER_LAPLACIAN = 0,
     GBLS_FILTER_MEAN = 1,

@@ -4,10 +4,9 @@
 // Same template parameters and member functions as the reference class, a
 // LevelSetTracker (the drop-in one) with filters; every filter uploads the
 // grid, runs the filter and the tracker pass on the device and writes the
-// result back into the same tree.  Device forms exist for laplacian(),
-// mean(width), gaussian(width) (half widths 1..3) and offset(value);
-// meanCurvature(), fillet(), median() and every call with an alpha mask
-// throw NotImplementedError.
+// result back into the same tree.  Every filter has a device form
+// (mean, gaussian and median for half widths 1..3); calls with an alpha
+// mask throw NotImplementedError.
 //
 //   openvdb_gb300::tools::LevelSetFilter<openvdb::FloatGrid> filter(*grid);
 //   filter.gaussian(1);

@@ -1373,6 +1373,8 @@ void filter_pass(gbls_handle& h, FilterArgs a, const char* msg) {
     a.src = h.layout(h.mc, h.vc);
     a.out = h.vals[vo].p;
     a.gamma = h.gamma;
+    a.keys = h.K();
+    a.nodes = h.nodes();
     start_intr(h, msg);
     if (h.mode == GBLS_MODE_PARITY) launch_filter_parity(a, h.stream);
     else launch_filter_fast(a, h.stream);
@@ -2574,10 +2576,26 @@ int gbls_filter(gbls_handle* h, int filter, int width, float value) {
             }
             break;
         }
-        case GBLS_FILTER_MEAN_CURVATURE:
-        case GBLS_FILTER_FILLET:
-        case GBLS_FILTER_MEDIAN:
-            fail(GBLS_ERR_UNSUPPORTED, "this filter has no device form yet");
+        case GBLS_FILTER_MEAN_CURVATURE:  // Filter::meanCurvature :283-293
+        case GBLS_FILTER_FILLET: {        // Filter::fillet :295-303
+            FilterArgs a{};
+            a.op = filter == GBLS_FILTER_FILLET ? FILTER_FILLET : FILTER_MEAN_CURVATURE;
+            a.dt = (dx * dx) / 3.0f;
+            a.inv2dx = float(0.5 / double(dx));  // CurvatureStencil(grid, dx)
+            a.invdx2 = float(4.0 * double(a.inv2dx) * double(a.inv2dx));
+            filter_pass(*h, a, filter == GBLS_FILTER_FILLET ? "Filleting level set" : "Mean-curvature flow of level set");
+            track(*h);
+            break;
+        }
+        case GBLS_FILTER_MEDIAN: {  // Filter::median :244-253
+            FilterArgs a{};
+            a.op = FILTER_MEDIAN;
+            a.width = std::max(1, width);
+            if (a.width > 3) fail(GBLS_ERR_UNSUPPORTED, "median widths above 3 voxels exceed the device stencil halo");
+            filter_pass(*h, a, "Median-value flow of level set");
+            track(*h);
+            break;
+        }
         default:
             fail(GBLS_ERR_VALUE, "unknown filter");
         }

@@ -146,7 +146,10 @@ void launch_cfl(const CflArgs& a, cudaStream_t s) {
 
 void launch_filter_fast(const FilterArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    filter_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    if (a.op >= FILTER_MEAN_CURVATURE)
+        filter_full_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    else
+        filter_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 }  // namespace gbls

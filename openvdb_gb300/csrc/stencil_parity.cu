@@ -31,7 +31,10 @@ void launch_morph_stage_parity(const MorphArgs& a, cudaStream_t s) {
 
 void launch_filter_parity(const FilterArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    filter_kernel<ParityArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    if (a.op >= FILTER_MEAN_CURVATURE)
+        filter_full_kernel<ParityArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    else
+        filter_kernel<ParityArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 }  // namespace gbls

@@ -301,8 +301,8 @@ class LevelSetAdvection:
 class LevelSetFilter(LevelSetTracker):
     """tools::LevelSetFilter<FloatGrid> (tools/LevelSetFilter.h:47-160): filters
     on a DeviceLevelSet, each followed by track() with this tracker's state.
-    Masks (the optional alpha-mask argument) and the meanCurvature, fillet and
-    median filters have no device form (NotImplementedError / GBLS status)."""
+    Masks (the optional alpha-mask argument) have no device form
+    (NotImplementedError); widths above 3 are refused (GBLS status)."""
 
     def _filter(self, op, width=1, value=0.0, mask=None):
         if mask is not None:

@@ -182,7 +182,8 @@ MORPH_CASES = {
 
 # LevelSetFilter (tools/LevelSetFilter.h): filters applied in sequence to one
 # fixture; each op is (filter, width, value) with filter 0 laplacian, 1 mean,
-# 2 gaussian, 3 offset; tracker schemes as (spatial, temporal, normCount).
+# 2 gaussian, 3 offset, 4 meanCurvature, 5 fillet, 6 median; tracker schemes
+# as (spatial, temporal, normCount).
 FILTER_CASES = {
     "filter_sphere_ops": dict(
         fixture=("sphere", 14.0, (0.5, -1.0, 2.0), 1.0, 3.0),
@@ -193,6 +194,18 @@ FILTER_CASES = {
         fixture=("torus", 14.0, 4.0, (0.0, 0.0, 0.0)),
         tracker=(HJ, RK2, 1),
         ops=[(0, 1, 0.0), (0, 1, 0.0), (2, 1, 0.0), (3, 1, 0.4)],
+    ),
+    # 4 meanCurvature, 5 fillet, 6 median(width): stencils with edge and
+    # corner neighbours
+    "filter_curvature_median": dict(
+        fixture=("sphere", 12.0, (1.5, -2.0, 0.5), 1.0, 3.0),
+        tracker=(HJ, RK1, 3),
+        ops=[(4, 1, 0.0), (6, 1, 0.0), (4, 1, 0.0), (5, 1, 0.0), (6, 2, 0.0), (6, 3, 0.0)],
+    ),
+    "filter_torus_fillet": dict(
+        fixture=("torus", 14.0, 4.5, (0.5, 0.0, -0.5)),
+        tracker=(HJ, RK1, 1),
+        ops=[(5, 1, 0.0), (5, 1, 0.0), (4, 1, 0.0), (6, 1, 0.0), (5, 1, 0.0)],
     ),
 }
 
