@@ -897,6 +897,7 @@ void normalize_pass(gbls_handle& h, const uint64_t* pmask, int trim, int carry =
     const float mdt = dx * (h.tr_temporal == GBLS_TVD_RK1 ? 0.3f : h.tr_temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f);
     const float invdx = 1.0f / dx;
     NormArgs base{};
+    base.spatial = h.tr_spatial;
     base.nleaf = h.nleaf;
     base.slot = h.S();
     base.nbr = h.nbr.p;
@@ -1114,8 +1115,6 @@ void check_scheme(int spatial, int temporal) {
         fail(GBLS_ERR_VALUE, "Spatial difference scheme not supported!");
     if (temporal < GBLS_TVD_RK1 || temporal > GBLS_TVD_RK3)
         fail(GBLS_ERR_VALUE, "Temporal integration scheme not supported!");
-    if (spatial != GBLS_HJWENO5_BIAS)
-        fail(GBLS_ERR_UNSUPPORTED, "the device path implements the HJWENO5_BIAS spatial scheme");
 }
 
 // Device form of a field for level set h at time t.  A dense field whose
@@ -1225,8 +1224,9 @@ void rk_stage(gbls_handle& h, const RkArgs& a) {
 }
 
 // The TVD-RK stages of one substep (tools/LevelSetAdvect.h:360-405).
-void advect_stages(gbls_handle& h, const gbls_field* f, int temporal, float t0, float dt, bool backward) {
+void advect_stages(gbls_handle& h, const gbls_field* f, int spatial, int temporal, float t0, float dt, bool backward) {
     RkArgs base{};
+    base.spatial = spatial;
     base.nleaf = h.nleaf;
     base.keys = h.K();
     base.slot = h.S();
@@ -1290,8 +1290,9 @@ LookupGrid lookup_grid(gbls_handle& g) {
 // The RK stages of one morphing substep (Morph::advect, LevelSetMorph.h:
 // 479-510): euler01 / euler12 / euler34 / euler13 over the same buffers as
 // the advection stages.
-void morph_stages(gbls_handle& h, int temporal, float dt) {
+void morph_stages(gbls_handle& h, int spatial, int temporal, float dt) {
     MorphArgs base{};
+    base.spatial = spatial;
     base.nleaf = h.nleaf;
     base.slot = h.S();
     base.nbr = h.nbr.p;
@@ -2317,7 +2318,7 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
             h->stats.voxel_updates += upd;
             h->stats.substeps += uint64_t(nrun);
             h->nactive = int64_t(upd);  // the RK stages' algorithmic bytes count the running instances
-            advect_stages(*h, nullptr, temporal, t0, 0.0f, !forward);
+            advect_stages(*h, nullptr, spatial, temporal, t0, 0.0f, !forward);
             h->nactive = -1;
             for (int i = 0; i < n; ++i) {
                 if (!run[size_t(i)]) continue;
@@ -2498,12 +2499,12 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             ++h->stats.substeps;
             if (h->tape_on) {
                 if (temporal != GBLS_TVD_RK3 || h->tr_temporal != GBLS_TVD_RK1 || h->norm_count != 1 ||
-                    h->trim != GBLS_TRIM_ALL)
-                    fail(GBLS_ERR_UNSUPPORTED, "the adjoint records TVD_RK3 advection with a TVD_RK1 tracker, "
-                                               "normCount 1 and full trimming");
+                    h->trim != GBLS_TRIM_ALL || spatial != GBLS_HJWENO5_BIAS || h->tr_spatial != GBLS_HJWENO5_BIAS)
+                    fail(GBLS_ERR_UNSUPPORTED, "the adjoint records HJWENO5 TVD_RK3 advection with an HJWENO5 "
+                                               "TVD_RK1 tracker, normCount 1 and full trimming");
                 tape_begin_substep(*h, t0, dt, !forward);
             }
-            advect_stages(*h, field, temporal, t0, dt, !forward);
+            advect_stages(*h, field, spatial, temporal, t0, dt, !forward);
             t0 += forward ? dt : -dt;
             ++count;
             const bool more = forward ? t0 < t1 : t0 > t1;
@@ -2622,6 +2623,9 @@ int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int
         DeviceGuard g(h->device);
         check_scheme(spatial, temporal);
         check_scheme(h->tr_spatial, h->tr_temporal);
+        // LevelSetMorphing::advect accepts FIRST_BIAS and HJWENO5_BIAS only (:243-262)
+        if (spatial != GBLS_FIRST_BIAS && spatial != GBLS_HJWENO5_BIAS)
+            fail(GBLS_ERR_VALUE, "Spatial difference scheme not supported!");
         if (h->ninst > 1 || target->ninst > 1 || (alpha_mask && alpha_mask->ninst > 1))
             fail(GBLS_ERR_UNSUPPORTED, "morphing works on single level sets, not batches");
         if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "the adjoint records advection only");
@@ -2652,7 +2656,7 @@ int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int
             if (h->nactive < 0) h->nactive = active_count(*h);
             h->stats.voxel_updates += uint64_t(h->nactive);
             ++h->stats.substeps;
-            morph_stages(*h, temporal, dt);
+            morph_stages(*h, spatial, temporal, dt);
             t0 += dt;
             ++count;
             track(*h);

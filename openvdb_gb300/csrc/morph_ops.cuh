@@ -41,6 +41,7 @@ struct MorphSpeedArgs {
 };
 
 struct MorphArgs {
+    int spatial;            // FIRST_BIAS or HJWENO5_BIAS
     int64_t nleaf;
     const int32_t* slot;
     const int32_t* nbr;
@@ -159,9 +160,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) morph_stage_kernel(const Morp
             float up[3], down[3];
 #pragma unroll
             for (int ax = 0; ax < 3; ++ax) {
-                const Diff6 D = line_diffs<A>(tile_line(tile, x, y, z, ax));
-                up[ax] = diff_fd<A>(D);
-                down[ax] = diff_bd<A>(D);
+                const Line7 L = tile_line(tile, x, y, z, ax);
+                up[ax] = scheme_fd<A>(L, a.spatial);
+                down[ax] = scheme_bd<A>(L, a.spatial);
             }
             const float g2 = A::mul(a.invdxdx, godunov<A>(c > 0.0f, down, up));
             const float vv = A::sub(c, A::mul(A::mul(a.dt, sp), g2));

@@ -7,14 +7,18 @@
 
 namespace gbls {
 
+// The packed FP32x2 kernels evaluate HJ-WENO5; other schemes run the scalar ones.
 void launch_rk_fast(const RkArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    rk_stage_kernel_x2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    if (a.spatial == 4)
+        rk_stage_kernel_x2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    else
+        rk_stage_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 void launch_norm_fast(const NormArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    if (!a.copy_only && !a.has_phi)
+    if (!a.copy_only && !a.has_phi && a.spatial == 4)
         normalize_kernel_x2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
     else
         normalize_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);

@@ -176,6 +176,50 @@ __device__ __forceinline__ float line_bd(const Line7& L) {
     return hj_bd<A>(L.v[0], L.v[1], L.v[2], L.v[3], L.v[4], L.v[5]);
 }
 
+// The other biased schemes (math/FiniteDifference.h D1<FD_1ST> .. D1<BD_WENO5>,
+// :702-1375, selected by BIAS_SCHEME, math/Operators.h:139-186) from the
+// values S(-3..3) of a line, operation by operation.  FD_3RD evaluates in
+// double with explicit rounding.
+__device__ __forceinline__ float fd3(float xp3, float xp2, float xp1, float xp0) {
+    const double a = __dsub_rn(__ddiv_rn(double(xp3), 3.0), __dmul_rn(1.5, double(xp2)));
+    const double b = __dadd_rn(a, __dmul_rn(3.0, double(xp1)));
+    return __double2float_rn(__dsub_rn(b, __ddiv_rn(__dmul_rn(11.0, double(xp0)), 6.0)));
+}
+template <class A>
+__device__ __forceinline__ float fd2(float xp2, float xp1, float xp0) {
+    return A::sub(A::mul(2.0f, xp1), A::add(A::mul(0.5f, xp2), A::mul(1.5f, xp0)));
+}
+template <class A>
+__device__ inline float scheme_fd(const Line7& L, int scheme) {
+    const float* v = L.v;
+    switch (scheme) {
+    case 0: return A::sub(v[4], v[3]);                                   // FD_1ST
+    case 1: return fd2<A>(v[5], v[4], v[3]);                             // FD_2ND
+    case 2: return fd3(v[6], v[5], v[4], v[3]);                          // FD_3RD
+    case 3: return A::sub(A::weno5(v[6], v[5], v[4], v[3], v[2]),       // FD_WENO5
+                          A::weno5(v[5], v[4], v[3], v[2], v[1]));
+    default: return diff_fd<A>(line_diffs<A>(L));                        // FD_HJWENO5
+    }
+}
+template <class A>
+__device__ inline float scheme_bd(const Line7& L, int scheme) {
+    const float* v = L.v;
+    switch (scheme) {
+    case 0: return -A::sub(v[2], v[3]);                                  // BD_1ST = -FD_1ST(xm1, xm0)
+    case 1: return -fd2<A>(v[1], v[2], v[3]);                            // BD_2ND
+    case 2: return -fd3(v[0], v[1], v[2], v[3]);                         // BD_3RD
+    case 3: return -A::sub(A::weno5(v[0], v[1], v[2], v[3], v[4]),      // BD_WENO5
+                           A::weno5(v[1], v[2], v[3], v[4], v[5]));
+    default: return diff_bd<A>(line_diffs<A>(L));                        // BD_HJWENO5
+    }
+}
+// ISGradientBiased per axis: V < 0 ? FD : BD (math/Operators.h:195-226).
+template <class A>
+__device__ __forceinline__ float scheme_upwind(const Line7& L, bool fd, int scheme) {
+    if (scheme == 4) return line_upwind<A>(L, fd);
+    return fd ? scheme_fd<A>(L, scheme) : scheme_bd<A>(L, scheme);
+}
+
 // std::max / std::min as used by math::Max / math::Min.
 __device__ __forceinline__ float ref_max(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float ref_min(float a, float b) { return (b < a) ? b : a; }
@@ -292,6 +336,7 @@ __device__ __forceinline__ void eval_field(const FieldParams& f, int i, int j, i
 
 // ---- kernel arguments -------------------------------------------------------
 struct RkArgs {
+    int spatial;           // BiasedGradientScheme (GBLS_*_BIAS)
     int64_t nleaf;
     const uint64_t* keys;
     const int32_t* slot;
@@ -315,6 +360,7 @@ struct RkArgs {
 };
 
 struct NormArgs {
+    int spatial;            // tracker BiasedGradientScheme
     int64_t nleaf;
     const int32_t* slot;
     const int32_t* nbr;
@@ -442,7 +488,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             const Line7 L = tile_line(tile, x, y, z, ax);
-            g[ax] = A::ijt(line_upwind<A>(L, vel[ax] < 0.0f), a.invdx, a.invdx_f);
+            g[ax] = A::ijt(scheme_upwind<A>(L, vel[ax] < 0.0f, a.spatial), a.invdx, a.invdx_f);
         }
         const float dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
         const float c = tile[tile_index(x, y, z)];
@@ -506,9 +552,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
             float up[3], down[3];
 #pragma unroll
             for (int ax = 0; ax < 3; ++ax) {
-                const Diff6 D = line_diffs<A>(tile_line(tile, x, y, z, ax));
-                up[ax] = diff_fd<A>(D);
-                down[ax] = diff_bd<A>(D);
+                const Line7 L = tile_line(tile, x, y, z, ax);
+                up[ax] = scheme_fd<A>(L, a.spatial);
+                down[ax] = scheme_bd<A>(L, a.spatial);
             }
             const float nsq = godunov<A>(phi0 > 0.0f, down, up);
             float vv = A::div(phi0, A::add(A::sqrt(A::add(A::mul(phi0, phi0), nsq)), 1e-8f));

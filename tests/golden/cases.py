@@ -113,6 +113,36 @@ CASES = {
         schemes=(HJ, RK2, HJ, RK1, 3),
         ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
     ),
+    # the other biased schemes for advection and tracker (the oracle's C++
+    # restatement implements HJWENO5 only: port=False)
+    "sphere12_first_bias": dict(
+        fixture=("sphere", 12.0, (0.0, 1.0, 2.0), 1.0, 3.0),
+        field=("constant", (-0.7, 0.4, 1.1)),
+        schemes=(0, RK1, 0, RK1, 3),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+        port=False,
+    ),
+    "sphere12_second_bias": dict(
+        fixture=("sphere", 12.0, (0.0, 1.0, 2.0), 1.0, 3.0),
+        field=("rotation", (0.3, -0.2, 0.1), (0.02, -0.03, 0.05), (0.0, 1.0, 2.0)),
+        schemes=(1, RK2, 1, RK1, 2),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+        port=False,
+    ),
+    "sphere12_third_bias": dict(
+        fixture=("sphere", 12.0, (0.0, 1.0, 2.0), 1.0, 3.0),
+        field=("constant", (0.6, -0.9, 0.2)),
+        schemes=(2, RK3, 2, RK2, 1),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+        port=False,
+    ),
+    "sphere12_weno5_bias": dict(
+        fixture=("sphere", 12.0, (0.0, 1.0, 2.0), 1.0, 3.0),
+        field=("dense", 32, 4.0, 1.0, 11),
+        schemes=(3, RK3, 3, RK3, 1),
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+        port=False,
+    ),
     "sphere_half_voxel": dict(
         fixture=("sphere", 6.0, (0.25, -0.5, 1.0), 0.5, 3.0),
         field=("constant", (0.5, 0.25, -0.3)),
@@ -169,6 +199,12 @@ MORPH_CASES = {
         target=("torus", 14.0, 5.0, (0.5, -0.5, 0.0)),
         schemes=(HJ, RK3, HJ, RK1, 1),
         ops=[("morph", 0.0, 1.0), ("morph", 1.0, 2.0), ("morph", 2.0, 3.0)],
+    ),
+    "morph_first_bias_rk3": dict(
+        source=("sphere", 11.0, (0.0, 0.0, 0.0), 1.0, 3.0),
+        target=("sphere", 13.0, (1.0, -1.0, 0.5), 1.0, 3.0),
+        schemes=(0, RK3, 0, RK1, 2),
+        ops=[("morph", 0.0, 1.0), ("morph", 1.0, 2.0)],
     ),
     "morph_masked_rk1": dict(
         source=("sphere", 14.0, (0.0, 0.0, 0.0), 1.0, 3.0),
