@@ -17,9 +17,8 @@
 //   advection.setNormCount(1);
 //   size_t substeps = advection.advect(0.0f, 1.0f);
 //
-// Differences: the HJWENO5_BIAS spatial scheme only (others throw
-// NotImplementedError); setCFL() is an addition (0, the default, keeps the
-// reference's CFL number of the temporal scheme).
+// Difference: setCFL() is an addition (0, the default, keeps the reference's
+// CFL number of the temporal scheme).
 #pragma once
 
 #include <openvdb/tools/LevelSetAdvect.h>

@@ -6,8 +6,8 @@
 // alpha mask (level sets with the source's transform), runs the CFL loop on
 // the device (speed sampling, RK stages, tracker pass per substep) and writes
 // the result back into the source grid's tree; it returns the number of CFL
-// substeps.  Differences: HJWENO5_BIAS only; a target or mask whose transform
-// differs from the source's (trilinear sampling) throws NotImplementedError.
+// substeps.  Difference: a target or mask whose transform differs from the
+// source's (trilinear sampling) throws NotImplementedError.
 //
 //   openvdb_gb300::tools::LevelSetMorphing<openvdb::FloatGrid> morph(*source, *target);
 //   morph.setTemporalScheme(openvdb::math::TVD_RK3);
