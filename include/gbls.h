@@ -107,6 +107,7 @@ typedef struct gbls_grid_counts {
     int64_t upper_count;
     int64_t root_tile_count;
     int64_t active_voxel_count;
+    float background;           /* current background (dilate / erode / resize change it) */
 } gbls_grid_counts;
 
 /* ---- velocity fields ----------------------------------------------------

@@ -59,6 +59,7 @@ class GridCounts(C.Structure):
         ("upper_count", C.c_int64),
         ("root_tile_count", C.c_int64),
         ("active_voxel_count", C.c_int64),
+        ("background", C.c_float),
     ]
 
 

@@ -1784,6 +1784,7 @@ int gbls_get_counts(gbls_handle* h, gbls_grid_counts* out) {
         out->upper_count = int64_t(h->upper_keys_h.size());
         out->root_tile_count = int64_t(h->root_keys_h.size());
         out->active_voxel_count = active_count(*h);
+        out->background = h->gamma;
     });
 }
 
@@ -2183,6 +2184,7 @@ int gbls_batch_get_counts(gbls_handle* h, int32_t instance, gbls_grid_counts* ou
         out->upper_count = R.u1 - R.u0;
         out->root_tile_count = R.r1 - R.r0;
         out->active_voxel_count = 0;
+        out->background = h->gamma;
         if (R.l1 > R.l0) {
             h->u64s.reserve(1, h->stream);
             CU(cudaMemsetAsync(h->u64s.p, 0, sizeof(unsigned long long), h->stream));

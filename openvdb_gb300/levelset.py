@@ -195,7 +195,8 @@ class LevelSetTracker:
         return np.float32(self._grid.voxel_size)
 
     def getHalfWidth(self):
-        return float(np.float32(self._grid.background) / np.float32(self._grid.voxel_size))
+        # background / dx in float, with the device's current background
+        return float(np.float32(self._grid.counts().background) / np.float32(self._grid.voxel_size))
 
     def grid(self):
         return self._grid
