@@ -82,10 +82,10 @@ __device__ __forceinline__ void scatter_add(const LeafStage& st, float* lam, int
     else if (z < 0) { r = 5; z += 8; }
     else if (z >= 8) { r = 6; z -= 8; }
     const int v = (x << 6) | (y << 3) | z;
-    const int w = v >> 6, b = v & 63;
-    const uint64_t m = st.am[r][w];
-    if (!((m >> b) & 1)) return;
-    const int rank = st.pre[r][w] + __popcll(m & ((uint64_t(1) << b) - 1));
+    const uint4 q = st.rec[r][v >> 5];  // half word (v >> 6, (v >> 5) & 1)
+    const int bb = v & 31;
+    if (!((q.x >> bb) & 1)) return;
+    const uint32_t rank = q.z + uint32_t(__popc(q.x & ((1u << bb) - 1u)));
     atomicAdd(lam + size_t(st.slot[r]) * LEAF_VOX + rank, val);
 }
 

@@ -551,6 +551,10 @@ struct gbls_handle {
         if (nfree >= need) return;
         const int64_t old = slot_cap;
         int64_t nc = std::max(old + (need - nfree), int64_t(double(old) * 1.5) + 1024);
+        // the stencil staging records address values by the 32-bit offset slot*512
+        constexpr int64_t kMaxSlots = int64_t(1) << 23;
+        if (old + (need - nfree) > kMaxSlots) fail(GBLS_ERR_OUT_OF_MEMORY, "more than 2^23 leaves in one handle");
+        nc = std::min(nc, kMaxSlots);
         for (int b = 0; b < 3; ++b) {
             am[b].reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
             sm[b].reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);

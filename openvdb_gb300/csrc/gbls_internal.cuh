@@ -171,13 +171,16 @@ __device__ __forceinline__ int tile_index(int x, int y, int z) {
     return (x + 3) * (TILE_DIM * TILE_DIM) + (y + 3) * TILE_DIM + (z + 3);
 }
 
-// Per-CTA staging of the masks of a leaf and its 6 face neighbours.
+// Per-CTA staging of a leaf and its 6 face neighbours.
 struct LeafStage {
-    uint64_t am[7][8];
-    uint64_t sm[7][8];
-    int pre[7][9];
-    int preh[7][16];       // rank of the first voxel of each 32-bit half word
-    const float* vp[7];    // packed values of each staged leaf (null for a tile)
+    uint64_t am[1][8];     // active mask of the centre leaf
+    uint64_t sm[1][8];     // sign mask of the centre leaf
+    // One 16-byte record per staged leaf r (0 = centre, 1..6 = -x,+x,-y,+y,
+    // -z,+z) and 32-bit half word: active half mask, sign half mask, rank of
+    // the half's first voxel, and the offset slot*512 of the leaf's values
+    // (0 for a tile).  A tile element is staged from one record load.
+    uint4 rec[7][16];
+    const float* vb;       // the layout's value array (rec offsets are relative to it)
     int slot[7];
 };
 
@@ -187,17 +190,18 @@ struct LeafStage {
 constexpr int STAGE_THREADS = 64;
 
 // Stage the masks of a leaf (slot s) and of its face neighbours nb[6] from
-// layout L, with per-word and per-half-word prefix counts.  Threads 56..63
+// layout L as half-word records.  Threads 56..63
 // load pm[8] (the processed-voxel mask of the centre) when pmask is given.
 // Ends with a barrier.
 __device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const int32_t* nb,
                                    const uint64_t* pmask, uint64_t* pm) {
     const int t = threadIdx.x;
     uint32_t clo = 0, c = 0;
+    int sl = 0;
+    uint64_t a = 0, g = 0;
     if (t < 56) {
         const int r = t >> 3, w = t & 7;
-        const int sl = (r == 0) ? s : nb[r - 1];
-        uint64_t a, g;
+        sl = (r == 0) ? s : nb[r - 1];
         if (sl >= 0) {
             a = L.amask[size_t(sl) * 8 + w];
             g = L.smask[size_t(sl) * 8 + w];
@@ -205,12 +209,11 @@ __device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const 
             a = 0;
             g = (sl == NBR_TILE_NEG) ? ~uint64_t(0) : uint64_t(0);
         }
-        st.am[r][w] = a;
-        st.sm[r][w] = g;
-        if (w == 0) {
-            st.slot[r] = sl;
-            st.vp[r] = sl >= 0 ? L.vals + size_t(sl) * LEAF_VOX : nullptr;
+        if (r == 0) {
+            st.am[0][w] = a;
+            st.sm[0][w] = g;
         }
+        if (w == 0) st.slot[r] = sl;
         clo = uint32_t(__popc(uint32_t(a)));
         c = clo + uint32_t(__popc(uint32_t(a >> 32)));
     } else if (pmask) {
@@ -225,41 +228,50 @@ __device__ inline void stage_masks(LeafStage& st, const Layout& L, int s, const 
     }
     if (t < 56) {
         const int r = t >> 3, w = t & 7;
-        st.pre[r][w + 1] = int(v);
-        if (w == 0) st.pre[r][0] = 0;
-        st.preh[r][2 * w] = int(v - c);
-        st.preh[r][2 * w + 1] = int(v - c + clo);
+        const uint32_t base = sl >= 0 ? uint32_t(sl) * uint32_t(LEAF_VOX) : 0u;
+        st.rec[r][2 * w] = make_uint4(uint32_t(a), uint32_t(g), v - c, base);
+        st.rec[r][2 * w + 1] = make_uint4(uint32_t(a >> 32), uint32_t(g >> 32), v - c + clo, base);
+    } else if (t == 56) {
+        st.vb = L.vals;
     }
     __syncthreads();
 }
 
-// Value of bit b of word w of staged leaf r (packed value, else +-gamma).
-__device__ __forceinline__ float staged_load(const LeafStage& st, int r, int w, int b, float gamma) {
-    const int h = b >> 5, bb = b & 31;
-    const uint32_t m = reinterpret_cast<const uint32_t*>(&st.am[r][w])[h];
-    if ((m >> bb) & 1) return __ldg(st.vp[r] + st.preh[r][2 * w + h] + __popc(m & ((1u << bb) - 1u)));
-    const uint32_t g = reinterpret_cast<const uint32_t*>(&st.sm[r][w])[h];
-    return ((g >> bb) & 1) ? -gamma : gamma;
+// Value of bit bb of the half word whose record is q (packed value, else
+// +-gamma by the sign bit).
+__device__ __forceinline__ float record_load(const uint4 q, int bb, const float* vb, float gamma) {
+    const float inactive = ((q.y >> bb) & 1) ? -gamma : gamma;
+    if ((q.x >> bb) & 1) return __ldg(vb + (q.w + q.z + uint32_t(__popc(q.x & ((1u << bb) - 1u)))));
+    return inactive;
 }
 
 // Fill the 14^3 tile (centre block + three-voxel face slabs).  Thread t
 // handles bit t of each centre word and the (t>>3, t&7) column of every slab
-// layer; all 26 loads of a thread are independent.  Requires
-// blockDim.x == STAGE_THREADS.  No barrier at the end.
+// layer; all 26 loads of a thread are independent, and each reads its mask
+// bits and rank from one 16-byte half-word record (18 distinct records per
+// thread).  Requires blockDim.x == STAGE_THREADS.  No barrier at the end.
 __device__ inline void load_tile(float* tile, const LeafStage& st, float gamma) {
     const int t = threadIdx.x;
-    const int a = t >> 3, c = t & 7;
+    const int a = t >> 3, c = t & 7, h = t >> 5, bt = t & 31;
+    const float* vb = st.vb;
     float cv[8], fv[18];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) cv[k] = staged_load(st, 0, k, t, gamma);
+    for (int k = 0; k < 8; ++k) cv[k] = record_load(st.rec[0][2 * k + h], bt, vb, gamma);
+    {
+        // -y: bits (5+d)<<3|c of word a (high half); +y: bits d<<3|c (low half);
+        // -z: bits c<<3|(5+d) and +z: bits c<<3|d (half c>>2)
+        const uint4 qmy = st.rec[3][2 * a + 1], qpy = st.rec[4][2 * a];
+        const uint4 qmz = st.rec[5][2 * a + (c >> 2)], qpz = st.rec[6][2 * a + (c >> 2)];
+        const int zb = (c & 3) << 3;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        fv[0 * 3 + d] = staged_load(st, 1, 5 + d, t, gamma);                 // -x: (5+d, a, c)
-        fv[1 * 3 + d] = staged_load(st, 2, d, t, gamma);                     // +x: (d, a, c)
-        fv[2 * 3 + d] = staged_load(st, 3, a, ((5 + d) << 3) | c, gamma);    // -y: (a, 5+d, c)
-        fv[3 * 3 + d] = staged_load(st, 4, a, (d << 3) | c, gamma);          // +y: (a, d, c)
-        fv[4 * 3 + d] = staged_load(st, 5, a, (c << 3) | (5 + d), gamma);    // -z: (a, c, 5+d)
-        fv[5 * 3 + d] = staged_load(st, 6, a, (c << 3) | d, gamma);          // +z: (a, c, d)
+        for (int d = 0; d < 3; ++d) {
+            fv[0 * 3 + d] = record_load(st.rec[1][2 * (5 + d) + h], bt, vb, gamma);  // -x: (5+d, a, c)
+            fv[1 * 3 + d] = record_load(st.rec[2][2 * d + h], bt, vb, gamma);        // +x: (d, a, c)
+            fv[2 * 3 + d] = record_load(qmy, ((5 + d) << 3 | c) & 31, vb, gamma);     // -y: (a, 5+d, c)
+            fv[3 * 3 + d] = record_load(qpy, (d << 3) | c, vb, gamma);                // +y: (a, d, c)
+            fv[4 * 3 + d] = record_load(qmz, zb | (5 + d), vb, gamma);                // -z: (a, c, 5+d)
+            fv[5 * 3 + d] = record_load(qpz, zb | d, vb, gamma);                      // +z: (a, c, d)
+        }
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) tile[tile_index(k, a, c)] = cv[k];

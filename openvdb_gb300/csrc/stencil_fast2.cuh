@@ -56,18 +56,25 @@ __device__ __forceinline__ Diff6x2 line_diffs2(const float* tile, int c0, int c1
 __device__ __forceinline__ float2 fd2(const Diff6x2& D) { return weno5x2(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]); }
 __device__ __forceinline__ float2 bd2(const Diff6x2& D) { return weno5x2(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]); }
 
-// FAST RK stage on voxel pairs (same semantics as rk_stage_kernel<FastArith>).
-__global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkArgs a) {
+// FAST RK stage on voxel pairs (the semantics of rk_stage_kernel<FastArith>).
+// The field is read through a pointer (the launch parameter, or a batch
+// instance's entry) instead of a shared copy.  For the deformation field the
+// leaf's factors are staged once: u = Xu[x] Yu[y] Zu[z], v = Xv[x] Yv[y] Zu[z],
+// w = Xv[x] Yu[y] Zw[z] with Xu = 2 amp sin^2(pi x), Xv = -amp sin(2 pi x),
+// Yu = sin(2 pi y), Yv = sin^2(pi y), Zu = sin(2 pi z), Zw = sin^2(pi z)
+// (amp negated for backward time), so a voxel pair costs six packed products.
+// At most 64 registers per thread keep 16 CTAs resident per SM.
+__global__ void __launch_bounds__(STENCIL_THREADS, 16) rk_stage_kernel_x2(const __grid_constant__ RkArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ uint16_t list[LEAF_VOX];
     __shared__ float vtab[6][8];
-    __shared__ FieldParams sf;
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
     const uint64_t key = a.keys[l];
     float dt = a.dt, t0 = a.t0;
+    const FieldParams* fp = &a.field;
     if (a.inst_run) {
         const uint32_t inst = key_instance(key);
         if (!a.inst_run[inst]) {
@@ -81,27 +88,31 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkAr
         }
         dt = a.inst_dt[inst];
         t0 = a.inst_t0[inst];
-        if (threadIdx.x == 0) sf = a.inst_field[inst];
-    } else if (threadIdx.x == 0) {
-        sf = a.field;
+        fp = a.inst_field + inst;
     }
-    stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
-    load_tile(tile, st, a.gamma);
-    const int n = build_list(list, st.am[0]);
-    __syncthreads();
+    const FieldParams& sf = *fp;
     int ox, oy, oz;
     key_origin(key, ox, oy, oz);
     const bool tabbed = sf.kind == 2 && sf.tab && ox - sf.tab_lo >= 0 && oy - sf.tab_lo >= 0 &&
                         oz - sf.tab_lo >= 0 && ox + 8 - sf.tab_lo <= sf.tab_n &&
                         oy + 8 - sf.tab_lo <= sf.tab_n && oz + 8 - sf.tab_lo <= sf.tab_n;
-    if (tabbed) {
-        if (threadIdx.x < 48) {
-            const int ax = threadIdx.x >> 4, fn = (threadIdx.x >> 3) & 1, q = threadIdx.x & 7;
-            const int o = ax == 0 ? ox : ax == 1 ? oy : oz;
-            vtab[ax * 2 + fn][q] = sf.tab[2 * (o + q - sf.tab_lo) + fn];
+    if (tabbed && threadIdx.x >= 40) {
+        const int ax = (threadIdx.x - 40) >> 3, q = threadIdx.x & 7;
+        const int o = (ax == 0 ? ox : ax == 1 ? oy : oz) + q - sf.tab_lo;
+        const float sn = sf.tab[2 * o], s2 = sf.tab[2 * o + 1];
+        const float amp = a.backward ? -sf.amp : sf.amp;
+        if (ax == 0) {
+            vtab[0][q] = 2.0f * amp * sn * sn;
+            vtab[1][q] = -amp * s2;
+        } else {
+            vtab[2 * ax][q] = s2;
+            vtab[2 * ax + 1][q] = sn * sn;
         }
-        __syncthreads();
     }
+    stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
+    load_tile(tile, st, a.gamma);
+    const int n = build_list(list, st.am[0]);
+    __syncthreads();
     const int npairs = (n + 1) >> 1;
     const float2 dt2 = f2(dt), invdx2 = f2(a.invdx_f);
     for (int p = threadIdx.x; p < npairs; p += STENCIL_THREADS) {
@@ -111,23 +122,19 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkAr
         const int x1 = v1 >> 6, y1 = (v1 >> 3) & 7, z1 = v1 & 7;
         float ve0[3], ve1[3];
         if (tabbed) {
-            const float2 sx = make_float2(vtab[0][x0], vtab[0][x1]), s2x = make_float2(vtab[1][x0], vtab[1][x1]);
-            const float2 sy = make_float2(vtab[2][y0], vtab[2][y1]), s2y = make_float2(vtab[3][y0], vtab[3][y1]);
-            const float2 sz = make_float2(vtab[4][z0], vtab[4][z1]), s2z = make_float2(vtab[5][z0], vtab[5][z1]);
-            const float2 amp = f2(sf.amp);
-            const float2 u = mul2(mul2(mul2(mul2(f2(2.0f), sx), sx), s2y), s2z);
-            const float2 w = mul2(mul2(mul2(s2x, sy), sy), s2z);
-            const float2 q = mul2(mul2(mul2(s2x, s2y), sz), sz);
-            const float2 a0 = mul2(u, amp), a1 = mul2(w, amp), a2 = mul2(q, amp);
-            ve0[0] = a0.x; ve1[0] = a0.y;
-            ve0[1] = -a1.x; ve1[1] = -a1.y;
-            ve0[2] = -a2.x; ve1[2] = -a2.y;
+            const float2 xu = make_float2(vtab[0][x0], vtab[0][x1]), xv = make_float2(vtab[1][x0], vtab[1][x1]);
+            const float2 yu = make_float2(vtab[2][y0], vtab[2][y1]), yv = make_float2(vtab[3][y0], vtab[3][y1]);
+            const float2 zu = make_float2(vtab[4][z0], vtab[4][z1]), zw = make_float2(vtab[5][z0], vtab[5][z1]);
+            const float2 u = mul2(mul2(xu, yu), zu), v = mul2(mul2(xv, yv), zu), w = mul2(mul2(xv, yu), zw);
+            ve0[0] = u.x; ve1[0] = u.y;
+            ve0[1] = v.x; ve1[1] = v.y;
+            ve0[2] = w.x; ve1[2] = w.y;
         } else {
             eval_field(sf, ox + x0, oy + y0, oz + z0, t0, ve0);
             eval_field(sf, ox + x1, oy + y1, oz + z1, t0, ve1);
-        }
-        if (a.backward) {
-            for (int k = 0; k < 3; ++k) { ve0[k] = -ve0[k]; ve1[k] = -ve1[k]; }
+            if (a.backward) {
+                for (int k = 0; k < 3; ++k) { ve0[k] = -ve0[k]; ve1[k] = -ve1[k]; }
+            }
         }
         const int c0 = tile_index(x0, y0, z0), c1 = tile_index(x1, y1, z1);
         float2 dot = f2(0.0f);
@@ -157,7 +164,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel_x2(const RkAr
 // FAST renormalisation stage (RK1 form, no convex combination) on voxel
 // pairs, with trimming: same semantics as normalize_kernel<FastArith> for
 // has_phi == 0 and copy_only == 0.
-__global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel_x2(const NormArgs a) {
+__global__ void __launch_bounds__(STENCIL_THREADS, 16) normalize_kernel_x2(const __grid_constant__ NormArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ float res[LEAF_VOX];
