@@ -6,6 +6,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <functional>
 #include <memory>
@@ -134,10 +135,12 @@ __global__ void k_emit_candidates(int64_t n, const uint64_t* keys, const int32_t
 
 // Give the sorted unique new leaves their slots; their masks start empty and
 // every voxel takes the tile value (tree/InternalNode.h:2874-2876).
-__global__ void k_new_leaves(int64_t n, const uint64_t* cand, const int32_t* free_slots,
-                             int64_t nfree, uint64_t* new_keys, int32_t* new_slots, uint64_t* am,
-                             uint64_t* sm) {
+// The count is n, or *n_dev when n_dev is set (launched for a capacity).
+__global__ void k_new_leaves(int64_t n, const unsigned long long* n_dev, const uint64_t* cand,
+                             const int32_t* free_slots, int64_t nfree, uint64_t* new_keys, int32_t* new_slots,
+                             uint64_t* am, uint64_t* sm) {
     const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (n_dev) n = int64_t(*n_dev);
     if (j >= n) return;
     const uint64_t c = cand[j];
     const int32_t s = free_slots[nfree - 1 - j];
@@ -151,9 +154,12 @@ __global__ void k_new_leaves(int64_t n, const uint64_t* cand, const int32_t* fre
 }
 
 // Merge two sorted, disjoint key lists (with their slots) into tree order.
+// nb is *nb_dev when nb_dev is set.
 __global__ void k_merge(int64_t na, const uint64_t* ka, const int32_t* sa, int64_t nb,
-                        const uint64_t* kb, const int32_t* sb, uint64_t* ko, int32_t* so) {
+                        const unsigned long long* nb_dev, const uint64_t* kb, const int32_t* sb, uint64_t* ko,
+                        int32_t* so) {
     const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (nb_dev) nb = int64_t(*nb_dev);
     if (i < na) {
         const int64_t pos = i + lower_bound_u64(kb, nb, ka[i]);
         ko[pos] = ka[i];
@@ -236,13 +242,111 @@ __global__ void k_andnot(int64_t n, const int32_t* slot, uint64_t* m, const uint
 }
 
 // Lower nodes missing for new leaves (rare): append lower keys.
-__global__ void k_missing_lower(int64_t n, const uint64_t* new_keys, const uint64_t* lower_keys,
-                                int64_t nlower, uint64_t* out, unsigned long long* count) {
+__global__ void k_missing_lower(int64_t n, const unsigned long long* n_dev, const uint64_t* new_keys,
+                                const uint64_t* lower_keys, int64_t nlower, uint64_t* out,
+                                unsigned long long* count) {
     const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (n_dev) n = int64_t(*n_dev);
     if (j >= n) return;
     const uint64_t lk = new_keys[j] >> 12;
     if (find_u64(lower_keys, nlower, lk) >= 0) return;
     out[atomicAdd(count, 1ull)] = lk;
+}
+
+// Sorted distinct candidates of one dilation when there are at most
+// SMALL_SORT_CAP of them (the usual case: the 64-sphere workload emits about
+// 12k candidates, 6.6k distinct new leaves per substep): one CTA radix-sorts
+// them in shared memory over the key bits that vary and compacts the
+// distinct values, so the dilation needs no host read of the candidate
+// count.  More candidates set st->overflow and leave the work to the
+// device-wide sort.
+constexpr int SMALL_SORT_THREADS = 1024;
+constexpr int SMALL_SORT_ITEMS = 12;
+constexpr int64_t SMALL_SORT_CAP = int64_t(SMALL_SORT_THREADS) * SMALL_SORT_ITEMS;
+using SmallSort = cub::BlockRadixSort<uint64_t, SMALL_SORT_THREADS, SMALL_SORT_ITEMS>;
+using SmallScan = cub::BlockScan<int, SMALL_SORT_THREADS>;
+union SmallSortStorage {
+    typename SmallSort::TempStorage sort;
+    uint64_t keys[SMALL_SORT_CAP];
+};
+constexpr size_t SMALL_SORT_SMEM = sizeof(SmallSortStorage);
+
+__global__ void __launch_bounds__(SMALL_SORT_THREADS) k_sort_unique_small(const uint64_t* cand, DevStatus* st,
+                                                                          uint64_t* out) {
+    extern __shared__ __align__(16) unsigned char small_sort_smem[];
+    SmallSortStorage& sm = *reinterpret_cast<SmallSortStorage*>(small_sort_smem);
+    __shared__ typename SmallScan::TempStorage scan;
+    __shared__ uint64_t red_or[SMALL_SORT_THREADS / 32], red_and[SMALL_SORT_THREADS / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int64_t n = int64_t(st->n_cand);
+    if (n > SMALL_SORT_CAP) {
+        if (t == 0) {
+            st->overflow = 1;
+            st->n_unique = 0;
+        }
+        return;
+    }
+    uint64_t k[SMALL_SORT_ITEMS];
+    uint64_t vor = 0, vand = ~uint64_t(0);
+#pragma unroll
+    for (int i = 0; i < SMALL_SORT_ITEMS; ++i) {
+        const int64_t idx = int64_t(t) * SMALL_SORT_ITEMS + i;
+        k[i] = idx < n ? cand[idx] : 0;
+        if (idx < n) {
+            vor |= k[i];
+            vand &= k[i];
+        }
+    }
+    // the bits in which the candidates differ
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vor |= __shfl_xor_sync(0xffffffffu, vor, o);
+        vand &= __shfl_xor_sync(0xffffffffu, vand, o);
+    }
+    if (lane == 0) {
+        red_or[warp] = vor;
+        red_and[warp] = vand;
+    }
+    __syncthreads();
+    vor = 0;
+    vand = ~uint64_t(0);
+#pragma unroll 4
+    for (int w = 0; w < SMALL_SORT_THREADS / 32; ++w) {
+        vor |= red_or[w];
+        vand &= red_and[w];
+    }
+    const uint64_t vary = vor ^ vand;
+    const int end_bit = vary ? 64 - __clzll(static_cast<long long>(vary)) : 1;
+    // padding sorts after every candidate on bits [0, end_bit): the common
+    // high bits with every low bit set
+    const uint64_t low = end_bit == 64 ? ~uint64_t(0) : ((uint64_t(1) << end_bit) - 1);
+    const uint64_t pad = (vor & ~low) | low;
+#pragma unroll
+    for (int i = 0; i < SMALL_SORT_ITEMS; ++i)
+        if (int64_t(t) * SMALL_SORT_ITEMS + i >= n) k[i] = pad;
+    SmallSort(sm.sort).Sort(k, 0, end_bit);  // blocked arrangement in and out
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SMALL_SORT_ITEMS; ++i) sm.keys[t * SMALL_SORT_ITEMS + i] = k[i];
+    __syncthreads();
+    // the first n sorted values are the candidates
+    bool head[SMALL_SORT_ITEMS];
+    int cnt = 0;
+#pragma unroll
+    for (int i = 0; i < SMALL_SORT_ITEMS; ++i) {
+        const int idx = t * SMALL_SORT_ITEMS + i;
+        head[i] = idx < n && (idx == 0 || sm.keys[idx] != sm.keys[idx - 1]);
+        cnt += head[i] ? 1 : 0;
+    }
+    int off = 0, total = 0;
+    SmallScan(scan).ExclusiveSum(cnt, off, total);
+#pragma unroll
+    for (int i = 0; i < SMALL_SORT_ITEMS; ++i)
+        if (head[i]) out[off++] = k[i];
+    if (t == 0) {
+        st->n_unique = (unsigned long long)total;
+        st->overflow = 0;
+    }
 }
 
 __global__ void k_keep_flags(int64_t n, const int32_t* cnt, int32_t* keep) {
@@ -429,11 +533,11 @@ struct gbls_handle {
     // node tables: device arrays + host mirrors of keys, upper signs, root tiles
     std::vector<uint64_t> lower_keys_h, upper_keys_h, upper_sign_h, root_keys_h;
     std::vector<uint8_t> root_sign_h;
-    DevArray<uint64_t> lower_keys, lower_sign, upper_keys, upper_sign, root_keys;
+    DevArray<uint64_t> lower_keys, lower_sign, lower_sign_spare, upper_keys, upper_sign, root_keys;
     DevArray<uint8_t> root_sign;
     bool nodes_checked = false;  // empty nodes of the input removed by a prune
     // scratch
-    DevArray<uint64_t> cand, cand_sorted, new_keys;
+    DevArray<uint64_t> cand, cand_sorted, new_keys, miss;
     DevArray<int32_t> new_slots, cnt, keep, idx, remap;
     DevArray<uint8_t> cub_tmp, flags;
     DevArray<int32_t> io_perm;   // upload: staged index of each leaf / lower / upper node
@@ -474,6 +578,14 @@ struct gbls_handle {
     };
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> event_pool;
+    cudaEvent_t sync_ev = nullptr;
+    bool small_sort_ready = false;  // dynamic shared memory of k_sort_unique_small set on this device
+    // Page-locked staging of the tracker's small node-table transfers, so
+    // they are asynchronous copies; pin_ev marks the last copy issued from it.
+    void* pin = nullptr;
+    size_t pin_cap = 0, pin_off = 0;
+    cudaEvent_t pin_ev = nullptr;
+    bool pin_busy = false;
 
     ~gbls_handle() {
         if (st_d) cudaFree(st_d);
@@ -481,6 +593,48 @@ struct gbls_handle {
         if (acc_d) cudaFree(acc_d);
         for (auto& p : pending) { event_pool.push_back(p.a); event_pool.push_back(p.b); }
         for (auto e : event_pool) cudaEventDestroy(e);
+        if (sync_ev) cudaEventDestroy(sync_ev);
+        if (pin_ev) cudaEventSynchronize(pin_ev), cudaEventDestroy(pin_ev);
+        if (pin) cudaFreeHost(pin);
+    }
+
+    // `bytes` of page-locked staging not read by a copy in flight: the next
+    // free part of the staging, else all of it once its copies completed.
+    void* pinned(size_t bytes) {
+        bytes = (bytes + 15) & ~size_t(15);
+        if (pin_busy && pin_off + bytes <= pin_cap) {
+            void* r = static_cast<char*>(pin) + pin_off;
+            pin_off += bytes;
+            return r;
+        }
+        if (pin_busy) {
+            CU(cudaEventSynchronize(pin_ev));
+            pin_busy = false;
+        }
+        if (bytes > pin_cap) {
+            if (pin) CU(cudaFreeHost(pin));
+            pin = nullptr;
+            const size_t nc = std::max<size_t>(std::max(bytes, pin_cap * 2), 65536);
+            CU(cudaHostAlloc(&pin, nc, cudaHostAllocDefault));
+            pin_cap = nc;
+        }
+        pin_off = bytes;
+        return pin;
+    }
+    // Copies from the staging were enqueued: it is reused after they complete.
+    void pinned_issued() {
+        if (!pin_ev) CU(cudaEventCreateWithFlags(&pin_ev, cudaEventDisableTiming));
+        CU(cudaEventRecord(pin_ev, stream));
+        pin_busy = true;
+    }
+    // Copy n elements of a device array to host memory (waits for them).
+    template <class T>
+    void download_small(const DevArray<T>& d, T* out, size_t n) {
+        if (!n) return;
+        T* st = static_cast<T*>(pinned(n * sizeof(T)));
+        CU(cudaMemcpyAsync(st, d.p, n * sizeof(T), cudaMemcpyDeviceToHost, stream));
+        sync();
+        std::memcpy(out, st, n * sizeof(T));
     }
 
     cudaEvent_t event() {
@@ -523,8 +677,24 @@ struct gbls_handle {
     int32_t* S() { return slot[kc].p; }
     Layout layout(int m, int v) const { return Layout{am[m].p, sm[m].p, vals[v].p}; }
 
+    // Wait for the stream.  The tracker's read-backs wait on a few small
+    // kernels, so the host polls an event for up to 2 ms (a blocking wait
+    // returns tens of microseconds after the work ends) and blocks after that.
     void sync() {
-        CU(cudaStreamSynchronize(stream));
+        if (!sync_ev) CU(cudaEventCreateWithFlags(&sync_ev, cudaEventDisableTiming));
+        CU(cudaEventRecord(sync_ev, stream));
+        const auto start = std::chrono::steady_clock::now();
+        for (;;) {
+            const cudaError_t e = cudaEventQuery(sync_ev);
+            if (e == cudaSuccess) break;
+            if (e != cudaErrorNotReady) CU(e);
+            if (std::chrono::steady_clock::now() - start > std::chrono::milliseconds(2)) {
+                CU(cudaEventSynchronize(sync_ev));
+                break;
+            }
+        }
+        pin_busy = false;  // every copy from the staging has completed
+        pin_off = 0;
         if (!pending.empty()) resolve_pending();
     }
     void read_status() {
@@ -581,12 +751,25 @@ struct gbls_handle {
         slot_cap = nc;
     }
 
+    // Upload the upper-node and root tables through the page-locked staging
+    // (the host tables may change right after: the copies read the staging).
     void upload_upper_root() {
-        upper_keys.upload(upper_keys_h.data(), upper_keys_h.size(), stream);
-        upper_sign.upload(upper_sign_h.data(), upper_sign_h.size(), stream);
-        root_keys.upload(root_keys_h.data(), root_keys_h.size(), stream);
-        root_sign.upload(root_sign_h.data(), root_sign_h.size(), stream);
-        sync();  // host vectors may change right after
+        const size_t b0 = upper_keys_h.size() * 8, b1 = upper_sign_h.size() * 8, b2 = root_keys_h.size() * 8,
+                     b3 = root_sign_h.size();
+        upper_keys.reserve(upper_keys_h.size(), stream);
+        upper_sign.reserve(upper_sign_h.size(), stream);
+        root_keys.reserve(root_keys_h.size(), stream);
+        root_sign.reserve(root_sign_h.size(), stream);
+        char* st = static_cast<char*>(pinned(b0 + b1 + b2 + b3 + 1));
+        std::memcpy(st, upper_keys_h.data(), b0);
+        std::memcpy(st + b0, upper_sign_h.data(), b1);
+        std::memcpy(st + b0 + b1, root_keys_h.data(), b2);
+        std::memcpy(st + b0 + b1 + b2, root_sign_h.data(), b3);
+        if (b0) CU(cudaMemcpyAsync(upper_keys.p, st, b0, cudaMemcpyHostToDevice, stream));
+        if (b1) CU(cudaMemcpyAsync(upper_sign.p, st + b0, b1, cudaMemcpyHostToDevice, stream));
+        if (b2) CU(cudaMemcpyAsync(root_keys.p, st + b0 + b1, b2, cudaMemcpyHostToDevice, stream));
+        if (b3) CU(cudaMemcpyAsync(root_sign.p, st + b0 + b1 + b2, b3, cudaMemcpyHostToDevice, stream));
+        pinned_issued();
     }
 
     void rebuild_nbr() {
@@ -606,12 +789,25 @@ int other_of(int a, int b) {
 }
 
 // Remap lower-node rows: src[r] = old row or -1-sign for a new row.
+// The new lower-node table: rows of the old table (src >= 0) or tiles of
+// one sign (src = -1 - sign).  The rows are written into the spare table,
+// which then becomes the current one (no allocation once the spare is
+// large enough).
 void remap_lower(gbls_handle& h, const std::vector<uint64_t>& new_keys, const std::vector<int32_t>& src) {
     const int64_t n = int64_t(new_keys.size());
-    DevArray<uint64_t> ns;
+    DevArray<uint64_t>& ns = h.lower_sign_spare;
     ns.reserve(size_t(std::max<int64_t>(n, 1)) * 64, h.stream);
-    h.remap.upload(src.data(), src.size(), h.stream);
+    h.remap.reserve(size_t(std::max<int64_t>(n, 1)), h.stream);
+    h.lower_keys.reserve(size_t(std::max<int64_t>(n, 1)), h.stream);
     if (n) {
+        // stage keys and row sources in page-locked memory: asynchronous copies
+        char* st = static_cast<char*>(h.pinned(size_t(n) * (sizeof(uint64_t) + sizeof(int32_t))));
+        std::memcpy(st, new_keys.data(), size_t(n) * sizeof(uint64_t));
+        std::memcpy(st + size_t(n) * sizeof(uint64_t), src.data(), size_t(n) * sizeof(int32_t));
+        CU(cudaMemcpyAsync(h.lower_keys.p, st, size_t(n) * sizeof(uint64_t), cudaMemcpyHostToDevice, h.stream));
+        CU(cudaMemcpyAsync(h.remap.p, st + size_t(n) * sizeof(uint64_t), size_t(n) * sizeof(int32_t),
+                           cudaMemcpyHostToDevice, h.stream));
+        h.pinned_issued();
         k_remap_rows<<<blocks_for(n * 64, 256), 256, 0, h.stream>>>(n, h.remap.p, h.lower_sign.p, ns.p);
         ++h.stats.kernel_launches;
     }
@@ -619,8 +815,6 @@ void remap_lower(gbls_handle& h, const std::vector<uint64_t>& new_keys, const st
     std::swap(h.lower_sign.p, ns.p);
     std::swap(h.lower_sign.cap, ns.cap);
     h.lower_keys_h = new_keys;
-    h.lower_keys.upload(new_keys.data(), new_keys.size(), h.stream);
-    h.sync();
 }
 
 int upper_bit(const gbls_handle& h, size_t ui, uint32_t slotn) {
@@ -697,8 +891,7 @@ void prune_nodes(gbls_handle& h, bool lower_changed) {
     const int64_t nl = int64_t(h.lower_keys_h.size());
     if (lower_changed && nl) {
         std::vector<uint8_t> fl(static_cast<size_t>(nl));
-        h.flags.download(fl.data(), size_t(nl), h.stream);
-        h.sync();
+        h.download_small(h.flags, fl.data(), size_t(nl));
         std::vector<uint64_t> keys;
         std::vector<int32_t> src;
         for (int64_t i = 0; i < nl; ++i) {
@@ -764,10 +957,42 @@ void dilate_topology(gbls_handle& h) {
                                                                  h.cand.p, &h.st_d->n_cand, h.run_ptr());
     ++h.stats.kernel_launches;
     CU(cudaGetLastError());
+    // Common case: at most SMALL_SORT_CAP candidates.  Sort, new leaves,
+    // merge and the missing-node search run on the device counts, and one
+    // read-back returns every count.  (The kernels are sized for `cap`; the
+    // ones after the sort read the distinct count on the device.)
+    const int64_t cap = std::min<int64_t>(L * 6, SMALL_SORT_CAP);
+    h.ensure_free_slots(cap);
+    h.ensure_leaf_cap(L + cap);
+    h.cand_sorted.reserve(size_t(cap), h.stream);
+    h.new_keys.reserve(size_t(cap), h.stream);
+    h.new_slots.reserve(size_t(cap), h.stream);
+    h.miss.reserve(size_t(cap), h.stream);
+    const int ko = 1 - h.kc;
+    const unsigned long long* nu = &h.st_d->n_unique;
+    if (!h.small_sort_ready) {
+        CU(cudaFuncSetAttribute(k_sort_unique_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(SMALL_SORT_SMEM)));
+        h.small_sort_ready = true;
+    }
+    k_sort_unique_small<<<1, SMALL_SORT_THREADS, SMALL_SORT_SMEM, h.stream>>>(h.cand.p, h.st_d, h.cand_sorted.p);
+    k_new_leaves<<<blocks_for(cap, 128), 128, 0, h.stream>>>(0, nu, h.cand_sorted.p, h.free_slots.p, h.nfree,
+                                                              h.new_keys.p, h.new_slots.p, h.am[h.mc].p,
+                                                              h.sm[h.mc].p);
+    k_merge<<<blocks_for(L + cap, 256), 256, 0, h.stream>>>(L, h.K(), h.S(), 0, nu, h.new_keys.p, h.new_slots.p,
+                                                            h.keys[ko].p, h.slot[ko].p);
+    k_missing_lower<<<blocks_for(cap, 128), 128, 0, h.stream>>>(0, nu, h.new_keys.p, h.lower_keys.p,
+                                                                 int64_t(h.lower_keys_h.size()), h.miss.p,
+                                                                 &h.st_d->n_lower_miss);
+    h.stats.kernel_launches += 4;
+    CU(cudaGetLastError());
     h.read_status();
-    const int64_t nc = int64_t(h.st_h->n_cand);
     int64_t nnew = 0;
-    if (nc > 0) {
+    if (!h.st_h->overflow) {
+        nnew = int64_t(h.st_h->n_unique);
+    } else {
+        // device-wide sort of many candidates, then the same steps on host counts
+        const int64_t nc = int64_t(h.st_h->n_cand);
         h.cand_sorted.reserve(size_t(nc), h.stream);
         h.u64s.reserve(1, h.stream);
         size_t b1 = 0, b2 = 0;
@@ -781,39 +1006,35 @@ void dilate_topology(gbls_handle& h) {
         CU(cudaMemcpyAsync(&n_u, h.u64s.p, sizeof(n_u), cudaMemcpyDeviceToHost, h.stream));
         h.sync();
         nnew = int64_t(n_u);
+        if (nnew > 0) {
+            h.ensure_free_slots(nnew);
+            h.ensure_leaf_cap(L + nnew);
+            h.new_keys.reserve(size_t(nnew), h.stream);
+            h.new_slots.reserve(size_t(nnew), h.stream);
+            h.miss.reserve(size_t(nnew), h.stream);
+            k_new_leaves<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(nnew, nullptr, h.cand.p, h.free_slots.p,
+                                                                       h.nfree, h.new_keys.p, h.new_slots.p,
+                                                                       h.am[h.mc].p, h.sm[h.mc].p);
+            k_merge<<<blocks_for(L + nnew, 256), 256, 0, h.stream>>>(L, h.K(), h.S(), nnew, nullptr, h.new_keys.p,
+                                                                     h.new_slots.p, h.keys[ko].p, h.slot[ko].p);
+            h.clear_status();
+            k_missing_lower<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(
+                nnew, nullptr, h.new_keys.p, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.miss.p,
+                &h.st_d->n_lower_miss);
+            h.stats.kernel_launches += 3;
+            CU(cudaGetLastError());
+            h.read_status();
+        }
     }
     if (nnew > 0) {
-        h.ensure_free_slots(nnew);
-        h.ensure_leaf_cap(L + nnew);
-        h.new_keys.reserve(size_t(nnew), h.stream);
-        h.new_slots.reserve(size_t(nnew), h.stream);
-        k_new_leaves<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(nnew, h.cand.p, h.free_slots.p, h.nfree,
-                                                                   h.new_keys.p, h.new_slots.p,
-                                                                   h.am[h.mc].p, h.sm[h.mc].p);
-        ++h.stats.kernel_launches;
-        CU(cudaGetLastError());
         h.nfree -= nnew;
-        const int ko = 1 - h.kc;
-        k_merge<<<blocks_for(L + nnew, 256), 256, 0, h.stream>>>(L, h.K(), h.S(), nnew, h.new_keys.p,
-                                                                 h.new_slots.p, h.keys[ko].p, h.slot[ko].p);
-        ++h.stats.kernel_launches;
-        CU(cudaGetLastError());
         h.kc = ko;
         h.nleaf = L + nnew;
         // lower / upper nodes for the new leaves
-        h.cand_sorted.reserve(size_t(nnew), h.stream);
-        h.clear_status();
-        k_missing_lower<<<blocks_for(nnew, 128), 128, 0, h.stream>>>(
-            nnew, h.new_keys.p, h.lower_keys.p, int64_t(h.lower_keys_h.size()), h.cand_sorted.p,
-            &h.st_d->n_lower_miss);
-        ++h.stats.kernel_launches;
-        CU(cudaGetLastError());
-        h.read_status();
         const int64_t nm = int64_t(h.st_h->n_lower_miss);
         if (nm > 0) {
             std::vector<uint64_t> miss(static_cast<size_t>(nm));
-            h.cand_sorted.download(miss.data(), size_t(nm), h.stream);
-            h.sync();
+            h.download_small(h.miss, miss.data(), size_t(nm));
             insert_nodes(h, miss);
         }
     }

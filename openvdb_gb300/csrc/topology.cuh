@@ -17,6 +17,8 @@ struct DevStatus {
     unsigned int pad;
     unsigned long long n_active;       // active voxels of the kept leaves
     unsigned long long io_err;         // upload value checks (IO_ERR_* bits of io.h)
+    unsigned long long n_unique;       // distinct candidates (single-CTA sort)
+    unsigned long long overflow;       // candidates beyond the single-CTA sort's capacity
 };
 
 // Face layer of a leaf mask that a missing neighbour on face f would receive.
