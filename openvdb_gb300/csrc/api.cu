@@ -521,7 +521,7 @@ struct gbls_handle {
     DevArray<uint64_t> keys[2];
     DevArray<int32_t> slot[2];
     int kc = 0;
-    DevArray<int32_t> nbr;
+    DevArray<int32_t> nbr, nbr_alt;  // face-neighbour table; a rebuild writes the other and swaps
     // slot storage: 3 mask sets, 3 value buffers, dilation mask
     int64_t slot_cap = 0;
     DevArray<uint64_t> am[3], sm[3];
@@ -579,6 +579,13 @@ struct gbls_handle {
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> event_pool;
     cudaEvent_t sync_ev = nullptr;
+    // During advection the tracker's dilation runs on `side`, concurrently
+    // with the RK stages of the same substep (they read values, the dilation
+    // writes topology): ev_fork precedes the RK stages, ev_rk follows them,
+    // ev_join ends the dilation.  on_side: `stream` is the side stream.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_rk = nullptr, ev_join = nullptr;
+    bool overlap_dilation = false, on_side = false;
     bool small_sort_ready = false;  // dynamic shared memory of k_sort_unique_small set on this device
     // Page-locked staging of the tracker's small node-table transfers, so
     // they are asynchronous copies; pin_ev marks the last copy issued from it.
@@ -596,6 +603,9 @@ struct gbls_handle {
         if (sync_ev) cudaEventDestroy(sync_ev);
         if (pin_ev) cudaEventSynchronize(pin_ev), cudaEventDestroy(pin_ev);
         if (pin) cudaFreeHost(pin);
+        if (side) cudaStreamSynchronize(side), cudaStreamDestroy(side);
+        for (cudaEvent_t e : {ev_fork, ev_rk, ev_join})
+            if (e) cudaEventDestroy(e);
     }
 
     // `bytes` of page-locked staging not read by a copy in flight: the next
@@ -693,9 +703,11 @@ struct gbls_handle {
                 break;
             }
         }
-        pin_busy = false;  // every copy from the staging has completed
-        pin_off = 0;
-        if (!pending.empty()) resolve_pending();
+        if (!on_side) {  // the side stream's syncs leave the RK stages running
+            pin_busy = false;  // every copy from the staging has completed
+            pin_off = 0;
+            if (!pending.empty()) resolve_pending();
+        }
     }
     void read_status() {
         CU(cudaMemcpyAsync(st_h, st_d, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
@@ -704,13 +716,19 @@ struct gbls_handle {
     }
     void clear_status() { CU(cudaMemsetAsync(st_d, 0, sizeof(DevStatus), stream)); }
 
+    bool leaf_cap_ok(int64_t n) const {
+        const size_t u = size_t(n);
+        return keys[0].cap >= u && keys[1].cap >= u && slot[0].cap >= u && slot[1].cap >= u &&
+               nbr.cap >= 6 * u && nbr_alt.cap >= 6 * u && cnt.cap >= u && keep.cap >= u && idx.cap >= u;
+    }
     void ensure_leaf_cap(int64_t n) {
         const size_t keep_n = size_t(nleaf);
         for (int b = 0; b < 2; ++b) {
             keys[b].reserve(n, stream, b == kc ? keep_n : 0);
             slot[b].reserve(n, stream, b == kc ? keep_n : 0);
         }
-        nbr.reserve(size_t(n) * 6, stream);
+        nbr.reserve(size_t(n) * 6, stream, size_t(nleaf) * 6);
+        nbr_alt.reserve(size_t(n) * 6, stream);
         cnt.reserve(n, stream);
         keep.reserve(n, stream);
         idx.reserve(n, stream);
@@ -772,11 +790,35 @@ struct gbls_handle {
         pinned_issued();
     }
 
+    // Rebuild into the other table (kernels enqueued earlier keep reading
+    // the current one) and make it current.
     void rebuild_nbr() {
         if (nleaf == 0) return;
-        k_build_nbr<<<blocks_for(nleaf * 6, 256), 256, 0, stream>>>(nleaf, K(), S(), nodes(), nbr.p);
+        nbr_alt.reserve(size_t(nleaf) * 6, stream);
+        k_build_nbr<<<blocks_for(nleaf * 6, 256), 256, 0, stream>>>(nleaf, K(), S(), nodes(), nbr_alt.p);
         ++stats.kernel_launches;
         CU(cudaGetLastError());
+        std::swap(nbr.p, nbr_alt.p);
+        std::swap(nbr.cap, nbr_alt.cap);
+    }
+
+    // Capacity for a dilation of the current leaves in the common case, taken
+    // before the RK stages are enqueued so that the concurrent dilation
+    // reallocates nothing they read.
+    void prepare_dilation() {
+        if (!side) {
+            CU(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+            for (cudaEvent_t* e : {&ev_fork, &ev_rk, &ev_join}) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        }
+        const int64_t L = nleaf;
+        const int64_t cap = std::min<int64_t>(L * 6, SMALL_SORT_CAP);
+        ensure_free_slots(cap);
+        ensure_leaf_cap(L + cap);
+        cand.reserve(size_t(L) * 6, stream);
+        cand_sorted.reserve(size_t(cap), stream);
+        new_keys.reserve(size_t(cap), stream);
+        new_slots.reserve(size_t(cap), stream);
+        miss.reserve(size_t(cap), stream);
     }
 };
 
@@ -948,8 +990,34 @@ void prune_nodes(gbls_handle& h, bool lower_changed) {
 }
 
 // ---- dilation: new leaves, node creation, neighbour table, dmask ----------
+// While h.overlap_dilation is set the dilation runs on the side stream after
+// ev_fork (concurrently with the RK stages that follow it on the main
+// stream) and the main stream waits for it; growing an array first waits for
+// the RK stages (ev_rk).
+struct SideStreamScope {
+    gbls_handle& h;
+    bool on;
+    explicit SideStreamScope(gbls_handle& h_) : h(h_), on(h_.overlap_dilation && h_.side) {
+        if (!on) return;
+        CU(cudaStreamWaitEvent(h.side, h.ev_fork, 0));
+        std::swap(h.stream, h.side);
+        h.on_side = true;
+    }
+    void wait_rk() {
+        if (on) CU(cudaStreamWaitEvent(h.stream, h.ev_rk, 0));
+    }
+    ~SideStreamScope() {
+        if (!on) return;
+        cudaEventRecord(h.ev_join, h.stream);
+        std::swap(h.stream, h.side);
+        h.on_side = false;
+        cudaStreamWaitEvent(h.stream, h.ev_join, 0);
+    }
+};
+
 void dilate_topology(gbls_handle& h) {
     if (h.nleaf == 0) return;
+    SideStreamScope scope(h);
     const int64_t L = h.nleaf;
     h.cand.reserve(size_t(L) * 6, h.stream);
     h.clear_status();
@@ -962,6 +1030,7 @@ void dilate_topology(gbls_handle& h) {
     // read-back returns every count.  (The kernels are sized for `cap`; the
     // ones after the sort read the distinct count on the device.)
     const int64_t cap = std::min<int64_t>(L * 6, SMALL_SORT_CAP);
+    if (h.nfree < cap || !h.leaf_cap_ok(L + cap)) scope.wait_rk();  // not prepared: grow after the RK stages
     h.ensure_free_slots(cap);
     h.ensure_leaf_cap(L + cap);
     h.cand_sorted.reserve(size_t(cap), h.stream);
@@ -992,6 +1061,7 @@ void dilate_topology(gbls_handle& h) {
         nnew = int64_t(h.st_h->n_unique);
     } else {
         // device-wide sort of many candidates, then the same steps on host counts
+        scope.wait_rk();
         const int64_t nc = int64_t(h.st_h->n_cand);
         h.cand_sorted.reserve(size_t(nc), h.stream);
         h.u64s.reserve(1, h.stream);
@@ -2707,7 +2777,10 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
         float next_v2 = 0.0f;
         struct Reset {
             gbls_handle* h;
-            ~Reset() { h->before_prune_sync = nullptr; }
+            ~Reset() {
+                h->before_prune_sync = nullptr;
+                h->overlap_dilation = false;
+            }
         } reset{h};
         while (forward ? t0 < t1 : t0 > t1) {
             if (!check_intr(*h)) { interrupted = true; break; }
@@ -2731,7 +2804,16 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                                                "TVD_RK1 tracker, normCount 1 and full trimming");
                 tape_begin_substep(*h, t0, dt, !forward);
             }
+            const bool overlap = !h->tape_on;
+            if (overlap) {
+                h->prepare_dilation();
+                CU(cudaEventRecord(h->ev_fork, h->stream));
+            }
             advect_stages(*h, field, spatial, temporal, t0, dt, !forward);
+            if (overlap) {
+                CU(cudaEventRecord(h->ev_rk, h->stream));
+                h->overlap_dilation = true;
+            }
             t0 += forward ? dt : -dt;
             ++count;
             const bool more = forward ? t0 < t1 : t0 > t1;
@@ -2744,6 +2826,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                 };
             }
             track(*h);
+            h->overlap_dilation = false;
             h->before_prune_sync = nullptr;
             if (queued) {
                 next_v2 = status_max_speed(*h);
