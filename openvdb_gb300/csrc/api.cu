@@ -567,6 +567,7 @@ struct gbls_handle {
     // ends a tracker pass (the next substep's CFL reduction), so that one
     // synchronisation serves both
     std::function<void()> before_prune_sync;
+    std::function<void()> after_normalize;  // called by track() after the renormalisation is enqueued
     // measurement
     gbls_stats stats{};
     int64_t nactive = -1;  // active voxels, -1 = unknown
@@ -584,7 +585,11 @@ struct gbls_handle {
     // writes topology): ev_fork precedes the RK stages, ev_rk follows them,
     // ev_join ends the dilation.  on_side: `stream` is the side stream.
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_rk = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_rk = nullptr, ev_join = nullptr, ev_norm = nullptr, ev_cfl = nullptr;
+    // The next substep's CFL maximum, reduced on the side stream while the
+    // main stream prunes: device word and its page-locked copy.
+    unsigned int* cfl_d = nullptr;
+    unsigned int* cfl_h = nullptr;
     bool overlap_dilation = false, on_side = false;
     bool small_sort_ready = false;  // dynamic shared memory of k_sort_unique_small set on this device
     // Page-locked staging of the tracker's small node-table transfers, so
@@ -604,8 +609,10 @@ struct gbls_handle {
         if (pin_ev) cudaEventSynchronize(pin_ev), cudaEventDestroy(pin_ev);
         if (pin) cudaFreeHost(pin);
         if (side) cudaStreamSynchronize(side), cudaStreamDestroy(side);
-        for (cudaEvent_t e : {ev_fork, ev_rk, ev_join})
+        for (cudaEvent_t e : {ev_fork, ev_rk, ev_join, ev_norm, ev_cfl})
             if (e) cudaEventDestroy(e);
+        if (cfl_d) cudaFree(cfl_d);
+        if (cfl_h) cudaFreeHost(cfl_h);
     }
 
     // `bytes` of page-locked staging not read by a copy in flight: the next
@@ -807,8 +814,15 @@ struct gbls_handle {
     // reallocates nothing they read.
     void prepare_dilation() {
         if (!side) {
-            CU(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-            for (cudaEvent_t* e : {&ev_fork, &ev_rk, &ev_join}) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+            // highest priority: the dilation's small grids (a single-CTA sort)
+            // are dispatched as soon as RK-stage CTAs retire
+            int lo = 0, hi = 0;
+            CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            CU(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+            for (cudaEvent_t* e : {&ev_fork, &ev_rk, &ev_join, &ev_norm, &ev_cfl})
+                CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+            CU(cudaMalloc(&cfl_d, sizeof(unsigned int)));
+            CU(cudaHostAlloc(&cfl_h, sizeof(unsigned int), cudaHostAllocDefault));
         }
         const int64_t L = nleaf;
         const int64_t cap = std::min<int64_t>(L * 6, SMALL_SORT_CAP);
@@ -1371,6 +1385,7 @@ void track(gbls_handle& h) {
         CU(cudaGetLastError());
     }
     normalize_pass(h, h.dmask.p, h.trim);
+    if (h.after_normalize) h.after_normalize();
     if (tp) tape_values(h, tp->nm, h.mc, -1, &tp->fin, nullptr, nullptr);
     if (h.nleaf > 0 && h.norm_count <= 0 && !h.trim) {
         // no normalisation and no trimming: the dilated mask becomes active as is
@@ -1478,6 +1493,30 @@ void enqueue_max_speed(gbls_handle& h, const gbls_field* f, float t, const unsig
     launch_cfl(a, h.stream);
     h.stats.kernel_launches += 2;
     CU(cudaGetLastError());
+}
+
+// The CFL maximum of the renormalised level set at time t on the side
+// stream, concurrently with the prune on the main stream: the leaves before
+// the prune have the same active voxels (a pruned leaf has none), so the
+// maximum is the same.  Result in h.cfl_d; ev_cfl follows it.
+void enqueue_max_speed_side(gbls_handle& h, const gbls_field* f, float t) {
+    CU(cudaEventRecord(h.ev_norm, h.stream));
+    CU(cudaStreamWaitEvent(h.side, h.ev_norm, 0));
+    CflArgs a{};
+    a.nleaf = h.nleaf;
+    a.keys = h.K();
+    a.slot = h.S();
+    a.amask = h.am[h.mc].p;
+    a.t0 = t;
+    a.field = field_params(h, f, t);
+    a.max_bits = h.cfl_d;
+    h.cfl_part.reserve(size_t(std::max<int64_t>(h.nleaf, 1)), h.side);
+    a.part = h.cfl_part.p;
+    CU(cudaMemsetAsync(h.cfl_d, 0, sizeof(unsigned int), h.side));
+    launch_cfl(a, h.side);
+    h.stats.kernel_launches += 2;
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(h.ev_cfl, h.side));
 }
 
 float status_max_speed(const gbls_handle& h) {
@@ -2779,6 +2818,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             gbls_handle* h;
             ~Reset() {
                 h->before_prune_sync = nullptr;
+                h->after_normalize = nullptr;
                 h->overlap_dilation = false;
             }
         } reset{h};
@@ -2804,7 +2844,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                                                "TVD_RK1 tracker, normCount 1 and full trimming");
                 tape_begin_substep(*h, t0, dt, !forward);
             }
-            const bool overlap = !h->tape_on;
+            const bool overlap = true;  // dilation (and the next CFL maximum) on the side stream
             if (overlap) {
                 h->prepare_dilation();
                 CU(cudaEventRecord(h->ev_fork, h->stream));
@@ -2820,16 +2860,30 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             bool queued = false;
             if (more && field->desc.kind != GBLS_FIELD_CONSTANT) {
                 const float tn = t0;
-                h->before_prune_sync = [h, field, tn, &queued] {
-                    enqueue_max_speed(*h, field, tn, &h->st_d->n_cand);
-                    queued = true;
-                };
+                if (overlap && !h->batch_run) {
+                    // reduce on the side stream while the main stream prunes;
+                    // the prune's read-back waits for it
+                    h->after_normalize = [h, field, tn] { enqueue_max_speed_side(*h, field, tn); };
+                    h->before_prune_sync = [h, &queued] {
+                        CU(cudaStreamWaitEvent(h->stream, h->ev_cfl, 0));
+                        CU(cudaMemcpyAsync(h->cfl_h, h->cfl_d, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                           h->stream));
+                        queued = true;
+                    };
+                } else {
+                    h->before_prune_sync = [h, field, tn, &queued] {
+                        enqueue_max_speed(*h, field, tn, &h->st_d->n_cand);
+                        queued = true;
+                    };
+                }
             }
             track(*h);
             h->overlap_dilation = false;
             h->before_prune_sync = nullptr;
+            h->after_normalize = nullptr;
             if (queued) {
-                next_v2 = status_max_speed(*h);
+                if (overlap && !h->batch_run) std::memcpy(&next_v2, h->cfl_h, sizeof(float));
+                else next_v2 = status_max_speed(*h);
                 have_next = true;
             }
         }
