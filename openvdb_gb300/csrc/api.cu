@@ -1739,7 +1739,12 @@ void filter_box(gbls_handle& h, int width) {
 bool is_pm_gamma(float v, float g) { return v == g || v == -g; }
 
 // Upload n level sets (instance i from descs[i]; n == 1 for a plain handle).
-void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
+// Upload n instances.  dev_leaves (a single level set): the leaf keys are
+// computed and checked on the device; returns false, having changed only
+// device scratch, when the leaves are not valid input in tree order, and the
+// caller repeats the upload with host-side keys (which sorts or reports the
+// error).
+bool upload_impl(gbls_handle& h, const gbls_grid_desc* descs, int n, bool dev_leaves) {
     if (n < 1 || n > GBLS_MAX_INSTANCES) fail(GBLS_ERR_INVALID_ARGUMENT, "instance count out of range");
     const gbls_grid_desc* d0 = descs;
     if (!(d0->voxel_size > 0.0)) fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
@@ -1779,10 +1784,13 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
         lv_base[size_t(q) + 1] = lv_base[size_t(q)] + d->leaf_count;
         lo_base[size_t(q) + 1] = lo_base[size_t(q)] + d->lower_count;
         up_base[size_t(q) + 1] = up_base[size_t(q)] + d->upper_count;
-        for (int64_t i = 0; i < d->leaf_count; ++i) {
-            const int32_t* o = d->leaf_origins + 3 * i;
-            check_origin(o, 8);
-            lv.push_back({leaf_key(o[0], o[1], o[2]) | ib, lv_base[size_t(q)] + i});
+        if (!dev_leaves) {
+            lv.reserve(lv.size() + size_t(d->leaf_count));
+            for (int64_t i = 0; i < d->leaf_count; ++i) {
+                const int32_t* o = d->leaf_origins + 3 * i;
+                check_origin(o, 8);
+                lv.push_back({leaf_key(o[0], o[1], o[2]) | ib, lv_base[size_t(q)] + i});
+            }
         }
         for (int64_t i = 0; i < d->lower_count; ++i) {
             const int32_t* o = d->lower_origins + 3 * i;
@@ -1809,12 +1817,14 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     order(lo, "duplicate lower node");
     order(up, "duplicate upper node");
     order(rt, "duplicate root tile");
-    const int64_t L = int64_t(lv.size()), NLO = int64_t(lo.size()), NUP = int64_t(up.size());
-    std::vector<uint64_t> keys(static_cast<size_t>(L)), lkeys(static_cast<size_t>(NLO)), ukeys(static_cast<size_t>(NUP));
-    std::vector<int32_t> perm(static_cast<size_t>(L + NLO + NUP));
-    for (int64_t i = 0; i < L; ++i) { keys[size_t(i)] = lv[size_t(i)].key; perm[size_t(i)] = int32_t(lv[size_t(i)].idx); }
-    for (int64_t i = 0; i < NLO; ++i) { lkeys[size_t(i)] = lo[size_t(i)].key; perm[size_t(L + i)] = int32_t(lo[size_t(i)].idx); }
-    for (int64_t i = 0; i < NUP; ++i) { ukeys[size_t(i)] = up[size_t(i)].key; perm[size_t(L + NLO + i)] = int32_t(up[size_t(i)].idx); }
+    const int64_t L = dev_leaves ? d0->leaf_count : int64_t(lv.size()), NLO = int64_t(lo.size()),
+                  NUP = int64_t(up.size());
+    const int64_t pl = dev_leaves ? 0 : L;  // leaf part of perm (identity on the device path)
+    std::vector<uint64_t> keys(static_cast<size_t>(pl)), lkeys(static_cast<size_t>(NLO)), ukeys(static_cast<size_t>(NUP));
+    std::vector<int32_t> perm(static_cast<size_t>(pl + NLO + NUP));
+    for (int64_t i = 0; i < pl; ++i) { keys[size_t(i)] = lv[size_t(i)].key; perm[size_t(i)] = int32_t(lv[size_t(i)].idx); }
+    for (int64_t i = 0; i < NLO; ++i) { lkeys[size_t(i)] = lo[size_t(i)].key; perm[size_t(pl + i)] = int32_t(lo[size_t(i)].idx); }
+    for (int64_t i = 0; i < NUP; ++i) { ukeys[size_t(i)] = up[size_t(i)].key; perm[size_t(pl + NLO + i)] = int32_t(up[size_t(i)].idx); }
     // every leaf under a lower node, every lower node under an upper node (sorted walks)
     auto parents = [](const std::vector<uint64_t>& child, int shift, const std::vector<uint64_t>& par, const char* msg) {
         size_t p = 0;
@@ -1824,7 +1834,7 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
             if (p == par.size() || par[p] != pk) fail(GBLS_ERR_INVALID_ARGUMENT, msg);
         }
     };
-    parents(keys, 12, lkeys, "leaf without lower node");
+    if (!dev_leaves) parents(keys, 12, lkeys, "leaf without lower node");
     parents(lkeys, 15, ukeys, "lower node without upper node");
     h.root_keys_h.clear();
     h.root_sign_h.clear();
@@ -1854,15 +1864,14 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     h.emask.reserve(size_t(scap) * 8, h.stream);
     h.free_slots.reserve(size_t(scap), h.stream);
     h.slot_cap = scap;
-    std::vector<int32_t> fs;
-    fs.reserve(size_t(scap - L));
-    for (int64_t q = scap - 1; q >= L; --q) fs.push_back(int32_t(q));
-    h.nfree = int64_t(fs.size());
-    std::vector<int32_t> slots(static_cast<size_t>(L));
-    for (int64_t i = 0; i < L; ++i) slots[size_t(i)] = int32_t(i);
-    h.free_slots.upload(fs.data(), fs.size(), h.stream);
-    h.keys[0].upload(keys.data(), keys.size(), h.stream);
-    h.slot[0].upload(slots.data(), slots.size(), h.stream);
+    h.nfree = scap - L;
+    launch_free_slots(scap - L, int32_t(scap), h.free_slots.p, h.stream);
+    if (!dev_leaves) {
+        std::vector<int32_t> slots(static_cast<size_t>(L));
+        for (int64_t i = 0; i < L; ++i) slots[size_t(i)] = int32_t(i);
+        h.keys[0].upload(keys.data(), keys.size(), h.stream);
+        h.slot[0].upload(slots.data(), slots.size(), h.stream);
+    }
     h.io_perm.upload(perm.data(), perm.size(), h.stream);
     h.lower_keys_h = lkeys;
     h.lower_keys.upload(lkeys.data(), lkeys.size(), h.stream);
@@ -1890,10 +1899,17 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     }
     h.clear_status();
     unsigned long long* err = &h.st_d->io_err;
-    launch_pack_leaves(L, h.io_perm.p, h.am[1].p, h.vals[1].p, g, h.am[0].p, h.sm[0].p, h.vals[0].p, err, h.stream);
-    launch_node_signs(NLO, 12, h.lower_keys.p, h.io_perm.p + L, lo_stage, h.keys[0].p, L, g, h.lower_sign.p, err,
+    if (dev_leaves) {
+        h.io_orig.reserve(size_t(L) * 3, h.stream);
+        CU(cudaMemcpyAsync(h.io_orig.p, d0->leaf_origins, size_t(L) * 12, cudaMemcpyHostToDevice, h.stream));
+        launch_leaf_keys(L, h.io_orig.p, h.lower_keys.p, NLO, h.keys[0].p, h.slot[0].p, err, h.stream);
+        ++h.stats.kernel_launches;
+    }
+    launch_pack_leaves(L, dev_leaves ? nullptr : h.io_perm.p, h.am[1].p, h.vals[1].p, g, h.am[0].p, h.sm[0].p,
+                       h.vals[0].p, err, h.stream);
+    launch_node_signs(NLO, 12, h.lower_keys.p, h.io_perm.p + pl, lo_stage, h.keys[0].p, L, g, h.lower_sign.p, err,
                       IO_ERR_LOWER_TILE, h.stream);
-    launch_node_signs(NUP, 15, h.upper_keys.p, h.io_perm.p + L + NLO, up_stage, h.lower_keys.p, NLO, g,
+    launch_node_signs(NUP, 15, h.upper_keys.p, h.io_perm.p + pl + NLO, up_stage, h.lower_keys.p, NLO, g,
                       h.upper_sign.p, err, IO_ERR_UPPER_TILE, h.stream);
     h.stats.kernel_launches += (L > 0) + (NLO > 0) + (NUP > 0);
     CU(cudaGetLastError());
@@ -1901,6 +1917,7 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     h.upper_sign.download(usign.data(), usign.size(), h.stream);
     h.read_status();
     const unsigned long long e = h.st_h->io_err;
+    if (dev_leaves && (e & IO_ERR_KEYS)) return false;
     if (e & IO_ERR_LEAF_VALUE) fail(GBLS_ERR_UNSUPPORTED, "inactive leaf value other than +-background");
     if (e & IO_ERR_LOWER_TILE) fail(GBLS_ERR_UNSUPPORTED, "lower-node tile other than +-background");
     if (e & IO_ERR_UPPER_TILE) fail(GBLS_ERR_UNSUPPORTED, "upper-node tile other than +-background");
@@ -1917,6 +1934,14 @@ void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     h.inst_active.reserve(size_t(n), h.stream);
     h.sync();
     h.nactive = -1;
+    return true;
+}
+
+void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
+    if (n == 1 && descs[0].leaf_count > 0 && descs[0].leaf_origins && descs[0].leaf_masks && descs[0].leaf_values &&
+        upload_impl(h, descs, n, true))
+        return;
+    upload_impl(h, descs, n, false);
 }
 
 // Index ranges [lo, hi) of instance `inst` in the leaf / lower / upper / root

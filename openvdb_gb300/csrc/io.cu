@@ -44,6 +44,35 @@ k_pack_leaves(int64_t n, const int32_t* perm, const uint64_t* in_masks, const fl
     }
 }
 
+__device__ __forceinline__ bool origin_ok(const int32_t* o) {
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ok &= (o[a] % 8 == 0) && o[a] >= -COORD_SAFE && o[a] < COORD_SAFE;
+    return ok;
+}
+
+__global__ void k_leaf_keys(int64_t n, const int32_t* orig, const uint64_t* lower_keys, int64_t nlower,
+                            uint64_t* keys, int32_t* slot, unsigned long long* err) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const int32_t* o = orig + 3 * i;
+    bool bad = !origin_ok(o);
+    const uint64_t k = leaf_key(o[0], o[1], o[2]);
+    if (i > 0) {
+        const int32_t* q = o - 3;
+        if (!(leaf_key(q[0], q[1], q[2]) < k)) bad = true;
+    }
+    if (find_u64(lower_keys, nlower, k >> 12) < 0) bad = true;
+    keys[i] = k;
+    slot[i] = int32_t(i);
+    if (bad) atomicOr(err, IO_ERR_KEYS);
+}
+
+__global__ void k_free_slots(int64_t n, int32_t top, int32_t* free_slots) {
+    const int64_t j = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (j < n) free_slots[j] = int32_t(top - 1 - j);
+}
+
 // Child bitmap of node `nk` (one bit per slot) in shared memory.
 __device__ void child_bitmap(uint32_t* bits, int nwords, uint64_t nk, int shift, const uint64_t* child_keys,
                              int64_t nchild) {
@@ -117,6 +146,17 @@ k_node_tiles(int64_t n, int shift, const uint64_t* node_keys, const uint64_t* si
 }
 
 }  // namespace
+
+void launch_leaf_keys(int64_t n, const int32_t* origins, const uint64_t* lower_keys, int64_t nlower,
+                      uint64_t* keys, int32_t* slot, unsigned long long* err, cudaStream_t s) {
+    if (n <= 0) return;
+    k_leaf_keys<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, origins, lower_keys, nlower, keys, slot, err);
+}
+
+void launch_free_slots(int64_t n, int32_t top, int32_t* free_slots, cudaStream_t s) {
+    if (n <= 0) return;
+    k_free_slots<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, top, free_slots);
+}
 
 void launch_pack_leaves(int64_t n, const int32_t* perm, const uint64_t* in_masks, const float* in_vals,
                         float gamma, uint64_t* am, uint64_t* sm, float* vals, unsigned long long* err,

@@ -13,6 +13,16 @@ namespace gbls {
 constexpr unsigned long long IO_ERR_LEAF_VALUE = 1;   // inactive leaf value other than +-background
 constexpr unsigned long long IO_ERR_LOWER_TILE = 2;   // lower-node tile other than +-background
 constexpr unsigned long long IO_ERR_UPPER_TILE = 4;   // upper-node tile other than +-background
+constexpr unsigned long long IO_ERR_KEYS = 8;         // leaf origins not aligned, in range, in tree order and
+                                                      // unique, each under a lower node (host path decides)
+
+// Keys (and identity slots) of n leaves from their origins, checked on the
+// device: sets IO_ERR_KEYS when an origin is misaligned or out of range, the
+// keys are not strictly increasing, or a leaf has no lower node.
+void launch_leaf_keys(int64_t n, const int32_t* origins, const uint64_t* lower_keys, int64_t nlower,
+                      uint64_t* keys, int32_t* slot, unsigned long long* err, cudaStream_t s);
+// free[j] = top - 1 - j for j < n (the free-slot stack after an upload).
+void launch_free_slots(int64_t n, int32_t top, int32_t* free_slots, cudaStream_t s);
 
 // Leaf l (tree order) takes the dense values and mask of staged leaf
 // perm[l]: writes am/sm/vals of slot l.  Sets IO_ERR_LEAF_VALUE in *err.

@@ -157,16 +157,20 @@ def test_adjoint_inverse_problem_128():
     phi0 = template.active_values().copy()
     tape.forward(phi0, times, record=False)  # warm-up
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    tape.forward(phi0, times, record=False)
-    t_plain = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    phiT, gT = tape.forward(phi0, times, record=True)
-    t_rec = time.perf_counter() - t0
-    d = phiT.astype(np.float64) - target(gT.active_coords())
-    t0 = time.perf_counter()
-    g_phi, g_vel = tape.backward((2.0 * d).astype(np.float32))
-    t_adj = time.perf_counter() - t0
+    # best of three of each (wall times of about 10 ms)
+    t_plain = t_rec = t_adj = float("inf")
+    for _ in range(3):
+        t0 = time.perf_counter()
+        tape.forward(phi0, times, record=False)
+        t_plain = min(t_plain, time.perf_counter() - t0)
+    for _ in range(3):
+        t0 = time.perf_counter()
+        phiT, gT = tape.forward(phi0, times, record=True)
+        t_rec = min(t_rec, time.perf_counter() - t0)
+        d = phiT.astype(np.float64) - target(gT.active_coords())
+        t0 = time.perf_counter()
+        g_phi, g_vel = tape.backward((2.0 * d).astype(np.float32))
+        t_adj = min(t_adj, time.perf_counter() - t0)
     print("adjoint 128^3: %d substeps, %d -> %d active voxels, L = %.6g" % (sum(tape.substeps), phi0.size,
                                                                             phiT.size, float((d * d).sum())))
     print("wall time: forward %.3f s, recorded forward %.3f s, adjoint %.3f s, (fwd+adj)/fwd = %.2f"
