@@ -24,82 +24,79 @@ void launch_norm_fast(const NormArgs& a, cudaStream_t s) {
         normalize_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
-// One CTA of 64 threads per leaf (thread t visits bit t of each active-mask
-// word), the leaf's six sine rows of the deformation table staged in shared
-// memory as in the RK kernel.  A single level set writes its leaf maxima to
-// a partial array reduced by cfl_reduce_kernel (no same-address atomics);
-// a batch publishes each leaf maximum with atomicMax on its instance's word
-// (spread over the instances).  Vec3f::lengthSqr (math/Vec3.h:212-218) and
-// the field use non-contracting intrinsics in eval_field's order, so the
-// maximum equals the reference's exactly (the maximum of non-negative floats
-// does not depend on order).
-constexpr int CFL_THREADS = 64;
+// Eight threads per leaf, thread w visiting the set bits of active-mask word
+// w (voxels x = w), 32 leaves per CTA of 256 threads: every leaf's chain of
+// dependent loads (slot, then mask and key, then the field's sine rows) is
+// in flight at once, which the reduction's few operations per voxel cannot
+// hide otherwise.  The deformation field reads its per-coordinate sine table
+// directly (L1-resident rows).  A single level set writes its leaf maxima to
+// a partial array reduced by cfl_reduce_kernel (no same-address atomics); a
+// batch publishes each leaf maximum with atomicMax on its instance's word.
+// Vec3f::lengthSqr (math/Vec3.h:212-218) and the field use non-contracting
+// intrinsics in eval_field's order, so the maximum equals the reference's
+// exactly (the maximum of non-negative floats does not depend on order).
+constexpr int CFL_THREADS = 256;
+constexpr int CFL_LEAVES = CFL_THREADS / 8;
 
 __global__ void __launch_bounds__(CFL_THREADS) cfl_max_kernel(const __grid_constant__ CflArgs a) {
     const int64_t n = a.nleaf_dev ? min(a.nleaf, int64_t(*a.nleaf_dev)) : a.nleaf;
-    const int64_t l = blockIdx.x;
-    const int t = threadIdx.x;
-    __shared__ float vtab[6][8];
-    __shared__ float wm[2];
-    if (l >= n) {
-        if (t == 0 && a.part) a.part[l] = 0.0f;
-        return;
-    }
-    const uint64_t key = a.keys[l];
-    const FieldParams* fp = &a.field;
-    float t0 = a.t0;
-    uint32_t inst = 0;
-    if (a.inst_run) {
-        inst = key_instance(key);
-        if (!a.inst_run[inst]) return;
-        fp = a.inst_field + inst;
-        t0 = a.inst_t0[inst];
-    }
-    const int s = a.slot[l];
-    int ox, oy, oz;
-    key_origin(key, ox, oy, oz);
-    const FieldParams& f = *fp;
-    const bool tabbed = f.kind == 2 && f.tab && ox - f.tab_lo >= 0 && oy - f.tab_lo >= 0 && oz - f.tab_lo >= 0 &&
-                        ox + 8 - f.tab_lo <= f.tab_n && oy + 8 - f.tab_lo <= f.tab_n && oz + 8 - f.tab_lo <= f.tab_n;
-    if (tabbed) {  // block-uniform
-        if (t < 48) {
-            const int ax = t >> 4, fn = (t >> 3) & 1, q = t & 7;
-            const int o = ax == 0 ? ox : ax == 1 ? oy : oz;
-            vtab[ax * 2 + fn][q] = f.tab[2 * (o + q - f.tab_lo) + fn];
-        }
-        __syncthreads();
-    }
-    const int y = t >> 3, z = t & 7;
+    const int64_t l = int64_t(blockIdx.x) * CFL_LEAVES + (threadIdx.x >> 3);
+    const int w = threadIdx.x & 7;
     float m = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint64_t w = a.amask[size_t(s) * 8 + k];
-        if (!((w >> t) & 1)) continue;
-        float vel[3];
-        if (tabbed) {  // eval_field's deformation branch with the staged sines
-            const float sx = vtab[0][k], s2x = vtab[1][k], sy = vtab[2][y], s2y = vtab[3][y];
-            const float sz = vtab[4][z], s2z = vtab[5][z];
-            const float u = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, sx), sx), s2y), s2z);
-            const float v = __fmul_rn(__fmul_rn(__fmul_rn(s2x, sy), sy), s2z);
-            const float ww = __fmul_rn(__fmul_rn(__fmul_rn(s2x, s2y), sz), sz);
-            vel[0] = __fmul_rn(u, f.amp);
-            vel[1] = -__fmul_rn(v, f.amp);
-            vel[2] = -__fmul_rn(ww, f.amp);
-        } else {
-            eval_field(f, ox + k, oy + y, oz + z, t0, vel);
-        }
-        const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(vel[0], vel[0]), __fmul_rn(vel[1], vel[1])),
-                                   __fmul_rn(vel[2], vel[2]));
-        m = ref_max(m, l2);
+    uint32_t inst = 0;
+    bool live = l < n && l < a.nleaf;
+    if (live && a.inst_run) {
+        inst = key_instance(a.keys[l]);
+        live = a.inst_run[inst] != 0;
     }
-    for (int o = 16; o > 0; o >>= 1) m = ref_max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (live) {
+        const int s = a.slot[l];
+        uint64_t bits = a.amask[size_t(s) * 8 + w];
+        const uint64_t key = a.keys[l];
+        const FieldParams& f = a.inst_run ? a.inst_field[inst] : a.field;
+        const float t0 = a.inst_run ? a.inst_t0[inst] : a.t0;
+        int ox, oy, oz;
+        key_origin(key, ox, oy, oz);
+        const bool tabbed = f.kind == 2 && f.tab && ox - f.tab_lo >= 0 && oy - f.tab_lo >= 0 &&
+                            oz - f.tab_lo >= 0 && ox + 8 - f.tab_lo <= f.tab_n && oy + 8 - f.tab_lo <= f.tab_n &&
+                            oz + 8 - f.tab_lo <= f.tab_n;
+        float sx = 0.0f, s2x = 0.0f;
+        if (tabbed) {
+            const int ia = ox + w - f.tab_lo;
+            sx = __ldg(f.tab + 2 * ia);
+            s2x = __ldg(f.tab + 2 * ia + 1);
+        }
+        while (bits) {
+            const int b = __ffsll(static_cast<long long>(bits)) - 1;
+            bits &= bits - 1;
+            const int y = b >> 3, z = b & 7;
+            float vel[3];
+            if (tabbed) {  // eval_field's deformation branch, sines from the table
+                const int ja = oy + y - f.tab_lo, ka = oz + z - f.tab_lo;
+                const float sy = __ldg(f.tab + 2 * ja), s2y = __ldg(f.tab + 2 * ja + 1);
+                const float sz = __ldg(f.tab + 2 * ka), s2z = __ldg(f.tab + 2 * ka + 1);
+                const float u = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(2.0f, sx), sx), s2y), s2z);
+                const float v = __fmul_rn(__fmul_rn(__fmul_rn(s2x, sy), sy), s2z);
+                const float ww = __fmul_rn(__fmul_rn(__fmul_rn(s2x, s2y), sz), sz);
+                vel[0] = __fmul_rn(u, f.amp);
+                vel[1] = -__fmul_rn(v, f.amp);
+                vel[2] = -__fmul_rn(ww, f.amp);
+            } else {
+                eval_field(f, ox + w, oy + y, oz + z, t0, vel);
+            }
+            const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(vel[0], vel[0]), __fmul_rn(vel[1], vel[1])),
+                                       __fmul_rn(vel[2], vel[2]));
+            m = ref_max(m, l2);
+        }
+    }
+    // maximum over the leaf's 8 lanes (groups of 8 consecutive lanes)
+    for (int o = 4; o > 0; o >>= 1) m = ref_max(m, __shfl_xor_sync(0xffffffffu, m, o, 8));
+    if (w != 0 || l >= a.nleaf) return;
     if (a.inst_run) {
-        if ((t & 31) == 0) atomicMax(a.max_bits + inst, __float_as_uint(m));
+        if (live) atomicMax(a.max_bits + inst, __float_as_uint(m));
         return;
     }
-    if ((t & 31) == 0) wm[t >> 5] = m;
-    __syncthreads();
-    if (t == 0) a.part[l] = ref_max(wm[0], wm[1]);
+    a.part[l] = m;
 }
 
 // Maximum of the per-leaf partials into max_bits[0] (one CTA).
@@ -144,7 +141,7 @@ void launch_morph_stage_fast(const MorphArgs& a, cudaStream_t s) {
 
 void launch_cfl(const CflArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    cfl_max_kernel<<<unsigned(a.nleaf), CFL_THREADS, 0, s>>>(a);
+    cfl_max_kernel<<<unsigned((a.nleaf + CFL_LEAVES - 1) / CFL_LEAVES), CFL_THREADS, 0, s>>>(a);
     if (!a.inst_run) cfl_reduce_kernel<<<1, 1024, 0, s>>>(a.part, a.nleaf, a.max_bits);
 }
 
