@@ -168,8 +168,6 @@ __global__ void __launch_bounds__(STENCIL_THREADS, 16) normalize_kernel_x2(const
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ float res[LEAF_VOX];
-    __shared__ uint16_t list[LEAF_VOX];
-    __shared__ uint8_t flag[LEAF_VOX];
     __shared__ uint64_t pm[8], um[8], fin[8], fsg[8];
     __shared__ uint32_t half[2][2][8];
     const int64_t l = blockIdx.x;
@@ -187,7 +185,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS, 16) normalize_kernel_x2(const
         fsg[t] = st.sm[0][t] & ~um[t];
     }
     load_tile(tile, st, a.gamma);
-    __syncthreads();
+    __syncthreads();  // the staging records are dead: the voxel list reuses their storage
+    uint16_t* list = reinterpret_cast<uint16_t*>(&st.rec[0][0]);
     const int n = build_list(list, um);
     __syncthreads();
     const float g = a.gamma;
@@ -225,16 +224,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS, 16) normalize_kernel_x2(const
             const int v = e ? v1 : v0;
             const float ph = e ? phi0.y : phi0.x;
             float val = e ? val2.y : val2.x;
-            if (!((pm[v >> 6] >> (v & 63)) & 1)) {  // active voxel outside the processed set
-                res[v] = ph;
-                flag[v] = uint8_t((carry ? 1 : 0) | (ph < 0.0f ? 2 : 0));
-                continue;
-            }
-            bool act = true, neg = val < 0.0f;
-            if ((trim & 1) && val <= -g) { act = false; neg = true; }
-            else if ((trim & 2) && val >= g) { act = false; neg = false; }
-            res[v] = val;
-            flag[v] = uint8_t((act ? 1 : 0) | (neg ? 2 : 0));
+            // an active voxel outside the processed set keeps its value
+            res[v] = ((pm[v >> 6] >> (v & 63)) & 1) ? val : ph;
         }
     }
     __syncthreads();
@@ -244,7 +235,21 @@ __global__ void __launch_bounds__(STENCIL_THREADS, 16) normalize_kernel_x2(const
         for (int k = 0; k < 8; ++k) {
             const int v = (k << 6) | t;
             const bool vis = (um[k] >> t) & 1;
-            const uint8_t f = vis ? flag[v] : uint8_t(0);
+            // the voxel's state after the pass from its result: processed
+            // voxels are trimmed by the TrimMode bits, the others stay active
+            // when `carry` is set
+            uint8_t f = 0;
+            if (vis) {
+                const float val = res[v];
+                bool act = true, neg = val < 0.0f;
+                if ((pm[k] >> t) & 1) {
+                    if ((trim & 1) && val <= -g) { act = false; neg = true; }
+                    else if ((trim & 2) && val >= g) { act = false; neg = false; }
+                } else {
+                    act = carry != 0;
+                }
+                f = uint8_t((act ? 1 : 0) | (neg ? 2 : 0));
+            }
             const uint32_t ba = __ballot_sync(0xffffffffu, f & 1);
             const uint32_t bn = __ballot_sync(0xffffffffu, (f >> 1) & 1);
             if (lane == 0) {
