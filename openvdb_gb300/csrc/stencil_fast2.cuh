@@ -67,7 +67,6 @@ __device__ __forceinline__ float2 bd2(const Diff6x2& D) { return weno5x2(D.d[0],
 __global__ void __launch_bounds__(STENCIL_THREADS, 16) rk_stage_kernel_x2(const __grid_constant__ RkArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
-    __shared__ uint16_t list[LEAF_VOX];
     __shared__ float vtab[6][8];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
@@ -111,6 +110,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS, 16) rk_stage_kernel_x2(const 
     }
     stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
     load_tile(tile, st, a.gamma);
+    __syncthreads();  // the staging records are dead: the voxel list reuses their storage
+    uint16_t* list = reinterpret_cast<uint16_t*>(&st.rec[0][0]);
     const int n = build_list(list, st.am[0]);
     __syncthreads();
     const int npairs = (n + 1) >> 1;
