@@ -591,7 +591,8 @@ struct gbls_handle {
     unsigned int* cfl_d = nullptr;
     unsigned int* cfl_h = nullptr;
     bool overlap_dilation = false, on_side = false;
-    bool small_sort_ready = false;  // dynamic shared memory of k_sort_unique_small set on this device
+    bool small_sort_ready = false;
+    std::vector<uint8_t> flags_h;  // lower-node flags read back with the prune's status  // dynamic shared memory of k_sort_unique_small set on this device
     // Page-locked staging of the tracker's small node-table transfers, so
     // they are asynchronous copies; pin_ev marks the last copy issued from it.
     void* pin = nullptr;
@@ -946,8 +947,14 @@ void insert_nodes(gbls_handle& h, std::vector<uint64_t> miss) {
 void prune_nodes(gbls_handle& h, bool lower_changed) {
     const int64_t nl = int64_t(h.lower_keys_h.size());
     if (lower_changed && nl) {
-        std::vector<uint8_t> fl(static_cast<size_t>(nl));
-        h.download_small(h.flags, fl.data(), size_t(nl));
+        std::vector<uint8_t> fl;
+        if (h.flags_h.size() == size_t(nl)) {
+            fl.swap(h.flags_h);  // read back with the prune's status
+        } else {
+            fl.resize(static_cast<size_t>(nl));
+            h.download_small(h.flags, fl.data(), size_t(nl));
+        }
+        h.flags_h.clear();
         std::vector<uint64_t> keys;
         std::vector<int32_t> src;
         for (int64_t i = 0; i < nl; ++i) {
@@ -1316,6 +1323,7 @@ void relayout(gbls_handle& h, const uint64_t* pmask, int carry, int trim) {
 void prune_compact(gbls_handle& h) {
     const int64_t L = h.nleaf;
     bool lower_changed = false;
+    h.flags_h.clear();
     if (L > 0) {
         k_keep_flags<<<blocks_for(L, 256), 256, 0, h.stream>>>(L, h.cnt.p, h.keep.p);
         ++h.stats.kernel_launches;
@@ -1344,6 +1352,13 @@ void prune_compact(gbls_handle& h) {
             ++h.stats.kernel_launches;
         }
         CU(cudaGetLastError());
+        // the lower-node flags come back with the status (one read-back)
+        uint8_t* fl_pin = nullptr;
+        if (nl) {
+            fl_pin = static_cast<uint8_t*>(h.pinned(size_t(nl)));
+            CU(cudaMemcpyAsync(fl_pin, h.flags.p, size_t(nl), cudaMemcpyDeviceToHost, h.stream));
+            h.pinned_issued();
+        }
         if (h.before_prune_sync) h.before_prune_sync();
         h.read_status();
         const int64_t kept = int64_t(h.st_h->n_cand);
@@ -1351,6 +1366,7 @@ void prune_compact(gbls_handle& h) {
         h.nleaf = kept;
         h.nactive = int64_t(h.st_h->n_active);
         lower_changed = h.st_h->n_lower_empty > 0;
+        if (lower_changed) h.flags_h.assign(fl_pin, fl_pin + nl);
     } else if (h.batch_run) {
         CU(cudaMemsetAsync(h.inst_active.p, 0, size_t(h.ninst) * sizeof(unsigned long long), h.stream));
     }
