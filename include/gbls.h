@@ -239,6 +239,14 @@ enum {
     GBLS_FILTER_MEDIAN = 6
 };
 int gbls_filter(gbls_handle* h, int filter, int width, float value);
+/* The same filter with an alpha mask: the `mask` argument of every filter of
+ * tools::LevelSetFilter<FloatGrid, FloatGrid> (tools/LevelSetFilter.h:92-160)
+ * with setMaskRange(mask_min, mask_max) (:77-83) and invertMask(invert_mask)
+ * (:89).  alpha_mask is another single level set on the same device with the
+ * same transform (looked up at each voxel's index; GBLS_ERR_UNSUPPORTED
+ * otherwise); GBLS_ERR_VALUE unless mask_min < mask_max. */
+int gbls_filter_masked(gbls_handle* h, int filter, int width, float value, gbls_handle* alpha_mask,
+                       float mask_min, float mask_max, int invert_mask);
 
 /* ---- level-set morphing ------------------------------------------------------
  * Replaces tools::LevelSetMorphing<FloatGrid>::advect (tools/LevelSetMorph.h:

@@ -57,6 +57,7 @@ def lib():
         "gbls_advect": ([vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
                          P(C.c_uint64)], C.c_int),
         "gbls_filter": ([vp, C.c_int, C.c_int, C.c_float], C.c_int),
+        "gbls_filter_masked": ([vp, C.c_int, C.c_int, C.c_float, vp, C.c_float, C.c_float, C.c_int], C.c_int),
         "gbls_morph": ([vp, vp, vp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                         P(C.c_uint64)], C.c_int),
         "gbls_get_stats": ([vp, P(_abi.Stats)], C.c_int),

@@ -592,6 +592,13 @@ struct gbls_handle {
     unsigned int* cfl_h = nullptr;
     bool overlap_dilation = false, on_side = false;
     bool small_sort_ready = false;
+    // alpha mask of the filter call in progress (gbls_filter_masked)
+    struct {
+        bool on = false;
+        gbls_handle* grid = nullptr;
+        float min = 0.0f, inv_norm = 1.0f;
+        int invert = 0;
+    } filter_mask;
     std::vector<uint8_t> flags_h;  // lower-node flags read back with the prune's status  // dynamic shared memory of k_sort_unique_small set on this device
     // Page-locked staging of the tracker's small node-table transfers, so
     // they are asynchronous copies; pin_ev marks the last copy issued from it.
@@ -1726,6 +1733,13 @@ void filter_pass(gbls_handle& h, FilterArgs a, const char* msg) {
     a.gamma = h.gamma;
     a.keys = h.K();
     a.nodes = h.nodes();
+    if (h.filter_mask.on) {
+        a.has_mask = 1;
+        a.mask = lookup_grid(*h.filter_mask.grid);
+        a.mask_min = h.filter_mask.min;
+        a.mask_inv_norm = h.filter_mask.inv_norm;
+        a.invert = h.filter_mask.invert;
+    }
     start_intr(h, msg);
     if (h.mode == GBLS_MODE_PARITY) launch_filter_parity(a, h.stream);
     else launch_filter_fast(a, h.stream);
@@ -3013,6 +3027,37 @@ int gbls_filter(gbls_handle* h, int filter, int width, float value) {
         return GBLS_ERR_INTERRUPTED;
     }
     return rc;
+}
+
+// LevelSetFilter's filters with an alpha mask (tools/LevelSetFilter.h: the
+// `mask` argument of every filter, setMaskRange :77-83, invertMask :89): the
+// filter call of gbls_filter with the mask level set looked up at each
+// voxel's index.
+int gbls_filter_masked(gbls_handle* h, int filter, int width, float value, gbls_handle* alpha_mask,
+                       float mask_min, float mask_max, int invert_mask) {
+    if (!h || !alpha_mask) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    const int rc = guarded([&] {
+        DeviceGuard g(h->device);
+        if (!(mask_min < mask_max)) fail(GBLS_ERR_VALUE, "Invalid mask range (expects min < max)");
+        if (alpha_mask == h) fail(GBLS_ERR_UNSUPPORTED, "the alpha mask must be another level set");
+        if (alpha_mask->ninst > 1) fail(GBLS_ERR_UNSUPPORTED, "the alpha mask must be a single level set");
+        if (alpha_mask->device != h->device || alpha_mask->voxel_size != h->voxel_size ||
+            alpha_mask->map_type != h->map_type || alpha_mask->translation[0] != h->translation[0] ||
+            alpha_mask->translation[1] != h->translation[1] || alpha_mask->translation[2] != h->translation[2])
+            fail(GBLS_ERR_UNSUPPORTED, "the alpha mask must share the level set's device and transform "
+                                       "(the trilinear sampling of non-aligned grids has no device form)");
+        alpha_mask->sync();  // its tables are read on h's stream
+    });
+    if (rc != GBLS_OK) return rc;
+    h->filter_mask.on = true;
+    h->filter_mask.grid = alpha_mask;
+    h->filter_mask.min = mask_min;
+    h->filter_mask.inv_norm = 1.0f / (mask_max - mask_min);  // AlphaMask: mInvNorm(1/(max-min))
+    h->filter_mask.invert = invert_mask ? 1 : 0;
+    const int r = gbls_filter(h, filter, width, value);
+    h->filter_mask.on = false;
+    h->filter_mask.grid = nullptr;
+    return r;
 }
 
 // LevelSetMorphing::advect (tools/LevelSetMorph.h:243-262, Morph::advect

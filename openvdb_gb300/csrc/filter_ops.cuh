@@ -9,8 +9,14 @@
 //              order and scaled by 1/(2w+1) (Filter::Avg :206-219, boxImpl
 //              :327-349); w <= 3, the tile's halo;
 //   OFFSET     phi + offset (offsetImpl :479-497).
+// With an alpha mask (tools::AlphaMask, tools/Interpolation.h:545-579: a =
+// SmoothUnitStep((mask(ijk) - min) / (max - min)), b = 1 - a, swapped when
+// inverted) a voxel with a > 0 takes b * phi + a * filtered (OFFSET:
+// phi + a * offset; FILLET: filtered = phi + min(0, dt * kappa)), the others
+// keep their value (the reference leaves the copied buffer entry).
 #pragma once
 
+#include "morph_ops.cuh"
 #include "stencil_ops.cuh"
 
 namespace gbls {
@@ -39,16 +45,38 @@ struct FilterArgs {
     // full-tile passes: the 26 neighbour leaves are found by key
     const uint64_t* keys;
     NodeTables nodes;
+    // alpha mask: a device level set with the same transform, looked up at
+    // each voxel's own index
+    int has_mask, invert;
+    LookupGrid mask;
+    float mask_min, mask_inv_norm;  // min, 1 / (max - min)
 };
+
+// AlphaMask::operator() at voxel (word k, bit b) of the staged mask leaf:
+// returns a > 0 with a, b.
+template <class A>
+__device__ __forceinline__ bool filter_alpha(const FilterArgs& f, const LookupStage& mk, int k, int bit, float& al,
+                                             float& bl) {
+    al = smooth_unit_step<A>(A::mul(A::sub(lookup_value(mk, k, bit, f.mask.gamma), f.mask_min), f.mask_inv_norm));
+    bl = A::sub(1.0f, al);
+    if (f.invert) {
+        const float t = al;
+        al = bl;
+        bl = t;
+    }
+    return al > 0.0f;
+}
 
 template <class A>
 __global__ void __launch_bounds__(STENCIL_THREADS) filter_kernel(const FilterArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ uint16_t list[LEAF_VOX];
+    __shared__ LookupStage mk;
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
+    if (a.has_mask) stage_lookup(mk, a.mask, a.keys[l]);
     stage_masks(st, a.src, s, a.nbr + 6 * l, nullptr, nullptr);
     load_tile(tile, st, a.gamma);
     const int n = build_list(list, st.am[0]);
@@ -76,6 +104,12 @@ __global__ void __launch_bounds__(STENCIL_THREADS) filter_kernel(const FilterArg
             r = A::mul(sum, a.frac);
         } else {
             r = A::add(c, a.offset);
+        }
+        if (a.has_mask) {
+            float al, bl;
+            if (!filter_alpha<A>(a, mk, x, v & 63, al, bl)) r = c;
+            else if (a.op == FILTER_OFFSET) r = A::add(c, A::mul(al, a.offset));
+            else r = A::add(A::mul(bl, c), A::mul(al, r));
         }
         a.out[size_t(s) * LEAF_VOX + i] = r;
     }
@@ -222,9 +256,11 @@ __global__ void __launch_bounds__(STENCIL_THREADS) filter_full_kernel(const Filt
     __shared__ float tile[TILE_VOX];
     __shared__ FullStage st;
     __shared__ uint16_t list[LEAF_VOX];
+    __shared__ LookupStage mk;
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
+    if (a.has_mask) stage_lookup(mk, a.mask, a.keys[l]);
     stage_full(st, a, l);
     load_full_tile(tile, st, a.gamma);
     const int n = build_list(list, st.am[13]);
@@ -243,13 +279,22 @@ __global__ void __launch_bounds__(STENCIL_THREADS) filter_full_kernel(const Filt
                 // meanCurvatureNormGrad: alpha * invDx2 / (2 |grad|^2), 0 without a gradient
                 const float k = ok ? float(alpha_mean(c) * double(a.invdx2) / (2 * (c.normGrad * c.normGrad))) : 0.0f;
                 r = A::add(c0, A::mul(a.dt, k));
-            } else if (ok) {  // FILLET: principalCurvatures().first, applied when negative
-                const double ng = c.normGrad;
-                const double mean = alpha_mean(c) * double(a.inv2dx) / (ng * ng * ng);
-                const double tmp = sqrt(mean * mean - alpha_gauss(c) * double(a.invdx2) / ((ng * ng) * (ng * ng)));
-                const float k = float(mean - tmp);
-                if (k < 0.0f) r = A::add(c0, A::mul(a.dt, k));
+            } else {  // FILLET: principalCurvatures().first (0 without a gradient)
+                float k = 0.0f;
+                if (ok) {
+                    const double ng = c.normGrad;
+                    const double mean = alpha_mean(c) * double(a.inv2dx) / (ng * ng * ng);
+                    const double tmp =
+                        sqrt(mean * mean - alpha_gauss(c) * double(a.invdx2) / ((ng * ng) * (ng * ng)));
+                    k = float(mean - tmp);
+                }
+                if (a.has_mask) r = A::add(c0, ref_min(0.0f, A::mul(a.dt, k)));  // phi + Min(0, dt kappa)
+                else if (k < 0.0f) r = A::add(c0, A::mul(a.dt, k));              // applied when negative
             }
+        }
+        if (a.has_mask) {
+            float al, bl;
+            r = filter_alpha<A>(a, mk, x, v & 63, al, bl) ? A::add(A::mul(bl, c0), A::mul(al, r)) : c0;
         }
         a.out[size_t(s) * LEAF_VOX + i] = r;
     }

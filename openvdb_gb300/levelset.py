@@ -300,15 +300,40 @@ class LevelSetAdvection:
 
 
 class LevelSetFilter(LevelSetTracker):
-    """tools::LevelSetFilter<FloatGrid> (tools/LevelSetFilter.h:47-160): filters
-    on a DeviceLevelSet, each followed by track() with this tracker's state.
-    Masks (the optional alpha-mask argument) have no device form
-    (NotImplementedError); widths above 3 are refused (GBLS status)."""
+    """tools::LevelSetFilter<FloatGrid, FloatGrid> (tools/LevelSetFilter.h:47-160):
+    filters on a DeviceLevelSet, each followed by track() with this tracker's
+    state.  The optional alpha mask of every filter is a DeviceLevelSet on the
+    same device with the same transform (setMaskRange, invertMask as the
+    reference); widths above 3 are refused (GBLS status)."""
+
+    def __init__(self, grid, interrupter=None):
+        super().__init__(grid, interrupter)
+        self._min_mask, self._max_mask, self._invert = 0.0, 1.0, False
+
+    def minMask(self):
+        return self._min_mask
+
+    def maxMask(self):
+        return self._max_mask
+
+    def setMaskRange(self, lo, hi):
+        if not lo < hi:
+            raise ValueError("Invalid mask range (expects min < max)")
+        self._min_mask, self._max_mask = float(lo), float(hi)
+
+    def isMaskInverted(self):
+        return self._invert
+
+    def invertMask(self, invert=True):
+        self._invert = bool(invert)
 
     def _filter(self, op, width=1, value=0.0, mask=None):
-        if mask is not None:
-            raise NotImplementedError("masked level-set filters have no device form")
-        rc = lib().gbls_filter(self._grid.handle, int(op), int(width), np.float32(value))
+        if mask is None:
+            rc = lib().gbls_filter(self._grid.handle, int(op), int(width), np.float32(value))
+        else:
+            rc = lib().gbls_filter_masked(self._grid.handle, int(op), int(width), np.float32(value), mask.handle,
+                                          np.float32(self._min_mask), np.float32(self._max_mask),
+                                          1 if self._invert else 0)
         if rc == _abi.ERR_INTERRUPTED:
             return
         _call(rc)

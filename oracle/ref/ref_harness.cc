@@ -333,28 +333,40 @@ int vdbref_from_desc(const gbls_grid_desc* d, void** out) {
 // tools::LevelSetFilter<FloatGrid>: op 0 laplacian, 1 mean(width),
 // 2 gaussian(width), 3 offset(value), 4 meanCurvature, 5 fillet,
 // 6 median(width), with the given tracker state.
-int vdbref_filter(void* g, int op, int width, float value, int tspatial, int ttemporal, int normCount, int trim) {
+// With `mask` (may be null): the filter's alpha-mask argument, with
+// setMaskRange(minMask, maxMask) and invertMask(invert).
+int vdbref_filter_masked(void* g, void* mask, int op, int width, float value, int tspatial, int ttemporal,
+                         int normCount, int trim, float minMask, float maxMask, int invert) {
     try {
         FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
-        tools::LevelSetFilter<FloatGrid> f(grid);
+        tools::LevelSetFilter<FloatGrid, FloatGrid> f(grid);
         f.setSpatialScheme(math::BiasedGradientScheme(tspatial));
         f.setTemporalScheme(math::TemporalIntegrationScheme(ttemporal));
         f.setNormCount(normCount);
         f.setTrimming(tools::lstrack::TrimMode(trim));
+        const FloatGrid* m = mask ? static_cast<RefGrid*>(mask)->grid.get() : nullptr;
+        if (m) {
+            f.setMaskRange(minMask, maxMask);
+            f.invertMask(invert != 0);
+        }
         switch (op) {
-        case 0: f.laplacian(); break;
-        case 1: f.mean(width); break;
-        case 2: f.gaussian(width); break;
-        case 3: f.offset(value); break;
-        case 4: f.meanCurvature(); break;
-        case 5: f.fillet(); break;
-        case 6: f.median(width); break;
+        case 0: f.laplacian(m); break;
+        case 1: f.mean(width, m); break;
+        case 2: f.gaussian(width, m); break;
+        case 3: f.offset(value, m); break;
+        case 4: f.meanCurvature(m); break;
+        case 5: f.fillet(m); break;
+        case 6: f.median(width, m); break;
         default: return fail(GBLS_ERR_VALUE, "unknown filter");
         }
         return 0;
     } catch (const std::exception& e) {
         return fail(GBLS_ERR_VALUE, e.what());
     }
+}
+
+int vdbref_filter(void* g, int op, int width, float value, int tspatial, int ttemporal, int normCount, int trim) {
+    return vdbref_filter_masked(g, nullptr, op, width, value, tspatial, ttemporal, normCount, trim, 0.0f, 1.0f, 0);
 }
 
 // tools::LevelSetMorphing<FloatGrid>::advect towards `target`, with an

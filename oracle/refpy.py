@@ -42,6 +42,8 @@ def lib():
         L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
         L.vdbref_set_threads.argtypes = [C.c_int]
         L.vdbref_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4
+        L.vdbref_filter_masked.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4 + \
+            [C.c_float, C.c_float, C.c_int]
         L.vdbref_morph.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_float] * 4 + [C.c_int,
                                                                                     C.POINTER(C.c_uint64)]
         _lib = L
@@ -128,10 +130,14 @@ class RefGrid:
         return n.value
 
     def filter(self, op, width=1, value=0.0, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1, norm_count=3,
-               trim=_abi.TRIM_ALL):
+               trim=_abi.TRIM_ALL, mask=None, mask_range=(0.0, 1.0), invert=False):
         """tools::LevelSetFilter: op 0 laplacian, 1 mean, 2 gaussian, 3 offset, 4 meanCurvature,
-        5 fillet, 6 median."""
-        _check(lib().vdbref_filter(self.h, op, width, value, spatial, temporal, norm_count, trim))
+        5 fillet, 6 median; `mask` (a RefGrid) is the filter's alpha mask."""
+        if mask is None:
+            _check(lib().vdbref_filter(self.h, op, width, value, spatial, temporal, norm_count, trim))
+        else:
+            _check(lib().vdbref_filter_masked(self.h, mask.h, op, width, value, spatial, temporal, norm_count,
+                                              trim, mask_range[0], mask_range[1], 1 if invert else 0))
 
     def tracker_op(self, op, arg=0, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1,
                    norm_count=3, trim=_abi.TRIM_ALL):

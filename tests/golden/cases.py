@@ -218,8 +218,9 @@ MORPH_CASES = {
 
 # LevelSetFilter (tools/LevelSetFilter.h): filters applied in sequence to one
 # fixture; each op is (filter, width, value) with filter 0 laplacian, 1 mean,
-# 2 gaussian, 3 offset, 4 meanCurvature, 5 fillet, 6 median; tracker schemes
-# as (spatial, temporal, normCount).
+# 2 gaussian, 3 offset, 4 meanCurvature, 5 fillet, 6 median, or
+# (filter, width, value, (mask min, mask max), invert) with the case's alpha
+# mask level set; tracker schemes as (spatial, temporal, normCount).
 FILTER_CASES = {
     "filter_sphere_ops": dict(
         fixture=("sphere", 14.0, (0.5, -1.0, 2.0), 1.0, 3.0),
@@ -242,6 +243,16 @@ FILTER_CASES = {
         fixture=("torus", 14.0, 4.5, (0.5, 0.0, -0.5)),
         tracker=(HJ, RK1, 1),
         ops=[(5, 1, 0.0), (5, 1, 0.0), (4, 1, 0.0), (6, 1, 0.0), (5, 1, 0.0)],
+    ),
+    # every filter with an alpha mask (a sphere level set overlapping part of
+    # the fixture: voxels with alpha 0, fractional and 1), both polarities
+    "filter_masked": dict(
+        fixture=("sphere", 14.0, (0.5, -1.0, 2.0), 1.0, 3.0),
+        mask=("sphere", 9.0, (7.0, 3.0, 1.0), 1.0, 3.0),
+        tracker=(HJ, RK1, 3),
+        ops=[(0, 1, 0.0, (-2.0, 2.0), False), (1, 1, 0.0, (-1.0, 3.0), True), (3, 1, 1.1, (-2.0, 2.0), False),
+             (2, 1, 0.0, (-2.0, 2.0), True), (4, 1, 0.0, (-2.5, 1.5), False), (5, 1, 0.0, (-3.0, 1.0), False),
+             (6, 1, 0.0, (-2.0, 2.0), True), (3, 1, -0.6, (-1.0, 1.0), True), (5, 1, 0.0, (-2.0, 2.0), True)],
     ),
 }
 

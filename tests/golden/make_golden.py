@@ -8,7 +8,7 @@ sets come from openvdb_gb300.fixtures; for spheres the generator first
 checks that they equal the reference's own createLevelSetSphere bit for bit.
 Each case also runs with one and with all oracle threads, which must agree.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--filters-only]
 """
 import json
 import os
@@ -69,6 +69,20 @@ def run_reference(name, case, threads):
 
 def main():
     nthreads = os.cpu_count() or 1
+    if "--filters-only" in sys.argv:  # recompute the LevelSetFilter cases, keep the rest
+        path = os.path.join(HERE, "parity_cases.json")
+        result = json.load(open(path))
+        filt = {}
+        for name, case in FILTER_CASES.items():
+            a = run_filter(case, 1)
+            b = run_filter(case, nthreads)
+            assert a == b, "reference result depends on the thread count: " + name
+            filt[name] = a
+            print("%-32s ops=%d final active=%s" % (name, len(a) - 1, a[-1]["summary"]["active"]))
+        result["__filter__"] = filt
+        with open(path, "w") as f:
+            json.dump(result, f, indent=1, sort_keys=True)
+        return
     result = {}
     for name, case in CASES.items():
         a = run_reference(name, case, 1)
@@ -124,12 +138,17 @@ def run_filter(case, threads):
     refpy.set_threads(threads)
     src = make_fixture(case["fixture"])
     g = refpy.RefGrid.from_host(src)
+    mask = refpy.RefGrid.from_host(make_fixture(case["mask"])) if "mask" in case else None
     tsp, ttp, nc = case["tracker"]
     out = [{"op": "input", "digest": digest(src), "summary": summary(src)}]
-    for op, width, value in case["ops"]:
-        g.filter(op, width, value, spatial=tsp, temporal=ttp, norm_count=nc)
+    for op in case["ops"]:
+        kw = {}
+        if len(op) > 3:
+            kw = dict(mask=mask, mask_range=op[3], invert=op[4])
+        g.filter(op[0], op[1], op[2], spatial=tsp, temporal=ttp, norm_count=nc, **kw)
         h = g.to_host()
-        out.append({"op": [op, width, value], "digest": digest(h), "summary": summary(h)})
+        out.append({"op": [list(x) if isinstance(x, tuple) else x for x in op], "digest": digest(h),
+                    "summary": summary(h)})
     return out
 
 

@@ -3,7 +3,8 @@
 tests/golden/parity_cases.json["__filter__"] holds the digest of the full
 canonical grid after every filter call of the reference compiled from source
 (laplacian, mean curvature, fillet, mean and gaussian box filters, median,
-offsets; each followed by the tracker pass).  PARITY mode must reproduce every grid bit for bit.
+offsets, with and without an alpha mask; each followed by the tracker pass).
+PARITY mode must reproduce every grid bit for bit.
 """
 import json
 import os
@@ -31,11 +32,19 @@ def test_filter_parity(name):
     f.setSpatialScheme(tsp)
     f.setTemporalScheme(ttp)
     f.setNormCount(nc)
-    calls = {0: lambda w, v: f.laplacian(), 1: lambda w, v: f.mean(w), 2: lambda w, v: f.gaussian(w),
-             3: lambda w, v: f.offset(v), 4: lambda w, v: f.meanCurvature(), 5: lambda w, v: f.fillet(),
-             6: lambda w, v: f.median(w)}
-    for k, (op, width, value) in enumerate(case["ops"]):
-        calls[op](width, value)
+    mask = DeviceLevelSet(make_fixture(case["mask"])) if "mask" in case else None
+    if mask is not None:
+        mask.set_precision(PARITY)
+    calls = {0: lambda w, v, m: f.laplacian(m), 1: lambda w, v, m: f.mean(w, m), 2: lambda w, v, m: f.gaussian(w, m),
+             3: lambda w, v, m: f.offset(v, m), 4: lambda w, v, m: f.meanCurvature(m), 5: lambda w, v, m: f.fillet(m),
+             6: lambda w, v, m: f.median(w, m)}
+    for k, op in enumerate(case["ops"]):
+        m = None
+        if len(op) > 3:
+            f.setMaskRange(*op[3])
+            f.invertMask(op[4])
+            m = mask
+        calls[op[0]](op[1], op[2], m)
         assert digest(dev.to_host()) == gold[k + 1]["digest"], (name, k, op, gold[k + 1]["summary"])
 
 
@@ -47,3 +56,21 @@ def test_filter_widths_beyond_the_halo_are_refused():
         with pytest.raises(GblsError) as e:
             call()
         assert e.value.code == _abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+def test_filter_mask_checks():
+    """setMaskRange refuses min >= max (ValueError, as the reference); the mask
+    must be another level set with the same transform."""
+    from openvdb_gb300 import _abi, fixtures
+    dev = DeviceLevelSet(fixtures.sphere(8.0))
+    f = LevelSetFilter(dev)
+    with pytest.raises(ValueError):
+        f.setMaskRange(1.0, 1.0)
+    with pytest.raises(GblsError) as e:
+        f.laplacian(dev)
+    assert e.value.code == _abi.ERR_UNSUPPORTED
+    other = DeviceLevelSet(fixtures.sphere(8.0, voxel_size=0.5))
+    with pytest.raises(GblsError) as e:
+        f.laplacian(other)
+    assert e.value.code == _abi.ERR_UNSUPPORTED
