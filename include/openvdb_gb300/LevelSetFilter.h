@@ -5,8 +5,11 @@
 // LevelSetTracker (the drop-in one) with filters; every filter uploads the
 // grid, runs the filter and the tracker pass on the device and writes the
 // result back into the same tree.  Every filter has a device form
-// (mean, gaussian and median for half widths 1..3); calls with an alpha
-// mask throw NotImplementedError.
+// (mean, gaussian and median for half widths 1..3), with or without an alpha
+// mask.  The mask is uploaded as a device level set: a mask grid that is not
+// a narrow-band level set (positive background, inactive values
+// +-background) or whose transform differs from the filtered grid's has no
+// device form and throws (RuntimeError / NotImplementedError).
 //
 //   openvdb_gb300::tools::LevelSetFilter<openvdb::FloatGrid> filter(*grid);
 //   filter.gaussian(1);
@@ -59,12 +62,20 @@ public:
 
 private:
     void apply(int filter, int width, float value, const MaskType* mask) {
-        if (mask) OPENVDB_THROW(openvdb::NotImplementedError, "masked level-set filters have no device form");
-        this->run([=](gbls_handle* h) { return gbls_filter(h, filter, width, value); });
+        if (!mask) {
+            this->run([=](gbls_handle* h) { return gbls_filter(h, filter, width, value); });
+            return;
+        }
+        mMaskDevice.upload(*mask);
+        gbls_handle* m = mMaskDevice.get();
+        const float lo = float(mMinMask), hi = float(mMaxMask);
+        const int inv = mInvertMask ? 1 : 0;
+        this->run([=](gbls_handle* h) { return gbls_filter_masked(h, filter, width, value, m, lo, hi, inv); });
     }
 
     AlphaType mMinMask, mMaxMask;
     bool mInvertMask;
+    detail::Handle mMaskDevice;  // the alpha mask as a device level set
 };
 
 }  // namespace tools

@@ -195,14 +195,22 @@ int main() {
     } catch (const openvdb::Exception& e) {
         std::printf("ok %d morph without a device: %s\n", ++g_n, e.what());
     }
-    // 8. filters: the tracker base, mask range checks, masks refused
+    // 8. filters: the tracker base, mask range checks; a mask that is not a
+    //    level set (zero background) is refused with an OpenVDB exception
     og::tools::LevelSetFilter<FloatGrid> filt(*src2);
     CHECK(filt.getNormCount() == 3 && filt.minMask() == 0.0f && filt.maxMask() == 1.0f);
+    threw = false;
+    try {
+        filt.setMaskRange(1.0f, 1.0f);
+    } catch (const ValueError&) {
+        threw = true;
+    }
+    CHECK(threw);
     FloatGrid maskGrid(0.0f);
     threw = false;
     try {
         filt.gaussian(1, &maskGrid);
-    } catch (const NotImplementedError&) {
+    } catch (const openvdb::Exception&) {
         threw = true;
     }
     CHECK(threw);
