@@ -202,6 +202,16 @@ int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr);
 /* ---- LevelSetTracker operations ---------------------------------------- */
 int gbls_track(gbls_handle* h);                              /* :302-315 */
 int gbls_normalize(gbls_handle* h);                          /* :394-446 */
+/* Replaces LevelSetTracker::normalize(const MaskT* mask) (tools/LevelSetTracker.h:
+ * 94, 398-416; Normalizer :661-670): renormalise only the active voxels of the
+ * mask leaves whose origins are leaves of the level set; the other active
+ * voxels keep their values.  The mask is given as mask_leaf_count leaf origins
+ * (xyz, multiples of 8) and 8 active-mask words per leaf (bit x<<6|y<<3|z).
+ * GBLS_ERR_UNSUPPORTED when the mask covers a voxel that is inactive in the
+ * level set (the reference would give that inactive voxel a value other than
+ * +-background) or for a batch handle. */
+int gbls_normalize_masked(gbls_handle* h, int64_t mask_leaf_count, const int32_t* mask_leaf_origins,
+                          const uint64_t* mask_leaf_masks);
 int gbls_prune(gbls_handle* h);                              /* :279-300 */
 int gbls_dilate(gbls_handle* h, int iterations);             /* :317-337 */
 int gbls_erode(gbls_handle* h, int iterations);              /* :339-349 */

@@ -12,6 +12,8 @@
 //   tracker.track();
 #pragma once
 
+#include <vector>
+
 #include <openvdb/tools/LevelSetTracker.h>
 #include <openvdb/util/NullInterrupter.h>
 
@@ -76,12 +78,25 @@ public:
     LevelSetTracker(const LevelSetTracker&) = delete;
     LevelSetTracker& operator=(const LevelSetTracker&) = delete;
 
-    // The masked form restricts renormalisation to a mask; the device
-    // library renormalises the whole band only.
+    // The masked form renormalises only the active voxels of the mask tree's
+    // leaves that share an origin with a leaf of the level set
+    // (gbls_normalize_masked); MaskType is a tree type.  A mask covering a
+    // voxel that is inactive in the level set throws NotImplementedError.
     template <typename MaskType>
     void normalize(const MaskType* mask) {
-        if (mask) OPENVDB_THROW(openvdb::NotImplementedError, "masked normalize has no device form");
-        run([](gbls_handle* h) { return gbls_normalize(h); });
+        if (!mask) {
+            run([](gbls_handle* h) { return gbls_normalize(h); });
+            return;
+        }
+        std::vector<int32_t> origins;
+        std::vector<uint64_t> words;
+        for (auto leaf = mask->cbeginLeaf(); leaf; ++leaf) {
+            const openvdb::Coord o = leaf->origin();
+            origins.insert(origins.end(), {o.x(), o.y(), o.z()});
+            for (int w = 0; w < 8; ++w) words.push_back(leaf->getValueMask().template getWord<uint64_t>(w));
+        }
+        const int64_t n = int64_t(origins.size() / 3);
+        run([&](gbls_handle* h) { return gbls_normalize_masked(h, n, origins.data(), words.data()); });
     }
     void normalize() { this->normalize<MaskTreeType>(nullptr); }
     void track() { run([](gbls_handle* h) { return gbls_track(h); }); }

@@ -48,6 +48,7 @@ def lib():
         "gbls_set_interrupter": ([vp, P(_abi.Interrupter)], C.c_int),
         "gbls_track": ([vp], C.c_int),
         "gbls_normalize": ([vp], C.c_int),
+        "gbls_normalize_masked": ([vp, C.c_int64, vp, vp], C.c_int),
         "gbls_prune": ([vp], C.c_int),
         "gbls_dilate": ([vp, C.c_int], C.c_int),
         "gbls_erode": ([vp, C.c_int], C.c_int),

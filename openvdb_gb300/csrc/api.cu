@@ -349,6 +349,26 @@ __global__ void __launch_bounds__(SMALL_SORT_THREADS) k_sort_unique_small(const 
     }
 }
 
+// Processed-voxel mask of a masked renormalisation (Normalizer with a mask,
+// tools/LevelSetTracker.h:661-670): for every leaf of the level set, the
+// active voxels of the mask leaf with the same origin (found by key among the
+// sorted mask keys), none without one.  A mask voxel that is inactive in the
+// level set sets *err (the renormalised value of an inactive voxel has no
+// place in the packed layout).
+__global__ void k_mask_from_leaves(int64_t n, const uint64_t* keys, const int32_t* slot, const uint64_t* am,
+                                   const uint64_t* mkeys, const uint64_t* mmasks, int64_t nm, uint64_t* pmask,
+                                   unsigned long long* err) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n * 8) return;
+    const int64_t l = i >> 3;
+    const int w = int(i & 7);
+    const int64_t j = find_u64(mkeys, nm, keys[l]);
+    const uint64_t bits = j >= 0 ? mmasks[size_t(j) * 8 + w] : 0;
+    const size_t s = size_t(slot[l]);
+    pmask[s * 8 + w] = bits;
+    if (bits & ~am[s * 8 + w]) atomicAdd(err, 1ull);
+}
+
 __global__ void k_keep_flags(int64_t n, const int32_t* cnt, int32_t* keep) {
     const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     if (l >= n) return;
@@ -2263,6 +2283,56 @@ int gbls_normalize(gbls_handle* h) {
         DeviceGuard g(h->device);
         check_scheme(h->tr_spatial, h->tr_temporal);
         normalize_pass(*h, h->am[h->mc].p, 0);
+        h->sync();
+    });
+}
+
+// LevelSetTracker::normalize(mask) (tools/LevelSetTracker.h:94, 398-416,
+// Normalizer :661-670): the renormalisation restricted to the active voxels
+// of the mask leaves that share an origin with a leaf of the level set, the
+// other active voxels unchanged.  The mask arrives as its leaves' origins and
+// active masks (x<<6 | y<<3 | z bit order).
+int gbls_normalize_masked(gbls_handle* h, int64_t mask_leaf_count, const int32_t* mask_leaf_origins,
+                          const uint64_t* mask_leaf_masks) {
+    if (!h || mask_leaf_count < 0 || (mask_leaf_count > 0 && (!mask_leaf_origins || !mask_leaf_masks))) {
+        g_last_error = "null argument or negative count";
+        return GBLS_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        check_scheme(h->tr_spatial, h->tr_temporal);
+        if (h->ninst > 1) fail(GBLS_ERR_UNSUPPORTED, "masked normalisation works on single level sets");
+        const int64_t nm = mask_leaf_count;
+        std::vector<std::pair<uint64_t, int64_t>> mk(static_cast<size_t>(nm));
+        for (int64_t i = 0; i < nm; ++i) {
+            const int32_t* o = mask_leaf_origins + 3 * i;
+            for (int a = 0; a < 3; ++a) {
+                if (o[a] % 8 != 0) fail(GBLS_ERR_INVALID_ARGUMENT, "mask leaf origin not aligned");
+                if (o[a] < -COORD_SAFE || o[a] >= COORD_SAFE) fail(GBLS_ERR_DOMAIN, "coordinate outside the supported range");
+            }
+            mk[size_t(i)] = {leaf_key(o[0], o[1], o[2]), i};
+        }
+        std::sort(mk.begin(), mk.end());
+        for (size_t i = 1; i < mk.size(); ++i)
+            if (mk[i].first == mk[i - 1].first) fail(GBLS_ERR_INVALID_ARGUMENT, "duplicate mask leaf");
+        std::vector<uint64_t> keys(static_cast<size_t>(nm)), masks(static_cast<size_t>(nm) * 8);
+        for (int64_t i = 0; i < nm; ++i) {
+            keys[size_t(i)] = mk[size_t(i)].first;
+            std::memcpy(&masks[size_t(i) * 8], mask_leaf_masks + mk[size_t(i)].second * 8, 64);
+        }
+        if (h->nleaf == 0) return;
+        DevArray<uint64_t> dkeys, dmasks;
+        dkeys.upload(keys.data(), keys.size(), h->stream);
+        dmasks.upload(masks.data(), masks.size(), h->stream);
+        h->clear_status();
+        k_mask_from_leaves<<<blocks_for(h->nleaf * 8, 256), 256, 0, h->stream>>>(
+            h->nleaf, h->K(), h->S(), h->am[h->mc].p, dkeys.p, dmasks.p, nm, h->emask.p, &h->st_d->n_cand);
+        ++h->stats.kernel_launches;
+        CU(cudaGetLastError());
+        h->read_status();
+        if (h->st_h->n_cand) fail(GBLS_ERR_UNSUPPORTED, "the mask covers voxels that are inactive in the level set");
+        normalize_pass(*h, h->emask.p, 0, 1);
+        h->nactive = -1;
         h->sync();
     });
 }

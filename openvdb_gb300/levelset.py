@@ -214,8 +214,18 @@ class LevelSetTracker:
     def track(self):
         _call(lib().gbls_track(self._grid.handle))
 
-    def normalize(self):
-        _call(lib().gbls_normalize(self._grid.handle))
+    def normalize(self, mask=None):
+        """normalize() or normalize(&mask): `mask` is (leaf origins [n, 3],
+        active masks [n, 8] uint64) of the mask tree's leaves; only their
+        active voxels in leaves of the level set are renormalised."""
+        if mask is None:
+            _call(lib().gbls_normalize(self._grid.handle))
+            return
+        o = np.ascontiguousarray(mask[0], dtype=np.int32).reshape(-1, 3)
+        m = np.ascontiguousarray(mask[1], dtype=np.uint64).reshape(-1, 8)
+        if len(o) != len(m):
+            raise ValueError("mask origins and masks differ in length")
+        _call(lib().gbls_normalize_masked(self._grid.handle, len(o), o.ctypes.data, m.ctypes.data))
 
     def prune(self):
         _call(lib().gbls_prune(self._grid.handle))

@@ -417,6 +417,26 @@ int vdbref_advect(void* g, const gbls_field_desc* f, int spatial, int temporal, 
     }
 }
 
+// LevelSetTracker::normalize(&mask) with a MaskTree holding the given leaf
+// origins and active masks.
+int vdbref_normalize_masked(void* g, int64_t n, const int32_t* origins, const uint64_t* masks, int tspatial,
+                            int ttemporal, int normCount, int trim) {
+    try {
+        FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+        MaskTree mask;
+        for (int64_t i = 0; i < n; ++i) {
+            auto* leaf = mask.touchLeaf(Coord(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]));
+            for (int w = 0; w < 8; ++w) leaf->getValueMask().template getWord<uint64_t>(w) = masks[8 * i + w];
+        }
+        tools::LevelSetTracker<FloatGrid> tr(grid);
+        configureTracker(tr, tspatial, ttemporal, normCount, trim);
+        tr.normalize(&mask);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
 // op: 0 track, 1 normalize, 2 prune, 3 dilate(arg), 4 erode(arg), 5 resize(arg)
 int vdbref_tracker_op(void* g, int op, int arg, int tspatial, int ttemporal, int normCount,
                       int trim, int* result) {

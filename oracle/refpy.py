@@ -8,6 +8,8 @@ time (the development container); `available()` reports whether it loaded.
 import ctypes as C
 import os
 
+import numpy as np
+
 from openvdb_gb300 import _abi
 from openvdb_gb300.grid import HostGrid
 
@@ -42,6 +44,7 @@ def lib():
         L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
         L.vdbref_set_threads.argtypes = [C.c_int]
         L.vdbref_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4
+        L.vdbref_normalize_masked.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p] + [C.c_int] * 4
         L.vdbref_filter_masked.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4 + \
             [C.c_float, C.c_float, C.c_int]
         L.vdbref_morph.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_float] * 4 + [C.c_int,
@@ -151,6 +154,14 @@ class RefGrid:
 
     def normalize(self, **kw):
         self.tracker_op(1, **kw)
+
+    def normalize_masked(self, origins, masks, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK1, norm_count=3,
+                         trim=_abi.TRIM_ALL):
+        """LevelSetTracker::normalize(&mask), the mask a MaskTree of the given leaves."""
+        o = np.ascontiguousarray(origins, dtype=np.int32)
+        m = np.ascontiguousarray(masks, dtype=np.uint64)
+        _check(lib().vdbref_normalize_masked(self.h, len(o), o.ctypes.data, m.ctypes.data, spatial, temporal,
+                                             norm_count, trim))
 
     def prune(self, **kw):
         self.tracker_op(2, **kw)

@@ -4,6 +4,8 @@ Each case builds an input level set, then applies a list of operations:
   ("advect", t0, t1)            LevelSetAdvection::advect with the case schemes
   ("track",) ("normalize",) ("prune",) ("dilate", n)
                                 LevelSetTracker operations
+  ("normalize_masked", lo, hi)  LevelSetTracker::normalize(&mask) with the mask of
+                                box_mask(grid, lo, hi)
   ("state", {...})              change tracker state (norm_count, tr_temporal, trim)
 The golden file records, after every operation, the SHA-256 digest of the
 grid's canonical arrays (openvdb_gb300.grid.digest) and the substep count.
@@ -15,6 +17,30 @@ from openvdb_gb300.fields import Field
 
 HJ = _abi.HJWENO5_BIAS
 RK1, RK2, RK3 = _abi.TVD_RK1, _abi.TVD_RK2, _abi.TVD_RK3
+
+
+def box_mask(grid, lo, hi):
+    """Leaf origins and active masks of the active voxels of `grid` whose index
+    lies in the box [lo, hi] (inclusive), plus one full leaf at (800, 800, 800)
+    where the test level sets have none."""
+    origins, masks = [], []
+    yz = np.arange(64)
+    for o, m in zip(grid.leaf_origins, grid.leaf_masks):
+        gy, gz = o[1] + (yz >> 3), o[2] + (yz & 7)
+        inside_yz = (gy >= lo[1]) & (gy <= hi[1]) & (gz >= lo[2]) & (gz <= hi[2])
+        pattern = np.uint64(0)
+        for b in np.nonzero(inside_yz)[0]:
+            pattern |= np.uint64(1) << np.uint64(b)
+        words = np.zeros(8, np.uint64)
+        for x in range(8):
+            if lo[0] <= o[0] + x <= hi[0]:
+                words[x] = m[x] & pattern
+        if words.any():
+            origins.append(o)
+            masks.append(words)
+    origins.append(np.array([800, 800, 800], np.int32))
+    masks.append(np.full(8, np.iinfo(np.uint64).max, np.uint64))
+    return np.array(origins, np.int32), np.array(masks, np.uint64)
 
 
 def smoothed_noise(n, sigma, amplitude, seed):
@@ -86,6 +112,16 @@ CASES = {
              ("state", {"trim": _abi.TRIM_EXTERIOR}), ("track",),
              ("state", {"trim": _abi.TRIM_NONE}), ("track",),
              ("state", {"trim": _abi.TRIM_ALL, "norm_count": 0}), ("track",)],
+    ),
+    # normalize(mask): the renormalisation restricted to the active voxels in
+    # an index box (the mask also holds a leaf the level set does not have)
+    "tracker_masked_normalize": dict(
+        port=False,  # the oracle's C++ restatement has no masked normalize
+        fixture=("sphere", 18.0, (0.5, 1.0, -2.0), 1.0, 3.0),
+        field=("constant", (0.0, 0.0, 0.0)),
+        schemes=(HJ, RK1, HJ, RK1, 3),
+        ops=[("normalize_masked", (-20, -20, -20), (4, 30, 30)), ("state", {"tr_temporal": RK2, "norm_count": 2}),
+             ("normalize_masked", (-6, -30, -5), (30, 9, 30)), ("track",)],
     ),
     "union8_deformation": dict(
         fixture=("union8",),

@@ -8,7 +8,7 @@ sets come from openvdb_gb300.fixtures; for spheres the generator first
 checks that they equal the reference's own createLevelSetSphere bit for bit.
 Each case also runs with one and with all oracle threads, which must agree.
 
-Usage: python tests/golden/make_golden.py [--filters-only]
+Usage: python tests/golden/make_golden.py [--filters-only | --only=case1,case2]
 """
 import json
 import os
@@ -19,7 +19,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from cases import BATCH, CASES, FILTER_CASES, MORPH_CASES, make_batch, make_field, make_fixture  # noqa: E402
+from cases import BATCH, CASES, FILTER_CASES, MORPH_CASES, box_mask, make_batch, make_field, make_fixture  # noqa: E402
 from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
 from oracle import refpy  # noqa: E402
 
@@ -58,6 +58,8 @@ def run_reference(name, case, threads):
             g.prune(**kw)
         elif op[0] == "dilate":
             g.dilate(op[1], **kw)
+        elif op[0] == "normalize_masked":
+            g.normalize_masked(*box_mask(g.to_host(), op[1], op[2]), **kw)
         else:
             raise ValueError(op)
         h = g.to_host()
@@ -69,6 +71,19 @@ def run_reference(name, case, threads):
 
 def main():
     nthreads = os.cpu_count() or 1
+    only = [a.split("=", 1)[1].split(",") for a in sys.argv if a.startswith("--only=")]
+    if only:  # recompute the named advection / tracker cases, keep the rest
+        path = os.path.join(HERE, "parity_cases.json")
+        result = json.load(open(path))
+        for name in only[0]:
+            a = run_reference(name, CASES[name], 1)
+            b = run_reference(name, CASES[name], nthreads)
+            assert a == b, "reference result depends on the thread count: " + name
+            result[name] = a
+            print("%-32s ops=%d final active=%s" % (name, len(a) - 1, a[-1].get("summary", {}).get("active")))
+        with open(path, "w") as f:
+            json.dump(result, f, indent=1, sort_keys=True)
+        return
     if "--filters-only" in sys.argv:  # recompute the LevelSetFilter cases, keep the rest
         path = os.path.join(HERE, "parity_cases.json")
         result = json.load(open(path))

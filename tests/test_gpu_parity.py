@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from cases import CASES, make_field, make_fixture
+from cases import CASES, box_mask, make_field, make_fixture
 from openvdb_gb300 import PARITY, DeviceLevelSet, LevelSetAdvection, LevelSetTracker, digest, summary
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -63,6 +63,8 @@ def run_case(name, mode=PARITY, check=True):
             tr.track()
         elif op[0] == "normalize":
             tr.normalize()
+        elif op[0] == "normalize_masked":
+            tr.normalize(box_mask(dev.to_host(), op[1], op[2]))
         elif op[0] == "prune":
             tr.prune()
         elif op[0] == "dilate":
