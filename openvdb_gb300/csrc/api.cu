@@ -612,6 +612,14 @@ struct gbls_handle {
     unsigned int* cfl_h = nullptr;
     bool overlap_dilation = false, on_side = false;
     bool small_sort_ready = false;
+    // CFL maximum of an analytic field at the end time of the last advect
+    // call, reused by the next call that starts there with the same field
+    // (any other operation on the level set clears it)
+    struct {
+        bool valid = false;
+        float t = 0.0f, v2 = 0.0f;
+        gbls_field_desc desc{};
+    } cfl_cache;
     // alpha mask of the filter call in progress (gbls_filter_masked)
     struct {
         bool on = false;
@@ -2113,6 +2121,12 @@ struct DeviceGuard {
 // ---------------------------------------------------------------------------
 extern "C" {
 
+// Every operation that changes a level set outside gbls_advect drops the
+// cached CFL maximum.
+static void touched(gbls_handle* h) {
+    if (h) h->cfl_cache.valid = false;
+}
+
 int gbls_abi_version(void) { return GBLS_ABI_VERSION; }
 
 const char* gbls_last_error(void) { return g_last_error.c_str(); }
@@ -2152,6 +2166,7 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
 }
 
 int gbls_upload(gbls_handle* h, const gbls_grid_desc* desc) {
+    touched(h);
     if (!h || !desc) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2236,6 +2251,7 @@ int gbls_get_tracker_state(gbls_handle* h, int* spatial, int* temporal, int* nor
 }
 
 int gbls_set_trimming(gbls_handle* h, int trim_mode) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     if (trim_mode < GBLS_TRIM_NONE || trim_mode > GBLS_TRIM_ALL) {
         g_last_error = "bad trim mode";
@@ -2268,6 +2284,7 @@ int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr) {
 }
 
 int gbls_track(gbls_handle* h) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2278,6 +2295,7 @@ int gbls_track(gbls_handle* h) {
 }
 
 int gbls_normalize(gbls_handle* h) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2294,6 +2312,7 @@ int gbls_normalize(gbls_handle* h) {
 // active masks (x<<6 | y<<3 | z bit order).
 int gbls_normalize_masked(gbls_handle* h, int64_t mask_leaf_count, const int32_t* mask_leaf_origins,
                           const uint64_t* mask_leaf_masks) {
+    touched(h);
     if (!h || mask_leaf_count < 0 || (mask_leaf_count > 0 && (!mask_leaf_origins || !mask_leaf_masks))) {
         g_last_error = "null argument or negative count";
         return GBLS_ERR_INVALID_ARGUMENT;
@@ -2338,6 +2357,7 @@ int gbls_normalize_masked(gbls_handle* h, int64_t mask_leaf_count, const int32_t
 }
 
 int gbls_prune(gbls_handle* h) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2353,6 +2373,7 @@ int gbls_prune(gbls_handle* h) {
 // NN_FACE dilation, the background grows by dx, and (normCount > 0) the
 // newly activated voxels are renormalised with the others held fixed.
 int gbls_dilate(gbls_handle* h, int iterations) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2379,6 +2400,7 @@ int gbls_dilate(gbls_handle* h, int iterations) {
 // LevelSetTracker::erode (tools/LevelSetTracker.h:339-349): NN_FACE erosion,
 // pruneLevelSet, then the background shrinks by iterations * dx.
 int gbls_erode(gbls_handle* h, int iterations) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2404,6 +2426,7 @@ int gbls_erode(gbls_handle* h, int iterations) {
 
 // LevelSetTracker::resize (tools/LevelSetTracker.h:351-364).
 int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
+    touched(h);
     if (changed) *changed = 0;
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     const int w_old = int(std::floor(h->gamma / float(h->voxel_size)));
@@ -2417,6 +2440,7 @@ int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
 
 // ---- adjoint -----------------------------------------------------------------
 int gbls_adjoint_record(gbls_handle* h, int enable) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2586,11 +2610,13 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
 
 int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final, float* dl_initial,
                           float* dl_velocity) {
+    touched(h);
     return adjoint_backward(h, field, dl_final, dl_initial, dl_velocity, false);
 }
 
 int gbls_adjoint_backward_accumulate(gbls_handle* h, const gbls_field* field, const float* dl_final,
                                      float* dl_initial, float* dl_velocity_device) {
+    touched(h);
     if (h && dl_velocity_device) {
         cudaPointerAttributes at{};
         if (cudaPointerGetAttributes(&at, dl_velocity_device) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
@@ -2936,9 +2962,20 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                               std::sqrt(3.0f);
         const float C = cfl > 0.0f ? cfl : cfl_ref;
         // the CFL reduction of substep k+1 rides on the read-back that ends
-        // the tracker pass of substep k
+        // the tracker pass of substep k; the first substep reuses the maximum
+        // the previous call reduced for its end time when nothing else has
+        // changed the level set since (analytic fields: the descriptor
+        // determines the field)
         bool have_next = false;
         float next_v2 = 0.0f;
+        const bool analytic = field->desc.kind == GBLS_FIELD_DEFORMATION || field->desc.kind == GBLS_FIELD_ROTATION;
+        const bool cacheable = analytic && !h->batch_run && !h->tape_on;
+        if (cacheable && h->cfl_cache.valid && h->cfl_cache.t == t0 &&
+            std::memcmp(&h->cfl_cache.desc, &field->desc, sizeof(gbls_field_desc)) == 0) {
+            have_next = true;
+            next_v2 = h->cfl_cache.v2;
+        }
+        h->cfl_cache.valid = false;
         struct Reset {
             gbls_handle* h;
             ~Reset() {
@@ -2983,7 +3020,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             ++count;
             const bool more = forward ? t0 < t1 : t0 > t1;
             bool queued = false;
-            if (more && field->desc.kind != GBLS_FIELD_CONSTANT) {
+            if ((more || cacheable) && field->desc.kind != GBLS_FIELD_CONSTANT) {
                 const float tn = t0;
                 if (overlap && !h->batch_run) {
                     // reduce on the side stream while the main stream prunes;
@@ -3010,6 +3047,12 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                 if (overlap && !h->batch_run) std::memcpy(&next_v2, h->cfl_h, sizeof(float));
                 else next_v2 = status_max_speed(*h);
                 have_next = true;
+                if (!more) {  // the end time's maximum, for the next call
+                    h->cfl_cache.valid = true;
+                    h->cfl_cache.t = t0;
+                    h->cfl_cache.v2 = next_v2;
+                    h->cfl_cache.desc = field->desc;
+                }
             }
         }
         h->sync();
@@ -3025,6 +3068,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
 // LevelSetFilter (tools/LevelSetFilter.h:93-157): one filter, then the
 // tracker pass with h's tracker state (the filter is a LevelSetTracker).
 int gbls_filter(gbls_handle* h, int filter, int width, float value) {
+    touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     bool interrupted = false;
     const int rc = guarded([&] {
@@ -3135,6 +3179,7 @@ int gbls_filter_masked(gbls_handle* h, int filter, int width, float value, gbls_
 // the speed sampled once, the RK stages and a tracker pass.
 int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial, int temporal, float t0,
                float t1, float mask_min, float mask_max, int invert_mask, uint64_t* substeps) {
+    touched(h);
     if (substeps) *substeps = 0;
     if (!h || !target) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     uint64_t count = 0;
