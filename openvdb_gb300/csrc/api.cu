@@ -10,6 +10,7 @@
 #include <cmath>
 #include <functional>
 #include <memory>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -272,14 +273,14 @@ union SmallSortStorage {
 constexpr size_t SMALL_SORT_SMEM = sizeof(SmallSortStorage);
 
 __global__ void __launch_bounds__(SMALL_SORT_THREADS) k_sort_unique_small(const uint64_t* cand, DevStatus* st,
-                                                                          uint64_t* out) {
+                                                                          uint64_t* out, int64_t limit) {
     extern __shared__ __align__(16) unsigned char small_sort_smem[];
     SmallSortStorage& sm = *reinterpret_cast<SmallSortStorage*>(small_sort_smem);
     __shared__ typename SmallScan::TempStorage scan;
     __shared__ uint64_t red_or[SMALL_SORT_THREADS / 32], red_and[SMALL_SORT_THREADS / 32];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int64_t n = int64_t(st->n_cand);
-    if (n > SMALL_SORT_CAP) {
+    if (n > SMALL_SORT_CAP || n > limit) {
         if (t == 0) {
             st->overflow = 1;
             st->n_unique = 0;
@@ -611,7 +612,11 @@ struct gbls_handle {
     unsigned int* cfl_d = nullptr;
     unsigned int* cfl_h = nullptr;
     bool overlap_dilation = false, on_side = false;
-    bool small_sort_ready = false;
+    bool small_sort_ready = false;  // dynamic shared memory of k_sort_unique_small set on this device
+    // Candidates above this many take the device-wide sort (SMALL_SORT_CAP;
+    // the environment variable GBLS_SMALL_SORT_LIMIT, read when the handle
+    // is created, lowers it so tests can exercise that path).
+    int64_t small_sort_limit = SMALL_SORT_CAP;
     // CFL maximum of an analytic field at the end time of the last advect
     // call, reused by the next call that starts there with the same field
     // (any other operation on the level set clears it)
@@ -627,7 +632,7 @@ struct gbls_handle {
         float min = 0.0f, inv_norm = 1.0f;
         int invert = 0;
     } filter_mask;
-    std::vector<uint8_t> flags_h;  // lower-node flags read back with the prune's status  // dynamic shared memory of k_sort_unique_small set on this device
+    std::vector<uint8_t> flags_h;  // lower-node flags read back with the prune's status
     // Page-locked staging of the tracker's small node-table transfers, so
     // they are asynchronous copies; pin_ev marks the last copy issued from it.
     void* pin = nullptr;
@@ -1100,7 +1105,8 @@ void dilate_topology(gbls_handle& h) {
                                 int(SMALL_SORT_SMEM)));
         h.small_sort_ready = true;
     }
-    k_sort_unique_small<<<1, SMALL_SORT_THREADS, SMALL_SORT_SMEM, h.stream>>>(h.cand.p, h.st_d, h.cand_sorted.p);
+    k_sort_unique_small<<<1, SMALL_SORT_THREADS, SMALL_SORT_SMEM, h.stream>>>(h.cand.p, h.st_d, h.cand_sorted.p,
+                                                                               h.small_sort_limit);
     k_new_leaves<<<blocks_for(cap, 128), 128, 0, h.stream>>>(0, nu, h.cand_sorted.p, h.free_slots.p, h.nfree,
                                                               h.new_keys.p, h.new_slots.p, h.am[h.mc].p,
                                                               h.sm[h.mc].p);
@@ -2121,6 +2127,14 @@ struct DeviceGuard {
 // ---------------------------------------------------------------------------
 extern "C" {
 
+// SMALL_SORT_CAP, or the smaller non-negative GBLS_SMALL_SORT_LIMIT.
+static int64_t small_sort_limit_from_env() {
+    const char* e = std::getenv("GBLS_SMALL_SORT_LIMIT");
+    if (!e || !*e) return SMALL_SORT_CAP;
+    const long long v = std::atoll(e);
+    return v < 0 ? SMALL_SORT_CAP : std::min<int64_t>(int64_t(v), SMALL_SORT_CAP);
+}
+
 // Every operation that changes a level set outside gbls_advect drops the
 // cached CFL maximum.
 static void touched(gbls_handle* h) {
@@ -2151,6 +2165,7 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
         DeviceGuard g(g_device);
         h = new gbls_handle;
         h->device = g_device;
+        h->small_sort_limit = small_sort_limit_from_env();
         CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
         CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
         CU(cudaMalloc(&h->acc_d, 2 * sizeof(unsigned long long)));
@@ -2636,6 +2651,7 @@ int gbls_batch_create(int32_t n, const gbls_grid_desc* descs, gbls_handle** out)
     const int rc = guarded([&] {
         DeviceGuard g(g_device);
         h = new gbls_handle;
+        h->small_sort_limit = small_sort_limit_from_env();
         h->device = g_device;
         CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
         CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));

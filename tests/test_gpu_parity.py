@@ -88,6 +88,17 @@ def test_parity_bit_exact(name):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", ["sphere20_deformation", "tracker_ops", "union8_deformation"])
+def test_parity_with_device_wide_candidate_sort(name, monkeypatch):
+    """The dilation's fallback for more candidates than one CTA sorts (the
+    device-wide sort, then new leaves and merge on host counts), forced for
+    every dilation of handles created while GBLS_SMALL_SORT_LIMIT is 0: the
+    same grids, bit for bit."""
+    monkeypatch.setenv("GBLS_SMALL_SORT_LIMIT", "0")
+    run_case(name)
+
+
+@pytest.mark.gpu
 def test_batch_bit_exact_per_instance():
     """Batched advection: every instance equals its own reference advect call
     (independent CFL substep sequences in shared launches)."""
