@@ -91,6 +91,44 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ---- replicas over torchrun ranks --------------------------------------------
+# The path is not sharded: with N ranks every rank advects its own copy of the
+# workload on its own GPU (weak scaling), the timed regions are bracketed by
+# barriers, and the line reports the units of all ranks over the slowest
+# rank's time.
+
+def dist_setup():
+    """(rank, world size, torch.distributed or None) from the torchrun
+    environment; one process per GPU (LOCAL_RANK)."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend, init_method="env://")
+    return dist.get_rank(), ws, dist
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def replica_totals(units, seconds, dist):
+    """(sum of units over ranks, max of seconds over ranks)."""
+    if dist is None:
+        return float(units), float(seconds)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=dev)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(u.item()), float(t.item())
+
+
 def measured_peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -134,8 +172,9 @@ def run_gb300(args):
     from openvdb_gb300.levelset import DeviceField
 
     torch.cuda.init()
-    dev_index = 0
+    dev_index = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev_index)
+    rank, world, dist = dist_setup()
     t_build = time.perf_counter()
     host, field = build_workload()
     t_build = time.perf_counter() - t_build
@@ -158,6 +197,8 @@ def run_gb300(args):
     dev.set_profiling(True)
     clocks = ClockSampler()
     clocks.start()
+    torch.cuda.synchronize()
+    dist_barrier(dist)
     times = []
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
@@ -171,11 +212,12 @@ def run_gb300(args):
         times.append(e0.elapsed_time(e1) / 1e3)
         t += 1.0
     torch.cuda.synchronize()
+    dist_barrier(dist)
     clk = clocks.stop()
     dev.set_profiling(False)
     st = dev.stats()
-    total = sum(times)
-    value = st["voxel_updates"] / total
+    all_updates, total = replica_totals(st["voxel_updates"], sum(times), dist)
+    value = all_updates / total
 
     peak, peak_kind = measured_peaks()
     rk_gbs = st["rk_bytes"] / (st["rk_ms"] / 1e3) / 1e9 if st["rk_ms"] > 0 else 0.0
@@ -212,6 +254,7 @@ def run_gb300(args):
         te = t
         e2e_updates = 0
         h2d = d2h = 0
+        dist_barrier(dist)
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             h2d += host_bytes(g)
@@ -224,7 +267,8 @@ def run_gb300(args):
             te += 1.0
         el = time.perf_counter() - t0
         d.close()
-        e2e = {"value": e2e_updates / el, "unit": UNIT, "h2d_bytes_per_step": h2d // args.e2e_steps,
+        e2e_all, el = replica_totals(e2e_updates, el, dist)
+        e2e = {"value": e2e_all / el, "unit": UNIT, "h2d_bytes_per_step": h2d // args.e2e_steps,
                "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
 
     cfg = dict(WORKLOAD)
@@ -232,11 +276,17 @@ def run_gb300(args):
                 "leaves_initial": int(host.leaf_count), "fixture_build_s": round(t_build, 2),
                 "substeps": int(st["substeps"]), "t_start": float(t - args.steps),
                 "active_voxels_end": int(st["active_voxels"]),
-                "rho_dilated": (st["dilated_voxels"] / st["voxel_updates"]) if st["voxel_updates"] else None})
+                "rho_dilated": (st["dilated_voxels"] / st["voxel_updates"]) if st["voxel_updates"] else None,
+                "replicas": world})
+    if dist is not None:
+        dist_barrier(dist)
+        dist.destroy_process_group()
+    if rank != 0:
+        return
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
-        "scaling": "replicas", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
         "config": cfg,
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -319,7 +369,7 @@ def run_batch(args):
     out = {
         "metric": METRIC, "value": st["voxel_updates"] / total, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
-        "scaling": "replicas", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
         "config": cfg,
         "roofline": {"bound": "hbm", "kernel": "rk_stage", "achieved": rk_gbs, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": rk_gbs / peak, "traffic": None,
