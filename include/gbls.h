@@ -368,6 +368,34 @@ int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* view);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);
 
+/* ---- .vdb files (host) ----------------------------------------------------
+ * OpenVDB's file format 225 for level-set FloatGrids (Tree_float_5_4_3),
+ * read and written on the host; errors through gbls_host_last_error.
+ * gbls_vdb_write replaces io::File::write (io/File.h:130, the stream layout
+ * of io/Archive.cc:1010-1080 and 1261-1450): `count` grids from exchange
+ * descriptors (tree order), named `names[i]` (NULL or "" allowed; unique
+ * names are made as io::Archive::write makes them), with the grid class
+ * "level set" and the statistics metadata io::Archive adds
+ * (file_bbox_min/max, file_voxel_count, file_compression), data compressed
+ * with COMPRESS_ACTIVE_MASK only (readable by every OpenVDB build).
+ * gbls_vdb_grid_count / gbls_vdb_grid_info list the grids (io::File::
+ * getGrids / readAllGridMetadata, io/File.h:107-150): unique name, grid type
+ * (with a "_HalfFloat" suffix for half-float storage) and class, written as
+ * NUL-terminated strings truncated to the given capacities.
+ * gbls_vdb_read replaces io::File::readGrid (io/File.h:150): the grid named
+ * `name` (unique name first, then grid name), or the `index`-th grid when
+ * `name` is NULL, as a host grid for gbls_host_grid_view / gbls_upload.
+ * GBLS_ERR_RUNTIME: not a VDB file, truncated or corrupt, non-uniform scale
+ * (the tracker's RuntimeError); GBLS_ERR_INVALID_ARGUMENT: no such grid;
+ * GBLS_ERR_UNSUPPORTED: another grid type, active tiles, Blosc/zlib data,
+ * instanced trees, rotated transforms, format versions before 222.         */
+int gbls_vdb_write(const char* path, int32_t count, const gbls_grid_desc* grids,
+                   const char* const* names);
+int gbls_vdb_grid_count(const char* path, int32_t* count);
+int gbls_vdb_grid_info(const char* path, int32_t index, char* name, int64_t name_cap,
+                       char* grid_type, int64_t type_cap, char* grid_class, int64_t class_cap);
+int gbls_vdb_read(const char* path, const char* name, int32_t index, gbls_host_grid** out);
+
 #ifdef __cplusplus
 }
 #endif

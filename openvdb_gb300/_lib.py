@@ -79,6 +79,11 @@ def lib():
         "gbls_host_grid_view": ([vp, P(_abi.GridDesc)], C.c_int),
         "gbls_host_grid_free": ([vp], C.c_int),
         "gbls_host_last_error": ([], C.c_char_p),
+        "gbls_vdb_write": ([C.c_char_p, C.c_int32, P(_abi.GridDesc), P(C.c_char_p)], C.c_int),
+        "gbls_vdb_grid_count": ([C.c_char_p, P(C.c_int32)], C.c_int),
+        "gbls_vdb_grid_info": ([C.c_char_p, C.c_int32, C.c_char_p, C.c_int64, C.c_char_p, C.c_int64,
+                                C.c_char_p, C.c_int64], C.c_int),
+        "gbls_vdb_read": ([C.c_char_p, C.c_char_p, C.c_int32, P(vp)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -23,21 +23,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "../../include/gbls.h"
-
-struct gbls_host_grid {
-    double voxel_size = 1.0;
-    float background = 3.0f;
-    std::vector<int32_t> leaf_origins;
-    std::vector<uint64_t> leaf_masks;
-    std::vector<float> leaf_values;
-    std::vector<int32_t> lower_origins;
-    std::vector<float> lower_tiles;
-    std::vector<int32_t> upper_origins;
-    std::vector<float> upper_tiles;
-    std::vector<int32_t> root_tile_origins;
-    std::vector<float> root_tile_values;
-};
+#include "host_grid.h"
 
 namespace {
 
@@ -296,6 +282,10 @@ void raster_parallel(int32_t imin, int32_t imax, Band&& band, std::map<uint64_t,
 
 }  // namespace
 
+namespace gbls_host {
+void set_error(const std::string& msg) { g_fix_error = msg; }
+}  // namespace gbls_host
+
 extern "C" {
 
 int gbls_host_sphere(float radius, const float center[3], float voxel_size, float half_width,
@@ -450,7 +440,8 @@ int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* d) {
     if (!g || !d) { g_fix_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     std::memset(d, 0, sizeof(*d));
     d->voxel_size = g->voxel_size;
-    d->map_type = GBLS_MAP_UNIFORM_SCALE;
+    for (int i = 0; i < 3; ++i) d->translation[i] = g->translation[i];
+    d->map_type = g->map_type;
     d->background = g->background;
     d->leaf_count = int64_t(g->leaf_origins.size() / 3);
     d->leaf_origins = g->leaf_origins.data();

@@ -28,6 +28,7 @@ def _from_native(handle):
 
         g = HostGrid(
             voxel_size=d.voxel_size, background=d.background, map_type=d.map_type,
+            translation=tuple(d.translation),
             leaf_origins=arr(d.leaf_origins, d.leaf_count, (3,), np.int32),
             leaf_masks=arr(d.leaf_masks, d.leaf_count, (8,), np.uint64),
             leaf_values=arr(d.leaf_values, d.leaf_count, (512,), np.float32),

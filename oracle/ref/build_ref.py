@@ -39,6 +39,7 @@ REF_SOURCES = [
     "openvdb/openvdb/util/Assert.cc",
     "ext/imath/openvdb/math/Half.cc",
     "openvdb/openvdb/io/Compression.cc",
+    "openvdb/openvdb/io/GridDescriptor.cc",
 ]
 
 

@@ -17,8 +17,11 @@
 #include <openvdb/tools/LevelSetTracker.h>
 #include <openvdb/tools/VelocityFields.h>
 
+#include <openvdb/io/GridDescriptor.h>
+
 #include <cstring>
 #include <exception>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -456,6 +459,145 @@ int vdbref_tracker_op(void* g, int op, int arg, int tspatial, int ttemporal, int
         }
         if (result) *result = r;
         return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_RUNTIME, e.what());
+    }
+}
+
+// ---- .vdb files through the reference's own serialisers ---------------------
+// io/Archive.cc needs Boost and is not built, so the file framing around the
+// grid record is restated here (header: io/Archive.cc:1010-1080; file
+// metadata, grid count and one grid record: io/Archive.cc:1269-1450); every
+// byte inside the record comes from the reference: io::GridDescriptor::
+// writeHeader/writeStreamPos, MetaMap::writeMeta, math::Transform::write,
+// Grid::writeTopology and Grid::writeBuffers, with the stream's compression
+// set to COMPRESS_ACTIVE_MASK (a build without Blosc/zlib).  The grid carries
+// class, name and the statistics io::Archive adds (file_bbox_min/max,
+// file_voxel_count, file_compression), not file_mem_bytes or the
+// delayed-load record.  `uuid36` is written verbatim so files compare
+// byte for byte.
+
+void registerIoTypes() {
+    static bool done = false;
+    if (done) return;
+    done = true;
+    if (!FloatGrid::isRegistered()) FloatGrid::registerGrid();
+    if (!math::UniformScaleMap::isRegistered()) math::UniformScaleMap::registerMap();
+    if (!math::UniformScaleTranslateMap::isRegistered()) math::UniformScaleTranslateMap::registerMap();
+    if (!math::TranslationMap::isRegistered()) math::TranslationMap::registerMap();
+    if (!math::ScaleMap::isRegistered()) math::ScaleMap::registerMap();
+    if (!math::ScaleTranslateMap::isRegistered()) math::ScaleTranslateMap::registerMap();
+    if (!math::AffineMap::isRegistered()) math::AffineMap::registerMap();
+    if (!StringMetadata::isRegisteredType()) StringMetadata::registerType();
+    if (!Vec3IMetadata::isRegisteredType()) Vec3IMetadata::registerType();
+    if (!Int64Metadata::isRegisteredType()) Int64Metadata::registerType();
+    if (!BoolMetadata::isRegisteredType()) BoolMetadata::registerType();
+}
+
+int vdbref_write_vdb(void* g, const char* name, const char* path, const char* uuid36, int half) {
+    try {
+        registerIoTypes();
+        FloatGrid& src = *static_cast<RefGrid*>(g)->grid;
+        GridBase::Ptr copy = src.copyGrid();
+        copy->setName(name);
+        copy->setGridClass(GRID_LEVEL_SET);
+        if (half) copy->setSaveFloatAsHalf(true);
+        const uint32_t compression = io::COMPRESS_ACTIVE_MASK;
+        const CoordBBox bbox = copy->evalActiveVoxelBoundingBox();
+        copy->insertMeta(GridBase::META_FILE_BBOX_MIN, Vec3IMetadata(bbox.min().asVec3i()));
+        copy->insertMeta(GridBase::META_FILE_BBOX_MAX, Vec3IMetadata(bbox.max().asVec3i()));
+        copy->insertMeta(GridBase::META_FILE_VOXEL_COUNT, Int64Metadata(copy->activeVoxelCount()));
+        copy->insertMeta(GridBase::META_FILE_COMPRESSION, StringMetadata(io::compressionToString(compression)));
+
+        std::ofstream os(path, std::ios::binary | std::ios::trunc);
+        if (!os) return fail(GBLS_ERR_RUNTIME, "cannot open output file");
+        io::setVersion(os, VersionId(OPENVDB_LIBRARY_MAJOR_VERSION, OPENVDB_LIBRARY_MINOR_VERSION),
+                       OPENVDB_FILE_VERSION);
+        io::setDataCompression(os, compression);
+        const int64_t magic = OPENVDB_MAGIC;
+        os.write(reinterpret_cast<const char*>(&magic), 8);
+        uint32_t v = OPENVDB_FILE_VERSION;
+        os.write(reinterpret_cast<const char*>(&v), 4);
+        v = OPENVDB_LIBRARY_MAJOR_VERSION;
+        os.write(reinterpret_cast<const char*>(&v), 4);
+        v = OPENVDB_LIBRARY_MINOR_VERSION;
+        os.write(reinterpret_cast<const char*>(&v), 4);
+        const char seekable = 1;
+        os.write(&seekable, 1);
+        os.write(uuid36, 36);
+        MetaMap().writeMeta(os);
+        const int32_t count = 1;
+        os.write(reinterpret_cast<const char*>(&count), 4);
+
+        io::GridDescriptor gd(name, copy->type(), copy->saveFloatAsHalf());
+        gd.writeHeader(os);
+        const int64_t offsetPos = int64_t(os.tellp());
+        gd.writeStreamPos(os);
+        gd.setGridPos(os.tellp());
+        os.write(reinterpret_cast<const char*>(&compression), 4);
+        copy->writeMeta(os);
+        copy->writeTransform(os);
+        copy->writeTopology(os);
+        gd.setBlockPos(os.tellp());
+        copy->writeBuffers(os);
+        gd.setEndPos(os.tellp());
+        os.seekp(offsetPos, std::ios_base::beg);
+        gd.writeStreamPos(os);
+        gd.seekToEnd(os);
+        if (!os) return fail(GBLS_ERR_RUNTIME, "write failed");
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_RUNTIME, e.what());
+    }
+}
+
+// Reads grid `name` (unique name or grid name) with the reference's
+// io::GridDescriptor::read, Grid::readMeta/readTransform/readTopology/
+// readBuffers; the header is parsed as io::Archive::readHeader does.
+int vdbref_read_vdb(const char* path, const char* name, void** out) {
+    try {
+        registerIoTypes();
+        std::ifstream is(path, std::ios::binary);
+        if (!is) return fail(GBLS_ERR_RUNTIME, "cannot open input file");
+        int64_t magic = 0;
+        uint32_t fileVersion = 0, major = 0, minor = 0;
+        char hasOffsets = 0;
+        char uuid[36];
+        is.read(reinterpret_cast<char*>(&magic), 8);
+        is.read(reinterpret_cast<char*>(&fileVersion), 4);
+        is.read(reinterpret_cast<char*>(&major), 4);
+        is.read(reinterpret_cast<char*>(&minor), 4);
+        is.read(&hasOffsets, 1);
+        is.read(uuid, 36);
+        if (!is || magic != OPENVDB_MAGIC) return fail(GBLS_ERR_RUNTIME, "not a VDB file");
+        io::setVersion(is, VersionId(major, minor), fileVersion);
+        MetaMap fileMeta;
+        fileMeta.readMeta(is);
+        int32_t count = 0;
+        is.read(reinterpret_cast<char*>(&count), 4);
+        for (int32_t i = 0; i < count; ++i) {
+            io::GridDescriptor gd;
+            GridBase::Ptr grid = gd.read(is);
+            if (gd.uniqueName() != name && gd.gridName() != name) {
+                if (!hasOffsets) return fail(GBLS_ERR_UNSUPPORTED, "grid skipping needs grid offsets");
+                gd.seekToEnd(is);
+                continue;
+            }
+            uint32_t c = 0;
+            is.read(reinterpret_cast<char*>(&c), 4);
+            io::setDataCompression(is, c);
+            grid->readMeta(is);
+            grid->readTransform(is);
+            grid->readTopology(is);
+            grid->readBuffers(is);
+            FloatGrid::Ptr fg = GridBase::grid<FloatGrid>(grid);
+            if (!fg) return fail(GBLS_ERR_UNSUPPORTED, "not a FloatGrid");
+            auto* rg = new RefGrid;
+            rg->grid = fg;
+            *out = rg;
+            return 0;
+        }
+        return fail(GBLS_ERR_INVALID_ARGUMENT, std::string("no grid named ") + name);
     } catch (const std::exception& e) {
         return fail(GBLS_ERR_RUNTIME, e.what());
     }

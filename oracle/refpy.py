@@ -49,6 +49,8 @@ def lib():
             [C.c_float, C.c_float, C.c_int]
         L.vdbref_morph.argtypes = [C.c_void_p] * 3 + [C.c_int] * 5 + [C.c_float] * 4 + [C.c_int,
                                                                                     C.POINTER(C.c_uint64)]
+        L.vdbref_write_vdb.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int]
+        L.vdbref_read_vdb.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]
         _lib = L
     return _lib
 
@@ -101,6 +103,19 @@ class RefGrid:
         h = C.c_void_p()
         _check(lib().vdbref_from_desc(C.byref(d), C.byref(h)))
         return cls(h.value)
+
+    @classmethod
+    def read_vdb(cls, path, name):
+        """The grid `name` of a .vdb file, read by the reference's own
+        GridDescriptor / MetaMap / Transform / tree deserialisers."""
+        h = C.c_void_p()
+        _check(lib().vdbref_read_vdb(os.fsencode(path), name.encode(), C.byref(h)))
+        return cls(h.value)
+
+    def write_vdb(self, path, name, uuid="0" * 36, half=False):
+        """A one-grid .vdb file written by the reference's own serialisers
+        (class, name and statistics metadata; active-mask compression)."""
+        _check(lib().vdbref_write_vdb(self.h, name.encode(), os.fsencode(path), uuid.encode(), int(half)))
 
     def counts(self):
         c = _abi.GridCounts()
