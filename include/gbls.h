@@ -396,6 +396,19 @@ int gbls_vdb_grid_info(const char* path, int32_t index, char* name, int64_t name
                        char* grid_type, int64_t type_cap, char* grid_class, int64_t class_cap);
 int gbls_vdb_read(const char* path, const char* name, int32_t index, gbls_host_grid** out);
 
+/* ---- NanoVDB export (host) -------------------------------------------------
+ * Replaces nanovdb::tools::createNanoGrid(openvdb::FloatGrid, StatsMode,
+ * CheckMode) (nanovdb/tools/CreateNanoGrid.h:162-168): the NanoGrid<float>
+ * buffer (NanoVDB 32.9, breadth-first) of a level set in the exchange
+ * layout, byte for byte what the reference writes.  stats_mode: 0 Disable,
+ * 1 BBox, 2 MinMax, 3 All (node statistics combined in tree order);
+ * checksum_mode: 0 Disable, 1 Partial (CRC-32 of the grid and tree headers).
+ * With out == NULL only *size is set; otherwise out_capacity must be at least
+ * the size.  Errors through gbls_host_last_error: GBLS_ERR_UNSUPPORTED for
+ * names of 256 characters or more and checksum mode Full.                  */
+int gbls_nanovdb_export(const gbls_grid_desc* desc, const char* name, int32_t stats_mode,
+                        int32_t checksum_mode, uint8_t* out, int64_t out_capacity, int64_t* size);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,454 @@
+// NanoVDB export of a level set, on the host.
+//
+// gbls_nanovdb_export stands in for nanovdb::tools::createNanoGrid applied
+// to an openvdb::FloatGrid (nanovdb/tools/CreateNanoGrid.h:162-168): the
+// breadth-first NanoGrid<float> buffer of NanoVDB 32.9 --
+//   GridData (672 B) | TreeData (64 B) | RootData (64 B) + root tiles (32 B
+//   each, in the source root's Coord order) | upper nodes (270,400 B) |
+//   lower nodes (33,856 B) | leaves (2,144 B), nodes in tree order
+// (CreateNanoGrid.h:930-957 offsets, 1188-1221 leaves, 1481-1527 internal
+// nodes, 1589-1614 root, 1660-1733 tree and grid; NanoVDB.h:1418-1573 Map,
+// 1944-2000 GridData, 2393-2400 TreeData, 2621-2700 RootData,
+// 3181-3215 InternalData).  The index-to-world map is the one CreateNanoGrid
+// derives from the grid's affine matrix and its inverse (openvdb/math/
+// Mat4.h:485-560 for a scale + translate matrix).  Statistics follow
+// nanovdb::tools::updateGridStats (tools/GridStats.h:244-442, 577-760):
+// per-node active bounding boxes, extrema, and the running mean / variance
+// combined child by child in tree order (the serial form of the reduction),
+// in double precision.  The checksum is the CRC-32 of the grid and tree
+// headers (tools/GridChecksum.h:206-230, 300-323; CheckMode::Partial).
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "host_grid.h"
+
+namespace {
+
+constexpr uint64_t kMagicGrid = 0x314244566f6e614eULL;  // "NanoVDB1"
+constexpr uint32_t kVersion = (32u << 21) | (9u << 10) | 2u;
+constexpr size_t kGridBytes = 672, kTreeBytes = 64, kRootBytes = 64, kTileBytes = 32;
+constexpr size_t kUpperBytes = 270400, kLowerBytes = 33856, kLeafBytes = 2144;
+constexpr size_t kUpperTableAt = 8256, kLowerTableAt = 1088;
+enum : uint32_t { kHasBBox = 2, kHasMinMax = 4, kHasAverage = 8, kHasStdDeviation = 16, kIsBreadthFirst = 32 };
+enum { kStatsDisable = 0, kStatsBBox = 1, kStatsMinMax = 2, kStatsAll = 3 };
+
+struct ExportError {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string& msg) { throw ExportError{code, msg}; }
+
+inline bool bit(const uint64_t* m, int i) { return (m[i >> 6] >> (i & 63)) & 1u; }
+
+template <class T> inline void put(std::vector<uint8_t>& b, size_t at, const T& v) { std::memcpy(b.data() + at, &v, sizeof(T)); }
+
+// Running extrema, mean and variance (nanovdb::tools::Stats<float, 0>).
+struct Stats {
+    float mn = FLT_MAX, mx = -FLT_MAX;
+    uint64_t n = 0;
+    double avg = 0.0, aux = 0.0;
+    void add(float v) {
+        if (v < mn) mn = v;
+        if (v > mx) mx = v;
+        n += 1;
+        const double delta = double(v) - avg;
+        avg += delta / double(n);
+        aux += delta * (double(v) - avg);
+    }
+    void add(const Stats& o, bool moments) {
+        if (!moments) {  // Extrema::add(Extrema)
+            if (o.mn < mn) mn = o.mn;
+            if (o.mx > mx) mx = o.mx;
+            return;
+        }
+        if (o.n == 0) return;
+        const double denom = 1.0 / double(n + o.n);
+        const double delta = o.avg - avg;
+        avg += denom * delta * double(o.n);
+        aux += o.aux + denom * delta * delta * double(n) * double(o.n);
+        if (o.mn < mn) mn = o.mn;
+        if (o.mx > mx) mx = o.mx;
+        n += o.n;
+    }
+    double dev() const { return std::sqrt(n < 2 ? 0.0 : aux / double(n)); }
+};
+
+struct BBox {
+    int32_t lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+    bool empty() const { return lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]; }
+    void add(const BBox& o) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], o.lo[k]);
+            hi[k] = std::max(hi[k], o.hi[k]);
+        }
+    }
+};
+
+struct NodeStats {
+    Stats stats;
+    BBox bbox;
+};
+
+// Writes min / max / average / standard deviation at `at` in the statistics
+// mode's extent (tools/GridStats.h:541-557).
+void put_stats(std::vector<uint8_t>& b, size_t at, const Stats& s, int mode) {
+    if (mode >= kStatsMinMax) {
+        put<float>(b, at, s.mn);
+        put<float>(b, at + 4, s.mx);
+    }
+    if (mode == kStatsAll) {
+        put<float>(b, at + 8, float(s.avg));
+        put<float>(b, at + 12, float(s.dev()));
+    }
+}
+
+void put_bbox(std::vector<uint8_t>& b, size_t at, const BBox& x) {
+    std::memcpy(b.data() + at, x.lo, 12);
+    std::memcpy(b.data() + at + 12, x.hi, 12);
+}
+
+// nanovdb Map (NanoVDB.h:1418-1573) of a uniform scale + translation.
+struct MapD {
+    double mat[9], inv[9], vec[3];
+    void apply(const double xyz[3], double out[3]) const {  // math::matMult with fma
+        for (int r = 0; r < 3; ++r)
+            out[r] = std::fma(xyz[0], mat[3 * r], std::fma(xyz[1], mat[3 * r + 1], std::fma(xyz[2], mat[3 * r + 2], vec[r])));
+    }
+};
+
+// Gauss-Jordan elimination with partial pivoting on a 4x4 matrix (rows
+// scaled by division, elimination below then above the pivots), the form
+// openvdb::math::Mat4::invert takes (openvdb/math/Mat4.h) when the 3x3
+// determinant is too small for the cofactor inverse.
+void gauss_jordan(const double a[4][4], double inv[4][4]) {
+    double t[4][4];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            t[r][c] = a[r][c];
+            inv[r][c] = r == c ? 1.0 : 0.0;
+        }
+    for (int i = 0; i < 4; ++i) {
+        int row = i;
+        double mx = std::fabs(t[i][i]);
+        for (int k = i + 1; k < 4; ++k)
+            if (std::fabs(t[k][i]) > mx) {
+                row = k;
+                mx = std::fabs(t[k][i]);
+            }
+        if (mx == 0.0) fail(GBLS_ERR_RUNTIME, "singular index-to-world matrix");
+        if (row != i)
+            for (int k = 0; k < 4; ++k) {
+                std::swap(t[row][k], t[i][k]);
+                std::swap(inv[row][k], inv[i][k]);
+            }
+        const double pivot = t[i][i];
+        for (int k = 0; k < 4; ++k) {
+            t[i][k] /= pivot;
+            inv[i][k] /= pivot;
+        }
+        for (int j = i + 1; j < 4; ++j) {
+            const double f = t[j][i];
+            if (f == 0.0) continue;
+            for (int k = 0; k < 4; ++k) {
+                t[j][k] -= t[i][k] * f;
+                inv[j][k] -= inv[i][k] * f;
+            }
+        }
+    }
+    for (int i = 3; i > 0; --i)
+        for (int j = 0; j < i; ++j) {
+            const double f = t[j][i];
+            if (f == 0.0) continue;
+            for (int k = 0; k < 4; ++k) inv[j][k] -= inv[i][k] * f;
+        }
+}
+
+MapD make_map(const gbls_grid_desc& d) {
+    MapD m{};
+    const double s = d.map_type == GBLS_MAP_TRANSLATION ? 1.0 : d.voxel_size;
+    double vec[3];
+    for (int k = 0; k < 3; ++k) vec[k] = d.map_type == GBLS_MAP_UNIFORM_SCALE ? 0.0 : d.translation[k];
+    for (int k = 0; k < 9; ++k) m.mat[k] = m.inv[k] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        m.mat[4 * k] = s;
+        m.vec[k] = vec[k];
+    }
+    // Mat4d::inverse of diag(s, s, s, 1) with the translation in its last
+    // row: 1/det(A) times the cofactors, or Gauss-Jordan when |det(A)| <= 1e-8
+    const double det = s * s * s;
+    if (std::fabs(det) <= 1e-8) {
+        const double a[4][4] = {{s, 0, 0, 0}, {0, s, 0, 0}, {0, 0, s, 0}, {vec[0], vec[1], vec[2], 1.0}};
+        double inv[4][4];
+        gauss_jordan(a, inv);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) m.inv[3 * r + c] = inv[c][r];  // stored transposed
+    } else {
+        const double inv = (1.0 / det) * (s * s);
+        for (int k = 0; k < 3; ++k) m.inv[4 * k] = inv;
+    }
+    return m;
+}
+
+void put_map(std::vector<uint8_t>& b, size_t at, const MapD& m) {
+    for (int k = 0; k < 9; ++k) put<float>(b, at + 4 * k, float(m.mat[k]));
+    for (int k = 0; k < 9; ++k) put<float>(b, at + 36 + 4 * k, float(m.inv[k]));
+    for (int k = 0; k < 3; ++k) put<float>(b, at + 72 + 4 * k, float(m.vec[k]));
+    put<float>(b, at + 84, 1.0f);
+    for (int k = 0; k < 9; ++k) put<double>(b, at + 88 + 8 * k, m.mat[k]);
+    for (int k = 0; k < 9; ++k) put<double>(b, at + 160 + 8 * k, m.inv[k]);
+    for (int k = 0; k < 3; ++k) put<double>(b, at + 232 + 8 * k, m.vec[k]);
+    put<double>(b, at + 256, 1.0);
+}
+
+uint32_t crc32(const uint8_t* p, size_t n) {
+    uint32_t lut[256];
+    for (uint32_t i = 0; i < 256; ++i) {
+        uint32_t c = i;
+        for (int k = 0; k < 8; ++k) c = (c >> 1) ^ ((c & 1) ? 0xEDB88320u : 0u);
+        lut[i] = c;
+    }
+    uint32_t crc = ~0u;
+    for (size_t i = 0; i < n; ++i) crc = lut[(crc ^ p[i]) & 0xFF] ^ (crc >> 8);
+    return ~crc;
+}
+
+inline uint64_t root_key(const int32_t* o) {
+    return uint64_t(uint32_t(o[2]) >> 12) | (uint64_t(uint32_t(o[1]) >> 12) << 21) |
+           (uint64_t(uint32_t(o[0]) >> 12) << 42);
+}
+
+std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int mode, int checksum) {
+    if (d.leaf_count < 0 || d.lower_count < 0 || d.upper_count < 0 || d.root_tile_count < 0)
+        fail(GBLS_ERR_INVALID_ARGUMENT, "negative count in grid descriptor");
+    if (mode < kStatsDisable || mode > kStatsAll) fail(GBLS_ERR_INVALID_ARGUMENT, "statistics mode must be 0-3");
+    if (checksum != 0 && checksum != 1)
+        fail(GBLS_ERR_UNSUPPORTED, "checksum mode must be 0 (disable) or 1 (partial)");
+    if (name.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
+    const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count, nt = d.root_tile_count;
+    const size_t table = size_t(nu + nt);
+    const size_t tree_at = kGridBytes, root_at = tree_at + kTreeBytes;
+    const size_t upper_at = root_at + kRootBytes + kTileBytes * table;
+    const size_t lower_at = upper_at + kUpperBytes * size_t(nu);
+    const size_t leaf_at = lower_at + kLowerBytes * size_t(nl);
+    const size_t total = leaf_at + kLeafBytes * size_t(nf);
+    std::vector<uint8_t> b(total, 0);
+    const bool minmax = mode >= kStatsMinMax, moments = mode == kStatsAll;
+
+    // leaves
+    std::vector<NodeStats> leaf_stats(static_cast<size_t>(nf));
+    for (int64_t f = 0; f < nf; ++f) {
+        const size_t at = leaf_at + kLeafBytes * size_t(f);
+        const int32_t* o = d.leaf_origins + 3 * f;
+        const uint64_t* m = d.leaf_masks + 8 * f;
+        const float* v = d.leaf_values + 512 * f;
+        std::memcpy(b.data() + at, o, 12);
+        std::memcpy(b.data() + at + 16, m, 64);
+        std::memcpy(b.data() + at + 96, v, 2048);
+        if (mode == kStatsDisable) continue;
+        NodeStats& ns = leaf_stats[size_t(f)];
+        bool any = false;
+        for (int i = 0; i < 512; ++i) {
+            if (!bit(m, i)) continue;
+            const int32_t c[3] = {o[0] + (i >> 6), o[1] + ((i >> 3) & 7), o[2] + (i & 7)};
+            for (int k = 0; k < 3; ++k) {
+                ns.bbox.lo[k] = std::min(ns.bbox.lo[k], c[k]);
+                ns.bbox.hi[k] = std::max(ns.bbox.hi[k], c[k]);
+            }
+            if (minmax) ns.stats.add(v[i]);
+            any = true;
+        }
+        if (!any) continue;
+        std::memcpy(b.data() + at, ns.bbox.lo, 12);
+        for (int k = 0; k < 3; ++k) b[at + 12 + k] = uint8_t(ns.bbox.hi[k] - ns.bbox.lo[k]);
+        b[at + 15] = 2;  // has a bounding box; rendering enabled
+        put_stats(b, at + 80, ns.stats, mode);
+    }
+
+    // internal nodes: child offsets, tile values, then statistics from the children
+    auto internal = [&](int64_t count, size_t base, size_t bytes, size_t table_at, int log2, const int32_t* origins,
+                        const float* tiles, int64_t child_count, const int32_t* child_origins, size_t child_base,
+                        size_t child_bytes, int child_log2, const std::vector<NodeStats>& child_stats,
+                        std::vector<NodeStats>& out_stats) {
+        const int dim = 1 << log2, nvals = 1 << (3 * log2), child_shift = child_log2;
+        out_stats.assign(size_t(count), NodeStats());
+        int64_t c = 0;
+        for (int64_t i = 0; i < count; ++i) {
+            const size_t at = base + bytes * size_t(i);
+            const int32_t* o = origins + 3 * i;
+            std::memcpy(b.data() + at, o, 12);
+            const int64_t c0 = c;
+            std::vector<uint8_t> is_child(size_t(nvals), 0);
+            for (; c < child_count; ++c) {
+                const int32_t* co = child_origins + 3 * c;
+                const int32_t span = dim << child_shift;
+                if ((co[0] & ~(span - 1)) != o[0] || (co[1] & ~(span - 1)) != o[1] || (co[2] & ~(span - 1)) != o[2]) break;
+                const int n = ((((co[0] - o[0]) >> child_shift) << (2 * log2)) | (((co[1] - o[1]) >> child_shift) << log2) |
+                               ((co[2] - o[2]) >> child_shift));
+                if (is_child[size_t(n)]) fail(GBLS_ERR_INVALID_ARGUMENT, "grid descriptor is not in tree order");
+                is_child[size_t(n)] = 1;
+                b[at + 32 + size_t(nvals / 8) + size_t(n >> 3)] |= uint8_t(1u << (n & 7));  // child mask
+                put<int64_t>(b, at + table_at + 8 * size_t(n),
+                             int64_t(child_base + child_bytes * size_t(c)) - int64_t(at));
+            }
+            for (int n = 0; n < nvals; ++n)
+                if (!is_child[size_t(n)]) put<float>(b, at + table_at + 8 * size_t(n), tiles[size_t(i) * size_t(nvals) + size_t(n)]);
+            if (mode == kStatsDisable) continue;
+            NodeStats& total = out_stats[size_t(i)];
+            // children are consecutive in tree order, which is their table order
+            for (int64_t k = c0; k < c; ++k) {
+                total.stats.add(child_stats[size_t(k)].stats, moments);
+                total.bbox.add(child_stats[size_t(k)].bbox);
+            }
+            put_bbox(b, at, total.bbox);  // empty (max, min) when no child has active values
+            if (total.bbox.empty()) {
+                put<uint64_t>(b, at + 24, 1);  // no active values: skip rendering
+                continue;
+            }
+            put<uint64_t>(b, at + 24, 2);
+            put_stats(b, at + 32 + size_t(nvals / 4), total.stats, mode);
+        }
+        if (c != child_count) fail(GBLS_ERR_INVALID_ARGUMENT, "grid descriptor is not in tree order (orphan child node)");
+    };
+    std::vector<NodeStats> lower_stats, upper_stats;
+    internal(nl, lower_at, kLowerBytes, kLowerTableAt, 4, d.lower_origins, d.lower_tiles, nf, d.leaf_origins, leaf_at,
+             kLeafBytes, 3, leaf_stats, lower_stats);
+    internal(nu, upper_at, kUpperBytes, kUpperTableAt, 5, d.upper_origins, d.upper_tiles, nl, d.lower_origins,
+             lower_at, kLowerBytes, 7, lower_stats, upper_stats);
+
+    // root: children and tiles merged in Coord order
+    std::vector<std::pair<int64_t, bool>> entries;  // (index, is child)
+    for (int64_t i = 0; i < nu; ++i) entries.push_back({i, true});
+    for (int64_t i = 0; i < nt; ++i) entries.push_back({i, false});
+    auto origin_of = [&](const std::pair<int64_t, bool>& e) {
+        return e.second ? d.upper_origins + 3 * e.first : d.root_tile_origins + 3 * e.first;
+    };
+    std::stable_sort(entries.begin(), entries.end(), [&](const auto& a, const auto& c) {
+        const int32_t *p = origin_of(a), *q = origin_of(c);
+        return std::lexicographical_compare(p, p + 3, q, q + 3);
+    });
+    NodeStats root_total;
+    for (size_t t = 0; t < entries.size(); ++t) {
+        const size_t at = root_at + kRootBytes + kTileBytes * t;
+        const int32_t* o = origin_of(entries[t]);
+        put<uint64_t>(b, at, root_key(o));
+        if (entries[t].second) {
+            put<int64_t>(b, at + 8, int64_t(upper_at + kUpperBytes * size_t(entries[t].first)) - int64_t(root_at));
+            root_total.stats.add(upper_stats.empty() ? Stats() : upper_stats[size_t(entries[t].first)].stats, moments);
+            if (!upper_stats.empty()) root_total.bbox.add(upper_stats[size_t(entries[t].first)].bbox);
+        } else {
+            put<float>(b, at + 20, d.root_tile_values[entries[t].first]);
+        }
+    }
+    put<uint32_t>(b, root_at + 24, uint32_t(table));
+    put<float>(b, root_at + 28, d.background);
+    BBox root_bbox;
+    if (table == 0 || mode == kStatsDisable) {
+        put<float>(b, root_at + 32, d.background);
+        put<float>(b, root_at + 36, d.background);
+    } else {
+        root_bbox = root_total.bbox;
+        if (mode == kStatsBBox) {
+            put<float>(b, root_at + 32, d.background);
+            put<float>(b, root_at + 36, d.background);
+        } else {
+            put_stats(b, root_at + 32, root_total.stats, mode);
+        }
+    }
+    put_bbox(b, root_at, root_bbox);
+
+    // tree
+    int64_t voxels = 0;
+    for (int64_t f = 0; f < nf; ++f)
+        for (int w = 0; w < 8; ++w) voxels += __builtin_popcountll(d.leaf_masks[8 * f + w]);
+    put<int64_t>(b, tree_at, nf ? int64_t(leaf_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 8, nl ? int64_t(lower_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 16, nu ? int64_t(upper_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 24, int64_t(root_at - tree_at));
+    put<uint32_t>(b, tree_at + 32, uint32_t(nf));
+    put<uint32_t>(b, tree_at + 36, uint32_t(nl));
+    put<uint32_t>(b, tree_at + 40, uint32_t(nu));
+    put<uint64_t>(b, tree_at + 56, uint64_t(voxels));
+
+    // grid
+    const MapD map = make_map(d);
+    put<uint64_t>(b, 0, kMagicGrid);
+    put<uint64_t>(b, 8, ~uint64_t(0));
+    put<uint32_t>(b, 16, kVersion);
+    uint32_t flags = kIsBreadthFirst;
+    if (mode != kStatsDisable) {
+        if (!root_bbox.empty()) flags |= kHasBBox;
+        if (minmax) flags |= kHasMinMax;
+        if (moments) flags |= kHasAverage | kHasStdDeviation;
+    }
+    put<uint32_t>(b, 20, flags);
+    put<uint32_t>(b, 28, 1);  // grid count
+    put<uint64_t>(b, 32, uint64_t(total));
+    std::memcpy(b.data() + 40, name.data(), name.size());
+    put_map(b, 296, map);
+    double wlo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, whi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    if (mode != kStatsDisable && !root_bbox.empty()) {
+        const int32_t lo[3] = {root_bbox.lo[0], root_bbox.lo[1], root_bbox.lo[2]};
+        const int32_t hi[3] = {root_bbox.hi[0] + 1, root_bbox.hi[1] + 1, root_bbox.hi[2] + 1};
+        for (int corner = 0; corner < 8; ++corner) {
+            const double p[3] = {double((corner & 4) ? hi[0] : lo[0]), double((corner & 2) ? hi[1] : lo[1]),
+                                 double((corner & 1) ? hi[2] : lo[2])};
+            double w[3];
+            map.apply(p, w);
+            for (int k = 0; k < 3; ++k) {
+                wlo[k] = std::min(wlo[k], w[k]);
+                whi[k] = std::max(whi[k], w[k]);
+            }
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        put<double>(b, 560 + 8 * k, wlo[k]);
+        put<double>(b, 584 + 8 * k, whi[k]);
+    }
+    const double one[3] = {1.0, 1.0, 1.0}, zero[3] = {0.0, 0.0, 0.0};
+    double a1[3], a0[3];
+    map.apply(one, a1);
+    map.apply(zero, a0);
+    for (int k = 0; k < 3; ++k) put<double>(b, 608 + 8 * k, a1[k] - a0[k]);
+    put<uint32_t>(b, 632, 1);  // GridClass::LevelSet
+    put<uint32_t>(b, 636, 1);  // GridType::Float
+    put<int64_t>(b, 640, int64_t(total));  // no blind data
+    if (checksum == 1) {
+        const uint32_t head = crc32(b.data() + 16, kGridBytes + kTreeBytes - 16);
+        put<uint64_t>(b, 8, (~uint64_t(0) << 32) | head);
+    }
+    return b;
+}
+
+thread_local std::vector<uint8_t> g_last;
+
+}  // namespace
+
+extern "C" {
+
+int gbls_nanovdb_export(const gbls_grid_desc* desc, const char* name, int32_t stats_mode, int32_t checksum_mode,
+                        uint8_t* out, int64_t out_capacity, int64_t* size) {
+    try {
+        if (!desc || !size) fail(GBLS_ERR_INVALID_ARGUMENT, "null argument");
+        std::vector<uint8_t> b = build(*desc, name ? name : "", stats_mode, checksum_mode);
+        *size = int64_t(b.size());
+        if (out) {
+            if (out_capacity < *size) fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer too small");
+            std::memcpy(out, b.data(), b.size());
+        }
+        return GBLS_OK;
+    } catch (const ExportError& e) {
+        gbls_host::set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        gbls_host::set_error("out of host memory");
+        return GBLS_ERR_OUT_OF_MEMORY;
+    }
+}
+
+}  // extern "C"

@@ -90,12 +90,14 @@ def build(verbose=False):
         "-I" + os.path.join(HERE, "tbbshim"),
         "-I" + os.path.join(ref, "openvdb"),
         "-I" + os.path.join(ref, "ext/imath"),
+        "-I" + os.path.join(ref, "nanovdb"),
         "-I" + os.path.join(REPO, "include"),
         "-pthread",
     ]
     flags = [f for f in flags if not f.startswith("-DOPENVDB_USE_DELAYED")]
     srcs = [os.path.join(ref, s) for s in REF_SOURCES] + [os.path.join(HERE, "ref_harness.cc"),
-                                                       os.path.join(HERE, "io_stubs.cc")]
+                                                       os.path.join(HERE, "io_stubs.cc"),
+                                                       os.path.join(HERE, "nano_harness.cc")]
     hdr_deps = [os.path.join(HERE, "ref_harness.cc"), os.path.join(REPO, "include", "gbls.h"),
                 os.path.join(REPO, "include", "gbls_fields.h")]
 

@@ -464,6 +464,14 @@ int vdbref_tracker_op(void* g, int op, int arg, int tspatial, int ttemporal, int
     }
 }
 
+}  // extern "C"
+
+namespace vdbref_detail {
+openvdb::FloatGrid::Ptr grid_of(void* g) { return static_cast<RefGrid*>(g)->grid; }
+}
+
+extern "C" {
+
 // ---- .vdb files through the reference's own serialisers ---------------------
 // io/Archive.cc needs Boost and is not built, so the file framing around the
 // grid record is restated here (header: io/Archive.cc:1010-1080; file

@@ -51,6 +51,9 @@ def lib():
                                                                                     C.POINTER(C.c_uint64)]
         L.vdbref_write_vdb.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int]
         L.vdbref_read_vdb.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]
+        L.vdbref_nano_float.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_int64,
+                                        C.POINTER(C.c_int64)]
+        L.vdbref_nano_last_error.restype = C.c_char_p
         _lib = L
     return _lib
 
@@ -116,6 +119,18 @@ class RefGrid:
         """A one-grid .vdb file written by the reference's own serialisers
         (class, name and statistics metadata; active-mask compression)."""
         _check(lib().vdbref_write_vdb(self.h, name.encode(), os.fsencode(path), uuid.encode(), int(half)))
+
+    def nanovdb(self, name, stats=3, checksum=1):
+        """nanovdb::tools::createNanoGrid(grid, StatsMode(stats), CheckMode(checksum))
+        of the reference, as a uint8 array."""
+        n = C.c_int64()
+        L = lib()
+        if L.vdbref_nano_float(self.h, name.encode(), stats, checksum, None, 0, C.byref(n)):
+            raise RuntimeError(L.vdbref_nano_last_error().decode())
+        buf = np.zeros(n.value, np.uint8)
+        if L.vdbref_nano_float(self.h, name.encode(), stats, checksum, buf.ctypes.data, n.value, C.byref(n)):
+            raise RuntimeError(L.vdbref_nano_last_error().decode())
+        return buf
 
     def counts(self):
         c = _abi.GridCounts()

@@ -1,0 +1,97 @@
+"""NanoVDB export (host code, no GPU).
+
+Every statistics mode (Disable, BBox, MinMax, All) and both checksum modes
+are compared byte for byte with the reference's own
+nanovdb::tools::createNanoGrid of the same FloatGrid (compiled from the
+reference sources into oracle/_ref; serial statistics).  Grids: a sphere,
+a union across several root entries with negative origins, explicit root
+tiles, a translated map, planted inactive values, an empty grid, and voxel
+sizes on both sides of the matrix inverse's Gauss-Jordan branch.  The
+header checks below run everywhere.
+"""
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+from openvdb_gb300 import HostGrid, fixtures
+from openvdb_gb300.nanovdb import to_nanovdb
+
+import test_vdbfile as tv
+
+
+def _refpy():
+    refpy = pytest.importorskip("oracle.refpy")
+    if not refpy.available():
+        pytest.skip("reference oracle library not built on this host")
+    return refpy
+
+
+def _grids():
+    g = dict(tv.grids())
+    g["empty"] = HostGrid(voxel_size=0.1, background=0.3)
+    g["root_tiles"] = tv._clone(g["union"], root_tile_origins=np.array([[8192, 0, 0], [-8192, 4096, 0]], np.int32),
+                                root_tile_values=np.array([-3.0, 3.0], np.float32))
+    g["dx_0.001_translated"] = tv._clone(g["sphere"], voxel_size=0.001, translation=(0.25, -1.0, 3.5), map_type=1)
+    g["dx_0.003"] = tv._clone(g["sphere"], voxel_size=0.003)
+    return g
+
+
+GRIDS = None
+
+
+def grids():
+    global GRIDS
+    if GRIDS is None:
+        GRIDS = _grids()
+    return GRIDS
+
+
+NAMES = ["sphere", "union", "translated", "planted", "empty", "root_tiles", "dx_0.001_translated", "dx_0.003"]
+
+
+@pytest.mark.parametrize("checksum", ["disable", "partial"])
+@pytest.mark.parametrize("stats", ["disable", "bbox", "minmax", "all"])
+@pytest.mark.parametrize("name", NAMES)
+def test_bytes_equal_reference(name, stats, checksum):
+    refpy = _refpy()
+    g = grids()[name]
+    mine = to_nanovdb(g, name, stats, checksum)
+    ref = refpy.RefGrid.from_host(g).nanovdb(name, ["disable", "bbox", "minmax", "all"].index(stats),
+                                             ["disable", "partial"].index(checksum))
+    assert mine.size == ref.size
+    assert np.array_equal(mine, ref)
+
+
+def test_header_fields_and_checksum():
+    g = grids()["union"]
+    b = to_nanovdb(g, "union").tobytes()
+    magic, checksum, version, flags, index, count, size = struct.unpack_from("<QQIIIIQ", b, 0)
+    assert magic == 0x314244566F6E614E and version == (32 << 21) | (9 << 10) | 2
+    assert flags == 0b111110 and (index, count, size) == (0, 1, len(b))
+    assert b[40:45] == b"union" and b[45] == 0
+    assert checksum >> 32 == 0xFFFFFFFF and checksum & 0xFFFFFFFF == zlib.crc32(b[16:672 + 64])
+    node_offsets = struct.unpack_from("<4q", b, 672)
+    node_counts = struct.unpack_from("<3I", b, 672 + 32)
+    voxels = struct.unpack_from("<Q", b, 672 + 56)[0]
+    assert node_counts == (len(g.leaf_origins), len(g.lower_origins), len(g.upper_origins))
+    assert voxels == g.active_voxel_count()
+    leaf_at = 672 + node_offsets[0]
+    assert leaf_at + 2144 * len(g.leaf_origins) == len(b)
+    first = np.frombuffer(b, np.float32, 512, leaf_at + 96)
+    assert np.array_equal(first, g.leaf_values[0])
+
+
+def test_rejects_long_names_and_full_checksum():
+    g = grids()["sphere"]
+    from openvdb_gb300._lib import GblsError
+    with pytest.raises(GblsError):
+        to_nanovdb(g, "x" * 300)
+    from openvdb_gb300 import nanovdb
+    nanovdb.CHECKSUM["full"] = 2
+    try:
+        with pytest.raises(GblsError):
+            to_nanovdb(g, "s", checksum="full")
+    finally:
+        del nanovdb.CHECKSUM["full"]
