@@ -408,6 +408,18 @@ int gbls_vdb_read(const char* path, const char* name, int32_t index, gbls_host_g
  * names of 256 characters or more and checksum mode Full.                  */
 int gbls_nanovdb_export(const gbls_grid_desc* desc, const char* name, int32_t stats_mode,
                         int32_t checksum_mode, uint8_t* out, int64_t out_capacity, int64_t* size);
+/* NanoVDB index grid: createNanoGrid<FloatGrid, ValueOnIndex>(grid, channels,
+ * includeStats, includeTiles) (CreateNanoGrid.h:184-190): nodes hold offsets
+ * into a value array (background first, four statistics slots per node when
+ * both flags are set, active values per leaf), leaves their 9-bit prefix
+ * sums; with channels = 1 the value array follows as blind data
+ * "channel_0".  Byte for byte the reference's buffer, except the alignment
+ * padding after the channel, which the reference leaves uninitialised.
+ * channels > 1 is GBLS_ERR_UNSUPPORTED: the reference copies channel i from
+ * (its start - value count), across that padding.                          */
+int gbls_nanovdb_export_index(const gbls_grid_desc* desc, const char* name, int32_t channels,
+                              int32_t include_stats, int32_t include_tiles, int32_t checksum_mode,
+                              uint8_t* out, int64_t out_capacity, int64_t* size);
 
 #ifdef __cplusplus
 }

@@ -425,7 +425,230 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
     return b;
 }
 
-thread_local std::vector<uint8_t> g_last;
+// NanoGrid<ValueOnIndex> (CreateNanoGrid.h:184-190, 1099-1186 value counts,
+// 1228-1267 leaves, 1531-1585 internal nodes, 1618-1656 root, 1796-1880
+// value channel): nodes hold offsets into a value array -- 0 the background,
+// then (with tiles) four statistics slots of the root and of every internal
+// node (the background value: an OpenVDB source has no statistics), then per
+// leaf its active values in index order followed (with stats) by four
+// background slots.  Leaves carry their first offset and the 9-bit prefix
+// sums of active voxels over their mask words.  `channels` copies of the value
+// array follow as blind data ("channel_<i>", ChannelArray, level-set
+// semantic).  Node statistics are bounding boxes only (updateGridStats with
+// StatsMode::BBox, as the converter does for index grids).
+std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& name, int channels, bool stats,
+                                 bool tiles, int checksum) {
+    if (d.leaf_count < 0 || d.lower_count < 0 || d.upper_count < 0 || d.root_tile_count < 0)
+        fail(GBLS_ERR_INVALID_ARGUMENT, "negative count in grid descriptor");
+    if (channels < 0) fail(GBLS_ERR_INVALID_ARGUMENT, "negative channel count");
+    // The converter fills channel i > 0 from (its own start - value count),
+    // which reads across the previous channel's alignment padding: only 0 or 1
+    // channels have well-defined contents.
+    if (channels > 1) fail(GBLS_ERR_UNSUPPORTED, "more than one value channel");
+    if (checksum != 0 && checksum != 1) fail(GBLS_ERR_UNSUPPORTED, "checksum mode must be 0 (disable) or 1 (partial)");
+    if (name.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
+    const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count, nt = d.root_tile_count;
+    const uint64_t nstat = stats ? 4 : 0;
+    // value offsets (countValues / countTileValues)
+    uint64_t count = 1;
+    std::vector<uint64_t> upper_off(static_cast<size_t>(nu)), lower_off(static_cast<size_t>(nl)),
+        leaf_off(static_cast<size_t>(nf));
+    if (tiles) {
+        count += nstat;  // root statistics (a level set has no active root tiles)
+        for (int64_t i = 0; i < nu; ++i) upper_off[size_t(i)] = count, count += nstat;
+        for (int64_t i = 0; i < nl; ++i) lower_off[size_t(i)] = count, count += nstat;
+    }
+    std::vector<int> active(static_cast<size_t>(nf));
+    for (int64_t f = 0; f < nf; ++f) {
+        int a = 0;
+        for (int w = 0; w < 8; ++w) a += __builtin_popcountll(d.leaf_masks[8 * f + w]);
+        active[size_t(f)] = a;
+        leaf_off[size_t(f)] = count;
+        count += uint64_t(a) + nstat;
+    }
+    const size_t table = size_t(nu + nt);
+    const size_t tree_at = kGridBytes, root_at = tree_at + kTreeBytes;
+    const size_t upper_at = root_at + 96 + kTileBytes * table;
+    const size_t lower_at = upper_at + kUpperBytes * size_t(nu);
+    const size_t leaf_at = lower_at + kLowerBytes * size_t(nl);
+    const size_t meta_at = leaf_at + 96 * size_t(nf);
+    const size_t blind_at = meta_at + 288 * size_t(channels);
+    const size_t channel_bytes = (count * 4 + 31) / 32 * 32;
+    const size_t total = blind_at + channel_bytes * size_t(channels);
+    std::vector<uint8_t> b(total, 0);
+
+    // leaves: origin, mask, offset, prefix sums; bounding boxes
+    std::vector<BBox> leaf_box(static_cast<size_t>(nf));
+    for (int64_t f = 0; f < nf; ++f) {
+        const size_t at = leaf_at + 96 * size_t(f);
+        const int32_t* o = d.leaf_origins + 3 * f;
+        const uint64_t* m = d.leaf_masks + 8 * f;
+        std::memcpy(b.data() + at, o, 12);
+        std::memcpy(b.data() + at + 16, m, 64);
+        put<uint64_t>(b, at + 80, leaf_off[size_t(f)]);
+        uint64_t sum = uint64_t(__builtin_popcountll(m[0])), prefix = sum;
+        for (int w = 1, sh = 9; w < 7; ++w, sh += 9) {
+            sum += uint64_t(__builtin_popcountll(m[w]));
+            prefix |= sum << sh;
+        }
+        put<uint64_t>(b, at + 88, prefix);
+        uint8_t flags = stats ? 16 : 0;
+        BBox& bx = leaf_box[size_t(f)];
+        for (int i = 0; i < 512; ++i) {
+            if (!bit(m, i)) continue;
+            const int32_t c[3] = {o[0] + (i >> 6), o[1] + ((i >> 3) & 7), o[2] + (i & 7)};
+            for (int k = 0; k < 3; ++k) {
+                bx.lo[k] = std::min(bx.lo[k], c[k]);
+                bx.hi[k] = std::max(bx.hi[k], c[k]);
+            }
+        }
+        if (!bx.empty()) {
+            std::memcpy(b.data() + at, bx.lo, 12);
+            for (int k = 0; k < 3; ++k) b[at + 12 + k] = uint8_t(bx.hi[k] - bx.lo[k]);
+            flags |= 2;
+        }
+        b[at + 15] = flags;
+    }
+    // internal nodes: child offsets (tile slots 0: no active tiles), stats offsets, boxes
+    auto internal = [&](int64_t cnt, size_t base, size_t bytes, size_t table_at, int log2, const int32_t* origins,
+                        const std::vector<uint64_t>& offs, int64_t child_count, const int32_t* child_origins,
+                        size_t child_base, size_t child_bytes, int child_shift, const std::vector<BBox>& child_box,
+                        std::vector<BBox>& out_box) {
+        const int nvals = 1 << (3 * log2);
+        out_box.assign(size_t(cnt), BBox());
+        int64_t c = 0;
+        for (int64_t i = 0; i < cnt; ++i) {
+            const size_t at = base + bytes * size_t(i);
+            const int32_t* o = origins + 3 * i;
+            const int32_t span = (1 << log2) << child_shift;
+            for (; c < child_count; ++c) {
+                const int32_t* co = child_origins + 3 * c;
+                if ((co[0] & ~(span - 1)) != o[0] || (co[1] & ~(span - 1)) != o[1] || (co[2] & ~(span - 1)) != o[2]) break;
+                const int n = ((((co[0] - o[0]) >> child_shift) << (2 * log2)) | (((co[1] - o[1]) >> child_shift) << log2) |
+                               ((co[2] - o[2]) >> child_shift));
+                b[at + 32 + size_t(nvals / 8) + size_t(n >> 3)] |= uint8_t(1u << (n & 7));
+                put<int64_t>(b, at + table_at + 8 * size_t(n), int64_t(child_base + child_bytes * size_t(c)) - int64_t(at));
+                out_box[size_t(i)].add(child_box[size_t(c)]);
+            }
+            if (tiles && stats)
+                for (int k = 0; k < 4; ++k) put<uint64_t>(b, at + 32 + size_t(nvals / 4) + 8 * size_t(k), offs[size_t(i)] + uint64_t(k));
+            put_bbox(b, at, out_box[size_t(i)]);
+            put<uint64_t>(b, at + 24, out_box[size_t(i)].empty() ? 1 : 2);
+        }
+        if (c != child_count) fail(GBLS_ERR_INVALID_ARGUMENT, "grid descriptor is not in tree order (orphan child node)");
+    };
+    std::vector<BBox> lower_box, upper_box;
+    internal(nl, lower_at, kLowerBytes, kLowerTableAt, 4, d.lower_origins, lower_off, nf, d.leaf_origins, leaf_at, 96, 3,
+             leaf_box, lower_box);
+    internal(nu, upper_at, kUpperBytes, kUpperTableAt, 5, d.upper_origins, upper_off, nl, d.lower_origins, lower_at,
+             kLowerBytes, 7, lower_box, upper_box);
+    // root
+    std::vector<std::pair<int64_t, bool>> entries;
+    for (int64_t i = 0; i < nu; ++i) entries.push_back({i, true});
+    for (int64_t i = 0; i < nt; ++i) entries.push_back({i, false});
+    auto origin_of = [&](const std::pair<int64_t, bool>& e) {
+        return e.second ? d.upper_origins + 3 * e.first : d.root_tile_origins + 3 * e.first;
+    };
+    std::stable_sort(entries.begin(), entries.end(), [&](const auto& a2, const auto& c2) {
+        const int32_t *p = origin_of(a2), *q = origin_of(c2);
+        return std::lexicographical_compare(p, p + 3, q, q + 3);
+    });
+    BBox root_box;
+    for (size_t t = 0; t < entries.size(); ++t) {
+        const size_t at = root_at + 96 + kTileBytes * t;
+        put<uint64_t>(b, at, root_key(origin_of(entries[t])));
+        if (entries[t].second) {
+            put<int64_t>(b, at + 8, int64_t(upper_at + kUpperBytes * size_t(entries[t].first)) - int64_t(root_at));
+            root_box.add(upper_box[size_t(entries[t].first)]);
+        }
+    }
+    put_bbox(b, root_at, root_box);
+    put<uint32_t>(b, root_at + 24, uint32_t(table));
+    if (tiles && stats && table > 0)  // the statistics pass resets an empty root's slots to 0
+        for (int k = 0; k < 4; ++k) put<uint64_t>(b, root_at + 40 + 8 * size_t(k), uint64_t(k + 1));
+    // tree
+    int64_t voxels = 0;
+    for (int a : active) voxels += a;
+    put<int64_t>(b, tree_at, nf ? int64_t(leaf_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 8, nl ? int64_t(lower_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 16, nu ? int64_t(upper_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 24, int64_t(root_at - tree_at));
+    put<uint32_t>(b, tree_at + 32, uint32_t(nf));
+    put<uint32_t>(b, tree_at + 36, uint32_t(nl));
+    put<uint32_t>(b, tree_at + 40, uint32_t(nu));
+    put<uint64_t>(b, tree_at + 56, uint64_t(voxels));
+    // value channels
+    for (int ch = 0; ch < channels; ++ch) {
+        const size_t mat = meta_at + 288 * size_t(ch), dat = blind_at + channel_bytes * size_t(ch);
+        put<int64_t>(b, mat, int64_t(dat) - int64_t(mat));
+        put<uint64_t>(b, mat + 8, count);
+        put<uint32_t>(b, mat + 16, 4);
+        put<uint32_t>(b, mat + 20, 10);  // GridBlindDataSemantic::LevelSet
+        put<uint32_t>(b, mat + 24, 4);   // GridBlindDataClass::ChannelArray
+        put<uint32_t>(b, mat + 28, 1);   // GridType::Float
+        const std::string cn = "channel_" + std::to_string(ch);
+        std::memcpy(b.data() + mat + 32, cn.data(), cn.size());
+        float* v = reinterpret_cast<float*>(b.data() + dat);
+        const float bg = d.background;
+        v[0] = bg;
+        if (tiles && stats) {
+            for (int k = 0; k < 4; ++k) v[1 + k] = bg;
+            for (int64_t i = 0; i < nu; ++i) for (int k = 0; k < 4; ++k) v[upper_off[size_t(i)] + uint64_t(k)] = bg;
+            for (int64_t i = 0; i < nl; ++i) for (int k = 0; k < 4; ++k) v[lower_off[size_t(i)] + uint64_t(k)] = bg;
+        }
+        for (int64_t f = 0; f < nf; ++f) {
+            uint64_t o = leaf_off[size_t(f)];
+            const uint64_t* m = d.leaf_masks + 8 * f;
+            for (int i = 0; i < 512; ++i)
+                if (bit(m, i)) v[o++] = d.leaf_values[512 * f + i];
+            for (uint64_t k = 0; k < nstat; ++k) v[o++] = bg;
+        }
+    }
+    // grid
+    const MapD map = make_map(d);
+    put<uint64_t>(b, 0, kMagicGrid);
+    put<uint64_t>(b, 8, ~uint64_t(0));
+    put<uint32_t>(b, 16, kVersion);
+    put<uint32_t>(b, 20, kIsBreadthFirst | (root_box.empty() ? 0u : kHasBBox));
+    put<uint32_t>(b, 28, 1);
+    put<uint64_t>(b, 32, uint64_t(total));
+    std::memcpy(b.data() + 40, name.data(), name.size());
+    put_map(b, 296, map);
+    double wlo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, whi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    if (!root_box.empty()) {
+        for (int corner = 0; corner < 8; ++corner) {
+            const double p[3] = {double((corner & 4) ? root_box.hi[0] + 1 : root_box.lo[0]),
+                                 double((corner & 2) ? root_box.hi[1] + 1 : root_box.lo[1]),
+                                 double((corner & 1) ? root_box.hi[2] + 1 : root_box.lo[2])};
+            double w[3];
+            map.apply(p, w);
+            for (int k = 0; k < 3; ++k) {
+                wlo[k] = std::min(wlo[k], w[k]);
+                whi[k] = std::max(whi[k], w[k]);
+            }
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        put<double>(b, 560 + 8 * k, wlo[k]);
+        put<double>(b, 584 + 8 * k, whi[k]);
+    }
+    const double one[3] = {1.0, 1.0, 1.0}, zero[3] = {0.0, 0.0, 0.0};
+    double a1[3], a0[3];
+    map.apply(one, a1);
+    map.apply(zero, a0);
+    for (int k = 0; k < 3; ++k) put<double>(b, 608 + 8 * k, a1[k] - a0[k]);
+    put<uint32_t>(b, 632, 8);   // GridClass::IndexGrid
+    put<uint32_t>(b, 636, 20);  // GridType::OnIndex
+    put<int64_t>(b, 640, channels ? int64_t(meta_at) : int64_t(total));
+    put<uint32_t>(b, 648, uint32_t(channels));
+    put<uint64_t>(b, 656, count);
+    if (checksum == 1) {
+        const uint32_t head = crc32(b.data() + 16, kGridBytes + kTreeBytes - 16);
+        put<uint64_t>(b, 8, (~uint64_t(0) << 32) | head);
+    }
+    return b;
+}
+
 
 }  // namespace
 
@@ -436,6 +659,28 @@ int gbls_nanovdb_export(const gbls_grid_desc* desc, const char* name, int32_t st
     try {
         if (!desc || !size) fail(GBLS_ERR_INVALID_ARGUMENT, "null argument");
         std::vector<uint8_t> b = build(*desc, name ? name : "", stats_mode, checksum_mode);
+        *size = int64_t(b.size());
+        if (out) {
+            if (out_capacity < *size) fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer too small");
+            std::memcpy(out, b.data(), b.size());
+        }
+        return GBLS_OK;
+    } catch (const ExportError& e) {
+        gbls_host::set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        gbls_host::set_error("out of host memory");
+        return GBLS_ERR_OUT_OF_MEMORY;
+    }
+}
+
+int gbls_nanovdb_export_index(const gbls_grid_desc* desc, const char* name, int32_t channels, int32_t include_stats,
+                              int32_t include_tiles, int32_t checksum_mode, uint8_t* out, int64_t out_capacity,
+                              int64_t* size) {
+    try {
+        if (!desc || !size) fail(GBLS_ERR_INVALID_ARGUMENT, "null argument");
+        std::vector<uint8_t> b = build_index(*desc, name ? name : "", channels, include_stats != 0, include_tiles != 0,
+                                             checksum_mode);
         *size = int64_t(b.size());
         if (out) {
             if (out_capacity < *size) fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer too small");

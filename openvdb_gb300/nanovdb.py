@@ -30,6 +30,22 @@ def to_nanovdb(grid, name="", stats="all", checksum="partial"):
     return buf
 
 
+def to_nanovdb_index(grid, name="", channel=True, include_stats=True, include_tiles=True,
+                     checksum="partial"):
+    """NanoGrid<ValueOnIndex> buffer of `grid` (createNanoGrid<FloatGrid,
+    ValueOnIndex>(grid, channels, includeStats, includeTiles)); with
+    `channel` the values follow as the blind-data array "channel_0"."""
+    L = lib()
+    d = grid.desc()
+    n = C.c_int64()
+    args = (name.encode(), int(bool(channel)), int(bool(include_stats)), int(bool(include_tiles)),
+            CHECKSUM[checksum])
+    check(L.gbls_nanovdb_export_index(C.byref(d), *args, None, 0, C.byref(n)), host=True)
+    buf = np.empty(n.value, np.uint8)
+    check(L.gbls_nanovdb_export_index(C.byref(d), *args, buf.ctypes.data, n.value, C.byref(n)), host=True)
+    return buf
+
+
 def to_device(grid, name="", stats="all", checksum="partial", device="cuda"):
     """The same buffer as a torch uint8 tensor on `device`."""
     import torch

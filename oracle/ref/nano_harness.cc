@@ -50,4 +50,29 @@ int vdbref_nano_float(void* g, const char* name, int stats, int checksum, uint8_
     }
 }
 
+// createNanoGrid<FloatGrid, ValueOnIndex>(grid, channels, includeStats, includeTiles).
+int vdbref_nano_onindex(void* g, const char* name, int channels, int stats, int tiles, int checksum, uint8_t* out,
+                        int64_t out_cap, int64_t* size) {
+    try {
+        openvdb::FloatGrid::Ptr grid = vdbref_detail::grid_of(g);
+        grid->setName(name);
+        auto handle = nanovdb::tools::createNanoGrid<openvdb::FloatGrid, nanovdb::ValueOnIndex>(
+            *grid, uint32_t(channels), stats != 0, tiles != 0);
+        if (checksum == 0) nanovdb::tools::updateChecksum(handle.data() ? reinterpret_cast<nanovdb::GridData*>(handle.data()) : nullptr,
+                                                          nanovdb::CheckMode::Disable);
+        *size = int64_t(handle.bufferSize());
+        if (out) {
+            if (out_cap < *size) {
+                gNanoError = "buffer too small";
+                return GBLS_ERR_INVALID_ARGUMENT;
+            }
+            std::memcpy(out, handle.data(), size_t(*size));
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        gNanoError = e.what();
+        return GBLS_ERR_RUNTIME;
+    }
+}
+
 }  // extern "C"

@@ -54,6 +54,8 @@ def lib():
         L.vdbref_nano_float.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_int64,
                                         C.POINTER(C.c_int64)]
         L.vdbref_nano_last_error.restype = C.c_char_p
+        L.vdbref_nano_onindex.argtypes = [C.c_void_p, C.c_char_p] + [C.c_int] * 4 + [C.c_void_p, C.c_int64,
+                                                                              C.POINTER(C.c_int64)]
         _lib = L
     return _lib
 
@@ -129,6 +131,18 @@ class RefGrid:
             raise RuntimeError(L.vdbref_nano_last_error().decode())
         buf = np.zeros(n.value, np.uint8)
         if L.vdbref_nano_float(self.h, name.encode(), stats, checksum, buf.ctypes.data, n.value, C.byref(n)):
+            raise RuntimeError(L.vdbref_nano_last_error().decode())
+        return buf
+
+    def nanovdb_index(self, name, channels=1, stats=True, tiles=True, checksum=1):
+        """createNanoGrid<FloatGrid, ValueOnIndex>(grid, channels, stats, tiles) of the reference."""
+        n = C.c_int64()
+        L = lib()
+        args = (self.h, name.encode(), channels, int(stats), int(tiles), checksum)
+        if L.vdbref_nano_onindex(*args, None, 0, C.byref(n)):
+            raise RuntimeError(L.vdbref_nano_last_error().decode())
+        buf = np.zeros(n.value, np.uint8)
+        if L.vdbref_nano_onindex(*args, buf.ctypes.data, n.value, C.byref(n)):
             raise RuntimeError(L.vdbref_nano_last_error().decode())
         return buf
 

@@ -95,3 +95,40 @@ def test_rejects_long_names_and_full_checksum():
             to_nanovdb(g, "s", checksum="full")
     finally:
         del nanovdb.CHECKSUM["full"]
+
+
+@pytest.mark.parametrize("tiles", [False, True])
+@pytest.mark.parametrize("stats", [False, True])
+@pytest.mark.parametrize("channel", [False, True])
+@pytest.mark.parametrize("name", NAMES)
+def test_index_grid_bytes_equal_reference(name, channel, stats, tiles):
+    """createNanoGrid<FloatGrid, ValueOnIndex>; the alignment padding after
+    the value channel is uninitialised in the reference and is masked."""
+    from openvdb_gb300.nanovdb import to_nanovdb_index
+    refpy = _refpy()
+    g = grids()[name]
+    mine = to_nanovdb_index(g, name, channel, stats, tiles)
+    ref = refpy.RefGrid.from_host(g).nanovdb_index(name, int(channel), stats, tiles)
+    assert mine.size == ref.size
+    count = int(np.frombuffer(mine.tobytes(), np.uint64, 1, 656)[0])
+    pad = ((count * 4 + 31) // 32 * 32 - count * 4) if channel else 0
+    assert np.array_equal(mine[: mine.size - pad], ref[: ref.size - pad])
+
+
+def test_index_grid_values_and_offsets():
+    """Every active value is found at its leaf's offset plus its rank."""
+    from openvdb_gb300.nanovdb import to_nanovdb_index
+    g = grids()["union"]
+    b = to_nanovdb_index(g, "u").tobytes()
+    count = struct.unpack_from("<Q", b, 656)[0]
+    meta_at = struct.unpack_from("<q", b, 640)[0]
+    data_at = meta_at + struct.unpack_from("<q", b, meta_at)[0]
+    values = np.frombuffer(b, np.float32, count, data_at)
+    leaf_at = 672 + struct.unpack_from("<q", b, 672)[0]
+    for f in range(len(g.leaf_origins)):
+        off, prefix = struct.unpack_from("<QQ", b, leaf_at + 96 * f + 80)
+        bits = np.unpackbits(g.leaf_masks[f].view(np.uint8), bitorder="little").astype(bool)
+        assert np.array_equal(values[off: off + bits.sum()], g.leaf_values[f][bits])
+        sums = np.cumsum([bin(int(w)).count("1") for w in g.leaf_masks[f]])[:7]
+        assert all(((prefix >> (9 * i)) & 511) == sums[i] for i in range(7))
+    assert values[0] == np.float32(g.background)
