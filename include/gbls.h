@@ -402,10 +402,11 @@ int gbls_vdb_read(const char* path, const char* name, int32_t index, gbls_host_g
  * buffer (NanoVDB 32.9, breadth-first) of a level set in the exchange
  * layout, byte for byte what the reference writes.  stats_mode: 0 Disable,
  * 1 BBox, 2 MinMax, 3 All (node statistics combined in tree order);
- * checksum_mode: 0 Disable, 1 Partial (CRC-32 of the grid and tree headers).
+ * checksum_mode: 0 Disable, 1 Partial (CRC-32 of the grid and tree headers),
+ * 2 Full (also the blocked CRC-32 of the nodes).
  * With out == NULL only *size is set; otherwise out_capacity must be at least
  * the size.  Errors through gbls_host_last_error: GBLS_ERR_UNSUPPORTED for
- * names of 256 characters or more and checksum mode Full.                  */
+ * names of 256 characters or more.                                          */
 int gbls_nanovdb_export(const gbls_grid_desc* desc, const char* name, int32_t stats_mode,
                         int32_t checksum_mode, uint8_t* out, int64_t out_capacity, int64_t* size);
 /* NanoVDB index grid: createNanoGrid<FloatGrid, ValueOnIndex>(grid, channels,

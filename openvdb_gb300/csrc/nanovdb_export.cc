@@ -15,8 +15,9 @@
 // nanovdb::tools::updateGridStats (tools/GridStats.h:244-442, 577-760):
 // per-node active bounding boxes, extrema, and the running mean / variance
 // combined child by child in tree order (the serial form of the reduction),
-// in double precision.  The checksum is the CRC-32 of the grid and tree
-// headers (tools/GridChecksum.h:206-230, 300-323; CheckMode::Partial).
+// in double precision.  Checksums: the CRC-32 of the grid and tree headers
+// (CheckMode::Partial) and the blocked CRC of the nodes (CheckMode::Full),
+// tools/GridChecksum.h:172-230, 280-323.
 #include <algorithm>
 #include <cfloat>
 #include <climits>
@@ -218,6 +219,30 @@ uint32_t crc32(const uint8_t* p, size_t n) {
     return ~crc;
 }
 
+// CRC-32 of each 4 KiB block (the last one takes the remainder), then of the
+// block checksums (util::blockedCrc32, tools/GridChecksum.h:172-185).
+uint32_t blocked_crc32(const uint8_t* p, size_t n) {
+    if (n == 0) return ~0u;
+    const size_t blocks = n >> 12;
+    std::vector<uint32_t> sums(blocks);
+    for (size_t i = 0; i < blocks; ++i) {
+        size_t len = size_t(1) << 12;
+        if (i + 1 == blocks) len += n - (blocks << 12);
+        sums[i] = crc32(p + (i << 12), len);
+    }
+    return crc32(reinterpret_cast<const uint8_t*>(sums.data()), 4 * blocks);
+}
+
+// Head CRC (grid and tree headers) and, for CheckMode::Full, the blocked
+// CRC of everything after them (tools/GridChecksum.h:206-230, 280-300).
+void put_checksum(std::vector<uint8_t>& b, int mode) {
+    if (mode == 0) return;
+    const uint32_t head = crc32(b.data() + 16, kGridBytes + kTreeBytes - 16);
+    const uint32_t tail = mode == 2 ? blocked_crc32(b.data() + kGridBytes + kTreeBytes, b.size() - kGridBytes - kTreeBytes)
+                                    : ~0u;
+    put<uint64_t>(b, 8, (uint64_t(tail) << 32) | head);
+}
+
 inline uint64_t root_key(const int32_t* o) {
     return uint64_t(uint32_t(o[2]) >> 12) | (uint64_t(uint32_t(o[1]) >> 12) << 21) |
            (uint64_t(uint32_t(o[0]) >> 12) << 42);
@@ -227,8 +252,7 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
     if (d.leaf_count < 0 || d.lower_count < 0 || d.upper_count < 0 || d.root_tile_count < 0)
         fail(GBLS_ERR_INVALID_ARGUMENT, "negative count in grid descriptor");
     if (mode < kStatsDisable || mode > kStatsAll) fail(GBLS_ERR_INVALID_ARGUMENT, "statistics mode must be 0-3");
-    if (checksum != 0 && checksum != 1)
-        fail(GBLS_ERR_UNSUPPORTED, "checksum mode must be 0 (disable) or 1 (partial)");
+    if (checksum < 0 || checksum > 2) fail(GBLS_ERR_INVALID_ARGUMENT, "checksum mode must be 0-2");
     if (name.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
     const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count, nt = d.root_tile_count;
     const size_t table = size_t(nu + nt);
@@ -418,10 +442,7 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
     put<uint32_t>(b, 632, 1);  // GridClass::LevelSet
     put<uint32_t>(b, 636, 1);  // GridType::Float
     put<int64_t>(b, 640, int64_t(total));  // no blind data
-    if (checksum == 1) {
-        const uint32_t head = crc32(b.data() + 16, kGridBytes + kTreeBytes - 16);
-        put<uint64_t>(b, 8, (~uint64_t(0) << 32) | head);
-    }
+    put_checksum(b, checksum);
     return b;
 }
 
@@ -445,7 +466,7 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
     // which reads across the previous channel's alignment padding: only 0 or 1
     // channels have well-defined contents.
     if (channels > 1) fail(GBLS_ERR_UNSUPPORTED, "more than one value channel");
-    if (checksum != 0 && checksum != 1) fail(GBLS_ERR_UNSUPPORTED, "checksum mode must be 0 (disable) or 1 (partial)");
+    if (checksum < 0 || checksum > 2) fail(GBLS_ERR_INVALID_ARGUMENT, "checksum mode must be 0-2");
     if (name.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
     const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count, nt = d.root_tile_count;
     const uint64_t nstat = stats ? 4 : 0;
@@ -642,10 +663,7 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
     put<int64_t>(b, 640, channels ? int64_t(meta_at) : int64_t(total));
     put<uint32_t>(b, 648, uint32_t(channels));
     put<uint64_t>(b, 656, count);
-    if (checksum == 1) {
-        const uint32_t head = crc32(b.data() + 16, kGridBytes + kTreeBytes - 16);
-        put<uint64_t>(b, 8, (~uint64_t(0) << 32) | head);
-    }
+    put_checksum(b, checksum);
     return b;
 }
 

@@ -14,7 +14,7 @@ import numpy as np
 from ._lib import check, lib
 
 STATS = {"disable": 0, "bbox": 1, "minmax": 2, "all": 3}
-CHECKSUM = {"disable": 0, "partial": 1}
+CHECKSUM = {"disable": 0, "partial": 1, "full": 2}
 
 
 def to_nanovdb(grid, name="", stats="all", checksum="partial"):

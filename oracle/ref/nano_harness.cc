@@ -58,8 +58,9 @@ int vdbref_nano_onindex(void* g, const char* name, int channels, int stats, int 
         grid->setName(name);
         auto handle = nanovdb::tools::createNanoGrid<openvdb::FloatGrid, nanovdb::ValueOnIndex>(
             *grid, uint32_t(channels), stats != 0, tiles != 0);
-        if (checksum == 0) nanovdb::tools::updateChecksum(handle.data() ? reinterpret_cast<nanovdb::GridData*>(handle.data()) : nullptr,
-                                                          nanovdb::CheckMode::Disable);
+        if (checksum != 1)
+            nanovdb::tools::updateChecksum(reinterpret_cast<nanovdb::GridData*>(handle.data()),
+                                           checksum == 0 ? nanovdb::CheckMode::Disable : nanovdb::CheckMode::Full);
         *size = int64_t(handle.bufferSize());
         if (out) {
             if (out_cap < *size) {

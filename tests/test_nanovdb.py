@@ -51,7 +51,7 @@ def grids():
 NAMES = ["sphere", "union", "translated", "planted", "empty", "root_tiles", "dx_0.001_translated", "dx_0.003"]
 
 
-@pytest.mark.parametrize("checksum", ["disable", "partial"])
+@pytest.mark.parametrize("checksum", ["disable", "partial", "full"])
 @pytest.mark.parametrize("stats", ["disable", "bbox", "minmax", "all"])
 @pytest.mark.parametrize("name", NAMES)
 def test_bytes_equal_reference(name, stats, checksum):
@@ -59,7 +59,7 @@ def test_bytes_equal_reference(name, stats, checksum):
     g = grids()[name]
     mine = to_nanovdb(g, name, stats, checksum)
     ref = refpy.RefGrid.from_host(g).nanovdb(name, ["disable", "bbox", "minmax", "all"].index(stats),
-                                             ["disable", "partial"].index(checksum))
+                                             ["disable", "partial", "full"].index(checksum))
     assert mine.size == ref.size
     assert np.array_equal(mine, ref)
 
@@ -83,18 +83,22 @@ def test_header_fields_and_checksum():
     assert np.array_equal(first, g.leaf_values[0])
 
 
-def test_rejects_long_names_and_full_checksum():
-    g = grids()["sphere"]
+def test_rejects_long_names():
     from openvdb_gb300._lib import GblsError
     with pytest.raises(GblsError):
-        to_nanovdb(g, "x" * 300)
-    from openvdb_gb300 import nanovdb
-    nanovdb.CHECKSUM["full"] = 2
-    try:
-        with pytest.raises(GblsError):
-            to_nanovdb(g, "s", checksum="full")
-    finally:
-        del nanovdb.CHECKSUM["full"]
+        to_nanovdb(grids()["sphere"], "x" * 300)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_index_grid_full_checksum(name):
+    """CheckMode::Full on an index grid without a value channel (with one, the
+    reference's checksum covers its uninitialised padding)."""
+    from openvdb_gb300.nanovdb import to_nanovdb_index
+    refpy = _refpy()
+    g = grids()[name]
+    mine = to_nanovdb_index(g, name, False, True, True, checksum="full")
+    ref = refpy.RefGrid.from_host(g).nanovdb_index(name, 0, True, True, checksum=2)
+    assert np.array_equal(mine, ref)
 
 
 @pytest.mark.parametrize("tiles", [False, True])
