@@ -418,6 +418,12 @@ int gbls_nanovdb_export(const gbls_grid_desc* desc, const char* name, int32_t st
  * padding after the channel, which the reference leaves uninitialised.
  * channels > 1 is GBLS_ERR_UNSUPPORTED: the reference copies channel i from
  * (its start - value count), across that padding.                          */
+/* NanoGrid<float> buffer -> host grid in the exchange layout (the
+ * direction of nanovdb::tools::nanoToOpenVDB, nanovdb/tools/NanoToOpenVDB.h),
+ * for gbls_host_grid_view / gbls_create.  GBLS_ERR_UNSUPPORTED for other value
+ * types, active tiles and rotated maps; GBLS_ERR_RUNTIME for a non-NanoVDB or
+ * truncated buffer.                                                          */
+int gbls_nanovdb_import(const uint8_t* buffer, int64_t size, gbls_host_grid** out);
 int gbls_nanovdb_export_index(const gbls_grid_desc* desc, const char* name, int32_t channels,
                               int32_t include_stats, int32_t include_tiles, int32_t checksum_mode,
                               uint8_t* out, int64_t out_capacity, int64_t* size);

@@ -86,6 +86,7 @@ def lib():
         "gbls_vdb_read": ([C.c_char_p, C.c_char_p, C.c_int32, P(vp)], C.c_int),
         "gbls_nanovdb_export": ([P(_abi.GridDesc), C.c_char_p, C.c_int32, C.c_int32, vp, C.c_int64,
                                  P(C.c_int64)], C.c_int),
+        "gbls_nanovdb_import": ([vp, C.c_int64, P(vp)], C.c_int),
         "gbls_nanovdb_export_index": ([P(_abi.GridDesc), C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                        vp, C.c_int64, P(C.c_int64)], C.c_int),
     }

@@ -668,6 +668,122 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
 }
 
 
+// NanoGrid<float> -> exchange layout (the direction of
+// nanovdb::tools::nanoToOpenVDB, nanovdb/tools/NanoToOpenVDB.h): the tree is
+// walked through its links -- root table in Coord order, then child masks in
+// slot order -- so the result is in tree order whatever the buffer's node
+// layout; node origins come from the root keys and the slot indices.
+template <class T> inline T get(const uint8_t* b, size_t at) {
+    T v;
+    std::memcpy(&v, b + at, sizeof(T));
+    return v;
+}
+
+gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
+    auto need = [&](size_t at, size_t n) {
+        if (at > size_t(size) || n > size_t(size) - at) fail(GBLS_ERR_RUNTIME, "truncated NanoVDB buffer");
+    };
+    need(0, kGridBytes + kTreeBytes);
+    const uint64_t magic = get<uint64_t>(b, 0);
+    if (magic != kMagicGrid && magic != 0x304244566f6e614eULL) fail(GBLS_ERR_RUNTIME, "not a NanoVDB grid");
+    if ((get<uint32_t>(b, 16) >> 21) != 32) fail(GBLS_ERR_UNSUPPORTED, "NanoVDB major version other than 32");
+    if (get<uint32_t>(b, 636) != 1) fail(GBLS_ERR_UNSUPPORTED, "not a NanoGrid<float>");
+    double mat[9], vec[3];
+    for (int k = 0; k < 9; ++k) mat[k] = get<double>(b, 296 + 88 + 8 * k);
+    for (int k = 0; k < 3; ++k) vec[k] = get<double>(b, 296 + 232 + 8 * k);
+    if (mat[1] != 0 || mat[2] != 0 || mat[3] != 0 || mat[5] != 0 || mat[6] != 0 || mat[7] != 0)
+        fail(GBLS_ERR_UNSUPPORTED, "rotated or sheared NanoVDB map");
+    if (!(mat[0] == mat[4] && mat[4] == mat[8]) || !(mat[0] > 0))
+        fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
+    auto* g = new gbls_host_grid;
+    try {
+        g->voxel_size = mat[0];
+        for (int k = 0; k < 3; ++k) g->translation[k] = vec[k];
+        g->map_type = (vec[0] == 0 && vec[1] == 0 && vec[2] == 0) ? GBLS_MAP_UNIFORM_SCALE
+                                                                 : GBLS_MAP_UNIFORM_SCALE_TRANSLATE;
+        const size_t root_at = kGridBytes + size_t(get<int64_t>(b, kGridBytes + 24));
+        need(root_at, kRootBytes);
+        const uint32_t table = get<uint32_t>(b, root_at + 24);
+        need(root_at + kRootBytes, size_t(table) * kTileBytes);
+        g->background = get<float>(b, root_at + 28);
+        struct Entry {
+            int32_t o[3];
+            int64_t child;
+            float value;
+        };
+        std::vector<Entry> entries(table);
+        for (uint32_t t = 0; t < table; ++t) {
+            const size_t at = root_at + kRootBytes + kTileBytes * t;
+            const uint64_t key = get<uint64_t>(b, at);
+            Entry& e = entries[t];
+            e.o[0] = int32_t(uint32_t(((key >> 42) & 0x1FFFFF) << 12));
+            e.o[1] = int32_t(uint32_t(((key >> 21) & 0x1FFFFF) << 12));
+            e.o[2] = int32_t(uint32_t((key & 0x1FFFFF) << 12));
+            e.child = get<int64_t>(b, at + 8);
+            if (!e.child && get<uint32_t>(b, at + 16)) fail(GBLS_ERR_UNSUPPORTED, "active root tile in a level set");
+            e.value = get<float>(b, at + 20);
+        }
+        std::sort(entries.begin(), entries.end(), [](const Entry& x, const Entry& y) {
+            return std::lexicographical_compare(x.o, x.o + 3, y.o, y.o + 3);
+        });
+        // one internal node: its tile values, and its children as (address, origin) in slot order
+        struct Child {
+            size_t at;
+            int32_t o[3];
+        };
+        auto node = [&](size_t at, int log2, size_t bytes, size_t table_at, const int32_t* origin, int child_shift,
+                        std::vector<float>& tiles, std::vector<Child>& children) {
+            need(at, bytes);
+            const int nvals = 1 << (3 * log2), dim = 1 << log2;
+            const uint8_t* vmask = b + at + 32;
+            const uint8_t* cmask = vmask + nvals / 8;
+            const size_t base = tiles.size();
+            tiles.resize(base + size_t(nvals), 0.0f);
+            for (int n = 0; n < nvals; ++n) {
+                if ((vmask[n >> 3] >> (n & 7)) & 1) fail(GBLS_ERR_UNSUPPORTED, "active tile in a level set");
+                if ((cmask[n >> 3] >> (n & 7)) & 1) {
+                    Child c;
+                    c.at = size_t(int64_t(at) + get<int64_t>(b, at + table_at + 8 * size_t(n)));
+                    c.o[0] = origin[0] + (((n >> (2 * log2)) & (dim - 1)) << child_shift);
+                    c.o[1] = origin[1] + (((n >> log2) & (dim - 1)) << child_shift);
+                    c.o[2] = origin[2] + ((n & (dim - 1)) << child_shift);
+                    children.push_back(c);
+                } else {
+                    tiles[base + size_t(n)] = get<float>(b, at + table_at + 8 * size_t(n));
+                }
+            }
+        };
+        for (const Entry& e : entries) {
+            if (!e.child) {
+                g->root_tile_origins.insert(g->root_tile_origins.end(), e.o, e.o + 3);
+                g->root_tile_values.push_back(e.value);
+                continue;
+            }
+            g->upper_origins.insert(g->upper_origins.end(), e.o, e.o + 3);
+            std::vector<Child> lowers;
+            node(size_t(int64_t(root_at) + e.child), 5, kUpperBytes, kUpperTableAt, e.o, 7, g->upper_tiles, lowers);
+            for (const Child& lo : lowers) {
+                g->lower_origins.insert(g->lower_origins.end(), lo.o, lo.o + 3);
+                std::vector<Child> leaves;
+                node(lo.at, 4, kLowerBytes, kLowerTableAt, lo.o, 3, g->lower_tiles, leaves);
+                for (const Child& lf : leaves) {
+                    need(lf.at, kLeafBytes);
+                    const size_t f = g->leaf_origins.size() / 3;
+                    g->leaf_origins.insert(g->leaf_origins.end(), lf.o, lf.o + 3);
+                    g->leaf_masks.resize(8 * (f + 1));
+                    std::memcpy(g->leaf_masks.data() + 8 * f, b + lf.at + 16, 64);
+                    g->leaf_values.resize(512 * (f + 1));
+                    std::memcpy(g->leaf_values.data() + 512 * f, b + lf.at + 96, 2048);
+                }
+            }
+        }
+        return g;
+    } catch (...) {
+        delete g;
+        throw;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -704,6 +820,20 @@ int gbls_nanovdb_export_index(const gbls_grid_desc* desc, const char* name, int3
             if (out_capacity < *size) fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer too small");
             std::memcpy(out, b.data(), b.size());
         }
+        return GBLS_OK;
+    } catch (const ExportError& e) {
+        gbls_host::set_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        gbls_host::set_error("out of host memory");
+        return GBLS_ERR_OUT_OF_MEMORY;
+    }
+}
+
+int gbls_nanovdb_import(const uint8_t* buffer, int64_t size, gbls_host_grid** out) {
+    try {
+        if (!buffer || !out || size < 0) fail(GBLS_ERR_INVALID_ARGUMENT, "null argument");
+        *out = import_float(buffer, size);
         return GBLS_OK;
     } catch (const ExportError& e) {
         gbls_host::set_error(e.msg);

@@ -46,6 +46,16 @@ def to_nanovdb_index(grid, name="", channel=True, include_stats=True, include_ti
     return buf
 
 
+def from_nanovdb(buffer):
+    """HostGrid of a NanoGrid<float> buffer (bytes or a uint8 array)."""
+    from .fixtures import _from_native
+    a = np.ascontiguousarray(np.frombuffer(bytes(buffer), np.uint8) if isinstance(buffer, (bytes, bytearray))
+                             else buffer, dtype=np.uint8)
+    h = C.c_void_p()
+    check(lib().gbls_nanovdb_import(a.ctypes.data, a.size, C.byref(h)), host=True)
+    return _from_native(h)
+
+
 def to_device(grid, name="", stats="all", checksum="partial", device="cuda"):
     """The same buffer as a torch uint8 tensor on `device`."""
     import torch

@@ -15,7 +15,7 @@ import zlib
 import numpy as np
 import pytest
 
-from openvdb_gb300 import HostGrid, fixtures
+from openvdb_gb300 import HostGrid, digest, fixtures
 from openvdb_gb300.nanovdb import to_nanovdb
 
 import test_vdbfile as tv
@@ -31,8 +31,8 @@ def _refpy():
 def _grids():
     g = dict(tv.grids())
     g["empty"] = HostGrid(voxel_size=0.1, background=0.3)
-    g["root_tiles"] = tv._clone(g["union"], root_tile_origins=np.array([[8192, 0, 0], [-8192, 4096, 0]], np.int32),
-                                root_tile_values=np.array([-3.0, 3.0], np.float32))
+    g["root_tiles"] = tv._clone(g["union"], root_tile_origins=np.array([[-8192, 4096, 0], [8192, 0, 0]], np.int32),
+                                root_tile_values=np.array([3.0, -3.0], np.float32))  # tree (Coord) order
     g["dx_0.001_translated"] = tv._clone(g["sphere"], voxel_size=0.001, translation=(0.25, -1.0, 3.5), map_type=1)
     g["dx_0.003"] = tv._clone(g["sphere"], voxel_size=0.003)
     return g
@@ -136,3 +136,29 @@ def test_index_grid_values_and_offsets():
         sums = np.cumsum([bin(int(w)).count("1") for w in g.leaf_masks[f]])[:7]
         assert all(((prefix >> (9 * i)) & 511) == sums[i] for i in range(7))
     assert values[0] == np.float32(g.background)
+
+
+@pytest.mark.parametrize("stats", ["disable", "all"])
+@pytest.mark.parametrize("name", NAMES)
+def test_import_round_trip(name, stats):
+    """NanoGrid<float> -> exchange layout returns the grid bit for bit, also
+    from the reference converter's buffer."""
+    from openvdb_gb300.nanovdb import from_nanovdb
+    g = grids()[name]
+    back = from_nanovdb(to_nanovdb(g, name, stats))
+    assert digest(back) == digest(g)
+    assert np.allclose(back.translation, g.translation) and back.voxel_size == g.voxel_size
+    refpy = pytest.importorskip("oracle.refpy")
+    if refpy.available():
+        ref = refpy.RefGrid.from_host(g).nanovdb(name, ["disable", "bbox", "minmax", "all"].index(stats), 1)
+        assert digest(from_nanovdb(ref)) == digest(g)
+
+
+def test_import_rejects_garbage():
+    from openvdb_gb300._lib import GblsError
+    from openvdb_gb300.nanovdb import from_nanovdb
+    with pytest.raises(GblsError):
+        from_nanovdb(b"\0" * 1000)
+    buf = to_nanovdb(grids()["sphere"], "s")
+    with pytest.raises(GblsError):
+        from_nanovdb(buf[: buf.size // 2])
