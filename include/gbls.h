@@ -226,7 +226,12 @@ int gbls_field_destroy(gbls_field* f);
  * substeps; each substep runs the temporal scheme's RK stages with the
  * biased spatial scheme, then the tracker pass.  cfl <= 0 selects the
  * reference constant {0.3,0.9,1.0}/sqrt(3) for RK1/2/3 (:459-461).
- * *substeps receives the CFL count the reference returns.                  */
+ * cfl > 0 imposes a CFL number the reference has no parameter for: the
+ * result is that of the reference's advect(tau, tau') called on greedy
+ * intervals tau' = tau + cfl*dx/max|v| (max|v| sampled at tau; the last
+ * interval ends at t1), each with the reference's own substep loop.
+ * *substeps receives the CFL count the reference returns (summed over the
+ * intervals).                                                               */
 int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial_scheme,
                 int temporal_scheme, float t0, float t1, float cfl, uint64_t* substeps);
 

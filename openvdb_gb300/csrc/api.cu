@@ -19,6 +19,7 @@
 
 #include "../../include/gbls.h"
 #include "adjoint.h"
+#include "cfl_clock.h"
 #include "gbls_internal.cuh"
 #include "filter_ops.cuh"
 #include "io.h"
@@ -2738,10 +2739,7 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
         h->inst_field.upload(fp.data(), fp.size(), h->stream);
         if (t0 - t1 == 0.0f) { h->sync(); return; }
         const bool forward = t0 < t1;
-        const float dx = float(h->voxel_size);
-        const float cfl_ref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) /
-                              std::sqrt(3.0f);
-        const float C = cfl > 0.0f ? cfl : cfl_ref;
+        std::vector<CflClock> clock(static_cast<size_t>(n), CflClock(t0, t1, cfl, temporal, float(h->voxel_size)));
         std::vector<float> t(static_cast<size_t>(n), t0), dt(static_cast<size_t>(n), 0.0f);
         std::vector<uint8_t> done(static_cast<size_t>(n), 0), run(static_cast<size_t>(n), 0);
         std::vector<unsigned long long> act(static_cast<size_t>(n), 0);
@@ -2801,11 +2799,7 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
                     std::memcpy(&maxv2, &mx[size_t(i)], 4);
                 }
                 float d = 0.0f;
-                if (maxv2 > 1e-5f || maxv2 < -1e-5f) {
-                    const float span = std::fabs(t1 - t[size_t(i)]);
-                    const float lim = C * dx / std::sqrt(maxv2);
-                    d = (lim < span) ? lim : span;
-                }
+                if (maxv2 > 1e-5f || maxv2 < -1e-5f) d = clock[size_t(i)].next(t[size_t(i)], maxv2);
                 if (d == 0.0f) {
                     run[size_t(i)] = 0;
                     done[size_t(i)] = 1;
@@ -2825,7 +2819,7 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
             h->nactive = -1;
             for (int i = 0; i < n; ++i) {
                 if (!run[size_t(i)]) continue;
-                t[size_t(i)] += forward ? dt[size_t(i)] : -dt[size_t(i)];
+                clock[size_t(i)].advance(t[size_t(i)], dt[size_t(i)]);
                 ++count[size_t(i)];
             }
             track(*h);
@@ -2973,10 +2967,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
         check_scheme(h->tr_spatial, h->tr_temporal);
         if (t0 - t1 == 0.0f) return;  // math::isZero(time0 - time1)
         const bool forward = t0 < t1;
-        const float dx = float(h->voxel_size);
-        const float cfl_ref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) /
-                              std::sqrt(3.0f);
-        const float C = cfl > 0.0f ? cfl : cfl_ref;
+        CflClock clock(t0, t1, cfl, temporal, float(h->voxel_size));
         // the CFL reduction of substep k+1 rides on the read-back that ends
         // the tracker pass of substep k; the first substep reuses the maximum
         // the previous call reduced for its end time when nothing else has
@@ -3008,9 +2999,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             have_next = false;
             end_intr(*h);
             if (!(maxv2 > 1e-5f) && !(maxv2 < -1e-5f)) break;  // isApproxZero(maxAbsV, Delta)
-            const float span = std::fabs(t1 - t0);
-            const float lim = C * dx / std::sqrt(maxv2);
-            const float dt = (lim < span) ? lim : span;  // math::Min
+            const float dt = clock.next(t0, maxv2);
             if (dt == 0.0f) break;
             if (h->nactive < 0) h->nactive = active_count(*h);
             h->stats.voxel_updates += uint64_t(h->nactive);
@@ -3032,7 +3021,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
                 CU(cudaEventRecord(h->ev_rk, h->stream));
                 h->overlap_dilation = true;
             }
-            t0 += forward ? dt : -dt;
+            clock.advance(t0, dt);
             ++count;
             const bool more = forward ? t0 < t1 : t0 > t1;
             bool queued = false;

@@ -1,0 +1,65 @@
+// Substep lengths of LevelSetAdvection::advect under an imposed CFL number.
+//
+// The reference fixes the CFL number of its substep loop by temporal scheme
+// (1/sqrt(3) * {0.3, 0.9, 1.0}, tools/LevelSetAdvect.h:459-463).  A caller
+// that wants a smaller CFL number c runs the reference's own advect(tau, tau')
+// over greedy intervals: at the start of an interval, with max|v|^2 sampled
+// at tau, tau' = tau + c*dx/|v|max (or t1 when that reaches it), and inside
+// the interval the reference's loop takes its own substeps
+// dt = min(|tau' - t0|, CFL_ref*dx/|v|max) (tools/LevelSetAdvect.h:464-466)
+// until t0 reaches tau'.  Normally that is one substep of length
+// tau' - tau; when tau + (tau' - tau) rounds short of tau' the reference
+// takes a second, short substep, and this clock reproduces it.  Without an
+// imposed CFL number (c == 0) the single interval is [t0, t1], which is the
+// reference's advect(t0, t1) itself.
+#pragma once
+
+#include <cmath>
+
+#include "../../include/gbls.h"
+
+namespace gbls {
+
+struct CflClock {
+    float t1 = 0.0f;
+    bool forward = true;
+    float cfl = 0.0f;   // imposed CFL number (0: none)
+    float cref = 0.0f;  // the reference's CFL number for the temporal scheme
+    float dx = 1.0f;
+    bool open = false;  // inside an interval
+    float end = 0.0f;   // the interval's end time
+
+    CflClock(float t0, float t1_, float cfl_, int temporal, float dx_)
+        : t1(t1_), forward(t0 < t1_), cfl(cfl_ > 0.0f ? cfl_ : 0.0f), dx(dx_) {
+        cref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) / std::sqrt(3.0f);
+    }
+
+    bool running(float t) const { return forward ? t < t1 : t > t1; }
+
+    // Length of the substep that starts at t with max |v|^2 = maxv2 (not
+    // approximately zero); 0 ends the loop (an interval that rounds to zero
+    // length, where the reference's advect(tau, tau) returns at once).
+    float next(float t, float maxv2) {
+        if (!open) {
+            end = t1;
+            if (cfl > 0.0f) {
+                const float lim = cfl * dx / std::sqrt(maxv2);
+                const float span = std::fabs(t1 - t);
+                if (lim < span) end = forward ? t + lim : t - lim;
+            }
+            if (end - t == 0.0f) return 0.0f;  // math::isZero(time0 - time1)
+            open = true;
+        }
+        const float span = std::fabs(end - t);
+        const float lim = cref * dx / std::sqrt(maxv2);
+        return (lim < span) ? lim : span;  // math::Min(dt, CFL*dx/sqrt(maxAbsV))
+    }
+
+    // t advanced by the substep dt; closes the interval when t reaches its end.
+    void advance(float& t, float dt) {
+        t += forward ? dt : -dt;
+        if (!(forward ? t < end : t > end)) open = false;
+    }
+};
+
+}  // namespace gbls

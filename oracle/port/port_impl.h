@@ -532,10 +532,31 @@ struct Advector {
             maxAbsV = fmaxr(maxAbsV, v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         }
         if (!(maxAbsV > 1e-5f) && !(maxAbsV < -1e-5f)) return 0.0f;
+        return maxAbsV;
+    }
+
+    // The substep length at t0 for max |v|^2 = maxAbsV.  cfl == 0: the
+    // reference's sampleField (tools/LevelSetAdvect.h:459-466) over [t0, t1].
+    // cfl > 0: the reference's advect(tau, tau') driven over greedy intervals
+    // tau' = tau + cfl*dx/|v|max (t1 when that reaches it), each interval
+    // running the reference's own loop, so a second short substep appears
+    // when tau + (tau' - tau) rounds short of tau'.
+    bool open = false;
+    float end = 0.0f;
+    float substep(float t0, float t1, float maxAbsV) {
         const float CFLref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) / std::sqrt(3.0f);
-        const float CFL = cfl > 0.0f ? cfl : CFLref;
-        const float dt = std::fabs(t1 - t0), dx = float(g.voxel_size);
-        return fminr(dt, CFL * dx / std::sqrt(maxAbsV));
+        const float dx = float(g.voxel_size);
+        const bool fwd = t0 < t1;
+        if (!open) {
+            end = t1;
+            if (cfl > 0.0f) {
+                const float lim = cfl * dx / std::sqrt(maxAbsV);
+                if (lim < std::fabs(t1 - t0)) end = fwd ? t0 + lim : t0 - lim;
+            }
+            if (end - t0 == 0.0f) return 0.0f;
+            open = true;
+        }
+        return fminr(std::fabs(end - t0), CFLref * dx / std::sqrt(maxAbsV));
     }
 
     // euler<N,D>(dt, phiBuffer, resultBuffer)
@@ -572,10 +593,13 @@ struct Advector {
         uint64_t count = 0;
         if (t0 - t1 == 0.0f) return 0;
         const bool fwd = t0 < t1;
+        open = false;
         while (fwd ? t0 < t1 : t0 > t1) {
             if (interrupted && interrupted()) break;
             copy_aux(g, temporal == GBLS_TVD_RK3 ? 2 : 1);
-            const float dt = sample_field(t0, t1);
+            const float maxAbsV = sample_field(t0, t1);
+            if (maxAbsV == 0.0f) break;
+            const float dt = substep(t0, t1, maxAbsV);
             if (dt == 0.0f) break;
             if (updates) *updates += offsets.back();
             if (temporal == GBLS_TVD_RK1) {
@@ -589,6 +613,7 @@ struct Advector {
                 euler(dt, 1, 2, Real(1.0f / 3.0f), true); swap_buf(g, 2);
             }
             t0 += fwd ? dt : -dt;
+            if (!(fwd ? t0 < end : t0 > end)) open = false;
             ++count;
             track(g, tr);
         }

@@ -114,6 +114,56 @@ size_t runAdvect(FloatGrid& grid, const FieldT& field, int s, int t, int ts, int
     return adv.advect(t0, t1);
 }
 
+// max |v|^2 over the active voxels at time t, as Advect::sampleField computes
+// it (tools/LevelSetAdvect.h:441-456): aligned fields at the voxel, others at
+// its world position, Vec3f::lengthSqr in float, math::Max over all voxels.
+template<typename FieldT>
+float maxSpeedSqr(const FloatGrid& grid, const FieldT& field, float t) {
+    const bool aligned = field.transform() == grid.transform();
+    const math::MapBase::ConstPtr map = grid.transform().baseMap();
+    float m = 0.0f;
+    for (auto leaf = grid.tree().cbeginLeaf(); leaf; ++leaf) {
+        for (auto it = leaf->cbeginValueOn(); it; ++it) {
+            const auto v = aligned ? field(it.getCoord(), t) : field(map->applyMap(it.getCoord().asVec3d()), t);
+            m = math::Max(m, float(v.lengthSqr()));
+        }
+    }
+    return m;
+}
+
+// A CFL number below the reference's fixed one (tools/LevelSetAdvect.h:459-463)
+// imposed by the caller: LevelSetAdvection::advect(tau, tau') over greedy
+// intervals, tau' = tau + cfl*dx/max|v| with max|v| sampled at tau over the
+// current active voxels, the last interval ending at t1.  The reference's own
+// loop runs inside each interval; its substep counts are summed.
+template<typename FieldT>
+size_t runAdvectCfl(FloatGrid& grid, const FieldT& field, int s, int t, int ts, int tt, int nc,
+                    float t0, float t1, float cfl) {
+    tools::LevelSetAdvection<FloatGrid, FieldT> adv(grid, field);
+    adv.setSpatialScheme(math::BiasedGradientScheme(s));
+    adv.setTemporalScheme(math::TemporalIntegrationScheme(t));
+    adv.setTrackerSpatialScheme(math::BiasedGradientScheme(ts));
+    adv.setTrackerTemporalScheme(math::TemporalIntegrationScheme(tt));
+    adv.setNormCount(nc);
+    size_t count = 0;
+    if (math::isZero(t0 - t1)) return 0;
+    const bool fwd = t0 < t1;
+    const float dx = float(grid.voxelSize()[0]);
+    float tau = t0;
+    while (fwd ? tau < t1 : tau > t1) {
+        if (grid.tree().leafCount() == 0) break;
+        const float m = maxSpeedSqr(grid, field, tau);
+        if (math::isApproxZero(m, math::Delta<float>::value())) break;
+        const float lim = cfl * dx / std::sqrt(m);
+        const float span = std::fabs(t1 - tau);
+        const float end = (lim < span) ? (fwd ? tau + lim : tau - lim) : t1;
+        if (end - tau == 0.0f) break;
+        count += adv.advect(tau, end);
+        tau = end;
+    }
+    return count;
+}
+
 void configureTracker(tools::LevelSetTracker<FloatGrid>& tr, int ts, int tt, int nc, int trim) {
     tr.setSpatialScheme(math::BiasedGradientScheme(ts));
     tr.setTemporalScheme(math::TemporalIntegrationScheme(tt));
@@ -398,26 +448,37 @@ int vdbref_morph(void* g, void* target, void* mask, int spatial, int temporal, i
     }
 }
 
-int vdbref_advect(void* g, const gbls_field_desc* f, int spatial, int temporal, int tspatial,
-                  int ttemporal, int normCount, float t0, float t1, uint64_t* count) {
+// cfl <= 0: the reference's advect(t0, t1); cfl > 0: runAdvectCfl.
+int vdbref_advect_cfl(void* g, const gbls_field_desc* f, int spatial, int temporal, int tspatial,
+                      int ttemporal, int normCount, float t0, float t1, float cfl, uint64_t* count) {
     try {
         FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
         size_t n = 0;
+        auto run = [&](const auto& field) {
+            return cfl > 0.0f
+                ? runAdvectCfl(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1, cfl)
+                : runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
+        };
         if (f->kind == GBLS_FIELD_CONSTANT || f->kind == GBLS_FIELD_DENSE) {
             Vec3fGrid::Ptr vel = makeVelocityGrid(*f, grid.transform());
             tools::DiscreteField<Vec3fGrid> field(*vel);
-            n = runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
+            n = run(field);
         } else {
             AnalyticField field;
             field.desc = *f;
             field.xform = grid.transform().copy();
-            n = runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
+            n = run(field);
         }
         if (count) *count = n;
         return 0;
     } catch (const std::exception& e) {
         return fail(GBLS_ERR_VALUE, e.what());
     }
+}
+
+int vdbref_advect(void* g, const gbls_field_desc* f, int spatial, int temporal, int tspatial,
+                  int ttemporal, int normCount, float t0, float t1, uint64_t* count) {
+    return vdbref_advect_cfl(g, f, spatial, temporal, tspatial, ttemporal, normCount, t0, t1, 0.0f, count);
 }
 
 // LevelSetTracker::normalize(&mask) with a MaskTree holding the given leaf

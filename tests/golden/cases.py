@@ -7,6 +7,9 @@ Each case builds an input level set, then applies a list of operations:
   ("normalize_masked", lo, hi)  LevelSetTracker::normalize(&mask) with the mask of
                                 box_mask(grid, lo, hi)
   ("state", {...})              change tracker state (norm_count, tr_temporal, trim)
+A case with "cfl" > 0 advects under that imposed CFL number: the reference's
+advect(tau, tau') over greedy intervals of cfl*dx/max|v| (the interval driver
+of oracle/ref/ref_harness.cc), the device through gbls_advect(..., cfl).
 The golden file records, after every operation, the SHA-256 digest of the
 grid's canonical arrays (openvdb_gb300.grid.digest) and the substep count.
 """
@@ -72,6 +75,32 @@ CASES = {
         field=("constant", (1.0, 0.5, 0.25)),
         schemes=(HJ, RK3, HJ, RK1, 1),
         ops=[("advect", float(t), float(t + 1)) for t in range(10)],
+    ),
+    # configuration 1 as specified: CFL 0.5 imposed by the interval driver
+    "cfg1_sphere64_cfl05": dict(
+        fixture=("sphere", 64.0, (0.0, 0.0, 0.0), 1.0, 3.0),
+        field=("constant", (1.0, 0.5, 0.25)),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        cfl=0.5,
+        ops=[("advect", float(t), float(t + 1)) for t in range(10)],
+    ),
+    "union8_deformation_cfl05": dict(
+        fixture=("union8",),
+        field=("deformation", 128.0, 10.0, 1.0),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        cfl=0.5,
+        ops=[("advect", float(t), float(t + 1)) for t in range(3)],
+    ),
+    # the benchmark workload: 64 seeded spheres (csgUnion of createLevelSetSphere
+    # in the reference), LeVeque deformation on 1024^3 x cos(pi t/100), CFL 0.5,
+    # its first two unit steps
+    "bench64_cfl05": dict(
+        fixture=("sixty_four", 2024),
+        field=("deformation", 1024.0, 100.0, 1.0),
+        schemes=(HJ, RK3, HJ, RK1, 1),
+        cfl=0.5,
+        large=True,
+        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
     ),
     "sphere20_deformation": dict(
         fixture=("sphere", 20.0, (32.0, 30.0, 34.0), 1.0, 3.0),
@@ -214,6 +243,9 @@ def make_fixture(spec):
     if spec[0] == "union8":
         c, r = union8()
         return fixtures.union_of_spheres(c, r)
+    if spec[0] == "sixty_four":
+        c, r = fixtures.sixty_four_spheres(seed=spec[1])
+        return fixtures.union_of_spheres(c, r, 1.0, 3.0)
     if spec[0] == "torus":
         return fixtures.torus(spec[1], spec[2], spec[3])
     raise ValueError(spec[0])
@@ -296,6 +328,10 @@ FILTER_CASES = {
 # Batched advection: each instance must equal its own reference advect call.
 BATCH = dict(n=6, seed=11, rmin=6.0, rmax=20.0, schemes=(HJ, RK3, HJ, RK1, 1),
              ops=[(0.0, 1.0), (1.0, 2.0)])
+
+
+# The batched configuration's per-instance imposed CFL number.
+BATCH_CFL = dict(BATCH, cfl=0.5)
 
 
 def make_batch():

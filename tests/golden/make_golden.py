@@ -19,7 +19,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from cases import BATCH, CASES, FILTER_CASES, MORPH_CASES, box_mask, make_batch, make_field, make_fixture  # noqa: E402
+from cases import BATCH, BATCH_CFL, CASES, FILTER_CASES, MORPH_CASES, box_mask, make_batch, make_field, make_fixture, union8  # noqa: E402
 from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
 from oracle import refpy  # noqa: E402
 
@@ -31,6 +31,12 @@ def run_reference(name, case, threads):
     if fx[0] == "sphere":
         ref_sphere = refpy.RefGrid.sphere(fx[1], fx[2], fx[3], fx[4]).to_host()
         assert bitwise_equal(host, ref_sphere), "fixture differs from createLevelSetSphere: " + name
+    if fx[0] in ("union8", "sixty_four"):
+        # the union fixtures equal the reference's csgUnion of createLevelSetSphere
+        from openvdb_gb300 import fixtures
+        c, r = union8() if fx[0] == "union8" else fixtures.sixty_four_spheres(seed=fx[1])
+        ref_union = refpy.RefGrid.union_of_spheres(c, r).to_host()
+        assert bitwise_equal(host, ref_union), "fixture differs from csgUnion of the spheres: " + name
     g = refpy.RefGrid.from_host(host)
     assert bitwise_equal(g.to_host(), host), "round trip through the reference grid: " + name
     field = make_field(case["field"])
@@ -49,7 +55,7 @@ def run_reference(name, case, threads):
         kw = dict(spatial=tsp, temporal=ttp, norm_count=nc, trim=trim)
         if op[0] == "advect":
             rec["count"] = g.advect(field, op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp,
-                                    tracker_temporal=ttp, norm_count=nc)
+                                    tracker_temporal=ttp, norm_count=nc, cfl=case.get("cfl", 0.0))
         elif op[0] == "track":
             g.track(**kw)
         elif op[0] == "normalize":
@@ -84,6 +90,13 @@ def main():
         with open(path, "w") as f:
             json.dump(result, f, indent=1, sort_keys=True)
         return
+    if "--batch-cfl-only" in sys.argv:  # recompute the imposed-CFL batch case, keep the rest
+        path = os.path.join(HERE, "parity_cases.json")
+        result = json.load(open(path))
+        result["__batch_cfl05__"] = run_batch(BATCH_CFL)
+        with open(path, "w") as f:
+            json.dump(result, f, indent=1, sort_keys=True)
+        return
     if "--filters-only" in sys.argv:  # recompute the LevelSetFilter cases, keep the rest
         path = os.path.join(HERE, "parity_cases.json")
         result = json.load(open(path))
@@ -108,6 +121,7 @@ def main():
         print("%-32s ops=%d final leaves=%s active=%s" % (name, len(a) - 1, last.get("summary", {}).get("leaves"),
                                                           last.get("summary", {}).get("active")))
     result["__batch__"] = run_batch()
+    result["__batch_cfl05__"] = run_batch(BATCH_CFL)
     morph = {}
     for name, case in MORPH_CASES.items():
         a = run_morph(name, case, 1)
@@ -167,17 +181,17 @@ def run_filter(case, threads):
     return out
 
 
-def run_batch():
+def run_batch(spec=BATCH):
     """Each instance of the batch case advected alone by the reference."""
     grids, fields = make_batch()
-    sp, tp, tsp, ttp, nc = BATCH["schemes"]
+    sp, tp, tsp, ttp, nc = spec["schemes"]
     out = []
     for g, f in zip(grids, fields):
         r = refpy.RefGrid.from_host(g)
         rec = [{"op": "input", "digest": digest(g), "summary": summary(g)}]
-        for t0, t1 in BATCH["ops"]:
+        for t0, t1 in spec["ops"]:
             n = r.advect(f, t0, t1, spatial=sp, temporal=tp, tracker_spatial=tsp, tracker_temporal=ttp,
-                         norm_count=nc)
+                         norm_count=nc, cfl=spec.get("cfl", 0.0))
             h = r.to_host()
             rec.append({"op": ["advect", t0, t1], "count": n, "digest": digest(h), "summary": summary(h)})
         out.append(rec)

@@ -44,6 +44,7 @@ def run_case(name, mode=PARITY, check=True):
     adv.setTrackerSpatialScheme(tsp)
     adv.setTrackerTemporalScheme(ttp)
     adv.setNormCount(nc)
+    adv.cfl = case.get("cfl", 0.0)
     tr = adv.tracker
     results = []
     for step, (op, rec) in enumerate(zip(case["ops"], gold[1:]), start=1):
@@ -99,21 +100,24 @@ def test_parity_with_device_wide_candidate_sort(name, monkeypatch):
 
 
 @pytest.mark.gpu
-def test_batch_bit_exact_per_instance():
+@pytest.mark.parametrize("key", ["__batch__", "__batch_cfl05__"])
+def test_batch_bit_exact_per_instance(key):
     """Batched advection: every instance equals its own reference advect call
-    (independent CFL substep sequences in shared launches)."""
-    from cases import BATCH, make_batch
+    (independent CFL substep sequences in shared launches), at the reference
+    CFL number and under the imposed CFL 0.5."""
+    from cases import BATCH, BATCH_CFL, make_batch
     from openvdb_gb300 import DeviceBatch
-    gold = GOLD["__batch__"]
+    spec = BATCH_CFL if key == "__batch_cfl05__" else BATCH
+    gold = GOLD[key]
     grids, fields = make_batch()
     for g, rec in zip(grids, gold):
         assert digest(g) == rec[0]["digest"]
     b = DeviceBatch(grids)
     b.set_precision(PARITY)
-    sp, tp, tsp, ttp, nc = BATCH["schemes"]
+    sp, tp, tsp, ttp, nc = spec["schemes"]
     b.set_tracker(tsp, ttp, nc)
-    for step, (t0, t1) in enumerate(BATCH["ops"], start=1):
-        counts = b.advect(fields, t0, t1, spatial=sp, temporal=tp)
+    for step, (t0, t1) in enumerate(spec["ops"], start=1):
+        counts = b.advect(fields, t0, t1, spatial=sp, temporal=tp, cfl=spec.get("cfl", 0.0))
         for i, rec in enumerate(gold):
             assert counts[i] == rec[step]["count"], (i, step, counts[i], rec[step]["count"])
             h = b.to_host(i)

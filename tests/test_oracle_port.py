@@ -32,7 +32,7 @@ def run_port(name, threads=0):
         kw = dict(spatial=tsp, temporal=ttp, norm_count=nc, trim=trim)
         if op[0] == "advect":
             n = g.advect(field, op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp,
-                         tracker_temporal=ttp, norm_count=nc)
+                         tracker_temporal=ttp, norm_count=nc, cfl=case.get("cfl", 0.0))
             assert n == rec["count"], (name, step, n, rec["count"])
         elif op[0] == "track":
             g.track(**kw)
@@ -55,14 +55,16 @@ def test_port_thread_independent():
     run_port("sphere20_deformation", threads=1)
 
 
-def test_port_batch_instances_match_reference():
-    from cases import BATCH, make_batch
+@pytest.mark.parametrize("key", ["__batch__", "__batch_cfl05__"])
+def test_port_batch_instances_match_reference(key):
+    from cases import BATCH, BATCH_CFL, make_batch
+    spec = BATCH_CFL if key == "__batch_cfl05__" else BATCH
     grids, fields = make_batch()
-    sp, tp, tsp, ttp, nc = BATCH["schemes"]
-    for g, f, rec in zip(grids, fields, GOLD["__batch__"]):
+    sp, tp, tsp, ttp, nc = spec["schemes"]
+    for g, f, rec in zip(grids, fields, GOLD[key]):
         p = port.PortGrid(g)
-        for step, (t0, t1) in enumerate(BATCH["ops"], start=1):
+        for step, (t0, t1) in enumerate(spec["ops"], start=1):
             n = p.advect(f, t0, t1, spatial=sp, temporal=tp, tracker_spatial=tsp, tracker_temporal=ttp,
-                         norm_count=nc)
+                         norm_count=nc, cfl=spec.get("cfl", 0.0))
             assert n == rec[step]["count"]
             assert digest(p.to_host()) == rec[step]["digest"]
