@@ -44,13 +44,22 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self):
+    def __init__(self, device=0):
         self.proc = None
         self.lines = []
+        self.device = device
+
+    def _gpu_id(self):
+        """The sampled GPU by UUID: CUDA's device order need not be nvidia-smi's."""
+        try:
+            import torch
+            return "GPU-%s" % torch.cuda.get_device_properties(self.device).uuid
+        except Exception:
+            return os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self._gpu_id(),
                                           "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
                                          text=True)
@@ -137,6 +146,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def workload_config(args):
+    """The `config` both arms print: the workload, the arithmetic mode and the
+    timed window (unit steps t = warmup .. warmup + steps)."""
+    cfg = dict(WORKLOAD)
+    cfg.update({"mode": args.mode, "t_start": float(args.warmup), "unit_steps": int(args.steps)})
+    return cfg
+
+
 def build_workload():
     from openvdb_gb300 import Field, fixtures
     centers, radii = fixtures.sixty_four_spheres(seed=2024)
@@ -195,7 +212,7 @@ def run_gb300(args):
 
     dev.reset_stats()
     dev.set_profiling(True)
-    clocks = ClockSampler()
+    clocks = ClockSampler(dev_index)
     clocks.start()
     torch.cuda.synchronize()
     dist_barrier(dist)
@@ -271,13 +288,12 @@ def run_gb300(args):
         e2e = {"value": e2e_all / el, "unit": UNIT, "h2d_bytes_per_step": h2d // args.e2e_steps,
                "d2h_bytes_per_step": d2h // args.e2e_steps, "steps": args.e2e_steps}
 
-    cfg = dict(WORKLOAD)
-    cfg.update({"mode": args.mode, "active_voxels_initial": int(host.active_voxel_count()),
-                "leaves_initial": int(host.leaf_count), "fixture_build_s": round(t_build, 2),
-                "substeps": int(st["substeps"]), "t_start": float(t - args.steps),
-                "active_voxels_end": int(st["active_voxels"]),
-                "rho_dilated": (st["dilated_voxels"] / st["voxel_updates"]) if st["voxel_updates"] else None,
-                "replicas": world})
+    cfg = workload_config(args)
+    run = {"active_voxels_initial": int(host.active_voxel_count()), "leaves_initial": int(host.leaf_count),
+           "fixture_build_s": round(t_build, 2), "substeps": int(st["substeps"]),
+           "active_voxels_end": int(st["active_voxels"]),
+           "rho_dilated": (st["dilated_voxels"] / st["voxel_updates"]) if st["voxel_updates"] else None,
+           "replicas": world}
     if dist is not None:
         dist_barrier(dist)
         dist.destroy_process_group()
@@ -287,7 +303,7 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
-        "config": cfg,
+        "config": cfg, "run": run,
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "launches": int(launches),
@@ -337,7 +353,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     b.reset_stats()
     b.set_profiling(True)
-    clocks = ClockSampler()
+    clocks = ClockSampler(0)
     clocks.start()
     times, subs = [], []
     for _ in range(args.steps):
@@ -499,11 +515,17 @@ def run_reference(args):
     if not ok:
         print(json.dumps({"impl": "reference", "unavailable": "CPU oracle port not built on this host"}))
         return
-    res = port.bench_reference(steps=args.steps, warmup=args.warmup, seconds=args.cpu_seconds)
-    res.update({"impl": "reference", "metric": METRIC, "unit": UNIT, "higher_is_better": True,
-                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "config": WORKLOAD})
-    res["e2e"] = {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    print(json.dumps(res))
+    res = port.bench_reference(steps=args.steps, warmup=args.warmup)
+    ref_args = argparse.Namespace(**vars(args))
+    ref_args.mode = "parity"  # the reference's arithmetic
+    out = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": UNIT, "higher_is_better": True,
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
+           "config": workload_config(ref_args),
+           "run": {"substeps": res["substeps"], "t_start": res["t_start"]},
+           "cpu_baseline": res["cpu_baseline"],
+           "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
 
 
 def main():

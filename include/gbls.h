@@ -55,10 +55,14 @@ enum { GBLS_TVD_RK1 = 0, GBLS_TVD_RK2 = 1, GBLS_TVD_RK3 = 2 };
 enum { GBLS_TRIM_NONE = 0, GBLS_TRIM_INTERIOR = 1, GBLS_TRIM_EXTERIOR = 2, GBLS_TRIM_ALL = 3 };
 
 /* Arithmetic mode of the stencil kernels.
- * PARITY evaluates the WENO5 weights in FP64 exactly as
- *   math/FiniteDifference.h:301-321 does and every FP32 operation in the
- *   reference's order without contraction: results are bit-identical to the
- *   reference CPU path.
+ * PARITY gives results bit-identical to the reference CPU path: every FP32
+ *   operation in the reference's order without contraction, and the WENO5
+ *   weights, which math/FiniteDifference.h:301-321 computes in FP64, as
+ *   double-word FP32 pairs with an error bound that decides the reference's
+ *   float result (the rare undecided evaluations run the FP64 formula).
+ *   The environment variable GBLS_PARITY_FP64=1, read when a handle is
+ *   created, selects kernels that evaluate every weight in FP64 instead
+ *   (the same bits, slower; for cross-checking).
  * FAST evaluates everything in FP32 (contracted, shared sub-expressions). */
 enum { GBLS_MODE_PARITY = 0, GBLS_MODE_FAST = 1 };
 
@@ -348,9 +352,10 @@ int gbls_set_profiling(gbls_handle* h, int enable);
  * allocates no device memory: for host applications that give the library a
  * fixed device-memory budget and forbid allocations afterwards.  Scratch is a
  * 512 KiB static device array (at most 2,097,152 leaves; larger grids are
- * rejected with GBLS_ERR_INVALID_ARGUMENT).  The first call on each device
- * looks up that array's device address and should precede any stream
- * capture.  Calls that overlap on the GPU share the array and race.        */
+ * rejected with GBLS_ERR_INVALID_ARGUMENT; the environment variable
+ * GBLS_NOALLOC_MAX_LEAVES can lower that limit).  Every call looks up the
+ * array's device address on the handle's device.  Calls that overlap on the
+ * GPU share the array and race.                                             */
 int gbls_count_active_noalloc(gbls_handle* h, int64_t* out);
 
 /* ---- host construction of level sets ------------------------------------
@@ -370,6 +375,11 @@ int gbls_host_union_of_spheres(int64_t n, const float* centers, const float* rad
 int gbls_host_torus(float major_radius, float minor_radius, const float center[3],
                     float voxel_size, float half_width, gbls_host_grid** out);
 int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* view);
+/* math::WENO5<float> (math/FiniteDifference.h:301-321) by the double-word
+ * evaluation that the PARITY kernels run on the FP32 pipes, on n operand
+ * quintuples v[5i..5i+4]: decided[i] = 1 when out[i] is the reference's
+ * float, 0 when the kernels would evaluate the FP64 formula instead.     */
+int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint8_t* decided);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);
 

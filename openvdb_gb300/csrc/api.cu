@@ -618,6 +618,10 @@ struct gbls_handle {
     // the environment variable GBLS_SMALL_SORT_LIMIT, read when the handle
     // is created, lowers it so tests can exercise that path).
     int64_t small_sort_limit = SMALL_SORT_CAP;
+    // PARITY mode runs the ExactArith kernels (FP32 pipes, the same bits as
+    // the FP64 kernels); GBLS_PARITY_FP64=1 when the handle is created
+    // selects the FP64 kernels instead, for cross-checking.
+    bool parity_fp64 = false;
     // CFL maximum of an analytic field at the end time of the last advect
     // call, reused by the next call that starts there with the same field
     // (any other operation on the level set clears it)
@@ -1188,7 +1192,7 @@ void launch_norm(gbls_handle& h, const NormArgs& a0) {
         e1 = h.event();
         CU(cudaEventRecord(e0, h.stream));
     }
-    if (h.mode == GBLS_MODE_PARITY) launch_norm_parity(a, h.stream);
+    if (h.mode == GBLS_MODE_PARITY) (h.parity_fp64 ? launch_norm_parity : launch_norm_exact)(a, h.stream);
     else launch_norm_fast(a, h.stream);
     CU(cudaGetLastError());
     if (h.profiling) {
@@ -1601,7 +1605,7 @@ void rk_stage(gbls_handle& h, const RkArgs& a) {
         e1 = h.event();
         CU(cudaEventRecord(e0, h.stream));
     }
-    if (h.mode == GBLS_MODE_PARITY) launch_rk_parity(a, h.stream);
+    if (h.mode == GBLS_MODE_PARITY) (h.parity_fp64 ? launch_rk_parity : launch_rk_exact)(a, h.stream);
     else launch_rk_fast(a, h.stream);
     CU(cudaGetLastError());
     // FP32 values of the active voxels: stencil read + result write (+ phi_n read)
@@ -1703,7 +1707,7 @@ void morph_stages(gbls_handle& h, int spatial, int temporal, float dt) {
         a.beta = 1.0f - alpha;
         a.has_phi = has_phi;
         start_intr(h, "Morphing level set");
-        if (h.mode == GBLS_MODE_PARITY) launch_morph_stage_parity(a, h.stream);
+        if (h.mode == GBLS_MODE_PARITY) (h.parity_fp64 ? launch_morph_stage_parity : launch_morph_stage_exact)(a, h.stream);
         else launch_morph_stage_fast(a, h.stream);
         CU(cudaGetLastError());
         ++h.stats.kernel_launches;
@@ -1776,7 +1780,7 @@ void filter_pass(gbls_handle& h, FilterArgs a, const char* msg) {
         a.invert = h.filter_mask.invert;
     }
     start_intr(h, msg);
-    if (h.mode == GBLS_MODE_PARITY) launch_filter_parity(a, h.stream);
+    if (h.mode == GBLS_MODE_PARITY) (h.parity_fp64 ? launch_filter_parity : launch_filter_exact)(a, h.stream);
     else launch_filter_fast(a, h.stream);
     CU(cudaGetLastError());
     ++h.stats.kernel_launches;
@@ -2136,6 +2140,11 @@ static int64_t small_sort_limit_from_env() {
     return v < 0 ? SMALL_SORT_CAP : std::min<int64_t>(int64_t(v), SMALL_SORT_CAP);
 }
 
+static bool parity_fp64_from_env() {
+    const char* e = std::getenv("GBLS_PARITY_FP64");
+    return e && *e && std::atoi(e) != 0;
+}
+
 // Every operation that changes a level set outside gbls_advect drops the
 // cached CFL maximum.
 static void touched(gbls_handle* h) {
@@ -2167,6 +2176,7 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
         h = new gbls_handle;
         h->device = g_device;
         h->small_sort_limit = small_sort_limit_from_env();
+        h->parity_fp64 = parity_fp64_from_env();
         CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
         CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
         CU(cudaMalloc(&h->acc_d, 2 * sizeof(unsigned long long)));
@@ -2653,6 +2663,7 @@ int gbls_batch_create(int32_t n, const gbls_grid_desc* descs, gbls_handle** out)
         DeviceGuard g(g_device);
         h = new gbls_handle;
         h->small_sort_limit = small_sort_limit_from_env();
+        h->parity_fp64 = parity_fp64_from_env();
         h->device = g_device;
         CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
         CU(cudaMallocHost(&h->st_h, sizeof(DevStatus)));
@@ -2879,8 +2890,8 @@ int gbls_set_profiling(gbls_handle* h, int enable) {
 }  // extern "C"
 
 namespace gbls {
-int noalloc_count_active(int device, int64_t nleaf, const int32_t* slot, const uint64_t* am,
-                         cudaStream_t stream, int64_t* out, std::string* err);
+int noalloc_count_active(int64_t nleaf, const int32_t* slot, const uint64_t* am, cudaStream_t stream,
+                         int64_t* out, int* launches, std::string* err);
 }
 
 extern "C" {
@@ -2893,7 +2904,9 @@ int gbls_count_active_noalloc(gbls_handle* h, int64_t* out) {
     return guarded([&] {
         DeviceGuard g(h->device);
         std::string err;
-        const int rc = gbls::noalloc_count_active(h->device, h->nleaf, h->S(), h->am[h->mc].p, h->stream, out, &err);
+        int launches = 0;
+        const int rc = gbls::noalloc_count_active(h->nleaf, h->S(), h->am[h->mc].p, h->stream, out, &launches, &err);
+        h->stats.kernel_launches += uint64_t(launches);
         if (rc == 1) fail(GBLS_ERR_INVALID_ARGUMENT, err);
         if (rc != 0) fail(GBLS_ERR_CUDA, err);
     });

@@ -1,0 +1,18 @@
+// Host entry to the double-word WENO5 of weno_exact.h (the same operations
+// the PARITY kernels evaluate on the device), for tests on machines without
+// a GPU.
+#include <cstdint>
+
+#include "../../include/gbls.h"
+#include "weno_exact.h"
+
+extern "C" int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint8_t* decided) {
+    if (n < 0 || (n > 0 && (!v || !out || !decided))) return GBLS_ERR_INVALID_ARGUMENT;
+    for (int64_t i = 0; i < n; ++i) {
+        float r = 0.0f;
+        const float* q = v + 5 * i;
+        decided[i] = uint8_t(gbls::xw::weno5<float>(q[0], q[1], q[2], q[3], q[4], r) ? 1 : 0);
+        out[i] = r;
+    }
+    return GBLS_OK;
+}

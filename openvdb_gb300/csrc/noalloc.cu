@@ -16,13 +16,18 @@
 // overlap on the GPU (other streams, other threads) share the array and race.
 //
 // The array's name in host code is a host-side stand-in, not a device
-// address.  The first call on each device therefore looks up the device
-// address with cudaGetSymbolAddress while that device is current and caches
-// it; that first call should come before any stream capture.
+// address.  Every call therefore looks up the device address with
+// cudaGetSymbolAddress while the handle's device is current (a host-side
+// lookup that allocates nothing); not caching it keeps a call correct after
+// a device reset reloads the module and moves the array.
+//
+// The environment variable GBLS_NOALLOC_MAX_LEAVES, read by every call,
+// lowers the leaf limit (never raises it), so tests can reach the rejection
+// path and the exact limit on small grids.
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
+#include <cstdlib>
 #include <string>
 
 namespace gbls {
@@ -69,41 +74,36 @@ __global__ void __launch_bounds__(1024) k_noalloc_final(int nblocks, unsigned lo
     }
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-unsigned long long* g_scratch_addr[kMaxDevices] = {};
+int64_t leaf_limit() {
+    const char* e = std::getenv("GBLS_NOALLOC_MAX_LEAVES");
+    if (!e || !*e) return NOALLOC_MAX_LEAVES;
+    const long long v = std::atoll(e);
+    return (v < 0 || v > NOALLOC_MAX_LEAVES) ? NOALLOC_MAX_LEAVES : int64_t(v);
+}
 
 }  // namespace
 
 // Count the active voxels of `nleaf` leaves (slot table `slot`, active
 // masks `am`, both device arrays) on `stream` and store the count in *out.
-// The current device must be `device`.  Returns a cudaError_t-like status:
-// 0 on success, otherwise sets *err.
-int noalloc_count_active(int device, int64_t nleaf, const int32_t* slot, const uint64_t* am,
-                         cudaStream_t stream, int64_t* out, std::string* err) {
-    if (nleaf < 0 || nleaf > NOALLOC_MAX_LEAVES) {
-        *err = "gbls_count_active_noalloc supports at most " + std::to_string(NOALLOC_MAX_LEAVES) +
-               " leaves (got " + std::to_string(nleaf) + ")";
+// The current device must be the handle's.  Returns 0 on success (with the
+// number of kernels launched in *launches), 1 for a grid over the leaf
+// limit, 2 for a CUDA error; *err describes a failure.
+int noalloc_count_active(int64_t nleaf, const int32_t* slot, const uint64_t* am, cudaStream_t stream,
+                         int64_t* out, int* launches, std::string* err) {
+    *launches = 0;
+    const int64_t limit = leaf_limit();
+    if (nleaf < 0 || nleaf > limit) {
+        *err = "gbls_count_active_noalloc supports at most " + std::to_string(limit) + " leaves (got " +
+               std::to_string(nleaf) + ")";
         return 1;
     }
-    if (device < 0 || device >= kMaxDevices) {
-        *err = "device index out of range for gbls_count_active_noalloc";
-        return 1;
+    void* p = nullptr;
+    const cudaError_t se = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (se != cudaSuccess) {
+        *err = std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(se);
+        return 2;
     }
-    unsigned long long* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[device]) {
-            void* p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess) {
-                *err = std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
-                return 2;
-            }
-            g_scratch_addr[device] = static_cast<unsigned long long*>(p);
-        }
-        scratch = g_scratch_addr[device];
-    }
+    unsigned long long* scratch = static_cast<unsigned long long*>(p);
     if (nleaf == 0) {
         *out = 0;
         return 0;
@@ -111,6 +111,7 @@ int noalloc_count_active(int device, int64_t nleaf, const int32_t* slot, const u
     const int nblocks = int((nleaf + NOALLOC_LEAVES_PER_BLOCK - 1) / NOALLOC_LEAVES_PER_BLOCK);
     k_noalloc_partial<<<nblocks, NOALLOC_THREADS, 0, stream>>>(nleaf, slot, am, scratch);
     k_noalloc_final<<<1, 1024, 0, stream>>>(nblocks, scratch);
+    *launches = 2;
     cudaError_t e = cudaGetLastError();
     unsigned long long host = 0;
     if (e == cudaSuccess)

@@ -10,6 +10,9 @@ struct CflArgs;
 // Bit-faithful to the reference arithmetic (FP64 WENO weights).
 void launch_rk_parity(const RkArgs& a, cudaStream_t s);
 void launch_norm_parity(const NormArgs& a, cudaStream_t s);
+// The same bits as the parity launchers on the FP32 pipes (ExactArith).
+void launch_rk_exact(const RkArgs& a, cudaStream_t s);
+void launch_norm_exact(const NormArgs& a, cudaStream_t s);
 // FP32 arithmetic.
 void launch_rk_fast(const RkArgs& a, cudaStream_t s);
 void launch_norm_fast(const NormArgs& a, cudaStream_t s);
@@ -22,8 +25,10 @@ void launch_morph_speed_parity(const MorphSpeedArgs& a, unsigned int* max_bits, 
 void launch_morph_stage_parity(const MorphArgs& a, cudaStream_t s);
 void launch_morph_speed_fast(const MorphSpeedArgs& a, unsigned int* max_bits, cudaStream_t s);
 void launch_morph_stage_fast(const MorphArgs& a, cudaStream_t s);
+void launch_morph_stage_exact(const MorphArgs& a, cudaStream_t s);
 // LevelSetFilter passes.
 struct FilterArgs;
 void launch_filter_parity(const FilterArgs& a, cudaStream_t s);
 void launch_filter_fast(const FilterArgs& a, cudaStream_t s);
+void launch_filter_exact(const FilterArgs& a, cudaStream_t s);
 }  // namespace gbls

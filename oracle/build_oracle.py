@@ -18,7 +18,8 @@ SRC = os.path.join(HERE, "port", "levelset_port.cc")
 
 def build(verbose=False):
     os.makedirs(OUT, exist_ok=True)
-    deps = [SRC, os.path.join(HERE, "port", "port_impl.h"), os.path.join(REPO, "include", "gbls.h"),
+    deps = [SRC, os.path.join(HERE, "port", "port_impl.h"), os.path.join(HERE, "port", "fixture_port.h"),
+            os.path.join(REPO, "include", "gbls.h"),
             os.path.join(REPO, "include", "gbls_fields.h")]
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB

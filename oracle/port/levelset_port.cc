@@ -71,6 +71,8 @@ struct Pool {
     }
 };
 
+#include "fixture_port.h"
+
 namespace p32 {
 using Real = float;
 #include "port_impl.h"
@@ -111,6 +113,12 @@ extern "C" {
 
 const char* oport_last_error() { return g_err.c_str(); }
 
+// math::WENO5<float> (math/FiniteDifference.h:301-321) on n operand
+// quintuples v[5*i .. 5*i+4].
+void oport_weno5(int64_t n, const float* v, float* out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = p32::weno5(v[5 * i], v[5 * i + 1], v[5 * i + 2], v[5 * i + 3], v[5 * i + 4]);
+}
+
 // precision 32: bit-identical to the reference; 64: the same scheme in FP64
 void* oport_create_prec(const gbls_grid_desc* d, int threads, int precision) {
     Handle* h = new Handle;
@@ -125,6 +133,16 @@ void* oport_create_prec(const gbls_grid_desc* d, int threads, int precision) {
     return h;
 }
 void* oport_create(const gbls_grid_desc* d, int threads) { return oport_create_prec(d, threads, 32); }
+
+// The union of n narrow-band spheres (createLevelSetSphere + csgUnion,
+// fixture_port.h) built by the oracle itself.
+void* oport_create_spheres(int64_t n, const float* centers, const float* radii, float voxel_size,
+                           float half_width, int threads, int precision) {
+    fixture::Union u;
+    u.build(n, centers, radii, voxel_size, half_width, nthreads_of(threads));
+    const gbls_grid_desc d = u.view(voxel_size);
+    return oport_create_prec(&d, threads, precision);
+}
 void oport_free(void* h) { delete static_cast<Handle*>(h); }
 void oport_set_threads(void* h, int threads) {
     dispatch(h, [&](p32::Grid& g) { g.pool.nthreads = nthreads_of(threads); return 0; },

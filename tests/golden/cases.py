@@ -93,14 +93,14 @@ CASES = {
     ),
     # the benchmark workload: 64 seeded spheres (csgUnion of createLevelSetSphere
     # in the reference), LeVeque deformation on 1024^3 x cos(pi t/100), CFL 0.5,
-    # its first two unit steps
+    # its first 25 unit steps (the benchmark's warm-up and timed window)
     "bench64_cfl05": dict(
         fixture=("sixty_four", 2024),
         field=("deformation", 1024.0, 100.0, 1.0),
         schemes=(HJ, RK3, HJ, RK1, 1),
         cfl=0.5,
         large=True,
-        ops=[("advect", 0.0, 1.0), ("advect", 1.0, 2.0)],
+        ops=[("advect", float(t), float(t + 1)) for t in range(25)],
     ),
     "sphere20_deformation": dict(
         fixture=("sphere", 20.0, (32.0, 30.0, 34.0), 1.0, 3.0),

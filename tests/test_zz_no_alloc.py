@@ -37,3 +37,39 @@ def test_count_active_noalloc_matches_get_counts():
         m = C.c_int64(-1)
         assert L.gbls_count_active_noalloc(dev.handle, C.byref(m)) == 0
         assert m.value == n.value
+
+
+@pytest.mark.gpu
+def test_count_active_noalloc_limit_memory_and_launches(monkeypatch):
+    """The leaf limit (lowered through GBLS_NOALLOC_MAX_LEAVES): a grid of
+    exactly the limit is counted, one leaf over it is rejected with
+    GBLS_ERR_INVALID_ARGUMENT.  Calls leave the device's free memory as it
+    was, and each counted call adds its two kernels to the launch counter."""
+    import torch
+    from openvdb_gb300 import DeviceLevelSet, _abi, fixtures
+    from openvdb_gb300._abi import GridCounts
+    from openvdb_gb300._lib import lib
+
+    L = lib()
+    L.gbls_count_active_noalloc.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    L.gbls_count_active_noalloc.restype = C.c_int
+    dev = DeviceLevelSet(fixtures.sphere(24.0, (0.5, 1.5, -2.0), 1.0, 3.0))
+    counts = GridCounts()
+    assert L.gbls_get_counts(dev.handle, C.byref(counts)) == 0
+    n = C.c_int64(-1)
+    assert L.gbls_count_active_noalloc(dev.handle, C.byref(n)) == 0  # warm-up: module and stream set up
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    dev.reset_stats()
+    monkeypatch.setenv("GBLS_NOALLOC_MAX_LEAVES", str(counts.leaf_count))
+    for _ in range(3):
+        n = C.c_int64(-1)
+        assert L.gbls_count_active_noalloc(dev.handle, C.byref(n)) == 0, L.gbls_last_error()
+        assert n.value == counts.active_voxel_count
+    assert dev.stats()["kernel_launches"] == 6
+    monkeypatch.setenv("GBLS_NOALLOC_MAX_LEAVES", str(counts.leaf_count - 1))
+    n = C.c_int64(-1)
+    assert L.gbls_count_active_noalloc(dev.handle, C.byref(n)) == _abi.ERR_INVALID_ARGUMENT
+    assert b"at most" in L.gbls_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
