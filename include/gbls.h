@@ -380,6 +380,11 @@ int gbls_host_grid_view(gbls_host_grid* g, gbls_grid_desc* view);
  * quintuples v[5i..5i+4]: decided[i] = 1 when out[i] is the reference's
  * float, 0 when the kernels would evaluate the FP64 formula instead.     */
 int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint8_t* decided);
+/* The sign of that result where the three candidate sums of WENO5 agree,
+ * which lets the PARITY renormalisation skip derivatives that
+ * GodunovsNormSqrd clamps to zero: sign[i] = +1 (result >= 0), -1
+ * (result <= 0) or 0 (undecided).                                          */
+int gbls_host_weno5_sign(int64_t n, const float* v, int8_t* sign);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);
 

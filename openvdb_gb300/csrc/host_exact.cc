@@ -16,3 +16,14 @@ extern "C" int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint
     }
     return GBLS_OK;
 }
+
+// The sign that xw::weno5_sign certifies for each quintuple (+1: result
+// >= 0, -1: result <= 0, 0: undecided).
+extern "C" int gbls_host_weno5_sign(int64_t n, const float* v, int8_t* sign) {
+    if (n < 0 || (n > 0 && (!v || !sign))) return GBLS_ERR_INVALID_ARGUMENT;
+    for (int64_t i = 0; i < n; ++i) {
+        const float* q = v + 5 * i;
+        sign[i] = int8_t(gbls::xw::weno5_sign(q[0], q[1], q[2], q[3], q[4]));
+    }
+    return GBLS_OK;
+}

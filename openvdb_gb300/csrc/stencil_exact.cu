@@ -2,34 +2,21 @@
 // as the FP64 kernels of stencil_parity.cu, which stay available as
 // GBLS_PARITY_FP64=1 for cross-checking.  Built with -fmad=false like the
 // FP64 unit.
-#include <cstdlib>
-
 #include "stencil.h"
 #include "filter_ops.cuh"
 #include "morph_ops.cuh"
 #include "stencil_ops.cuh"
-#include "stencil_exact2.cuh"
 
 namespace gbls {
 
-// HJ-WENO5 runs the packed voxel-pair kernels; the other schemes and the
-// renormalisation forms with a convex combination or a copy run the
-// scalar ExactArith kernels.
-static bool dbg_env(const char* n) { const char* e = std::getenv(n); return e && *e == '1'; }
 void launch_rk_exact(const RkArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    if (a.spatial == 4 && dbg_env("GBLS_DBG_PACKED"))
-        rk_stage_kernel_exact2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
-    else
-        rk_stage_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    rk_stage_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 void launch_norm_exact(const NormArgs& a, cudaStream_t s) {
     if (a.nleaf <= 0) return;
-    if (!a.copy_only && !a.has_phi && a.spatial == 4 && dbg_env("GBLS_DBG_PACKED"))
-        normalize_kernel_exact2<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
-    else
-        normalize_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    normalize_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
 void launch_morph_stage_exact(const MorphArgs& a, cudaStream_t s) {

@@ -94,6 +94,9 @@ struct ExactArith : ParityArith {
     }
 };
 
+template <class A> struct IsExact { static constexpr bool value = false; };
+template <> struct IsExact<ExactArith> { static constexpr bool value = true; };
+
 struct FastArith {
     static constexpr bool kParity = false;
     __device__ __forceinline__ static float add(float a, float b) { return a + b; }
@@ -262,6 +265,43 @@ __device__ __forceinline__ float godunov(bool outside, const float* dm, const fl
             term = ref_max(A::mul(a, a), A::mul(b, b));
         }
         acc = (k == 0) ? term : A::add(acc, term);
+    }
+    return acc;
+}
+
+// godunov<ExactArith> of the HJ-WENO5 derivatives of the lines through a
+// voxel, evaluating only the derivatives whose value it uses: outside
+// (phi0 > 0) a backward derivative known to be <= 0 enters as
+// (max(dm,0))^2 = 0 and a forward one known to be >= 0 as (min(dp,0))^2 =
+// 0, inside the mirror images; a derivative left out is replaced by 0,
+// whose square is the same +0.  The signs come from xw::weno5_sign.
+__device__ inline float godunov_hj_exact(const float* tile, int x, int y, int z, bool outside) {
+    // one WENO5 call site in loops that are not unrolled: the double-word
+    // evaluation is long, and copies of it would not fit the instruction cache
+    float acc = 0.0f;
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
+        const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
+        const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
+        const bool need_dm = outside ? sb != -1 : sb != 1;
+        const bool need_dp = outside ? sf != 1 : sf != -1;
+        float dm = 0.0f, dp = 0.0f;
+#pragma unroll 1
+        for (int e = 0; e < 2; ++e) {
+            if (!(e ? need_dp : need_dm)) continue;
+            float q[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) q[k] = e ? D.d[5 - k] : D.d[k];  // FD: D5..D1, BD: D0..D4
+            const float w = ExactArith::weno5(q[0], q[1], q[2], q[3], q[4]);
+            if (e) dp = w;
+            else dm = w;
+        }
+        // the axis' term of GodunovsNormSqrd, summed in axis order
+        const float a = outside ? ref_max(dm, 0.0f) : ref_min(dm, 0.0f);
+        const float b = outside ? ref_min(dp, 0.0f) : ref_max(dp, 0.0f);
+        const float term = ref_max(ExactArith::mul(a, a), ExactArith::mul(b, b));
+        acc = ax == 0 ? term : ExactArith::add(acc, term);
     }
     return acc;
 }
@@ -506,13 +546,26 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
             eval_field(sf, ox + x, oy + y, oz + z, t0, vel);
         }
         if (a.backward) { vel[0] = -vel[0]; vel[1] = -vel[1]; vel[2] = -vel[2]; }
-        float g[3];
+        float dot = 0.0f;
+        if (IsExact<A>::value && a.spatial == 4) {
+            // one WENO5 call site in a loop that is not unrolled (instruction
+            // cache); dot = (v0 g0 + v1 g1) + v2 g2 in that order
+#pragma unroll 1
+            for (int ax = 0; ax < 3; ++ax) {
+                const float v = ax == 0 ? vel[0] : ax == 1 ? vel[1] : vel[2];
+                const float g = A::ijt(line_upwind<A>(tile_line(tile, x, y, z, ax), v < 0.0f), a.invdx, a.invdx_f);
+                const float m = A::mul(v, g);
+                dot = ax == 0 ? m : A::add(dot, m);
+            }
+        } else {
+            float g[3];
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            const Line7 L = tile_line(tile, x, y, z, ax);
-            g[ax] = A::ijt(scheme_upwind<A>(L, vel[ax] < 0.0f, a.spatial), a.invdx, a.invdx_f);
+            for (int ax = 0; ax < 3; ++ax) {
+                const Line7 L = tile_line(tile, x, y, z, ax);
+                g[ax] = A::ijt(scheme_upwind<A>(L, vel[ax] < 0.0f, a.spatial), a.invdx, a.invdx_f);
+            }
+            dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
         }
-        const float dot = A::add(A::add(A::mul(vel[0], g[0]), A::mul(vel[1], g[1])), A::mul(vel[2], g[2]));
         const float c = tile[tile_index(x, y, z)];
         const float r = A::sub(c, A::mul(dt, dot));
         float o = r;
@@ -571,14 +624,19 @@ __global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormAr
             continue;
         }
         if (!a.copy_only) {
-            float up[3], down[3];
+            float nsq;
+            if (IsExact<A>::value && a.spatial == 4) {
+                nsq = godunov_hj_exact(tile, x, y, z, phi0 > 0.0f);
+            } else {
+                float up[3], down[3];
 #pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-                const Line7 L = tile_line(tile, x, y, z, ax);
-                up[ax] = scheme_fd<A>(L, a.spatial);
-                down[ax] = scheme_bd<A>(L, a.spatial);
+                for (int ax = 0; ax < 3; ++ax) {
+                    const Line7 L = tile_line(tile, x, y, z, ax);
+                    up[ax] = scheme_fd<A>(L, a.spatial);
+                    down[ax] = scheme_bd<A>(L, a.spatial);
+                }
+                nsq = godunov<A>(phi0 > 0.0f, down, up);
             }
-            const float nsq = godunov<A>(phi0 > 0.0f, down, up);
             float vv = A::div(phi0, A::add(A::sqrt(A::add(A::mul(phi0, phi0), nsq)), 1e-8f));
             vv = A::sub(phi0, A::mul(A::mul(a.mdt, vv), A::sub(A::mul(A::sqrt(nsq), a.invdx), 1.0f)));
             if (a.has_phi) {

@@ -18,13 +18,14 @@
 // v1-4*v2, v2-v4 and its square, 4*v4) are evaluated in float exactly as
 // there.
 //
-// The evaluation is written once over a lane type: float (host and
-// device) and, on the device, float2 with the packed FP32x2 operations
-// (FADD2 / FMUL2 / FFMA2), which evaluate two voxels per instruction.
-// Every add, multiply and fused multiply-add is correctly rounded, never
-// contracted.  The reciprocal is the only operation that differs between
-// host (correctly rounded) and device (the hardware approximation, within
-// one ulp); it only seeds the divisions, whose error bound allows for it.
+// Host and device evaluate the same operations: every add, multiply and
+// fused multiply-add is correctly rounded and never contracted (explicit
+// round-to-nearest intrinsics on the device, -ffp-contract=off on the
+// host).  The reciprocal is the only operation that differs between host
+// (correctly rounded) and device (the hardware approximation, within one
+// ulp); it only seeds the divisions, whose error bound allows for it.  The
+// evaluation is written over a lane type V (float here), the form a
+// vectorised variant would take.
 #pragma once
 
 #include <cmath>
@@ -33,7 +34,6 @@
 
 #if defined(__CUDACC__)
 #define GBLS_XHD __host__ __device__ __forceinline__
-#define GBLS_XD __device__ __forceinline__
 #else
 #define GBLS_XHD inline
 #endif
@@ -100,47 +100,6 @@ GBLS_XHD float bitsf(uint32_t u) {
     return f;
 #endif
 }
-
-// ---- float2 lanes (device) ----------------------------------------------
-// Packed FP32x2 instructions written as PTX with an explicit rounding
-// modifier, which ptxas never fuses into a multiply-add: each operation is
-// rounded once, as the reference's float operations are.
-#if defined(__CUDACC__)
-GBLS_XD unsigned long long as_b64(float2 a) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-GBLS_XD float2 as_f2(unsigned long long r) {
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-GBLS_XD float2 add(float2 a, float2 b) {
-    unsigned long long r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(as_b64(a)), "l"(as_b64(b)));
-    return as_f2(r);
-}
-GBLS_XD float2 sub(float2 a, float2 b) {
-    unsigned long long r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(as_b64(a)), "l"(as_b64(b)));
-    return as_f2(r);
-}
-GBLS_XD float2 mul(float2 a, float2 b) {
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(as_b64(a)), "l"(as_b64(b)));
-    return as_f2(r);
-}
-GBLS_XD float2 fma(float2 a, float2 b, float2 c) {
-    unsigned long long r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(as_b64(a)), "l"(as_b64(b)), "l"(as_b64(c)));
-    return as_f2(r);
-}
-GBLS_XD float2 rcp(float2 a) { return make_float2(rcp(a.x), rcp(a.y)); }
-GBLS_XD float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
-GBLS_XD float2 vabs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
-GBLS_XD float2 splat(float c, float2) { return make_float2(c, c); }
-#endif
 
 // A double-word number h + l with |l| <= ulp(h)/2 (h = fl(h + l)).
 template <class V>
@@ -242,17 +201,6 @@ GBLS_XHD unsigned zero_mask(float a, float b, float c, float d, float e) {
     return (a == 0.0f && b == 0.0f && c == 0.0f && d == 0.0f && e == 0.0f) ? 1u : 0u;
 }
 GBLS_XHD float select_lanes(unsigned m, float a, float b) { return (m & 1u) ? a : b; }
-#if defined(__CUDACC__)
-GBLS_XD unsigned round_mask(DW<float2> t, float2 e) {
-    return (rounds_to_hi(t.h.x, t.l.x, e.x) ? 1u : 0u) | (rounds_to_hi(t.h.y, t.l.y, e.y) ? 2u : 0u);
-}
-GBLS_XD unsigned zero_mask(float2 a, float2 b, float2 c, float2 d, float2 e) {
-    return zero_mask(a.x, b.x, c.x, d.x, e.x) | (zero_mask(a.y, b.y, c.y, d.y, e.y) << 1);
-}
-GBLS_XD float2 select_lanes(unsigned m, float2 a, float2 b) {  // lane k from a where bit k is set
-    return make_float2((m & 1u) ? a.x : b.x, (m & 2u) ? a.y : b.y);
-}
-#endif
 
 // WENO5 of the reference on every lane.  Returns the mask of lanes whose
 // result `out` is the reference's float; the other lanes need the FP64
@@ -271,8 +219,21 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     // u1 = double(w1) + 3.0*v3; u3 = (3.0*v3 - double(4*v4)) + v5 (double sums)
     const DW<V> v3x3 = two_prod(splat(3.0f, v1), v3);
     const DW<V> u1 = dw_add_f(v3x3, w1);
-    const DW<V> i3 = dw_add_f(v3x3, neg(f4));
-    const DW<V> u3 = dw_add_f(i3, v5);
+    // u3 by error-free sums: u3 = us.h + ub.h + ub.l + ua.l exactly, so the
+    // pair (us.h + ub.h) is exact when ua.l and ub.l vanish.  When moreover the
+    // nonzero terms 3v3, 4v4, v5 lie within 2^20 of one another, both of the
+    // reference's double sums are exact (47 bits at most), so the pair is
+    // the reference's u3 itself.
+    const DW<V> i3 = two_sum(v3x3.h, neg(f4));
+    const DW<V> us = two_sum(i3.h, v5);
+    const DW<V> ua = two_sum(i3.l, v3x3.l);
+    const DW<V> ub = two_sum(ua.h, us.l);
+    const DW<V> u3 = two_sum(us.h, ub.h);
+    const V m3a = vabs(v3x3.h), m3b = vabs(f4), m3c = vabs(v5);
+    const V big = fmaxf(fmaxf(m3a, m3b), m3c);
+    const V inf = splat(__builtin_huge_valf(), v1);
+    const V small = fminf(fminf(m3a > 0.0f ? m3a : inf, m3b > 0.0f ? m3b : inf), m3c > 0.0f ? m3c : inf);
+    const bool u3_exact = ua.l == 0.0f && ub.l == 0.0f && !(big > mul(small, splat(0x1p20f, v1)));
     const DW<V> ub1 = dw_scale(dw_mul(u1, u1), quarter), ub3 = dw_scale(dw_mul(u3, u3), quarter);
     // d = (C*pa + 0.25*pb) + eps, every term >= 0
     const DW<V> C = dw_const(kC_h, kC_l, v1), EPS = dw_const(kEps_h, kEps_l, v1);
@@ -296,15 +257,16 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     // A_k: 2^-40 covers the double-word chain and the reference's own
     // roundings (about 2^-42.4 and 2^-49).  An error du in u moves d by
     // 0.25*2|u|du, and A by twice that relative to d: for u1 (one sum, du
-    // within 2^-46 |u1|) and for the |u3| part of u3 that stays below
-    // 2^-43 because d >= 0.25 u^2; the inner sum of u3, 3v3 - 4v4, errs by
-    // up to 2^-46 of its own magnitude, which can exceed |u3| by far, so
-    // A3 takes 2^-45 |u3| |3v3 - 4v4| / d3 more (a factor of two spare).
+    // within 2^-46 |u1|) that stays below 2^-43 because d >= 0.25 u^2.
+    // u3 is exact on both sides in the common case (u3_exact); otherwise
+    // the reference's inner sum 3v3 - 4v4 and ours err by up to 2^-46 of
+    // its magnitude, which can exceed |u3| by far, so A3 takes
+    // 2^-45 |u3| |3v3 - 4v4| / d3 more (a factor of two spare).
     // p_k: the reference's products are exact, its two sums err by up to
     // 2^-52 of T_k = sum of |terms|, the cascade by 2^-47 T_k; the sum of
     // the products A_k p_k (cascade) by 2^-46 of S = sum |A_k p_k|, which
     // the 2^-40 terms cover.  The total, doubled, is e_num.
-    const V q3 = mul(mul(mul(vabs(u3.h), vabs(i3.h)), splat(0x1p-45f, v1)), mul(d3.h, r3));
+    const V q3 = u3_exact ? zero : mul(mul(mul(vabs(u3.h), vabs(i3.h)), splat(0x1p-45f, v1)), mul(d3.h, r3));
     const V e40 = splat(0x1p-40f, v1), e46 = splat(0x1p-46f, v1);
     const V e3 = add(e40, q3);
     const V T1 = add(add(vabs(mul(two, v1)), vabs(mul(splat(7.0f, v1), v2))), vabs(mul(splat(11.0f, v1), v3)));
@@ -341,6 +303,29 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
         ok |= z;
     }
     return ok;
+}
+
+// The sign of WENO5's result from its three candidate sums when they agree.
+// The result is ((A1 p1 + A2 p2) + A3 p3) / (6 (A1 + A2 + A3)) with every
+// A_k > 0 (and both roundings to float keep the sign), so when no p_k is
+// negative the result is >= 0 (a zero of either sign included), and when
+// no p_k is positive it is <= 0.  Each p_k is estimated in float by two
+// fused multiply-adds, within 2u T_k of the exact sum (T_k = sum of
+// |terms|), so an estimate beyond 4u T_k has the exact sum's sign; T_k = 0
+// makes p_k exactly zero.  Returns +1 (result >= 0 for certain), -1
+// (result <= 0 for certain) or 0 (undecided).
+GBLS_XHD int weno5_sign(float v1, float v2, float v3, float v4, float v5) {
+    const float t1 = add(add(vabs(mul(2.0f, v1)), vabs(mul(7.0f, v2))), vabs(mul(11.0f, v3)));
+    const float t2 = add(add(vabs(mul(5.0f, v3)), vabs(v2)), vabs(mul(2.0f, v4)));
+    const float t3 = add(add(vabs(mul(2.0f, v3)), vabs(mul(5.0f, v4))), vabs(v5));
+    const float e1 = fma(11.0f, v3, fma(-7.0f, v2, mul(2.0f, v1)));
+    const float e2 = fma(2.0f, v4, fma(5.0f, v3, -v2));
+    const float e3 = fma(-1.0f, v5, fma(5.0f, v4, mul(2.0f, v3)));
+    const float m1 = mul(t1, 0x1p-22f), m2 = mul(t2, 0x1p-22f), m3 = mul(t3, 0x1p-22f);
+    const bool z1 = t1 == 0.0f, z2 = t2 == 0.0f, z3 = t3 == 0.0f;
+    const bool nonneg = (z1 || e1 > m1) && (z2 || e2 > m2) && (z3 || e3 > m3);
+    const bool nonpos = (z1 || e1 < -m1) && (z2 || e2 < -m2) && (z3 || e3 < -m3);
+    return nonneg ? 1 : nonpos ? -1 : 0;
 }
 
 // Vec3d(g) * invdx (double) rounded to float (GradientBiased's applyIJT,

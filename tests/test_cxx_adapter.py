@@ -15,7 +15,9 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-REF = os.environ.get("GBLS_REFERENCE_ROOT", "/root/reference")
+from oracle.ref.build_ref import reference_root  # noqa: E402
+
+REF = reference_root()
 REFLIB = os.path.join(REPO, "oracle", "_ref", "libvdbref.so")
 
 

@@ -85,3 +85,19 @@ def test_exact_weno5_matches_reference(kind):
     undecided = 1.0 - dec.mean()
     print("%s: %d evaluations, %.2e left to FP64" % (kind, v.shape[0], undecided))
     assert undecided < 2e-3
+
+
+@pytest.mark.parametrize("kind", ["uniform", "sphere_lines", "smooth", "zeros_jumps", "walks"])
+def test_weno5_sign_is_certain(kind):
+    """Where weno5_sign certifies a sign, the reference's result has it (a
+    zero of either sign counts for both)."""
+    rng = np.random.Generator(np.random.PCG64(7))
+    v = _inputs(kind, 200_000, rng)
+    ref = port.weno5(v)
+    sign = np.empty(v.shape[0], np.int8)
+    P = C.POINTER
+    assert _lib.lib().gbls_host_weno5_sign(v.shape[0], v.ctypes.data_as(P(C.c_float)),
+                                           sign.ctypes.data_as(P(C.c_int8))) == 0
+    assert not np.any((sign == 1) & (ref < 0)), "certified >= 0 but negative"
+    assert not np.any((sign == -1) & (ref > 0)), "certified <= 0 but positive"
+    print("%s: sign certified for %.1f%%" % (kind, 100.0 * np.mean(sign != 0)))
