@@ -124,4 +124,25 @@ GBLS_HD void gbls_rotation(int i, int j, int k, const float c[3], const float om
     out[2] = GBLS_FADD(c[2], GBLS_FSUB(GBLS_FMUL(omega[0], dy), GBLS_FMUL(omega[1], dx)));
 }
 
+#if !defined(__CUDA_ARCH__)
+/* tools::EnrightField<float>::operator()(xyz, time) (tools/VelocityFields.h:
+ * 126-141): the reference's own formula with the C library's sinf / cosf, on
+ * the host only (the device's sinf rounds differently), so fields of this
+ * kind reach the device through GBLS_FIELD_HOST_SAMPLED.  xyz is the world
+ * position in double, as the reference's map.applyMap returns it. */
+static inline void gbls_enright(double x, double y, double z, float time, float out[3]) {
+    const float pi = (float)3.141592653589793238462643383279502884e+00;
+    const float phase = pi / 3.0f;
+    const float Px = pi * (float)x, Py = pi * (float)y, Pz = pi * (float)z;
+    const float tr = cosf(time * phase);
+    const float a = sinf(2.0f * Py);
+    const float b = -sinf(2.0f * Px);
+    const float c = sinf(2.0f * Pz);
+    const float sx = sinf(Px), sy = sinf(Py), sz = sinf(Pz);
+    out[0] = tr * (2.0f * (sx * sx) * a * c);
+    out[1] = tr * (b * (sy * sy) * c);
+    out[2] = tr * (b * a * (sz * sz));
+}
+#endif
+
 #endif /* GBLS_FIELDS_H */

@@ -272,22 +272,62 @@ struct RotationField {
     openvdb::Vec3f constant{0.0f, 0.0f, 0.0f}, omega{0.0f, 0.0f, 0.0f}, center{0.0f, 0.0f, 0.0f};
 };
 
+// Storage a gbls_field_desc points into, alive for one advect call.
+struct FieldStore {
+    std::vector<float> values;        // a dense velocity box
+    std::shared_ptr<void> context;    // a host sampler's state
+};
+
+namespace detail {
+// Advect::sample<Aligned> (tools/LevelSetAdvect.h:476-493) over the active
+// voxels the library hands to a HOST_SAMPLED field: field(ijk, t) when the
+// field's transform equals the level set's, else field(map.applyMap(ijk), t).
+template <typename FieldT>
+struct HostSampler {
+    const FieldT* field;
+    openvdb::math::MapBase::ConstPtr map;
+    bool aligned;
+    static void sample(void* user, int64_t n, const int32_t* ijk, float t, float* velocity) {
+        const HostSampler* s = static_cast<const HostSampler*>(user);
+        for (int64_t i = 0; i < n; ++i) {
+            const openvdb::Coord c(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2]);
+            const auto v = s->aligned ? (*s->field)(c, t) : (*s->field)(s->map->applyMap(c.asVec3d()), t);
+            velocity[3 * i] = float(v[0]);
+            velocity[3 * i + 1] = float(v[1]);
+            velocity[3 * i + 2] = float(v[2]);
+        }
+    }
+};
+}  // namespace detail
+
 // How a FieldT reaches the device: describe() fills a gbls_field_desc (with
 // storage kept alive in `store`) for advecting level set `ls` over [t0, t1].
-// Specialise it for other field types; the primary template refuses them.
+// The primary template serves every functor with the reference's interface
+// (tools/LevelSetAdvect.h:32-52), its default EnrightField included: the
+// library samples it on the host once per substep, in the reference's voxel
+// order (GBLS_FIELD_HOST_SAMPLED).  The specialisations below give the
+// device forms of the fields it can evaluate itself.
 template <typename FieldT>
 struct FieldTraits {
     template <typename GridT>
-    static gbls_field_desc describe(const FieldT&, const GridT&, float, float, std::vector<float>&) {
-        OPENVDB_THROW(openvdb::NotImplementedError,
-                      "this velocity field type has no device form; specialise openvdb_gb300::FieldTraits");
+    static gbls_field_desc describe(const FieldT& f, const GridT& ls, float, float, FieldStore& store) {
+        auto s = std::make_shared<detail::HostSampler<FieldT>>();
+        s->field = &f;
+        s->map = ls.transform().baseMap();
+        s->aligned = f.transform() == ls.transform();
+        gbls_field_desc d{};
+        d.kind = GBLS_FIELD_HOST_SAMPLED;
+        d.host_sample = &detail::HostSampler<FieldT>::sample;
+        d.host_user = s.get();
+        store.context = s;
+        return d;
     }
 };
 
 template <>
 struct FieldTraits<ConstantField> {
     template <typename GridT>
-    static gbls_field_desc describe(const ConstantField& f, const GridT&, float, float, std::vector<float>&) {
+    static gbls_field_desc describe(const ConstantField& f, const GridT&, float, float, FieldStore&) {
         gbls_field_desc d{};
         d.kind = GBLS_FIELD_CONSTANT;
         for (int i = 0; i < 3; ++i) d.constant[i] = f.velocity[i];
@@ -298,7 +338,7 @@ struct FieldTraits<ConstantField> {
 template <>
 struct FieldTraits<DeformationField> {
     template <typename GridT>
-    static gbls_field_desc describe(const DeformationField& f, const GridT&, float, float, std::vector<float>&) {
+    static gbls_field_desc describe(const DeformationField& f, const GridT&, float, float, FieldStore&) {
         gbls_field_desc d{};
         d.kind = GBLS_FIELD_DEFORMATION;
         d.domain = f.domain;
@@ -311,7 +351,7 @@ struct FieldTraits<DeformationField> {
 template <>
 struct FieldTraits<RotationField> {
     template <typename GridT>
-    static gbls_field_desc describe(const RotationField& f, const GridT&, float, float, std::vector<float>&) {
+    static gbls_field_desc describe(const RotationField& f, const GridT&, float, float, FieldStore&) {
         gbls_field_desc d{};
         d.kind = GBLS_FIELD_ROTATION;
         for (int i = 0; i < 3; ++i) {
@@ -341,7 +381,8 @@ template <typename VelGridT, typename SamplerT>
 struct FieldTraits<openvdb::tools::DiscreteField<VelGridT, SamplerT>> {
     using FieldT = openvdb::tools::DiscreteField<VelGridT, SamplerT>;
     template <typename GridT>
-    static gbls_field_desc describe(const FieldT& f, const GridT& ls, float t0, float t1, std::vector<float>& store) {
+    static gbls_field_desc describe(const FieldT& f, const GridT& ls, float t0, float t1, FieldStore& fstore) {
+        std::vector<float>& store = fstore.values;
         gbls_field_desc d{};
         d.kind = GBLS_FIELD_DENSE;
         openvdb::CoordBBox band;

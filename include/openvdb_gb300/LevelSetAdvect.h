@@ -70,7 +70,7 @@ public:
 
     // tools/LevelSetAdvect.h:216-289 + Advect::advect :338-418.
     size_t advect(ValueType time0, ValueType time1) {
-        std::vector<float> store;
+        FieldStore store;
         const gbls_field_desc fd =
             FieldTraits<FieldT>::describe(mField, mTracker.grid(), float(time0), float(time1), store);
         gbls_field* field = nullptr;

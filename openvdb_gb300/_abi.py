@@ -5,7 +5,7 @@ checked against the compiled library in tests/test_abi.py.
 """
 import ctypes as C
 
-GBLS_ABI_VERSION = 2
+GBLS_ABI_VERSION = 3
 
 # status codes
 OK = 0
@@ -27,7 +27,7 @@ TVD_RK1, TVD_RK2, TVD_RK3 = 0, 1, 2
 TRIM_NONE, TRIM_INTERIOR, TRIM_EXTERIOR, TRIM_ALL = 0, 1, 2, 3
 MODE_PARITY, MODE_FAST = 0, 1
 MAP_UNIFORM_SCALE, MAP_UNIFORM_SCALE_TRANSLATE, MAP_TRANSLATION = 0, 1, 2
-FIELD_CONSTANT, FIELD_DENSE, FIELD_DEFORMATION, FIELD_ROTATION = 0, 1, 2, 3
+FIELD_CONSTANT, FIELD_DENSE, FIELD_DEFORMATION, FIELD_ROTATION, FIELD_HOST_SAMPLED = 0, 1, 2, 3, 4
 
 
 class GridDesc(C.Structure):
@@ -79,7 +79,18 @@ class FieldDesc(C.Structure):
         ("dense_map_type", C.c_int32),
         ("dense_voxel_size", C.c_double),
         ("dense_translation", C.c_double * 3),
+        ("host_sample", C.c_void_p),
+        ("host_user", C.c_void_p),
     ]
+
+
+class HostMap(C.Structure):
+    """gbls_host_map: index -> world, x * scale + translation."""
+    _fields_ = [("scale", C.c_double), ("translation", C.c_double * 3)]
+
+
+# gbls_host_sample_fn: (user, n, ijk[n][3] int32, t, velocity[n][3] float)
+HOST_SAMPLE = C.CFUNCTYPE(None, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.c_float, C.POINTER(C.c_float))
 
 
 INTERRUPT_START = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p)

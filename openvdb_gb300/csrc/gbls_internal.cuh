@@ -308,6 +308,10 @@ struct FieldParams {
     float domain, period, scale;
     float omega[3];
     float center[3];
+    // HOST_SAMPLED: the velocity of active voxel `rank` of leaf l (leaf list
+    // order) is sampled[3 * (prefix[l] + rank) ...]
+    const float* sampled;
+    const int64_t* prefix;
 };
 
 }  // namespace gbls

@@ -130,6 +130,13 @@ __global__ void __launch_bounds__(STENCIL_THREADS, 16) rk_stage_kernel_x2(const 
             ve0[0] = u.x; ve1[0] = u.y;
             ve0[1] = v.x; ve1[1] = v.y;
             ve0[2] = w.x; ve1[2] = w.y;
+        } else if (sf.kind == 4) {  // GBLS_FIELD_HOST_SAMPLED: ranks i0, i1 of leaf l
+            const float* q0 = sf.sampled + 3 * (sf.prefix[l] + i0);
+            const float* q1 = sf.sampled + 3 * (sf.prefix[l] + i1);
+            for (int k = 0; k < 3; ++k) { ve0[k] = q0[k]; ve1[k] = q1[k]; }
+            if (a.backward) {
+                for (int k = 0; k < 3; ++k) { ve0[k] = -ve0[k]; ve1[k] = -ve1[k]; }
+            }
         } else {
             eval_field(sf, ox + x0, oy + y0, oz + z0, t0, ve0);
             eval_field(sf, ox + x1, oy + y1, oz + z1, t0, ve1);

@@ -80,6 +80,7 @@ struct ParityArith {
 static __device__ __noinline__ float weno5_fp64(float v1, float v2, float v3, float v4, float v5) {
     return ParityArith::weno5(v1, v2, v3, v4, v5);
 }
+static __device__ __noinline__ float ijt_fp64(float g, double invdx) { return ParityArith::ijt(g, invdx, 0.0f); }
 
 struct ExactArith : ParityArith {
     __device__ __forceinline__ static float weno5(float v1, float v2, float v3, float v4, float v5) {
@@ -87,10 +88,11 @@ struct ExactArith : ParityArith {
         if (xw::weno5<float>(v1, v2, v3, v4, v5, r)) return r;
         return weno5_fp64(v1, v2, v3, v4, v5);
     }
-    // applyIJT: with dx = 1 the double product is g itself
-    __device__ __forceinline__ static float ijt(float g, double invdx, float f) {
+    // applyIJT: with dx = 1 the double product is g itself; otherwise the
+    // FP64 product, in a call the compiler cannot execute speculatively
+    __device__ __forceinline__ static float ijt(float g, double invdx, float) {
         if (__double_as_longlong(invdx) == 0x3FF0000000000000ll) return g;
-        return ParityArith::ijt(g, invdx, f);
+        return ijt_fp64(g, invdx);
     }
 };
 
@@ -542,6 +544,9 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
             vel[0] = __fmul_rn(u, sf.amp);
             vel[1] = -__fmul_rn(w, sf.amp);
             vel[2] = -__fmul_rn(q, sf.amp);
+        } else if (sf.kind == 4) {  // GBLS_FIELD_HOST_SAMPLED: rank i of leaf l
+            const float* q = sf.sampled + 3 * (sf.prefix[l] + i);
+            vel[0] = q[0]; vel[1] = q[1]; vel[2] = q[2];
         } else {
             eval_field(sf, ox + x, oy + y, oz + z, t0, vel);
         }

@@ -3,8 +3,9 @@
 The reference advects in any functor with operator()(Coord, t)
 (tools/LevelSetAdvect.h:32-52).  The kinds here cover the reference's
 DiscreteField (tools/VelocityFields.h:42-94), aligned or with its own
-transform (trilinear BoxSampler), plus two
-analytic fields whose arithmetic is defined in include/gbls_fields.h.
+transform (trilinear BoxSampler), two analytic fields whose arithmetic is
+defined in include/gbls_fields.h, and any functor sampled on the host once
+per substep (the reference's default EnrightField among them).
 """
 import ctypes as C
 
@@ -54,6 +55,46 @@ class Field:
                    dense_map_type=1 + mt, dense_voxel_size=voxel_size, dense_translation=translation)
 
     @classmethod
+    def host_sampled(cls, fn):
+        """Any velocity functor (the reference's FieldT), sampled on the host
+        once per CFL substep: fn(ijk, t) receives the index coordinates of
+        the active voxels, an (n, 3) int32 array in the reference's order,
+        and returns their (n, 3) velocities in index space per time unit.
+        An exception inside fn leaves the velocities of that substep at 0
+        (ctypes reports it on stderr)."""
+        f = cls(_abi.FIELD_HOST_SAMPLED)
+
+        def sample(user, n, ijk, t, vel):
+            if n <= 0:
+                return
+            a = np.ctypeslib.as_array(ijk, shape=(n, 3))
+            out = np.ctypeslib.as_array(vel, shape=(n, 3))
+            out[...] = np.asarray(fn(a, float(t)), np.float32).reshape(n, 3)
+
+        f._sampler = _abi.HOST_SAMPLE(sample)
+        f._sampler_ptr = C.cast(f._sampler, C.c_void_p).value
+        return f
+
+    @classmethod
+    def enright(cls, voxel_size=1.0, translation=(0.0, 0.0, 0.0)):
+        """The reference's default field, tools::EnrightField<float>
+        (tools/VelocityFields.h:101-141), sampled on the host by the
+        library's gbls_host_sample_enright at each voxel's world position
+        (index * voxel_size + translation, in double).  voxel_size and
+        translation must be the level set's map exactly: a grid made with a
+        float voxel size (gbls_host_sphere, the reference's
+        createLevelSetSphere) holds that float widened to double, so pass
+        the grid's own voxel_size rather than a decimal literal."""
+        from ._lib import lib
+        f = cls(_abi.FIELD_HOST_SAMPLED)
+        f._map = _abi.HostMap()
+        f._map.scale = float(voxel_size)
+        f._map.translation[:] = [float(x) for x in translation]
+        f._sampler_ptr = C.cast(lib().gbls_host_sample_enright, C.c_void_p).value
+        f._user_ptr = C.addressof(f._map)
+        return f
+
+    @classmethod
     def deformation(cls, domain=1024.0, period=100.0, scale=1.0):
         return cls(_abi.FIELD_DEFORMATION, domain=domain, period=period, scale=scale)
 
@@ -78,4 +119,6 @@ class Field:
         d.dense_map_type = self.dense_map_type
         d.dense_voxel_size = self.dense_voxel_size
         d.dense_translation[:] = self.dense_translation
+        d.host_sample = getattr(self, "_sampler_ptr", None)
+        d.host_user = getattr(self, "_user_ptr", None)
         return d

@@ -476,6 +476,22 @@ int vdbref_advect_cfl(void* g, const gbls_field_desc* f, int spatial, int tempor
     }
 }
 
+// LevelSetAdvection<FloatGrid> with its default field, tools::EnrightField<float>.
+int vdbref_advect_enright(void* g, int spatial, int temporal, int tspatial, int ttemporal, int normCount, float t0,
+                          float t1, float cfl, uint64_t* count) {
+    try {
+        FloatGrid& grid = *static_cast<RefGrid*>(g)->grid;
+        tools::EnrightField<float> field;
+        const size_t n = cfl > 0.0f
+            ? runAdvectCfl(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1, cfl)
+            : runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
+        if (count) *count = n;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
 int vdbref_advect(void* g, const gbls_field_desc* f, int spatial, int temporal, int tspatial,
                   int ttemporal, int normCount, float t0, float t1, uint64_t* count) {
     return vdbref_advect_cfl(g, f, spatial, temporal, tspatial, ttemporal, normCount, t0, t1, 0.0f, count);

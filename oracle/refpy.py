@@ -43,6 +43,7 @@ def lib():
             [C.c_float, C.c_float, C.POINTER(C.c_uint64)]
         L.vdbref_advect_cfl.argtypes = [C.c_void_p, C.POINTER(_abi.FieldDesc)] + [C.c_int] * 5 + \
             [C.c_float] * 3 + [C.POINTER(C.c_uint64)]
+        L.vdbref_advect_enright.argtypes = [C.c_void_p] + [C.c_int] * 5 + [C.c_float] * 3 + [C.POINTER(C.c_uint64)]
         L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
         L.vdbref_set_threads.argtypes = [C.c_int]
         L.vdbref_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4
@@ -168,6 +169,15 @@ class RefGrid:
         fd = field.desc() if hasattr(field, "desc") else field
         _check(lib().vdbref_advect_cfl(self.h, C.byref(fd), spatial, temporal, tracker_spatial,
                                        tracker_temporal, norm_count, t0, t1, cfl, C.byref(n)))
+        return n.value
+
+    def advect_enright(self, t0, t1, spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK2,
+                       tracker_spatial=_abi.HJWENO5_BIAS, tracker_temporal=_abi.TVD_RK1, norm_count=3, cfl=0.0):
+        """LevelSetAdvection<FloatGrid>::advect with its default field,
+        tools::EnrightField<float>."""
+        n = C.c_uint64()
+        _check(lib().vdbref_advect_enright(self.h, spatial, temporal, tracker_spatial, tracker_temporal, norm_count,
+                                           t0, t1, cfl, C.byref(n)))
         return n.value
 
     def morph(self, target, t0, t1, mask=None, mask_range=(0.0, 1.0), invert=False,

@@ -130,8 +130,9 @@ int main() {
     vel->setTransform(sphere->transform().copy());
     vel->tree().setValue(Coord(1, 2, 3), Vec3s(2.0f, 3.0f, 4.0f));
     tools::DiscreteField<Vec3SGrid> field(*vel);
-    std::vector<float> store;
-    gbls_field_desc d = og::FieldTraits<tools::DiscreteField<Vec3SGrid>>::describe(field, *sphere, 0.0f, 1.0f, store);
+    og::FieldStore fstore;
+    std::vector<float>& store = fstore.values;
+    gbls_field_desc d = og::FieldTraits<tools::DiscreteField<Vec3SGrid>>::describe(field, *sphere, 0.0f, 1.0f, fstore);
     CHECK(d.kind == GBLS_FIELD_DENSE && d.dense_values == store.data());
     auto at = [&](int x, int y, int z, int c) {
         const size_t i = ((size_t(x - d.dense_origin[0]) * d.dense_dims[1] + size_t(y - d.dense_origin[1])) *
@@ -147,7 +148,7 @@ int main() {
     vel2->setTransform(math::Transform::createLinearTransform(0.5));
     tools::DiscreteField<Vec3SGrid> field2(*vel2);
     // non-aligned: the grid's own values and transform
-    gbls_field_desc d2 = og::FieldTraits<tools::DiscreteField<Vec3SGrid>>::describe(field2, *sphere, 0.0f, 1.0f, store);
+    gbls_field_desc d2 = og::FieldTraits<tools::DiscreteField<Vec3SGrid>>::describe(field2, *sphere, 0.0f, 1.0f, fstore);
     CHECK(d2.kind == GBLS_FIELD_DENSE && d2.dense_map_type == 1 + GBLS_MAP_UNIFORM_SCALE && d2.dense_voxel_size == 0.5);
     auto at2 = [&](int x, int y, int z, int c) {
         const size_t i = ((size_t(x - d2.dense_origin[0]) * d2.dense_dims[1] + size_t(y - d2.dense_origin[1])) *
@@ -158,6 +159,26 @@ int main() {
     for (int a = 0; a < 3; ++a)  // the band (world = index at voxel size 1) in 0.5-voxel index space
         CHECK(d2.dense_origin[a] <= 2 * band.min()[a] && d2.dense_origin[a] + d2.dense_dims[a] - 1 >= 2 * band.max()[a]);
     std::printf("ok %d DiscreteField dense box (%d x %d x %d)\n", ++g_n, d.dense_dims[0], d.dense_dims[1], d.dense_dims[2]);
+
+    // 5b. any other functor (the reference's default EnrightField): sampled on
+    //     the host at the voxels' world positions, as sample<false> does
+    {
+        FloatGrid::Ptr unit = tools::createLevelSetSphere<FloatGrid>(0.15f, Vec3f(0.35f), 0.01f, 3.0f);
+        tools::EnrightField<float> enright;
+        og::FieldStore es;
+        const gbls_field_desc de = og::FieldTraits<tools::EnrightField<float>>::describe(enright, *unit, 0.0f, 1.0f, es);
+        CHECK(de.kind == GBLS_FIELD_HOST_SAMPLED && de.host_sample && de.host_user == es.context.get());
+        const int32_t ijk[6] = {35, 20, 40, -3, 7, 11};
+        float v[6];
+        de.host_sample(de.host_user, 2, ijk, 0.25f, v);
+        bool same = true;
+        for (int i = 0; i < 2; ++i) {
+            const Vec3f r = enright(unit->transform().indexToWorld(Coord(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2])), 0.25f);
+            same = same && v[3 * i] == r[0] && v[3 * i + 1] == r[1] && v[3 * i + 2] == r[2];
+        }
+        CHECK(same);
+        std::printf("ok %d EnrightField sampled on the host like sample<false>\n", ++g_n);
+    }
 
     // 6. advect: runs on a GPU, else an OpenVDB exception (no GPU here)
     og::tools::LevelSetAdvection<FloatGrid, og::ConstantField> adv(*sphere, og::ConstantField{Vec3f(1.0f, 0.5f, 0.25f)});

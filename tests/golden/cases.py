@@ -102,6 +102,16 @@ CASES = {
         large=True,
         ops=[("advect", float(t), float(t + 1)) for t in range(25)],
     ),
+    # the reference's default FieldT, tools::EnrightField<float>, with the
+    # default schemes (HJWENO5 + TVD_RK2, tracker TVD_RK1, normCount 3): the
+    # classic Enright sphere in the unit box, sampled on the host
+    "enright_sphere_default_field": dict(
+        port=False,  # the oracle's C++ restatement takes device-style fields only
+        fixture=("sphere", 0.15, (0.35, 0.35, 0.35), 0.01, 3.0),
+        field=("enright", 0.01),
+        schemes=(HJ, RK2, HJ, RK1, 3),
+        ops=[("advect", 0.0, 0.02), ("advect", 0.02, 0.05)],
+    ),
     "sphere20_deformation": dict(
         fixture=("sphere", 20.0, (32.0, 30.0, 34.0), 1.0, 3.0),
         field=("deformation", 64.0, 8.0, 1.0),
@@ -229,6 +239,11 @@ def make_field(spec):
         n, sigma, amp, seed = spec[1:]
         return Field.dense(smoothed_noise(n, sigma, amp, seed), origin=(0, 0, 0),
                            background=(0.0, 0.0, 0.0))
+    if kind == "enright":
+        # the grid's map holds the float voxel size the sphere was made with
+        # (createLinearTransform(double(voxelSize))), and the field is
+        # evaluated at index * that double
+        return Field.enright(voxel_size=float(np.float32(spec[1])))
     if kind == "dense_xform":
         n, sigma, amp, seed, voxel, translation, origin = spec[1:]
         return Field.dense_xform(smoothed_noise(n, sigma, amp, seed), voxel, translation, origin=origin,

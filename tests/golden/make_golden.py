@@ -53,7 +53,10 @@ def run_reference(name, case, threads):
             out.append(rec)
             continue
         kw = dict(spatial=tsp, temporal=ttp, norm_count=nc, trim=trim)
-        if op[0] == "advect":
+        if op[0] == "advect" and case["field"][0] == "enright":
+            rec["count"] = g.advect_enright(op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp,
+                                            tracker_temporal=ttp, norm_count=nc, cfl=case.get("cfl", 0.0))
+        elif op[0] == "advect":
             rec["count"] = g.advect(field, op[1], op[2], spatial=sp, temporal=tp, tracker_spatial=tsp,
                                     tracker_temporal=ttp, norm_count=nc, cfl=case.get("cfl", 0.0))
         elif op[0] == "track":

@@ -42,4 +42,4 @@ def test_cxx_adapter(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("ok ") == 8
+    assert r.stdout.count("ok ") == 9
