@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define GBLS_ABI_VERSION 2
+#define GBLS_ABI_VERSION 3
 
 /* ---- status codes ---------------------------------------------------- */
 typedef enum gbls_status {
@@ -122,13 +122,40 @@ typedef struct gbls_grid_counts {
  *  DENSE        aligned DiscreteField<Vec3fGrid>: the value stored at ijk inside
  *               [dense_origin, dense_origin+dense_dims), dense_background outside
  *  DEFORMATION  LeVeque's divergence-free deformation, see gbls_fields.h
- *  ROTATION     constant + omega x (ijk - center)                            */
+ *  ROTATION     constant + omega x (ijk - center)
+ *  HOST_SAMPLED any functor: the caller's host_sample(host_user, n, ijk, t,
+ *               velocity) is called once per CFL substep, at the substep's
+ *               start time t, with the index coordinates ijk[n][3] of the n
+ *               active voxels in the reference's velocity order (leaves in
+ *               tree order, voxels in offset order within a leaf), and fills
+ *               velocity[n][3] (index-space units per time unit, as
+ *               Advect::sampleField stores it, tools/LevelSetAdvect.h:
+ *               426-493; the library negates it for backward advection and
+ *               takes max|v|^2 from it).  The C++ drop-in passes every FieldT
+ *               this way, calling field(ijk, t) or field(map(ijk), t) exactly
+ *               as the reference's sample<Aligned> does.                     */
 enum {
     GBLS_FIELD_CONSTANT = 0,
     GBLS_FIELD_DENSE = 1,
     GBLS_FIELD_DEFORMATION = 2,
-    GBLS_FIELD_ROTATION = 3
+    GBLS_FIELD_ROTATION = 3,
+    GBLS_FIELD_HOST_SAMPLED = 4
 };
+typedef void (*gbls_host_sample_fn)(void* user, int64_t n, const int32_t* ijk, float t, float* velocity);
+
+/* A level set's linear map, index -> world: x * scale + translation (scale 1
+ * for a translation map, translation 0 for a uniform scale). */
+typedef struct gbls_host_map {
+    double scale;
+    double translation[3];
+} gbls_host_map;
+
+/* A gbls_host_sample_fn for the reference's default velocity functor,
+ * tools::EnrightField<float> (tools/VelocityFields.h:101-141): user points to
+ * the level set's gbls_host_map; each voxel's world position goes through
+ * the field's float formula with the C library's sinf / cosf, as the
+ * reference evaluates it (tools/LevelSetAdvect.h:476-493).                  */
+void gbls_host_sample_enright(void* user, int64_t n, const int32_t* ijk, float t, float* velocity);
 
 typedef struct gbls_field_desc {
     int32_t kind;
@@ -151,6 +178,8 @@ typedef struct gbls_field_desc {
     int32_t dense_map_type;
     double dense_voxel_size;
     double dense_translation[3];
+    gbls_host_sample_fn host_sample;   /* HOST_SAMPLED: the functor's sampler   */
+    void* host_user;                   /* HOST_SAMPLED: its first argument      */
 } gbls_field_desc;
 
 typedef struct gbls_handle gbls_handle;   /* a device-resident level set      */
@@ -224,6 +253,9 @@ int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed); /* :351-364 
 /* ---- velocity fields ---------------------------------------------------- */
 int gbls_field_create(const gbls_field_desc* desc, gbls_field** out);
 int gbls_field_destroy(gbls_field* f);
+/* New values for a DENSE field's grid from device memory [nx][ny][nz][3],
+ * copied on `stream` (NULL: the default stream) before the call returns. */
+int gbls_field_set_dense_device(gbls_field* f, const float* values, void* stream);
 
 /* ---- LevelSetAdvection::advect (tools/LevelSetAdvect.h:216-418) ---------
  * Advects from t0 to t1 (t0 > t1 advects backward) with CFL-limited
@@ -285,8 +317,13 @@ int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int
  * is enabled, every CFL substep of gbls_advect (TVD_RK3 advection, TVD_RK1
  * tracker with normCount 1 and full trimming) is written to a tape on the
  * device.  gbls_adjoint_backward then runs the transposed substeps in reverse
- * with the recorded topology, upwind directions, Godunov branches, trimming
- * and dt held fixed:
+ * with the recorded topology, upwind directions, Godunov branches and
+ * trimming held fixed.  The substep lengths depend on the velocity (a
+ * CFL-limited dt = CFL*dx/sqrt(max|v|^2) through the voxel holding the
+ * maximum, the last substep of an interval through the ones before it, an
+ * imposed CFL number's interval ends likewise), and dL/dv includes that
+ * dependence.  Every sum runs in a fixed order: the results are
+ * deterministic.
  *   dl_final[n_final]     dL/dphi on the active voxels after the last
  *                         recorded substep, in canonical order (tree-ordered
  *                         leaves, voxels in leaf order)
@@ -295,7 +332,9 @@ int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int
  *   dl_velocity           receives dL/dv on a DENSE field's grid
  *                         [nx][ny][nz][3] (may be NULL; zero for other kinds)
  * `field` must be the field the recorded substeps used.  Recording again
- * (or disabling it) discards the tape.                                     */
+ * discards the tape but keeps its device arrays for the new one (a
+ * re-recorded forward pass of the same size allocates nothing); disabling
+ * recording releases them.                                                  */
 int gbls_adjoint_record(gbls_handle* h, int enable);
 int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int64_t* substeps);
 int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final,
@@ -306,6 +345,19 @@ int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* 
  * velocity gradient of its segments in place.  No reference counterpart.    */
 int gbls_adjoint_backward_accumulate(gbls_handle* h, const gbls_field* field, const float* dl_final,
                                      float* dl_initial, float* dl_velocity_device);
+/* As gbls_adjoint_backward_accumulate with dl_final and dl_initial in device
+ * memory as well (dL/dv ADDED into dl_velocity_device, which may be NULL):
+ * the device-resident path of a torch.autograd.Function.  No reference
+ * counterpart.                                                               */
+int gbls_adjoint_backward_device(gbls_handle* h, const gbls_field* field, const float* dl_final,
+                                 float* dl_initial, float* dl_velocity_device);
+/* The active values of the level set in canonical order (tree-ordered
+ * leaves, voxels in leaf order) to / from device memory of the handle's
+ * device, on the handle's stream; setting them refreshes the sign mask and
+ * leaves the topology unchanged.  No reference counterpart (the reference
+ * edits values through tree accessors).                                     */
+int gbls_get_active_values_device(gbls_handle* h, float* out);
+int gbls_set_active_values_device(gbls_handle* h, const float* in);
 
 /* ---- batches of independent level sets --------------------------------------
  * A batch handle holds n level sets (instances) that share the voxel size and

@@ -4,7 +4,8 @@ torch.autograd.Function around them.
 The forward pass is LevelSetAdvection::advect (HJWENO5 + TVD-RK3, tracker
 TVD-RK1 with one renormalisation) with recording enabled; the backward pass
 runs the recorded substeps in reverse with the topology, upwind directions,
-Godunov branches, trimming and CFL time steps held at their forward values.
+Godunov branches and trimming held at their forward values, and with the
+CFL time steps' dependence on the velocity carried.
 Inputs: the active values of the initial level set (canonical order) and a
 dense velocity grid; output: the active values after advection.
 """
@@ -35,6 +36,16 @@ def _declare():
     L.gbls_adjoint_backward.restype = C.c_int
     L.gbls_adjoint_backward_accumulate.argtypes = [vp, vp, P, P, vp]
     L.gbls_adjoint_backward_accumulate.restype = C.c_int
+    L.gbls_adjoint_backward_device.argtypes = [vp, vp, vp, vp, vp]
+    L.gbls_adjoint_backward_device.restype = C.c_int
+    L.gbls_get_active_values_device.argtypes = [vp, vp]
+    L.gbls_get_active_values_device.restype = C.c_int
+    L.gbls_set_active_values_device.argtypes = [vp, vp]
+    L.gbls_set_active_values_device.restype = C.c_int
+    L.gbls_field_set_dense_device.argtypes = [vp, vp, vp]
+    L.gbls_field_set_dense_device.restype = C.c_int
+    L.gbls_set_stream.argtypes = [vp, vp]
+    L.gbls_set_stream.restype = C.c_int
     _declared = True
 
 
@@ -75,7 +86,10 @@ class AdvectionTape:
         """Advect the template with active values phi0 through consecutive
         intervals times[k] -> times[k+1]; returns (phi_final, final HostGrid)."""
         g = with_active_values(self.template, phi0)
-        self.dev = DeviceLevelSet(g)
+        if self.dev is None:
+            self.dev = DeviceLevelSet(g)
+        else:
+            self.dev.upload(g)  # keeps the handle's allocations and its tape's arrays
         self.dev.set_precision(self.mode)
         adv = LevelSetAdvection(self.dev, self.field)
         adv.setTemporalScheme(TVD_RK3)
@@ -115,6 +129,69 @@ class AdvectionTape:
         return d0
 
 
+class DeviceTape:
+    """AdvectionTape with every array on the device: the initial values,
+    the velocity grid, the final values and both gradients are CUDA tensors,
+    and the handle runs on torch's current stream.  The template's topology
+    is uploaded once per forward (it is the advected object, not data)."""
+
+    def __init__(self, template, shape, origin=(0, 0, 0), background=(0.0, 0.0, 0.0), mode=PARITY, cfl=0.0,
+                 device=0):
+        _declare()
+        self.template = template
+        self.mode = mode
+        self.cfl = cfl
+        self.device = device
+        self.shape = tuple(shape)
+        # the field object: a dense grid of this shape whose values the
+        # forward pass replaces on the device
+        self.field = DeviceField(Field.dense(np.zeros(self.shape, np.float32), origin, background))
+        self.dev = DeviceLevelSet(template, device=device)
+        self.dev.set_precision(mode)
+        self.substeps = []
+
+    def _stream(self):
+        import torch
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def forward(self, phi0, velocity, times, record=True):
+        """phi0: float32 CUDA tensor of the template's active values;
+        velocity: float32 CUDA tensor of `shape`.  Returns phi_T (CUDA)."""
+        import torch
+        assert phi0.is_cuda and phi0.dtype == torch.float32 and phi0.is_contiguous()
+        assert velocity.is_cuda and velocity.dtype == torch.float32 and tuple(velocity.shape) == self.shape
+        velocity = velocity.contiguous()
+        s = self._stream()
+        _call(lib().gbls_field_set_dense_device(self.field._h, C.c_void_p(velocity.data_ptr()), s))
+        self.dev.upload(self.template)
+        _call(lib().gbls_set_stream(self.dev.handle, s))
+        _call(lib().gbls_set_active_values_device(self.dev.handle, C.c_void_p(phi0.data_ptr())))
+        adv = LevelSetAdvection(self.dev, self.field)
+        adv.setTemporalScheme(TVD_RK3)
+        adv.setTrackerTemporalScheme(TVD_RK1)
+        adv.setNormCount(1)
+        adv.cfl = self.cfl
+        _call(lib().gbls_adjoint_record(self.dev.handle, 1 if record else 0))
+        self.substeps = [adv.advect(times[k], times[k + 1]) for k in range(len(times) - 1)]
+        out = torch.empty(self.dev.active_voxel_count(), dtype=torch.float32, device=phi0.device)
+        _call(lib().gbls_get_active_values_device(self.dev.handle, C.c_void_p(out.data_ptr())))
+        return out
+
+    def backward(self, dl_final):
+        """dL/dphi_T (CUDA tensor) -> (dL/dphi0, dL/dvelocity), CUDA tensors."""
+        import torch
+        n0, nf, ns = C.c_int64(), C.c_int64(), C.c_int64()
+        _call(lib().gbls_adjoint_sizes(self.dev.handle, C.byref(n0), C.byref(nf), C.byref(ns)))
+        dlf = dl_final.detach().to(torch.float32).contiguous()
+        assert dlf.is_cuda and dlf.numel() == nf.value, (dlf.numel(), nf.value)
+        d0 = torch.empty(n0.value, dtype=torch.float32, device=dlf.device)
+        dv = torch.zeros(self.shape, dtype=torch.float32, device=dlf.device)
+        _call(lib().gbls_set_stream(self.dev.handle, self._stream()))
+        _call(lib().gbls_adjoint_backward_device(self.dev.handle, self.field._h, C.c_void_p(dlf.data_ptr()),
+                                                 C.c_void_p(d0.data_ptr()), C.c_void_p(dv.data_ptr())))
+        return d0, dv
+
+
 class CheckpointedAdvection:
     """Adjoint of a long advection with checkpoints: the forward pass keeps the
     level set only at the start of every segment of `every` intervals (host
@@ -139,7 +216,12 @@ class CheckpointedAdvection:
         self.field = DeviceField(Field.dense(self.velocity, self.origin, self.background))
 
     def _tape(self, grid):
-        return AdvectionTape(grid, self.velocity, self.origin, self.background, self.mode, self.cfl, field=self.field)
+        """One tape (one device handle) serves every segment in turn."""
+        if getattr(self, "_shared", None) is None:
+            self._shared = AdvectionTape(grid, self.velocity, self.origin, self.background, self.mode, self.cfl,
+                                         field=self.field)
+        self._shared.template = grid
+        return self._shared
 
     def forward(self, phi0, times):
         """Advect through times[0] -> times[-1]; returns (phi_final, final HostGrid)."""
@@ -152,10 +234,10 @@ class CheckpointedAdvection:
             seg = self.times[a:a + self.every + 1]
             self.segments.append((g, seg))
             tape = self._tape(g)
+            before = tape.dev.stats()["voxel_updates"] if tape.dev is not None else 0
             _, g = tape.forward(g.active_values(), seg, record=False)
             self.substeps += sum(tape.substeps)
-            self.voxel_updates += tape.dev.stats()["voxel_updates"]
-            tape.dev.close()
+            self.voxel_updates += tape.dev.stats()["voxel_updates"] - before
         return g.active_values().copy(), g
 
     def backward(self, dl_final, dvel=None):
@@ -168,30 +250,31 @@ class CheckpointedAdvection:
         self.recorded_voxel_updates = 0
         for g, seg in reversed(self.segments):
             tape = self._tape(g)
+            before = tape.dev.stats()["voxel_updates"] if tape.dev is not None else 0
             tape.forward(g.active_values(), seg, record=True)
             recorded += sum(tape.substeps)
-            self.recorded_voxel_updates += tape.dev.stats()["voxel_updates"]
+            self.recorded_voxel_updates += tape.dev.stats()["voxel_updates"] - before
             lam = tape.backward_accumulate(lam, dvel)
-            tape.dev.close()
         return lam, dvel, recorded
 
 
 def make_autograd_function():
-    """torch.autograd.Function: (phi0 active values, dense velocity) -> phi_final."""
+    """torch.autograd.Function (phi0, velocity, tape, times) -> phi_T, with
+    phi0 the template's active values and velocity the dense grid, both
+    float32 CUDA tensors, and tape a DeviceTape: forward and backward stay on
+    the device (gbls_set_active_values_device, gbls_adjoint_backward_device)."""
     import torch
 
     class LevelSetAdvect(torch.autograd.Function):
         @staticmethod
         def forward(ctx, phi0, velocity, tape, times):
-            tape.set_velocity(velocity.detach().cpu().numpy())
-            out, _ = tape.forward(phi0.detach().cpu().numpy(), times)
+            out = tape.forward(phi0.detach(), velocity.detach(), times, record=True)
             ctx.tape = tape
-            return torch.from_numpy(out).to(phi0.device)
+            return out
 
         @staticmethod
         def backward(ctx, grad_out):
-            d0, dv = ctx.tape.backward(grad_out.detach().cpu().numpy())
-            dev = grad_out.device
-            return torch.from_numpy(d0).to(dev), torch.from_numpy(dv).to(dev), None, None
+            d0, dv = ctx.tape.backward(grad_out)
+            return d0, dv, None, None
 
     return LevelSetAdvect

@@ -10,29 +10,42 @@ namespace gbls {
 
 namespace {
 
-// Shu's WENO5 (the FastArith formula, weights not rescaled) and its gradient
-// g[k] = dW/dv_{k+1}, by reverse-mode differentiation of the expression.
-__device__ __forceinline__ float weno5_grad(float v1, float v2, float v3, float v4, float v5, float g[5]) {
+// Gradient of Shu's WENO5 (the FastArith formula: weights scaled by
+// d1^2 d2^2 d3^2) by reverse-mode differentiation, arranged so that FP32
+// keeps it accurate to a few ulps where the data are smooth.  Two things
+// lose it otherwise: the smoothness indicators are third differences of the
+// level set, which the differences of first differences D_k cancel to 1e-3
+// of |D| on a radius-40 sphere, and the weight adjoints (p_k - 6W)/(6S)
+// cancel p_k against the weighted mean.  So the caller passes E_a =
+// v_{a+1} - v_a (second differences of the line, from error-free first
+// differences) and every indicator and p_k - p_j is a short combination of
+// them, and A_k-bar = sum_j A_j (p_k - p_j) / (6 S^2).
+// v1..v5: the operands (for the linear part p_k); E[0..3] = E_1..E_4.
+__device__ __forceinline__ float weno5_grad(float v1, float v2, float v3, float v4, float v5, const float E[4],
+                                            float g[5]) {
     const float C = 13.0f / 12.0f, eps = 1.0e-8f;
-    const float t1 = v1 - 2.0f * v2 + v3, u1 = v1 - 4.0f * v2 + 3.0f * v3;
-    const float t2 = v2 - 2.0f * v3 + v4, u2 = v2 - v4;
-    const float t3 = v3 - 2.0f * v4 + v5, u3 = 3.0f * v3 - 4.0f * v4 + v5;
+    const float E1 = E[0], E2 = E[1], E3 = E[2], E4 = E[3];
+    const float t1 = E2 - E1, u1 = 3.0f * E2 - E1;
+    const float t2 = E3 - E2, u2 = -(E2 + E3);
+    const float t3 = E4 - E3, u3 = E4 - 3.0f * E3;
+    const float p12 = -2.0f * E1 + 4.0f * E2 - 2.0f * E3;
+    const float p13 = -2.0f * E1 + 5.0f * E2 - 4.0f * E3 + E4;
+    const float p23 = E2 - 2.0f * E3 + E4;
     const float d1 = C * t1 * t1 + 0.25f * u1 * u1 + eps;
     const float d2 = C * t2 * t2 + 0.25f * u2 * u2 + eps;
     const float d3 = C * t3 * t3 + 0.25f * u3 * u3 + eps;
-    // scale the weights by d1^2 d2^2 d3^2 as the forward does (ratios unchanged)
     const float q1 = d1 * d1, q2 = d2 * d2, q3 = d3 * d3;
     const float A1 = 0.1f * (q2 * q3), A2 = 0.6f * (q1 * q3), A3 = 0.3f * (q1 * q2);
     const float p1 = 2.0f * v1 - 7.0f * v2 + 11.0f * v3;
     const float p2 = 5.0f * v3 - v2 + 2.0f * v4;
     const float p3 = 2.0f * v3 + 5.0f * v4 - v5;
     const float S = A1 + A2 + A3;
-    const float N = A1 * p1 + A2 * p2 + A3 * p3;
-    const float W = N / (6.0f * S);
-    // reverse: W = N / (6 S)
+    const float W = (A1 * p1 + A2 * p2 + A3 * p3) / (6.0f * S);
     const float Nb = 1.0f / (6.0f * S);
-    const float Sb = -W / S;
-    const float A1b = Nb * p1 + Sb, A2b = Nb * p2 + Sb, A3b = Nb * p3 + Sb;
+    const float NbS = Nb / S;
+    const float A1b = (A2 * p12 + A3 * p13) * NbS;
+    const float A2b = (A3 * p23 - A1 * p12) * NbS;
+    const float A3b = -(A1 * p13 + A2 * p23) * NbS;
     const float p1b = Nb * A1, p2b = Nb * A2, p3b = Nb * A3;
     // A1 = 0.1 q2 q3 etc. with q_k = d_k^2
     const float q1b = A2b * 0.6f * q3 + A3b * 0.3f * q2;
@@ -50,19 +63,33 @@ __device__ __forceinline__ float weno5_grad(float v1, float v2, float v3, float 
     return W;
 }
 
+// a + b = s + e exactly (Knuth's TwoSum)
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+    const float s = a + b;
+    const float ap = s - b;
+    const float bp = s - ap;
+    e = (a - ap) + (b - bp);
+    return s;
+}
+
 // HJ-WENO5 derivative along one line and its gradient with respect to the
 // seven line values S(-3..3): FD = W(D5..D1), BD = W(D0..D4), D_k = S_{k+1}-S_k.
+// The second differences F_k = D_{k+1} - D_k come from the error-free D_k.
 __device__ __forceinline__ float hj_grad(const Line7& L, bool fd, float dS[7]) {
-    float D[6];
+    float D[6], Dl[6], F[5];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) D[k] = L.v[k + 1] - L.v[k];
+    for (int k = 0; k < 6; ++k) D[k] = two_sum(L.v[k + 1], -L.v[k], Dl[k]);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) F[k] = (D[k + 1] - D[k]) + (Dl[k + 1] - Dl[k]);
     float g[5], dD[6] = {0, 0, 0, 0, 0, 0};
     float w;
-    if (fd) {
-        w = weno5_grad(D[5], D[4], D[3], D[2], D[1], g);
+    if (fd) {  // v = (D5, D4, D3, D2, D1): E_a = D_{5-a} - D_{6-a} = -F_{5-a}
+        const float E[4] = {-F[4], -F[3], -F[2], -F[1]};
+        w = weno5_grad(D[5], D[4], D[3], D[2], D[1], E, g);
         dD[5] = g[0]; dD[4] = g[1]; dD[3] = g[2]; dD[2] = g[3]; dD[1] = g[4];
-    } else {
-        w = weno5_grad(D[0], D[1], D[2], D[3], D[4], g);
+    } else {  // v = (D0, ..., D4): E_a = F_{a-1}
+        const float E[4] = {F[0], F[1], F[2], F[3]};
+        w = weno5_grad(D[0], D[1], D[2], D[3], D[4], E, g);
 #pragma unroll
         for (int k = 0; k < 5; ++k) dD[k] = g[k];
     }
@@ -71,80 +98,167 @@ __device__ __forceinline__ float hj_grad(const Line7& L, bool fd, float dS[7]) {
     return w;
 }
 
-// lam[packed index of tile point (x,y,z)] += val when that point is an
-// active voxel of the staged layout (inactive points and tiles are constants).
-__device__ __forceinline__ void scatter_add(const LeafStage& st, float* lam, int x, int y, int z, float val) {
-    int r = 0;
-    if (x < 0) { r = 1; x += 8; }
-    else if (x >= 8) { r = 2; x -= 8; }
-    else if (y < 0) { r = 3; y += 8; }
-    else if (y >= 8) { r = 4; y -= 8; }
-    else if (z < 0) { r = 5; z += 8; }
-    else if (z >= 8) { r = 6; z -= 8; }
-    const int v = (x << 6) | (y << 3) | z;
-    const uint4 q = st.rec[r][v >> 5];  // half word (v >> 6, (v >> 5) & 1)
-    const int bb = v & 31;
-    if (!((q.x >> bb) & 1)) return;
-    const uint32_t rank = q.z + uint32_t(__popc(q.x & ((1u << bb) - 1u)));
-    atomicAdd(lam + size_t(st.slot[r]) * LEAF_VOX + rank, val);
+// Shu's WENO5 value by the operations of weno5_grad's forward part.
+__device__ __forceinline__ float weno5_val(float v1, float v2, float v3, float v4, float v5) {
+    const float C = 13.0f / 12.0f, eps = 1.0e-8f;
+    const float t1 = v1 - 2.0f * v2 + v3, u1 = v1 - 4.0f * v2 + 3.0f * v3;
+    const float t2 = v2 - 2.0f * v3 + v4, u2 = v2 - v4;
+    const float t3 = v3 - 2.0f * v4 + v5, u3 = 3.0f * v3 - 4.0f * v4 + v5;
+    const float d1 = C * t1 * t1 + 0.25f * u1 * u1 + eps;
+    const float d2 = C * t2 * t2 + 0.25f * u2 * u2 + eps;
+    const float d3 = C * t3 * t3 + 0.25f * u3 * u3 + eps;
+    const float q1 = d1 * d1, q2 = d2 * d2, q3 = d3 * d3;
+    const float A1 = 0.1f * (q2 * q3), A2 = 0.6f * (q1 * q3), A3 = 0.3f * (q1 * q2);
+    const float p1 = 2.0f * v1 - 7.0f * v2 + 11.0f * v3;
+    const float p2 = 5.0f * v3 - v2 + 2.0f * v4;
+    const float p3 = 2.0f * v3 + 5.0f * v4 - v5;
+    const float S = A1 + A2 + A3;
+    const float N = A1 * p1 + A2 * p2 + A3 * p3;
+    return N / (6.0f * S);
 }
 
-__device__ __forceinline__ void axis_point(int ax, int x, int y, int z, int k, int& px, int& py, int& pz) {
-    px = x + (ax == 0 ? k : 0);
-    py = y + (ax == 1 ? k : 0);
-    pz = z + (ax == 2 ? k : 0);
+__device__ __forceinline__ float hj_val(const Line7& L, bool fd) {
+    float D[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) D[k] = L.v[k + 1] - L.v[k];
+    return fd ? weno5_val(D[5], D[4], D[3], D[2], D[1]) : weno5_val(D[0], D[1], D[2], D[3], D[4]);
+}
+
+// Transposed stencil sums in a fixed order.  The stage kernels below hold
+// one leaf per CTA and, axis by axis, the seven coefficients cf[k][q] =
+// d out_q / d in_{q + (k-3) e_ax} * lam_out_q of every source voxel q in
+// shared memory; each target point then sums its sources in k order.
+// Targets inside the leaf accumulate in acc (and go to part[leaf][v]);
+// targets in the three-voxel slabs of the six face neighbours go to the
+// leaf's halo record, halo[(leaf * 6 + face) * 192 + d*64 + a*8 + c] with the
+// slab point numbered as load_tile numbers it.  adj_combine_kernel then adds
+// part and the neighbours' halo records into the packed adjoint, so no sum
+// depends on the order in which CTAs run.
+constexpr int HALO_FACE = 192;
+
+__device__ __forceinline__ void gather_axis(int ax, const float (*cf)[LEAF_VOX], float* acc, float* halo, int64_t l) {
+    const int t = threadIdx.x;
+    const int stride = ax == 0 ? 64 : ax == 1 ? 8 : 1;
+#pragma unroll 1
+    for (int w = 0; w < 8; ++w) {
+        const int v = 64 * w + t;
+        const int pa = ax == 0 ? (v >> 6) : ax == 1 ? ((v >> 3) & 7) : (v & 7);
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const int qa = pa - k + 3;
+            if (qa >= 0 && qa < 8) sum += cf[k][v + (qa - pa) * stride];
+        }
+        acc[v] += sum;
+    }
+#pragma unroll 1
+    for (int j = t; j < 2 * HALO_FACE; j += STENCIL_THREADS) {
+        const int plus = j >= HALO_FACE ? 1 : 0;
+        const int r = j - plus * HALO_FACE;
+        const int d = r >> 6, aa = (r >> 3) & 7, cc = r & 7;
+        const int pa = plus ? 8 + d : -3 + d;
+        const int base = ax == 0 ? (aa << 3 | cc) : ax == 1 ? (aa << 6 | cc) : (aa << 6 | cc << 3);
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const int qa = pa - k + 3;
+            if (qa >= 0 && qa < 8) sum += cf[k][base + qa * stride];
+        }
+        halo[(size_t(l) * 6 + 2 * ax + plus) * HALO_FACE + r] = sum;
+    }
+}
+
+// Rank of bit t in word w of mask m (pre: popcounts of the words before).
+__device__ __forceinline__ int mask_rank(const uint64_t* m, const int* pre, int w, int t) {
+    return pre[w] + __popcll(m[w] & ((uint64_t(1) << t) - 1));
 }
 
 __global__ void __launch_bounds__(STENCIL_THREADS) adj_rk_kernel(const AdjRkArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
-    __shared__ uint16_t list[LEAF_VOX];
+    __shared__ float sv[3][LEAF_VOX];   // velocity as the stage used it, by position
+    __shared__ float slo[LEAF_VOX];     // lam_out by position (0: inactive)
+    __shared__ float cf[7][LEAF_VOX];
+    __shared__ float acc[LEAF_VOX];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     stage_masks(st, a.src, int(l), a.nbr + 6 * l, nullptr, nullptr);
     load_tile(tile, st, a.gamma);
-    const int n = build_list(list, st.am[0]);
-    __syncthreads();
+    const int t = threadIdx.x;
+    int pre[8];
+    {
+        int c = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) { pre[w] = c; c += __popcll(st.am[0][w]); }
+    }
     int ox, oy, oz;
     key_origin(a.keys[l], ox, oy, oz);
-    for (int i = threadIdx.x; i < n; i += STENCIL_THREADS) {
-        const float lo = a.lam_out[size_t(l) * LEAF_VOX + i];
-        if (lo == 0.0f) continue;
-        const int v = list[i];
-        const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
-        float vel[3];
-        eval_field(a.field, ox + x, oy + y, oz + z, a.t0, vel);
-        if (a.backward) { vel[0] = -vel[0]; vel[1] = -vel[1]; vel[2] = -vel[2]; }
-        if (a.alpha != 0.0f) atomicAdd(a.lam_phin + size_t(l) * LEAF_VOX + i, a.alpha * lo);
-        atomicAdd(a.lam_in + size_t(l) * LEAF_VOX + i, a.beta * lo);
-        const float coef = -a.beta * a.dt * lo;
-        float dv[3];
+#pragma unroll 1
+    for (int w = 0; w < 8; ++w) {
+        const int v = 64 * w + t;
+        float lo = 0.0f;
+        if ((st.am[0][w] >> t) & 1) lo = a.lam_out[size_t(l) * LEAF_VOX + mask_rank(st.am[0], pre, w, t)];
+        float vel[3] = {0.0f, 0.0f, 0.0f};
+        if (lo != 0.0f) {
+            eval_field(a.field, ox + w, oy + (t >> 3), oz + (t & 7), a.t0, vel);
+            if (a.backward) { vel[0] = -vel[0]; vel[1] = -vel[1]; vel[2] = -vel[2]; }
+        }
+        slo[v] = lo;
+        acc[v] = a.beta * lo;
+        sv[0][v] = vel[0];
+        sv[1][v] = vel[1];
+        sv[2][v] = vel[2];
+    }
+    __syncthreads();
+    float gdt = 0.0f;  // this thread's part of dL/d(dt)
+    const float sgn = a.backward ? -1.0f : 1.0f;
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll 1
+        for (int w = 0; w < 8; ++w) {
+            const int v = 64 * w + t;
+            const float lo = slo[v];
+            if (lo == 0.0f) {
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            const Line7 L = tile_line(tile, x, y, z, ax);
+                for (int k = 0; k < 7; ++k) cf[k][v] = 0.0f;
+                continue;
+            }
+            const int x = w, y = t >> 3, z = t & 7;
+            const float va = sv[ax][v];
             float dS[7];
-            const float w = hj_grad(L, vel[ax] < 0.0f, dS);
-            dv[ax] = coef * w * a.invdx;
-            const float c = coef * vel[ax] * a.invdx;
+            const float wv = hj_grad(tile_line(tile, x, y, z, ax), va < 0.0f, dS);
+            const float coef = -a.beta * a.dt * lo;
+            const float c = coef * va * a.invdx;
 #pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                if (dS[k] == 0.0f) continue;
-                int px, py, pz;
-                axis_point(ax, x, y, z, k - 3, px, py, pz);
-                scatter_add(st, a.lam_in, px, py, pz, c * dS[k]);
+            for (int k = 0; k < 7; ++k) cf[k][v] = c * dS[k];
+            gdt -= a.beta * lo * va * (wv * a.invdx);
+            if (a.dvel && a.field.kind == 1) {  // aligned dense velocity grid
+                const int ia = ox + x - a.field.dense_origin[0], ja = oy + y - a.field.dense_origin[1],
+                          ka = oz + z - a.field.dense_origin[2];
+                if (ia >= 0 && ja >= 0 && ka >= 0 && ia < a.field.dense_dims[0] && ja < a.field.dense_dims[1] &&
+                    ka < a.field.dense_dims[2]) {
+                    // the voxel's own cell: no other thread of the launch writes it
+                    float* p = a.dvel + 3 * ((size_t(ia) * a.field.dense_dims[1] + ja) * a.field.dense_dims[2] + ka);
+                    p[ax] += sgn * (coef * wv * a.invdx);
+                }
             }
         }
-        if (a.dvel && a.field.kind == 1) {  // aligned dense velocity grid
-            const int ia = ox + x - a.field.dense_origin[0], ja = oy + y - a.field.dense_origin[1],
-                      ka = oz + z - a.field.dense_origin[2];
-            if (ia >= 0 && ja >= 0 && ka >= 0 && ia < a.field.dense_dims[0] && ja < a.field.dense_dims[1] &&
-                ka < a.field.dense_dims[2]) {
-                float* p = a.dvel + 3 * ((size_t(ia) * a.field.dense_dims[1] + ja) * a.field.dense_dims[2] + ka);
-                const float sgn = a.backward ? -1.0f : 1.0f;
-                atomicAdd(p, sgn * dv[0]);
-                atomicAdd(p + 1, sgn * dv[1]);
-                atomicAdd(p + 2, sgn * dv[2]);
-            }
+        __syncthreads();
+        gather_axis(ax, cf, acc, a.halo, l);
+        __syncthreads();
+    }
+#pragma unroll 1
+    for (int w = 0; w < 8; ++w) a.part[size_t(l) * LEAF_VOX + 64 * w + t] = acc[64 * w + t];
+    if (a.dt_part) {  // fixed-order block sum
+        __shared__ double wsum[STENCIL_THREADS / 32];
+        double d = gdt;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if ((t & 31) == 0) wsum[t >> 5] = d;
+        __syncthreads();
+        if (t == 0) {
+            double s = 0.0;
+            for (int k = 0; k < STENCIL_THREADS / 32; ++k) s += wsum[k];
+            a.dt_part[l] += s;
         }
     }
 }
@@ -152,30 +266,41 @@ __global__ void __launch_bounds__(STENCIL_THREADS) adj_rk_kernel(const AdjRkArgs
 __global__ void __launch_bounds__(STENCIL_THREADS) adj_norm_kernel(const AdjNormArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
-    __shared__ uint16_t list[LEAF_VOX];
     __shared__ uint64_t pm[8];
+    __shared__ float scg[LEAF_VOX];       // lam4 * d phi4 / dG by position
+    __shared__ float scoef[3][LEAF_VOX];  // d G / d (selected one-sided derivative), per axis
+    __shared__ uint8_t sside[3][LEAF_VOX];  // 1: the upwind (FD) side was selected
+    __shared__ float cf[7][LEAF_VOX];
+    __shared__ float acc[LEAF_VOX];
     const int64_t l = blockIdx.x;
     if (l >= a.nleaf) return;
     stage_masks(st, a.src, int(l), a.nbr + 6 * l, a.pmask, pm);
     load_tile(tile, st, a.gamma);
     __syncthreads();
-    const int n = build_list(list, pm);
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += STENCIL_THREADS) {
-        const float lam = a.lam4[size_t(l) * LEAF_VOX + i];
+    const int t = threadIdx.x;
+    int pre[8];
+    {
+        int c = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) { pre[w] = c; c += __popcll(pm[w]); }
+    }
+#pragma unroll 1
+    for (int w = 0; w < 8; ++w) {
+        const int v = 64 * w + t;
+        const float lam = ((pm[w] >> t) & 1) ? a.lam4[size_t(l) * LEAF_VOX + mask_rank(pm, pre, w, t)] : 0.0f;
+        acc[v] = 0.0f;
+        scg[v] = 0.0f;
+        scoef[0][v] = scoef[1][v] = scoef[2][v] = 0.0f;
         if (lam == 0.0f) continue;
-        const int v = list[i];
-        const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+        const int x = w, y = t >> 3, z = t & 7;
         const float phi0 = tile[tile_index(x, y, z)];
         const bool outside = phi0 > 0.0f;
         float G = 0.0f;
-        float dtdn[3], dtup[3];
-        float gu[3][7], gd[3][7];
-#pragma unroll
+#pragma unroll 1
         for (int ax = 0; ax < 3; ++ax) {
             const Line7 L = tile_line(tile, x, y, z, ax);
-            const float up = hj_grad(L, true, gu[ax]);
-            const float dn = hj_grad(L, false, gd[ax]);
+            const float up = hj_val(L, true);
+            const float dn = hj_val(L, false);
             float aa, bb;
             if (outside) { aa = fmaxf(dn, 0.0f); bb = fminf(up, 0.0f); }
             else { aa = fminf(dn, 0.0f); bb = fmaxf(up, 0.0f); }
@@ -183,8 +308,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS) adj_norm_kernel(const AdjNorm
             G += take_b ? bb * bb : aa * aa;
             const bool dn_live = outside ? dn > 0.0f : dn < 0.0f;
             const bool up_live = outside ? up < 0.0f : up > 0.0f;
-            dtdn[ax] = (!take_b && dn_live) ? 2.0f * aa : 0.0f;
-            dtup[ax] = (take_b && up_live) ? 2.0f * bb : 0.0f;
+            scoef[ax][v] = take_b ? (up_live ? 2.0f * bb : 0.0f) : (dn_live ? 2.0f * aa : 0.0f);
+            sside[ax][v] = take_b ? 1 : 0;
         }
         const float eps = 1e-8f;
         const float r = sqrtf(phi0 * phi0 + G);
@@ -196,21 +321,127 @@ __global__ void __launch_bounds__(STENCIL_THREADS) adj_norm_kernel(const AdjNorm
         const float ds_dG = r > 0.0f ? -phi0 / (re * re) * (0.5f / r) : 0.0f;
         const float dphi4_dphi0 = 1.0f - a.mdt * ds_dphi * fac;
         const float dphi4_dG = -a.mdt * (ds_dG * fac + (sg > 0.0f ? s * a.invdx * 0.5f / sg : 0.0f));
-        float centre = lam * dphi4_dphi0;
-        const float cg = lam * dphi4_dG;
+        acc[v] = lam * dphi4_dphi0;
+        scg[v] = lam * dphi4_dG;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll 1
+        for (int w = 0; w < 8; ++w) {
+            const int v = 64 * w + t;
+            const float c = scg[v] * scoef[ax][v];
+            if (c == 0.0f) {
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-#pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                const float c = cg * (dtdn[ax] * gd[ax][k] + dtup[ax] * gu[ax][k]);
-                if (k == 3) { centre += c; continue; }
-                if (c == 0.0f) continue;
-                int px, py, pz;
-                axis_point(ax, x, y, z, k - 3, px, py, pz);
-                scatter_add(st, a.lam3, px, py, pz, c);
+                for (int k = 0; k < 7; ++k) cf[k][v] = 0.0f;
+                continue;
             }
+            float g[7];
+            hj_grad(tile_line(tile, w, t >> 3, t & 7, ax), sside[ax][v] != 0, g);
+#pragma unroll
+            for (int k = 0; k < 7; ++k) cf[k][v] = c * g[k];
         }
-        scatter_add(st, a.lam3, x, y, z, centre);
+        __syncthreads();
+        gather_axis(ax, cf, acc, a.halo, l);
+        __syncthreads();
+    }
+#pragma unroll 1
+    for (int w = 0; w < 8; ++w) a.part[size_t(l) * LEAF_VOX + 64 * w + t] = acc[64 * w + t];
+}
+
+// lam[active voxel] += part + the face neighbours' halo records (fixed
+// order: -x, +x, -y, +y, -z, +z); then lam_phin += alpha * lam_out.
+__global__ void __launch_bounds__(64) adj_combine_kernel(const AdjCombineArgs a) {
+    const int64_t l = blockIdx.x;
+    if (l >= a.nleaf) return;
+    const int t = threadIdx.x;
+    int32_t nb[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) nb[f] = a.nbr[6 * l + f];
+    const int y = t >> 3, z = t & 7;
+    int base = 0;
+#pragma unroll 1
+    for (int x = 0; x < 8; ++x) {
+        const uint64_t m = a.am[size_t(l) * 8 + x];
+        const int rank = base + __popcll(m & ((uint64_t(1) << t) - 1));
+        base += __popcll(m);
+        if (!((m >> t) & 1)) continue;
+        float val = a.part[size_t(l) * LEAF_VOX + 64 * x + t];
+        auto H = [&](int32_t n, int face, int d, int aa, int cc) {
+            return a.halo[(size_t(n) * 6 + face) * HALO_FACE + d * 64 + aa * 8 + cc];
+        };
+        if (x < 3 && nb[0] >= 0) val += H(nb[0], 1, x, y, z);
+        if (x >= 5 && nb[1] >= 0) val += H(nb[1], 0, x - 5, y, z);
+        if (y < 3 && nb[2] >= 0) val += H(nb[2], 3, y, x, z);
+        if (y >= 5 && nb[3] >= 0) val += H(nb[3], 2, y - 5, x, z);
+        if (z < 3 && nb[4] >= 0) val += H(nb[4], 5, z, x, y);
+        if (z >= 5 && nb[5] >= 0) val += H(nb[5], 4, z - 5, x, y);
+        const size_t i = size_t(l) * LEAF_VOX + rank;
+        a.lam[i] += val;
+        if (a.lam_phin && a.alpha != 0.0f) a.lam_phin[i] += a.alpha * a.lam_out[i];
+    }
+}
+
+__global__ void __launch_bounds__(64) adj_argmax_kernel(const AdjArgmaxArgs a) {
+    const int64_t l = blockIdx.x;
+    if (l >= a.nleaf) return;
+    const int w = threadIdx.x >> 3, q = threadIdx.x & 7;  // word w, byte q
+    const uint64_t bits = (a.am[size_t(l) * 8 + w] >> (8 * q)) & 0xffu;
+    if (!bits) return;
+    int ox, oy, oz;
+    key_origin(a.keys[l], ox, oy, oz);
+    for (int b = 0; b < 8; ++b) {
+        if (!((bits >> b) & 1)) continue;
+        const int v = 64 * w + 8 * q + b;
+        float vel[3];
+        eval_field(a.field, ox + (v >> 6), oy + ((v >> 3) & 7), oz + (v & 7), a.t0, vel);
+        // |v|^2 as the CFL reduction forms it
+        const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(vel[0], vel[0]), __fmul_rn(vel[1], vel[1])),
+                                   __fmul_rn(vel[2], vel[2]));
+        if (l2 == a.maxv2) {
+            atomicMin(a.argkey, static_cast<unsigned long long>(l) * LEAF_VOX + unsigned(v));
+            return;  // this thread's later voxels come after this one
+        }
+    }
+}
+
+__global__ void adj_argcell_kernel(const AdjArgmaxArgs a) {
+    const unsigned long long k = *a.argkey;
+    int64_t cell = -1;
+    if (k != ~0ull && int64_t(k / LEAF_VOX) < a.nleaf) {
+        const int64_t l = int64_t(k / LEAF_VOX);
+        const int v = int(k % LEAF_VOX);
+        int ox, oy, oz;
+        key_origin(a.keys[l], ox, oy, oz);
+        const FieldParams& f = a.field;
+        const int i = ox + (v >> 6) - f.dense_origin[0], j = oy + ((v >> 3) & 7) - f.dense_origin[1],
+                  kk = oz + (v & 7) - f.dense_origin[2];
+        if (i >= 0 && j >= 0 && kk >= 0 && i < f.dense_dims[0] && j < f.dense_dims[1] && kk < f.dense_dims[2])
+            cell = (int64_t(i) * f.dense_dims[1] + j) * f.dense_dims[2] + kk;
+    }
+    *a.argcell = cell;
+}
+
+__global__ void __launch_bounds__(1024) adj_dt_reduce_kernel(const double* part, int64_t n, double* out) {
+    double d = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) d += part[i];
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    __shared__ double ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < 32; ++k) t += ws[k];
+        *out = t;
+    }
+}
+
+__global__ void adj_dt_scatter_kernel(int64_t n, const int64_t* cell, const float* mbar, const float* dense,
+                                      float* dvel) {
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t c = cell[k];
+        if (c < 0 || mbar[k] == 0.0f) continue;
+        for (int e = 0; e < 3; ++e) dvel[3 * c + e] += 2.0f * mbar[k] * dense[3 * c + e];
     }
 }
 
@@ -302,11 +533,25 @@ void launch_adj_rk(const AdjRkArgs& a, cudaStream_t s) {
 void launch_adj_norm(const AdjNormArgs& a, cudaStream_t s) {
     if (a.nleaf > 0) adj_norm_kernel<<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
+void launch_adj_combine(const AdjCombineArgs& a, cudaStream_t s) {
+    if (a.nleaf > 0) adj_combine_kernel<<<unsigned(a.nleaf), 64, 0, s>>>(a);
+}
 void launch_adj_expand(const AdjExpandArgs& a, cudaStream_t s) {
     if (a.nleaf > 0) adj_expand_kernel<<<unsigned(a.nleaf), 64, 0, s>>>(a);
 }
 void launch_adj_map(const AdjMapArgs& a, cudaStream_t s) {
     if (a.nleaf > 0) adj_map_kernel<<<unsigned(a.nleaf), 64, 0, s>>>(a);
+}
+void launch_adj_argmax(const AdjArgmaxArgs& a, cudaStream_t s) {
+    if (a.nleaf > 0) adj_argmax_kernel<<<unsigned(a.nleaf), 64, 0, s>>>(a);
+    adj_argcell_kernel<<<1, 1, 0, s>>>(a);
+}
+void launch_adj_dt_reduce(const double* part, int64_t n, double* out, cudaStream_t s) {
+    adj_dt_reduce_kernel<<<1, 1024, 0, s>>>(part, n, out);
+}
+void launch_adj_dt_scatter(int64_t n, const int64_t* cell, const float* mbar, const float* dense, float* dvel,
+                           cudaStream_t s) {
+    if (n > 0) adj_dt_scatter_kernel<<<1, 1, 0, s>>>(n, cell, mbar, dense, dvel);
 }
 
 }  // namespace gbls

@@ -465,6 +465,104 @@ __global__ void k_count_active_inst(int64_t n, const uint64_t* keys, const int32
     if (c) atomicAdd(out + key_instance(keys[l]), c);
 }
 
+// Active voxels per leaf, in leaf-list order.
+__global__ void k_leaf_active(int64_t n, const int32_t* slot, const uint64_t* am, int64_t* cnt) {
+    const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (l >= n) return;
+    int64_t c = 0;
+    for (int w = 0; w < 8; ++w) c += __popcll(am[size_t(slot[l]) * 8 + w]);
+    cnt[l] = c;
+}
+
+// Index coordinates of the active voxels in the reference's velocity order
+// (leaves in tree order, voxels in offset order): leaf l's active voxel of
+// rank r goes to entry prefix[l] + r.  One CTA of 64 threads per leaf,
+// thread t owning bit t of every mask word.
+__global__ void __launch_bounds__(64) k_active_ijk(int64_t n, const uint64_t* keys, const int32_t* slot,
+                                                  const uint64_t* am, const int64_t* prefix, int32_t* ijk) {
+    const int64_t l = blockIdx.x;
+    if (l >= n) return;
+    const int t = threadIdx.x;
+    int32_t ox, oy, oz;
+    key_origin(keys[l], ox, oy, oz);
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    int64_t base = prefix[l];
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t w = am[size_t(slot[l]) * 8 + k];
+        if ((w >> t) & 1) {
+            const int v = (k << 6) | t;
+            int32_t* q = ijk + 3 * (base + __popcll(w & low));
+            q[0] = ox + (v >> 6);
+            q[1] = oy + ((v >> 3) & 7);
+            q[2] = oz + (v & 7);
+        }
+        base += __popcll(w);
+    }
+}
+
+// Active voxels per leaf of a mask array indexed through slot (or
+// directly), 0 for leaves with keep[l] == 0.
+__global__ void k_mask_count(int64_t n, const int32_t* slot, const uint64_t* m, const int32_t* keep, int64_t* cnt) {
+    const int64_t l = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (l >= n) return;
+    const size_t s = size_t(slot ? slot[l] : int32_t(l));
+    int64_t c = 0;
+    if (!keep || keep[l])
+        for (int w = 0; w < 8; ++w) c += __popcll(m[s * 8 + w]);
+    cnt[l] = c;
+}
+
+// Packed per-leaf values (leaf storage s = slot[l] or l, [s*512 + rank]) to
+// one array in leaf order (to_packed: packed[prefix[l] + rank]), or back
+// (to leaf dst_leaf[l] when given, else s).  Leaves with keep[l] == 0 are
+// skipped.  One CTA of 64 threads per leaf, thread t owning bit t of every
+// mask word.
+__global__ void __launch_bounds__(64) k_packed_move(int64_t n, const int32_t* slot, const int32_t* keep,
+                                                   const int32_t* dst_leaf, const uint64_t* m,
+                                                   const int64_t* prefix, const float* src, float* dst,
+                                                   int to_packed) {
+    const int64_t l = blockIdx.x;
+    if (l >= n || (keep && !keep[l])) return;
+    const size_t s = size_t(slot ? slot[l] : int32_t(l));
+    const size_t d = dst_leaf ? size_t(dst_leaf[l]) : s;
+    const int t = threadIdx.x;
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    int base = 0;
+    for (int w = 0; w < 8; ++w) {
+        const uint64_t mw = m[s * 8 + w];
+        if ((mw >> t) & 1) {
+            const int r = base + __popcll(mw & low);
+            if (to_packed) dst[prefix[l] + r] = src[s * LEAF_VOX + r];
+            else dst[d * LEAF_VOX + r] = src[prefix[l] + r];
+        }
+        base += __popcll(mw);
+    }
+}
+
+// The sign mask records value < 0 for every voxel: refresh its active bits
+// after new active values.
+__global__ void __launch_bounds__(64) k_active_signs(int64_t n, const int32_t* slot, const uint64_t* am,
+                                                    const float* vals, uint64_t* sm) {
+    const int64_t l = blockIdx.x;
+    if (l >= n) return;
+    const size_t s = size_t(slot[l]);
+    const int t = threadIdx.x;
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    __shared__ uint32_t neg[8][2];
+    int base = 0;
+    for (int w = 0; w < 8; ++w) {
+        const uint64_t mw = am[s * 8 + w];
+        const bool on = (mw >> t) & 1;
+        const bool old = (sm[s * 8 + w] >> t) & 1;
+        const bool x = on ? vals[s * LEAF_VOX + base + __popcll(mw & low)] < 0.0f : old;
+        const uint32_t b = __ballot_sync(0xffffffffu, x);
+        if ((t & 31) == 0) neg[w][t >> 5] = b;
+        base += __popcll(mw);
+    }
+    __syncthreads();
+    if (t < 8) sm[s * 8 + t] = uint64_t(neg[t][0]) | (uint64_t(neg[t][1]) << 32);
+}
+
 // Pack leaf values into the slot layout (upload) / unpack (download).
 __global__ void k_unpack(int64_t n, const int32_t* slot, const uint64_t* am, const uint64_t* sm,
                          const float* vals, float gamma, float* dense) {
@@ -508,6 +606,10 @@ struct TapeStep {
     DevArray<float> phin, phi1, phi2;
     float dt = 0.0f, t0 = 0.0f;
     bool backward = false;
+    // how dt was set (its derivative with respect to the velocity): max
+    // |v|^2 at the substep's start and the clock's choices (CflClock)
+    float maxv2 = 0.0f, open_lim = 0.0f;
+    bool limited = false, opened = false, end_lim = false, first = false;
     // tracker part on the dilated (merged) list
     int64_t nm = 0;
     DevArray<uint64_t> keys_m, am3, sm3, pmask, fin;
@@ -584,6 +686,14 @@ struct gbls_handle {
     bool tape_on = false;
     std::vector<std::unique_ptr<TapeStep>> tape;
     TapeStep* tape_cur = nullptr;
+    // steps of discarded tapes, kept with their device arrays: a re-recorded
+    // forward pass of the same size allocates nothing
+    std::vector<std::unique_ptr<TapeStep>> tape_pool;
+    void discard_tape() {
+        for (auto& t : tape) tape_pool.push_back(std::move(t));
+        tape.clear();
+        tape_cur = nullptr;
+    }
     DevArray<int32_t> tape_inv;
     // work enqueued by the advection loop right before the read-back that
     // ends a tracker pass (the next substep's CFL reduction), so that one
@@ -622,6 +732,13 @@ struct gbls_handle {
     // the FP64 kernels); GBLS_PARITY_FP64=1 when the handle is created
     // selects the FP64 kernels instead, for cross-checking.
     bool parity_fp64 = false;
+    // HOST_SAMPLED fields: per-leaf active prefix, active voxel coordinates
+    // and the sampled velocities of the current substep
+    DevArray<int64_t> hs_count, hs_prefix;
+    DevArray<int32_t> hs_ijk;
+    DevArray<float> hs_vel;
+    std::vector<int32_t> hs_ijk_h;
+    std::vector<float> hs_vel_h;
     // CFL maximum of an analytic field at the end time of the last advect
     // call, reused by the next call that starts there with the same field
     // (any other operation on the level set clears it)
@@ -1225,8 +1342,16 @@ void tape_values(gbls_handle& h, int64_t n, int m, int v, DevArray<uint64_t>* am
 }
 
 void tape_begin_substep(gbls_handle& h, float t0, float dt, bool backward) {
-    h.tape.emplace_back(new TapeStep);
+    if (h.tape_pool.empty()) {
+        h.tape.emplace_back(new TapeStep);
+    } else {
+        h.tape.push_back(std::move(h.tape_pool.back()));
+        h.tape_pool.pop_back();
+    }
     TapeStep& st = *h.tape.back();
+    st.nm = 0;
+    st.limited = st.opened = st.end_lim = st.first = false;
+    st.maxv2 = st.open_lim = 0.0f;
     h.tape_cur = &st;
     st.n = h.nleaf;
     st.dt = dt;
@@ -1532,7 +1657,56 @@ FieldParams field_params(const gbls_handle& h, const gbls_field* f, float t) {
     p.domain = d.domain;
     p.period = d.period;
     p.scale = d.scale;
+    if (d.kind == GBLS_FIELD_HOST_SAMPLED) {
+        p.sampled = h.hs_vel.p;
+        p.prefix = h.hs_prefix.p;
+    }
     return p;
+}
+
+int64_t active_count(gbls_handle& h);
+
+// Advect::sampleField for a HOST_SAMPLED field (tools/LevelSetAdvect.h:
+// 426-464): the active voxels' index coordinates in the reference's order go
+// to the caller's sampler, whose velocities are uploaded for the RK stages;
+// returns max |v|^2 over them (Vec3f::lengthSqr in float, math::Max).
+float host_sampled_max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
+    const int64_t L = h.nleaf;
+    const int64_t n = h.nactive >= 0 ? h.nactive : active_count(h);
+    h.nactive = n;
+    h.hs_count.reserve(size_t(std::max<int64_t>(L, 1)), h.stream);
+    h.hs_prefix.reserve(size_t(std::max<int64_t>(L, 1)), h.stream);
+    h.hs_ijk.reserve(size_t(std::max<int64_t>(3 * n, 1)), h.stream);
+    h.hs_vel.reserve(size_t(std::max<int64_t>(3 * n, 1)), h.stream);
+    h.hs_ijk_h.resize(size_t(3 * n));
+    h.hs_vel_h.assign(size_t(3 * n), 0.0f);
+    if (L > 0) {
+        k_leaf_active<<<blocks_for(L, 256), 256, 0, h.stream>>>(L, h.S(), h.am[h.mc].p, h.hs_count.p);
+        size_t bytes = 0;
+        CU(cub::DeviceScan::ExclusiveSum(nullptr, bytes, h.hs_count.p, h.hs_prefix.p, int(L), h.stream));
+        h.cub_tmp.reserve(bytes, h.stream);
+        bytes = h.cub_tmp.cap;
+        CU(cub::DeviceScan::ExclusiveSum(h.cub_tmp.p, bytes, h.hs_count.p, h.hs_prefix.p, int(L), h.stream));
+        k_active_ijk<<<unsigned(L), 64, 0, h.stream>>>(L, h.K(), h.S(), h.am[h.mc].p, h.hs_prefix.p, h.hs_ijk.p);
+        h.stats.kernel_launches += 3;
+        CU(cudaGetLastError());
+        if (n > 0)
+            CU(cudaMemcpyAsync(h.hs_ijk_h.data(), h.hs_ijk.p, size_t(3 * n) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               h.stream));
+    }
+    h.sync();
+    f->desc.host_sample(f->desc.host_user, n, h.hs_ijk_h.data(), t, h.hs_vel_h.data());
+    float m = 0.0f;
+    for (int64_t i = 0; i < n; ++i) {
+        const float* v = h.hs_vel_h.data() + 3 * i;
+        const float l2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        m = (m < l2) ? l2 : m;  // math::Max
+    }
+    if (n > 0)
+        CU(cudaMemcpyAsync(h.hs_vel.p, h.hs_vel_h.data(), size_t(3 * n) * sizeof(float), cudaMemcpyHostToDevice,
+                           h.stream));
+    h.sync();  // the host copy may be refilled by the next substep's sampler
+    return m;
 }
 
 // max |v|^2 over the active voxels at time t (sampleField, :447-455).
@@ -1588,6 +1762,7 @@ float status_max_speed(const gbls_handle& h) {
 }
 
 float max_speed_sqr(gbls_handle& h, const gbls_field* f, float t) {
+    if (f->desc.kind == GBLS_FIELD_HOST_SAMPLED) return host_sampled_max_speed_sqr(h, f, t);
     if (f->desc.kind == GBLS_FIELD_CONSTANT) {
         const float* c = f->desc.constant;
         return c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
@@ -2198,8 +2373,7 @@ int gbls_upload(gbls_handle* h, const gbls_grid_desc* desc) {
         DeviceGuard g(h->device);
         if (h->ninst != 1) fail(GBLS_ERR_INVALID_ARGUMENT, "batch handles take their level sets at creation");
         h->sync();
-        h->tape.clear();
-        h->tape_cur = nullptr;
+        h->discard_tape();
         try {
             upload(*h, desc, 1);
         } catch (...) {
@@ -2471,8 +2645,8 @@ int gbls_adjoint_record(gbls_handle* h, int enable) {
     return guarded([&] {
         DeviceGuard g(h->device);
         h->sync();
-        h->tape.clear();
-        h->tape_cur = nullptr;
+        h->discard_tape();
+        if (!enable) h->tape_pool.clear();  // releases the tape's device memory
         h->tape_on = enable != 0;
     });
 }
@@ -2492,6 +2666,61 @@ std::vector<int> mask_counts(gbls_handle& h, const DevArray<uint64_t>& m, int64_
     return c;
 }
 }  // namespace
+
+namespace {
+// Leaf-order offsets of packed active values: cnt/pre over n leaves.
+void packed_prefix(gbls_handle& h, int64_t n, const int32_t* slot, const uint64_t* m, const int32_t* keep,
+                   DevArray<int64_t>& cnt, DevArray<int64_t>& pre) {
+    cnt.reserve(size_t(std::max<int64_t>(n, 1)), h.stream);
+    pre.reserve(size_t(std::max<int64_t>(n, 1)), h.stream);
+    if (n <= 0) return;
+    k_mask_count<<<blocks_for(n, 256), 256, 0, h.stream>>>(n, slot, m, keep, cnt.p);
+    size_t bytes = 0;
+    CU(cub::DeviceScan::ExclusiveSum(nullptr, bytes, cnt.p, pre.p, int(n), h.stream));
+    h.cub_tmp.reserve(bytes, h.stream);
+    bytes = h.cub_tmp.cap;
+    CU(cub::DeviceScan::ExclusiveSum(h.cub_tmp.p, bytes, cnt.p, pre.p, int(n), h.stream));
+    h.stats.kernel_launches += 2;
+    CU(cudaGetLastError());
+}
+}  // namespace
+
+int gbls_get_active_values_device(gbls_handle* h, float* out) {
+    touched(h);
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        DevArray<int64_t> cnt, pre;
+        packed_prefix(*h, h->nleaf, h->S(), h->am[h->mc].p, nullptr, cnt, pre);
+        if (h->nleaf > 0)
+            k_packed_move<<<unsigned(h->nleaf), 64, 0, h->stream>>>(h->nleaf, h->S(), nullptr, nullptr,
+                                                                    h->am[h->mc].p, pre.p, h->vals[h->vc].p, out, 1);
+        ++h->stats.kernel_launches;
+        CU(cudaGetLastError());
+        h->sync();
+    });
+}
+
+int gbls_set_active_values_device(gbls_handle* h, const float* in) {
+    touched(h);
+    if (!h || !in) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (h->tape_on && !h->tape.empty()) fail(GBLS_ERR_UNSUPPORTED, "values change under a recorded tape");
+        DevArray<int64_t> cnt, pre;
+        packed_prefix(*h, h->nleaf, h->S(), h->am[h->mc].p, nullptr, cnt, pre);
+        if (h->nleaf > 0) {
+            k_packed_move<<<unsigned(h->nleaf), 64, 0, h->stream>>>(h->nleaf, h->S(), nullptr, nullptr,
+                                                                    h->am[h->mc].p, pre.p, in, h->vals[h->vc].p, 0);
+            k_active_signs<<<unsigned(h->nleaf), 64, 0, h->stream>>>(h->nleaf, h->S(), h->am[h->mc].p,
+                                                                     h->vals[h->vc].p, h->sm[h->mc].p);
+        }
+        h->stats.kernel_launches += 2;
+        h->cfl_cache.valid = false;
+        CU(cudaGetLastError());
+        h->sync();
+    });
+}
 
 int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int64_t* substeps) {
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
@@ -2516,8 +2745,9 @@ int gbls_adjoint_sizes(gbls_handle* h, int64_t* n_initial, int64_t* n_final, int
 // dL/dvelocity on its grid.
 // Reverse sweep over the tape.  dL/dv goes to host memory (zeroed first) or,
 // with vel_on_device, is added into the caller's device array.
+// dl_on_device: dl_final and dl_initial are device arrays (else host).
 static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float* dl_final, float* dl_initial,
-                     float* dl_velocity, bool vel_on_device) {
+                            float* dl_velocity, bool vel_on_device, bool dl_on_device = false) {
     if (!h || !field || !dl_final || !dl_initial) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
         DeviceGuard g(h->device);
@@ -2526,22 +2756,33 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
         cudaStream_t st = h->stream;
         // final list = kept leaves of the last merged list, with masks fin
         TapeStep& last = *h->tape[size_t(S - 1)];
-        std::vector<int32_t> keep(static_cast<size_t>(last.nm));
-        if (last.nm) last.keep.download(keep.data(), keep.size(), st);
-        const auto finc = mask_counts(*h, last.fin, last.nm);
-        std::vector<float> lam_h;
-        int64_t nf = 0, off = 0;
-        for (int64_t i = 0; i < last.nm; ++i) if (keep[size_t(i)]) ++nf;
-        lam_h.assign(size_t(std::max<int64_t>(nf, 1)) * LEAF_VOX, 0.0f);
-        int64_t j = 0;
-        for (int64_t i = 0; i < last.nm; ++i) {
-            if (!keep[size_t(i)]) continue;
-            for (int r = 0; r < finc[size_t(i)]; ++r) lam_h[size_t(j) * LEAF_VOX + r] = dl_final[off + r];
-            off += finc[size_t(i)];
-            ++j;
+        DevArray<float> lam_next, lam4, lam3, lamA, lp2, lp1, lpn, dvel, part, halo;
+        DevArray<int64_t> pcnt, ppre;
+        if (dl_on_device) {
+            lam_next.reserve(size_t(std::max<int64_t>(last.nm, 1)) * LEAF_VOX, st);
+            packed_prefix(*h, last.nm, nullptr, last.fin.p, last.keep.p, pcnt, ppre);
+            if (last.nm > 0)
+                k_packed_move<<<unsigned(last.nm), 64, 0, st>>>(last.nm, nullptr, last.keep.p, last.idx.p, last.fin.p,
+                                                                ppre.p, dl_final, lam_next.p, 0);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+        } else {
+            std::vector<int32_t> keep(static_cast<size_t>(last.nm));
+            if (last.nm) last.keep.download(keep.data(), keep.size(), st);
+            const auto finc = mask_counts(*h, last.fin, last.nm);
+            std::vector<float> lam_h;
+            int64_t nf = 0, off = 0;
+            for (int64_t i = 0; i < last.nm; ++i) if (keep[size_t(i)]) ++nf;
+            lam_h.assign(size_t(std::max<int64_t>(nf, 1)) * LEAF_VOX, 0.0f);
+            int64_t j = 0;
+            for (int64_t i = 0; i < last.nm; ++i) {
+                if (!keep[size_t(i)]) continue;
+                for (int r = 0; r < finc[size_t(i)]; ++r) lam_h[size_t(j) * LEAF_VOX + r] = dl_final[off + r];
+                off += finc[size_t(i)];
+                ++j;
+            }
+            lam_next.upload(lam_h.data(), lam_h.size(), st);
         }
-        DevArray<float> lam_next, lam4, lam3, lamA, lp2, lp1, lpn, dvel;
-        lam_next.upload(lam_h.data(), lam_h.size(), st);
         if (field_params(*h, field, 0.0f).xform)
             fail(GBLS_ERR_UNSUPPORTED, "the adjoint differentiates velocity grids aligned with the level set only");
         const bool want_vel = dl_velocity && field->desc.kind == GBLS_FIELD_DENSE;
@@ -2559,6 +2800,18 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
         }
         const float dx = float(h->voxel_size);
         const float mdt = dx * 0.3f, invdx = 1.0f / dx;
+        // the time steps' dependence on the velocity: dL/d(dt) per substep
+        // and the voxel holding each substep's maximum |v|^2
+        DevArray<double> dt_part, gdt;
+        DevArray<float> mbar_d;
+        DevArray<unsigned long long> argkey;
+        DevArray<int64_t> argcell;
+        if (want_vel) {
+            gdt.reserve(size_t(S), st);
+            argkey.reserve(size_t(S), st);
+            argcell.reserve(size_t(S), st);
+            CU(cudaMemsetAsync(argkey.p, 0xff, size_t(S) * sizeof(unsigned long long), st));
+        }
         for (int s = S - 1; s >= 0; --s) {
             TapeStep& tp = *h->tape[size_t(s)];
             const size_t nm = size_t(std::max<int64_t>(tp.nm, 1)) * LEAF_VOX, n = size_t(std::max<int64_t>(tp.n, 1)) * LEAF_VOX;
@@ -2567,17 +2820,29 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
             CU(cudaMemsetAsync(lam3.p, 0, nm * 4, st));
             AdjExpandArgs ea{tp.nm, tp.pmask.p, tp.fin.p, tp.keep.p, tp.idx.p, lam_next.p, lam4.p};
             launch_adj_expand(ea, st);
+            const size_t nmax = size_t(std::max<int64_t>(std::max(tp.nm, tp.n), 1));
+            part.reserve(nmax * LEAF_VOX, st);
+            halo.reserve(nmax * 6 * 192, st);
             AdjNormArgs na{};
             na.nleaf = tp.nm;
             na.nbr = tp.nbr_m.p;
             na.src = Layout{tp.am3.p, tp.sm3.p, tp.phi3.p};
             na.pmask = tp.pmask.p;
             na.lam4 = lam4.p;
-            na.lam3 = lam3.p;
+            na.part = part.p;
+            na.halo = halo.p;
             na.gamma = tp.gamma;
             na.mdt = mdt;
             na.invdx = invdx;
             launch_adj_norm(na, st);
+            AdjCombineArgs ca{};
+            ca.nleaf = tp.nm;
+            ca.nbr = tp.nbr_m.p;
+            ca.am = tp.am3.p;
+            ca.part = part.p;
+            ca.halo = halo.p;
+            ca.lam = lam3.p;
+            launch_adj_combine(ca, st);
             lamA.reserve(n, st);
             AdjMapArgs ma{tp.n, tp.keys.p, tp.am.p, tp.keys_m.p, tp.nm, lam3.p, lamA.p};
             launch_adj_map(ma, st);
@@ -2599,34 +2864,109 @@ static int adjoint_backward(gbls_handle* h, const gbls_field* field, const float
             ra.field = field_params(*h, field, tp.t0);
             ra.field.tab = nullptr;  // direct evaluation in the adjoint
             ra.dvel = dv;
-            // stage 3: phi3 = 1/3 phin + 2/3 (phi2 - dt v.grad phi2)
-            ra.src = Layout{tp.am.p, tp.sm.p, tp.phi2.p};
-            ra.lam_out = lamA.p; ra.lam_in = lp2.p; ra.lam_phin = lpn.p;
-            ra.alpha = 1.0f / 3.0f; ra.beta = 1.0f - 1.0f / 3.0f;
-            launch_adj_rk(ra, st);
-            // stage 2: phi2 = 3/4 phin + 1/4 (phi1 - dt v.grad phi1)
-            ra.src = Layout{tp.am.p, tp.sm.p, tp.phi1.p};
-            ra.lam_out = lp2.p; ra.lam_in = lp1.p; ra.lam_phin = lpn.p;
-            ra.alpha = 3.0f / 4.0f; ra.beta = 1.0f - 3.0f / 4.0f;
-            launch_adj_rk(ra, st);
-            // stage 1: phi1 = phin - dt v.grad phin
-            ra.src = Layout{tp.am.p, tp.sm.p, tp.phin.p};
-            ra.lam_out = lp1.p; ra.lam_in = lpn.p; ra.lam_phin = lpn.p;
-            ra.alpha = 0.0f; ra.beta = 1.0f;
-            launch_adj_rk(ra, st);
+            if (want_vel) {
+                dt_part.reserve(size_t(std::max<int64_t>(tp.n, 1)), st);
+                CU(cudaMemsetAsync(dt_part.p, 0, size_t(std::max<int64_t>(tp.n, 1)) * sizeof(double), st));
+                ra.dt_part = dt_part.p;
+            }
+            ra.part = part.p;
+            ra.halo = halo.p;
+            AdjCombineArgs rc{};
+            rc.nleaf = tp.n;
+            rc.nbr = tp.nbr.p;
+            rc.am = tp.am.p;
+            rc.part = part.p;
+            rc.halo = halo.p;
+            auto stage = [&](const float* phi, float* lam_out, float* lam_in, float alpha) {
+                ra.src = Layout{tp.am.p, tp.sm.p, phi};
+                ra.lam_out = lam_out;
+                ra.alpha = alpha;
+                ra.beta = 1.0f - alpha;
+                launch_adj_rk(ra, st);
+                rc.lam = lam_in;
+                rc.lam_out = lam_out;
+                rc.lam_phin = lpn.p;
+                rc.alpha = alpha;
+                launch_adj_combine(rc, st);
+            };
+            stage(tp.phi2.p, lamA.p, lp2.p, 1.0f / 3.0f);  // phi3 = 1/3 phin + 2/3 (phi2 - dt v.grad phi2)
+            stage(tp.phi1.p, lp2.p, lp1.p, 3.0f / 4.0f);   // phi2 = 3/4 phin + 1/4 (phi1 - dt v.grad phi1)
+            stage(tp.phin.p, lp1.p, lpn.p, 0.0f);          // phi1 = phin - dt v.grad phin
+            if (want_vel) {
+                launch_adj_dt_reduce(dt_part.p, tp.n, gdt.p + s, st);
+                AdjArgmaxArgs aa{};
+                aa.nleaf = tp.n;
+                aa.keys = tp.keys.p;
+                aa.am = tp.am.p;
+                aa.field = ra.field;
+                aa.t0 = tp.t0;
+                aa.maxv2 = tp.maxv2;
+                aa.argkey = argkey.p + s;
+                aa.argcell = argcell.p + s;
+                launch_adj_argmax(aa, st);
+                h->stats.kernel_launches += 3;
+            }
             CU(cudaGetLastError());
-            h->stats.kernel_launches += 6;
+            h->stats.kernel_launches += 10;
             std::swap(lam_next.p, lpn.p);
             std::swap(lam_next.cap, lpn.cap);
         }
+        if (want_vel) {
+            // reverse sweep of the substep clock (CflClock): tau_{k+1} =
+            // tau_k + sgn dt_k; dt_k = CFL_ref dx / sqrt(m_k) when limited,
+            // else sgn (E - tau_k) with E the interval's end, E = tau_o +
+            // sgn lim_o (lim_o = cfl dx / sqrt(m_o)) for an interval opened
+            // at substep o under an imposed CFL number, else t1 (fixed); the
+            // first substep of a call starts at the caller's t0 (fixed).
+            std::vector<double> G(static_cast<size_t>(S));
+            gdt.download(G.data(), G.size(), st);
+            h->sync();
+            std::vector<float> mbar(static_cast<size_t>(S), 0.0f);
+            double tb = 0.0, Eb = 0.0;
+            for (int k = S - 1; k >= 0; --k) {
+                const TapeStep& tk = *h->tape[size_t(k)];
+                const double sg = tk.backward ? -1.0 : 1.0, m = double(tk.maxv2);
+                const double dtb = G[size_t(k)] + sg * tb;
+                double mb = 0.0;
+                if (tk.limited) {
+                    mb += dtb * (-double(tk.dt) / (2.0 * m));
+                } else {
+                    Eb += sg * dtb;
+                    tb -= sg * dtb;
+                }
+                if (tk.opened) {
+                    if (tk.end_lim) {
+                        tb += Eb;
+                        mb += sg * Eb * (-double(tk.open_lim) / (2.0 * m));
+                    }
+                    Eb = 0.0;
+                }
+                if (tk.first) tb = 0.0;
+                mbar[size_t(k)] = float(mb);
+            }
+            mbar_d.upload(mbar.data(), mbar.size(), st);
+            launch_adj_dt_scatter(S, argcell.p, mbar_d.p, field->dense.p, dv, st);
+            CU(cudaGetLastError());
+            h->stats.kernel_launches += 1;
+        }
         // initial list: the first step's list and masks
         TapeStep& first = *h->tape[0];
+        if (dl_on_device) {
+            packed_prefix(*h, first.n, nullptr, first.am.p, nullptr, pcnt, ppre);
+            if (first.n > 0)
+                k_packed_move<<<unsigned(first.n), 64, 0, st>>>(first.n, nullptr, nullptr, nullptr, first.am.p, ppre.p,
+                                                                lam_next.p, dl_initial, 1);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+            h->sync();
+            return;
+        }
         const auto c0 = mask_counts(*h, first.am, first.n);
         std::vector<float> out(size_t(std::max<int64_t>(first.n, 1)) * LEAF_VOX);
         lam_next.download(out.data(), size_t(first.n) * LEAF_VOX, st);
         if (want_vel && !vel_on_device) dvel.download(dl_velocity, nvel, st);
         h->sync();
-        off = 0;
+        int64_t off = 0;
         for (int64_t l = 0; l < first.n; ++l) {
             for (int r = 0; r < c0[size_t(l)]; ++r) dl_initial[off + r] = out[size_t(l) * LEAF_VOX + r];
             off += c0[size_t(l)];
@@ -2638,6 +2978,25 @@ int gbls_adjoint_backward(gbls_handle* h, const gbls_field* field, const float* 
                           float* dl_velocity) {
     touched(h);
     return adjoint_backward(h, field, dl_final, dl_initial, dl_velocity, false);
+}
+
+int gbls_adjoint_backward_device(gbls_handle* h, const gbls_field* field, const float* dl_final,
+                                 float* dl_initial, float* dl_velocity) {
+    touched(h);
+    if (h) {
+        for (const void* p : {static_cast<const void*>(dl_final), static_cast<const void*>(dl_initial),
+                              static_cast<const void*>(dl_velocity)}) {
+            if (!p) continue;
+            cudaPointerAttributes at{};
+            if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+                at.device != h->device) {
+                cudaGetLastError();
+                g_last_error = "gbls_adjoint_backward_device takes device memory of the handle's device";
+                return GBLS_ERR_INVALID_ARGUMENT;
+            }
+        }
+    }
+    return adjoint_backward(h, field, dl_final, dl_initial, dl_velocity, true, true);
 }
 
 int gbls_adjoint_backward_accumulate(gbls_handle* h, const gbls_field* field, const float* dl_final,
@@ -2912,13 +3271,27 @@ int gbls_count_active_noalloc(gbls_handle* h, int64_t* out) {
     });
 }
 
+int gbls_field_set_dense_device(gbls_field* f, const float* values, void* stream) {
+    if (!f || !values) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        if (f->desc.kind != GBLS_FIELD_DENSE) fail(GBLS_ERR_INVALID_ARGUMENT, "not a DENSE field");
+        DeviceGuard g(f->device);
+        const size_t n = size_t(f->desc.dense_dims[0]) * f->desc.dense_dims[1] * f->desc.dense_dims[2] * 3;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        CU(cudaMemcpyAsync(f->dense.p, values, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        CU(cudaStreamSynchronize(s));
+    });
+}
+
 int gbls_field_create(const gbls_field_desc* desc, gbls_field** out) {
     if (!desc || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     *out = nullptr;
     gbls_field* f = nullptr;
     const int rc = guarded([&] {
-        if (desc->kind < GBLS_FIELD_CONSTANT || desc->kind > GBLS_FIELD_ROTATION)
+        if (desc->kind < GBLS_FIELD_CONSTANT || desc->kind > GBLS_FIELD_HOST_SAMPLED)
             fail(GBLS_ERR_VALUE, "unknown field kind");
+        if (desc->kind == GBLS_FIELD_HOST_SAMPLED && !desc->host_sample)
+            fail(GBLS_ERR_INVALID_ARGUMENT, "HOST_SAMPLED field without a sampler");
         DeviceGuard g(g_device);
         f = new gbls_field;
         f->desc = *desc;
@@ -3018,11 +3391,20 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             h->stats.voxel_updates += uint64_t(h->nactive);
             ++h->stats.substeps;
             if (h->tape_on) {
+                if (field->desc.kind == GBLS_FIELD_HOST_SAMPLED)
+                    fail(GBLS_ERR_UNSUPPORTED, "the adjoint records fields the device evaluates, not HOST_SAMPLED");
                 if (temporal != GBLS_TVD_RK3 || h->tr_temporal != GBLS_TVD_RK1 || h->norm_count != 1 ||
                     h->trim != GBLS_TRIM_ALL || spatial != GBLS_HJWENO5_BIAS || h->tr_spatial != GBLS_HJWENO5_BIAS)
                     fail(GBLS_ERR_UNSUPPORTED, "the adjoint records HJWENO5 TVD_RK3 advection with an HJWENO5 "
                                                "TVD_RK1 tracker, normCount 1 and full trimming");
                 tape_begin_substep(*h, t0, dt, !forward);
+                TapeStep& ts = *h->tape.back();
+                ts.maxv2 = maxv2;
+                ts.limited = clock.limited;
+                ts.opened = clock.opened;
+                ts.end_lim = clock.end_lim;
+                ts.open_lim = clock.open_lim;
+                ts.first = count == 0;
             }
             const bool overlap = true;  // dilation (and the next CFL maximum) on the side stream
             if (overlap) {
@@ -3038,7 +3420,8 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
             ++count;
             const bool more = forward ? t0 < t1 : t0 > t1;
             bool queued = false;
-            if ((more || cacheable) && field->desc.kind != GBLS_FIELD_CONSTANT) {
+            if ((more || cacheable) && field->desc.kind != GBLS_FIELD_CONSTANT &&
+                field->desc.kind != GBLS_FIELD_HOST_SAMPLED) {
                 const float tn = t0;
                 if (overlap && !h->batch_run) {
                     // reduce on the side stream while the main stream prunes;

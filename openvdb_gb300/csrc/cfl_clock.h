@@ -28,6 +28,12 @@ struct CflClock {
     float dx = 1.0f;
     bool open = false;  // inside an interval
     float end = 0.0f;   // the interval's end time
+    // how the last substep was set (the adjoint's time-step derivative):
+    // limited: CFL_ref*dx/|v|max (else the rest of the interval); opened:
+    // the substep opened its interval, whose end is t +- open_lim when
+    // end_lim (else t1)
+    bool limited = false, opened = false, end_lim = false;
+    float open_lim = 0.0f;
 
     CflClock(float t0, float t1_, float cfl_, int temporal, float dx_)
         : t1(t1_), forward(t0 < t1_), cfl(cfl_ > 0.0f ? cfl_ : 0.0f), dx(dx_) {
@@ -40,19 +46,27 @@ struct CflClock {
     // approximately zero); 0 ends the loop (an interval that rounds to zero
     // length, where the reference's advect(tau, tau) returns at once).
     float next(float t, float maxv2) {
+        opened = false;
         if (!open) {
             end = t1;
+            end_lim = false;
             if (cfl > 0.0f) {
                 const float lim = cfl * dx / std::sqrt(maxv2);
                 const float span = std::fabs(t1 - t);
-                if (lim < span) end = forward ? t + lim : t - lim;
+                if (lim < span) {
+                    end = forward ? t + lim : t - lim;
+                    end_lim = true;
+                    open_lim = lim;
+                }
             }
             if (end - t == 0.0f) return 0.0f;  // math::isZero(time0 - time1)
             open = true;
+            opened = true;
         }
         const float span = std::fabs(end - t);
         const float lim = cref * dx / std::sqrt(maxv2);
-        return (lim < span) ? lim : span;  // math::Min(dt, CFL*dx/sqrt(maxAbsV))
+        limited = lim < span;
+        return limited ? lim : span;  // math::Min(dt, CFL*dx/sqrt(maxAbsV))
     }
 
     // t advanced by the substep dt; closes the interval when t reaches its end.

@@ -37,7 +37,7 @@ class FieldDesc(C.Structure):
                 ("dense_background", C.c_float * 3), ("domain", C.c_float), ("period", C.c_float),
                 ("scale", C.c_float), ("omega", C.c_float * 3), ("center", C.c_float * 3),
                 ("dense_map_type", C.c_int32), ("dense_voxel_size", C.c_double),
-                ("dense_translation", C.c_double * 3)]
+                ("dense_translation", C.c_double * 3), ("host_sample", C.c_void_p), ("host_user", C.c_void_p)]
 
 
 def deformation(domain=1024.0, period=100.0, scale=1.0):
@@ -87,6 +87,13 @@ def lib():
         L.oport_tracker_op.argtypes = [vp] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
         L.oport_advect.argtypes = [vp, vp] + [C.c_int] * 5 + \
             [C.c_float, C.c_float, C.c_float, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.oport_tangent_lanes.restype = C.c_int
+        L.oport_topology.argtypes = [vp, C.c_int, vp]
+        L.oport_topology_count.argtypes = [vp]
+        L.oport_topology_count.restype = C.c_int64
+        L.oport_set_tangents.argtypes = [vp, C.POINTER(C.c_double)]
+        L.oport_active_tangents.argtypes = [vp, C.POINTER(C.c_double)]
+        L.oport_set_velocity_tangent.argtypes = [vp, C.POINTER(C.c_double), C.c_int64]
         _lib = L
     return _lib
 
@@ -104,13 +111,23 @@ def _check(rc):
         raise RuntimeError("oracle port error %d: %s" % (rc, lib().oport_last_error().decode()))
 
 
+TANGENT = 1  # PortGrid precision: FP32 values with FP64 tangents
+
+
+def tangent_lanes():
+    """Directions one TANGENT run carries."""
+    return int(lib().oport_tangent_lanes())
+
+
 class PortGrid:
     """A level set held by the C++ restatement."""
 
     def __init__(self, host, threads=0, precision=32):
         """precision 32: bit-identical to the reference; 64: the same scheme
-        (same constants, same operations) evaluated in FP64.  `host` is a
-        HostGrid (its gbls_grid_desc is passed by address)."""
+        (same constants, same operations) evaluated in FP64; 1 (TANGENT):
+        the FP32 computation with an FP64 directional derivative carried
+        beside every value (tangent-linear mode).  `host` is a HostGrid
+        (its gbls_grid_desc is passed by address)."""
         self.updates = 0
         if host is None:
             self.h = None
@@ -138,6 +155,47 @@ class PortGrid:
         v = np.ascontiguousarray(values, np.float64)
         assert v.size == self.counts().active_voxel_count
         _check(lib().oport_set_active_values(self.h, v.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def set_tangents(self, d):
+        """TANGENT grids: the derivatives of the active values along the
+        probe directions, d[lane, active] (canonical active order; fewer
+        than tangent_lanes() rows leave the others at zero)."""
+        n = self.counts().active_voxel_count
+        v = np.zeros((tangent_lanes(), n), np.float64)
+        d = np.asarray(d, np.float64).reshape(-1, n)
+        v[:d.shape[0]] = d
+        _check(lib().oport_set_tangents(self.h, v.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def active_tangents(self):
+        """TANGENT grids: (tangent_lanes(), active) derivatives."""
+        out = np.zeros((tangent_lanes(), self.counts().active_voxel_count), np.float64)
+        _check(lib().oport_active_tangents(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def set_velocity_tangent(self, dv):
+        """TANGENT grids: the derivatives of a dense field's values along
+        the probe directions, dv[lane, nx, ny, nz, 3] (None: zero)."""
+        if dv is None:
+            self._vel_tangent = None
+            _check(lib().oport_set_velocity_tangent(self.h, None, 0))
+            return
+        dv = np.asarray(dv, np.float64)
+        v = np.zeros((tangent_lanes(),) + dv.shape[1:], np.float64)
+        v[:dv.shape[0]] = dv
+        self._vel_tangent = v
+        _check(lib().oport_set_velocity_tangent(self.h, v.ctypes.data_as(C.POINTER(C.c_double)), v.size))
+
+    def record_topology(self):
+        """Record the band after every trim from now on."""
+        _check(lib().oport_topology(self.h, 1, None))
+
+    def replay_topology(self, source=None):
+        """Impose the band recorded by `source` (a PortGrid; None: this
+        grid's own record) on every trim from now on, in order."""
+        _check(lib().oport_topology(self.h, 2, source.h if source is not None else None))
+
+    def topology_count(self):
+        return int(lib().oport_topology_count(self.h))
 
     def __del__(self):
         if getattr(self, "h", None) and self.h.value and _lib is not None:

@@ -13,20 +13,10 @@ inline void set_on(uint64_t* m, int n) { m[n >> 6] |= uint64_t(1) << (n & 63); }
 inline void set_off(uint64_t* m, int n) { m[n >> 6] &= ~(uint64_t(1) << (n & 63)); }
 
 // ---- arithmetic of the reference (math/FiniteDifference.h:301-321) -------
-// The C++ expression of math/FiniteDifference.h:301-321 with ValueType Real:
-// for float it mixes float and double exactly as the reference does.
-inline Real weno5(Real v1, Real v2, Real v3, Real v4, Real v5) {
-    const double C = 13.0 / 12.0;
-    const double eps = 1.0e-6 * static_cast<double>(0.01f);
-    auto p2 = [](auto x) { return x * x; };
-    const double A1 = 0.1 / p2(C * p2(v1 - 2 * v2 + v3) + 0.25 * p2(v1 - 4 * v2 + 3.0 * v3) + eps),
-                 A2 = 0.6 / p2(C * p2(v2 - 2 * v3 + v4) + 0.25 * p2(v2 - v4) + eps),
-                 A3 = 0.3 / p2(C * p2(v3 - 2 * v4 + v5) + 0.25 * p2(3.0 * v3 - 4 * v4 + v5) + eps);
-    return static_cast<Real>(static_cast<Real>(A1 * (2.0 * v1 - 7.0 * v2 + 11.0 * v3) +
-                                               A2 * (5.0 * v3 - v2 + 2.0 * v4) +
-                                               A3 * (2.0 * v3 + 5.0 * v4 - v5)) /
-                             (6.0 * (A1 + A2 + A3)));
-}
+// weno5_r: the C++ expression of the reference with ValueType Real (for
+// float it mixes float and double exactly as the reference does); for the
+// tangent-linear Real, the same value plus its FP64 derivative.
+inline Real weno5(Real v1, Real v2, Real v3, Real v4, Real v5) { return weno5_r(v1, v2, v3, v4, v5); }
 // D1<FD_HJWENO5>::difference(xp3, xp2, xp1, xp0, xm1, xm2)
 inline Real hj_fd(Real xp3, Real xp2, Real xp1, Real xp0, Real xm1, Real xm2) {
     return weno5(xp3 - xp2, xp2 - xp1, xp1 - xp0, xp0 - xm1, xm1 - xm2);
@@ -50,6 +40,7 @@ struct Grid {
     std::map<uint64_t, std::vector<uint64_t>> upper; // upper key -> 512 sign words
     std::map<uint64_t, uint8_t> root;                // upper key -> tile sign
     Pool pool;
+    TopoTape* topo = nullptr;                        // trim record / replay (tests)
 
     ~Grid() { for (Leaf* l : leaves) delete l; }
 
@@ -169,6 +160,23 @@ struct Field {
             out[c] = lerp(a0, a1, uvw[0]);
         }
     }
+    // Tangent run: derivatives of the aligned dense velocity values along
+    // the probe directions ([kLanes][nx][ny][nz][3], empty when the velocity
+    // is held fixed); out[component][lane].
+    std::vector<double> dense_tangent;
+    void eval_tangent(int i, int j, int k, double out[3][kLanes]) const {
+        for (int c = 0; c < 3; ++c)
+            for (int q = 0; q < kLanes; ++q) out[c][q] = 0.0;
+        if (dense_tangent.empty() || d.kind != GBLS_FIELD_DENSE || xform) return;
+        const int a = i - d.dense_origin[0], b = j - d.dense_origin[1], c = k - d.dense_origin[2];
+        if (a >= 0 && b >= 0 && c >= 0 && a < d.dense_dims[0] && b < d.dense_dims[1] && c < d.dense_dims[2]) {
+            const size_t lane = size_t(3) * d.dense_dims[0] * d.dense_dims[1] * d.dense_dims[2];
+            const size_t at = 3 * ((size_t(a) * d.dense_dims[1] + b) * d.dense_dims[2] + c);
+            if (dense_tangent.size() < lane * kLanes) return;
+            for (int q = 0; q < kLanes; ++q)
+                for (int e = 0; e < 3; ++e) out[e][q] = dense_tangent[q * lane + at + e];
+        }
+    }
     void eval(int i, int j, int k, float t, float out[3]) const {
         switch (d.kind) {
         case GBLS_FIELD_CONSTANT: out[0] = d.constant[0]; out[1] = d.constant[1]; out[2] = d.constant[2]; break;
@@ -229,8 +237,8 @@ void norm_stage(Grid& g, const Tracker& tr, int phiBuf, int resBuf, Real alpha, 
                     nsq += fmaxr(fminr(dn[2], 0) * fminr(dn[2], 0), fmaxr(up[2], 0) * fmaxr(up[2], 0));
                 }
                 // eval (tools/LevelSetTracker.h:623-643)
-                Real v = phi0 / (std::sqrt(phi0 * phi0 + nsq) + Real(1e-8f));
-                v = phi0 - mDt * v * (std::sqrt(nsq) * mInvDx - Real(1));
+                Real v = phi0 / (sqrt_r(phi0 * phi0 + nsq) + Real(1e-8f));
+                v = phi0 - mDt * v * (sqrt_r(nsq) * mInvDx - Real(1));
                 L->buf[resBuf][n] = hasPhi ? alpha * L->buf[phiBuf][n] + beta * v : v;
             }
         }
@@ -384,6 +392,26 @@ void erode(Grid& g, int iter) {
 void trim(Grid& g, int mode) {
     if (mode == GBLS_TRIM_NONE) return;
     const Real gamma = g.gamma;
+    if (g.topo && g.topo->replay) {
+        // the recorded outcome instead of the thresholds: a voxel the record
+        // drops leaves the band at +-gamma by its sign, every other one stays
+        static const std::array<uint64_t, 8> none{};
+        if (g.topo->pos >= g.topo->masks.size()) {  // more trims than recorded
+            g.topo->overrun = true;
+            return;
+        }
+        const auto& rec = g.topo->masks[g.topo->pos++];
+        for (Leaf* L : g.leaves) {
+            auto it = rec.find(L->key);
+            const auto& m = it == rec.end() ? none : it->second;
+            for (int n = 0; n < 512; ++n) {
+                if (!on(L->mask, n) || ((m[n >> 6] >> (n & 63)) & 1)) continue;
+                set_off(L->mask, n);
+                L->buf[0][n] = L->buf[0][n] < Real(0.0f) ? -gamma : gamma;
+            }
+        }
+        return;
+    }
     g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
         for (size_t i = a; i < b; ++i) {
             Leaf* L = g.leaves[i];
@@ -395,6 +423,15 @@ void trim(Grid& g, int mode) {
             }
         }
     });
+    if (g.topo) {
+        std::unordered_map<uint64_t, std::array<uint64_t, 8>> rec;
+        for (const Leaf* L : g.leaves) {
+            std::array<uint64_t, 8> m;
+            std::memcpy(m.data(), L->mask, 64);
+            rec[L->key] = m;
+        }
+        g.topo->masks.push_back(std::move(rec));
+    }
 }
 
 // pruneLevelSet (tools/Prune.h:266-330, 391-397): bottom-up
@@ -498,7 +535,9 @@ struct Advector {
     int temporal = GBLS_TVD_RK3;
     float cfl = 0.0f;
     std::vector<size_t> offsets;
-    std::vector<float> vel;  // [active][3]
+    using Vel = typename VelOf<Real>::type;  // float, or TL for the tangent run
+    using Time = Real;
+    std::vector<Vel> vel;  // [active][3]
 
     float sample_field(float t0, float t1) {
         if (g.leaves.empty()) return 0.0f;
@@ -509,31 +548,50 @@ struct Advector {
             for (int w = 0; w < 8; ++w) acc += size_t(__builtin_popcountll(g.leaves[i]->mask[w]));
         }
         offsets[g.leaves.size()] = acc;
-        vel.assign(acc * 3, 0.0f);
+        vel.assign(acc * 3, Vel(0.0f));
         const bool fwd = t0 < t1;
         g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
             for (size_t i = a; i < b; ++i) {
                 const Leaf* L = g.leaves[i];
                 int32_t ox, oy, oz;
                 origin_of(L->key, ox, oy, oz);
-                float* v = vel.data() + 3 * offsets[i];
+                Vel* v = vel.data() + 3 * offsets[i];
                 for (int n = 0; n < 512; ++n) {
                     if (!on(L->mask, n)) continue;
                     float o[3];
+                    double od[3][kLanes];
                     field.eval(ox + (n >> 6), oy + ((n >> 3) & 7), oz + (n & 7), t0, o);
-                    v[0] = fwd ? o[0] : -o[0]; v[1] = fwd ? o[1] : -o[1]; v[2] = fwd ? o[2] : -o[2];
+                    field.eval_tangent(ox + (n >> 6), oy + ((n >> 3) & 7), oz + (n & 7), od);
+                    for (int c = 0; c < 3; ++c) {
+                        if (!fwd)
+                            for (int q = 0; q < kLanes; ++q) od[c][q] = -od[c][q];
+                        v[c] = vel_make(fwd ? o[c] : -o[c], od[c], Vel(0.0f));
+                    }
                     v += 3;
                 }
             }
         });
         float maxAbsV = 0;
+        size_t arg = acc;
         for (size_t i = 0; i < acc; ++i) {
-            const float* v = vel.data() + 3 * i;
-            maxAbsV = fmaxr(maxAbsV, v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            const Vel* v = vel.data() + 3 * i;
+            const float x = vel_value(v[0]), y = vel_value(v[1]), z = vel_value(v[2]);
+            const float m = float(fmaxr(Real(maxAbsV), Real(x * x + y * y + z * z)));
+            if (m != maxAbsV) arg = i;  // std::max keeps the first of equal maxima
+            maxAbsV = m;
         }
         if (!(maxAbsV > 1e-5f) && !(maxAbsV < -1e-5f)) return 0.0f;
+        // |v|^2 at the first voxel holding the maximum: its tangent is the
+        // time step's dependence on the velocity (tangent runs)
+        max_v2 = Time(maxAbsV);
+        if (arg < acc) {
+            const Vel* v = vel.data() + 3 * arg;
+            const Time x = Time(v[0]), y = Time(v[1]), z = Time(v[2]);
+            max_v2 = x * x + y * y + z * z;
+        }
         return maxAbsV;
     }
+    Time max_v2 = Time(0.0f);
 
     // The substep length at t0 for max |v|^2 = maxAbsV.  cfl == 0: the
     // reference's sampleField (tools/LevelSetAdvect.h:459-466) over [t0, t1].
@@ -541,26 +599,32 @@ struct Advector {
     // tau' = tau + cfl*dx/|v|max (t1 when that reaches it), each interval
     // running the reference's own loop, so a second short substep appears
     // when tau + (tau' - tau) rounds short of tau'.
+    // Times: float in the FP32 instance (the reference's), double in the
+    // FP64 one, TL in tangent runs, where the substep depends on the
+    // velocity through max |v|^2 and on the earlier substeps of its
+    // interval through the time reached.
     bool open = false;
-    float end = 0.0f;
-    float substep(float t0, float t1, float maxAbsV) {
+    Time end = Time(0.0f);
+    static Time abs_t(Time x) { return x < Time(0.0f) ? -x : x; }
+    Time substep(Time t0, float t1, Time maxAbsV) {
         const float CFLref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) / std::sqrt(3.0f);
         const float dx = float(g.voxel_size);
-        const bool fwd = t0 < t1;
+        const bool fwd = t0 < Time(t1);
         if (!open) {
-            end = t1;
+            end = Time(t1);
             if (cfl > 0.0f) {
-                const float lim = cfl * dx / std::sqrt(maxAbsV);
-                if (lim < std::fabs(t1 - t0)) end = fwd ? t0 + lim : t0 - lim;
+                const Time lim = Time(cfl * dx) / sqrt_r(maxAbsV);
+                if (lim < abs_t(Time(t1) - t0)) end = fwd ? t0 + lim : t0 - lim;
             }
-            if (end - t0 == 0.0f) return 0.0f;
+            if (end - t0 == Time(0.0f)) return Time(0.0f);
             open = true;
         }
-        return fminr(std::fabs(end - t0), CFLref * dx / std::sqrt(maxAbsV));
+        const Time a = abs_t(end - t0), b = Time(CFLref * dx) / sqrt_r(maxAbsV);
+        return b < a ? b : a;  // math::Min
     }
 
     // euler<N,D>(dt, phiBuffer, resultBuffer)
-    void euler(float dt, int phiBuf, int resBuf, Real alpha, bool hasPhi) {
+    void euler(Time dt, int phiBuf, int resBuf, Real alpha, bool hasPhi) {
         const double invdx = 1.0 / g.voxel_size;
         const Real beta = Real(1) - alpha;
         g.pool.run(g.leaves.size(), [&](size_t a, size_t b) {
@@ -568,7 +632,7 @@ struct Advector {
             for (size_t i = a; i < b; ++i) {
                 Leaf* L = g.leaves[i];
                 gather(g, L, 0, t);
-                const float* v = vel.data() + 3 * offsets[i];
+                const Vel* v = vel.data() + 3 * offsets[i];
                 for (int n = 0; n < 512; ++n) {
                     if (!on(L->mask, n)) continue;
                     const int x = n >> 6, y = (n >> 3) & 7, z = n & 7;
@@ -580,7 +644,7 @@ struct Advector {
                     const Real gz = v[2] < 0 ? hj_fd(S(0, 0, 3), S(0, 0, 2), S(0, 0, 1), S(0, 0, 0), S(0, 0, -1), S(0, 0, -2))
                                               : hj_bd(S(0, 0, -3), S(0, 0, -2), S(0, 0, -1), S(0, 0, 0), S(0, 0, 1), S(0, 0, 2));
                     // Vec3d -> applyIJT (x 1/dx in double) -> Vec3f
-                    const Real g0 = Real(double(gx) * invdx), g1 = Real(double(gy) * invdx), g2 = Real(double(gz) * invdx);
+                    const Real g0 = ijt_r(gx, invdx), g1 = ijt_r(gy, invdx), g2 = ijt_r(gz, invdx);
                     const Real av = S(0, 0, 0) - Real(dt) * (Real(v[0]) * g0 + Real(v[1]) * g1 + Real(v[2]) * g2);
                     L->buf[resBuf][n] = hasPhi ? alpha * L->buf[phiBuf][n] + beta * av : av;
                     v += 3;
@@ -594,13 +658,14 @@ struct Advector {
         if (t0 - t1 == 0.0f) return 0;
         const bool fwd = t0 < t1;
         open = false;
-        while (fwd ? t0 < t1 : t0 > t1) {
+        Time t = Time(t0);
+        while (fwd ? t < Time(t1) : t > Time(t1)) {
             if (interrupted && interrupted()) break;
             copy_aux(g, temporal == GBLS_TVD_RK3 ? 2 : 1);
-            const float maxAbsV = sample_field(t0, t1);
+            const float maxAbsV = sample_field(float(t), t1);
             if (maxAbsV == 0.0f) break;
-            const float dt = substep(t0, t1, maxAbsV);
-            if (dt == 0.0f) break;
+            const Time dt = substep(t, t1, max_v2);
+            if (dt == Time(0.0f)) break;
             if (updates) *updates += offsets.back();
             if (temporal == GBLS_TVD_RK1) {
                 euler(dt, 0, 1, Real(0), false); swap_buf(g, 1);
@@ -612,8 +677,8 @@ struct Advector {
                 euler(dt, 1, 2, Real(3.0f / 4.0f), true); swap_buf(g, 2);
                 euler(dt, 1, 2, Real(1.0f / 3.0f), true); swap_buf(g, 2);
             }
-            t0 += fwd ? dt : -dt;
-            if (!(fwd ? t0 < end : t0 > end)) open = false;
+            t += fwd ? dt : -dt;
+            if (!(fwd ? t < end : t > end)) open = false;
             ++count;
             track(g, tr);
         }
