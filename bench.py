@@ -252,6 +252,24 @@ def run_gb300(args):
             if len(f) == 2 and f[0] == dominant + "_" + args.mode:
                 traffic = int(f[1])
 
+    # FP32-pipe roof of the dominant kernel: FP32 thread instructions per
+    # voxel-stage from one ncu capture (profiles/fp32_ops.txt: "<kernel>_<mode>
+    # <count>" per line) times the voxel-stages per second it sustained here,
+    # against 152 SMs x 128 FP32 lanes x the SM clock sampled under load
+    roof32 = None
+    fp = os.path.join(HERE, "profiles", "fp32_ops.txt")
+    if os.path.exists(fp) and clk and clk.get("sm_mhz"):
+        kms = st["rk_ms"] if dominant == "rk_stage" else st["norm_ms"]
+        stages = 3 * st["voxel_updates"] if dominant == "rk_stage" else st["dilated_voxels"]
+        for line in open(fp):
+            f = line.split()
+            if len(f) == 2 and f[0] == dominant + "_" + args.mode and kms > 0:
+                ach = float(f[1]) * stages / (kms / 1e3) / 1e9
+                pk = 152 * 128 * clk["sm_mhz"] * 1e6 / 1e9
+                roof32 = {"bound": "fp32", "kernel": dominant, "achieved": ach, "peak": pk,
+                          "unit": "G thread-inst/s", "frac": ach / pk,
+                          "inst_per_voxel_stage": float(f[1]), "peak_source": "152 SMs x 128 lanes x sampled SM clock"}
+
     # end to end through the host-facing API: upload, advect one time unit, download
     e2e = None
     if args.e2e_steps > 0:
@@ -310,12 +328,58 @@ def run_gb300(args):
                      "rk_stage_gbs": rk_gbs, "normalize_gbs": norm_gbs,
                      "rk_stage_ms": st["rk_ms"], "normalize_ms": st["norm_ms"],
                      "step_ms_total": 1e3 * total},
+        "roofline_fp32": roof32,
         "e2e": e2e,
         "gpu_launches": int(st["kernel_launches"]),
         "clocks": clk,
         "cpu_baseline": cpu_baseline(args) if args.cpu_baseline else None,
     }
+    if args.extras:
+        out["adjoint"] = adjoint_cost(mode, args.mode)
+        out["batched"] = batch_measure(args, steps=3, warmup=3, cpu=False)
     print(json.dumps(out))
+
+
+def adjoint_cost(mode, mode_name, reps=3):
+    """The 128^3 adjoint configuration (20 unit steps of RK3-HJWENO5, dense
+    128^3 x 3 velocity): plain forward, recorded forward and reverse sweep of
+    the device-resident tape, each timed with CUDA events on the stream the
+    tape runs on (best of `reps`); cost_ratio = (recorded forward + adjoint) /
+    plain forward."""
+    import torch
+    from openvdb_gb300 import fixtures
+    from openvdb_gb300.adjoint import DeviceTape
+    template, vel, target, times = fixtures.adjoint_128()
+    tape = DeviceTape(template, vel.shape, mode=mode)
+    phi0 = torch.tensor(template.active_values(), device="cuda")
+    v = torch.tensor(vel, device="cuda")
+    phiT = tape.forward(phi0, v, times, record=True)  # warm-up; the loss gradient at its end
+    coords = tape.dev.to_host().active_coords()
+    dl = (2.0 * (phiT - torch.tensor(target(coords), dtype=torch.float32, device="cuda"))).contiguous()
+    tape.backward(dl)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    best = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        tape.forward(phi0, v, times, record=False)
+        ev[1].record(stream)
+        ev[2].record(stream)
+        tape.forward(phi0, v, times, record=True)
+        ev[3].record(stream)
+        tape.backward(dl)
+        ev[4].record(stream)
+        ev[4].synchronize()
+        r = (ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3]), ev[3].elapsed_time(ev[4]))
+        if best is None or sum(r[1:]) / r[0] < sum(best[1:]) / best[0]:
+            best = r
+    fwd, rec, adj = best
+    return {"workload": "adjoint 128^3: sphere r=40 -> 5%-perturbed sphere r=44, smoothed-noise velocity "
+                        "(sigma 4, amplitude 1), 20 unit steps, RK3-HJWENO5, tracker RK1",
+            "mode": mode_name, "forward_ms": fwd, "recorded_forward_ms": rec, "adjoint_ms": adj,
+            "cost_ratio": (rec + adj) / fwd, "substeps": int(sum(tape.substeps)),
+            "timing": "CUDA events on the tape's stream, best of %d" % reps}
 
 
 BATCH_WORKLOAD = {"workload": "512 seeded instances (50/50 sphere/torus, R log-uniform [8,128], tube ratio "
@@ -325,17 +389,14 @@ BATCH_WORKLOAD = {"workload": "512 seeded instances (50/50 sphere/torus, R log-u
                   "l2": "flushed between steps (256 MiB write)"}
 
 
-def run_batch(args):
+def batch_measure(args, steps, warmup, cpu=True):
     """The batched configuration: every instance advanced by one time unit per
-    step, each with its own CFL substeps, in one gbls_batch_advect call."""
+    step, each with its own CFL substeps, in one gbls_batch_advect call.
+    Returns the line's fields."""
     import torch
-    import __graft_entry__
-    __graft_entry__.build()
     from openvdb_gb300 import FAST, PARITY, fixtures
     from openvdb_gb300.levelset import DeviceBatch
 
-    torch.cuda.init()
-    torch.cuda.set_device(0)
     t_build = time.perf_counter()
     specs, fields = fixtures.batch_instances(n=512, seed=7)
     grids = [fixtures.build_instance(sp) for sp in specs]
@@ -347,7 +408,7 @@ def run_batch(args):
     b.set_stream(stream.cuda_stream)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     t = 0.0
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.advect(fields, t, t + 1.0, cfl=args.cfl)
         t += 1.0
     torch.cuda.synchronize()
@@ -356,7 +417,7 @@ def run_batch(args):
     clocks = ClockSampler(0)
     clocks.start()
     times, subs = [], []
-    for _ in range(args.steps):
+    for _ in range(steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -381,10 +442,10 @@ def run_batch(args):
     cfg.update({"mode": args.mode, "active_voxels_initial": int(sum(g.active_voxel_count() for g in grids)),
                 "active_voxels_end": int(active), "fixture_build_s": round(t_build, 2),
                 "instance_substeps": int(st["substeps"]), "max_substeps_per_step": int(max(subs)),
-                "t_start": float(t - args.steps)})
+                "t_start": float(t - steps)})
     out = {
-        "metric": METRIC, "value": st["voxel_updates"] / total, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": st["voxel_updates"] / total, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": 1e3 * total / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fixtures)",
         "config": cfg,
         "roofline": {"bound": "hbm", "kernel": "rk_stage", "achieved": rk_gbs, "peak": peak,
@@ -396,11 +457,20 @@ def run_batch(args):
         "clocks": clk,
         "cpu_baseline": None,
     }
-    if args.cpu_baseline:
+    if cpu and args.cpu_baseline:
         from oracle import build_oracle, port
         build_oracle.build()
         out["cpu_baseline"] = port.bench_batch_sample(args.cpu_seconds)
-    print(json.dumps(out))
+    return out
+
+
+def run_batch(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    torch.cuda.init()
+    torch.cuda.set_device(0)
+    print(json.dumps(batch_measure(args, args.steps, args.warmup)))
 
 
 ADJOINT_WORKLOAD = {"workload": "inverse problem: sphere r=160 -> torus R=160 r=48 (y axis) in 512^3, dense "
@@ -534,11 +604,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="fast", choices=["fast", "parity"])
+    ap.add_argument("--mode", default="parity", choices=["fast", "parity"],
+                    help="parity: bit-identical to the reference (default); fast: FP32 WENO5 weights")
     ap.add_argument("--cfl", type=float, default=0.5)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--extras", type=int, default=1,
+                    help="add the 128^3 adjoint cost ratio and the batched 512-instance figures to the line")
     ap.add_argument("--workload", default="sphere64", choices=["sphere64", "batch512", "adjoint512"],
                     help="sphere64: the headline 64-sphere line; batch512: the batched configuration; "
                          "adjoint512: the checkpointed inverse problem (--steps = iterations)")

@@ -10,16 +10,19 @@ namespace gbls {
 
 namespace {
 
-// Gradient of Shu's WENO5 (the FastArith formula: weights scaled by
-// d1^2 d2^2 d3^2) by reverse-mode differentiation, arranged so that FP32
-// keeps it accurate to a few ulps where the data are smooth.  Two things
-// lose it otherwise: the smoothness indicators are third differences of the
-// level set, which the differences of first differences D_k cancel to 1e-3
-// of |D| on a radius-40 sphere, and the weight adjoints (p_k - 6W)/(6S)
-// cancel p_k against the weighted mean.  So the caller passes E_a =
-// v_{a+1} - v_a (second differences of the line, from error-free first
-// differences) and every indicator and p_k - p_j is a short combination of
-// them, and A_k-bar = sum_j A_j (p_k - p_j) / (6 S^2).
+// Gradient of Shu's WENO5 by reverse-mode differentiation, arranged so that
+// FP32 keeps it accurate to a few ulps where the data are smooth.  Three
+// things lose it otherwise: the smoothness indicators d_k are third
+// differences of the level set, which differences of first differences D_k
+// cancel to 1e-3 of |D| on a radius-40 sphere; the weight adjoints
+// (p_k - 6W)/(6S) cancel p_k against the weighted mean; and unnormalised
+// weights (gamma_k / d_k^2 products) overflow on flat lines.  So the caller
+// passes E_a = v_{a+1} - v_a (second differences of the line, from
+// error-free first differences), every indicator and every p_k - p_j is a
+// short combination of them, and with the normalised weights w_k the
+// adjoints are
+//   dW/dp_k = w_k / 6,
+//   dW/dd_k = 2 (sum_{j != k} w_j B_j) / d_k,  B_j = sum_i w_i (p_j - p_i) / 6.
 // v1..v5: the operands (for the linear part p_k); E[0..3] = E_1..E_4.
 __device__ __forceinline__ float weno5_grad(float v1, float v2, float v3, float v4, float v5, const float E[4],
                                             float g[5]) {
@@ -34,24 +37,20 @@ __device__ __forceinline__ float weno5_grad(float v1, float v2, float v3, float 
     const float d1 = C * t1 * t1 + 0.25f * u1 * u1 + eps;
     const float d2 = C * t2 * t2 + 0.25f * u2 * u2 + eps;
     const float d3 = C * t3 * t3 + 0.25f * u3 * u3 + eps;
-    const float q1 = d1 * d1, q2 = d2 * d2, q3 = d3 * d3;
-    const float A1 = 0.1f * (q2 * q3), A2 = 0.6f * (q1 * q3), A3 = 0.3f * (q1 * q2);
+    const float a1 = 0.1f / (d1 * d1), a2 = 0.6f / (d2 * d2), a3 = 0.3f / (d3 * d3);
+    const float rs = 1.0f / (a1 + a2 + a3);
+    const float w1 = a1 * rs, w2 = a2 * rs, w3 = a3 * rs;
     const float p1 = 2.0f * v1 - 7.0f * v2 + 11.0f * v3;
     const float p2 = 5.0f * v3 - v2 + 2.0f * v4;
     const float p3 = 2.0f * v3 + 5.0f * v4 - v5;
-    const float S = A1 + A2 + A3;
-    const float W = (A1 * p1 + A2 * p2 + A3 * p3) / (6.0f * S);
-    const float Nb = 1.0f / (6.0f * S);
-    const float NbS = Nb / S;
-    const float A1b = (A2 * p12 + A3 * p13) * NbS;
-    const float A2b = (A3 * p23 - A1 * p12) * NbS;
-    const float A3b = -(A1 * p13 + A2 * p23) * NbS;
-    const float p1b = Nb * A1, p2b = Nb * A2, p3b = Nb * A3;
-    // A1 = 0.1 q2 q3 etc. with q_k = d_k^2
-    const float q1b = A2b * 0.6f * q3 + A3b * 0.3f * q2;
-    const float q2b = A1b * 0.1f * q3 + A3b * 0.3f * q1;
-    const float q3b = A1b * 0.1f * q2 + A2b * 0.6f * q1;
-    const float d1b = q1b * 2.0f * d1, d2b = q2b * 2.0f * d2, d3b = q3b * 2.0f * d3;
+    const float W = (w1 * p1 + w2 * p2 + w3 * p3) * (1.0f / 6.0f);
+    const float B1 = (w2 * p12 + w3 * p13) * (1.0f / 6.0f);
+    const float B2 = (w3 * p23 - w1 * p12) * (1.0f / 6.0f);
+    const float B3 = -(w1 * p13 + w2 * p23) * (1.0f / 6.0f);
+    const float d1b = 2.0f * (B2 * w2 + B3 * w3) / d1;
+    const float d2b = 2.0f * (B1 * w1 + B3 * w3) / d2;
+    const float d3b = 2.0f * (B1 * w1 + B2 * w2) / d3;
+    const float p1b = w1 * (1.0f / 6.0f), p2b = w2 * (1.0f / 6.0f), p3b = w3 * (1.0f / 6.0f);
     const float t1b = d1b * 2.0f * C * t1, u1b = d1b * 0.5f * u1;
     const float t2b = d2b * 2.0f * C * t2, u2b = d2b * 0.5f * u2;
     const float t3b = d3b * 2.0f * C * t3, u3b = d3b * 0.5f * u3;

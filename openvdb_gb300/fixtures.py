@@ -105,3 +105,44 @@ def build_instance(spec):
     if kind == "sphere":
         return sphere(R, center)
     return torus(R, max(1.6, R * ratio), center)
+
+
+def smoothed_noise(n, sigma, amplitude, seed):
+    """Seeded Gaussian-smoothed noise velocity on an n^3 grid, shape
+    (n, n, n, 3), float32: standard normal components convolved per axis
+    with a periodic Gaussian of width sigma voxels (truncated at 3 sigma),
+    scaled so that the largest component magnitude is `amplitude`."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    v = rng.standard_normal((n, n, n, 3))
+    r = int(3 * sigma)
+    x = np.arange(-r, r + 1)
+    k = np.exp(-0.5 * (x / sigma) ** 2)
+    k /= k.sum()
+    for ax in range(3):
+        v = np.apply_along_axis(lambda a: np.convolve(np.pad(a, r, mode="wrap"), k, "valid"), ax, v)
+    v *= amplitude / np.abs(v).max()
+    return v.astype(np.float32)
+
+
+def adjoint_128():
+    """The 128^3 adjoint configuration: phi_0 a radius-40 sphere centred in
+    the domain, a seeded 5%-perturbed radius-44 sphere as the target
+    (returned as a function of index coordinates), a smoothed-noise velocity
+    grid (sigma 4 voxels, amplitude 1 voxel per time unit, seed 9) and 20
+    unit steps."""
+    center = np.array([64.0, 64.0, 64.0])
+    rng = np.random.Generator(np.random.PCG64(44))
+    axes = rng.standard_normal((4, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    amps = rng.uniform(-1.0, 1.0, 4)
+    amps /= np.abs(amps).sum()
+
+    def target(coords):
+        c = coords.astype(np.float64) - center
+        r = np.linalg.norm(c, axis=1)
+        nrm = c / np.maximum(r, 1e-9)[:, None]
+        return r - 44.0 * (1.0 + 0.05 * (nrm @ axes.T) @ amps)
+
+    template = sphere(40.0, tuple(center))
+    vel = smoothed_noise(128, 4.0, 1.0, seed=9)
+    return template, vel, target, [float(t) for t in range(21)]

@@ -48,16 +48,8 @@ def box_mask(grid, lo, hi):
 
 def smoothed_noise(n, sigma, amplitude, seed):
     """Seeded Gaussian-smoothed noise velocity on an n^3 grid, shape (n,n,n,3)."""
-    rng = np.random.Generator(np.random.PCG64(seed))
-    v = rng.standard_normal((n, n, n, 3))
-    r = int(3 * sigma)
-    x = np.arange(-r, r + 1)
-    k = np.exp(-0.5 * (x / sigma) ** 2)
-    k /= k.sum()
-    for ax in range(3):
-        v = np.apply_along_axis(lambda a: np.convolve(np.pad(a, r, mode="wrap"), k, "valid"), ax, v)
-    v *= amplitude / np.abs(v).max()
-    return v.astype(np.float32)
+    from openvdb_gb300.fixtures import smoothed_noise as f
+    return f(n, sigma, amplitude, seed)
 
 
 def union8():

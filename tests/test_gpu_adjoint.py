@@ -40,24 +40,11 @@ def small_problem(cfl):
 def config4_problem():
     """phi_0 a radius-40 sphere, the target a seeded 5%-perturbed radius-44
     sphere on a 128^3 domain, a seeded smoothed-noise velocity grid (sigma 4
-    voxels, amplitude 1 voxel per time unit), 20 unit steps of RK3-HJWENO5."""
+    voxels, amplitude 1 voxel per time unit), 20 unit steps of RK3-HJWENO5
+    (openvdb_gb300.fixtures.adjoint_128)."""
     from openvdb_gb300 import fixtures
-    center = np.array([64.0, 64.0, 64.0])
-    rng = np.random.Generator(np.random.PCG64(44))
-    axes = rng.standard_normal((4, 3))
-    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
-    amps = rng.uniform(-1.0, 1.0, 4)
-    amps /= np.abs(amps).sum()
-
-    def target(coords):
-        c = coords.astype(np.float64) - center
-        r = np.linalg.norm(c, axis=1)
-        n = c / np.maximum(r, 1e-9)[:, None]
-        return r - 44.0 * (1.0 + 0.05 * (n @ axes.T) @ amps)
-
-    template = fixtures.sphere(40.0, tuple(center))
-    vel = smoothed_noise(128, 4.0, 1.0, seed=9)
-    return Problem(template, vel, [float(t) for t in range(21)], target)
+    template, vel, target, times = fixtures.adjoint_128()
+    return Problem(template, vel, times, target)
 
 
 def probes(pb, n_phi, n_vel, seed):
