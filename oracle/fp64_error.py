@@ -26,8 +26,10 @@ import numpy as np
 from oracle import build_oracle, port
 
 
-def _compare(a, b):
-    """(max |a - b| over voxels active in both, active-state differences)."""
+def _compare(a, b, gamma=3.0):
+    """(max |a - b| over voxels active in both, active-state differences,
+    voxels in both, the 99.99th percentile of |a - b| and the number of voxels
+    where it exceeds 1e-5 gamma)."""
     ha, hb = a.to_host(), b.to_host()
     ka = {tuple(o): i for i, o in enumerate(ha.leaf_origins.tolist())}
     common = [(ka[tuple(o)], j) for j, o in enumerate(hb.leaf_origins.tolist()) if tuple(o) in ka]
@@ -37,22 +39,25 @@ def _compare(a, b):
     both = ma & mb
     d = np.abs(ha.leaf_values[ia][both].astype(np.float64) - hb.leaf_values[ib][both].astype(np.float64))
     flips = int((ma ^ mb).sum()) + int(ha.active_voxel_count() - ma.sum()) + int(hb.active_voxel_count() - mb.sum())
-    return (float(d.max()) if d.size else 0.0), flips, int(both.sum())
+    p = float(np.percentile(d, 99.99)) if d.size else 0.0
+    return (float(d.max()) if d.size else 0.0), flips, int(both.sum()), p, int((d > 1e-5 * gamma).sum())
 
 
 def _run(make, field, steps, gamma=3.0):
     grids = [make(32), make(64)]
-    worst, flips, per_step = 0.0, 0, []
+    worst, flips, worst_p, worst_big, per_step = 0.0, 0, 0.0, 0, []
     t = 0.0
     for k in range(steps):
         for g in grids:
             g.advect(field, t, t + 1.0, temporal=port.TVD_RK3, tracker_temporal=port.TVD_RK1, norm_count=1,
                      cfl=0.5)
         t += 1.0
-        d, f, n = _compare(*grids)
-        worst, flips = max(worst, d), max(flips, f)
-        per_step.append({"step": k + 1, "max_dphi_over_gamma": d / gamma, "flips": f, "voxels": n})
-    return {"max_dphi_over_gamma": worst / gamma, "max_flips": flips, "steps": per_step}
+        d, f, n, p, big = _compare(*grids, gamma=gamma)
+        worst, flips, worst_p, worst_big = max(worst, d), max(flips, f), max(worst_p, p), max(worst_big, big)
+        per_step.append({"step": k + 1, "max_dphi_over_gamma": d / gamma, "flips": f, "voxels": n,
+                         "p9999_over_gamma": p / gamma, "voxels_above_1e-5_gamma": big})
+    return {"max_dphi_over_gamma": worst / gamma, "max_flips": flips, "p9999_over_gamma": worst_p / gamma,
+            "max_voxels_above_1e-5_gamma": worst_big, "steps": per_step}
 
 
 def config1():
@@ -75,9 +80,13 @@ def config3(count=64):
         host = fixtures.build_instance(spec)
         fd = field.desc()
         r = _run(lambda p, h=host: port.PortGrid(h, precision=p), fd, 50)
-        out.append({"max_dphi_over_gamma": r["max_dphi_over_gamma"], "max_flips": r["max_flips"]})
+        out.append({k: r[k] for k in ("max_dphi_over_gamma", "max_flips", "p9999_over_gamma",
+                                       "max_voxels_above_1e-5_gamma")})
     return {"instances": count, "max_dphi_over_gamma": max(o["max_dphi_over_gamma"] for o in out),
-            "max_flips": max(o["max_flips"] for o in out), "per_instance": out}
+            "max_flips": max(o["max_flips"] for o in out),
+            "p9999_over_gamma": max(o["p9999_over_gamma"] for o in out),
+            "max_voxels_above_1e-5_gamma": max(o["max_voxels_above_1e-5_gamma"] for o in out),
+            "per_instance": out}
 
 
 def main(argv):
