@@ -209,6 +209,10 @@ def run_gb300(args):
         adv.advect(t, t + 1.0)
         t += 1.0
     torch.cuda.synchronize()
+    # launch shapes chosen on the warmed-up level set (cached per device)
+    from openvdb_gb300 import autotune
+    tuning = autotune.tune(dev.handle, dfield._h, mode, dev.leaf_count())
+    torch.cuda.synchronize()
 
     dev.reset_stats()
     dev.set_profiling(True)
@@ -329,6 +333,7 @@ def run_gb300(args):
                      "rk_stage_ms": st["rk_ms"], "normalize_ms": st["norm_ms"],
                      "step_ms_total": 1e3 * total},
         "roofline_fp32": roof32,
+        "launch_config": tuning,
         "e2e": e2e,
         "gpu_launches": int(st["kernel_launches"]),
         "clocks": clk,
@@ -412,6 +417,12 @@ def batch_measure(args, steps, warmup, cpu=True):
         b.advect(fields, t, t + 1.0, cfl=args.cfl)
         t += 1.0
     torch.cuda.synchronize()
+    from openvdb_gb300 import autotune
+    from openvdb_gb300.levelset import DeviceField
+    timing_field = DeviceField(fields[0])  # launch timing only: any device-evaluated field
+    tuning = autotune.tune(b.handle, timing_field._h, FAST if args.mode == "fast" else PARITY,
+                           sum(b.counts(i).leaf_count for i in range(b.n)))
+    torch.cuda.synchronize()
     b.reset_stats()
     b.set_profiling(True)
     clocks = ClockSampler(0)
@@ -452,6 +463,7 @@ def batch_measure(args, steps, warmup, cpu=True):
                      "peak_source": peak_kind, "unit": "GB/s", "frac": rk_gbs / peak, "traffic": None,
                      "launches": int(st["rk_launches"]), "rk_stage_gbs": rk_gbs, "normalize_gbs": norm_gbs,
                      "rk_stage_ms": st["rk_ms"], "normalize_ms": st["norm_ms"], "step_ms_total": 1e3 * total},
+        "launch_config": tuning,
         "e2e": None,
         "gpu_launches": int(st["kernel_launches"]),
         "clocks": clk,

@@ -84,6 +84,12 @@ class FieldDesc(C.Structure):
     ]
 
 
+class LaunchConfig(C.Structure):
+    """gbls_launch_config: launch shapes of the stencil and CFL kernels."""
+    _fields_ = [("stencil_min_ctas_rk", C.c_int32), ("stencil_min_ctas_norm", C.c_int32),
+                ("cfl_leaves_per_block", C.c_int32)]
+
+
 class HostMap(C.Structure):
     """gbls_host_map: index -> world, x * scale + translation."""
     _fields_ = [("scale", C.c_double), ("translation", C.c_double * 3)]

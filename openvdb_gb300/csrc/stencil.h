@@ -11,13 +11,14 @@ struct CflArgs;
 void launch_rk_parity(const RkArgs& a, cudaStream_t s);
 void launch_norm_parity(const NormArgs& a, cudaStream_t s);
 // The same bits as the parity launchers on the FP32 pipes (ExactArith).
-void launch_rk_exact(const RkArgs& a, cudaStream_t s);
-void launch_norm_exact(const NormArgs& a, cudaStream_t s);
+void launch_rk_exact(const RkArgs& a, cudaStream_t s, int min_ctas = 0);
+void launch_norm_exact(const NormArgs& a, cudaStream_t s, int min_ctas = 0);
 // FP32 arithmetic.
 void launch_rk_fast(const RkArgs& a, cudaStream_t s);
 void launch_norm_fast(const NormArgs& a, cudaStream_t s);
 // Max |v|^2 over active voxels (exact in both modes).
-void launch_cfl(const CflArgs& a, cudaStream_t s);
+// leaves_per_block: 8, 16, 32 (default) or 64 leaves per CTA, 8 threads each
+void launch_cfl(const CflArgs& a, cudaStream_t s, int leaves_per_block = 32);
 // LevelSetMorphing: speed sampling (+ max |s| into *max_bits) and RK stages.
 struct MorphSpeedArgs;
 struct MorphArgs;

@@ -9,14 +9,25 @@
 
 namespace gbls {
 
-void launch_rk_exact(const RkArgs& a, cudaStream_t s) {
+// min_ctas: the register budget as the minimum resident CTAs per SM given to
+// the compiler (0: none, its own heuristic; 1: registers unconstrained; 14 or
+// 16: at most 72 or 64 registers per thread).
+void launch_rk_exact(const RkArgs& a, cudaStream_t s, int min_ctas) {
     if (a.nleaf <= 0) return;
-    rk_stage_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    const unsigned g = unsigned(a.nleaf);
+    if (min_ctas == 16) rk_stage_kernel<ExactArith, 16><<<g, STENCIL_THREADS, 0, s>>>(a);
+    else if (min_ctas == 14) rk_stage_kernel<ExactArith, 14><<<g, STENCIL_THREADS, 0, s>>>(a);
+    else if (min_ctas == 1) rk_stage_kernel<ExactArith, 1><<<g, STENCIL_THREADS, 0, s>>>(a);
+    else rk_stage_kernel<ExactArith><<<g, STENCIL_THREADS, 0, s>>>(a);
 }
 
-void launch_norm_exact(const NormArgs& a, cudaStream_t s) {
+void launch_norm_exact(const NormArgs& a, cudaStream_t s, int min_ctas) {
     if (a.nleaf <= 0) return;
-    normalize_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
+    const unsigned g = unsigned(a.nleaf);
+    if (min_ctas == 16) normalize_kernel<ExactArith, 16><<<g, STENCIL_THREADS, 0, s>>>(a);
+    else if (min_ctas == 14) normalize_kernel<ExactArith, 14><<<g, STENCIL_THREADS, 0, s>>>(a);
+    else if (min_ctas == 1) normalize_kernel<ExactArith, 1><<<g, STENCIL_THREADS, 0, s>>>(a);
+    else normalize_kernel<ExactArith><<<g, STENCIL_THREADS, 0, s>>>(a);
 }
 
 void launch_morph_stage_exact(const MorphArgs& a, cudaStream_t s) {

@@ -35,12 +35,11 @@ void launch_norm_fast(const NormArgs& a, cudaStream_t s) {
 // Vec3f::lengthSqr (math/Vec3.h:212-218) and the field use non-contracting
 // intrinsics in eval_field's order, so the maximum equals the reference's
 // exactly (the maximum of non-negative floats does not depend on order).
-constexpr int CFL_THREADS = 256;
-constexpr int CFL_LEAVES = CFL_THREADS / 8;
-
-__global__ void __launch_bounds__(CFL_THREADS) cfl_max_kernel(const __grid_constant__ CflArgs a) {
+// LEAVES leaves per CTA, 8 threads per leaf (one per mask word)
+template <int LEAVES>
+__global__ void __launch_bounds__(LEAVES * 8) cfl_max_kernel(const __grid_constant__ CflArgs a) {
     const int64_t n = a.nleaf_dev ? min(a.nleaf, int64_t(*a.nleaf_dev)) : a.nleaf;
-    const int64_t l = int64_t(blockIdx.x) * CFL_LEAVES + (threadIdx.x >> 3);
+    const int64_t l = int64_t(blockIdx.x) * LEAVES + (threadIdx.x >> 3);
     const int w = threadIdx.x & 7;
     float m = 0.0f;
     uint32_t inst = 0;
@@ -139,9 +138,17 @@ void launch_morph_stage_fast(const MorphArgs& a, cudaStream_t s) {
     morph_stage_kernel<FastArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
-void launch_cfl(const CflArgs& a, cudaStream_t s) {
+template <int LEAVES>
+void launch_cfl_shape(const CflArgs& a, cudaStream_t s) {
+    cfl_max_kernel<LEAVES><<<unsigned((a.nleaf + LEAVES - 1) / LEAVES), LEAVES * 8, 0, s>>>(a);
+}
+
+void launch_cfl(const CflArgs& a, cudaStream_t s, int leaves_per_block) {
     if (a.nleaf <= 0) return;
-    cfl_max_kernel<<<unsigned((a.nleaf + CFL_LEAVES - 1) / CFL_LEAVES), CFL_THREADS, 0, s>>>(a);
+    if (leaves_per_block == 8) launch_cfl_shape<8>(a, s);
+    else if (leaves_per_block == 16) launch_cfl_shape<16>(a, s);
+    else if (leaves_per_block == 64) launch_cfl_shape<64>(a, s);
+    else launch_cfl_shape<32>(a, s);
     if (!a.inst_run) cfl_reduce_kernel<<<1, 1024, 0, s>>>(a.part, a.nleaf, a.max_bits);
 }
 

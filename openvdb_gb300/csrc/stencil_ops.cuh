@@ -483,8 +483,10 @@ __device__ __forceinline__ int build_list(uint16_t* list, const uint64_t* m) {
 // (tools/LevelSetAdvect.h:543-572): for every active voxel
 //   a = phi_c - dt * (v . GradientBiased<HJWENO5>(phi))
 //   out = N ? alpha*phin + beta*a : a
-template <class A>
-__global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs a) {
+// MINB: the minimum resident CTAs per SM the compiler must allow (register
+// budget; 0 gives none), one of the launch shapes the autotuner chooses among.
+template <class A, int MINB = 0>
+__global__ void __launch_bounds__(STENCIL_THREADS, MINB) rk_stage_kernel(const RkArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ uint16_t list[LEAF_VOX];
@@ -587,8 +589,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS) rk_stage_kernel(const RkArgs 
 // form :661-670 when `carry` keeps the other active voxels), optionally
 // followed by Trim (tools/LevelSetTracker.h:473-506), writing the result in
 // the layout of the surviving active set.  Voxels visited: pmask | active.
-template <class A>
-__global__ void __launch_bounds__(STENCIL_THREADS) normalize_kernel(const NormArgs a) {
+template <class A, int MINB = 0>
+__global__ void __launch_bounds__(STENCIL_THREADS, MINB) normalize_kernel(const NormArgs a) {
     __shared__ float tile[TILE_VOX];
     __shared__ LeafStage st;
     __shared__ float res[LEAF_VOX];
