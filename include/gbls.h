@@ -230,6 +230,30 @@ int gbls_get_tracker_state(gbls_handle* h, int* spatial_scheme, int* temporal_sc
                            int* norm_count, int* grain_size);
 int gbls_set_trimming(gbls_handle* h, int trim_mode);       /* :171 */
 int gbls_set_precision(gbls_handle* h, int mode);           /* GBLS_MODE_* */
+
+/* ---- launch shapes (no reference counterpart) ------------------------------
+ * The choices an autotuner makes per device and workload:
+ *   stencil_min_ctas_rk / _norm  register budget of the PARITY RK-stage and
+ *                                renormalisation kernels as the minimum
+ *                                resident 64-thread CTAs per SM given to the
+ *                                compiler: 0 (none: its heuristic, the
+ *                                default), 1 (unconstrained), 14 or 16;
+ *   cfl_leaves_per_block         leaves per CTA of the CFL maximum (8 threads
+ *                                per leaf): 8, 16, 32 (default) or 64.
+ * Results do not depend on them.  gbls_time_launch_config times one RK stage,
+ * one renormalisation stage and one CFL maximum of the current level set
+ * under a configuration (reps launches after a warm-up, mean ms per launch
+ * in ms[0..2]) and leaves the level set and the handle's configuration as
+ * they were.                                                                 */
+typedef struct gbls_launch_config {
+    int32_t stencil_min_ctas_rk;
+    int32_t stencil_min_ctas_norm;
+    int32_t cfl_leaves_per_block;
+} gbls_launch_config;
+int gbls_set_launch_config(gbls_handle* h, const gbls_launch_config* config);
+int gbls_get_launch_config(gbls_handle* h, gbls_launch_config* config);
+int gbls_time_launch_config(gbls_handle* h, const gbls_field* field, const gbls_launch_config* config,
+                            int reps, float* ms);
 int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr);
 
 /* ---- LevelSetTracker operations ---------------------------------------- */
@@ -311,6 +335,22 @@ int gbls_filter_masked(gbls_handle* h, int filter, int width, float value, gbls_
 int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial_scheme,
                int temporal_scheme, float t0, float t1, float mask_min, float mask_max, int invert_mask,
                uint64_t* substeps);
+
+/* ---- VolumeAdvection (tools/VolumeAdvect.h:76-560) ----------------------------
+ * VolumeAdvection<Vec3fGrid, false>::advect<FloatGrid, Sampler<1, false>>(grid,
+ * time_step) on the handle's grid (a FloatGrid volume such as a fog density:
+ * inactive values +-background, tiles +-background, no active tiles), in
+ * place: the grid is replaced by the advected copy, as the reference returns
+ * it (dilated by ceil(max|v| dt / dx) voxels, sampled backwards along the
+ * characteristics, limited, pruned).  `velocity` is the velocity grid: a
+ * DENSE field (its own transform, or the volume's when dense_map_type is 0;
+ * dense_background outside the box) or a CONSTANT one (a grid holding only
+ * its background).  integrator: 0 SEMI, 1 MID, 2 RK3, 3 RK4, 4 MAC, 5 BFECC
+ * (tools::Scheme::SemiLagrangian); limiter: 0 NO_LIMITER, 1 CLAMP, 2 REVERT
+ * (the reference's default is CLAMP); substeps: setSubSteps (values below 1
+ * count as 1).  max_velocity (may be NULL) receives getMaxVelocity().       */
+int gbls_volume_advect(gbls_handle* h, const gbls_field* velocity, int integrator, int limiter, int substeps,
+                       double time_step, double* max_velocity);
 
 /* ---- adjoint ---------------------------------------------------------------
  * No counterpart in the reference (it has no derivatives).  While recording

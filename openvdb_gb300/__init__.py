@@ -4,4 +4,4 @@ from . import _abi
 from .fields import Field
 from .grid import HostArena, HostGrid, bitwise_equal, compare, digest, summary, topology_equal
 from .levelset import (FAST, PARITY, DeviceBatch, DeviceField, DeviceLevelSet, LevelSetAdvection,
-                       LevelSetFilter, LevelSetMorphing, LevelSetTracker)
+                       LevelSetFilter, LevelSetMorphing, LevelSetTracker, VolumeAdvection)

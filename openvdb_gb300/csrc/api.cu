@@ -27,6 +27,7 @@
 #include "stencil.h"
 #include "stencil_ops.cuh"
 #include "topology.cuh"
+#include "volume.h"
 
 using namespace gbls;
 
@@ -732,6 +733,8 @@ struct gbls_handle {
     // the FP64 kernels); GBLS_PARITY_FP64=1 when the handle is created
     // selects the FP64 kernels instead, for cross-checking.
     bool parity_fp64 = false;
+    // launch shapes (gbls_set_launch_config; the autotuner's choices)
+    int rk_min_ctas = 0, norm_min_ctas = 0, cfl_leaves = 32;
     // HOST_SAMPLED fields: per-leaf active prefix, active voxel coordinates
     // and the sampled velocities of the current substep
     DevArray<int64_t> hs_count, hs_prefix;
@@ -1309,8 +1312,12 @@ void launch_norm(gbls_handle& h, const NormArgs& a0) {
         e1 = h.event();
         CU(cudaEventRecord(e0, h.stream));
     }
-    if (h.mode == GBLS_MODE_PARITY) (h.parity_fp64 ? launch_norm_parity : launch_norm_exact)(a, h.stream);
-    else launch_norm_fast(a, h.stream);
+    if (h.mode == GBLS_MODE_PARITY) {
+        if (h.parity_fp64) launch_norm_parity(a, h.stream);
+        else launch_norm_exact(a, h.stream, h.norm_min_ctas);
+    } else {
+        launch_norm_fast(a, h.stream);
+    }
     CU(cudaGetLastError());
     if (h.profiling) {
         CU(cudaEventRecord(e1, h.stream));
@@ -1726,7 +1733,7 @@ void enqueue_max_speed(gbls_handle& h, const gbls_field* f, float t, const unsig
     a.max_bits = &h.st_d->max_v2_bits;
     h.cfl_part.reserve(size_t(std::max<int64_t>(h.nleaf, 1)), h.stream);
     a.part = h.cfl_part.p;
-    launch_cfl(a, h.stream);
+    launch_cfl(a, h.stream, h.cfl_leaves);
     h.stats.kernel_launches += 2;
     CU(cudaGetLastError());
 }
@@ -1749,7 +1756,7 @@ void enqueue_max_speed_side(gbls_handle& h, const gbls_field* f, float t) {
     h.cfl_part.reserve(size_t(std::max<int64_t>(h.nleaf, 1)), h.side);
     a.part = h.cfl_part.p;
     CU(cudaMemsetAsync(h.cfl_d, 0, sizeof(unsigned int), h.side));
-    launch_cfl(a, h.side);
+    launch_cfl(a, h.side, h.cfl_leaves);
     h.stats.kernel_launches += 2;
     CU(cudaGetLastError());
     CU(cudaEventRecord(h.ev_cfl, h.side));
@@ -1780,8 +1787,12 @@ void rk_stage(gbls_handle& h, const RkArgs& a) {
         e1 = h.event();
         CU(cudaEventRecord(e0, h.stream));
     }
-    if (h.mode == GBLS_MODE_PARITY) (h.parity_fp64 ? launch_rk_parity : launch_rk_exact)(a, h.stream);
-    else launch_rk_fast(a, h.stream);
+    if (h.mode == GBLS_MODE_PARITY) {
+        if (h.parity_fp64) launch_rk_parity(a, h.stream);
+        else launch_rk_exact(a, h.stream, h.rk_min_ctas);
+    } else {
+        launch_rk_fast(a, h.stream);
+    }
     CU(cudaGetLastError());
     // FP32 values of the active voxels: stencil read + result write (+ phi_n read)
     const double bytes = double(h.nactive) * (a.has_phi ? 12.0 : 8.0);
@@ -2459,6 +2470,112 @@ int gbls_set_trimming(gbls_handle* h, int trim_mode) {
     }
     h->trim = trim_mode;
     return GBLS_OK;
+}
+
+// ---- launch shapes ------------------------------------------------------------
+static bool launch_config_ok(const gbls_launch_config* c) {
+    auto ctas = [](int v) { return v == 0 || v == 1 || v == 14 || v == 16; };
+    const int l = c->cfl_leaves_per_block;
+    return ctas(c->stencil_min_ctas_rk) && ctas(c->stencil_min_ctas_norm) && (l == 8 || l == 16 || l == 32 || l == 64);
+}
+
+int gbls_set_launch_config(gbls_handle* h, const gbls_launch_config* c) {
+    if (!h || !c) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (!launch_config_ok(c)) { g_last_error = "launch configuration out of range"; return GBLS_ERR_VALUE; }
+    h->rk_min_ctas = c->stencil_min_ctas_rk;
+    h->norm_min_ctas = c->stencil_min_ctas_norm;
+    h->cfl_leaves = c->cfl_leaves_per_block;
+    return GBLS_OK;
+}
+
+int gbls_get_launch_config(gbls_handle* h, gbls_launch_config* c) {
+    if (!h || !c) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    c->stencil_min_ctas_rk = h->rk_min_ctas;
+    c->stencil_min_ctas_norm = h->norm_min_ctas;
+    c->cfl_leaves_per_block = h->cfl_leaves;
+    return GBLS_OK;
+}
+
+// One RK stage, one renormalisation stage over the active voxels and one CFL
+// maximum of the current level set under configuration c, each launched
+// reps times after one warm-up launch; mean milliseconds per launch in
+// ms[0..2].  The results go to spare buffers: the level set is unchanged.
+int gbls_time_launch_config(gbls_handle* h, const gbls_field* f, const gbls_launch_config* c, int reps,
+                            float* ms) {
+    touched(h);
+    if (!h || !f || !c || !ms) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (!launch_config_ok(c)) { g_last_error = "launch configuration out of range"; return GBLS_ERR_VALUE; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (h->nleaf == 0) fail(GBLS_ERR_INVALID_ARGUMENT, "empty level set");
+        if (f->desc.kind == GBLS_FIELD_HOST_SAMPLED) fail(GBLS_ERR_UNSUPPORTED, "timing takes a device-evaluated field");
+        if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "timing while the adjoint records");
+        const int n = std::max(1, reps);
+        const int rk0 = h->rk_min_ctas, nm0 = h->norm_min_ctas, cl0 = h->cfl_leaves;
+        const bool prof = h->profiling;
+        h->profiling = false;
+        h->rk_min_ctas = c->stencil_min_ctas_rk;
+        h->norm_min_ctas = c->stencil_min_ctas_norm;
+        h->cfl_leaves = c->cfl_leaves_per_block;
+        const int vo = other_of(h->vc, h->vc), mo = other_of(h->mc, h->mc);
+        RkArgs r{};
+        r.spatial = GBLS_HJWENO5_BIAS;
+        r.nleaf = h->nleaf;
+        r.keys = h->K();
+        r.slot = h->S();
+        r.nbr = h->nbr.p;
+        r.dt = 0.25f;
+        r.gamma = h->gamma;
+        r.invdx = 1.0 / h->voxel_size;
+        r.invdx_f = float(1.0 / h->voxel_size);
+        r.field = field_params(*h, f, 0.0f);
+        r.src = h->layout(h->mc, h->vc);
+        r.phin = h->vals[h->vc].p;
+        r.out = h->vals[vo].p;
+        r.beta = 1.0f;
+        NormArgs q{};
+        q.spatial = GBLS_HJWENO5_BIAS;
+        q.nleaf = h->nleaf;
+        q.slot = h->S();
+        q.nbr = h->nbr.p;
+        q.pmask = h->am[h->mc].p;
+        q.gamma = h->gamma;
+        q.mdt = float(h->voxel_size) * 0.3f;
+        q.invdx = float(1.0 / h->voxel_size);
+        q.out_count = h->cnt.p;
+        q.keys = h->K();
+        q.src = h->layout(h->mc, h->vc);
+        q.phi = q.src;
+        q.beta = 1.0f;
+        q.out_vals = h->vals[vo].p;
+        q.out_amask = h->am[mo].p;
+        q.out_smask = h->sm[mo].p;
+        cudaEvent_t e0 = h->event(), e1 = h->event();
+        auto timed = [&](const std::function<void()>& launch) {
+            launch();
+            CU(cudaEventRecord(e0, h->stream));
+            for (int i = 0; i < n; ++i) launch();
+            CU(cudaEventRecord(e1, h->stream));
+            CU(cudaEventSynchronize(e1));
+            float t = 0.0f;
+            CU(cudaEventElapsedTime(&t, e0, e1));
+            return t / float(n);
+        };
+        ms[0] = timed([&] { rk_stage(*h, r); });
+        ms[1] = timed([&] { launch_norm(*h, q); });
+        ms[2] = timed([&] {
+            h->clear_status();
+            enqueue_max_speed(*h, f, 0.0f, nullptr);
+        });
+        h->sync();
+        h->event_pool.push_back(e0);
+        h->event_pool.push_back(e1);
+        h->stats.kernel_launches += uint64_t(3 * (n + 1));
+        h->rk_min_ctas = rk0;
+        h->norm_min_ctas = nm0;
+        h->cfl_leaves = cl0;
+        h->profiling = prof;
+    });
 }
 
 int gbls_set_precision(gbls_handle* h, int mode) {
@@ -3151,7 +3268,7 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
                 a.inst_run = h->inst_run.p;
                 a.inst_t0 = h->inst_t0.p;
                 a.inst_field = h->inst_field.p;
-                launch_cfl(a, h->stream);
+                launch_cfl(a, h->stream, h->cfl_leaves);
                 ++h->stats.kernel_launches;
                 CU(cudaGetLastError());
                 h->inst_max.download(mx.data(), size_t(n), h->stream);
@@ -3578,6 +3695,211 @@ int gbls_filter_masked(gbls_handle* h, int filter, int width, float value, gbls_
 // LevelSetMorphing::advect (tools/LevelSetMorph.h:243-262, Morph::advect
 // :479-510): CFL substeps from t0 towards t1 (forward time only), each with
 // the speed sampled once, the RK stages and a tracker pass.
+// ---- VolumeAdvection (tools/VolumeAdvect.h) ------------------------------------
+namespace {
+VolMap volume_map(const gbls_handle& h) {
+    VolMap m{};
+    m.scale = h.voxel_size;
+    m.inv = 1.0 / h.voxel_size;
+    for (int a = 0; a < 3; ++a) m.t[a] = h.translation[a];
+    return m;
+}
+
+VolGrid live_grid(gbls_handle& h) {
+    VolGrid g{};
+    g.keys = h.K();
+    g.slot = h.S();
+    g.nleaf = h.nleaf;
+    g.amask = h.am[h.mc].p;
+    g.smask = h.sm[h.mc].p;
+    g.vals = h.vals[h.vc].p;
+    g.nodes = h.nodes();
+    g.background = h.gamma;
+    return g;
+}
+
+VolOut live_out(gbls_handle& h) {
+    VolOut o{};
+    o.nleaf = h.nleaf;
+    o.keys = h.K();
+    o.slot = h.S();
+    o.amask = h.am[h.mc].p;
+    return o;
+}
+
+// The grid as it is now, in arrays of its own (leaf-index numbering), so
+// that it can be sampled while the handle's topology changes.
+struct VolSnapshot {
+    DevArray<uint64_t> keys, am, sm, lower_keys, lower_sign, upper_keys, upper_sign, root_keys;
+    DevArray<uint8_t> root_sign;
+    DevArray<float> vals;
+    VolGrid grid{};
+
+    void take(gbls_handle& h) {
+        const int64_t n = h.nleaf;
+        const size_t nn = size_t(std::max<int64_t>(n, 1));
+        keys.reserve(nn, h.stream);
+        am.reserve(nn * 8, h.stream);
+        sm.reserve(nn * 8, h.stream);
+        vals.reserve(nn * LEAF_VOX, h.stream);
+        if (n > 0) CU(cudaMemcpyAsync(keys.p, h.K(), size_t(n) * 8, cudaMemcpyDeviceToDevice, h.stream));
+        launch_tape_gather(n, h.S(), h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, am.p, sm.p, vals.p, h.stream);
+        NodeTables t = h.nodes();
+        auto copy = [&](auto& dst, const auto* src, int64_t count) {
+            dst.reserve(size_t(std::max<int64_t>(count, 1)), h.stream);
+            if (count > 0) CU(cudaMemcpyAsync(dst.p, src, size_t(count) * sizeof(*src), cudaMemcpyDeviceToDevice, h.stream));
+        };
+        copy(lower_keys, t.lower_keys, t.nlower);
+        copy(lower_sign, t.lower_sign, t.nlower * 64);
+        copy(upper_keys, t.upper_keys, t.nupper);
+        copy(upper_sign, t.upper_sign, t.nupper * 512);
+        copy(root_keys, t.root_keys, t.nroot);
+        copy(root_sign, t.root_sign, t.nroot);
+        CU(cudaGetLastError());
+        grid = VolGrid{};
+        grid.keys = keys.p;
+        grid.slot = nullptr;
+        grid.nleaf = n;
+        grid.amask = am.p;
+        grid.smask = sm.p;
+        grid.vals = vals.p;
+        grid.nodes = NodeTables{lower_keys.p, lower_sign.p, upper_keys.p, upper_sign.p, root_keys.p, root_sign.p,
+                                t.nlower, t.nupper, t.nroot};
+        grid.background = h.gamma;
+    }
+};
+}  // namespace
+
+// VolumeAdvection<Vec3fGrid, false>::advect<FloatGrid, Sampler<1, false>>
+// (tools/VolumeAdvect.h:205-222, cook and Advect :270-560) on the handle's
+// grid, in place.  integrator: Scheme::SemiLagrangian (SEMI, MID, RK3, RK4,
+// MAC, BFECC); limiter: Scheme::Limiter (NO_LIMITER, CLAMP, REVERT).
+int gbls_volume_advect(gbls_handle* h, const gbls_field* field, int integrator, int limiter, int substeps,
+                       double time_step, double* max_velocity) {
+    touched(h);
+    if (!h || !field) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (integrator < 0 || integrator > 5) fail(GBLS_ERR_VALUE, "Spatial difference scheme not supported!");
+        if (limiter < 0 || limiter > 2) fail(GBLS_ERR_VALUE, "unknown limiter");
+        if (h->ninst != 1) fail(GBLS_ERR_UNSUPPORTED, "volume advection works on single grids, not batches");
+        if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "the adjoint records level-set advection only");
+        const gbls_field_desc& fd = field->desc;
+        if (fd.kind != GBLS_FIELD_DENSE && fd.kind != GBLS_FIELD_CONSTANT)
+            fail(GBLS_ERR_UNSUPPORTED, "volume advection samples a velocity grid: DENSE or CONSTANT fields");
+        const int steps = std::max(1, substeps);  // setSubSteps clamps to 1
+        const VolMap map = volume_map(*h);
+        VolVelocity vel{};
+        vel.kind = fd.kind == GBLS_FIELD_DENSE ? 1 : 0;
+        for (int c = 0; c < 3; ++c) {
+            vel.constant[c] = fd.constant[c];
+            vel.background[c] = fd.kind == GBLS_FIELD_DENSE ? fd.dense_background[c] : fd.constant[c];
+            vel.origin[c] = fd.dense_origin[c];
+            vel.dims[c] = fd.dense_dims[c];
+        }
+        vel.dense = field->dense.p;
+        if (fd.kind == GBLS_FIELD_DENSE && fd.dense_map_type != 0) {
+            const int mt = fd.dense_map_type - 1;
+            vel.map.scale = mt == GBLS_MAP_TRANSLATION ? 1.0 : fd.dense_voxel_size;
+            vel.map.inv = 1.0 / vel.map.scale;
+            for (int a = 0; a < 3; ++a) vel.map.t[a] = mt == GBLS_MAP_UNIFORM_SCALE ? 0.0 : fd.dense_translation[a];
+        } else {
+            vel.map = map;  // the velocity grid shares the volume's transform
+        }
+        // getMaxVelocity: max |v| over the velocity grid's values and its background
+        auto len = [](const float* v) {
+            const float s = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+            return double(float(std::sqrt(double(s))));
+        };
+        double vmax = len(vel.background);
+        if (vel.kind == 1) {
+            h->clear_status();
+            launch_vol_max_speed(vel.dense, int64_t(vel.dims[0]) * vel.dims[1] * vel.dims[2],
+                                 &h->st_d->max_v2_bits, h->stream);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+            h->read_status();
+            float m;
+            std::memcpy(&m, &h->st_h->max_v2_bits, 4);
+            vmax = std::max(vmax, double(m));
+        }
+        if (max_velocity) *max_velocity = vmax;
+        const double dt = time_step / steps;
+        const int n = int(std::ceil(vmax * std::fabs(dt) / h->voxel_size));  // getMaxDistance
+        const float rdt = float(-dt);  // the method of characteristics backtracks
+        const bool second = integrator == 4 || integrator == 5;
+        const int order = second ? 1 : integrator == 0 ? 1 : integrator == 1 ? 2 : integrator == 2 ? 3 : 4;
+        VolSnapshot snap;
+        DevArray<float> out1;
+        for (int step = 0; step < steps; ++step) {
+            if (h->nleaf == 0) break;
+            snap.take(*h);
+            for (int i = 0; i < n; ++i) {  // dilateActiveValues(tree, n, NN_FACE, EXPAND_TILES)
+                dilate_topology(*h);
+                relayout(*h, h->dmask.p, 0, 0);  // new voxels active with their old values
+            }
+            h->nactive = -1;
+            if (h->nleaf > 0) {
+                VolRkArgs r{};
+                r.out = live_out(*h);
+                r.map = map;
+                r.vel = vel;
+                r.order = order;
+                // forward: out0 = sample of the input along the characteristic
+                r.dst = h->vals[h->vc].p;
+                r.src = snap.grid;
+                r.dt = rdt;
+                launch_vol_rk(r, h->stream);
+                ++h->stats.kernel_launches;
+                if (second) {
+                    out1.reserve(h->vals[h->vc].cap, h->stream);
+                    VolCombineArgs c{};
+                    c.out = r.out;
+                    c.in = snap.grid;
+                    // backward from the output: out1
+                    r.src = live_grid(*h);
+                    r.dst = out1.p;
+                    r.dt = -rdt;
+                    launch_vol_rk(r, h->stream);
+                    c.out0 = h->vals[h->vc].p;
+                    c.out1 = out1.p;
+                    c.op = integrator == 4 ? VOL_COMBINE_MAC : VOL_COMBINE_BFECC;
+                    launch_vol_combine(c, h->stream);
+                    h->stats.kernel_launches += 2;
+                    if (integrator == 5) {  // forward again from the corrected field, then out0 = out1
+                        r.src = live_grid(*h);
+                        r.dst = out1.p;
+                        r.dt = rdt;
+                        launch_vol_rk(r, h->stream);
+                        ++h->stats.kernel_launches;
+                        const size_t bytes = h->vals[h->vc].cap * sizeof(float);
+                        CU(cudaMemcpyAsync(h->vals[h->vc].p, out1.p, bytes, cudaMemcpyDeviceToDevice, h->stream));
+                    }
+                }
+                VolLimitArgs lm{};
+                lm.out = live_out(*h);
+                lm.vals = h->vals[h->vc].p;
+                lm.keep = h->dmask.p;
+                lm.in = snap.grid;
+                lm.map = map;
+                lm.vel = vel;
+                lm.dt = rdt;
+                lm.limiter = limiter;
+                lm.do_limit = second && limiter != 0 ? 1 : 0;  // isLimiterOn
+                lm.background = h->gamma;
+                launch_vol_limit(lm, h->stream);
+                ++h->stats.kernel_launches;
+                CU(cudaGetLastError());
+                relayout(*h, h->dmask.p, 0, 0);  // the kept voxels stay active
+                prune_compact(*h);               // pruneInactive
+            }
+        }
+        h->nactive = -1;
+        h->cfl_cache.valid = false;
+        h->sync();
+    });
+}
+
 int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial, int temporal, float t0,
                float t1, float mask_min, float mask_max, int invert_mask, uint64_t* substeps) {
     touched(h);

@@ -126,6 +126,64 @@ class DeviceLevelSet:
         _call(lib().gbls_set_profiling(self._h, 1 if enable else 0))
 
 
+class VolumeAdvection:
+    """tools::VolumeAdvection<Vec3fGrid> (tools/VolumeAdvect.h:76-262) with the
+    reference's method names, advecting FloatGrid volumes (fog densities)
+    held by a DeviceLevelSet through gbls_volume_advect.  advect(grid, dt)
+    replaces the grid's contents with the advected copy (the reference returns
+    a new grid and leaves its input unchanged)."""
+
+    SEMI, MID, RK3, RK4, MAC, BFECC = range(6)
+    NO_LIMITER, CLAMP, REVERT = range(3)
+
+    def __init__(self, velocity):
+        """`velocity`: a Field (DENSE or CONSTANT) or a DeviceField."""
+        self._field = velocity if isinstance(velocity, DeviceField) else DeviceField(velocity)
+        self._integrator = self.SEMI
+        self._limiter = self.CLAMP
+        self._substeps = 1
+        self._max_velocity = None
+
+    def spatialOrder(self):
+        return 2 if self._integrator in (self.MAC, self.BFECC) else 1
+
+    def temporalOrder(self):
+        return {self.SEMI: 1, self.MID: 2, self.RK3: 3, self.RK4: 4, self.BFECC: 2, self.MAC: 2}[self._integrator]
+
+    def setIntegrator(self, integrator):
+        self._integrator = int(integrator)
+
+    def getIntegrator(self):
+        return self._integrator
+
+    def setLimiter(self, limiter):
+        self._limiter = int(limiter)
+
+    def getLimiter(self):
+        return self._limiter
+
+    def isLimiterOn(self):
+        return self.spatialOrder() > 1 and self._limiter != self.NO_LIMITER
+
+    def setSubSteps(self, substeps):
+        self._substeps = max(1, int(substeps))
+
+    def getSubSteps(self):
+        return self._substeps
+
+    def getMaxVelocity(self):
+        """max |v| over the velocity grid's values and background (known after
+        the first advect call)."""
+        return self._max_velocity
+
+    def advect(self, grid, time_step):
+        m = C.c_double()
+        _call(lib().gbls_volume_advect(grid.handle, self._field._h, self._integrator, self._limiter,
+                                       self._substeps, float(time_step), C.byref(m)))
+        self._max_velocity = m.value
+        return grid
+
+
 class DeviceField:
     """A velocity field uploaded to the GPU (gbls_field)."""
 

@@ -16,6 +16,7 @@
 #include <openvdb/tools/LevelSetSphere.h>
 #include <openvdb/tools/LevelSetTracker.h>
 #include <openvdb/tools/VelocityFields.h>
+#include <openvdb/tools/VolumeAdvect.h>
 
 #include <openvdb/io/GridDescriptor.h>
 
@@ -486,6 +487,27 @@ int vdbref_advect_enright(void* g, int spatial, int temporal, int tspatial, int 
             ? runAdvectCfl(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1, cfl)
             : runAdvect(grid, field, spatial, temporal, tspatial, ttemporal, normCount, t0, t1);
         if (count) *count = n;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(GBLS_ERR_VALUE, e.what());
+    }
+}
+
+// tools::VolumeAdvection<Vec3fGrid, false>::advect<FloatGrid, Sampler<1, false>>
+// (tools/VolumeAdvect.h:205-222): the grid is replaced by the advected copy.
+// The velocity grid comes from the dense descriptor (its own transform, or
+// the volume's); max_velocity receives getMaxVelocity().
+int vdbref_volume_advect(void* g, const gbls_field_desc* f, int integrator, int limiter, int substeps,
+                         double time_step, double* max_velocity) {
+    try {
+        RefGrid* r = static_cast<RefGrid*>(g);
+        Vec3fGrid::Ptr vel = makeVelocityGrid(*f, r->grid->transform());
+        tools::VolumeAdvection<Vec3fGrid, false> adv(*vel);
+        adv.setIntegrator(tools::Scheme::SemiLagrangian(integrator));
+        adv.setLimiter(tools::Scheme::Limiter(limiter));
+        adv.setSubSteps(substeps);
+        if (max_velocity) *max_velocity = adv.getMaxVelocity();
+        r->grid = adv.advect<FloatGrid, tools::Sampler<1, false>>(*r->grid, time_step);
         return 0;
     } catch (const std::exception& e) {
         return fail(GBLS_ERR_VALUE, e.what());

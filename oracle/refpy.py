@@ -45,6 +45,8 @@ def lib():
             [C.c_float] * 3 + [C.POINTER(C.c_uint64)]
         L.vdbref_advect_enright.argtypes = [C.c_void_p] + [C.c_int] * 5 + [C.c_float] * 3 + [C.POINTER(C.c_uint64)]
         L.vdbref_tracker_op.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.POINTER(C.c_int)]
+        L.vdbref_volume_advect.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                           C.POINTER(C.c_double)]
         L.vdbref_set_threads.argtypes = [C.c_int]
         L.vdbref_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float] + [C.c_int] * 4
         L.vdbref_normalize_masked.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p] + [C.c_int] * 4
@@ -179,6 +181,16 @@ class RefGrid:
         _check(lib().vdbref_advect_enright(self.h, spatial, temporal, tracker_spatial, tracker_temporal, norm_count,
                                            t0, t1, cfl, C.byref(n)))
         return n.value
+
+    def volume_advect(self, field, time_step, integrator=0, limiter=1, substeps=1):
+        """tools::VolumeAdvection<Vec3fGrid>::advect<FloatGrid, BoxSampler>
+        (tools/VolumeAdvect.h:205-222) in the dense velocity `field`; the grid
+        becomes the advected copy.  Returns getMaxVelocity()."""
+        fd = field.desc() if hasattr(field, "desc") else field
+        m = C.c_double()
+        _check(lib().vdbref_volume_advect(self.h, C.addressof(fd), integrator, limiter, substeps, time_step,
+                                          C.byref(m)))
+        return m.value
 
     def morph(self, target, t0, t1, mask=None, mask_range=(0.0, 1.0), invert=False,
               spatial=_abi.HJWENO5_BIAS, temporal=_abi.TVD_RK2, tracker_spatial=_abi.HJWENO5_BIAS,

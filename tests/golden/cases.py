@@ -345,3 +345,57 @@ def make_batch():
     from openvdb_gb300 import fixtures
     specs, fields = fixtures.batch_instances(BATCH["n"], BATCH["seed"], BATCH["rmin"], BATCH["rmax"])
     return [fixtures.build_instance(s) for s in specs], fields
+
+
+# VolumeAdvection (tools/VolumeAdvect.h): a FloatGrid volume advected by
+# tools::VolumeAdvection<Vec3fGrid>::advect<FloatGrid, BoxSampler> through the
+# listed ("volume", integrator, limiter, substeps, time_step) calls.
+# integrator: 0 SEMI, 1 MID, 2 RK3, 3 RK4, 4 MAC, 5 BFECC; limiter: 0 none,
+# 1 CLAMP, 2 REVERT.  Volumes: ("fog_shell", radius, center, voxel_size) is
+# the level-set sphere's narrow band turned into a density 0.5 - phi/6 (zero
+# outside the band, zero background and tiles); ("fog_ball", radius, center,
+# voxel_size) a sphere whose band reaches the centre, density -phi/radius
+# clamped to [0, 1].
+VOLUME_CASES = {
+    "vol_shell_noise_all_schemes": dict(
+        volume=("fog_shell", 12.0, (16.0, 16.0, 16.0), 1.0),
+        field=("dense", 32, 3.0, 1.5, 3),
+        ops=[("volume", 0, 1, 1, 1.0), ("volume", 1, 1, 1, 1.0), ("volume", 2, 1, 1, 1.0),
+             ("volume", 3, 1, 1, 1.0), ("volume", 4, 0, 1, 1.0), ("volume", 4, 1, 1, 1.0),
+             ("volume", 4, 2, 1, 1.0), ("volume", 5, 0, 1, 1.0), ("volume", 5, 1, 1, 1.0),
+             ("volume", 5, 2, 1, 1.0)],
+    ),
+    "vol_ball_xform_substeps": dict(
+        volume=("fog_ball", 8.0, (2.0, -1.0, 0.5), 1.0),
+        field=("dense_xform", 24, 2.0, 1.2, 11, 1.5, (0.25, -0.5, 0.75), (-10, -10, -10)),
+        ops=[("volume", 4, 1, 2, 1.5), ("volume", 2, 1, 3, -1.0), ("volume", 5, 2, 2, 0.75)],
+    ),
+    "vol_half_voxel_constant": dict(
+        volume=("fog_ball", 4.0, (0.3, 0.2, -0.1), 0.5),
+        field=("constant", (1.25, -0.6, 0.35)),
+        ops=[("volume", 3, 1, 1, 2.0), ("volume", 0, 1, 3, 1.0), ("volume", 5, 1, 1, 0.5)],
+    ),
+}
+
+
+def make_volume(spec):
+    """A FloatGrid volume from the level-set sphere fixture (see VOLUME_CASES)."""
+    from openvdb_gb300 import fixtures
+    kind, radius, center, dx = spec
+    if kind == "fog_shell":
+        g = fixtures.sphere(radius, center, dx, 3.0)
+        m = g.active_mask_bool()
+        g.leaf_values = np.where(m, np.float32(0.5) - g.leaf_values / np.float32(6.0),
+                                 np.float32(0.0)).astype(np.float32)
+    elif kind == "fog_ball":
+        g = fixtures.sphere(radius, center, dx, radius / dx + 2.0)
+        m = g.active_mask_bool()
+        d = np.clip(-g.leaf_values / np.float32(radius), np.float32(0.0), np.float32(1.0)).astype(np.float32)
+        g.leaf_values = np.where(m, d, np.float32(0.0)).astype(np.float32)
+    else:
+        raise ValueError(kind)
+    g.background = 0.0
+    g.lower_tiles[:] = 0.0
+    g.upper_tiles[:] = 0.0
+    g.root_tile_values[:] = 0.0
+    return g

@@ -19,7 +19,8 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, HERE)
 
-from cases import BATCH, BATCH_CFL, CASES, FILTER_CASES, MORPH_CASES, box_mask, make_batch, make_field, make_fixture, union8  # noqa: E402
+from cases import (BATCH, BATCH_CFL, CASES, FILTER_CASES, MORPH_CASES, VOLUME_CASES, box_mask, make_batch,  # noqa: E402
+                   make_field, make_fixture, make_volume, union8)
 from openvdb_gb300.grid import bitwise_equal, digest, summary  # noqa: E402
 from oracle import refpy  # noqa: E402
 
@@ -78,6 +79,22 @@ def run_reference(name, case, threads):
     return out
 
 
+def run_volume(case, threads):
+    """tools::VolumeAdvection on the case's volume: digest after every call."""
+    refpy.set_threads(threads)
+    host = make_volume(case["volume"])
+    g = refpy.RefGrid.from_host(host)
+    assert bitwise_equal(g.to_host(), host), "round trip through the reference grid"
+    field = make_field(case["field"])
+    out = [{"op": "input", "digest": digest(host), "summary": summary(host)}]
+    for op in case["ops"]:
+        _, integ, lim, sub, dt = op
+        mv = g.volume_advect(field, dt, integrator=integ, limiter=lim, substeps=sub)
+        h = g.to_host()
+        out.append({"op": list(op), "digest": digest(h), "summary": summary(h), "max_velocity": mv})
+    return out
+
+
 def main():
     nthreads = os.cpu_count() or 1
     only = [a.split("=", 1)[1].split(",") for a in sys.argv if a.startswith("--only=")]
@@ -97,6 +114,21 @@ def main():
         path = os.path.join(HERE, "parity_cases.json")
         result = json.load(open(path))
         result["__batch_cfl05__"] = run_batch(BATCH_CFL)
+        with open(path, "w") as f:
+            json.dump(result, f, indent=1, sort_keys=True)
+        return
+    if "--volumes-only" in sys.argv:  # recompute the VolumeAdvection cases, keep the rest
+        path = os.path.join(HERE, "parity_cases.json")
+        result = json.load(open(path))
+        vol = {}
+        for name, case in VOLUME_CASES.items():
+            a = run_volume(case, 1)
+            b = run_volume(case, nthreads)
+            assert a == b, "reference result depends on the thread count: " + name
+            vol[name] = a
+            print("%-32s ops=%d final active=%s leaves=%s" % (name, len(a) - 1, a[-1]["summary"]["active"],
+                                                             a[-1]["summary"]["leaves"]))
+        result["__volume__"] = vol
         with open(path, "w") as f:
             json.dump(result, f, indent=1, sort_keys=True)
         return
@@ -133,6 +165,7 @@ def main():
         morph[name] = a
         print("%-32s ops=%d final active=%s" % (name, len(a) - 1, a[-1]["summary"]["active"]))
     result["__morph__"] = morph
+    result["__volume__"] = {name: run_volume(case, nthreads) for name, case in VOLUME_CASES.items()}
     filt = {}
     for name, case in FILTER_CASES.items():
         a = run_filter(case, 1)
