@@ -351,6 +351,11 @@ int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int
  * count as 1).  max_velocity (may be NULL) receives getMaxVelocity().       */
 int gbls_volume_advect(gbls_handle* h, const gbls_field* velocity, int integrator, int limiter, int substeps,
                        double time_step, double* max_velocity);
+/* A handle for a general FloatGrid volume (the grid exchange of gbls_create
+ * without its level-set checks: any background).  Such a handle takes
+ * gbls_volume_advect, gbls_download and the counts; the level-set
+ * operations return GBLS_ERR_UNSUPPORTED.                                    */
+int gbls_create_volume(const gbls_grid_desc* desc, gbls_handle** out);
 
 /* ---- adjoint ---------------------------------------------------------------
  * No counterpart in the reference (it has no derivatives).  While recording

@@ -47,6 +47,7 @@ def lib():
         "gbls_set_precision": ([vp, C.c_int], C.c_int),
         "gbls_set_launch_config": ([vp, P(_abi.LaunchConfig)], C.c_int),
         "gbls_volume_advect": ([vp, vp, C.c_int, C.c_int, C.c_int, C.c_double, P(C.c_double)], C.c_int),
+        "gbls_create_volume": ([P(_abi.GridDesc), P(vp)], C.c_int),
         "gbls_get_launch_config": ([vp, P(_abi.LaunchConfig)], C.c_int),
         "gbls_time_launch_config": ([vp, vp, P(_abi.LaunchConfig), C.c_int, P(C.c_float)], C.c_int),
         "gbls_set_interrupter": ([vp, P(_abi.Interrupter)], C.c_int),

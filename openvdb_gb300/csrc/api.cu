@@ -735,6 +735,9 @@ struct gbls_handle {
     bool parity_fp64 = false;
     // launch shapes (gbls_set_launch_config; the autotuner's choices)
     int rk_min_ctas = 0, norm_min_ctas = 0, cfl_leaves = 32;
+    // a general FloatGrid volume (gbls_create_volume): any background, and
+    // only volume operations
+    bool volume = false;
     // HOST_SAMPLED fields: per-leaf active prefix, active voxel coordinates
     // and the sampled velocities of the current substep
     DevArray<int64_t> hs_count, hs_prefix;
@@ -2003,7 +2006,8 @@ bool upload_impl(gbls_handle& h, const gbls_grid_desc* descs, int n, bool dev_le
     if (n < 1 || n > GBLS_MAX_INSTANCES) fail(GBLS_ERR_INVALID_ARGUMENT, "instance count out of range");
     const gbls_grid_desc* d0 = descs;
     if (!(d0->voxel_size > 0.0)) fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
-    if (!(d0->background > 0.0f)) fail(GBLS_ERR_RUNTIME, "LevelSetTracker expected a level set (positive background)");
+    if (!h.volume && !(d0->background > 0.0f))
+        fail(GBLS_ERR_RUNTIME, "LevelSetTracker expected a level set (positive background)");
     if (d0->map_type < GBLS_MAP_UNIFORM_SCALE || d0->map_type > GBLS_MAP_TRANSLATION)
         fail(GBLS_ERR_VALUE, "MapType not supported!");
     h.voxel_size = d0->voxel_size;
@@ -2350,7 +2354,7 @@ int gbls_set_device(int device) {
     });
 }
 
-int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
+static int create_handle(const gbls_grid_desc* desc, gbls_handle** out, bool volume) {
     if (!desc || !out) {
         g_last_error = "null argument";
         return GBLS_ERR_INVALID_ARGUMENT;
@@ -2361,6 +2365,7 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
         DeviceGuard g(g_device);
         h = new gbls_handle;
         h->device = g_device;
+        h->volume = volume;
         h->small_sort_limit = small_sort_limit_from_env();
         h->parity_fp64 = parity_fp64_from_env();
         CU(cudaMalloc(&h->st_d, sizeof(DevStatus)));
@@ -2376,6 +2381,10 @@ int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) {
     *out = h;
     return GBLS_OK;
 }
+
+int gbls_create(const gbls_grid_desc* desc, gbls_handle** out) { return create_handle(desc, out, false); }
+
+int gbls_create_volume(const gbls_grid_desc* desc, gbls_handle** out) { return create_handle(desc, out, true); }
 
 int gbls_upload(gbls_handle* h, const gbls_grid_desc* desc) {
     touched(h);
@@ -2601,6 +2610,7 @@ int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr) {
 }
 
 int gbls_track(gbls_handle* h) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
@@ -2612,6 +2622,7 @@ int gbls_track(gbls_handle* h) {
 }
 
 int gbls_normalize(gbls_handle* h) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
@@ -2629,6 +2640,7 @@ int gbls_normalize(gbls_handle* h) {
 // active masks (x<<6 | y<<3 | z bit order).
 int gbls_normalize_masked(gbls_handle* h, int64_t mask_leaf_count, const int32_t* mask_leaf_origins,
                           const uint64_t* mask_leaf_masks) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h || mask_leaf_count < 0 || (mask_leaf_count > 0 && (!mask_leaf_origins || !mask_leaf_masks))) {
         g_last_error = "null argument or negative count";
@@ -2674,6 +2686,7 @@ int gbls_normalize_masked(gbls_handle* h, int64_t mask_leaf_count, const int32_t
 }
 
 int gbls_prune(gbls_handle* h) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
@@ -2690,6 +2703,7 @@ int gbls_prune(gbls_handle* h) {
 // NN_FACE dilation, the background grows by dx, and (normCount > 0) the
 // newly activated voxels are renormalised with the others held fixed.
 int gbls_dilate(gbls_handle* h, int iterations) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
@@ -2717,6 +2731,7 @@ int gbls_dilate(gbls_handle* h, int iterations) {
 // LevelSetTracker::erode (tools/LevelSetTracker.h:339-349): NN_FACE erosion,
 // pruneLevelSet, then the background shrinks by iterations * dx.
 int gbls_erode(gbls_handle* h, int iterations) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
@@ -2743,6 +2758,7 @@ int gbls_erode(gbls_handle* h, int iterations) {
 
 // LevelSetTracker::resize (tools/LevelSetTracker.h:351-364).
 int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (changed) *changed = 0;
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
@@ -3460,6 +3476,7 @@ int gbls_field_destroy(gbls_field* f) {
 
 int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int temporal, float t0, float t1,
                 float cfl, uint64_t* substeps) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     if (substeps) *substeps = 0;
     if (!h || !field) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     uint64_t count = 0;
@@ -3586,6 +3603,7 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
 // LevelSetFilter (tools/LevelSetFilter.h:93-157): one filter, then the
 // tracker pass with h's tracker state (the filter is a LevelSetTracker).
 int gbls_filter(gbls_handle* h, int filter, int width, float value) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     bool interrupted = false;
@@ -3667,6 +3685,7 @@ int gbls_filter(gbls_handle* h, int filter, int width, float value) {
 // voxel's index.
 int gbls_filter_masked(gbls_handle* h, int filter, int width, float value, gbls_handle* alpha_mask,
                        float mask_min, float mask_max, int invert_mask) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     if (!h || !alpha_mask) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     const int rc = guarded([&] {
         DeviceGuard g(h->device);
@@ -3783,6 +3802,7 @@ int gbls_volume_advect(gbls_handle* h, const gbls_field* field, int integrator, 
         if (integrator < 0 || integrator > 5) fail(GBLS_ERR_VALUE, "Spatial difference scheme not supported!");
         if (limiter < 0 || limiter > 2) fail(GBLS_ERR_VALUE, "unknown limiter");
         if (h->ninst != 1) fail(GBLS_ERR_UNSUPPORTED, "volume advection works on single grids, not batches");
+        if (!h->volume) fail(GBLS_ERR_UNSUPPORTED, "volume advection takes a handle made by gbls_create_volume");
         if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "the adjoint records level-set advection only");
         const gbls_field_desc& fd = field->desc;
         if (fd.kind != GBLS_FIELD_DENSE && fd.kind != GBLS_FIELD_CONSTANT)
@@ -3902,6 +3922,7 @@ int gbls_volume_advect(gbls_handle* h, const gbls_field* field, int integrator, 
 
 int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial, int temporal, float t0,
                float t1, float mask_min, float mask_max, int invert_mask, uint64_t* substeps) {
+    if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (substeps) *substeps = 0;
     if (!h || !target) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }

@@ -126,10 +126,26 @@ class DeviceLevelSet:
         _call(lib().gbls_set_profiling(self._h, 1 if enable else 0))
 
 
+class DeviceVolume(DeviceLevelSet):
+    """A FloatGrid volume (e.g. a fog density) resident on the GPU
+    (gbls_create_volume): any background; volume operations only."""
+
+    def __init__(self, grid, device=0):
+        L = lib()
+        _call(L.gbls_set_device(int(device)))
+        self._h = C.c_void_p()
+        self._keep = grid
+        d = grid.desc()
+        _call(L.gbls_create_volume(C.byref(d), C.byref(self._h)))
+        self._keep = None
+        self.voxel_size = grid.voxel_size
+        self.background = grid.background
+
+
 class VolumeAdvection:
     """tools::VolumeAdvection<Vec3fGrid> (tools/VolumeAdvect.h:76-262) with the
     reference's method names, advecting FloatGrid volumes (fog densities)
-    held by a DeviceLevelSet through gbls_volume_advect.  advect(grid, dt)
+    held by a DeviceVolume through gbls_volume_advect.  advect(grid, dt)
     replaces the grid's contents with the advected copy (the reference returns
     a new grid and leaves its input unchanged)."""
 

@@ -18,11 +18,11 @@ GOLD = json.load(open(os.path.join(HERE, "golden", "parity_cases.json")))["__vol
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", sorted(VOLUME_CASES))
 def test_volume_advection_bit_exact(name):
-    from openvdb_gb300 import DeviceLevelSet, VolumeAdvection, digest, summary
+    from openvdb_gb300 import DeviceVolume, VolumeAdvection, digest, summary
     case, gold = VOLUME_CASES[name], GOLD[name]
     host = make_volume(case["volume"])
     assert digest(host) == gold[0]["digest"]
-    dev = DeviceLevelSet(host)
+    dev = DeviceVolume(host)
     adv = VolumeAdvection(make_field(case["field"]))
     for op, want in zip(case["ops"], gold[1:]):
         _, integ, lim, sub, dt = op
@@ -34,3 +34,11 @@ def test_volume_advection_bit_exact(name):
         got = dev.to_host()
         assert summary(got) == want["summary"], (op, summary(got), want["summary"])
         assert digest(got) == want["digest"], op
+
+
+@pytest.mark.gpu
+def test_volume_handles_refuse_level_set_operations():
+    from openvdb_gb300 import DeviceVolume, LevelSetTracker
+    dev = DeviceVolume(make_volume(("fog_shell", 6.0, (0.0, 0.0, 0.0), 1.0)))
+    with pytest.raises(Exception):
+        LevelSetTracker(dev).normalize()
