@@ -7,7 +7,12 @@
 //   4. the tracker constructor rejects what the reference rejects;
 //   5. an aligned DiscreteField becomes a dense box holding field(ijk);
 //      a non-aligned one is refused;
-//   6. advect() either runs on a GPU or fails with an OpenVDB exception.
+//   6. advect() either runs on a GPU or fails with an OpenVDB exception;
+//   7-8. morphing and filters likewise;
+//   9. VolumeAdvection: getMaxVelocity and defaults equal the reference's,
+//      the velocity grid's dense box holds getValue at every box voxel;
+//  10. volume advect runs on a GPU and equals the reference's result, or
+//      fails with an OpenVDB exception.
 // Prints "ok <n>" per check; exits non-zero on the first failure.
 #include <openvdb/openvdb.h>
 #include <openvdb/tools/LevelSetSphere.h>
@@ -19,6 +24,9 @@
 #include "openvdb_gb300/LevelSetAdvect.h"
 #include "openvdb_gb300/LevelSetFilter.h"
 #include "openvdb_gb300/LevelSetMorph.h"
+#include "openvdb_gb300/VolumeAdvect.h"
+
+#include <cmath>
 
 using namespace openvdb;
 
@@ -240,6 +248,53 @@ int main() {
         std::printf("ok %d filter ran on a device\n", ++g_n);
     } catch (const openvdb::Exception& e) {
         std::printf("ok %d filter without a device: %s\n", ++g_n, e.what());
+    }
+    // 9. VolumeAdvection
+    {
+        Vec3fGrid::Ptr vel = Vec3fGrid::create(Vec3f(0.1f, 0.0f, -0.05f));
+        auto vacc = vel->getAccessor();
+        for (int i = -8; i < 8; ++i)
+            for (int j = -8; j < 8; ++j)
+                for (int k = -8; k < 8; ++k)
+                    vacc.setValue(Coord(i, j, k), Vec3f(0.3f * std::sin(0.2f * float(i)),
+                                                        0.2f * std::cos(0.3f * float(j)), 0.1f * float(k) / 8.0f));
+        FloatGrid::Ptr fog = FloatGrid::create(0.0f);
+        auto facc = fog->getAccessor();
+        for (int i = -5; i <= 5; ++i)
+            for (int j = -5; j <= 5; ++j)
+                for (int k = -5; k <= 5; ++k) {
+                    const float r = std::sqrt(float(i * i + j * j + k * k));
+                    if (r <= 5.0f) facc.setValue(Coord(i, j, k), 1.0f - r / 5.0f);
+                }
+        og::tools::VolumeAdvection<Vec3fGrid> va(*vel);
+        tools::VolumeAdvection<Vec3fGrid> vr(*vel);
+        CHECK(va.getMaxVelocity() == vr.getMaxVelocity() && va.getIntegrator() == vr.getIntegrator() &&
+              va.getLimiter() == vr.getLimiter() && va.getSubSteps() == vr.getSubSteps() &&
+              va.getMaxDistance(*fog, 1.0) == vr.getMaxDistance(*fog, 1.0));
+        std::vector<float> store;
+        const gbls_field_desc fd = og::detail::describeVelocityGrid(*vel, *fog, store);
+        CHECK(fd.kind == GBLS_FIELD_DENSE && fd.dense_dims[0] == 16 && fd.dense_dims[1] == 16 && fd.dense_dims[2] == 16);
+        size_t q = 0;
+        bool same_box = true;
+        for (int i = -8; i < 8; ++i)
+            for (int j = -8; j < 8; ++j)
+                for (int k = -8; k < 8; ++k, q += 3) {
+                    const Vec3f v = vacc.getValue(Coord(i, j, k));
+                    same_box &= store[q] == v[0] && store[q + 1] == v[1] && store[q + 2] == v[2];
+                }
+        CHECK(same_box && fd.dense_background[0] == 0.1f && fd.dense_map_type == 0);
+        std::printf("ok %d VolumeAdvection defaults, max velocity and velocity box\n", ++g_n);
+        va.setIntegrator(tools::Scheme::MAC);
+        vr.setIntegrator(tools::Scheme::MAC);
+        try {
+            FloatGrid::Ptr out = va.advect<FloatGrid, tools::Sampler<1, false>>(*fog, 1.0);
+            FloatGrid::Ptr ref = vr.advect<FloatGrid, tools::Sampler<1, false>>(*fog, 1.0);
+            og::detail::HostGrid a1 = og::detail::pack(*out), b1 = og::detail::pack(*ref);
+            CHECK(sameDesc(a1.desc(), b1.desc()));
+            std::printf("ok %d volume advect ran on a device, equal to the reference\n", ++g_n);
+        } catch (const openvdb::Exception& e) {
+            std::printf("ok %d volume advect without a device: %s\n", ++g_n, e.what());
+        }
     }
     gbls_host_grid_free(fix);
     return 0;

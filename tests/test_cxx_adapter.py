@@ -1,5 +1,6 @@
 """The C++ drop-in headers (include/openvdb_gb300/LevelSetAdvect.h,
-LevelSetTracker.h, GridExchange.h) compiled against the reference's own
+LevelSetTracker.h, LevelSetMorph.h, LevelSetFilter.h, VolumeAdvect.h,
+GridExchange.h) compiled against the reference's own
 OpenVDB headers and run on the host: grid <-> exchange-format conversion
 equal to the library's fixtures, exception mapping, constructor checks and
 DiscreteField sampling (tests/cxx/adapter_test.cc).
@@ -42,4 +43,4 @@ def test_cxx_adapter(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count("ok ") == 9
+    assert r.stdout.count("ok ") == 11
