@@ -340,9 +340,38 @@ def run_gb300(args):
         "cpu_baseline": cpu_baseline(args) if args.cpu_baseline else None,
     }
     if args.extras:
+        out["config1"] = config1_sphere(mode, args.mode, args.cfl)
         out["adjoint"] = adjoint_cost(mode, args.mode)
         out["batched"] = batch_measure(args, steps=3, warmup=3, cpu=False)
     print(json.dumps(out))
+
+
+def config1_sphere(mode, mode_name, cfl, steps=10):
+    """The small configuration: a radius-64 sphere (voxel size 1, half width 3)
+    advected by the constant velocity (1, 0.5, 0.25) for 10 unit steps, RK3,
+    tracker RK1 with one renormalisation; CUDA events around the 10 calls."""
+    import torch
+    from openvdb_gb300 import DeviceLevelSet, Field, fixtures
+    from openvdb_gb300.levelset import DeviceField
+    dev = DeviceLevelSet(fixtures.sphere(64.0, (0.0, 0.0, 0.0)))
+    dev.set_precision(mode)
+    stream = torch.cuda.Stream()
+    dev.set_stream(stream.cuda_stream)
+    adv = make_advection(dev, DeviceField(Field.constant_field((1.0, 0.5, 0.25))), cfl=cfl)
+    adv.advect(-1.0, 0.0)  # warm-up on the same level set, before t = 0
+    torch.cuda.synchronize()
+    dev.reset_stats()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for t in range(steps):
+        adv.advect(float(t), float(t + 1))
+    e1.record(stream)
+    e1.synchronize()
+    st = dev.stats()
+    ms = e0.elapsed_time(e1)
+    return {"workload": "sphere r=64, constant velocity (1, 0.5, 0.25), 10 unit steps, RK3-HJWENO5, CFL %g" % cfl,
+            "mode": mode_name, "value": st["voxel_updates"] / (ms / 1e3), "unit": UNIT, "ms": ms,
+            "substeps": int(st["substeps"]), "active_voxels_end": int(st["active_voxels"])}
 
 
 def adjoint_cost(mode, mode_name, reps=3):

@@ -308,6 +308,64 @@ __device__ inline float godunov_hj_exact(const float* tile, int x, int y, int z,
     return acc;
 }
 
+// GodunovsNormSqrd of every processed voxel of a leaf (the voxels of pm in
+// `list`), as godunov_hj_exact computes it, into gsq[v] (v the voxel's
+// position).  A warp that evaluates each voxel's derivatives in turn runs
+// the union of its lanes' needs (about six WENO5 per voxel); here the
+// derivatives a voxel needs become work items of a CTA-wide list, axis by
+// axis, so every lane evaluates one needed WENO5 at a time.  An axis term
+// max(a^2, b^2) is the maximum of its items' squares (+0 without items;
+// non-negative floats order like their bits), and the terms are summed in
+// axis order.  All threads call; starts and ends with a barrier.
+__device__ inline void godunov_exact_leaf(const float* tile, const uint16_t* list, int n, const uint64_t* pm,
+                                          float* gsq, uint32_t* term, uint16_t* queue, int* qn) {
+    const int t = threadIdx.x;
+    if (t < 3) qn[t] = 0;
+    __syncthreads();
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        for (int i = t; i < n; i += STAGE_THREADS) {
+            const int v = list[i];
+            if (!((pm[v >> 6] >> (v & 63)) & 1)) continue;
+            const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+            const bool outside = tile[tile_index(x, y, z)] > 0.0f;
+            const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
+            const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
+            const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
+            term[v] = 0u;
+            if (outside ? sb != -1 : sb != 1) queue[atomicAdd(&qn[ax], 1)] = uint16_t(v << 1);
+            if (outside ? sf != 1 : sf != -1) queue[atomicAdd(&qn[ax], 1)] = uint16_t((v << 1) | 1);
+        }
+        __syncthreads();
+        const int m = qn[ax];
+#pragma unroll 1
+        for (int j = t; j < m; j += STAGE_THREADS) {
+            const int e = queue[j];
+            const int v = e >> 1;
+            const bool fd = e & 1;
+            const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+            const bool outside = tile[tile_index(x, y, z)] > 0.0f;
+            const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
+            float q[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) q[k] = fd ? D.d[5 - k] : D.d[k];  // FD: D5..D1, BD: D0..D4
+            const float w = ExactArith::weno5(q[0], q[1], q[2], q[3], q[4]);
+            // dm enters as max(dm, 0) outside, min(dm, 0) inside; dp the other way
+            const float c = fd ? (outside ? ref_min(w, 0.0f) : ref_max(w, 0.0f))
+                               : (outside ? ref_max(w, 0.0f) : ref_min(w, 0.0f));
+            atomicMax(&term[v], __float_as_uint(ExactArith::mul(c, c)));
+        }
+        __syncthreads();
+        for (int i = t; i < n; i += STAGE_THREADS) {
+            const int v = list[i];
+            if (!((pm[v >> 6] >> (v & 63)) & 1)) continue;
+            const float tv = __uint_as_float(term[v]);
+            gsq[v] = ax == 0 ? tv : ExactArith::add(gsq[v], tv);
+        }
+    }
+    __syncthreads();
+}
+
 // ---- velocity --------------------------------------------------------------
 // Value of the dense velocity grid at its index (a, b, c) (background outside).
 __device__ __forceinline__ void dense_value(const FieldParams& f, int i, int j, int k, float out[3]) {
@@ -617,6 +675,15 @@ __global__ void __launch_bounds__(STENCIL_THREADS, MINB) normalize_kernel(const 
     __syncthreads();
     const int n = build_list(list, um);
     __syncthreads();
+    const bool exact_hj = IsExact<A>::value && a.spatial == 4 && !a.copy_only;
+    if constexpr (IsExact<A>::value) {
+        // the Godunov norms first, into res (each voxel's own slot, which the
+        // loop below reads before it writes the voxel's result there)
+        __shared__ uint32_t gterm[LEAF_VOX];
+        __shared__ uint16_t gqueue[2 * LEAF_VOX];
+        __shared__ int gqn[3];
+        if (exact_hj) godunov_exact_leaf(tile, list, n, pm, res, gterm, gqueue, gqn);
+    }
     const float g = a.gamma;
     for (int i = t; i < n; i += STENCIL_THREADS) {
         const int v = list[i];
@@ -632,8 +699,8 @@ __global__ void __launch_bounds__(STENCIL_THREADS, MINB) normalize_kernel(const 
         }
         if (!a.copy_only) {
             float nsq;
-            if (IsExact<A>::value && a.spatial == 4) {
-                nsq = godunov_hj_exact(tile, x, y, z, phi0 > 0.0f);
+            if (exact_hj) {
+                nsq = res[v];
             } else {
                 float up[3], down[3];
 #pragma unroll
