@@ -315,52 +315,82 @@ __device__ inline float godunov_hj_exact(const float* tile, int x, int y, int z,
 // derivatives a voxel needs become work items of a CTA-wide list, axis by
 // axis, so every lane evaluates one needed WENO5 at a time.  An axis term
 // max(a^2, b^2) is the maximum of its items' squares (+0 without items;
-// non-negative floats order like their bits), and the terms are summed in
-// axis order.  All threads call; starts and ends with a barrier.
+// non-negative floats order like their bits), kept in gsq as bits while the
+// axis runs, and the terms are summed in axis order in registers (thread t
+// owns list entries t + 64k).  The list of at most `cap` items lives in
+// dead staging memory; more than cap/2 processed voxels run in two rounds.
+// All threads call; starts and ends with a barrier.
 __device__ inline void godunov_exact_leaf(const float* tile, const uint16_t* list, int n, const uint64_t* pm,
-                                          float* gsq, uint32_t* term, uint16_t* queue, int* qn) {
+                                          float* gsq, uint16_t* queue, int cap, int* qn) {
     const int t = threadIdx.x;
-    if (t < 3) qn[t] = 0;
+    uint32_t* term = reinterpret_cast<uint32_t*>(gsq);
+    int np = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) np += __popcll(pm[w]);
+    const int rounds = 2 * np > cap ? 2 : 1;  // each half of the list holds at most 256 voxels
+    const int mid = rounds == 2 ? n / 2 : n;
+    if (t < 6) qn[t] = 0;
     __syncthreads();
+    float acc[8];
 #pragma unroll 1
     for (int ax = 0; ax < 3; ++ax) {
-        for (int i = t; i < n; i += STAGE_THREADS) {
-            const int v = list[i];
-            if (!((pm[v >> 6] >> (v & 63)) & 1)) continue;
-            const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
-            const bool outside = tile[tile_index(x, y, z)] > 0.0f;
-            const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
-            const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
-            const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
-            term[v] = 0u;
-            if (outside ? sb != -1 : sb != 1) queue[atomicAdd(&qn[ax], 1)] = uint16_t(v << 1);
-            if (outside ? sf != 1 : sf != -1) queue[atomicAdd(&qn[ax], 1)] = uint16_t((v << 1) | 1);
-        }
-        __syncthreads();
-        const int m = qn[ax];
 #pragma unroll 1
-        for (int j = t; j < m; j += STAGE_THREADS) {
-            const int e = queue[j];
-            const int v = e >> 1;
-            const bool fd = e & 1;
-            const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
-            const bool outside = tile[tile_index(x, y, z)] > 0.0f;
-            const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
-            float q[5];
+        for (int r = 0; r < rounds; ++r) {
+            const int lo = r == 0 ? 0 : mid, hi = r == 0 ? mid : n;
+            int* cnt = qn + 2 * ax + r;
+#pragma unroll 1
+            for (int i = lo + t; i < hi; i += STAGE_THREADS) {
+                const int v = list[i];
+                if (!((pm[v >> 6] >> (v & 63)) & 1)) continue;
+                const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+                const bool outside = tile[tile_index(x, y, z)] > 0.0f;
+                const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
+                const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
+                const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
+                term[v] = 0u;
+                if (outside ? sb != -1 : sb != 1) queue[atomicAdd(cnt, 1)] = uint16_t(v << 1);
+                if (outside ? sf != 1 : sf != -1) queue[atomicAdd(cnt, 1)] = uint16_t((v << 1) | 1);
+            }
+            __syncthreads();
+            const int m = *cnt;
+#pragma unroll 1
+            for (int j = t; j < m; j += STAGE_THREADS) {
+                const int e = queue[j];
+                const int v = e >> 1;
+                const bool fd = e & 1;
+                const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+                const bool outside = tile[tile_index(x, y, z)] > 0.0f;
+                const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
+                float q[5];
 #pragma unroll
-            for (int k = 0; k < 5; ++k) q[k] = fd ? D.d[5 - k] : D.d[k];  // FD: D5..D1, BD: D0..D4
-            const float w = ExactArith::weno5(q[0], q[1], q[2], q[3], q[4]);
-            // dm enters as max(dm, 0) outside, min(dm, 0) inside; dp the other way
-            const float c = fd ? (outside ? ref_min(w, 0.0f) : ref_max(w, 0.0f))
-                               : (outside ? ref_max(w, 0.0f) : ref_min(w, 0.0f));
-            atomicMax(&term[v], __float_as_uint(ExactArith::mul(c, c)));
+                for (int k = 0; k < 5; ++k) q[k] = fd ? D.d[5 - k] : D.d[k];  // FD: D5..D1, BD: D0..D4
+                const float wv = ExactArith::weno5(q[0], q[1], q[2], q[3], q[4]);
+                // dm enters as max(dm, 0) outside, min(dm, 0) inside; dp the other way
+                const float c = fd ? (outside ? ref_min(wv, 0.0f) : ref_max(wv, 0.0f))
+                                   : (outside ? ref_max(wv, 0.0f) : ref_min(wv, 0.0f));
+                atomicMax(&term[v], __float_as_uint(ExactArith::mul(c, c)));
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int i = t; i < n; i += STAGE_THREADS) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int i = t + k * STAGE_THREADS;
+            if (i < n) {
+                const int v = list[i];
+                if ((pm[v >> 6] >> (v & 63)) & 1) {
+                    const float tv = __uint_as_float(term[v]);
+                    acc[k] = ax == 0 ? tv : ExactArith::add(acc[k], tv);
+                }
+            }
+        }
+        __syncthreads();  // the next axis resets the terms
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int i = t + k * STAGE_THREADS;
+        if (i < n) {
             const int v = list[i];
-            if (!((pm[v >> 6] >> (v & 63)) & 1)) continue;
-            const float tv = __uint_as_float(term[v]);
-            gsq[v] = ax == 0 ? tv : ExactArith::add(gsq[v], tv);
+            if ((pm[v >> 6] >> (v & 63)) & 1) gsq[v] = acc[k];
         }
     }
     __syncthreads();
@@ -678,11 +708,12 @@ __global__ void __launch_bounds__(STENCIL_THREADS, MINB) normalize_kernel(const 
     const bool exact_hj = IsExact<A>::value && a.spatial == 4 && !a.copy_only;
     if constexpr (IsExact<A>::value) {
         // the Godunov norms first, into res (each voxel's own slot, which the
-        // loop below reads before it writes the voxel's result there)
-        __shared__ uint32_t gterm[LEAF_VOX];
-        __shared__ uint16_t gqueue[2 * LEAF_VOX];
-        __shared__ int gqn[3];
-        if (exact_hj) godunov_exact_leaf(tile, list, n, pm, res, gterm, gqueue, gqn);
+        // loop below reads before it writes the voxel's result there); the
+        // work list reuses the staging records, dead once the tile is loaded
+        __shared__ int gqn[6];
+        if (exact_hj)
+            godunov_exact_leaf(tile, list, n, pm, res, reinterpret_cast<uint16_t*>(&st.rec[0][0]),
+                               int(sizeof(st.rec) / sizeof(uint16_t)), gqn);
     }
     const float g = a.gamma;
     for (int i = t; i < n; i += STENCIL_THREADS) {
