@@ -545,6 +545,29 @@ int gbls_nanovdb_export_index(const gbls_grid_desc* desc, const char* name, int3
                               int32_t include_stats, int32_t include_tiles, int32_t checksum_mode,
                               uint8_t* out, int64_t out_capacity, int64_t* size);
 
+/* ---- NanoVDB on the device ---------------------------------------------------
+ * The same buffers written on the device straight from a handle's device
+ * tree, byte for byte what gbls_nanovdb_export / gbls_nanovdb_export_index
+ * write for the downloaded grid (and so what the reference's createNanoGrid
+ * writes, nanovdb/tools/CreateNanoGrid.h:162-190): the advected level set
+ * goes to NanoVDB's device consumers (ReadAccessor, the ValueOnIndex decode
+ * of nanovdb/NanoVDB.h:4144-4170, samplers, ray marchers) without a host
+ * round trip.  `instance` is -1 for a level-set handle, else the batch
+ * instance.  `out` is device memory, 32-byte aligned (cudaMalloc), at least
+ * *size bytes; with out == NULL only *size is set.  Runs on the handle's
+ * stream and returns with the buffer complete.                              */
+int gbls_nanovdb_export_device(gbls_handle* h, int32_t instance, const char* name, int32_t stats_mode,
+                               int32_t checksum_mode, void* out, int64_t out_capacity, int64_t* size);
+int gbls_nanovdb_export_index_device(gbls_handle* h, int32_t instance, const char* name, int32_t channels,
+                                     int32_t include_stats, int32_t include_tiles, int32_t checksum_mode,
+                                     void* out, int64_t out_capacity, int64_t* size);
+/* A level-set handle from a NanoGrid<float> buffer in device memory (or host
+ * memory): the tree is walked through its links as gbls_nanovdb_import
+ * walks it, the internal nodes are read on the host and the leaves gathered
+ * on the device.  A device buffer must be 32-byte aligned.  Errors as
+ * gbls_nanovdb_import and gbls_create.                                       */
+int gbls_create_from_nanovdb(const void* buffer, int64_t size, gbls_handle** out);
+
 #ifdef __cplusplus
 }
 #endif

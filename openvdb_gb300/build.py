@@ -23,7 +23,8 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contra
               "--expt-relaxed-constexpr", "-I" + os.path.join(REPO, "include")]
 CXX_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-pthread",
              "-I" + os.path.join(REPO, "include")]
-PER_UNIT = {"stencil_parity.cu": ["-fmad=false"], "stencil_exact.cu": ["-fmad=false"], "volume.cu": ["-fmad=false"]}
+PER_UNIT = {"stencil_parity.cu": ["-fmad=false"], "stencil_exact.cu": ["-fmad=false"], "volume.cu": ["-fmad=false"],
+            "nanovdb_device.cu": ["-fmad=false"]}
 
 
 def _nvcc():

@@ -24,6 +24,8 @@
 #include "filter_ops.cuh"
 #include "io.h"
 #include "morph_ops.cuh"
+#include "host_grid.h"
+#include "nanovdb_device.h"
 #include "stencil.h"
 #include "stencil_ops.cuh"
 #include "topology.cuh"
@@ -59,6 +61,9 @@ int guarded(F&& f) {
         f();
         return GBLS_OK;
     } catch (const Error& e) {
+        g_last_error = e.msg;
+        return e.code;
+    } catch (const gbls_nano::ExportError& e) {
         g_last_error = e.msg;
         return e.code;
     } catch (const std::bad_alloc&) {
@@ -2145,9 +2150,10 @@ bool upload_impl(gbls_handle& h, const gbls_grid_desc* descs, int n, bool dev_le
         const gbls_grid_desc* d = descs + q;
         const size_t a = size_t(lv_base[size_t(q)]), b = size_t(lo_base[size_t(q)]), c = size_t(up_base[size_t(q)]);
         if (d->leaf_count) {
-            CU(cudaMemcpyAsync(h.am[1].p + a * 8, d->leaf_masks, size_t(d->leaf_count) * 64, cudaMemcpyHostToDevice, h.stream));
+            // host or device arrays (a NanoVDB import gathers its leaves on the device)
+            CU(cudaMemcpyAsync(h.am[1].p + a * 8, d->leaf_masks, size_t(d->leaf_count) * 64, cudaMemcpyDefault, h.stream));
             CU(cudaMemcpyAsync(h.vals[1].p + a * LEAF_VOX, d->leaf_values, size_t(d->leaf_count) * LEAF_VOX * 4,
-                               cudaMemcpyHostToDevice, h.stream));
+                               cudaMemcpyDefault, h.stream));
         }
         if (d->lower_count)
             CU(cudaMemcpyAsync(lo_stage + b * LOWER_SLOTS, d->lower_tiles, size_t(d->lower_count) * LOWER_SLOTS * 4,
@@ -3977,6 +3983,227 @@ int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int
         g_last_error = "interrupted";
         return GBLS_ERR_INTERRUPTED;
     }
+    return rc;
+}
+
+}  // extern "C"
+
+// ---- NanoVDB on the device ----------------------------------------------------
+
+namespace {
+
+// The level set (or batch instance) of h as a device tree for the NanoVDB
+// writers, and a host descriptor with its counts, map, upper-node origins
+// and root tiles (the parts the host writes).
+struct NanoExport {
+    NanoDevTree t;
+    gbls_grid_desc d{};
+    std::vector<int32_t> upper_origins, root_origins;
+    std::vector<float> root_values;
+    int64_t voxels = 0;
+};
+
+NanoExport nano_export_view(gbls_handle& h, int instance) {
+    if (h.ninst > 1 && (instance < 0 || instance >= h.ninst)) fail(GBLS_ERR_INVALID_ARGUMENT, "no such instance");
+    if (h.ninst == 1 && instance > 0) fail(GBLS_ERR_INVALID_ARGUMENT, "no such instance");
+    h.sync();
+    const InstRange R = h.ninst > 1 ? inst_range(h, host_keys(h), instance)
+                                    : InstRange{0, h.nleaf, 0, int64_t(h.lower_keys_h.size()), 0,
+                                                int64_t(h.upper_keys_h.size()), 0, int64_t(h.root_keys_h.size())};
+    NanoExport e;
+    NanoDevTree& t = e.t;
+    t.nf = R.l1 - R.l0;
+    t.nl = R.lo1 - R.lo0;
+    t.nu = R.u1 - R.u0;
+    t.keys = h.K() + R.l0;
+    t.slot = h.S() + R.l0;
+    t.am = h.am[h.mc].p;
+    t.sm = h.sm[h.mc].p;
+    t.vals = h.vals[h.vc].p;
+    t.gamma = h.gamma;
+    t.lower_keys = h.lower_keys.p + R.lo0;
+    t.lower_sign = h.lower_sign.p + R.lo0 * 64;
+    t.upper_keys = h.upper_keys.p + R.u0;
+    t.upper_sign = h.upper_sign.p + R.u0 * 512;
+    for (int64_t i = R.u0; i < R.u1; ++i) {
+        int32_t x, y, z;
+        key_origin(h.upper_keys_h[size_t(i)] << 27, x, y, z);
+        e.upper_origins.insert(e.upper_origins.end(), {x, y, z});
+    }
+    for (int64_t i = R.r0; i < R.r1; ++i) {
+        int32_t x, y, z;
+        key_origin(h.root_keys_h[size_t(i)] << 27, x, y, z);
+        e.root_origins.insert(e.root_origins.end(), {x, y, z});
+        e.root_values.push_back(h.root_sign_h[size_t(i)] ? -h.gamma : h.gamma);
+    }
+    gbls_grid_desc& d = e.d;
+    d.voxel_size = h.voxel_size;
+    for (int i = 0; i < 3; ++i) d.translation[i] = h.translation[i];
+    d.map_type = h.map_type;
+    d.background = h.gamma;
+    d.leaf_count = t.nf;
+    d.lower_count = t.nl;
+    d.upper_count = t.nu;
+    d.upper_origins = e.upper_origins.data();
+    d.root_tile_count = R.r1 - R.r0;
+    d.root_tile_origins = e.root_origins.data();
+    d.root_tile_values = e.root_values.data();
+    if (t.nf) {
+        h.u64s.reserve(1, h.stream);
+        CU(cudaMemsetAsync(h.u64s.p, 0, sizeof(unsigned long long), h.stream));
+        k_count_active<<<blocks_for(t.nf * 8, 256), 256, 0, h.stream>>>(t.nf, t.slot, t.am, h.u64s.p);
+        ++h.stats.kernel_launches;
+        CU(cudaGetLastError());
+        unsigned long long n = 0;
+        CU(cudaMemcpyAsync(&n, h.u64s.p, sizeof(n), cudaMemcpyDeviceToHost, h.stream));
+        h.sync();
+        e.voxels = int64_t(n);
+    }
+    return e;
+}
+
+void check_device_out(const void* out, int64_t cap, int64_t size) {
+    if (cap < size) fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer too small");
+    if (reinterpret_cast<uintptr_t>(out) % 32) fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer not 32-byte aligned");
+    cudaPointerAttributes a{};
+    CU(cudaPointerGetAttributes(&a, out));
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        fail(GBLS_ERR_INVALID_ARGUMENT, "output buffer is not device memory");
+}
+
+// Grid and tree headers (and everything else host-written) are uploaded
+// first; the checksum word covers them and, for Full, the device bytes.
+void nano_finish(gbls_handle& h, uint8_t* out, std::vector<uint8_t>& top, size_t total, int checksum) {
+    CU(cudaMemcpyAsync(out, top.data(), top.size(), cudaMemcpyHostToDevice, h.stream));
+    if (checksum == 0) {
+        h.sync();
+        return;
+    }
+    const size_t head = gbls_nano::kGridBytes + gbls_nano::kTreeBytes;
+    const uint32_t tail = checksum == 2 ? nano_blocked_crc(out + head, total - head, h.stream) : ~0u;
+    const uint64_t word = gbls_nano::checksum_word(top.data(), checksum, tail);
+    std::memcpy(top.data() + 8, &word, 8);
+    CU(cudaMemcpyAsync(out + 8, top.data() + 8, 8, cudaMemcpyHostToDevice, h.stream));
+    h.sync();
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbls_nanovdb_export_device(gbls_handle* h, int32_t instance, const char* name, int32_t stats_mode,
+                               int32_t checksum_mode, void* out, int64_t out_capacity, int64_t* size) {
+    if (!h || !size) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        const std::string nm = name ? name : "";
+        if (stats_mode < 0 || stats_mode > 3) fail(GBLS_ERR_INVALID_ARGUMENT, "statistics mode must be 0-3");
+        if (checksum_mode < 0 || checksum_mode > 2) fail(GBLS_ERR_INVALID_ARGUMENT, "checksum mode must be 0-2");
+        if (nm.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
+        NanoExport e = nano_export_view(*h, instance);
+        const gbls_nano::FloatLayout L(e.t.nu, e.t.nl, e.t.nf, e.d.root_tile_count);
+        *size = int64_t(L.total);
+        if (!out) return;
+        check_device_out(out, out_capacity, *size);
+        uint8_t* o = static_cast<uint8_t*>(out);
+        CU(cudaMemsetAsync(o, 0, L.total, h->stream));
+        std::vector<gbls_nano::NodeStats> upper_stats;
+        nano_float_nodes(e.t, stats_mode, o, L, upper_stats, h->stream);
+        h->stats.kernel_launches += (e.t.nf > 0) + (e.t.nl > 0) + (e.t.nu > 0);
+        std::vector<uint8_t> top(L.upper_at, 0);
+        gbls_nano::write_float_top(top.data(), e.d, nm, stats_mode, upper_stats, e.voxels);
+        nano_finish(*h, o, top, L.total, checksum_mode);
+    });
+}
+
+int gbls_nanovdb_export_index_device(gbls_handle* h, int32_t instance, const char* name, int32_t channels,
+                                     int32_t include_stats, int32_t include_tiles, int32_t checksum_mode, void* out,
+                                     int64_t out_capacity, int64_t* size) {
+    if (!h || !size) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        const std::string nm = name ? name : "";
+        if (channels < 0) fail(GBLS_ERR_INVALID_ARGUMENT, "negative channel count");
+        if (channels > 1) fail(GBLS_ERR_UNSUPPORTED, "more than one value channel");
+        if (checksum_mode < 0 || checksum_mode > 2) fail(GBLS_ERR_INVALID_ARGUMENT, "checksum mode must be 0-2");
+        if (nm.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
+        const bool st = include_stats != 0, tiles = include_tiles != 0;
+        NanoExport e = nano_export_view(*h, instance);
+        uint64_t* leaf_off = nullptr;
+        const uint64_t count = nano_index_offsets(e.t, st, tiles, &leaf_off, h->stream);
+        struct OffGuard {
+            uint64_t* p;
+            cudaStream_t s;
+            ~OffGuard() { if (p) cudaFreeAsync(p, s); }
+        } og{leaf_off, h->stream};
+        const gbls_nano::IndexLayout L(e.t.nu, e.t.nl, e.t.nf, e.d.root_tile_count, channels, count);
+        *size = int64_t(L.total);
+        if (!out) return;
+        check_device_out(out, out_capacity, *size);
+        uint8_t* o = static_cast<uint8_t*>(out);
+        CU(cudaMemsetAsync(o, 0, L.total, h->stream));
+        std::vector<gbls_nano::BBox> upper_box;
+        nano_index_nodes(e.t, st, tiles, channels, leaf_off, o, L, upper_box, h->stream);
+        h->stats.kernel_launches += (e.t.nf > 0) + (e.t.nl > 0) + (e.t.nu > 0) + (channels > 0);
+        if (channels) {
+            std::vector<uint8_t> meta(gbls_nano::kBlindMetaBytes * size_t(channels), 0);
+            gbls_nano::write_index_meta(meta.data(), L, channels, count);
+            CU(cudaMemcpyAsync(o + L.meta_at, meta.data(), meta.size(), cudaMemcpyHostToDevice, h->stream));
+            h->sync();
+        }
+        std::vector<uint8_t> top(L.upper_at, 0);
+        gbls_nano::write_index_top(top.data(), e.d, nm, channels, st, tiles, upper_box, e.voxels, count);
+        nano_finish(*h, o, top, L.total, checksum_mode);
+    });
+}
+
+int gbls_create_from_nanovdb(const void* buffer, int64_t size, gbls_handle** out) {
+    if (!buffer || !out || size < 0) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    *out = nullptr;
+    gbls_host_grid* hg = nullptr;
+    uint64_t* d_at = nullptr;
+    uint64_t* d_masks = nullptr;
+    float* d_vals = nullptr;
+    gbls_grid_desc desc{};
+    int rc = guarded([&] {
+        DeviceGuard g(g_device);
+        cudaPointerAttributes a{};
+        CU(cudaPointerGetAttributes(&a, buffer));
+        const uint8_t* b = static_cast<const uint8_t*>(buffer);
+        if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) {
+            const gbls_nano::ByteReader read = [b](size_t at, size_t n, uint8_t* dst) { std::memcpy(dst, b + at, n); };
+            hg = gbls_nano::import_float(read, size, nullptr);
+            if (gbls_host_grid_view(hg, &desc) != GBLS_OK) fail(GBLS_ERR_RUNTIME, "host grid view");
+            return;
+        }
+        if (reinterpret_cast<uintptr_t>(buffer) % 32)
+            fail(GBLS_ERR_INVALID_ARGUMENT, "device NanoVDB buffer not 32-byte aligned");
+        const gbls_nano::ByteReader read = [b](size_t at, size_t n, uint8_t* dst) {
+            CU(cudaMemcpy(dst, b + at, n, cudaMemcpyDeviceToHost));
+        };
+        std::vector<uint64_t> leaf_at;
+        hg = gbls_nano::import_float(read, size, &leaf_at);
+        for (uint64_t at : leaf_at)
+            if (at % 32) fail(GBLS_ERR_UNSUPPORTED, "NanoVDB leaf not 32-byte aligned");
+        if (gbls_host_grid_view(hg, &desc) != GBLS_OK) fail(GBLS_ERR_RUNTIME, "host grid view");
+        const int64_t n = int64_t(leaf_at.size());
+        if (n) {
+            CU(cudaMalloc(&d_at, size_t(n) * 8));
+            CU(cudaMalloc(&d_masks, size_t(n) * 64));
+            CU(cudaMalloc(&d_vals, size_t(n) * LEAF_VOX * 4));
+            CU(cudaMemcpy(d_at, leaf_at.data(), size_t(n) * 8, cudaMemcpyHostToDevice));
+            nano_gather_leaves(b, d_at, n, d_masks, d_vals, 0);
+            CU(cudaDeviceSynchronize());
+        }
+        desc.leaf_count = n;
+        desc.leaf_masks = d_masks;
+        desc.leaf_values = d_vals;
+    });
+    if (rc == GBLS_OK) rc = create_handle(&desc, out, false);
+    cudaFree(d_at);
+    cudaFree(d_masks);
+    cudaFree(d_vals);
+    if (hg) gbls_host_grid_free(hg);
     return rc;
 }
 

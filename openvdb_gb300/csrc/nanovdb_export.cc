@@ -28,100 +28,13 @@
 #include <vector>
 
 #include "host_grid.h"
+#include "nanovdb_layout.h"
 
-namespace {
-
-constexpr uint64_t kMagicGrid = 0x314244566f6e614eULL;  // "NanoVDB1"
-constexpr uint32_t kVersion = (32u << 21) | (9u << 10) | 2u;
-constexpr size_t kGridBytes = 672, kTreeBytes = 64, kRootBytes = 64, kTileBytes = 32;
-constexpr size_t kUpperBytes = 270400, kLowerBytes = 33856, kLeafBytes = 2144;
-constexpr size_t kUpperTableAt = 8256, kLowerTableAt = 1088;
-enum : uint32_t { kHasBBox = 2, kHasMinMax = 4, kHasAverage = 8, kHasStdDeviation = 16, kIsBreadthFirst = 32 };
-enum { kStatsDisable = 0, kStatsBBox = 1, kStatsMinMax = 2, kStatsAll = 3 };
-
-struct ExportError {
-    int code;
-    std::string msg;
-};
-[[noreturn]] void fail(int code, const std::string& msg) { throw ExportError{code, msg}; }
+namespace gbls_nano {
 
 inline bool bit(const uint64_t* m, int i) { return (m[i >> 6] >> (i & 63)) & 1u; }
 
-template <class T> inline void put(std::vector<uint8_t>& b, size_t at, const T& v) { std::memcpy(b.data() + at, &v, sizeof(T)); }
-
-// Running extrema, mean and variance (nanovdb::tools::Stats<float, 0>).
-struct Stats {
-    float mn = FLT_MAX, mx = -FLT_MAX;
-    uint64_t n = 0;
-    double avg = 0.0, aux = 0.0;
-    void add(float v) {
-        if (v < mn) mn = v;
-        if (v > mx) mx = v;
-        n += 1;
-        const double delta = double(v) - avg;
-        avg += delta / double(n);
-        aux += delta * (double(v) - avg);
-    }
-    void add(const Stats& o, bool moments) {
-        if (!moments) {  // Extrema::add(Extrema)
-            if (o.mn < mn) mn = o.mn;
-            if (o.mx > mx) mx = o.mx;
-            return;
-        }
-        if (o.n == 0) return;
-        const double denom = 1.0 / double(n + o.n);
-        const double delta = o.avg - avg;
-        avg += denom * delta * double(o.n);
-        aux += o.aux + denom * delta * delta * double(n) * double(o.n);
-        if (o.mn < mn) mn = o.mn;
-        if (o.mx > mx) mx = o.mx;
-        n += o.n;
-    }
-    double dev() const { return std::sqrt(n < 2 ? 0.0 : aux / double(n)); }
-};
-
-struct BBox {
-    int32_t lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
-    bool empty() const { return lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]; }
-    void add(const BBox& o) {
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = std::min(lo[k], o.lo[k]);
-            hi[k] = std::max(hi[k], o.hi[k]);
-        }
-    }
-};
-
-struct NodeStats {
-    Stats stats;
-    BBox bbox;
-};
-
-// Writes min / max / average / standard deviation at `at` in the statistics
-// mode's extent (tools/GridStats.h:541-557).
-void put_stats(std::vector<uint8_t>& b, size_t at, const Stats& s, int mode) {
-    if (mode >= kStatsMinMax) {
-        put<float>(b, at, s.mn);
-        put<float>(b, at + 4, s.mx);
-    }
-    if (mode == kStatsAll) {
-        put<float>(b, at + 8, float(s.avg));
-        put<float>(b, at + 12, float(s.dev()));
-    }
-}
-
-void put_bbox(std::vector<uint8_t>& b, size_t at, const BBox& x) {
-    std::memcpy(b.data() + at, x.lo, 12);
-    std::memcpy(b.data() + at + 12, x.hi, 12);
-}
-
-// nanovdb Map (NanoVDB.h:1418-1573) of a uniform scale + translation.
-struct MapD {
-    double mat[9], inv[9], vec[3];
-    void apply(const double xyz[3], double out[3]) const {  // math::matMult with fma
-        for (int r = 0; r < 3; ++r)
-            out[r] = std::fma(xyz[0], mat[3 * r], std::fma(xyz[1], mat[3 * r + 1], std::fma(xyz[2], mat[3 * r + 2], vec[r])));
-    }
-};
+namespace {
 
 // Gauss-Jordan elimination with partial pivoting on a 4x4 matrix (rows
 // scaled by division, elimination below then above the pivots), the form
@@ -170,6 +83,8 @@ void gauss_jordan(const double a[4][4], double inv[4][4]) {
         }
 }
 
+}  // namespace
+
 MapD make_map(const gbls_grid_desc& d) {
     MapD m{};
     const double s = d.map_type == GBLS_MAP_TRANSLATION ? 1.0 : d.voxel_size;
@@ -196,7 +111,7 @@ MapD make_map(const gbls_grid_desc& d) {
     return m;
 }
 
-void put_map(std::vector<uint8_t>& b, size_t at, const MapD& m) {
+void put_map(uint8_t* b, size_t at, const MapD& m) {
     for (int k = 0; k < 9; ++k) put<float>(b, at + 4 * k, float(m.mat[k]));
     for (int k = 0; k < 9; ++k) put<float>(b, at + 36 + 4 * k, float(m.inv[k]));
     for (int k = 0; k < 3; ++k) put<float>(b, at + 72 + 4 * k, float(m.vec[k]));
@@ -207,70 +122,225 @@ void put_map(std::vector<uint8_t>& b, size_t at, const MapD& m) {
     put<double>(b, at + 256, 1.0);
 }
 
-uint32_t crc32(const uint8_t* p, size_t n) {
-    uint32_t lut[256];
-    for (uint32_t i = 0; i < 256; ++i) {
-        uint32_t c = i;
-        for (int k = 0; k < 8; ++k) c = (c >> 1) ^ ((c & 1) ? 0xEDB88320u : 0u);
-        lut[i] = c;
-    }
-    uint32_t crc = ~0u;
-    for (size_t i = 0; i < n; ++i) crc = lut[(crc ^ p[i]) & 0xFF] ^ (crc >> 8);
-    return ~crc;
-}
+namespace {
 
-// CRC-32 of each 4 KiB block (the last one takes the remainder), then of the
-// block checksums (util::blockedCrc32, tools/GridChecksum.h:172-185).
+// Blocked CRC of n bytes (util::blockedCrc32, tools/GridChecksum.h:172-185).
 uint32_t blocked_crc32(const uint8_t* p, size_t n) {
-    if (n == 0) return ~0u;
-    const size_t blocks = n >> 12;
+    const size_t blocks = crc_blocks(n);
     std::vector<uint32_t> sums(blocks);
     for (size_t i = 0; i < blocks; ++i) {
         size_t len = size_t(1) << 12;
         if (i + 1 == blocks) len += n - (blocks << 12);
         sums[i] = crc32(p + (i << 12), len);
     }
-    return crc32(reinterpret_cast<const uint8_t*>(sums.data()), 4 * blocks);
+    return crc_of_blocks(sums, n);
 }
 
-// Head CRC (grid and tree headers) and, for CheckMode::Full, the blocked
-// CRC of everything after them (tools/GridChecksum.h:206-230, 280-300).
 void put_checksum(std::vector<uint8_t>& b, int mode) {
     if (mode == 0) return;
-    const uint32_t head = crc32(b.data() + 16, kGridBytes + kTreeBytes - 16);
-    const uint32_t tail = mode == 2 ? blocked_crc32(b.data() + kGridBytes + kTreeBytes, b.size() - kGridBytes - kTreeBytes)
-                                    : ~0u;
-    put<uint64_t>(b, 8, (uint64_t(tail) << 32) | head);
+    const size_t head = kGridBytes + kTreeBytes;
+    const uint32_t tail = mode == 2 ? blocked_crc32(b.data() + head, b.size() - head) : ~0u;
+    put<uint64_t>(b.data(), 8, checksum_word(b.data(), mode, tail));
 }
 
-inline uint64_t root_key(const int32_t* o) {
-    return uint64_t(uint32_t(o[2]) >> 12) | (uint64_t(uint32_t(o[1]) >> 12) << 21) |
-           (uint64_t(uint32_t(o[0]) >> 12) << 42);
+// Root entries of a grid: its upper nodes and root tiles merged in Coord
+// order, as (index, is child).
+std::vector<std::pair<int64_t, bool>> root_entries(const gbls_grid_desc& d) {
+    std::vector<std::pair<int64_t, bool>> entries;
+    for (int64_t i = 0; i < d.upper_count; ++i) entries.push_back({i, true});
+    for (int64_t i = 0; i < d.root_tile_count; ++i) entries.push_back({i, false});
+    auto origin_of = [&](const std::pair<int64_t, bool>& e) {
+        return e.second ? d.upper_origins + 3 * e.first : d.root_tile_origins + 3 * e.first;
+    };
+    std::stable_sort(entries.begin(), entries.end(), [&](const auto& a, const auto& c) {
+        const int32_t *p = origin_of(a), *q = origin_of(c);
+        return std::lexicographical_compare(p, p + 3, q, q + 3);
+    });
+    return entries;
 }
 
-std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int mode, int checksum) {
+const int32_t* entry_origin(const gbls_grid_desc& d, const std::pair<int64_t, bool>& e) {
+    return e.second ? d.upper_origins + 3 * e.first : d.root_tile_origins + 3 * e.first;
+}
+
+// World-space bounding box of an index bounding box (corners through the
+// map) into grid bytes 560-607, and the voxel size at 608-631.
+void put_world_bbox(uint8_t* b, const MapD& map, const BBox& box, bool valid) {
+    double wlo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, whi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    if (valid) {
+        const int32_t lo[3] = {box.lo[0], box.lo[1], box.lo[2]};
+        const int32_t hi[3] = {box.hi[0] + 1, box.hi[1] + 1, box.hi[2] + 1};
+        for (int corner = 0; corner < 8; ++corner) {
+            const double p[3] = {double((corner & 4) ? hi[0] : lo[0]), double((corner & 2) ? hi[1] : lo[1]),
+                                 double((corner & 1) ? hi[2] : lo[2])};
+            double w[3];
+            map.apply(p, w);
+            for (int k = 0; k < 3; ++k) {
+                wlo[k] = std::min(wlo[k], w[k]);
+                whi[k] = std::max(whi[k], w[k]);
+            }
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        put<double>(b, 560 + 8 * k, wlo[k]);
+        put<double>(b, 584 + 8 * k, whi[k]);
+    }
+    const double one[3] = {1.0, 1.0, 1.0}, zero[3] = {0.0, 0.0, 0.0};
+    double a1[3], a0[3];
+    map.apply(one, a1);
+    map.apply(zero, a0);
+    for (int k = 0; k < 3; ++k) put<double>(b, 608 + 8 * k, a1[k] - a0[k]);
+}
+
+void put_tree(uint8_t* b, size_t tree_at, size_t root_at, size_t upper_at, size_t lower_at, size_t leaf_at,
+              int64_t nu, int64_t nl, int64_t nf, int64_t voxels) {
+    put<int64_t>(b, tree_at, nf ? int64_t(leaf_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 8, nl ? int64_t(lower_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 16, nu ? int64_t(upper_at - tree_at) : 0);
+    put<int64_t>(b, tree_at + 24, int64_t(root_at - tree_at));
+    put<uint32_t>(b, tree_at + 32, uint32_t(nf));
+    put<uint32_t>(b, tree_at + 36, uint32_t(nl));
+    put<uint32_t>(b, tree_at + 40, uint32_t(nu));
+    put<uint64_t>(b, tree_at + 56, uint64_t(voxels));
+}
+
+void check_desc(const gbls_grid_desc& d) {
     if (d.leaf_count < 0 || d.lower_count < 0 || d.upper_count < 0 || d.root_tile_count < 0)
         fail(GBLS_ERR_INVALID_ARGUMENT, "negative count in grid descriptor");
+}
+
+}  // namespace
+
+void write_float_top(uint8_t* b, const gbls_grid_desc& d, const std::string& name, int mode,
+                     const std::vector<NodeStats>& upper_stats, int64_t voxels) {
+    const FloatLayout L(d.upper_count, d.lower_count, d.leaf_count, d.root_tile_count);
+    const bool minmax = mode >= kStatsMinMax, moments = mode == kStatsAll;
+    // root: children and tiles merged in Coord order
+    const auto entries = root_entries(d);
+    NodeStats root_total;
+    for (size_t t = 0; t < entries.size(); ++t) {
+        const size_t at = L.root_at + kRootBytes + kTileBytes * t;
+        put<uint64_t>(b, at, root_key(entry_origin(d, entries[t])));
+        if (entries[t].second) {
+            put<int64_t>(b, at + 8, int64_t(L.upper_at + kUpperBytes * size_t(entries[t].first)) - int64_t(L.root_at));
+            root_total.stats.add(upper_stats.empty() ? Stats() : upper_stats[size_t(entries[t].first)].stats, moments);
+            if (!upper_stats.empty()) root_total.bbox.add(upper_stats[size_t(entries[t].first)].bbox);
+        } else {
+            put<float>(b, at + 20, d.root_tile_values[entries[t].first]);
+        }
+    }
+    put<uint32_t>(b, L.root_at + 24, uint32_t(L.table));
+    put<float>(b, L.root_at + 28, d.background);
+    BBox root_bbox;
+    if (L.table == 0 || mode == kStatsDisable) {
+        put<float>(b, L.root_at + 32, d.background);
+        put<float>(b, L.root_at + 36, d.background);
+    } else {
+        root_bbox = root_total.bbox;
+        if (mode == kStatsBBox) {
+            put<float>(b, L.root_at + 32, d.background);
+            put<float>(b, L.root_at + 36, d.background);
+        } else {
+            put_stats(b, L.root_at + 32, root_total.stats, mode);
+        }
+    }
+    put_bbox(b, L.root_at, root_bbox);
+    put_tree(b, L.tree_at, L.root_at, L.upper_at, L.lower_at, L.leaf_at, d.upper_count, d.lower_count, d.leaf_count,
+             voxels);
+    // grid
+    const MapD map = make_map(d);
+    put<uint64_t>(b, 0, kMagicGrid);
+    put<uint64_t>(b, 8, ~uint64_t(0));
+    put<uint32_t>(b, 16, kVersion);
+    uint32_t flags = kIsBreadthFirst;
+    if (mode != kStatsDisable) {
+        if (!root_bbox.empty()) flags |= kHasBBox;
+        if (minmax) flags |= kHasMinMax;
+        if (moments) flags |= kHasAverage | kHasStdDeviation;
+    }
+    put<uint32_t>(b, 20, flags);
+    put<uint32_t>(b, 28, 1);  // grid count
+    put<uint64_t>(b, 32, uint64_t(L.total));
+    std::memcpy(b + 40, name.data(), name.size());
+    put_map(b, 296, map);
+    put_world_bbox(b, map, root_bbox, mode != kStatsDisable && !root_bbox.empty());
+    put<uint32_t>(b, 632, 1);  // GridClass::LevelSet
+    put<uint32_t>(b, 636, 1);  // GridType::Float
+    put<int64_t>(b, 640, int64_t(L.total));  // no blind data
+}
+
+void write_index_top(uint8_t* b, const gbls_grid_desc& d, const std::string& name, int channels, bool stats,
+                     bool tiles, const std::vector<BBox>& upper_box, int64_t voxels, uint64_t count) {
+    const IndexLayout L(d.upper_count, d.lower_count, d.leaf_count, d.root_tile_count, channels, count);
+    const auto entries = root_entries(d);
+    BBox root_box;
+    for (size_t t = 0; t < entries.size(); ++t) {
+        const size_t at = L.root_at + kIndexRootBytes + kTileBytes * t;
+        put<uint64_t>(b, at, root_key(entry_origin(d, entries[t])));
+        if (entries[t].second) {
+            put<int64_t>(b, at + 8, int64_t(L.upper_at + kUpperBytes * size_t(entries[t].first)) - int64_t(L.root_at));
+            root_box.add(upper_box[size_t(entries[t].first)]);
+        }
+    }
+    put_bbox(b, L.root_at, root_box);
+    put<uint32_t>(b, L.root_at + 24, uint32_t(L.table));
+    if (tiles && stats && L.table > 0)  // the statistics pass resets an empty root's slots to 0
+        for (int k = 0; k < 4; ++k) put<uint64_t>(b, L.root_at + 40 + 8 * size_t(k), uint64_t(k + 1));
+    put_tree(b, L.tree_at, L.root_at, L.upper_at, L.lower_at, L.leaf_at, d.upper_count, d.lower_count, d.leaf_count,
+             voxels);
+    const MapD map = make_map(d);
+    put<uint64_t>(b, 0, kMagicGrid);
+    put<uint64_t>(b, 8, ~uint64_t(0));
+    put<uint32_t>(b, 16, kVersion);
+    put<uint32_t>(b, 20, kIsBreadthFirst | (root_box.empty() ? 0u : kHasBBox));
+    put<uint32_t>(b, 28, 1);
+    put<uint64_t>(b, 32, uint64_t(L.total));
+    std::memcpy(b + 40, name.data(), name.size());
+    put_map(b, 296, map);
+    put_world_bbox(b, map, root_box, !root_box.empty());
+    put<uint32_t>(b, 632, 8);   // GridClass::IndexGrid
+    put<uint32_t>(b, 636, 20);  // GridType::OnIndex
+    put<int64_t>(b, 640, channels ? int64_t(L.meta_at) : int64_t(L.total));
+    put<uint32_t>(b, 648, uint32_t(channels));
+    put<uint64_t>(b, 656, count);
+}
+
+void write_index_meta(uint8_t* m, const IndexLayout& L, int channels, uint64_t count) {
+    for (int ch = 0; ch < channels; ++ch) {
+        const size_t mat = L.meta_at + kBlindMetaBytes * size_t(ch), dat = L.blind_at + L.channel_bytes * size_t(ch);
+        const size_t at = kBlindMetaBytes * size_t(ch);
+        put<int64_t>(m, at, int64_t(dat) - int64_t(mat));
+        put<uint64_t>(m, at + 8, count);
+        put<uint32_t>(m, at + 16, 4);
+        put<uint32_t>(m, at + 20, 10);  // GridBlindDataSemantic::LevelSet
+        put<uint32_t>(m, at + 24, 4);   // GridBlindDataClass::ChannelArray
+        put<uint32_t>(m, at + 28, 1);   // GridType::Float
+        const std::string cn = "channel_" + std::to_string(ch);
+        std::memcpy(m + at + 32, cn.data(), cn.size());
+    }
+}
+
+namespace {
+
+std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int mode, int checksum) {
+    check_desc(d);
     if (mode < kStatsDisable || mode > kStatsAll) fail(GBLS_ERR_INVALID_ARGUMENT, "statistics mode must be 0-3");
     if (checksum < 0 || checksum > 2) fail(GBLS_ERR_INVALID_ARGUMENT, "checksum mode must be 0-2");
     if (name.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
-    const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count, nt = d.root_tile_count;
-    const size_t table = size_t(nu + nt);
-    const size_t tree_at = kGridBytes, root_at = tree_at + kTreeBytes;
-    const size_t upper_at = root_at + kRootBytes + kTileBytes * table;
-    const size_t lower_at = upper_at + kUpperBytes * size_t(nu);
-    const size_t leaf_at = lower_at + kLowerBytes * size_t(nl);
-    const size_t total = leaf_at + kLeafBytes * size_t(nf);
-    std::vector<uint8_t> b(total, 0);
+    const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count;
+    const FloatLayout L(nu, nl, nf, d.root_tile_count);
+    std::vector<uint8_t> b(L.total, 0);
     const bool minmax = mode >= kStatsMinMax, moments = mode == kStatsAll;
 
     // leaves
     std::vector<NodeStats> leaf_stats(static_cast<size_t>(nf));
+    int64_t voxels = 0;
     for (int64_t f = 0; f < nf; ++f) {
-        const size_t at = leaf_at + kLeafBytes * size_t(f);
+        const size_t at = L.leaf_at + kLeafBytes * size_t(f);
         const int32_t* o = d.leaf_origins + 3 * f;
         const uint64_t* m = d.leaf_masks + 8 * f;
         const float* v = d.leaf_values + 512 * f;
+        for (int w = 0; w < 8; ++w) voxels += __builtin_popcountll(m[w]);
         std::memcpy(b.data() + at, o, 12);
         std::memcpy(b.data() + at + 16, m, 64);
         std::memcpy(b.data() + at + 96, v, 2048);
@@ -291,7 +361,7 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
         std::memcpy(b.data() + at, ns.bbox.lo, 12);
         for (int k = 0; k < 3; ++k) b[at + 12 + k] = uint8_t(ns.bbox.hi[k] - ns.bbox.lo[k]);
         b[at + 15] = 2;  // has a bounding box; rendering enabled
-        put_stats(b, at + 80, ns.stats, mode);
+        put_stats(b.data(), at + 80, ns.stats, mode);
     }
 
     // internal nodes: child offsets, tile values, then statistics from the children
@@ -317,11 +387,12 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
                 if (is_child[size_t(n)]) fail(GBLS_ERR_INVALID_ARGUMENT, "grid descriptor is not in tree order");
                 is_child[size_t(n)] = 1;
                 b[at + 32 + size_t(nvals / 8) + size_t(n >> 3)] |= uint8_t(1u << (n & 7));  // child mask
-                put<int64_t>(b, at + table_at + 8 * size_t(n),
+                put<int64_t>(b.data(), at + table_at + 8 * size_t(n),
                              int64_t(child_base + child_bytes * size_t(c)) - int64_t(at));
             }
             for (int n = 0; n < nvals; ++n)
-                if (!is_child[size_t(n)]) put<float>(b, at + table_at + 8 * size_t(n), tiles[size_t(i) * size_t(nvals) + size_t(n)]);
+                if (!is_child[size_t(n)])
+                    put<float>(b.data(), at + table_at + 8 * size_t(n), tiles[size_t(i) * size_t(nvals) + size_t(n)]);
             if (mode == kStatsDisable) continue;
             NodeStats& total = out_stats[size_t(i)];
             // children are consecutive in tree order, which is their table order
@@ -329,119 +400,23 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
                 total.stats.add(child_stats[size_t(k)].stats, moments);
                 total.bbox.add(child_stats[size_t(k)].bbox);
             }
-            put_bbox(b, at, total.bbox);  // empty (max, min) when no child has active values
+            put_bbox(b.data(), at, total.bbox);  // empty (max, min) when no child has active values
             if (total.bbox.empty()) {
-                put<uint64_t>(b, at + 24, 1);  // no active values: skip rendering
+                put<uint64_t>(b.data(), at + 24, 1);  // no active values: skip rendering
                 continue;
             }
-            put<uint64_t>(b, at + 24, 2);
-            put_stats(b, at + 32 + size_t(nvals / 4), total.stats, mode);
+            put<uint64_t>(b.data(), at + 24, 2);
+            put_stats(b.data(), at + 32 + size_t(nvals / 4), total.stats, mode);
         }
         if (c != child_count) fail(GBLS_ERR_INVALID_ARGUMENT, "grid descriptor is not in tree order (orphan child node)");
     };
     std::vector<NodeStats> lower_stats, upper_stats;
-    internal(nl, lower_at, kLowerBytes, kLowerTableAt, 4, d.lower_origins, d.lower_tiles, nf, d.leaf_origins, leaf_at,
-             kLeafBytes, 3, leaf_stats, lower_stats);
-    internal(nu, upper_at, kUpperBytes, kUpperTableAt, 5, d.upper_origins, d.upper_tiles, nl, d.lower_origins,
-             lower_at, kLowerBytes, 7, lower_stats, upper_stats);
-
-    // root: children and tiles merged in Coord order
-    std::vector<std::pair<int64_t, bool>> entries;  // (index, is child)
-    for (int64_t i = 0; i < nu; ++i) entries.push_back({i, true});
-    for (int64_t i = 0; i < nt; ++i) entries.push_back({i, false});
-    auto origin_of = [&](const std::pair<int64_t, bool>& e) {
-        return e.second ? d.upper_origins + 3 * e.first : d.root_tile_origins + 3 * e.first;
-    };
-    std::stable_sort(entries.begin(), entries.end(), [&](const auto& a, const auto& c) {
-        const int32_t *p = origin_of(a), *q = origin_of(c);
-        return std::lexicographical_compare(p, p + 3, q, q + 3);
-    });
-    NodeStats root_total;
-    for (size_t t = 0; t < entries.size(); ++t) {
-        const size_t at = root_at + kRootBytes + kTileBytes * t;
-        const int32_t* o = origin_of(entries[t]);
-        put<uint64_t>(b, at, root_key(o));
-        if (entries[t].second) {
-            put<int64_t>(b, at + 8, int64_t(upper_at + kUpperBytes * size_t(entries[t].first)) - int64_t(root_at));
-            root_total.stats.add(upper_stats.empty() ? Stats() : upper_stats[size_t(entries[t].first)].stats, moments);
-            if (!upper_stats.empty()) root_total.bbox.add(upper_stats[size_t(entries[t].first)].bbox);
-        } else {
-            put<float>(b, at + 20, d.root_tile_values[entries[t].first]);
-        }
-    }
-    put<uint32_t>(b, root_at + 24, uint32_t(table));
-    put<float>(b, root_at + 28, d.background);
-    BBox root_bbox;
-    if (table == 0 || mode == kStatsDisable) {
-        put<float>(b, root_at + 32, d.background);
-        put<float>(b, root_at + 36, d.background);
-    } else {
-        root_bbox = root_total.bbox;
-        if (mode == kStatsBBox) {
-            put<float>(b, root_at + 32, d.background);
-            put<float>(b, root_at + 36, d.background);
-        } else {
-            put_stats(b, root_at + 32, root_total.stats, mode);
-        }
-    }
-    put_bbox(b, root_at, root_bbox);
-
-    // tree
-    int64_t voxels = 0;
-    for (int64_t f = 0; f < nf; ++f)
-        for (int w = 0; w < 8; ++w) voxels += __builtin_popcountll(d.leaf_masks[8 * f + w]);
-    put<int64_t>(b, tree_at, nf ? int64_t(leaf_at - tree_at) : 0);
-    put<int64_t>(b, tree_at + 8, nl ? int64_t(lower_at - tree_at) : 0);
-    put<int64_t>(b, tree_at + 16, nu ? int64_t(upper_at - tree_at) : 0);
-    put<int64_t>(b, tree_at + 24, int64_t(root_at - tree_at));
-    put<uint32_t>(b, tree_at + 32, uint32_t(nf));
-    put<uint32_t>(b, tree_at + 36, uint32_t(nl));
-    put<uint32_t>(b, tree_at + 40, uint32_t(nu));
-    put<uint64_t>(b, tree_at + 56, uint64_t(voxels));
-
-    // grid
-    const MapD map = make_map(d);
-    put<uint64_t>(b, 0, kMagicGrid);
-    put<uint64_t>(b, 8, ~uint64_t(0));
-    put<uint32_t>(b, 16, kVersion);
-    uint32_t flags = kIsBreadthFirst;
-    if (mode != kStatsDisable) {
-        if (!root_bbox.empty()) flags |= kHasBBox;
-        if (minmax) flags |= kHasMinMax;
-        if (moments) flags |= kHasAverage | kHasStdDeviation;
-    }
-    put<uint32_t>(b, 20, flags);
-    put<uint32_t>(b, 28, 1);  // grid count
-    put<uint64_t>(b, 32, uint64_t(total));
-    std::memcpy(b.data() + 40, name.data(), name.size());
-    put_map(b, 296, map);
-    double wlo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, whi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    if (mode != kStatsDisable && !root_bbox.empty()) {
-        const int32_t lo[3] = {root_bbox.lo[0], root_bbox.lo[1], root_bbox.lo[2]};
-        const int32_t hi[3] = {root_bbox.hi[0] + 1, root_bbox.hi[1] + 1, root_bbox.hi[2] + 1};
-        for (int corner = 0; corner < 8; ++corner) {
-            const double p[3] = {double((corner & 4) ? hi[0] : lo[0]), double((corner & 2) ? hi[1] : lo[1]),
-                                 double((corner & 1) ? hi[2] : lo[2])};
-            double w[3];
-            map.apply(p, w);
-            for (int k = 0; k < 3; ++k) {
-                wlo[k] = std::min(wlo[k], w[k]);
-                whi[k] = std::max(whi[k], w[k]);
-            }
-        }
-    }
-    for (int k = 0; k < 3; ++k) {
-        put<double>(b, 560 + 8 * k, wlo[k]);
-        put<double>(b, 584 + 8 * k, whi[k]);
-    }
-    const double one[3] = {1.0, 1.0, 1.0}, zero[3] = {0.0, 0.0, 0.0};
-    double a1[3], a0[3];
-    map.apply(one, a1);
-    map.apply(zero, a0);
-    for (int k = 0; k < 3; ++k) put<double>(b, 608 + 8 * k, a1[k] - a0[k]);
-    put<uint32_t>(b, 632, 1);  // GridClass::LevelSet
-    put<uint32_t>(b, 636, 1);  // GridType::Float
-    put<int64_t>(b, 640, int64_t(total));  // no blind data
+    internal(nl, L.lower_at, kLowerBytes, kLowerTableAt, 4, d.lower_origins, d.lower_tiles, nf, d.leaf_origins,
+             L.leaf_at, kLeafBytes, 3, leaf_stats, lower_stats);
+    internal(nu, L.upper_at, kUpperBytes, kUpperTableAt, 5, d.upper_origins, d.upper_tiles, nl, d.lower_origins,
+             L.lower_at, kLowerBytes, 7, lower_stats, upper_stats);
+    if (mode == kStatsDisable) upper_stats.clear();
+    write_float_top(b.data(), d, name, mode, upper_stats, voxels);
     put_checksum(b, checksum);
     return b;
 }
@@ -459,8 +434,7 @@ std::vector<uint8_t> build(const gbls_grid_desc& d, const std::string& name, int
 // StatsMode::BBox, as the converter does for index grids).
 std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& name, int channels, bool stats,
                                  bool tiles, int checksum) {
-    if (d.leaf_count < 0 || d.lower_count < 0 || d.upper_count < 0 || d.root_tile_count < 0)
-        fail(GBLS_ERR_INVALID_ARGUMENT, "negative count in grid descriptor");
+    check_desc(d);
     if (channels < 0) fail(GBLS_ERR_INVALID_ARGUMENT, "negative channel count");
     // The converter fills channel i > 0 from (its own start - value count),
     // which reads across the previous channel's alignment padding: only 0 or 1
@@ -468,7 +442,7 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
     if (channels > 1) fail(GBLS_ERR_UNSUPPORTED, "more than one value channel");
     if (checksum < 0 || checksum > 2) fail(GBLS_ERR_INVALID_ARGUMENT, "checksum mode must be 0-2");
     if (name.size() >= 256) fail(GBLS_ERR_UNSUPPORTED, "grid names of 256 characters or more (blind-data names)");
-    const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count, nt = d.root_tile_count;
+    const int64_t nu = d.upper_count, nl = d.lower_count, nf = d.leaf_count;
     const uint64_t nstat = stats ? 4 : 0;
     // value offsets (countValues / countTileValues)
     uint64_t count = 1;
@@ -487,32 +461,24 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
         leaf_off[size_t(f)] = count;
         count += uint64_t(a) + nstat;
     }
-    const size_t table = size_t(nu + nt);
-    const size_t tree_at = kGridBytes, root_at = tree_at + kTreeBytes;
-    const size_t upper_at = root_at + 96 + kTileBytes * table;
-    const size_t lower_at = upper_at + kUpperBytes * size_t(nu);
-    const size_t leaf_at = lower_at + kLowerBytes * size_t(nl);
-    const size_t meta_at = leaf_at + 96 * size_t(nf);
-    const size_t blind_at = meta_at + 288 * size_t(channels);
-    const size_t channel_bytes = (count * 4 + 31) / 32 * 32;
-    const size_t total = blind_at + channel_bytes * size_t(channels);
-    std::vector<uint8_t> b(total, 0);
+    const IndexLayout L(nu, nl, nf, d.root_tile_count, channels, count);
+    std::vector<uint8_t> b(L.total, 0);
 
     // leaves: origin, mask, offset, prefix sums; bounding boxes
     std::vector<BBox> leaf_box(static_cast<size_t>(nf));
     for (int64_t f = 0; f < nf; ++f) {
-        const size_t at = leaf_at + 96 * size_t(f);
+        const size_t at = L.leaf_at + kIndexLeafBytes * size_t(f);
         const int32_t* o = d.leaf_origins + 3 * f;
         const uint64_t* m = d.leaf_masks + 8 * f;
         std::memcpy(b.data() + at, o, 12);
         std::memcpy(b.data() + at + 16, m, 64);
-        put<uint64_t>(b, at + 80, leaf_off[size_t(f)]);
+        put<uint64_t>(b.data(), at + 80, leaf_off[size_t(f)]);
         uint64_t sum = uint64_t(__builtin_popcountll(m[0])), prefix = sum;
         for (int w = 1, sh = 9; w < 7; ++w, sh += 9) {
             sum += uint64_t(__builtin_popcountll(m[w]));
             prefix |= sum << sh;
         }
-        put<uint64_t>(b, at + 88, prefix);
+        put<uint64_t>(b.data(), at + 88, prefix);
         uint8_t flags = stats ? 16 : 0;
         BBox& bx = leaf_box[size_t(f)];
         for (int i = 0; i < 512; ++i) {
@@ -548,68 +514,29 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
                 const int n = ((((co[0] - o[0]) >> child_shift) << (2 * log2)) | (((co[1] - o[1]) >> child_shift) << log2) |
                                ((co[2] - o[2]) >> child_shift));
                 b[at + 32 + size_t(nvals / 8) + size_t(n >> 3)] |= uint8_t(1u << (n & 7));
-                put<int64_t>(b, at + table_at + 8 * size_t(n), int64_t(child_base + child_bytes * size_t(c)) - int64_t(at));
+                put<int64_t>(b.data(), at + table_at + 8 * size_t(n), int64_t(child_base + child_bytes * size_t(c)) - int64_t(at));
                 out_box[size_t(i)].add(child_box[size_t(c)]);
             }
             if (tiles && stats)
-                for (int k = 0; k < 4; ++k) put<uint64_t>(b, at + 32 + size_t(nvals / 4) + 8 * size_t(k), offs[size_t(i)] + uint64_t(k));
-            put_bbox(b, at, out_box[size_t(i)]);
-            put<uint64_t>(b, at + 24, out_box[size_t(i)].empty() ? 1 : 2);
+                for (int k = 0; k < 4; ++k)
+                    put<uint64_t>(b.data(), at + 32 + size_t(nvals / 4) + 8 * size_t(k), offs[size_t(i)] + uint64_t(k));
+            put_bbox(b.data(), at, out_box[size_t(i)]);
+            put<uint64_t>(b.data(), at + 24, out_box[size_t(i)].empty() ? 1 : 2);
         }
         if (c != child_count) fail(GBLS_ERR_INVALID_ARGUMENT, "grid descriptor is not in tree order (orphan child node)");
     };
     std::vector<BBox> lower_box, upper_box;
-    internal(nl, lower_at, kLowerBytes, kLowerTableAt, 4, d.lower_origins, lower_off, nf, d.leaf_origins, leaf_at, 96, 3,
-             leaf_box, lower_box);
-    internal(nu, upper_at, kUpperBytes, kUpperTableAt, 5, d.upper_origins, upper_off, nl, d.lower_origins, lower_at,
-             kLowerBytes, 7, lower_box, upper_box);
-    // root
-    std::vector<std::pair<int64_t, bool>> entries;
-    for (int64_t i = 0; i < nu; ++i) entries.push_back({i, true});
-    for (int64_t i = 0; i < nt; ++i) entries.push_back({i, false});
-    auto origin_of = [&](const std::pair<int64_t, bool>& e) {
-        return e.second ? d.upper_origins + 3 * e.first : d.root_tile_origins + 3 * e.first;
-    };
-    std::stable_sort(entries.begin(), entries.end(), [&](const auto& a2, const auto& c2) {
-        const int32_t *p = origin_of(a2), *q = origin_of(c2);
-        return std::lexicographical_compare(p, p + 3, q, q + 3);
-    });
-    BBox root_box;
-    for (size_t t = 0; t < entries.size(); ++t) {
-        const size_t at = root_at + 96 + kTileBytes * t;
-        put<uint64_t>(b, at, root_key(origin_of(entries[t])));
-        if (entries[t].second) {
-            put<int64_t>(b, at + 8, int64_t(upper_at + kUpperBytes * size_t(entries[t].first)) - int64_t(root_at));
-            root_box.add(upper_box[size_t(entries[t].first)]);
-        }
-    }
-    put_bbox(b, root_at, root_box);
-    put<uint32_t>(b, root_at + 24, uint32_t(table));
-    if (tiles && stats && table > 0)  // the statistics pass resets an empty root's slots to 0
-        for (int k = 0; k < 4; ++k) put<uint64_t>(b, root_at + 40 + 8 * size_t(k), uint64_t(k + 1));
-    // tree
+    internal(nl, L.lower_at, kLowerBytes, kLowerTableAt, 4, d.lower_origins, lower_off, nf, d.leaf_origins, L.leaf_at,
+             kIndexLeafBytes, 3, leaf_box, lower_box);
+    internal(nu, L.upper_at, kUpperBytes, kUpperTableAt, 5, d.upper_origins, upper_off, nl, d.lower_origins,
+             L.lower_at, kLowerBytes, 7, lower_box, upper_box);
     int64_t voxels = 0;
     for (int a : active) voxels += a;
-    put<int64_t>(b, tree_at, nf ? int64_t(leaf_at - tree_at) : 0);
-    put<int64_t>(b, tree_at + 8, nl ? int64_t(lower_at - tree_at) : 0);
-    put<int64_t>(b, tree_at + 16, nu ? int64_t(upper_at - tree_at) : 0);
-    put<int64_t>(b, tree_at + 24, int64_t(root_at - tree_at));
-    put<uint32_t>(b, tree_at + 32, uint32_t(nf));
-    put<uint32_t>(b, tree_at + 36, uint32_t(nl));
-    put<uint32_t>(b, tree_at + 40, uint32_t(nu));
-    put<uint64_t>(b, tree_at + 56, uint64_t(voxels));
+    write_index_top(b.data(), d, name, channels, stats, tiles, upper_box, voxels, count);
     // value channels
+    write_index_meta(b.data() + L.meta_at, L, channels, count);
     for (int ch = 0; ch < channels; ++ch) {
-        const size_t mat = meta_at + 288 * size_t(ch), dat = blind_at + channel_bytes * size_t(ch);
-        put<int64_t>(b, mat, int64_t(dat) - int64_t(mat));
-        put<uint64_t>(b, mat + 8, count);
-        put<uint32_t>(b, mat + 16, 4);
-        put<uint32_t>(b, mat + 20, 10);  // GridBlindDataSemantic::LevelSet
-        put<uint32_t>(b, mat + 24, 4);   // GridBlindDataClass::ChannelArray
-        put<uint32_t>(b, mat + 28, 1);   // GridType::Float
-        const std::string cn = "channel_" + std::to_string(ch);
-        std::memcpy(b.data() + mat + 32, cn.data(), cn.size());
-        float* v = reinterpret_cast<float*>(b.data() + dat);
+        float* v = reinterpret_cast<float*>(b.data() + L.blind_at + L.channel_bytes * size_t(ch));
         const float bg = d.background;
         v[0] = bg;
         if (tiles && stats) {
@@ -625,87 +552,58 @@ std::vector<uint8_t> build_index(const gbls_grid_desc& d, const std::string& nam
             for (uint64_t k = 0; k < nstat; ++k) v[o++] = bg;
         }
     }
-    // grid
-    const MapD map = make_map(d);
-    put<uint64_t>(b, 0, kMagicGrid);
-    put<uint64_t>(b, 8, ~uint64_t(0));
-    put<uint32_t>(b, 16, kVersion);
-    put<uint32_t>(b, 20, kIsBreadthFirst | (root_box.empty() ? 0u : kHasBBox));
-    put<uint32_t>(b, 28, 1);
-    put<uint64_t>(b, 32, uint64_t(total));
-    std::memcpy(b.data() + 40, name.data(), name.size());
-    put_map(b, 296, map);
-    double wlo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, whi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    if (!root_box.empty()) {
-        for (int corner = 0; corner < 8; ++corner) {
-            const double p[3] = {double((corner & 4) ? root_box.hi[0] + 1 : root_box.lo[0]),
-                                 double((corner & 2) ? root_box.hi[1] + 1 : root_box.lo[1]),
-                                 double((corner & 1) ? root_box.hi[2] + 1 : root_box.lo[2])};
-            double w[3];
-            map.apply(p, w);
-            for (int k = 0; k < 3; ++k) {
-                wlo[k] = std::min(wlo[k], w[k]);
-                whi[k] = std::max(whi[k], w[k]);
-            }
-        }
-    }
-    for (int k = 0; k < 3; ++k) {
-        put<double>(b, 560 + 8 * k, wlo[k]);
-        put<double>(b, 584 + 8 * k, whi[k]);
-    }
-    const double one[3] = {1.0, 1.0, 1.0}, zero[3] = {0.0, 0.0, 0.0};
-    double a1[3], a0[3];
-    map.apply(one, a1);
-    map.apply(zero, a0);
-    for (int k = 0; k < 3; ++k) put<double>(b, 608 + 8 * k, a1[k] - a0[k]);
-    put<uint32_t>(b, 632, 8);   // GridClass::IndexGrid
-    put<uint32_t>(b, 636, 20);  // GridType::OnIndex
-    put<int64_t>(b, 640, channels ? int64_t(meta_at) : int64_t(total));
-    put<uint32_t>(b, 648, uint32_t(channels));
-    put<uint64_t>(b, 656, count);
     put_checksum(b, checksum);
     return b;
 }
 
+}  // namespace
 
 // NanoGrid<float> -> exchange layout (the direction of
 // nanovdb::tools::nanoToOpenVDB, nanovdb/tools/NanoToOpenVDB.h): the tree is
 // walked through its links -- root table in Coord order, then child masks in
 // slot order -- so the result is in tree order whatever the buffer's node
-// layout; node origins come from the root keys and the slot indices.
-template <class T> inline T get(const uint8_t* b, size_t at) {
-    T v;
-    std::memcpy(&v, b + at, sizeof(T));
-    return v;
-}
-
-gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
+// layout; node origins come from the root keys and the slot indices.  The
+// walk reads whole records (headers, root tiles, nodes, leaves) through
+// `read`, so a device buffer is downloaded node by node and its leaves are
+// never read on the host when leaf_at is given.
+gbls_host_grid* import_float(const ByteReader& read, int64_t size, std::vector<uint64_t>* leaf_at) {
     auto need = [&](size_t at, size_t n) {
         if (at > size_t(size) || n > size_t(size) - at) fail(GBLS_ERR_RUNTIME, "truncated NanoVDB buffer");
     };
-    need(0, kGridBytes + kTreeBytes);
-    const uint64_t magic = get<uint64_t>(b, 0);
+    std::vector<uint8_t> rec;
+    auto fetch = [&](size_t at, size_t n) -> const uint8_t* {
+        need(at, n);
+        rec.resize(n + 1);
+        if (n) read(at, n, rec.data());
+        return rec.data();
+    };
+    auto get = [](const uint8_t* p, size_t at, auto v) {
+        std::memcpy(&v, p + at, sizeof(v));
+        return v;
+    };
+    const uint8_t* b = fetch(0, kGridBytes + kTreeBytes);
+    const uint64_t magic = get(b, 0, uint64_t());
     if (magic != kMagicGrid && magic != 0x304244566f6e614eULL) fail(GBLS_ERR_RUNTIME, "not a NanoVDB grid");
-    if ((get<uint32_t>(b, 16) >> 21) != 32) fail(GBLS_ERR_UNSUPPORTED, "NanoVDB major version other than 32");
-    if (get<uint32_t>(b, 636) != 1) fail(GBLS_ERR_UNSUPPORTED, "not a NanoGrid<float>");
+    if ((get(b, 16, uint32_t()) >> 21) != 32) fail(GBLS_ERR_UNSUPPORTED, "NanoVDB major version other than 32");
+    if (get(b, 636, uint32_t()) != 1) fail(GBLS_ERR_UNSUPPORTED, "not a NanoGrid<float>");
     double mat[9], vec[3];
-    for (int k = 0; k < 9; ++k) mat[k] = get<double>(b, 296 + 88 + 8 * k);
-    for (int k = 0; k < 3; ++k) vec[k] = get<double>(b, 296 + 232 + 8 * k);
+    for (int k = 0; k < 9; ++k) mat[k] = get(b, 296 + 88 + 8 * k, double());
+    for (int k = 0; k < 3; ++k) vec[k] = get(b, 296 + 232 + 8 * k, double());
     if (mat[1] != 0 || mat[2] != 0 || mat[3] != 0 || mat[5] != 0 || mat[6] != 0 || mat[7] != 0)
         fail(GBLS_ERR_UNSUPPORTED, "rotated or sheared NanoVDB map");
     if (!(mat[0] == mat[4] && mat[4] == mat[8]) || !(mat[0] > 0))
         fail(GBLS_ERR_RUNTIME, "The transform must have uniform scale for the LevelSetTracker to function");
+    const size_t root_at = kGridBytes + size_t(get(b, kGridBytes + 24, int64_t()));
     auto* g = new gbls_host_grid;
     try {
         g->voxel_size = mat[0];
         for (int k = 0; k < 3; ++k) g->translation[k] = vec[k];
         g->map_type = (vec[0] == 0 && vec[1] == 0 && vec[2] == 0) ? GBLS_MAP_UNIFORM_SCALE
                                                                  : GBLS_MAP_UNIFORM_SCALE_TRANSLATE;
-        const size_t root_at = kGridBytes + size_t(get<int64_t>(b, kGridBytes + 24));
-        need(root_at, kRootBytes);
-        const uint32_t table = get<uint32_t>(b, root_at + 24);
-        need(root_at + kRootBytes, size_t(table) * kTileBytes);
-        g->background = get<float>(b, root_at + 28);
+        b = fetch(root_at, kRootBytes);
+        const uint32_t table = get(b, 24, uint32_t());
+        g->background = get(b, 28, float());
+        b = fetch(root_at + kRootBytes, size_t(table) * kTileBytes);
         struct Entry {
             int32_t o[3];
             int64_t child;
@@ -713,15 +611,15 @@ gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
         };
         std::vector<Entry> entries(table);
         for (uint32_t t = 0; t < table; ++t) {
-            const size_t at = root_at + kRootBytes + kTileBytes * t;
-            const uint64_t key = get<uint64_t>(b, at);
+            const size_t at = kTileBytes * t;
+            const uint64_t key = get(b, at, uint64_t());
             Entry& e = entries[t];
             e.o[0] = int32_t(uint32_t(((key >> 42) & 0x1FFFFF) << 12));
             e.o[1] = int32_t(uint32_t(((key >> 21) & 0x1FFFFF) << 12));
             e.o[2] = int32_t(uint32_t((key & 0x1FFFFF) << 12));
-            e.child = get<int64_t>(b, at + 8);
-            if (!e.child && get<uint32_t>(b, at + 16)) fail(GBLS_ERR_UNSUPPORTED, "active root tile in a level set");
-            e.value = get<float>(b, at + 20);
+            e.child = get(b, at + 8, int64_t());
+            if (!e.child && get(b, at + 16, uint32_t())) fail(GBLS_ERR_UNSUPPORTED, "active root tile in a level set");
+            e.value = get(b, at + 20, float());
         }
         std::sort(entries.begin(), entries.end(), [](const Entry& x, const Entry& y) {
             return std::lexicographical_compare(x.o, x.o + 3, y.o, y.o + 3);
@@ -733,9 +631,9 @@ gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
         };
         auto node = [&](size_t at, int log2, size_t bytes, size_t table_at, const int32_t* origin, int child_shift,
                         std::vector<float>& tiles, std::vector<Child>& children) {
-            need(at, bytes);
+            const uint8_t* nb = fetch(at, bytes);
             const int nvals = 1 << (3 * log2), dim = 1 << log2;
-            const uint8_t* vmask = b + at + 32;
+            const uint8_t* vmask = nb + 32;
             const uint8_t* cmask = vmask + nvals / 8;
             const size_t base = tiles.size();
             tiles.resize(base + size_t(nvals), 0.0f);
@@ -743,13 +641,13 @@ gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
                 if ((vmask[n >> 3] >> (n & 7)) & 1) fail(GBLS_ERR_UNSUPPORTED, "active tile in a level set");
                 if ((cmask[n >> 3] >> (n & 7)) & 1) {
                     Child c;
-                    c.at = size_t(int64_t(at) + get<int64_t>(b, at + table_at + 8 * size_t(n)));
+                    c.at = size_t(int64_t(at) + get(nb, table_at + 8 * size_t(n), int64_t()));
                     c.o[0] = origin[0] + (((n >> (2 * log2)) & (dim - 1)) << child_shift);
                     c.o[1] = origin[1] + (((n >> log2) & (dim - 1)) << child_shift);
                     c.o[2] = origin[2] + ((n & (dim - 1)) << child_shift);
                     children.push_back(c);
                 } else {
-                    tiles[base + size_t(n)] = get<float>(b, at + table_at + 8 * size_t(n));
+                    tiles[base + size_t(n)] = get(nb, table_at + 8 * size_t(n), float());
                 }
             }
         };
@@ -767,13 +665,18 @@ gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
                 std::vector<Child> leaves;
                 node(lo.at, 4, kLowerBytes, kLowerTableAt, lo.o, 3, g->lower_tiles, leaves);
                 for (const Child& lf : leaves) {
-                    need(lf.at, kLeafBytes);
-                    const size_t f = g->leaf_origins.size() / 3;
                     g->leaf_origins.insert(g->leaf_origins.end(), lf.o, lf.o + 3);
+                    if (leaf_at) {
+                        need(lf.at, kLeafBytes);
+                        leaf_at->push_back(uint64_t(lf.at));
+                        continue;
+                    }
+                    const uint8_t* lb = fetch(lf.at, kLeafBytes);
+                    const size_t f = g->leaf_origins.size() / 3 - 1;
                     g->leaf_masks.resize(8 * (f + 1));
-                    std::memcpy(g->leaf_masks.data() + 8 * f, b + lf.at + 16, 64);
+                    std::memcpy(g->leaf_masks.data() + 8 * f, lb + 16, 64);
                     g->leaf_values.resize(512 * (f + 1));
-                    std::memcpy(g->leaf_values.data() + 512 * f, b + lf.at + 96, 2048);
+                    std::memcpy(g->leaf_values.data() + 512 * f, lb + 96, 2048);
                 }
             }
         }
@@ -784,7 +687,11 @@ gbls_host_grid* import_float(const uint8_t* b, int64_t size) {
     }
 }
 
+namespace {
 }  // namespace
+}  // namespace gbls_nano
+
+using namespace gbls_nano;
 
 extern "C" {
 
@@ -833,7 +740,8 @@ int gbls_nanovdb_export_index(const gbls_grid_desc* desc, const char* name, int3
 int gbls_nanovdb_import(const uint8_t* buffer, int64_t size, gbls_host_grid** out) {
     try {
         if (!buffer || !out || size < 0) fail(GBLS_ERR_INVALID_ARGUMENT, "null argument");
-        *out = import_float(buffer, size);
+        const ByteReader read = [buffer](size_t at, size_t n, uint8_t* dst) { std::memcpy(dst, buffer + at, n); };
+        *out = import_float(read, size, nullptr);
         return GBLS_OK;
     } catch (const ExportError& e) {
         gbls_host::set_error(e.msg);

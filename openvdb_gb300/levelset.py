@@ -61,6 +61,18 @@ class DeviceLevelSet:
         self._keep = None
         self.voxel_size = grid.voxel_size
         self.background = grid.background
+        self.device = int(device)
+
+    @classmethod
+    def _adopt(cls, handle, voxel_size, background, device):
+        """A DeviceLevelSet owning an already created gbls_handle."""
+        obj = cls.__new__(cls)
+        obj._h = handle
+        obj._keep = None
+        obj.voxel_size = voxel_size
+        obj.background = background
+        obj.device = int(device)
+        return obj
 
     @property
     def handle(self):
@@ -140,6 +152,7 @@ class DeviceVolume(DeviceLevelSet):
         self._keep = None
         self.voxel_size = grid.voxel_size
         self.background = grid.background
+        self.device = int(device)
 
 
 class VolumeAdvection:
@@ -552,6 +565,7 @@ class DeviceBatch:
         _call(L.gbls_batch_create(len(self._keep), descs, C.byref(self._h)))
         self._keep = None
         self.n = len(descs)
+        self.device = int(device)
 
     @property
     def handle(self):

@@ -6,6 +6,12 @@ createNanoGrid(openvdb::FloatGrid, StatsMode, CheckMode) writes
 (nanovdb/tools/CreateNanoGrid.h:162-168), so NanoVDB readers, renderers and
 GPU samplers take it unchanged.  to_device(grid) places the same buffer in
 device memory (a torch uint8 tensor) for CUDA consumers of NanoVDB.
+
+export_device(level_set) and export_index_device(level_set) write the
+buffers on the device straight from a DeviceLevelSet (or a DeviceBatch
+instance), the same bytes as the host exporters of its downloaded grid;
+from_device(buffer) makes a DeviceLevelSet from a NanoGrid<float> buffer in
+device (or host) memory, its leaves gathered on the device.
 """
 import ctypes as C
 
@@ -60,3 +66,71 @@ def to_device(grid, name="", stats="all", checksum="partial", device="cuda"):
     """The same buffer as a torch uint8 tensor on `device`."""
     import torch
     return torch.from_numpy(to_nanovdb(grid, name, stats, checksum)).to(device)
+
+
+def _device_buffer(level_set, fn, args):
+    """Size query, allocation and fill of a device buffer by a
+    gbls_nanovdb_export*_device entry point."""
+    import torch
+    L = lib()
+    n = C.c_int64()
+    check(fn(level_set.handle, *args, None, 0, C.byref(n)))
+    dev = torch.device("cuda", getattr(level_set, "device", 0))
+    buf = torch.empty(n.value, dtype=torch.uint8, device=dev)
+    torch.cuda.current_stream(dev).synchronize()  # the allocation may reuse memory of pending work
+    check(fn(level_set.handle, *args, C.c_void_p(buf.data_ptr()), n.value, C.byref(n)))
+    return buf
+
+
+def export_device(level_set, name="", stats="all", checksum="partial", instance=-1):
+    """NanoGrid<float> of a DeviceLevelSet (instance -1) or of instance i of a
+    DeviceBatch, written on the device: a torch uint8 CUDA tensor."""
+    L = lib()
+    return _device_buffer(level_set, L.gbls_nanovdb_export_device,
+                          (int(instance), name.encode(), STATS[stats], CHECKSUM[checksum]))
+
+
+def export_index_device(level_set, name="", channel=True, include_stats=True, include_tiles=True,
+                        checksum="partial", instance=-1):
+    """NanoGrid<ValueOnIndex> (with the value channel) of a device level set,
+    written on the device."""
+    L = lib()
+    return _device_buffer(level_set, L.gbls_nanovdb_export_index_device,
+                          (int(instance), name.encode(), int(bool(channel)), int(bool(include_stats)),
+                           int(bool(include_tiles)), CHECKSUM[checksum]))
+
+
+def from_device(buffer, device=0):
+    """DeviceLevelSet of a NanoGrid<float> buffer: a torch uint8 tensor (CUDA
+    or CPU) or a numpy array."""
+    import struct
+    from .levelset import DeviceLevelSet, _call
+    L = lib()
+    try:
+        import torch
+        is_tensor = isinstance(buffer, torch.Tensor)
+    except ImportError:
+        is_tensor = False
+    if is_tensor:
+        if buffer.dtype != torch.uint8 or not buffer.is_contiguous():
+            raise ValueError("a contiguous uint8 tensor is expected")
+        if buffer.is_cuda:
+            torch.cuda.current_stream(buffer.device).synchronize()
+        ptr, size = buffer.data_ptr(), buffer.numel()
+        head = bytes(buffer[:min(size, 800)].cpu().numpy())
+        keep = buffer
+    else:
+        a = np.ascontiguousarray(buffer, dtype=np.uint8)
+        ptr, size = a.ctypes.data, a.size
+        head = a[:800].tobytes()
+        keep = a
+    _call(L.gbls_set_device(int(device)))
+    h = C.c_void_p()
+    _call(L.gbls_create_from_nanovdb(C.c_void_p(ptr), size, C.byref(h)))
+    del keep
+    # the map's scale (the double matrix) and the root's background
+    voxel_size = struct.unpack_from("<d", head, 296 + 88)[0]
+    root_at = 672 + struct.unpack_from("<q", head, 672 + 24)[0]
+    background = struct.unpack_from("<f", head, root_at + 28)[0] if root_at + 32 <= len(head) else None
+    return DeviceLevelSet._adopt(h, voxel_size, background, device)
+
