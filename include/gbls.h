@@ -567,6 +567,16 @@ int gbls_nanovdb_export_index_device(gbls_handle* h, int32_t instance, const cha
  * on the device.  A device buffer must be 32-byte aligned.  Errors as
  * gbls_nanovdb_import and gbls_create.                                       */
 int gbls_create_from_nanovdb(const void* buffer, int64_t size, gbls_handle** out);
+/* A device consumer of those buffers: nanovdb::ReadAccessor::getValue and
+ * isActive (nanovdb/NanoVDB.h) at n index coordinates ijk[3i..3i+2], for a
+ * NanoGrid<float> (values) or a NanoGrid<ValueOnIndex> (indices into its
+ * value array: the LeafData<ValueOnIndex>::getValue decode,
+ * nanovdb/NanoVDB.h:4144-4170).  grid, ijk and the outputs are device
+ * arrays (active may be NULL); runs on `stream` (NULL: the default stream)
+ * and returns when done.  Every read is bounds-checked against `size`:
+ * GBLS_ERR_RUNTIME for a truncated or corrupt buffer.                      */
+int gbls_nanovdb_probe(const void* grid, int64_t size, const int32_t* ijk, int64_t n, float* values,
+                       uint64_t* indices, uint8_t* active, void* stream);
 
 #ifdef __cplusplus
 }

@@ -100,6 +100,7 @@ def lib():
         "gbls_nanovdb_export_index_device": ([vp, C.c_int32, C.c_char_p, C.c_int32, C.c_int32, C.c_int32,
                                               C.c_int32, vp, C.c_int64, P(C.c_int64)], C.c_int),
         "gbls_create_from_nanovdb": ([vp, C.c_int64, P(vp)], C.c_int),
+        "gbls_nanovdb_probe": ([vp, C.c_int64, vp, C.c_int64, vp, vp, vp, vp], C.c_int),
         "gbls_nanovdb_export_index": ([P(_abi.GridDesc), C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                        vp, C.c_int64, P(C.c_int64)], C.c_int),
     }

@@ -4157,6 +4157,22 @@ int gbls_nanovdb_export_index_device(gbls_handle* h, int32_t instance, const cha
     });
 }
 
+int gbls_nanovdb_probe(const void* grid, int64_t size, const int32_t* ijk, int64_t n, float* values,
+                       uint64_t* indices, uint8_t* active, void* stream) {
+    if (!grid || size < 0 || n < 0 || (n > 0 && !ijk)) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        cudaPointerAttributes a{};
+        CU(cudaPointerGetAttributes(&a, grid));
+        if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+            fail(GBLS_ERR_INVALID_ARGUMENT, "the NanoVDB buffer is not device memory");
+        const int e = nano_probe(static_cast<const uint8_t*>(grid), uint64_t(size), ijk, n, values, indices, active,
+                                 static_cast<cudaStream_t>(stream));
+        if (e & 2) fail(GBLS_ERR_UNSUPPORTED, "neither a NanoGrid<float> nor a NanoGrid<ValueOnIndex>");
+        if (e & 4) fail(GBLS_ERR_INVALID_ARGUMENT, "no output array for the grid's value type");
+        if (e & 1) fail(GBLS_ERR_RUNTIME, "truncated or corrupt NanoVDB buffer");
+    });
+}
+
 int gbls_create_from_nanovdb(const void* buffer, int64_t size, gbls_handle** out) {
     if (!buffer || !out || size < 0) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     *out = nullptr;

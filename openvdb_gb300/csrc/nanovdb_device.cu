@@ -295,6 +295,122 @@ k_gather_leaves(const uint8_t* buf, const uint64_t* at, int64_t n, uint64_t* mas
     for (int j = tid; j < LEAF_VOX / 4; j += LEAF_THREADS) o[j] = v[j];
 }
 
+// Bounds-checked reads of a probed buffer (any alignment).
+struct NanoBytes {
+    const uint8_t* b;
+    uint64_t size;
+    template <class T>
+    __device__ bool get(uint64_t at, T& v) const {
+        if (at > size || sizeof(T) > size - at) return false;
+        memcpy(&v, b + at, sizeof(T));
+        return true;
+    }
+    __device__ bool bit(uint64_t at, uint32_t n, bool& v) const {
+        uint8_t byte = 0;
+        const bool ok = get(at + (n >> 3), byte);
+        v = (byte >> (n & 7)) & 1;
+        return ok;
+    }
+};
+
+// ReadAccessor::getValue / isActive of a NanoGrid<float> (type 1) or
+// NanoGrid<ValueOnIndex> (type 20) at one index coordinate: root tiles
+// searched in table order by key, internal nodes through their child masks
+// and tables, the leaf's value (float) or its value index by the 9-bit
+// prefix-sum decode (nanovdb/NanoVDB.h:4144-4170).  err bit 1: a read
+// outside the buffer, bit 2: another grid type, bit 4: no output array for
+// the type.
+__global__ void k_probe(const uint8_t* buf, uint64_t size, const int32_t* ijk, int64_t n, float* fv, uint64_t* iv,
+                        uint8_t* act, int* err) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const NanoBytes g{buf, size};
+    uint32_t type = 0;
+    if (!g.get(636, type)) { atomicOr(err, 1); return; }
+    const bool isf = type == 1;
+    if (!isf && type != 20) { atomicOr(err, 2); return; }
+    if (isf ? !fv : !iv) { atomicOr(err, 4); return; }
+    const int32_t x = ijk[3 * i], y = ijk[3 * i + 1], z = ijk[3 * i + 2];
+    bool ok = true, active = false;
+    float fval = 0.0f;
+    uint64_t ival = 0;
+    int64_t rel = 0;
+    ok &= g.get(gbls_nano::kGridBytes + 24, rel);
+    const uint64_t root = gbls_nano::kGridBytes + uint64_t(rel);
+    uint32_t table = 0;
+    ok &= g.get(root + 24, table);
+    if (isf) ok &= g.get(root + 28, fval);  // background
+    else ok &= g.get(root + 32, ival);
+    const uint64_t tiles = root + (isf ? gbls_nano::kRootBytes : gbls_nano::kIndexRootBytes);
+    const uint64_t key = uint64_t(uint32_t(z) >> 12) | (uint64_t(uint32_t(y) >> 12) << 21) |
+                         (uint64_t(uint32_t(x) >> 12) << 42);
+    uint64_t node = 0;
+    for (uint32_t t = 0; ok && t < table; ++t) {
+        const uint64_t at = tiles + gbls_nano::kTileBytes * t;
+        uint64_t k = 0;
+        ok &= g.get(at, k);
+        if (k != key) continue;
+        int64_t child = 0;
+        ok &= g.get(at + 8, child);
+        if (child) {
+            node = root + uint64_t(child);
+        } else {
+            uint32_t state = 0;
+            ok &= g.get(at + 16, state);
+            active = state != 0;
+            if (isf) ok &= g.get(at + 20, fval);
+            else ok &= g.get(at + 24, ival);
+        }
+        break;
+    }
+    // upper (LOG2 5 over 7-bit children), then lower (LOG2 4 over leaves)
+    for (int level = 0; ok && node && level < 2; ++level) {
+        const int log2 = level == 0 ? 5 : 4, cshift = level == 0 ? 7 : 3;
+        const uint32_t mask = (1u << (log2 + cshift)) - 1u, nv = 1u << (3 * log2);
+        const uint32_t slot = (((uint32_t(x) & mask) >> cshift) << (2 * log2)) |
+                              (((uint32_t(y) & mask) >> cshift) << log2) | ((uint32_t(z) & mask) >> cshift);
+        const uint64_t tab = node + (level == 0 ? gbls_nano::kUpperTableAt : gbls_nano::kLowerTableAt);
+        bool is_child = false;
+        ok &= g.bit(node + 32 + nv / 8, slot, is_child);
+        if (is_child) {
+            int64_t off = 0;
+            ok &= g.get(tab + 8 * uint64_t(slot), off);
+            node += uint64_t(off);
+            continue;
+        }
+        ok &= g.bit(node + 32, slot, active);
+        if (isf) ok &= g.get(tab + 8 * uint64_t(slot), fval);
+        else ok &= g.get(tab + 8 * uint64_t(slot), ival);
+        node = 0;
+    }
+    if (ok && node) {  // a leaf
+        const uint32_t v = ((uint32_t(x) & 7u) << 6) | ((uint32_t(y) & 7u) << 3) | (uint32_t(z) & 7u);
+        uint64_t w = 0;
+        ok &= g.get(node + 16 + 8 * uint64_t(v >> 6), w);
+        const uint64_t bitm = uint64_t(1) << (v & 63u);
+        active = (w & bitm) != 0;
+        if (isf) {
+            ok &= g.get(node + 96 + 4 * uint64_t(v), fval);
+        } else if (!active) {
+            ival = 0;  // the background's index
+        } else {
+            uint64_t offset = 0, prefix = 0;
+            ok &= g.get(node + 80, offset);
+            ok &= g.get(node + 88, prefix);
+            uint32_t word = v >> 6;
+            ival = offset + uint64_t(__popcll(w & (bitm - 1u)));
+            if (word--) ival += (prefix >> (9u * word)) & 511u;
+        }
+    }
+    if (!ok) {
+        atomicOr(err, 1);
+        return;
+    }
+    if (isf) fv[i] = fval;
+    else iv[i] = ival;
+    if (act) act[i] = active ? 1 : 0;
+}
+
 template <class T>
 T* scratch(size_t n, cudaStream_t s) {
     void* p = nullptr;
@@ -403,6 +519,19 @@ void nano_gather_leaves(const uint8_t* buf, const uint64_t* at, int64_t n, uint6
     if (n <= 0) return;
     k_gather_leaves<<<unsigned(n), LEAF_THREADS, 0, s>>>(buf, at, n, masks, values);
     check(cudaGetLastError(), "k_gather_leaves");
+}
+
+int nano_probe(const uint8_t* buf, uint64_t size, const int32_t* ijk, int64_t n, float* values, uint64_t* indices,
+               uint8_t* active, cudaStream_t s) {
+    int* err = scratch<int>(1, s);
+    check(cudaMemsetAsync(err, 0, sizeof(int), s), "cudaMemsetAsync");
+    if (n > 0) k_probe<<<unsigned((n + 127) / 128), 128, 0, s>>>(buf, size, ijk, n, values, indices, active, err);
+    check(cudaGetLastError(), "k_probe");
+    int e = 0;
+    check(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s), "probe status");
+    check(cudaFreeAsync(err, s), "cudaFreeAsync");
+    check(cudaStreamSynchronize(s), "probe");
+    return e;
 }
 
 }  // namespace gbls

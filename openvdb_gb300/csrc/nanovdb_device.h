@@ -60,4 +60,12 @@ uint32_t nano_blocked_crc(const uint8_t* p, size_t n, cudaStream_t s);
 void nano_gather_leaves(const uint8_t* buf, const uint64_t* at, int64_t n, uint64_t* masks, float* values,
                         cudaStream_t s);
 
+// ReadAccessor::getValue / isActive of a NanoGrid<float> or
+// NanoGrid<ValueOnIndex> device buffer at n index coordinates (device
+// arrays): values for a float grid, indices for an index grid, active flags
+// when given.  Returns the kernel's error bits (1: a read outside the
+// buffer, 2: another grid type, 4: no output array for the type).
+int nano_probe(const uint8_t* buf, uint64_t size, const int32_t* ijk, int64_t n, float* values, uint64_t* indices,
+               uint8_t* active, cudaStream_t s);
+
 }  // namespace gbls

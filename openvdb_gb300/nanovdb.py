@@ -134,3 +134,23 @@ def from_device(buffer, device=0):
     background = struct.unpack_from("<f", head, root_at + 28)[0] if root_at + 32 <= len(head) else None
     return DeviceLevelSet._adopt(h, voxel_size, background, device)
 
+
+def probe(buffer, ijk):
+    """nanovdb::ReadAccessor getValue / isActive on a device NanoVDB buffer
+    (torch uint8 CUDA tensor) at index coordinates ijk (int32 CUDA tensor,
+    n x 3): (float32 values of a NanoGrid<float> or int64 value indices of a
+    NanoGrid<ValueOnIndex>, uint8 active flags), CUDA tensors."""
+    import torch
+    L = lib()
+    c = ijk.to(dtype=torch.int32).contiguous()
+    n = c.shape[0]
+    is_float = int(buffer[636:640].cpu().numpy().view(np.uint32)[0]) == 1
+    out = torch.empty(n, dtype=torch.float32 if is_float else torch.int64, device=buffer.device)
+    act = torch.empty(n, dtype=torch.uint8, device=buffer.device)
+    stream = torch.cuda.current_stream(buffer.device)
+    ptr = C.c_void_p(out.data_ptr())
+    check(L.gbls_nanovdb_probe(C.c_void_p(buffer.data_ptr()), buffer.numel(), C.c_void_p(c.data_ptr()), n,
+                               ptr if is_float else None, None if is_float else ptr, C.c_void_p(act.data_ptr()),
+                               C.c_void_p(stream.cuda_stream)))
+    return out, act
+

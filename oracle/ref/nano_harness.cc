@@ -76,4 +76,40 @@ int vdbref_nano_onindex(void* g, const char* name, int channels, int stats, int 
     }
 }
 
+// The reference's own ReadAccessor on a NanoVDB buffer (copied into an
+// aligned HostBuffer): getValue and isActive at n index coordinates, for a
+// NanoGrid<float> (fvals) or a NanoGrid<ValueOnIndex> (ivals, the
+// LeafData<ValueOnIndex>::getValue decode of nanovdb/NanoVDB.h:4144-4170).
+int vdbref_nano_probe(const uint8_t* buf, int64_t size, const int32_t* ijk, int64_t n, float* fvals, uint64_t* ivals,
+                      uint8_t* active) {
+    try {
+        nanovdb::HostBuffer hb = nanovdb::HostBuffer::create(uint64_t(size));
+        std::memcpy(hb.data(), buf, size_t(size));
+        nanovdb::GridHandle<nanovdb::HostBuffer> handle(std::move(hb));
+        if (auto* g = handle.grid<float>()) {
+            auto acc = g->getAccessor();
+            for (int64_t i = 0; i < n; ++i) {
+                const nanovdb::Coord c(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2]);
+                fvals[i] = acc.getValue(c);
+                active[i] = acc.isActive(c) ? 1 : 0;
+            }
+            return 0;
+        }
+        if (auto* g = handle.grid<nanovdb::ValueOnIndex>()) {
+            auto acc = g->getAccessor();
+            for (int64_t i = 0; i < n; ++i) {
+                const nanovdb::Coord c(ijk[3 * i], ijk[3 * i + 1], ijk[3 * i + 2]);
+                ivals[i] = acc.getValue(c);
+                active[i] = acc.isActive(c) ? 1 : 0;
+            }
+            return 0;
+        }
+        gNanoError = "neither a NanoGrid<float> nor a NanoGrid<ValueOnIndex>";
+        return GBLS_ERR_UNSUPPORTED;
+    } catch (const std::exception& e) {
+        gNanoError = e.what();
+        return GBLS_ERR_RUNTIME;
+    }
+}
+
 }  // extern "C"

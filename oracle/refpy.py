@@ -61,6 +61,8 @@ def lib():
         L.vdbref_nano_last_error.restype = C.c_char_p
         L.vdbref_nano_onindex.argtypes = [C.c_void_p, C.c_char_p] + [C.c_int] * 4 + [C.c_void_p, C.c_int64,
                                                                               C.POINTER(C.c_int64)]
+        L.vdbref_nano_probe.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
         _lib = L
     return _lib
 
@@ -244,3 +246,20 @@ class RefGrid:
 
     def resize(self, half_width=3, **kw):
         return bool(self.tracker_op(5, half_width, **kw))
+
+
+def nano_probe(buf, ijk):
+    """The reference's ReadAccessor on a NanoVDB buffer: (float values or
+    uint64 indices, active flags) at the index coordinates ijk (n x 3)."""
+    L = lib()
+    b = np.ascontiguousarray(buf, np.uint8)
+    c = np.ascontiguousarray(ijk, np.int32)
+    n = c.shape[0]
+    fv = np.zeros(n, np.float32)
+    iv = np.zeros(n, np.uint64)
+    act = np.zeros(n, np.uint8)
+    if L.vdbref_nano_probe(b.ctypes.data, b.size, c.ctypes.data, n, fv.ctypes.data, iv.ctypes.data, act.ctypes.data):
+        raise RuntimeError(L.vdbref_nano_last_error().decode())
+    is_float = int(np.frombuffer(b[636:640].tobytes(), np.uint32)[0]) == 1
+    return (fv if is_float else iv), act
+

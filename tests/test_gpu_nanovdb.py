@@ -178,3 +178,50 @@ def test_rejects_bad_output_buffers():
         export_device(ls, "x" * 300)
     assert L.gbls_nanovdb_export_index_device(ls.handle, -1, b"s", 2, 1, 1, 1, None, 0, C.byref(n)) == 8
     ls.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["union_float", "tiles_float", "negative_float", "union_index", "tiles_index",
+                                  "negative_index"])
+def test_device_probe_matches_reference_accessor(case):
+    """Device-written buffer -> device ReadAccessor: the reference's own
+    accessor's values, value indices and active flags on the same bytes."""
+    import hashlib
+    import os
+    import sys
+    import torch
+    from openvdb_gb300.nanovdb import probe
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    sys.path.insert(0, here)
+    import make_nanovdb_probe as mp
+    gold = np.load(os.path.join(here, "nanovdb_probe.npz"))
+    grid, kind, args = mp.CASES[case]
+    ls = DeviceLevelSet(mp.make_grid(grid))
+    if kind == "float":
+        buf = export_device(ls, case, STATS[args[0]], CHECKSUMS[args[1]])
+    else:
+        buf = export_index_device(ls, case, False, args[0], args[1], "partial")
+    assert hashlib.sha256(_host(buf).tobytes()).digest() == gold[case + "/sha256"].tobytes()
+    ijk = torch.from_numpy(gold[case + "/ijk"]).cuda()
+    vals, act = probe(buf, ijk)
+    exp = gold[case + "/values"]
+    got = _host(vals)
+    got = got.view(np.uint32) if kind == "float" else got.view(np.uint64)
+    assert np.array_equal(got, exp), np.flatnonzero(got != exp)[:8]
+    assert np.array_equal(_host(act), gold[case + "/active"])
+    ls.close()
+
+
+@pytest.mark.gpu
+def test_device_probe_bounds_checks_truncated_buffers():
+    import torch
+    from openvdb_gb300.nanovdb import probe
+    ls = DeviceLevelSet(grids()["sphere"])
+    buf = export_device(ls, "s")
+    ijk = torch.tensor([[0, 0, 0], [12, 0, 0], [15, -7, 1]], dtype=torch.int32, device="cuda")
+    v, a = probe(buf, ijk)
+    assert int(a.sum()) >= 1
+    for cut in (700, 900, buf.numel() // 2):
+        with pytest.raises(GblsError):
+            probe(buf[:cut], ijk)
+    ls.close()

@@ -162,3 +162,46 @@ def test_import_rejects_garbage():
     buf = to_nanovdb(grids()["sphere"], "s")
     with pytest.raises(GblsError):
         from_nanovdb(buf[: buf.size // 2])
+
+
+def _probe_golden():
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    sys.path.insert(0, here)
+    import make_nanovdb_probe as mp
+    return mp, np.load(os.path.join(here, "nanovdb_probe.npz"))
+
+
+def _writer_bytes(mp, case):
+    from openvdb_gb300.nanovdb import to_nanovdb_index
+    grid, kind, args = mp.CASES[case]
+    g = mp.make_grid(grid)
+    if kind == "float":
+        return to_nanovdb(g, case, ["disable", "bbox", "minmax", "all"][args[0]],
+                          ["disable", "partial", "full"][args[1]])
+    return to_nanovdb_index(g, case, False, args[0], args[1], "partial")
+
+
+@pytest.mark.parametrize("case", ["union_float", "tiles_float", "negative_float", "union_index", "tiles_index",
+                                  "negative_index"])
+def test_probe_golden_buffers_are_the_host_writers(case):
+    """The buffers the probe vectors were taken on are the host writer's
+    bytes (so the device writer, equal to it, feeds the device probe the
+    reference's buffer)."""
+    import hashlib
+    mp, gold = _probe_golden()
+    b = _writer_bytes(mp, case)
+    assert hashlib.sha256(b.tobytes()).digest() == gold[case + "/sha256"].tobytes()
+
+
+@pytest.mark.parametrize("case", ["union_float", "tiles_index", "negative_index"])
+def test_probe_golden_matches_reference(case):
+    """The committed probe vectors are what the reference's ReadAccessor
+    returns now."""
+    refpy = _refpy()
+    mp, gold = _probe_golden()
+    vals, act = refpy.nano_probe(_writer_bytes(mp, case), gold[case + "/ijk"])
+    exp = gold[case + "/values"]
+    assert np.array_equal(vals.view(exp.dtype) if vals.dtype == np.float32 else vals, exp)
+    assert np.array_equal(act, gold[case + "/active"])
