@@ -216,11 +216,14 @@ class CheckpointedAdvection:
         self.field = DeviceField(Field.dense(self.velocity, self.origin, self.background))
 
     def _tape(self, grid):
-        """One tape (one device handle) serves every segment in turn."""
+        """One tape (one device handle) serves every segment in turn, always
+        with the current velocity field."""
         if getattr(self, "_shared", None) is None:
             self._shared = AdvectionTape(grid, self.velocity, self.origin, self.background, self.mode, self.cfl,
                                          field=self.field)
         self._shared.template = grid
+        self._shared.velocity = self.velocity
+        self._shared.field = self.field
         return self._shared
 
     def forward(self, phi0, times):
