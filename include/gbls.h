@@ -480,7 +480,8 @@ int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint8_t* decide
 /* The sign of that result where the three candidate sums of WENO5 agree,
  * which lets the PARITY renormalisation skip derivatives that
  * GodunovsNormSqrd clamps to zero: sign[i] = +1 (result >= 0), -1
- * (result <= 0) or 0 (undecided).                                          */
+ * (result <= 0), 2 (five zero operands: the result is a zero) or 0
+ * (undecided).                                                             */
 int gbls_host_weno5_sign(int64_t n, const float* v, int8_t* sign);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);

@@ -18,7 +18,7 @@ extern "C" int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint
 }
 
 // The sign that xw::weno5_sign certifies for each quintuple (+1: result
-// >= 0, -1: result <= 0, 0: undecided).
+// >= 0, -1: result <= 0, 2: a zero, 0: undecided).
 extern "C" int gbls_host_weno5_sign(int64_t n, const float* v, int8_t* sign) {
     if (n < 0 || (n > 0 && (!v || !sign))) return GBLS_ERR_INVALID_ARGUMENT;
     for (int64_t i = 0; i < n; ++i) {

@@ -286,8 +286,8 @@ __device__ inline float godunov_hj_exact(const float* tile, int x, int y, int z,
         const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
         const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
         const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
-        const bool need_dm = outside ? sb != -1 : sb != 1;
-        const bool need_dp = outside ? sf != 1 : sf != -1;
+        const bool need_dm = sb != 2 && (outside ? sb != -1 : sb != 1);
+        const bool need_dp = sf != 2 && (outside ? sf != 1 : sf != -1);
         float dm = 0.0f, dp = 0.0f;
 #pragma unroll 1
         for (int e = 0; e < 2; ++e) {
@@ -348,8 +348,9 @@ __device__ inline void godunov_exact_leaf(const float* tile, const uint16_t* lis
                 const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
                 const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
                 term[v] = 0u;
-                if (outside ? sb != -1 : sb != 1) queue[atomicAdd(cnt, 1)] = uint16_t(v << 1);
-                if (outside ? sf != 1 : sf != -1) queue[atomicAdd(cnt, 1)] = uint16_t((v << 1) | 1);
+                // a derivative the norm clamps to zero, or a zero (flat line), adds nothing
+                if (sb != 2 && (outside ? sb != -1 : sb != 1)) queue[atomicAdd(cnt, 1)] = uint16_t(v << 1);
+                if (sf != 2 && (outside ? sf != 1 : sf != -1)) queue[atomicAdd(cnt, 1)] = uint16_t((v << 1) | 1);
             }
             __syncthreads();
             const int m = *cnt;

@@ -313,16 +313,20 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
 // fused multiply-adds, within 2u T_k of the exact sum (T_k = sum of
 // |terms|), so an estimate beyond 4u T_k has the exact sum's sign; T_k = 0
 // makes p_k exactly zero.  Returns +1 (result >= 0 for certain), -1
-// (result <= 0 for certain) or 0 (undecided).
+// (result <= 0 for certain), 2 (five zero operands: the result is a zero)
+// or 0 (undecided).
 GBLS_XHD int weno5_sign(float v1, float v2, float v3, float v4, float v5) {
-    const float t1 = add(add(vabs(mul(2.0f, v1)), vabs(mul(7.0f, v2))), vabs(mul(11.0f, v3)));
-    const float t2 = add(add(vabs(mul(5.0f, v3)), vabs(v2)), vabs(mul(2.0f, v4)));
-    const float t3 = add(add(vabs(mul(2.0f, v3)), vabs(mul(5.0f, v4))), vabs(v5));
+    // T_k by fused multiply-adds: within 3u of the exact sums, so 4u T_k still
+    // exceeds the estimates' 2u error bound
+    const float t1 = fma(11.0f, vabs(v3), fma(7.0f, vabs(v2), mul(2.0f, vabs(v1))));
+    const float t2 = fma(5.0f, vabs(v3), fma(2.0f, vabs(v4), vabs(v2)));
+    const float t3 = fma(5.0f, vabs(v4), fma(2.0f, vabs(v3), vabs(v5)));
     const float e1 = fma(11.0f, v3, fma(-7.0f, v2, mul(2.0f, v1)));
     const float e2 = fma(2.0f, v4, fma(5.0f, v3, -v2));
     const float e3 = fma(-1.0f, v5, fma(5.0f, v4, mul(2.0f, v3)));
     const float m1 = mul(t1, 0x1p-22f), m2 = mul(t2, 0x1p-22f), m3 = mul(t3, 0x1p-22f);
     const bool z1 = t1 == 0.0f, z2 = t2 == 0.0f, z3 = t3 == 0.0f;
+    if (z1 && z2 && z3) return 2;
     const bool nonneg = (z1 || e1 > m1) && (z2 || e2 > m2) && (z3 || e3 > m3);
     const bool nonpos = (z1 || e1 < -m1) && (z2 || e2 < -m2) && (z3 || e3 < -m3);
     return nonneg ? 1 : nonpos ? -1 : 0;

@@ -100,4 +100,6 @@ def test_weno5_sign_is_certain(kind):
                                            sign.ctypes.data_as(P(C.c_int8))) == 0
     assert not np.any((sign == 1) & (ref < 0)), "certified >= 0 but negative"
     assert not np.any((sign == -1) & (ref > 0)), "certified <= 0 but positive"
+    assert not np.any((sign == 2) & (ref != 0)), "certified zero but not zero"
+    assert np.array_equal(sign == 2, np.all(v == 0, axis=1)), "a zero certificate other than five zero operands"
     print("%s: sign certified for %.1f%%" % (kind, 100.0 * np.mean(sign != 0)))
