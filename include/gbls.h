@@ -64,7 +64,10 @@ enum { GBLS_TRIM_NONE = 0, GBLS_TRIM_INTERIOR = 1, GBLS_TRIM_EXTERIOR = 2, GBLS_
  *   created, selects kernels that evaluate every weight in FP64 instead
  *   (the same bits, slower; for cross-checking).
  * FAST evaluates everything in FP32 (contracted, shared sub-expressions). */
-enum { GBLS_MODE_PARITY = 0, GBLS_MODE_FAST = 1 };
+/* PARITY: bit-identical to the reference's FloatGrid path; FAST: FP32
+ * arithmetic; FP64: the same scheme with the values in double (the
+ * reference's DoubleGrid instantiation), the error oracle of the FP32 run.  */
+enum { GBLS_MODE_PARITY = 0, GBLS_MODE_FAST = 1, GBLS_MODE_FP64 = 2 };
 
 /* Transform kinds accepted (tools/LevelSetAdvect.h:257-276 accepts these four;
  * the device path supports the uniform-scale ones). */
@@ -230,6 +233,16 @@ int gbls_get_tracker_state(gbls_handle* h, int* spatial_scheme, int* temporal_sc
                            int* norm_count, int* grain_size);
 int gbls_set_trimming(gbls_handle* h, int trim_mode);       /* :171 */
 int gbls_set_precision(gbls_handle* h, int mode);           /* GBLS_MODE_* */
+/* GBLS_MODE_FP64 widens the level set's values to double (exactly); leaving
+ * it rounds them back to FP32.  In FP64 mode gbls_advect and the tracker
+ * operations run on double values with HJWENO5 (advection substeps in double
+ * time, |v|^2 of the CFL limit in double at the first voxel holding the
+ * maximum), gbls_download rounds to FP32 and gbls_get_active_values_f64
+ * returns the doubles; batches, volumes, morphing, filters, the adjoint,
+ * host-sampled fields and NanoVDB export are GBLS_ERR_UNSUPPORTED.          */
+/* The active values in canonical order (leaf tree order, voxel order within
+ * a leaf), as doubles, into host memory (FP32 level sets: widened).          */
+int gbls_get_active_values_f64(gbls_handle* h, double* out);
 
 /* ---- launch shapes (no reference counterpart) ------------------------------
  * The choices an autotuner makes per device and workload:

@@ -25,7 +25,7 @@ FIRST_BIAS, SECOND_BIAS, THIRD_BIAS, WENO5_BIAS, HJWENO5_BIAS = 0, 1, 2, 3, 4
 TVD_RK1, TVD_RK2, TVD_RK3 = 0, 1, 2
 # lstrack::TrimMode (tools/LevelSetTracker.h:45-50)
 TRIM_NONE, TRIM_INTERIOR, TRIM_EXTERIOR, TRIM_ALL = 0, 1, 2, 3
-MODE_PARITY, MODE_FAST = 0, 1
+MODE_PARITY, MODE_FAST, MODE_FP64 = 0, 1, 2
 MAP_UNIFORM_SCALE, MAP_UNIFORM_SCALE_TRANSLATE, MAP_TRANSLATION = 0, 1, 2
 FIELD_CONSTANT, FIELD_DENSE, FIELD_DEFORMATION, FIELD_ROTATION, FIELD_HOST_SAMPLED = 0, 1, 2, 3, 4
 

@@ -45,6 +45,7 @@ def lib():
         "gbls_get_tracker_state": ([vp] + [P(C.c_int)] * 4, C.c_int),
         "gbls_set_trimming": ([vp, C.c_int], C.c_int),
         "gbls_set_precision": ([vp, C.c_int], C.c_int),
+        "gbls_get_active_values_f64": ([vp, vp], C.c_int),
         "gbls_set_launch_config": ([vp, P(_abi.LaunchConfig)], C.c_int),
         "gbls_volume_advect": ([vp, vp, C.c_int, C.c_int, C.c_int, C.c_double, P(C.c_double)], C.c_int),
         "gbls_create_volume": ([P(_abi.GridDesc), P(vp)], C.c_int),

@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contra
 CXX_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-pthread",
              "-I" + os.path.join(REPO, "include")]
 PER_UNIT = {"stencil_parity.cu": ["-fmad=false"], "stencil_exact.cu": ["-fmad=false"], "volume.cu": ["-fmad=false"],
-            "nanovdb_device.cu": ["-fmad=false"]}
+            "nanovdb_device.cu": ["-fmad=false"], "stencil_f64.cu": ["-fmad=false"]}
 
 
 def _nvcc():

@@ -27,6 +27,7 @@
 #include "host_grid.h"
 #include "nanovdb_device.h"
 #include "stencil.h"
+#include "stencil_f64.h"
 #include "stencil_ops.cuh"
 #include "topology.cuh"
 #include "volume.h"
@@ -655,7 +656,11 @@ struct gbls_handle {
     // slot storage: 3 mask sets, 3 value buffers, dilation mask
     int64_t slot_cap = 0;
     DevArray<uint64_t> am[3], sm[3];
-    DevArray<float> vals[3];
+    DevArray<float> vals[3];  // FP32 values, or (f64) 512 doubles per slot in the same arrays
+    bool f64 = false;         // the FP64 instance (GBLS_MODE_FP64)
+    DevArray<float> f32_view; // f64: the current values rounded to float (downloads)
+    DevArray<unsigned long long> argk;
+    DevArray<double> argv;
     DevArray<uint64_t> dmask, emask;
     DevArray<int32_t> free_slots;
     int64_t nfree = 0;
@@ -927,7 +932,8 @@ struct gbls_handle {
         for (int b = 0; b < 3; ++b) {
             am[b].reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
             sm[b].reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
-            vals[b].reserve(size_t(nc) * LEAF_VOX, stream, size_t(old) * LEAF_VOX, 1.0);
+            const size_t vw = f64 ? 2 : 1;  // floats per value
+            vals[b].reserve(size_t(nc) * LEAF_VOX * vw, stream, size_t(old) * LEAF_VOX * vw, 1.0);
         }
         dmask.reserve(size_t(nc) * 8, stream, size_t(old) * 8, 1.0);
         emask.reserve(size_t(nc) * 8, stream, 0, 1.0);
@@ -1320,7 +1326,15 @@ void launch_norm(gbls_handle& h, const NormArgs& a0) {
         e1 = h.event();
         CU(cudaEventRecord(e0, h.stream));
     }
-    if (h.mode == GBLS_MODE_PARITY) {
+    if (h.f64) {
+        if (a.spatial != GBLS_HJWENO5_BIAS && !a.copy_only)
+            fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance renormalises with HJWENO5");
+        // Normalizer's mDt and 1/dx with ValueType double (dx = double(float(voxel size)))
+        const double dx = double(float(h.voxel_size));
+        a.mdt64 = dx * double(h.tr_temporal == GBLS_TVD_RK1 ? 0.3f : h.tr_temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f);
+        a.invdx64 = 1.0 / dx;
+        launch_norm_f64(a, h.stream);
+    } else if (h.mode == GBLS_MODE_PARITY) {
         if (h.parity_fp64) launch_norm_parity(a, h.stream);
         else launch_norm_exact(a, h.stream, h.norm_min_ctas);
     } else {
@@ -1795,7 +1809,11 @@ void rk_stage(gbls_handle& h, const RkArgs& a) {
         e1 = h.event();
         CU(cudaEventRecord(e0, h.stream));
     }
-    if (h.mode == GBLS_MODE_PARITY) {
+    if (h.f64) {
+        if (a.spatial != GBLS_HJWENO5_BIAS) fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance advects with HJWENO5");
+        if (a.inst_run) fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance runs single level sets");
+        launch_rk_f64(a, h.stream);
+    } else if (h.mode == GBLS_MODE_PARITY) {
         if (h.parity_fp64) launch_rk_parity(a, h.stream);
         else launch_rk_exact(a, h.stream, h.rk_min_ctas);
     } else {
@@ -1814,8 +1832,10 @@ void rk_stage(gbls_handle& h, const RkArgs& a) {
 }
 
 // The TVD-RK stages of one substep (tools/LevelSetAdvect.h:360-405).
-void advect_stages(gbls_handle& h, const gbls_field* f, int spatial, int temporal, float t0, float dt, bool backward) {
+void advect_stages(gbls_handle& h, const gbls_field* f, int spatial, int temporal, float t0, float dt, bool backward,
+                   double dt64 = 0.0) {
     RkArgs base{};
+    base.dt64 = dt64;
     base.spatial = spatial;
     base.nleaf = h.nleaf;
     base.keys = h.K();
@@ -1865,6 +1885,62 @@ void advect_stages(gbls_handle& h, const gbls_field* f, int spatial, int tempora
     }
 }
 
+// |v|^2 of the time step in double for the FP64 instance: (x*x + y*y) + z*z
+// of the widened components at the first active voxel (leaf order, voxel
+// order) whose Vec3f |v|^2 is the float maximum maxv2.
+double max_speed_sqr_f64(gbls_handle& h, const gbls_field* f, float t, float maxv2) {
+    if (f->desc.kind == GBLS_FIELD_CONSTANT) {
+        const double x = f->desc.constant[0], y = f->desc.constant[1], z = f->desc.constant[2];
+        return (x * x + y * y) + z * z;
+    }
+    h.argk.reserve(1, h.stream);
+    h.argv.reserve(1, h.stream);
+    launch_argmax_f64(h.nleaf, h.K(), h.S(), h.am[h.mc].p, field_params(h, f, t), t, maxv2, h.argk.p, h.argv.p,
+                      h.stream);
+    h.stats.kernel_launches += 2;
+    CU(cudaGetLastError());
+    double v = 0.0;
+    CU(cudaMemcpyAsync(&v, h.argv.p, sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+    h.sync();
+    if (!(v >= 0.0)) fail(GBLS_ERR_RUNTIME, "no active voxel holds the maximum speed");
+    return v;
+}
+
+// LevelSetAdvection::advect (tools/LevelSetAdvect.h:338-418) for the FP64
+// instance, the DoubleGrid instantiation: time and substep lengths in
+// double (the interval clock over double time), velocities sampled as Vec3f
+// at float(t), the RK stages and the tracker on double values.
+void advect_f64(gbls_handle& h, const gbls_field* field, int spatial, int temporal, float t0, float t1, float cfl,
+                uint64_t& count, bool& interrupted) {
+    if (spatial != GBLS_HJWENO5_BIAS || h.tr_spatial != GBLS_HJWENO5_BIAS)
+        fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance advects and tracks with HJWENO5");
+    if (field->desc.kind == GBLS_FIELD_HOST_SAMPLED)
+        fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance samples fields the device evaluates");
+    const bool forward = t0 < t1;
+    CflClockT<double> clock(t0, t1, cfl, temporal, float(h.voxel_size));
+    double t = t0;
+    h.cfl_cache.valid = false;
+    while (clock.running(t)) {
+        if (!check_intr(h)) { interrupted = true; break; }
+        if (h.nleaf == 0) break;  // sampleField returns 0 for an empty grid
+        const float tf = float(t);
+        start_intr(h, "Sampling advection field");
+        const float maxv2 = max_speed_sqr(h, field, tf);
+        end_intr(h);
+        if (!(maxv2 > 1e-5f) && !(maxv2 < -1e-5f)) break;  // isApproxZero(maxAbsV, Delta)
+        const double dt = clock.next(t, max_speed_sqr_f64(h, field, tf, maxv2));
+        if (dt == 0.0) break;
+        if (h.nactive < 0) h.nactive = active_count(h);
+        h.stats.voxel_updates += uint64_t(h.nactive);
+        ++h.stats.substeps;
+        advect_stages(h, field, spatial, temporal, tf, float(dt), !forward, dt);
+        clock.advance(t, dt);
+        ++count;
+        track(h);
+    }
+    h.sync();
+}
+
 // ---- LevelSetMorphing (tools/LevelSetMorph.h) -------------------------------
 LookupGrid lookup_grid(gbls_handle& g) {
     LookupGrid L{};
@@ -1881,6 +1957,7 @@ LookupGrid lookup_grid(gbls_handle& g) {
 // 479-510): euler01 / euler12 / euler34 / euler13 over the same buffers as
 // the advection stages.
 void morph_stages(gbls_handle& h, int spatial, int temporal, float dt) {
+    if (h.f64) fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance runs advection and tracking only");
     MorphArgs base{};
     base.spatial = spatial;
     base.nleaf = h.nleaf;
@@ -1956,6 +2033,7 @@ float morph_sample_speed(gbls_handle& h, gbls_handle& target, gbls_handle* mask,
 // One Filter::cook pass: every active voxel from the current values into the
 // free value buffer, which becomes current (swapLeafBuffer).
 void filter_pass(gbls_handle& h, FilterArgs a, const char* msg) {
+    if (h.f64) fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance runs advection and tracking only");
     if (h.nleaf == 0) return;
     const int vo = other_of(h.vc, h.vc);
     a.nleaf = h.nleaf;
@@ -2202,11 +2280,55 @@ bool upload_impl(gbls_handle& h, const gbls_grid_desc* descs, int n, bool dev_le
     return true;
 }
 
+// The FP64 instance keeps 512 doubles per slot in the value arrays: widen
+// the current FP32 values (exactly) into a new array twice the size, or
+// round the current doubles back to FP32.  The other two buffers only
+// change capacity: the RK stages and renormalisation write them in full.
+void widen_values(gbls_handle& h) {
+    const size_t n = size_t(h.slot_cap) * LEAF_VOX;
+    DevArray<float> w;
+    w.reserve(std::max<size_t>(2 * n, 32), h.stream);
+    launch_widen(h.vals[h.vc].p, reinterpret_cast<double*>(w.p), n, h.stream);
+    ++h.stats.kernel_launches;
+    CU(cudaGetLastError());
+    h.sync();
+    std::swap(h.vals[h.vc].p, w.p);
+    std::swap(h.vals[h.vc].cap, w.cap);
+    for (int b = 0; b < 3; ++b)
+        if (b != h.vc) h.vals[b].reserve(std::max<size_t>(2 * n, 32), h.stream);
+}
+
+void narrow_values(gbls_handle& h) {
+    const size_t n = size_t(h.slot_cap) * LEAF_VOX;
+    DevArray<float> w;
+    w.reserve(std::max<size_t>(n, 16), h.stream);
+    launch_narrow(reinterpret_cast<const double*>(h.vals[h.vc].p), w.p, n, h.stream);
+    ++h.stats.kernel_launches;
+    CU(cudaGetLastError());
+    h.sync();
+    std::swap(h.vals[h.vc].p, w.p);
+    std::swap(h.vals[h.vc].cap, w.cap);
+}
+
+// The current values as FP32 (the FP64 instance's rounded into f32_view).
+const float* current_f32(gbls_handle& h) {
+    if (!h.f64) return h.vals[h.vc].p;
+    const size_t n = size_t(h.slot_cap) * LEAF_VOX;
+    h.f32_view.reserve(std::max<size_t>(n, 16), h.stream);
+    launch_narrow(reinterpret_cast<const double*>(h.vals[h.vc].p), h.f32_view.p, n, h.stream);
+    ++h.stats.kernel_launches;
+    CU(cudaGetLastError());
+    return h.f32_view.p;
+}
+
 void upload(gbls_handle& h, const gbls_grid_desc* descs, int n) {
     if (n == 1 && descs[0].leaf_count > 0 && descs[0].leaf_origins && descs[0].leaf_masks && descs[0].leaf_values &&
-        upload_impl(h, descs, n, true))
+        upload_impl(h, descs, n, true)) {
+        if (h.f64) widen_values(h);
         return;
+    }
     upload_impl(h, descs, n, false);
+    if (h.f64) widen_values(h);
 }
 
 // Index ranges [lo, hi) of instance `inst` in the leaf / lower / upper / root
@@ -2261,7 +2383,7 @@ void download(gbls_handle& h, gbls_grid_desc* d, int inst) {
         float* dense = h.vals[other_of(h.vc, h.vc)].p;
         uint64_t* masks = h.am[other_of(h.mc, h.mc)].p;
         h.io_orig.reserve(size_t(L) * 3, h.stream);
-        k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S() + R.l0, h.am[h.mc].p, h.sm[h.mc].p, h.vals[h.vc].p, g,
+        k_unpack<<<unsigned(L), 128, 0, h.stream>>>(L, h.S() + R.l0, h.am[h.mc].p, h.sm[h.mc].p, current_f32(h), g,
                                                      dense);
         launch_leaf_headers(L, h.K() + R.l0, h.S() + R.l0, h.am[h.mc].p, h.io_orig.p, masks, h.stream);
         h.stats.kernel_launches += 2;
@@ -2523,6 +2645,7 @@ int gbls_time_launch_config(gbls_handle* h, const gbls_field* f, const gbls_laun
     return guarded([&] {
         DeviceGuard g(h->device);
         if (h->nleaf == 0) fail(GBLS_ERR_INVALID_ARGUMENT, "empty level set");
+        if (h->f64) fail(GBLS_ERR_UNSUPPORTED, "launch shapes are tuned on FP32 level sets");
         if (f->desc.kind == GBLS_FIELD_HOST_SAMPLED) fail(GBLS_ERR_UNSUPPORTED, "timing takes a device-evaluated field");
         if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "timing while the adjoint records");
         const int n = std::max(1, reps);
@@ -2595,12 +2718,25 @@ int gbls_time_launch_config(gbls_handle* h, const gbls_field* f, const gbls_laun
 
 int gbls_set_precision(gbls_handle* h, int mode) {
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
-    if (mode != GBLS_MODE_PARITY && mode != GBLS_MODE_FAST) {
+    if (mode != GBLS_MODE_PARITY && mode != GBLS_MODE_FAST && mode != GBLS_MODE_FP64) {
         g_last_error = "bad precision mode";
         return GBLS_ERR_VALUE;
     }
-    h->mode = mode;
-    return GBLS_OK;
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        const bool want = mode == GBLS_MODE_FP64;
+        if (want && (h->ninst != 1 || h->volume))
+            fail(GBLS_ERR_UNSUPPORTED, "the FP64 instance runs single level sets");
+        if (want && h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "the adjoint records FP32 level sets");
+        if (want != h->f64) {
+            h->sync();
+            if (want) widen_values(*h);
+            else narrow_values(*h);
+            h->f64 = want;
+            touched(h);
+        }
+        h->mode = mode;
+    });
 }
 
 int gbls_set_interrupter(gbls_handle* h, const gbls_interrupter* intr) {
@@ -2779,6 +2915,7 @@ int gbls_resize(gbls_handle* h, uint32_t half_width, int* changed) {
 
 // ---- adjoint -----------------------------------------------------------------
 int gbls_adjoint_record(gbls_handle* h, int enable) {
+    if (h && h->f64 && enable) { g_last_error = "the adjoint records FP32 level sets"; return GBLS_ERR_UNSUPPORTED; }
     touched(h);
     if (!h) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     return guarded([&] {
@@ -2827,6 +2964,7 @@ void packed_prefix(gbls_handle& h, int64_t n, const int32_t* slot, const uint64_
 int gbls_get_active_values_device(gbls_handle* h, float* out) {
     touched(h);
     if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (h->f64) { g_last_error = "an FP64 level set: gbls_get_active_values_f64"; return GBLS_ERR_UNSUPPORTED; }
     return guarded([&] {
         DeviceGuard g(h->device);
         DevArray<int64_t> cnt, pre;
@@ -2843,6 +2981,7 @@ int gbls_get_active_values_device(gbls_handle* h, float* out) {
 int gbls_set_active_values_device(gbls_handle* h, const float* in) {
     touched(h);
     if (!h || !in) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    if (h->f64) { g_last_error = "the FP64 instance takes its values from gbls_upload"; return GBLS_ERR_UNSUPPORTED; }
     return guarded([&] {
         DeviceGuard g(h->device);
         if (h->tape_on && !h->tape.empty()) fail(GBLS_ERR_UNSUPPORTED, "values change under a recorded tape");
@@ -2858,6 +2997,40 @@ int gbls_set_active_values_device(gbls_handle* h, const float* in) {
         h->cfl_cache.valid = false;
         CU(cudaGetLastError());
         h->sync();
+    });
+}
+
+int gbls_get_active_values_f64(gbls_handle* h, double* out) {
+    if (!h || !out) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        DeviceGuard g(h->device);
+        if (h->ninst != 1) fail(GBLS_ERR_UNSUPPORTED, "single level sets only");
+        DevArray<int64_t> cnt, pre;
+        packed_prefix(*h, h->nleaf, h->S(), h->am[h->mc].p, nullptr, cnt, pre);
+        if (h->nactive < 0) h->nactive = active_count(*h);
+        const int64_t n = h->nactive;
+        if (n == 0) return;
+        if (h->f64) {
+            DevArray<double> d;
+            d.reserve(size_t(n), h->stream);
+            launch_gather_active_f64(h->nleaf, h->S(), h->am[h->mc].p, pre.p,
+                                     reinterpret_cast<const double*>(h->vals[h->vc].p), d.p, h->stream);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+            CU(cudaMemcpyAsync(out, d.p, size_t(n) * 8, cudaMemcpyDeviceToHost, h->stream));
+            h->sync();
+        } else {
+            DevArray<float> f;
+            f.reserve(size_t(n), h->stream);
+            k_packed_move<<<unsigned(h->nleaf), 64, 0, h->stream>>>(h->nleaf, h->S(), nullptr, nullptr,
+                                                                    h->am[h->mc].p, pre.p, h->vals[h->vc].p, f.p, 1);
+            ++h->stats.kernel_launches;
+            CU(cudaGetLastError());
+            std::vector<float> tmp(static_cast<size_t>(n));
+            CU(cudaMemcpyAsync(tmp.data(), f.p, size_t(n) * 4, cudaMemcpyDeviceToHost, h->stream));
+            h->sync();
+            for (int64_t i = 0; i < n; ++i) out[i] = double(tmp[size_t(i)]);
+        }
     });
 }
 
@@ -3492,6 +3665,10 @@ int gbls_advect(gbls_handle* h, const gbls_field* field, int spatial, int tempor
         check_scheme(spatial, temporal);
         check_scheme(h->tr_spatial, h->tr_temporal);
         if (t0 - t1 == 0.0f) return;  // math::isZero(time0 - time1)
+        if (h->f64) {
+            advect_f64(*h, field, spatial, temporal, t0, t1, cfl, count, interrupted);
+            return;
+        }
         const bool forward = t0 < t1;
         CflClock clock(t0, t1, cfl, temporal, float(h->voxel_size));
         // the CFL reduction of substep k+1 rides on the read-back that ends
@@ -3929,6 +4106,10 @@ int gbls_volume_advect(gbls_handle* h, const gbls_field* field, int integrator, 
 int gbls_morph(gbls_handle* h, gbls_handle* target, gbls_handle* alpha_mask, int spatial, int temporal, float t0,
                float t1, float mask_min, float mask_max, int invert_mask, uint64_t* substeps) {
     if (h && h->volume) { g_last_error = "a volume handle takes volume operations only"; return GBLS_ERR_UNSUPPORTED; }
+    if ((h && h->f64) || (target && target->f64) || (alpha_mask && alpha_mask->f64)) {
+        g_last_error = "the FP64 instance runs advection and tracking only";
+        return GBLS_ERR_UNSUPPORTED;
+    }
     touched(h);
     if (substeps) *substeps = 0;
     if (!h || !target) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
@@ -4004,6 +4185,7 @@ struct NanoExport {
 };
 
 NanoExport nano_export_view(gbls_handle& h, int instance) {
+    if (h.f64) fail(GBLS_ERR_UNSUPPORTED, "NanoVDB export of an FP64 level set (NanoGrid<float> holds FP32 values)");
     if (h.ninst > 1 && (instance < 0 || instance >= h.ninst)) fail(GBLS_ERR_INVALID_ARGUMENT, "no such instance");
     if (h.ninst == 1 && instance > 0) fail(GBLS_ERR_INVALID_ARGUMENT, "no such instance");
     h.sync();

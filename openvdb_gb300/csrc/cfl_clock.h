@@ -20,60 +20,66 @@
 
 namespace gbls {
 
-struct CflClock {
+// T is the time type: float for the FloatGrid instance (the reference's
+// float time), double for the FP64 instance, where the substep lengths
+// T(c*dx) / sqrt(T(max |v|^2)) and the time reached are double.
+template <class T>
+struct CflClockT {
     float t1 = 0.0f;
     bool forward = true;
     float cfl = 0.0f;   // imposed CFL number (0: none)
     float cref = 0.0f;  // the reference's CFL number for the temporal scheme
     float dx = 1.0f;
     bool open = false;  // inside an interval
-    float end = 0.0f;   // the interval's end time
+    T end = T(0.0f);    // the interval's end time
     // how the last substep was set (the adjoint's time-step derivative):
     // limited: CFL_ref*dx/|v|max (else the rest of the interval); opened:
     // the substep opened its interval, whose end is t +- open_lim when
     // end_lim (else t1)
     bool limited = false, opened = false, end_lim = false;
-    float open_lim = 0.0f;
+    T open_lim = T(0.0f);
 
-    CflClock(float t0, float t1_, float cfl_, int temporal, float dx_)
+    CflClockT(float t0, float t1_, float cfl_, int temporal, float dx_)
         : t1(t1_), forward(t0 < t1_), cfl(cfl_ > 0.0f ? cfl_ : 0.0f), dx(dx_) {
         cref = (temporal == GBLS_TVD_RK1 ? 0.3f : temporal == GBLS_TVD_RK2 ? 0.9f : 1.0f) / std::sqrt(3.0f);
     }
 
-    bool running(float t) const { return forward ? t < t1 : t > t1; }
+    bool running(T t) const { return forward ? t < T(t1) : t > T(t1); }
 
     // Length of the substep that starts at t with max |v|^2 = maxv2 (not
     // approximately zero); 0 ends the loop (an interval that rounds to zero
     // length, where the reference's advect(tau, tau) returns at once).
-    float next(float t, float maxv2) {
+    T next(T t, T maxv2) {
         opened = false;
         if (!open) {
-            end = t1;
+            end = T(t1);
             end_lim = false;
             if (cfl > 0.0f) {
-                const float lim = cfl * dx / std::sqrt(maxv2);
-                const float span = std::fabs(t1 - t);
+                const T lim = T(cfl * dx) / std::sqrt(maxv2);
+                const T span = std::fabs(T(t1) - t);
                 if (lim < span) {
                     end = forward ? t + lim : t - lim;
                     end_lim = true;
                     open_lim = lim;
                 }
             }
-            if (end - t == 0.0f) return 0.0f;  // math::isZero(time0 - time1)
+            if (end - t == T(0.0f)) return T(0.0f);  // math::isZero(time0 - time1)
             open = true;
             opened = true;
         }
-        const float span = std::fabs(end - t);
-        const float lim = cref * dx / std::sqrt(maxv2);
+        const T span = std::fabs(end - t);
+        const T lim = T(cref * dx) / std::sqrt(maxv2);
         limited = lim < span;
         return limited ? lim : span;  // math::Min(dt, CFL*dx/sqrt(maxAbsV))
     }
 
     // t advanced by the substep dt; closes the interval when t reaches its end.
-    void advance(float& t, float dt) {
+    void advance(T& t, T dt) {
         t += forward ? dt : -dt;
         if (!(forward ? t < end : t > end)) open = false;
     }
 };
+
+using CflClock = CflClockT<float>;
 
 }  // namespace gbls

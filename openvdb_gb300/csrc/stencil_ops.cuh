@@ -510,6 +510,7 @@ struct RkArgs {
     const float* inst_t0;
     const FieldParams* inst_field;
     int copy_done;         // the stage's output becomes the result: copy finished instances
+    double dt64;           // FP64 instance: the substep length in double
 };
 
 struct NormArgs {
@@ -533,6 +534,7 @@ struct NormArgs {
     unsigned long long* acc;  // [2] += voxels processed, voxels written (may be null)
     const uint64_t* keys;     // batches: leaf keys (instance = key >> 54)
     const uint8_t* inst_run;  // batches: finished instances are copied through
+    double mdt64, invdx64;    // FP64 instance: mDt and 1/dx in double
 };
 
 struct CflArgs {

@@ -22,7 +22,7 @@ from .grid import HostGrid
 
 HJWENO5_BIAS = _abi.HJWENO5_BIAS
 TVD_RK1, TVD_RK2, TVD_RK3 = _abi.TVD_RK1, _abi.TVD_RK2, _abi.TVD_RK3
-PARITY, FAST = _abi.MODE_PARITY, _abi.MODE_FAST
+PARITY, FAST, FP64 = _abi.MODE_PARITY, _abi.MODE_FAST, _abi.MODE_FP64
 
 
 class ValueError_(ValueError):
@@ -121,7 +121,16 @@ class DeviceLevelSet:
         return g
 
     def set_precision(self, mode):
+        """PARITY, FAST, or FP64 (the values widened to double: the FP64
+        instance of the scheme, the error oracle of the FP32 run)."""
         _call(lib().gbls_set_precision(self._h, int(mode)))
+
+    def active_values_f64(self):
+        """Active values in canonical order as float64 (FP64 instance: its
+        doubles; FP32 level sets: widened)."""
+        out = np.zeros(self.active_voxel_count(), np.float64)
+        _call(lib().gbls_get_active_values_f64(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def set_stream(self, stream_ptr):
         _call(lib().gbls_set_stream(self._h, C.c_void_p(stream_ptr)))
