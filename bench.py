@@ -344,9 +344,16 @@ def run_gb300(args):
         "cpu_baseline": cpu_baseline(args) if args.cpu_baseline else None,
     }
     if args.extras:
-        out["config1"] = config1_sphere(mode, args.mode, args.cfl)
-        out["adjoint"] = adjoint_cost(mode, args.mode)
-        out["batched"] = batch_measure(args, steps=3, warmup=3, cpu=False)
+        def extra(fn, *a, **kw):
+            # a failing extra reports its error instead of losing the line
+            try:
+                return fn(*a, **kw)
+            except Exception as e:  # noqa: BLE001
+                return {"error": "%s: %s" % (type(e).__name__, e)}
+        out["config1"] = extra(config1_sphere, mode, args.mode, args.cfl)
+        out["adjoint"] = extra(adjoint_cost, mode, args.mode)
+        out["batched"] = extra(batch_measure, args, steps=3, warmup=3, cpu=False)
+        out["fp64_error"] = extra(fp64_errors, args.cfl)
     print(json.dumps(out))
 
 
@@ -376,6 +383,77 @@ def config1_sphere(mode, mode_name, cfl, steps=10):
     return {"workload": "sphere r=64, constant velocity (1, 0.5, 0.25), 10 unit steps, RK3-HJWENO5, CFL %g" % cfl,
             "mode": mode_name, "value": st["voxel_updates"] / (ms / 1e3), "unit": UNIT, "ms": ms,
             "substeps": int(st["substeps"]), "active_voxels_end": int(st["active_voxels"])}
+
+
+def _band_error(h32, h64, v64, gamma):
+    """The FP32 run (HostGrid h32) against the FP64 run (band h64, its active
+    values v64 in canonical order): max and 99.99th percentile of |phi32 -
+    phi64| / gamma over voxels active in both, voxels above 1e-5 gamma, and
+    active-state differences."""
+    import numpy as np
+    m64 = h64.active_mask_bool()
+    dense64 = np.zeros(m64.shape, np.float64)
+    dense64[m64] = v64  # leaf-major, voxel-minor: the canonical order
+    k64 = {tuple(o): i for i, o in enumerate(h64.leaf_origins.tolist())}
+    m32 = h32.active_mask_bool()
+    pairs = [(i, k64[tuple(o)]) for i, o in enumerate(h32.leaf_origins.tolist()) if tuple(o) in k64]
+    i32 = np.array([p[0] for p in pairs], np.int64)
+    i64 = np.array([p[1] for p in pairs], np.int64)
+    a, b = m32[i32], m64[i64]
+    both = a & b
+    d = np.abs(h32.leaf_values[i32][both].astype(np.float64) - dense64[i64][both]) / gamma
+    flips = int((a ^ b).sum()) + int(m32.sum() - a.sum()) + int(m64.sum() - b.sum())
+    return {"max_dphi_over_gamma": float(d.max()) if d.size else 0.0,
+            "p9999_over_gamma": float(np.percentile(d, 99.99)) if d.size else 0.0,
+            "voxels_above_1e-5_gamma": int((d > 1e-5).sum()), "active_state_differences": flips,
+            "voxels_compared": int(both.sum())}
+
+
+def fp64_errors(cfl):
+    """The FP32 PARITY run's error against the device's FP64 instance (the
+    same scheme with the values in double, bit-identical to the oracle's
+    FP64 run), per configuration: configuration 1 (10 unit steps) and the
+    64-sphere benchmark window from t = 0 (25 unit steps); the worst step."""
+    import torch
+    from openvdb_gb300 import FP64, PARITY, DeviceLevelSet, Field, fixtures
+    from openvdb_gb300.levelset import DeviceField
+    out = {}
+    cases = {"config1": (lambda: fixtures.sphere(64.0, (0.0, 0.0, 0.0)), lambda: Field.constant_field((1.0, 0.5, 0.25)),
+                         10),
+             "config2": (lambda: build_workload()[0], lambda: build_workload()[1], 25)}
+    for name, (make_grid, make_field, steps) in cases.items():
+        g, f = make_grid(), DeviceField(make_field())
+        runs = []
+        for mode in (PARITY, FP64):
+            d = DeviceLevelSet(g)
+            d.set_precision(mode)
+            runs.append((d, make_advection(d, f, cfl=cfl)))
+        worst, t64, upd64 = None, 0.0, 0
+        for step in range(steps):
+            for k, (d, adv) in enumerate(runs):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                d.reset_stats()
+                adv.advect(float(step), float(step + 1))
+                torch.cuda.synchronize()
+                if k == 1:
+                    t64 += time.perf_counter() - t0
+                    upd64 += d.stats()["voxel_updates"]
+            e = _band_error(runs[0][0].to_host(), runs[1][0].to_host(), runs[1][0].active_values_f64(),
+                            float(g.background))
+            if worst is None:
+                worst = dict(e)
+            else:
+                for key in ("max_dphi_over_gamma", "p9999_over_gamma"):
+                    worst[key] = max(worst[key], e[key])
+                for key in ("voxels_above_1e-5_gamma", "active_state_differences"):
+                    worst[key] = max(worst[key], e[key])
+        worst["steps"] = steps
+        worst["fp64_voxel_updates_per_s"] = upd64 / t64 if t64 > 0 else None
+        out[name] = worst
+        for d, _ in runs:
+            d.close()
+    return out
 
 
 def adjoint_cost(mode, mode_name, reps=3):
