@@ -409,11 +409,13 @@ def _band_error(h32, h64, v64, gamma):
             "voxels_compared": int(both.sum())}
 
 
-def fp64_errors(cfl):
+def fp64_errors(cfl, n_batch=16):
     """The FP32 PARITY run's error against the device's FP64 instance (the
     same scheme with the values in double, bit-identical to the oracle's
-    FP64 run), per configuration: configuration 1 (10 unit steps) and the
-    64-sphere benchmark window from t = 0 (25 unit steps); the worst step."""
+    FP64 run), per configuration: configuration 1 (10 unit steps), the
+    64-sphere benchmark window from t = 0 (25 unit steps) and the first
+    n_batch instances of the batch (50 unit steps each, on their own
+    handles); the worst step, and for the batch the worst instance."""
     import torch
     from openvdb_gb300 import FP64, PARITY, DeviceLevelSet, Field, fixtures
     from openvdb_gb300.levelset import DeviceField
@@ -421,6 +423,10 @@ def fp64_errors(cfl):
     cases = {"config1": (lambda: fixtures.sphere(64.0, (0.0, 0.0, 0.0)), lambda: Field.constant_field((1.0, 0.5, 0.25)),
                          10),
              "config2": (lambda: build_workload()[0], lambda: build_workload()[1], 25)}
+    # configuration 3: the first instances of the 512-instance batch, each on its own handle
+    specs, fields = fixtures.batch_instances(n=512, seed=7)
+    for i in range(n_batch):
+        cases["config3_%d" % i] = ((lambda sp=specs[i]: fixtures.build_instance(sp)), (lambda f=fields[i]: f), 50)
     for name, (make_grid, make_field, steps) in cases.items():
         g, f = make_grid(), DeviceField(make_field())
         runs = []
@@ -453,6 +459,13 @@ def fp64_errors(cfl):
         out[name] = worst
         for d, _ in runs:
             d.close()
+    inst = [out.pop(k) for k in list(out) if k.startswith("config3_")]
+    if inst:
+        out["config3"] = {"instances": len(inst), "steps": 50,
+                          "max_dphi_over_gamma": max(e["max_dphi_over_gamma"] for e in inst),
+                          "p9999_over_gamma": max(e["p9999_over_gamma"] for e in inst),
+                          "voxels_above_1e-5_gamma": max(e["voxels_above_1e-5_gamma"] for e in inst),
+                          "active_state_differences": max(e["active_state_differences"] for e in inst)}
     return out
 
 

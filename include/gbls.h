@@ -65,8 +65,9 @@ enum { GBLS_TRIM_NONE = 0, GBLS_TRIM_INTERIOR = 1, GBLS_TRIM_EXTERIOR = 2, GBLS_
  *   (the same bits, slower; for cross-checking).
  * FAST evaluates everything in FP32 (contracted, shared sub-expressions). */
 /* PARITY: bit-identical to the reference's FloatGrid path; FAST: FP32
- * arithmetic; FP64: the same scheme with the values in double (the
- * reference's DoubleGrid instantiation), the error oracle of the FP32 run.  */
+ * arithmetic; FP64: the FloatGrid scheme (its constants as floats) with the
+ * values and every value operation in double, the error oracle of the FP32
+ * run.                                                                      */
 enum { GBLS_MODE_PARITY = 0, GBLS_MODE_FAST = 1, GBLS_MODE_FP64 = 2 };
 
 /* Transform kinds accepted (tools/LevelSetAdvect.h:257-276 accepts these four;

@@ -1907,9 +1907,10 @@ double max_speed_sqr_f64(gbls_handle& h, const gbls_field* f, float t, float max
 }
 
 // LevelSetAdvection::advect (tools/LevelSetAdvect.h:338-418) for the FP64
-// instance, the DoubleGrid instantiation: time and substep lengths in
-// double (the interval clock over double time), velocities sampled as Vec3f
-// at float(t), the RK stages and the tracker on double values.
+// instance (the FloatGrid scheme with double values): time and substep
+// lengths in double (the interval clock over double time), velocities
+// sampled as Vec3f at float(t), the RK stages and the tracker on double
+// values.
 void advect_f64(gbls_handle& h, const gbls_field* field, int spatial, int temporal, float t0, float t1, float cfl,
                 uint64_t& count, bool& interrupted) {
     if (spatial != GBLS_HJWENO5_BIAS || h.tr_spatial != GBLS_HJWENO5_BIAS)

@@ -1,12 +1,15 @@
-// FP64 instance of the advection hot path: the same scheme with the level
-// set's values in double -- the reference's DoubleGrid instantiation of
-// LevelSetAdvection / LevelSetTracker (ValueType double: WENO5, the RK
-// stages, the Eikonal update and the trim thresholds in double; the
-// velocities stay Vec3f samples of the field, as for FloatGrid).  The value
-// buffers of a handle in this mode hold 512 doubles per slot; masks,
-// staging records, topology and the velocity evaluation are the FP32
-// path's.  Compiled without contraction: every double operation rounds once,
-// as the host's do.
+// FP64 instance of the advection hot path: the FloatGrid scheme of
+// LevelSetAdvection / LevelSetTracker with the level set's values and every
+// value operation in double -- WENO5 (the reference formula with ValueType
+// double), the RK stages, the Eikonal update and the trim thresholds -- while
+// the scheme's constants keep their FloatGrid values (the band width, the RK
+// weight 1/3 and the normaliser's time-step factor as floats, widened) and
+// the velocities stay Vec3f samples.  It is the precision oracle of the FP32
+// run, not the reference's DoubleGrid instantiation (whose constants are
+// double).  The value buffers of a handle in this mode hold 512 doubles per
+// slot; masks, staging records, topology and the velocity evaluation are the
+// FP32 path's.  Compiled without contraction: every double operation rounds
+// once, as the host's do.
 #include "stencil_f64.h"
 
 #include "stencil_ops.cuh"
@@ -144,8 +147,8 @@ __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b 
 // One stage of Normalizer::euler (tools/LevelSetTracker.h:623-676) with
 // ValueType double over the voxels of pmask (plus the carried active ones),
 // optionally followed by Trim; output in the layout of the surviving
-// active set.  The structure of normalize_kernel, the arithmetic of the
-// DoubleGrid instantiation: GodunovsNormSqrd of the six HJ-WENO5
+// active set.  The structure of normalize_kernel in double arithmetic:
+// GodunovsNormSqrd of the six HJ-WENO5
 // derivatives, v = phi0 / (sqrt(phi0^2 + G) + double(1e-8f)),
 // phi0 - mDt * v * (sqrt(G) * invDx - 1).
 __global__ void __launch_bounds__(STENCIL_THREADS) normalize_f64_kernel(const NormArgs a) {

@@ -1,9 +1,9 @@
 """The FP64 instance on the device (GBLS_MODE_FP64) against the oracle's FP64
 instance.
 
-Both run the same scheme with the level set's values in double -- the
-reference's DoubleGrid instantiation of LevelSetAdvection / LevelSetTracker:
-WENO5, the RK stages, the Eikonal update and the trim thresholds in double,
+Both run the FloatGrid scheme of LevelSetAdvection / LevelSetTracker with
+the level set's values in double: WENO5, the RK stages, the Eikonal update
+and the trim thresholds in double, the scheme's constants as floats,
 velocities sampled as Vec3f, substep lengths and time in double.  Every
 double operation rounds once on both sides, so the device's band (leaf
 origins and active masks) and its active values must equal the oracle's bit
