@@ -131,3 +131,33 @@ def test_fp32_error_against_device_fp64():
         err = np.abs(v32 - v64).max() / g.background
         print("max |phi32 - phi64| / gamma = %.3g" % err)
         assert err < 1e-4
+
+
+@pytest.mark.gpu
+def test_fp64_upload_and_empty_grid():
+    """A new level set uploaded into an FP64 handle is widened; an empty
+    level set advects to nothing; gbls_get_counts and downloads work."""
+    from openvdb_gb300 import HostGrid
+    g1 = fixtures.sphere(12.0, (3.5, -7.25, 1.0))
+    g2 = fixtures.torus(14.0, 4.0, (1.0, 2.0, -1.0))
+    d = DeviceLevelSet(g1)
+    d.set_precision(FP64)
+    d.upload(g2)
+    assert np.array_equal(d.active_values_f64(), g2.active_values().astype(np.float64))
+    p = port.PortGrid(g2, precision=64)
+    field = Field.constant_field((0.4, -0.8, 0.3))
+    adv = LevelSetAdvection(d, field)
+    adv.setTemporalScheme(TVD_RK3)
+    adv.setTrackerTemporalScheme(TVD_RK1)
+    adv.setNormCount(1)
+    adv.cfl = 0.5
+    assert adv.advect(0.0, 1.0) == p.advect(field.desc(), 0.0, 1.0, spatial=port.HJWENO5_BIAS, temporal=TVD_RK3,
+                                             tracker_spatial=port.HJWENO5_BIAS, tracker_temporal=TVD_RK1,
+                                             norm_count=1, cfl=0.5)
+    assert np.array_equal(d.active_values_f64(), p.active_values())
+    d.close()
+    e = DeviceLevelSet(HostGrid(voxel_size=1.0, background=3.0))
+    e.set_precision(FP64)
+    assert LevelSetAdvection(e, field).advect(0.0, 1.0) == 0
+    assert e.active_voxel_count() == 0 and e.active_values_f64().size == 0
+    e.close()
