@@ -546,6 +546,13 @@ __global__ void __launch_bounds__(64) k_packed_move(int64_t n, const int32_t* sl
     }
 }
 
+// dst[pairs[2i]] = pairs[2i + 1] for i < n (upper-node sign words changed
+// in place on the host).
+__global__ void k_scatter_words(int64_t n, const uint64_t* pairs, uint64_t* dst) {
+    const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    if (i < n) dst[pairs[2 * i]] = pairs[2 * i + 1];
+}
+
 // The sign mask records value < 0 for every voxel: refresh its active bits
 // after new active values.
 __global__ void __launch_bounds__(64) k_active_signs(int64_t n, const int32_t* slot, const uint64_t* am,
@@ -661,6 +668,7 @@ struct gbls_handle {
     DevArray<float> f32_view; // f64: the current values rounded to float (downloads)
     DevArray<unsigned long long> argk;
     DevArray<double> argv;
+    DevArray<uint64_t> scatter;  // (index, word) pairs for in-place sign-table updates
     DevArray<uint64_t> dmask, emask;
     DevArray<int32_t> free_slots;
     int64_t nfree = 0;
@@ -1125,6 +1133,7 @@ void insert_nodes(gbls_handle& h, std::vector<uint64_t> miss) {
 // erased (RootNode::eraseBackgroundTiles).
 void prune_nodes(gbls_handle& h, bool lower_changed) {
     const int64_t nl = int64_t(h.lower_keys_h.size());
+    std::vector<size_t> dirty;  // upper sign words changed in place (upper-node slots that became tiles)
     if (lower_changed && nl) {
         std::vector<uint8_t> fl;
         if (h.flags_h.size() == size_t(nl)) {
@@ -1151,31 +1160,40 @@ void prune_nodes(gbls_handle& h, bool lower_changed) {
             uint64_t& w = h.upper_sign_h[ui * 512 + (n >> 6)];
             if (fl[size_t(i)] == 2) w |= (uint64_t(1) << (n & 63));
             else w &= ~(uint64_t(1) << (n & 63));
+            dirty.push_back(ui * 512 + (n >> 6));
         }
         remap_lower(h, keys, src);
     }
-    // upper nodes without lower nodes
-    std::vector<uint64_t> ukeys, usign;
-    bool changed = lower_changed;
+    // upper nodes without lower nodes (the tables are rebuilt only when one is)
+    bool changed = false;
+    std::vector<size_t> drop;
     for (size_t u = 0; u < h.upper_keys_h.size(); ++u) {
         const uint64_t uk = h.upper_keys_h[u];
         auto it = std::lower_bound(h.lower_keys_h.begin(), h.lower_keys_h.end(), uk << 15);
-        const bool has = it != h.lower_keys_h.end() && ((*it) >> 15) == uk;
-        if (has) {
+        if (!(it != h.lower_keys_h.end() && ((*it) >> 15) == uk)) drop.push_back(u);
+    }
+    if (!drop.empty()) {
+        changed = true;
+        std::vector<uint64_t> ukeys, usign;
+        size_t d = 0;
+        for (size_t u = 0; u < h.upper_keys_h.size(); ++u) {
+            const uint64_t uk = h.upper_keys_h[u];
+            if (d < drop.size() && drop[d] == u) {
+                ++d;
+                if (h.upper_sign_h[u * 512] & 1) {
+                    auto rt = std::lower_bound(h.root_keys_h.begin(), h.root_keys_h.end(), uk);
+                    const size_t ri = size_t(rt - h.root_keys_h.begin());
+                    h.root_keys_h.insert(rt, uk);
+                    h.root_sign_h.insert(h.root_sign_h.begin() + ri, 1);
+                }
+                continue;
+            }
             ukeys.push_back(uk);
             usign.insert(usign.end(), h.upper_sign_h.begin() + u * 512, h.upper_sign_h.begin() + (u + 1) * 512);
-        } else {
-            changed = true;
-            if (h.upper_sign_h[u * 512] & 1) {
-                auto rt = std::lower_bound(h.root_keys_h.begin(), h.root_keys_h.end(), uk);
-                const size_t ri = size_t(rt - h.root_keys_h.begin());
-                h.root_keys_h.insert(rt, uk);
-                h.root_sign_h.insert(h.root_sign_h.begin() + ri, 1);
-            }
         }
+        h.upper_keys_h.swap(ukeys);
+        h.upper_sign_h.swap(usign);
     }
-    h.upper_keys_h.swap(ukeys);
-    h.upper_sign_h.swap(usign);
     // eraseBackgroundTiles
     for (size_t r = 0; r < h.root_sign_h.size();) {
         if (h.root_sign_h[r] == 0) {
@@ -1186,7 +1204,23 @@ void prune_nodes(gbls_handle& h, bool lower_changed) {
             ++r;
         }
     }
-    if (changed) h.upload_upper_root();
+    if (changed) {
+        h.upload_upper_root();
+    } else if (!dirty.empty()) {
+        // only sign words changed: send those words, not the whole tables
+        const int64_t m = int64_t(dirty.size());
+        uint64_t* st = static_cast<uint64_t*>(h.pinned(size_t(m) * 16));
+        for (int64_t i = 0; i < m; ++i) {
+            st[2 * i] = uint64_t(dirty[size_t(i)]);
+            st[2 * i + 1] = h.upper_sign_h[dirty[size_t(i)]];
+        }
+        h.scatter.reserve(size_t(m) * 2, h.stream);
+        CU(cudaMemcpyAsync(h.scatter.p, st, size_t(m) * 16, cudaMemcpyHostToDevice, h.stream));
+        h.pinned_issued();
+        k_scatter_words<<<blocks_for(m, 256), 256, 0, h.stream>>>(m, h.scatter.p, h.upper_sign.p);
+        ++h.stats.kernel_launches;
+        CU(cudaGetLastError());
+    }
 }
 
 // ---- dilation: new leaves, node creation, neighbour table, dmask ----------
