@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define GBLS_ABI_VERSION 3
+#define GBLS_ABI_VERSION 4
 
 /* ---- status codes ---------------------------------------------------- */
 typedef enum gbls_status {
@@ -253,7 +253,11 @@ int gbls_get_active_values_f64(gbls_handle* h, double* out);
  *                                compiler: 0 (none: its heuristic, the
  *                                default), 1 (unconstrained), 14 or 16;
  *   cfl_leaves_per_block         leaves per CTA of the CFL maximum (8 threads
- *                                per leaf): 8, 16, 32 (default) or 64.
+ *                                per leaf): 8, 16, 32 (default) or 64;
+ *   rk_ctas_per_leaf             CTAs sharing one leaf in the PARITY RK stage
+ *                                (each stages the leaf and takes every k-th
+ *                                group of 64 active voxels): 1 (default), 2
+ *                                or 4 -- more parallelism for small level sets.
  * Results do not depend on them.  gbls_time_launch_config times one RK stage,
  * one renormalisation stage and one CFL maximum of the current level set
  * under a configuration (reps launches after a warm-up, mean ms per launch
@@ -263,6 +267,7 @@ typedef struct gbls_launch_config {
     int32_t stencil_min_ctas_rk;
     int32_t stencil_min_ctas_norm;
     int32_t cfl_leaves_per_block;
+    int32_t rk_ctas_per_leaf;
 } gbls_launch_config;
 int gbls_set_launch_config(gbls_handle* h, const gbls_launch_config* config);
 int gbls_get_launch_config(gbls_handle* h, gbls_launch_config* config);

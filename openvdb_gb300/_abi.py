@@ -5,7 +5,7 @@ checked against the compiled library in tests/test_abi.py.
 """
 import ctypes as C
 
-GBLS_ABI_VERSION = 3
+GBLS_ABI_VERSION = 4
 
 # status codes
 OK = 0
@@ -87,7 +87,7 @@ class FieldDesc(C.Structure):
 class LaunchConfig(C.Structure):
     """gbls_launch_config: launch shapes of the stencil and CFL kernels."""
     _fields_ = [("stencil_min_ctas_rk", C.c_int32), ("stencil_min_ctas_norm", C.c_int32),
-                ("cfl_leaves_per_block", C.c_int32)]
+                ("cfl_leaves_per_block", C.c_int32), ("rk_ctas_per_leaf", C.c_int32)]
 
 
 class HostMap(C.Structure):

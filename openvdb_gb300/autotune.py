@@ -1,20 +1,23 @@
 """Launch-shape autotuner for the advection kernels (no reference counterpart).
 
-Three launch parameters change speed, not results (gbls_launch_config):
-the register budget of the PARITY RK-stage and renormalisation kernels,
-given as the minimum resident 64-thread CTAs per SM (0 = none, the
-compiler's heuristic; 1 = unconstrained; 14 or 16), and the leaves per CTA
-of the CFL maximum (8, 16, 32 or 64).  Each parameter drives one kernel, so the search is coordinate-wise:
+Four launch parameters change speed, not results (gbls_launch_config): the
+register budget of the PARITY RK-stage and renormalisation kernels, given as
+the minimum resident 64-thread CTAs per SM (0 = none, the compiler's
+heuristic; 1 = unconstrained; 14 or 16), the leaves per CTA of the CFL
+maximum (8, 16, 32 or 64), and the CTAs per leaf of the PARITY RK stage (1,
+2 or 4: each CTA stages the whole leaf and takes every k-th group of 64
+active voxels, more parallelism where a level set has few leaves).  Each
+parameter drives one kernel, so the search is coordinate-wise:
 gbls_time_launch_config times one RK stage, one renormalisation stage and one
 CFL maximum of the handle's current level set under each candidate, and the
 fastest value per parameter wins.  The choice is cached per device, precision
 mode and workload size class (log2 of the leaf count) in a JSON file:
 $GBLS_TUNE_CACHE, else ~/.cache/openvdb_gb300/launch_config.json.
 
-Each stencil kernel runs one leaf (a 14^3 tile staged from the leaf and its
-face neighbours) per 64-thread CTA; the leaves per CTA of the stencil
-kernels and the staging depth are fixed at one, because a persistent,
-software-pipelined stencil kernel with deeper staging was measured slower.
+The renormalisation kernel keeps one leaf per CTA (its output layout needs
+every voxel's result of the leaf), and the staging depth is one leaf: a
+persistent, software-pipelined stencil kernel with deeper staging was
+measured slower.
 """
 import ctypes as C
 import json
@@ -28,10 +31,11 @@ CANDIDATES = {
     "stencil_min_ctas_rk": (0, 1, 14, 16),
     "stencil_min_ctas_norm": (0, 1, 14, 16),
     "cfl_leaves_per_block": (8, 16, 32, 64),
+    "rk_ctas_per_leaf": (1, 2, 4),
 }
-DEFAULT = {"stencil_min_ctas_rk": 0, "stencil_min_ctas_norm": 0, "cfl_leaves_per_block": 32}
+DEFAULT = {"stencil_min_ctas_rk": 0, "stencil_min_ctas_norm": 0, "cfl_leaves_per_block": 32, "rk_ctas_per_leaf": 1}
 # which of the three timed kernels each parameter drives
-_TIMED = {"stencil_min_ctas_rk": 0, "stencil_min_ctas_norm": 1, "cfl_leaves_per_block": 2}
+_TIMED = {"stencil_min_ctas_rk": 0, "stencil_min_ctas_norm": 1, "cfl_leaves_per_block": 2, "rk_ctas_per_leaf": 0}
 
 
 def _check(rc):
@@ -106,7 +110,7 @@ def tune(handle, field_handle, mode, leaf_count, reps=5, use_cache=True):
     key = cache_key(mode, leaf_count)
     db = _load() if use_cache else {}
     if use_cache and key in db:
-        cfg = {k: int(db[key]["config"][k]) for k in DEFAULT}
+        cfg = {k: int(db[key]["config"].get(k, DEFAULT[k])) for k in DEFAULT}
         apply(handle, cfg)
         return {"config": cfg, "source": "cache", "key": key}
     cfg = dict(DEFAULT)

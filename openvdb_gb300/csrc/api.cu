@@ -752,7 +752,7 @@ struct gbls_handle {
     // selects the FP64 kernels instead, for cross-checking.
     bool parity_fp64 = false;
     // launch shapes (gbls_set_launch_config; the autotuner's choices)
-    int rk_min_ctas = 0, norm_min_ctas = 0, cfl_leaves = 32;
+    int rk_min_ctas = 0, norm_min_ctas = 0, cfl_leaves = 32, rk_parts = 1;
     // a general FloatGrid volume (gbls_create_volume): any background, and
     // only volume operations
     bool volume = false;
@@ -1849,7 +1849,11 @@ void rk_stage(gbls_handle& h, const RkArgs& a) {
         launch_rk_f64(a, h.stream);
     } else if (h.mode == GBLS_MODE_PARITY) {
         if (h.parity_fp64) launch_rk_parity(a, h.stream);
-        else launch_rk_exact(a, h.stream, h.rk_min_ctas);
+        else {
+            RkArgs b = a;
+            b.parts = h.rk_parts;
+            launch_rk_exact(b, h.stream, h.rk_min_ctas);
+        }
     } else {
         launch_rk_fast(a, h.stream);
     }
@@ -2647,8 +2651,9 @@ int gbls_set_trimming(gbls_handle* h, int trim_mode) {
 // ---- launch shapes ------------------------------------------------------------
 static bool launch_config_ok(const gbls_launch_config* c) {
     auto ctas = [](int v) { return v == 0 || v == 1 || v == 14 || v == 16; };
-    const int l = c->cfl_leaves_per_block;
-    return ctas(c->stencil_min_ctas_rk) && ctas(c->stencil_min_ctas_norm) && (l == 8 || l == 16 || l == 32 || l == 64);
+    const int l = c->cfl_leaves_per_block, p = c->rk_ctas_per_leaf;
+    return ctas(c->stencil_min_ctas_rk) && ctas(c->stencil_min_ctas_norm) && (l == 8 || l == 16 || l == 32 || l == 64) &&
+           (p == 1 || p == 2 || p == 4);
 }
 
 int gbls_set_launch_config(gbls_handle* h, const gbls_launch_config* c) {
@@ -2657,6 +2662,7 @@ int gbls_set_launch_config(gbls_handle* h, const gbls_launch_config* c) {
     h->rk_min_ctas = c->stencil_min_ctas_rk;
     h->norm_min_ctas = c->stencil_min_ctas_norm;
     h->cfl_leaves = c->cfl_leaves_per_block;
+    h->rk_parts = c->rk_ctas_per_leaf;
     return GBLS_OK;
 }
 
@@ -2665,6 +2671,7 @@ int gbls_get_launch_config(gbls_handle* h, gbls_launch_config* c) {
     c->stencil_min_ctas_rk = h->rk_min_ctas;
     c->stencil_min_ctas_norm = h->norm_min_ctas;
     c->cfl_leaves_per_block = h->cfl_leaves;
+    c->rk_ctas_per_leaf = h->rk_parts;
     return GBLS_OK;
 }
 
@@ -2684,12 +2691,13 @@ int gbls_time_launch_config(gbls_handle* h, const gbls_field* f, const gbls_laun
         if (f->desc.kind == GBLS_FIELD_HOST_SAMPLED) fail(GBLS_ERR_UNSUPPORTED, "timing takes a device-evaluated field");
         if (h->tape_on) fail(GBLS_ERR_UNSUPPORTED, "timing while the adjoint records");
         const int n = std::max(1, reps);
-        const int rk0 = h->rk_min_ctas, nm0 = h->norm_min_ctas, cl0 = h->cfl_leaves;
+        const int rk0 = h->rk_min_ctas, nm0 = h->norm_min_ctas, cl0 = h->cfl_leaves, rp0 = h->rk_parts;
         const bool prof = h->profiling;
         h->profiling = false;
         h->rk_min_ctas = c->stencil_min_ctas_rk;
         h->norm_min_ctas = c->stencil_min_ctas_norm;
         h->cfl_leaves = c->cfl_leaves_per_block;
+        h->rk_parts = c->rk_ctas_per_leaf;
         const int vo = other_of(h->vc, h->vc), mo = other_of(h->mc, h->mc);
         RkArgs r{};
         r.spatial = GBLS_HJWENO5_BIAS;
@@ -2747,6 +2755,7 @@ int gbls_time_launch_config(gbls_handle* h, const gbls_field* f, const gbls_laun
         h->rk_min_ctas = rk0;
         h->norm_min_ctas = nm0;
         h->cfl_leaves = cl0;
+        h->rk_parts = rp0;
         h->profiling = prof;
     });
 }

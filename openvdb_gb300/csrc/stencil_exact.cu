@@ -14,7 +14,7 @@ namespace gbls {
 // 16: at most 72 or 64 registers per thread).
 void launch_rk_exact(const RkArgs& a, cudaStream_t s, int min_ctas) {
     if (a.nleaf <= 0) return;
-    const unsigned g = unsigned(a.nleaf);
+    const unsigned g = unsigned(a.nleaf * (a.parts > 1 ? a.parts : 1));
     if (min_ctas == 16) rk_stage_kernel<ExactArith, 16><<<g, STENCIL_THREADS, 0, s>>>(a);
     else if (min_ctas == 14) rk_stage_kernel<ExactArith, 14><<<g, STENCIL_THREADS, 0, s>>>(a);
     else if (min_ctas == 1) rk_stage_kernel<ExactArith, 1><<<g, STENCIL_THREADS, 0, s>>>(a);

@@ -511,6 +511,8 @@ struct RkArgs {
     const FieldParams* inst_field;
     int copy_done;         // the stage's output becomes the result: copy finished instances
     double dt64;           // FP64 instance: the substep length in double
+    int parts;             // CTAs per leaf (exact kernel; 0 or 1: one): CTA b takes leaf b / parts
+                           // and every parts-th group of STENCIL_THREADS active voxels from b % parts
 };
 
 struct NormArgs {
@@ -583,7 +585,10 @@ __global__ void __launch_bounds__(STENCIL_THREADS, MINB) rk_stage_kernel(const R
     __shared__ uint16_t list[LEAF_VOX];
     __shared__ float vtab[6][8];
     __shared__ FieldParams sf;
-    const int64_t l = blockIdx.x;
+    const int parts = a.parts > 1 ? a.parts : 1;
+    const int64_t l = parts > 1 ? int64_t(blockIdx.x) / parts : int64_t(blockIdx.x);
+    const int part = parts > 1 ? int(blockIdx.x % unsigned(parts)) : 0;
+    const int first = part * STENCIL_THREADS, stride = parts * STENCIL_THREADS;
     if (l >= a.nleaf) return;
     const int s = a.slot[l];
     const uint64_t key = a.keys[l];
@@ -594,7 +599,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS, MINB) rk_stage_kernel(const R
             if (a.copy_done) {  // keep a finished instance's values in the result buffer
                 int n = 0;
                 for (int w = 0; w < 8; ++w) n += __popcll(a.src.amask[size_t(s) * 8 + w]);
-                for (int i = threadIdx.x; i < n; i += STENCIL_THREADS)
+                for (int i = first + threadIdx.x; i < n; i += stride)
                     a.out[size_t(s) * LEAF_VOX + i] = a.src.vals[size_t(s) * LEAF_VOX + i];
             }
             return;
@@ -623,7 +628,7 @@ __global__ void __launch_bounds__(STENCIL_THREADS, MINB) rk_stage_kernel(const R
         }
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < n; i += STENCIL_THREADS) {
+    for (int i = first + threadIdx.x; i < n; i += stride) {
         const int v = list[i];
         const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
         float vel[3];

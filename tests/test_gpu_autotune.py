@@ -25,12 +25,18 @@ def _run(cfg):
 
 @pytest.mark.gpu
 def test_every_launch_configuration_gives_the_same_bits():
+    """Every value of every parameter (the others at their defaults), and
+    the RK stage's register budgets crossed with its CTAs per leaf."""
     from openvdb_gb300 import autotune
     ref = _run(dict(autotune.DEFAULT))
-    for rk, nm, cl in itertools.product(*autotune.CANDIDATES.values()):
-        if (rk, nm, cl) == tuple(autotune.DEFAULT.values()):
-            continue
-        cfg = {"stencil_min_ctas_rk": rk, "stencil_min_ctas_norm": nm, "cfl_leaves_per_block": cl}
+    cfgs = []
+    for name, values in autotune.CANDIDATES.items():
+        for v in values:
+            if v != autotune.DEFAULT[name]:
+                cfgs.append(dict(autotune.DEFAULT, **{name: v}))
+    for rk, parts in itertools.product(autotune.CANDIDATES["stencil_min_ctas_rk"], (2, 4)):
+        cfgs.append(dict(autotune.DEFAULT, stencil_min_ctas_rk=rk, rk_ctas_per_leaf=parts))
+    for cfg in cfgs:
         assert _run(cfg) == ref, cfg
 
 
