@@ -271,47 +271,16 @@ __device__ __forceinline__ float godunov(bool outside, const float* dm, const fl
     return acc;
 }
 
-// godunov<ExactArith> of the HJ-WENO5 derivatives of the lines through a
-// voxel, evaluating only the derivatives whose value it uses: outside
-// (phi0 > 0) a backward derivative known to be <= 0 enters as
-// (max(dm,0))^2 = 0 and a forward one known to be >= 0 as (min(dp,0))^2 =
-// 0, inside the mirror images; a derivative left out is replaced by 0,
-// whose square is the same +0.  The signs come from xw::weno5_sign.
-__device__ inline float godunov_hj_exact(const float* tile, int x, int y, int z, bool outside) {
-    // one WENO5 call site in loops that are not unrolled: the double-word
-    // evaluation is long, and copies of it would not fit the instruction cache
-    float acc = 0.0f;
-#pragma unroll 1
-    for (int ax = 0; ax < 3; ++ax) {
-        const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
-        const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
-        const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
-        const bool need_dm = sb != 2 && (outside ? sb != -1 : sb != 1);
-        const bool need_dp = sf != 2 && (outside ? sf != 1 : sf != -1);
-        float dm = 0.0f, dp = 0.0f;
-#pragma unroll 1
-        for (int e = 0; e < 2; ++e) {
-            if (!(e ? need_dp : need_dm)) continue;
-            float q[5];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) q[k] = e ? D.d[5 - k] : D.d[k];  // FD: D5..D1, BD: D0..D4
-            const float w = ExactArith::weno5(q[0], q[1], q[2], q[3], q[4]);
-            if (e) dp = w;
-            else dm = w;
-        }
-        // the axis' term of GodunovsNormSqrd, summed in axis order
-        const float a = outside ? ref_max(dm, 0.0f) : ref_min(dm, 0.0f);
-        const float b = outside ? ref_min(dp, 0.0f) : ref_max(dp, 0.0f);
-        const float term = ref_max(ExactArith::mul(a, a), ExactArith::mul(b, b));
-        acc = ax == 0 ? term : ExactArith::add(acc, term);
-    }
-    return acc;
-}
-
-// GodunovsNormSqrd of every processed voxel of a leaf (the voxels of pm in
-// `list`), as godunov_hj_exact computes it, into gsq[v] (v the voxel's
-// position).  A warp that evaluates each voxel's derivatives in turn runs
-// the union of its lanes' needs (about six WENO5 per voxel); here the
+// GodunovsNormSqrd (math/FiniteDifference.h:324-357) of the HJ-WENO5
+// derivatives of every processed voxel of a leaf (the voxels of pm in
+// `list`) into gsq[v] (v the voxel's position), evaluating only the
+// derivatives whose value it uses: outside (phi0 > 0) a backward derivative
+// known to be <= 0 enters as (max(dm,0))^2 = 0 and a forward one known to be
+// >= 0 as (min(dp,0))^2 = 0, inside the mirror images, and a derivative that
+// is a zero (five zero differences) adds +0; a derivative left out counts as
+// 0, whose square is the same +0.  The signs come from xw::weno5_sign.
+// A warp that evaluates each voxel's derivatives in turn runs the union of
+// its lanes' needs (about six WENO5 per voxel); here the
 // derivatives a voxel needs become work items of a CTA-wide list, axis by
 // axis, so every lane evaluates one needed WENO5 at a time.  An axis term
 // max(a^2, b^2) is the maximum of its items' squares (+0 without items;
