@@ -3541,13 +3541,23 @@ int gbls_batch_advect(gbls_handle* h, const gbls_field_desc* fields, int spatial
             h->stats.voxel_updates += upd;
             h->stats.substeps += uint64_t(nrun);
             h->nactive = int64_t(upd);  // the RK stages' algorithmic bytes count the running instances
+            // the dilation of this pass on the side stream beside the RK stages
+            // (they read the masks it reads, and write none)
+            h->prepare_dilation();
+            CU(cudaEventRecord(h->ev_fork, h->stream));
             advect_stages(*h, nullptr, spatial, temporal, t0, 0.0f, !forward);
+            CU(cudaEventRecord(h->ev_rk, h->stream));
             h->nactive = -1;
             for (int i = 0; i < n; ++i) {
                 if (!run[size_t(i)]) continue;
                 clock[size_t(i)].advance(t[size_t(i)], dt[size_t(i)]);
                 ++count[size_t(i)];
             }
+            h->overlap_dilation = true;
+            struct Overlap {
+                gbls_handle* h;
+                ~Overlap() { h->overlap_dilation = false; }
+            } overlap{h};
             track(*h);
             h->inst_active.download(act.data(), size_t(n), h->stream);
             h->sync();
