@@ -469,6 +469,62 @@ def fp64_errors(cfl, n_batch=16):
     return out
 
 
+def fp64_errors_dense(cfl):
+    """The same statement for the adjoint configurations' forward runs (PARITY
+    against FP64, dense velocity grids): configuration 4 (radius-40 sphere in
+    128^3, smoothed-noise velocity, 20 steps, every step checked) and
+    configuration 5 (radius-160 sphere in 512^3, the inverse problem's initial
+    velocity, 200 steps, every 10th step checked)."""
+    from openvdb_gb300 import FP64, PARITY, DeviceLevelSet, Field, fixtures
+    from openvdb_gb300.levelset import DeviceField
+    template, vel, _, _ = fixtures.adjoint_128()
+    cases = {"config4": (template, vel, 20, 1),
+             "config5": (fixtures.sphere(160.0, (256.0, 256.0, 256.0)), _initial_velocity(512, 0.05, 5), 200, 10)}
+    out = {}
+    for name, (g, v, steps, every) in cases.items():
+        f = DeviceField(Field.dense(v, (0, 0, 0), (0.0, 0.0, 0.0)))
+        runs = []
+        for mode in (PARITY, FP64):
+            d = DeviceLevelSet(g)
+            d.set_precision(mode)
+            runs.append((d, make_advection(d, f, cfl=cfl)))
+        worst = None
+        for step in range(steps):
+            for d, adv in runs:
+                adv.advect(float(step), float(step + 1))
+            if (step + 1) % every and step + 1 != steps:
+                continue
+            e = _band_error(runs[0][0].to_host(), runs[1][0].to_host(), runs[1][0].active_values_f64(),
+                            float(g.background))
+            if worst is None:
+                worst = dict(e)
+            else:
+                for key in ("max_dphi_over_gamma", "p9999_over_gamma", "voxels_above_1e-5_gamma",
+                            "active_state_differences"):
+                    worst[key] = max(worst[key], e[key])
+        worst.update({"steps": steps, "checked_every": every})
+        out[name] = worst
+        for d, _ in runs:
+            d.close()
+        del f
+    return out
+
+
+def run_fp64_errors(args):
+    """--workload fp64errors: the FP32 (PARITY) run's error against the
+    device's FP64 instance for configurations 1-5, one JSON line."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    torch.cuda.init()
+    torch.cuda.set_device(0)
+    out = {"metric": "max |phi_FP32 - phi_FP64| / band width and active-state differences, per configuration",
+           "unit": "band width", "cfl": args.cfl}
+    out.update(fp64_errors(args.cfl))
+    out.update(fp64_errors_dense(args.cfl))
+    print(json.dumps(out))
+
+
 def adjoint_cost(mode, mode_name, reps=3):
     """The 128^3 adjoint configuration (20 unit steps of RK3-HJWENO5, dense
     128^3 x 3 velocity): plain forward, recorded forward and reverse sweep of
@@ -748,14 +804,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--extras", type=int, default=1,
                     help="add the 128^3 adjoint cost ratio and the batched 512-instance figures to the line")
-    ap.add_argument("--workload", default="sphere64", choices=["sphere64", "batch512", "adjoint512"],
+    ap.add_argument("--workload", default="sphere64", choices=["sphere64", "batch512", "adjoint512", "fp64errors"],
                     help="sphere64: the headline 64-sphere line; batch512: the batched configuration; "
-                         "adjoint512: the checkpointed inverse problem (--steps = iterations)")
+                         "adjoint512: the checkpointed inverse problem (--steps = iterations); "
+                         "fp64errors: the FP32 run's error against the device FP64 instance, configurations 1-5")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     else:
-        {"batch512": run_batch, "adjoint512": run_adjoint}.get(args.workload, run_gb300)(args)
+        {"batch512": run_batch, "adjoint512": run_adjoint, "fp64errors": run_fp64_errors}.get(args.workload,
+                                                                                              run_gb300)(args)
 
 
 if __name__ == "__main__":
