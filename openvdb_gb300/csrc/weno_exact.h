@@ -9,7 +9,8 @@
 // product transformations and the double-word algorithms of Joldes, Muller
 // and Popescu, "Tight and rigorous error bounds for basic building blocks of
 // double-word arithmetic", ACM TOMS 44(2), 2017: algorithms 4, 9, 12 and 17,
-// and cascaded sums of error-free terms), together with an upper bound of
+// a squaring without the low parts' square, and cascaded sums of error-free
+// terms), together with an upper bound of
 // its distance from the reference's double value.  When the interval of
 // that width around the pair holds no float rounding boundary, the float
 // the reference produces is known exactly; otherwise (about one evaluation
@@ -142,6 +143,27 @@ GBLS_XHD DW<V> dw_mul(DW<V> x, DW<V> y) {  // algorithm 12: 4u^2
     const V t = fma(x.h, y.l, mul(x.l, y.l));
     return fast_two_sum(c.h, add(c.l, fma(x.l, y.h, t)));
 }
+// x^2: h^2 = p + e exactly; t = fl(2hl + e) errs by at most u|2hl + e| <=
+// 3u^2 h^2, the dropped l^2 is at most u^2 h^2, and |t| <= |p| makes the
+// final sum exact: 4u^2
+template <class V>
+GBLS_XHD DW<V> dw_sqr(DW<V> x) {
+    const DW<V> c = two_prod(x.h, x.h);
+    return fast_two_sum(c.h, fma(x.h, add(x.l, x.l), c.l));
+}
+// x^2 / 4 as (x/2)^2, the halving exact: the same bound
+template <class V>
+GBLS_XHD DW<V> dw_sqr_quarter(DW<V> x) {
+    const V hh = mul(x.h, splat(0.5f, x.h));
+    const DW<V> c = two_prod(hh, hh);
+    return fast_two_sum(c.h, fma(hh, x.l, c.l));
+}
+// algorithm 10 (no low-part product): about 7u^2
+template <class V>
+GBLS_XHD DW<V> dw_mul_lite(DW<V> x, DW<V> y) {
+    const DW<V> c = two_prod(x.h, y.h);
+    return fast_two_sum(c.h, add(c.l, fma(x.l, y.h, mul(x.h, y.l))));
+}
 // algorithm 17 with th = xh * r, r an approximate reciprocal of yh (within
 // one ulp; th within two ulps of xh / yh, which the correction absorbs):
 // 15u^2 + O(u^3)
@@ -152,6 +174,13 @@ GBLS_XHD DW<V> dw_div(DW<V> x, DW<V> y, V r) {
     const V d = add(sub(x.h, p.h), sub(x.l, p.l));
     return fast_two_sum(th, mul(d, r));
 }
+// the same for a float numerator (x.l = 0)
+template <class V>
+GBLS_XHD DW<V> dw_div_f(V x, DW<V> y, V r) {
+    const V th = mul(x, r);
+    const DW<V> p = dw_mul_f(y, th);
+    return fast_two_sum(th, mul(sub(sub(x, p.h), p.l), r));
+}
 // Sum of three double words by a cascade of two error-free sums of the high
 // parts, the low parts and the sum errors added in float: absolute error
 // within about 2u^2 (|a| + |b| + |c|).
@@ -161,6 +190,19 @@ GBLS_XHD DW<V> dw_sum3(DW<V> a, DW<V> b, DW<V> c) {
     const DW<V> t = two_sum(s.h, c.h);
     const V low = add(add(add(a.l, b.l), c.l), add(s.l, t.l));
     return fast_two_sum(t.h, low);
+}
+// The same cascade with float terms (low parts zero, not added).
+template <class V>
+GBLS_XHD DW<V> dw_sum3_f(DW<V> a, V b, DW<V> c) {
+    const DW<V> s = two_sum(a.h, b);
+    const DW<V> t = two_sum(s.h, c.h);
+    return fast_two_sum(t.h, add(add(a.l, c.l), add(s.l, t.l)));
+}
+template <class V>
+GBLS_XHD DW<V> dw_sum3_ff(DW<V> a, V b, V c) {
+    const DW<V> s = two_sum(a.h, b);
+    const DW<V> t = two_sum(s.h, c);
+    return fast_two_sum(t.h, add(a.l, add(s.l, t.l)));
 }
 template <class V>
 GBLS_XHD DW<V> dw_scale(DW<V> x, V s) { return {mul(x.h, s), mul(x.l, s)}; }  // s a power of two
@@ -197,9 +239,7 @@ GBLS_XHD bool rounds_to_hi(float h, float l, float e) {
 }
 // Lane masks (bit k for lane k).
 GBLS_XHD unsigned round_mask(DW<float> t, float e) { return rounds_to_hi(t.h, t.l, e) ? 1u : 0u; }
-GBLS_XHD unsigned zero_mask(float a, float b, float c, float d, float e) {
-    return (a == 0.0f && b == 0.0f && c == 0.0f && d == 0.0f && e == 0.0f) ? 1u : 0u;
-}
+GBLS_XHD unsigned zero_mask(float a) { return a == 0.0f ? 1u : 0u; }
 GBLS_XHD float select_lanes(unsigned m, float a, float b) { return (m & 1u) ? a : b; }
 
 // WENO5 of the reference on every lane.  Returns the mask of lanes whose
@@ -234,24 +274,23 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     const V inf = splat(__builtin_huge_valf(), v1);
     const V small = fminf(fminf(m3a > 0.0f ? m3a : inf, m3b > 0.0f ? m3b : inf), m3c > 0.0f ? m3c : inf);
     const bool u3_exact = ua.l == 0.0f && ub.l == 0.0f && !(big > mul(small, splat(0x1p20f, v1)));
-    const DW<V> ub1 = dw_scale(dw_mul(u1, u1), quarter), ub3 = dw_scale(dw_mul(u3, u3), quarter);
+    const DW<V> ub1 = dw_sqr_quarter(u1), ub3 = dw_sqr_quarter(u3);
     // d = (C*pa + 0.25*pb) + eps, every term >= 0
     const DW<V> C = dw_const(kC_h, kC_l, v1), EPS = dw_const(kEps_h, kEps_l, v1);
     const DW<V> d1 = dw_sum3(dw_mul_f(C, pa1), ub1, EPS);
-    const DW<V> d2 = dw_sum3(dw_mul_f(C, pa2), DW<V>{mul(quarter, pb2), zero}, EPS);
+    const DW<V> d2 = dw_sum3_f(dw_mul_f(C, pa2), mul(quarter, pb2), EPS);
     const DW<V> d3 = dw_sum3(dw_mul_f(C, pa3), ub3, EPS);
-    const DW<V> D1 = dw_mul(d1, d1), D2 = dw_mul(d2, d2), D3 = dw_mul(d3, d3);
+    const DW<V> D1 = dw_sqr(d1), D2 = dw_sqr(d2), D3 = dw_sqr(d3);
     const V r1 = rcp(D1.h), r2 = rcp(D2.h), r3 = rcp(D3.h);
     const DW<V> A1 = dw_div(dw_const(kG1_h, kG1_l, v1), D1, r1);
     const DW<V> A2 = dw_div(dw_const(kG2_h, kG2_l, v1), D2, r2);
     const DW<V> A3 = dw_div(dw_const(kG3_h, kG3_l, v1), D3, r3);
     // p1 = (2v1 - 7v2) + 11v3, p2 = (5v3 - v2) + 2v4, p3 = (2v3 + 5v4) - v5;
     // each product is exact in double and as a pair
-    const DW<V> p1 = dw_sum3(two_prod(splat(-7.0f, v1), v2), DW<V>{mul(two, v1), zero},
-                             two_prod(splat(11.0f, v1), v3));
-    const DW<V> p2 = dw_sum3(two_prod(five, v3), DW<V>{neg(v2), zero}, DW<V>{mul(two, v4), zero});
-    const DW<V> p3 = dw_sum3(two_prod(five, v4), DW<V>{mul(two, v3), zero}, DW<V>{neg(v5), zero});
-    const DW<V> num = dw_sum3(dw_mul(A1, p1), dw_mul(A2, p2), dw_mul(A3, p3));
+    const DW<V> p1 = dw_sum3_f(two_prod(splat(-7.0f, v1), v2), mul(two, v1), two_prod(splat(11.0f, v1), v3));
+    const DW<V> p2 = dw_sum3_ff(two_prod(five, v3), neg(v2), mul(two, v4));
+    const DW<V> p3 = dw_sum3_ff(two_prod(five, v4), mul(two, v3), neg(v5));
+    const DW<V> num = dw_sum3(dw_mul_lite(A1, p1), dw_mul_lite(A2, p2), dw_mul_lite(A3, p3));
 
     // Error bound of num against the reference's double.  Relative error of
     // A_k: 2^-40 covers the double-word chain and the reference's own
@@ -269,9 +308,10 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     const V q3 = u3_exact ? zero : mul(mul(mul(vabs(u3.h), vabs(i3.h)), splat(0x1p-45f, v1)), mul(d3.h, r3));
     const V e40 = splat(0x1p-40f, v1), e46 = splat(0x1p-46f, v1);
     const V e3 = add(e40, q3);
-    const V T1 = add(add(vabs(mul(two, v1)), vabs(mul(splat(7.0f, v1), v2))), vabs(mul(splat(11.0f, v1), v3)));
-    const V T2 = add(add(vabs(mul(five, v3)), vabs(v2)), vabs(mul(two, v4)));
-    const V T3 = add(add(vabs(mul(two, v3)), vabs(mul(five, v4))), vabs(v5));
+    // (fused sums: within 2u of the exact T_k, which the doubling covers)
+    const V T1 = fma(splat(11.0f, v1), vabs(v3), fma(splat(7.0f, v1), vabs(v2), add(vabs(v1), vabs(v1))));
+    const V T2 = fma(two, vabs(v4), fma(five, vabs(v3), vabs(v2)));
+    const V T3 = fma(five, vabs(v4), fma(two, vabs(v3), vabs(v5)));
     const V a1 = vabs(A1.h), a2 = vabs(A2.h), a3 = vabs(A3.h);
     const V s1 = fma(vabs(p1.h), e40, mul(T1, e46));
     const V s2 = fma(vabs(p2.h), e40, mul(T2, e46));
@@ -287,14 +327,15 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     const V rd = rcp(den.h);
     const V e42 = splat(0x1p-42f, v1);
     const V e_den = add(mul(fma(a1, e40, fma(a2, e40, mul(a3, e3))), mul(six, rd)), e42);
-    const DW<V> q = dw_div(DW<V>{F, zero}, den, rd);
+    const DW<V> q = dw_div_f(F, den, rd);
     const V e_q = mul(mul(two, vabs(q.h)), add(e_den, e42));
     ok &= round_mask(q, e_q);
     out = q.h;
-    // five zero operands: the reference's result is the signed zero of
-    // ((A1 p1 + A2 p2) + A3 p3) with every A_k > 0; the same IEEE sign
-    // rules give it in float
-    const unsigned z = zero_mask(v1, v2, v3, v4, v5);
+    // five zero operands (T1 = T3 = 0: sums of non-negative terms vanish
+    // only when every term does): the reference's result is the signed
+    // zero of ((A1 p1 + A2 p2) + A3 p3) with every A_k > 0; the same IEEE
+    // sign rules give it in float
+    const unsigned z = zero_mask(add(T1, T3));
     if (z) {
         const V z1 = add(sub(mul(two, v1), mul(splat(7.0f, v1), v2)), mul(splat(11.0f, v1), v3));
         const V z2 = add(sub(mul(five, v3), v2), mul(two, v4));
