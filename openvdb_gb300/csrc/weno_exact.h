@@ -8,7 +8,7 @@
 // float pair (hi + lo, about 48 significant bits; the error-free sum and
 // product transformations and the double-word algorithms of Joldes, Muller
 // and Popescu, "Tight and rigorous error bounds for basic building blocks of
-// double-word arithmetic", ACM TOMS 44(2), 2017: algorithms 4, 9, 12 and 17,
+// double-word arithmetic", ACM TOMS 44(2), 2017: algorithms 4, 9, 10 and 17,
 // a squaring without the low parts' square, and cascaded sums of error-free
 // terms), together with an upper bound of
 // its distance from the reference's double value.  When the interval of
@@ -137,11 +137,11 @@ GBLS_XHD DW<V> dw_mul_f(DW<V> x, V y) {  // algorithm 9: 2u^2
     const DW<V> c = two_prod(x.h, y);
     return fast_two_sum(c.h, fma(x.l, y, c.l));
 }
+// The same pair before the final normalisation (|l| within about 2u |h|).
 template <class V>
-GBLS_XHD DW<V> dw_mul(DW<V> x, DW<V> y) {  // algorithm 12: 4u^2
-    const DW<V> c = two_prod(x.h, y.h);
-    const V t = fma(x.h, y.l, mul(x.l, y.l));
-    return fast_two_sum(c.h, add(c.l, fma(x.l, y.h, t)));
+GBLS_XHD DW<V> dw_mul_f_un(DW<V> x, V y) {
+    const DW<V> c = two_prod(x.h, y);
+    return {c.h, fma(x.l, y, c.l)};
 }
 // x^2: h^2 = p + e exactly; t = fl(2hl + e) errs by at most u|2hl + e| <=
 // 3u^2 h^2, the dropped l^2 is at most u^2 h^2, and |t| <= |p| makes the
@@ -158,23 +158,26 @@ GBLS_XHD DW<V> dw_sqr_quarter(DW<V> x) {
     const DW<V> c = two_prod(hh, hh);
     return fast_two_sum(c.h, fma(hh, x.l, c.l));
 }
-// algorithm 10 (no low-part product): about 7u^2
+// algorithm 10 (no low-part product): about 7u^2, before the final
+// normalisation (|l| within a few u |h|)
 template <class V>
-GBLS_XHD DW<V> dw_mul_lite(DW<V> x, DW<V> y) {
+GBLS_XHD DW<V> dw_mul_lite_un(DW<V> x, DW<V> y) {
     const DW<V> c = two_prod(x.h, y.h);
-    return fast_two_sum(c.h, add(c.l, fma(x.l, y.h, mul(x.h, y.l))));
+    return {c.h, add(c.l, fma(x.l, y.h, mul(x.h, y.l)))};
 }
-// algorithm 17 with th = xh * r, r an approximate reciprocal of yh (within
+// Algorithm 17 with th = xh * r, r an approximate reciprocal of yh (within
 // one ulp; th within two ulps of xh / yh, which the correction absorbs):
-// 15u^2 + O(u^3)
+// 15u^2 + O(u^3), returned before its final normalisation: the pair
+// (th, d r) holds the value the normalised pair would, with |d r| up to
+// about 8u |th| (th within two ulps of xh / yh, and x, y within u of their
+// high parts), for callers that tolerate that.
 template <class V>
-GBLS_XHD DW<V> dw_div(DW<V> x, DW<V> y, V r) {
+GBLS_XHD DW<V> dw_div_un(DW<V> x, DW<V> y, V r) {
     const V th = mul(x.h, r);
     const DW<V> p = dw_mul_f(y, th);
-    const V d = add(sub(x.h, p.h), sub(x.l, p.l));
-    return fast_two_sum(th, mul(d, r));
+    return {th, mul(add(sub(x.h, p.h), sub(x.l, p.l)), r)};
 }
-// the same for a float numerator (x.l = 0)
+// Algorithm 17 (normalised) for a float numerator (x.l = 0).
 template <class V>
 GBLS_XHD DW<V> dw_div_f(V x, DW<V> y, V r) {
     const V th = mul(x, r);
@@ -191,6 +194,14 @@ GBLS_XHD DW<V> dw_sum3(DW<V> a, DW<V> b, DW<V> c) {
     const V low = add(add(add(a.l, b.l), c.l), add(s.l, t.l));
     return fast_two_sum(t.h, low);
 }
+// The cascade before the final normalisation (|l| within a few u |h| when
+// the terms have one sign).
+template <class V>
+GBLS_XHD DW<V> dw_sum3_un(DW<V> a, DW<V> b, DW<V> c) {
+    const DW<V> s = two_sum(a.h, b.h);
+    const DW<V> t = two_sum(s.h, c.h);
+    return {t.h, add(add(add(a.l, b.l), c.l), add(s.l, t.l))};
+}
 // The same cascade with float terms (low parts zero, not added).
 template <class V>
 GBLS_XHD DW<V> dw_sum3_f(DW<V> a, V b, DW<V> c) {
@@ -204,8 +215,6 @@ GBLS_XHD DW<V> dw_sum3_ff(DW<V> a, V b, V c) {
     const DW<V> t = two_sum(s.h, c);
     return fast_two_sum(t.h, add(a.l, add(s.l, t.l)));
 }
-template <class V>
-GBLS_XHD DW<V> dw_scale(DW<V> x, V s) { return {mul(x.h, s), mul(x.l, s)}; }  // s a power of two
 
 // Double constants of the formula as double-word pairs (hi = float(c),
 // lo = float(c - hi), each within u^2 |c| of the double), evaluated by the
@@ -277,24 +286,29 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     const DW<V> ub1 = dw_sqr_quarter(u1), ub3 = dw_sqr_quarter(u3);
     // d = (C*pa + 0.25*pb) + eps, every term >= 0
     const DW<V> C = dw_const(kC_h, kC_l, v1), EPS = dw_const(kEps_h, kEps_l, v1);
-    const DW<V> d1 = dw_sum3(dw_mul_f(C, pa1), ub1, EPS);
-    const DW<V> d2 = dw_sum3_f(dw_mul_f(C, pa2), mul(quarter, pb2), EPS);
-    const DW<V> d3 = dw_sum3(dw_mul_f(C, pa3), ub3, EPS);
+    // (the products enter the cascades unnormalised: their low parts are
+    // added on their own, and every term is >= 0)
+    const DW<V> d1 = dw_sum3(dw_mul_f_un(C, pa1), ub1, EPS);
+    const DW<V> d2 = dw_sum3_f(dw_mul_f_un(C, pa2), mul(quarter, pb2), EPS);
+    const DW<V> d3 = dw_sum3(dw_mul_f_un(C, pa3), ub3, EPS);
     const DW<V> D1 = dw_sqr(d1), D2 = dw_sqr(d2), D3 = dw_sqr(d3);
     const V r1 = rcp(D1.h), r2 = rcp(D2.h), r3 = rcp(D3.h);
-    const DW<V> A1 = dw_div(dw_const(kG1_h, kG1_l, v1), D1, r1);
-    const DW<V> A2 = dw_div(dw_const(kG2_h, kG2_l, v1), D2, r2);
-    const DW<V> A3 = dw_div(dw_const(kG3_h, kG3_l, v1), D3, r3);
+    // the weights stay unnormalised: they enter only products and sums
+    const DW<V> A1 = dw_div_un(dw_const(kG1_h, kG1_l, v1), D1, r1);
+    const DW<V> A2 = dw_div_un(dw_const(kG2_h, kG2_l, v1), D2, r2);
+    const DW<V> A3 = dw_div_un(dw_const(kG3_h, kG3_l, v1), D3, r3);
     // p1 = (2v1 - 7v2) + 11v3, p2 = (5v3 - v2) + 2v4, p3 = (2v3 + 5v4) - v5;
     // each product is exact in double and as a pair
     const DW<V> p1 = dw_sum3_f(two_prod(splat(-7.0f, v1), v2), mul(two, v1), two_prod(splat(11.0f, v1), v3));
     const DW<V> p2 = dw_sum3_ff(two_prod(five, v3), neg(v2), mul(two, v4));
     const DW<V> p3 = dw_sum3_ff(two_prod(five, v4), mul(two, v3), neg(v5));
-    const DW<V> num = dw_sum3(dw_mul_lite(A1, p1), dw_mul_lite(A2, p2), dw_mul_lite(A3, p3));
+    const DW<V> num = dw_sum3(dw_mul_lite_un(A1, p1), dw_mul_lite_un(A2, p2), dw_mul_lite_un(A3, p3));
 
     // Error bound of num against the reference's double.  Relative error of
-    // A_k: 2^-40 covers the double-word chain and the reference's own
-    // roundings (about 2^-42.4 and 2^-49).  An error du in u moves d by
+    // A_k: 2^-40 covers the double-word chain (u1 2u^2; its quarter square
+    // 8u^2; d_k, a cascade of non-negative terms with unnormalised products,
+    // 13u^2; D_k 30u^2; the division 15u^2 more: about 46u^2 = 2^-42.5) and
+    // the reference's own roundings (about 2^-49).  An error du in u moves d by
     // 0.25*2|u|du, and A by twice that relative to d: for u1 (one sum, du
     // within 2^-46 |u1|) that stays below 2^-43 because d >= 0.25 u^2.
     // u3 is exact on both sides in the common case (u3_exact); otherwise
@@ -303,8 +317,10 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     // 2^-45 |u3| |3v3 - 4v4| / d3 more (a factor of two spare).
     // p_k: the reference's products are exact, its two sums err by up to
     // 2^-52 of T_k = sum of |terms|, the cascade by 2^-47 T_k; the sum of
-    // the products A_k p_k (cascade) by 2^-46 of S = sum |A_k p_k|, which
-    // the 2^-40 terms cover.  The total, doubled, is e_num.
+    // the products A_k p_k by 2^-44.2 of S = sum |A_k p_k| (14u^2, the
+    // weights' low parts up to 8u of their high parts) and their cascade,
+    // with unnormalised terms, by 2^-44.7 S, which the 2^-40 terms cover.
+    // The total, doubled, is e_num.
     const V q3 = u3_exact ? zero : mul(mul(mul(vabs(u3.h), vabs(i3.h)), splat(0x1p-45f, v1)), mul(d3.h, r3));
     const V e40 = splat(0x1p-40f, v1), e46 = splat(0x1p-46f, v1);
     const V e3 = add(e40, q3);
@@ -323,7 +339,7 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     // den = 6 * ((A1 + A2) + A3), positive; its relative uncertainty is the
     // A_k's weighted by A_k / sum, plus the sums and the product
     const V six = splat(6.0f, v1);
-    const DW<V> den = dw_mul_f(dw_sum3(A1, A2, A3), six);
+    const DW<V> den = dw_mul_f_un(dw_sum3_un(A1, A2, A3), six);
     const V rd = rcp(den.h);
     const V e42 = splat(0x1p-42f, v1);
     const V e_den = add(mul(fma(a1, e40, fma(a2, e40, mul(a3, e3))), mul(six, rd)), e42);
