@@ -502,6 +502,10 @@ int gbls_host_weno5_exact(int64_t n, const float* v, float* out, uint8_t* decide
  * (result <= 0), 2 (five zero operands: the result is a zero) or 0
  * (undecided).                                                             */
 int gbls_host_weno5_sign(int64_t n, const float* v, int8_t* sign);
+/* The same certificate for the backward operands d[6i..6i+4] (sb[i]) and
+ * the forward operands d[6i+5], d[6i+4], ..., d[6i+1] (sf[i]) of n lines
+ * of six differences at once, as the renormalisation evaluates it.         */
+int gbls_host_weno5_sign_pair(int64_t n, const float* d, int8_t* sb, int8_t* sf);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);
 

@@ -278,7 +278,7 @@ __device__ __forceinline__ float godunov(bool outside, const float* dm, const fl
 // known to be <= 0 enters as (max(dm,0))^2 = 0 and a forward one known to be
 // >= 0 as (min(dp,0))^2 = 0, inside the mirror images, and a derivative that
 // is a zero (five zero differences) adds +0; a derivative left out counts as
-// 0, whose square is the same +0.  The signs come from xw::weno5_sign.
+// 0, whose square is the same +0.  The signs come from xw::weno5_sign_pair.
 // A warp that evaluates each voxel's derivatives in turn runs the union of
 // its lanes' needs (about six WENO5 per voxel); here the
 // derivatives a voxel needs become work items of a CTA-wide list, axis by
@@ -314,8 +314,8 @@ __device__ inline void godunov_exact_leaf(const float* tile, const uint16_t* lis
                 const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
                 const bool outside = tile[tile_index(x, y, z)] > 0.0f;
                 const Diff6 D = line_diffs<ExactArith>(tile_line(tile, x, y, z, ax));
-                const int sb = xw::weno5_sign(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4]);  // BD operands
-                const int sf = xw::weno5_sign(D.d[5], D.d[4], D.d[3], D.d[2], D.d[1]);  // FD operands
+                int sb, sf;  // BD operands D0..D4, FD operands D5..D1
+                xw::weno5_sign_pair(D.d[0], D.d[1], D.d[2], D.d[3], D.d[4], D.d[5], sb, sf);
                 term[v] = 0u;
                 // a derivative the norm clamps to zero, or a zero (flat line), adds nothing
                 if (sb != 2 && (outside ? sb != -1 : sb != 1)) queue[atomicAdd(cnt, 1)] = uint16_t(v << 1);

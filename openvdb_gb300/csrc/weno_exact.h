@@ -171,17 +171,20 @@ GBLS_XHD DW<V> dw_mul_lite_un(DW<V> x, DW<V> y) {
 // (th, d r) holds the value the normalised pair would, with |d r| up to
 // about 8u |th| (th within two ulps of xh / yh, and x, y within u of their
 // high parts), for callers that tolerate that.
+// The product y th enters unnormalised: p.h = fl(yh th) is within a few
+// ulps of xh, so xh - p.h stays exact (Sterbenz), and the low part is
+// subtracted on its own.
 template <class V>
 GBLS_XHD DW<V> dw_div_un(DW<V> x, DW<V> y, V r) {
     const V th = mul(x.h, r);
-    const DW<V> p = dw_mul_f(y, th);
+    const DW<V> p = dw_mul_f_un(y, th);
     return {th, mul(add(sub(x.h, p.h), sub(x.l, p.l)), r)};
 }
-// Algorithm 17 (normalised) for a float numerator (x.l = 0).
+// Algorithm 17 (normalised) for a float numerator (x.l = 0), the same way.
 template <class V>
 GBLS_XHD DW<V> dw_div_f(V x, DW<V> y, V r) {
     const V th = mul(x, r);
-    const DW<V> p = dw_mul_f(y, th);
+    const DW<V> p = dw_mul_f_un(y, th);
     return fast_two_sum(th, mul(sub(sub(x, p.h), p.l), r));
 }
 // Sum of three double words by a cascade of two error-free sums of the high
@@ -372,21 +375,41 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
 // makes p_k exactly zero.  Returns +1 (result >= 0 for certain), -1
 // (result <= 0 for certain), 2 (five zero operands: the result is a zero)
 // or 0 (undecided).
-GBLS_XHD int weno5_sign(float v1, float v2, float v3, float v4, float v5) {
-    // T_k by fused multiply-adds: within 3u of the exact sums, so 4u T_k still
-    // exceeds the estimates' 2u error bound
-    const float t1 = fma(11.0f, vabs(v3), fma(7.0f, vabs(v2), mul(2.0f, vabs(v1))));
-    const float t2 = fma(5.0f, vabs(v3), fma(2.0f, vabs(v4), vabs(v2)));
-    const float t3 = fma(5.0f, vabs(v4), fma(2.0f, vabs(v3), vabs(v5)));
-    const float e1 = fma(11.0f, v3, fma(-7.0f, v2, mul(2.0f, v1)));
-    const float e2 = fma(2.0f, v4, fma(5.0f, v3, -v2));
-    const float e3 = fma(-1.0f, v5, fma(5.0f, v4, mul(2.0f, v3)));
-    const float m1 = mul(t1, 0x1p-22f), m2 = mul(t2, 0x1p-22f), m3 = mul(t3, 0x1p-22f);
-    const bool z1 = t1 == 0.0f, z2 = t2 == 0.0f, z3 = t3 == 0.0f;
+// One candidate sum's estimate e and its T (T_k by fused multiply-adds:
+// within 3u of the exact sums, so 4u T_k still exceeds the estimates' 2u
+// error bound).
+struct SignTerm {
+    float e, t;
+};
+GBLS_XHD SignTerm sign_p1(float v1, float v2, float v3) {  // 2v1 - 7v2 + 11v3
+    return {fma(11.0f, v3, fma(-7.0f, v2, mul(2.0f, v1))), fma(11.0f, vabs(v3), fma(7.0f, vabs(v2), mul(2.0f, vabs(v1))))};
+}
+GBLS_XHD SignTerm sign_p2(float v2, float v3, float v4) {  // 5v3 - v2 + 2v4
+    return {fma(2.0f, v4, fma(5.0f, v3, -v2)), fma(5.0f, vabs(v3), fma(2.0f, vabs(v4), vabs(v2)))};
+}
+GBLS_XHD SignTerm sign_p3(float v3, float v4, float v5) {  // 2v3 + 5v4 - v5
+    return {fma(-1.0f, v5, fma(5.0f, v4, mul(2.0f, v3))), fma(5.0f, vabs(v4), fma(2.0f, vabs(v3), vabs(v5)))};
+}
+GBLS_XHD int sign_of(SignTerm a, SignTerm b, SignTerm c) {
+    const float m1 = mul(a.t, 0x1p-22f), m2 = mul(b.t, 0x1p-22f), m3 = mul(c.t, 0x1p-22f);
+    const bool z1 = a.t == 0.0f, z2 = b.t == 0.0f, z3 = c.t == 0.0f;
     if (z1 && z2 && z3) return 2;
-    const bool nonneg = (z1 || e1 > m1) && (z2 || e2 > m2) && (z3 || e3 > m3);
-    const bool nonpos = (z1 || e1 < -m1) && (z2 || e2 < -m2) && (z3 || e3 < -m3);
+    const bool nonneg = (z1 || a.e > m1) && (z2 || b.e > m2) && (z3 || c.e > m3);
+    const bool nonpos = (z1 || a.e < -m1) && (z2 || b.e < -m2) && (z3 || c.e < -m3);
     return nonneg ? 1 : nonpos ? -1 : 0;
+}
+GBLS_XHD int weno5_sign(float v1, float v2, float v3, float v4, float v5) {
+    return sign_of(sign_p1(v1, v2, v3), sign_p2(v2, v3, v4), sign_p3(v3, v4, v5));
+}
+// weno5_sign of a line's backward operands (d0, d1, d2, d3, d4) and forward
+// operands (d5, d4, d3, d2, d1) together.  The backward operands' second and
+// third candidate sums, -d1 + 5d2 + 2d3 and 2d2 + 5d3 - d4, are the forward
+// operands' third and second, so four estimates serve both (any estimate
+// within 2u T of its sum certifies the same way).
+GBLS_XHD void weno5_sign_pair(float d0, float d1, float d2, float d3, float d4, float d5, int& sb, int& sf) {
+    const SignTerm y = sign_p2(d1, d2, d3), x = sign_p3(d2, d3, d4);
+    sb = sign_of(sign_p1(d0, d1, d2), y, x);
+    sf = sign_of(sign_p1(d5, d4, d3), x, y);
 }
 
 // Vec3d(g) * invdx (double) rounded to float (GradientBiased's applyIJT,

@@ -103,3 +103,32 @@ def test_weno5_sign_is_certain(kind):
     assert not np.any((sign == 2) & (ref != 0)), "certified zero but not zero"
     assert np.array_equal(sign == 2, np.all(v == 0, axis=1)), "a zero certificate other than five zero operands"
     print("%s: sign certified for %.1f%%" % (kind, 100.0 * np.mean(sign != 0)))
+
+
+@pytest.mark.parametrize("kind", ["uniform", "sphere_lines", "smooth", "zeros_jumps", "walks"])
+def test_weno5_sign_pair_is_certain(kind):
+    """The renormalisation's certificate for a line's backward (D0..D4) and
+    forward (D5..D1) operands at once: every certified sign agrees with the
+    reference's result, zeros are certified exactly for five zero operands,
+    and it certifies as often as two separate certificates."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    v = _inputs(kind, 200_000, rng)
+    # lines of six differences: five operands and one more of the same kind
+    d = np.ascontiguousarray(np.concatenate([v, np.roll(v[:, :1], 1, axis=0)], axis=1), np.float32)
+    bd = np.ascontiguousarray(d[:, :5])
+    fd = np.ascontiguousarray(d[:, [5, 4, 3, 2, 1]])
+    sb = np.empty(d.shape[0], np.int8)
+    sf = np.empty(d.shape[0], np.int8)
+    P = C.POINTER
+    assert _lib.lib().gbls_host_weno5_sign_pair(d.shape[0], d.ctypes.data_as(P(C.c_float)),
+                                                sb.ctypes.data_as(P(C.c_int8)), sf.ctypes.data_as(P(C.c_int8))) == 0
+    for ops, sign in ((bd, sb), (fd, sf)):
+        ref = port.weno5(ops)
+        assert not np.any((sign == 1) & (ref < 0)), "certified >= 0 but negative"
+        assert not np.any((sign == -1) & (ref > 0)), "certified <= 0 but positive"
+        assert not np.any((sign == 2) & (ref != 0)), "certified zero but not zero"
+        assert np.array_equal(sign == 2, np.all(ops == 0, axis=1))
+        single = np.empty(ops.shape[0], np.int8)
+        assert _lib.lib().gbls_host_weno5_sign(ops.shape[0], ops.ctypes.data_as(P(C.c_float)),
+                                               single.ctypes.data_as(P(C.c_int8))) == 0
+        assert abs(np.mean(sign != 0) - np.mean(single != 0)) < 1e-3
