@@ -716,6 +716,35 @@ ADJOINT_WORKLOAD = {"workload": "inverse problem: sphere r=160 -> torus R=160 r=
                     "temporal": "TVD_RK3", "cfl": 0.5, "tracker": "HJWENO5/TVD_RK1", "norm_count": 1}
 
 
+def run_profile_case(args):
+    """Small cases for ncu captures (inputs still larger than L2), one JSON
+    line each: sphere16 = the first 16 of the 64 benchmark spheres (3.25 M
+    active voxels), one advect(0, 0.2) call (one CFL substep: 3 RK stages, 1
+    renormalisation) of the benchmark scheme; adjoint128 = one best-of-1 pass
+    of the 128^3 adjoint configuration."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from openvdb_gb300 import FAST, PARITY, DeviceLevelSet, Field, fixtures
+    from openvdb_gb300.levelset import DeviceField
+    torch.cuda.init()
+    mode = FAST if args.mode == "fast" else PARITY
+    if args.workload == "adjoint128":
+        print(json.dumps(adjoint_cost(mode, args.mode, reps=1)))
+        return
+    c, r = fixtures.sixty_four_spheres(seed=2024)
+    d = DeviceLevelSet(fixtures.union_of_spheres(c[:16], r[:16], 1.0, 3.0))
+    d.set_precision(mode)
+    before = (d.active_voxel_count(), d.leaf_count())
+    a = make_advection(d, DeviceField(Field.deformation(domain=1024.0, period=100.0, scale=1.0)), cfl=args.cfl)
+    n = a.advect(0.0, 0.2)
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "sphere16: 16 of the 64 benchmark spheres, advect(0, 0.2)", "mode": args.mode,
+                      "active_before": before[0], "leaves_before": before[1], "substeps": n,
+                      "active_after": d.active_voxel_count(), "leaves_after": d.leaf_count()}))
+    d.close()
+
+
 def _initial_velocity(n, amp, seed):
     """Seeded smooth velocity: per component a sum of three separable sine modes."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -848,16 +877,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--extras", type=int, default=1,
                     help="add the 128^3 adjoint cost ratio and the batched 512-instance figures to the line")
-    ap.add_argument("--workload", default="sphere64", choices=["sphere64", "batch512", "adjoint512", "fp64errors"],
+    ap.add_argument("--workload", default="sphere64",
+                    choices=["sphere64", "batch512", "adjoint512", "fp64errors", "sphere16", "adjoint128"],
                     help="sphere64: the headline 64-sphere line; batch512: the batched configuration; "
                          "adjoint512: the checkpointed inverse problem (--steps = iterations); "
-                         "fp64errors: the FP32 run's error against the device FP64 instance, configurations 1-5")
+                         "fp64errors: the FP32 run's error against the device FP64 instance, configurations 1-5; "
+                         "sphere16 / adjoint128: small cases for ncu captures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     else:
-        {"batch512": run_batch, "adjoint512": run_adjoint, "fp64errors": run_fp64_errors}.get(args.workload,
-                                                                                              run_gb300)(args)
+        {"batch512": run_batch, "adjoint512": run_adjoint, "fp64errors": run_fp64_errors,
+         "sphere16": run_profile_case, "adjoint128": run_profile_case}.get(args.workload, run_gb300)(args)
 
 
 if __name__ == "__main__":
