@@ -506,6 +506,13 @@ int gbls_host_weno5_sign(int64_t n, const float* v, int8_t* sign);
  * the forward operands d[6i+5], d[6i+4], ..., d[6i+1] (sf[i]) of n lines
  * of six differences at once, as the renormalisation evaluates it.         */
 int gbls_host_weno5_sign_pair(int64_t n, const float* d, int8_t* sb, int8_t* sf);
+/* The same WENO5 on the device, as the PARITY kernels evaluate it (the
+ * double-word evaluation, the FP64 formula where it leaves the rounding
+ * undecided): out[i] for the quintuple v[5i..5i+4]; decided[i] = 1 where
+ * the double-word evaluation decided (decided may be NULL).  v, out and
+ * decided are device arrays; runs on `stream` (NULL: the default stream)
+ * and returns when done.                                                   */
+int gbls_weno5_exact_device(const float* v, int64_t n, float* out, uint8_t* decided, void* stream);
 int gbls_host_grid_free(gbls_host_grid* g);
 const char* gbls_host_last_error(void);
 

@@ -86,6 +86,7 @@ def lib():
         "gbls_host_weno5_exact": ([C.c_int64, P(C.c_float), P(C.c_float), P(C.c_uint8)], C.c_int),
         "gbls_host_weno5_sign": ([C.c_int64, P(C.c_float), P(C.c_int8)], C.c_int),
         "gbls_host_weno5_sign_pair": ([C.c_int64, P(C.c_float), P(C.c_int8), P(C.c_int8)], C.c_int),
+        "gbls_weno5_exact_device": ([C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
         "gbls_host_sample_enright": ([vp, C.c_int64, P(C.c_int32), C.c_float, P(C.c_float)], None),
         "gbls_host_grid_free": ([vp], C.c_int),
         "gbls_host_last_error": ([], C.c_char_p),

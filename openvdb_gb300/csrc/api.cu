@@ -4409,6 +4409,16 @@ int gbls_nanovdb_probe(const void* grid, int64_t size, const int32_t* ijk, int64
     });
 }
 
+int gbls_weno5_exact_device(const float* v, int64_t n, float* out, uint8_t* decided, void* stream) {
+    if (n < 0 || (n > 0 && (!v || !out))) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
+    return guarded([&] {
+        const cudaStream_t s = static_cast<cudaStream_t>(stream);
+        launch_weno5_exact(v, n, out, decided, s);
+        CU(cudaGetLastError());
+        CU(cudaStreamSynchronize(s));
+    });
+}
+
 int gbls_create_from_nanovdb(const void* buffer, int64_t size, gbls_handle** out) {
     if (!buffer || !out || size < 0) { g_last_error = "null argument"; return GBLS_ERR_INVALID_ARGUMENT; }
     *out = nullptr;

@@ -1,5 +1,7 @@
 // Host launchers of the stencil kernels (one set per arithmetic policy).
 #pragma once
+#include <cstdint>
+
 #include <cuda_runtime.h>
 
 namespace gbls {
@@ -13,6 +15,8 @@ void launch_norm_parity(const NormArgs& a, cudaStream_t s);
 // The same bits as the parity launchers on the FP32 pipes (ExactArith).
 void launch_rk_exact(const RkArgs& a, cudaStream_t s, int min_ctas = 0);
 void launch_norm_exact(const NormArgs& a, cudaStream_t s, int min_ctas = 0);
+// ExactArith's WENO5 on n quintuples (device arrays; decided may be null).
+void launch_weno5_exact(const float* v, int64_t n, float* out, uint8_t* decided, cudaStream_t s);
 // FP32 arithmetic.
 void launch_rk_fast(const RkArgs& a, cudaStream_t s);
 void launch_norm_fast(const NormArgs& a, cudaStream_t s);

@@ -43,4 +43,22 @@ void launch_filter_exact(const FilterArgs& a, cudaStream_t s) {
         filter_kernel<ExactArith><<<unsigned(a.nleaf), STENCIL_THREADS, 0, s>>>(a);
 }
 
+// The PARITY kernels' WENO5 on n operand quintuples v[5i..5i+4]: the
+// double-word evaluation, FP64 where it leaves the rounding undecided.
+__global__ void weno5_exact_kernel(const float* __restrict__ v, int64_t n, float* __restrict__ out,
+                                   uint8_t* __restrict__ decided) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* q = v + 5 * i;
+    float r;
+    const bool ok = xw::weno5<float>(q[0], q[1], q[2], q[3], q[4], r) != 0u;
+    out[i] = ok ? r : weno5_fp64(q[0], q[1], q[2], q[3], q[4]);
+    if (decided) decided[i] = ok ? 1 : 0;
+}
+
+void launch_weno5_exact(const float* v, int64_t n, float* out, uint8_t* decided, cudaStream_t s) {
+    if (n <= 0) return;
+    weno5_exact_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(v, n, out, decided);
+}
+
 }  // namespace gbls

@@ -252,6 +252,8 @@ GBLS_XHD bool rounds_to_hi(float h, float l, float e) {
 // Lane masks (bit k for lane k).
 GBLS_XHD unsigned round_mask(DW<float> t, float e) { return rounds_to_hi(t.h, t.l, e) ? 1u : 0u; }
 GBLS_XHD unsigned zero_mask(float a) { return a == 0.0f ? 1u : 0u; }
+GBLS_XHD unsigned below_mask(float a, float b) { return a < b ? 1u : 0u; }
+GBLS_XHD float vmax(float a, float b) { return a < b ? b : a; }
 GBLS_XHD float select_lanes(unsigned m, float a, float b) { return (m & 1u) ? a : b; }
 
 // WENO5 of the reference on every lane.  Returns the mask of lanes whose
@@ -336,7 +338,11 @@ GBLS_XHD unsigned weno5(V v1, V v2, V v3, V v4, V v5, V& out) {
     const V s2 = fma(vabs(p2.h), e40, mul(T2, e46));
     const V s3 = fma(vabs(p3.h), e3, mul(T3, e46));
     const V e_num = mul(two, fma(a1, s1, fma(a2, s2, mul(a3, s3))));
-    unsigned ok = round_mask(num, e_num);
+    // Range: the bounds above are relative ones, which hold while the
+    // weights and their low parts are normal floats.  D_k < 2^96 keeps A_k
+    // above 2^-100 and its low part above 2^-124 (and the reciprocal seeds
+    // normal); larger D_k (differences above about 2^20) are left to FP64.
+    unsigned ok = round_mask(num, e_num) & below_mask(vmax(vmax(D1.h, D2.h), D3.h), splat(0x1p96f, v1));
     const V F = num.h;  // static_cast<float>(num)
 
     // den = 6 * ((A1 + A2) + A3), positive; its relative uncertainty is the

@@ -132,3 +132,18 @@ def test_weno5_sign_pair_is_certain(kind):
         assert _lib.lib().gbls_host_weno5_sign(ops.shape[0], ops.ctypes.data_as(P(C.c_float)),
                                                single.ctypes.data_as(P(C.c_int8))) == 0
         assert abs(np.mean(sign != 0) - np.mean(single != 0)) < 1e-3
+
+
+@pytest.mark.parametrize("e", [-120, -100, -90, -60, -30, 10, 20, 24, 28, 30, 36, 45, 60, 90])
+def test_exact_weno5_scaled_operands(e):
+    """Operands scaled by 2^e: far from the level-set range the weights
+    reach the subnormal range (large differences) or the candidate sums and
+    the numerator approach underflow (tiny ones).  Every decided result is
+    still the reference's; the rest go to the FP64 formula."""
+    rng = np.random.Generator(np.random.PCG64(200 + e))
+    v = np.concatenate([_inputs(k, 60_000, rng) for k in ("uniform", "zeros_jumps", "walks")])
+    v = (v * np.float32(2.0 ** e)).astype(np.float32)
+    ref = port.weno5(v)
+    got, dec = _exact(v)
+    bad = np.nonzero(dec & (got.view(np.uint32) != ref.view(np.uint32)))[0]
+    assert bad.size == 0, [(v[i].tolist(), float(got[i]), float(ref[i])) for i in bad[:5]]
