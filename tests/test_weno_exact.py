@@ -147,3 +147,27 @@ def test_exact_weno5_scaled_operands(e):
     got, dec = _exact(v)
     bad = np.nonzero(dec & (got.view(np.uint32) != ref.view(np.uint32)))[0]
     assert bad.size == 0, [(v[i].tolist(), float(got[i]), float(ref[i])) for i in bad[:5]]
+
+
+@pytest.mark.parametrize("e", [-149, -135, -126, -100, -40, 20, 60, 100, 126])
+def test_weno5_sign_scaled_operands(e):
+    """The sign certificates (single and paired) at operands scaled by 2^e,
+    down to subnormal differences: no certified sign contradicts the
+    reference's result."""
+    rng = np.random.Generator(np.random.PCG64(300 + e))
+    v = np.concatenate([_inputs(k, 40_000, rng) for k in ("uniform", "zeros_jumps", "walks", "smooth")])
+    v = np.ascontiguousarray((v.astype(np.float64) * 2.0 ** e).astype(np.float32))
+    d = np.ascontiguousarray(np.concatenate([v, np.roll(v[:, :1], 1, axis=0)], axis=1), np.float32)
+    P = C.POINTER
+    sb = np.empty(d.shape[0], np.int8)
+    sf = np.empty(d.shape[0], np.int8)
+    s1 = np.empty(v.shape[0], np.int8)
+    assert _lib.lib().gbls_host_weno5_sign_pair(d.shape[0], d.ctypes.data_as(P(C.c_float)),
+                                                sb.ctypes.data_as(P(C.c_int8)), sf.ctypes.data_as(P(C.c_int8))) == 0
+    assert _lib.lib().gbls_host_weno5_sign(v.shape[0], v.ctypes.data_as(P(C.c_float)),
+                                           s1.ctypes.data_as(P(C.c_int8))) == 0
+    for ops, sign in ((np.ascontiguousarray(d[:, :5]), sb), (np.ascontiguousarray(d[:, [5, 4, 3, 2, 1]]), sf), (v, s1)):
+        ref = port.weno5(ops)
+        assert not np.any((sign == 1) & (ref < 0))
+        assert not np.any((sign == -1) & (ref > 0))
+        assert not np.any((sign == 2) & (ref != 0))
